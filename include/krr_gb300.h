@@ -1,0 +1,258 @@
+/*
+ * krr_gb300.h — C ABI of the GB300 wavefront path tracer.
+ *
+ * This is the drop-in boundary for KiRaRay's WavefrontPathTracer render pass
+ * (src/render/wavefront/integrator.h:24-104).  Every entry point returns an
+ * int status (KRR_OK on success); the reference terminates on error instead
+ * (src/util/check.h:8-51).  All work is asynchronous on the CUDA stream that
+ * is passed in (the reference uses one stream, src/core/device/context.h:45).
+ * Pointers named d_* are device pointers, h_* are host pointers.  No torch or
+ * other C++ types cross this boundary.
+ */
+#ifndef KRR_GB300_H
+#define KRR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+enum {
+    KRR_OK = 0,
+    KRR_ERR_INVALID_ARGUMENT = 1,
+    KRR_ERR_CUDA = 2,
+    KRR_ERR_OVERFLOW = 3,      /* a device queue or stack ran out of room   */
+    KRR_ERR_TIMEOUT = 4,       /* a bounded device-side wait gave up         */
+    KRR_ERR_NOT_READY = 5,     /* called before set_scene / resize           */
+    KRR_ERR_OUT_OF_MEMORY = 6
+};
+
+/* Human-readable text of the last error raised on this host thread. */
+const char *krr_last_error(void);
+const char *krr_status_string(int status);
+/* Library version, for the integration check. */
+int krr_version(void);
+
+/* ------------------------------------------------------------ ray records */
+/* One ray, 32 bytes: origin.xyz + tmin, direction.xyz + tmax.  The
+ * direction need not be normalised (the reference's shadow rays are not:
+ * src/core/raytracing.h:151-160). */
+typedef struct krr_ray {
+    float ox, oy, oz, tmin;
+    float dx, dy, dz, tmax;
+} krr_ray;
+
+/* One closest hit, 16 bytes: t, barycentrics (b1, b2) with the reference's
+ * convention b = (1-b1-b2, b1, b2) (src/render/shading.h:78-87) and the
+ * global triangle id (instance-major order of the scene's triangles), or
+ * KRR_MISS. */
+typedef struct krr_hit {
+    float t, b1, b2;
+    uint32_t prim;
+} krr_hit;
+
+#define KRR_MISS 0xFFFFFFFFu
+
+/* ----------------------------------------------------- scene description */
+/* Mirrors the reference's material schema (src/scene/krrscene.cpp:195-227)
+ * and MaterialType enum order (src/core/raytracing.h:24-31). */
+enum {
+    KRR_MATERIAL_NULL = 0,
+    KRR_MATERIAL_DIFFUSE = 1,
+    KRR_MATERIAL_DIELECTRIC = 2,
+    KRR_MATERIAL_CONDUCTOR = 3
+};
+
+typedef struct krr_material_desc {
+    int32_t type;                 /* KRR_MATERIAL_*                          */
+    float diffuse[3];             /* "diffuse"                               */
+    float specular[3];            /* "specular"                              */
+    float roughness;              /* "roughness" (stored as 1-roughness in the
+                                     specular alpha, as the reference does)  */
+    float specular_transmission;  /* "specular_transmission"                 */
+    float eta;                    /* "eta"                                   */
+    float anisotropic;            /* "anisotropic"                           */
+} krr_material_desc;
+
+/* One triangle mesh (src/core/mesh.h:25-56).  Vertex normals are required:
+ * the reference's Triangle::sample reads them unconditionally
+ * (src/core/shape.h:61-62). */
+typedef struct krr_mesh_desc {
+    const float *h_positions;     /* float3 [n_vertices]                     */
+    const float *h_normals;       /* float3 [n_vertices]                     */
+    const float *h_texcoords;     /* float2 [n_vertices] or NULL             */
+    const uint32_t *h_indices;    /* uint3  [n_triangles]                    */
+    int64_t n_vertices;
+    int64_t n_triangles;
+    int32_t material;             /* index into materials, -1 = null material */
+    float emission[3];            /* mesh radiance Le; all zero = not a light */
+    int32_t medium_inside;        /* index into media or -1                  */
+    int32_t medium_outside;       /* index into media or -1                  */
+} krr_mesh_desc;
+
+typedef struct krr_instance_desc {
+    int32_t mesh;
+    float transform[12];          /* row-major 3x4 object-to-world           */
+} krr_instance_desc;
+
+/* Infinite (environment) light, src/core/light.h:208-259. */
+typedef struct krr_infinite_light_desc {
+    float tint[3];
+    float scale;
+    float rotation[9];            /* row-major 3x3 light-to-world            */
+    const float *h_image;         /* float4 [height][width] or NULL          */
+    int32_t width, height;
+} krr_infinite_light_desc;
+
+/* Heterogeneous medium over a dense FP16 density grid (the reference's
+ * NanoVDBMedium<float>, src/render/media.h:144-227). */
+typedef struct krr_medium_desc {
+    const uint16_t *h_density;    /* IEEE half [nz][ny][nx], or NULL = homogeneous */
+    int32_t nx, ny, nz;
+    float bounds_min[3], bounds_max[3];
+    float sigma_t[3];
+    float albedo[3];
+    float g;                      /* Henyey-Greenstein asymmetry             */
+    float scale;                  /* density scale                           */
+    int32_t majorant_res[3];      /* majorant grid resolution                */
+} krr_medium_desc;
+
+typedef struct krr_camera_desc {
+    float position[3];
+    float rotation[9];            /* row-major 3x3 camera-to-world; the camera
+                                     looks down its local -Z (src/core/camera.h:45-57) */
+    float film_size[2];           /* mm */
+    float focal_length;           /* mm */
+    float focal_distance;
+    float lens_radius;
+    float aspect_ratio;
+    float shutter_open, shutter_time;
+    int32_t medium;               /* medium the camera sits in, or -1        */
+} krr_camera_desc;
+
+typedef struct krr_scene_desc {
+    const krr_mesh_desc *meshes;        int32_t n_meshes;
+    const krr_instance_desc *instances; int32_t n_instances;
+    const krr_material_desc *materials; int32_t n_materials;
+    const krr_infinite_light_desc *infinite_lights; int32_t n_infinite_lights;
+    const krr_medium_desc *media;       int32_t n_media;
+} krr_scene_desc;
+
+/* ------------------------------------------------ acceleration structure */
+/* Replaces OptixScene::buildTriangleMeshGAS / OptixSceneSingleLevel::
+ * buildAccelStructure (src/core/device/optix.cpp:143-250,357-398): builds a
+ * Morton-code LBVH on the GPU and collapses it into a compressed 8-wide BVH
+ * over the world-space triangles of all instances. */
+typedef struct krr_accel krr_accel;
+
+typedef struct krr_accel_stats {
+    int64_t n_triangles;
+    int64_t n_nodes;          /* 8-wide nodes                               */
+    int32_t max_depth;        /* 8-wide levels                              */
+    int32_t reserved;
+    double build_ms;          /* device time of the last build              */
+    double node_bytes;        /* bytes of the node array                    */
+    double triangle_bytes;    /* bytes of the leaf-ordered triangle array   */
+} krr_accel_stats;
+
+/* Build from host arrays of world-space triangles: h_vertices float3[3*n]. */
+int krr_accel_create_from_triangles(const float *h_vertices, int64_t n_triangles,
+                                    krr_accel **out, void *stream);
+int krr_accel_stats_get(const krr_accel *accel, krr_accel_stats *out);
+int krr_accel_destroy(krr_accel *accel);
+
+/* Closest hit for n rays (the reference's __raygen__Closest +
+ * __closesthit__Closest, src/render/wavefront/device.cu:43-81, without the
+ * shading setup).  Ties in t go to the smaller triangle id. */
+int krr_accel_trace_closest(const krr_accel *accel, const krr_ray *d_rays, int64_t n,
+                            krr_hit *d_hits, void *stream);
+/* Any hit in (tmin, tmax] (the reference's __raygen__Shadow,
+ * src/render/wavefront/device.cu:83-100).  d_occluded[i] = 1 if blocked.
+ * Triangles whose mask byte is zero are ignored (null-material surfaces). */
+int krr_accel_trace_any(const krr_accel *accel, const krr_ray *d_rays, int64_t n,
+                        uint8_t *d_occluded, void *stream);
+/* Per-triangle any-hit mask (global triangle order); NULL = all opaque. */
+int krr_accel_set_mask(krr_accel *accel, const uint8_t *h_mask);
+
+/* Counter-instrumented replay of a trace: h_counts[0] = 8-wide nodes visited,
+ * h_counts[1] = triangles tested, summed over the n rays.  Used to compute
+ * the algorithmic bytes per ray of the roofline. */
+int krr_accel_trace_stats(const krr_accel *accel, const krr_ray *d_rays, int64_t n,
+                          int32_t any_hit, unsigned long long *h_counts, void *stream);
+
+/* Same as krr_accel_trace_closest, with host buffers: copies the rays in and
+ * the hits out inside the call (pinned host memory is fastest). */
+int krr_accel_trace_closest_host(const krr_accel *accel, const krr_ray *h_rays, int64_t n,
+                                 krr_hit *h_hits, void *stream);
+
+/* -------------------------------------------- wavefront path tracer pass */
+typedef struct krr_wf krr_wf;
+
+/* Pass parameters (WavefrontPathTracer::from_json,
+ * src/render/wavefront/integrator.h:96-103). */
+typedef struct krr_wf_params {
+    int32_t nee;              /* "nee", default 1            */
+    int32_t enable_medium;    /* "enable_medium", default 1  */
+    int32_t max_depth;        /* "max_depth", default 10     */
+    float rr;                 /* "rr", default 0.8           */
+    int32_t enable_clamp;     /* "enable_clamp", default 0   */
+    float clamp_max;          /* "clamp_max", default 1e3    */
+    int32_t spp;              /* samples per pixel per frame */
+    uint32_t seed;            /* added to the per-pixel sample index */
+} krr_wf_params;
+
+void krr_wf_params_default(krr_wf_params *p);
+
+int krr_wf_create(const krr_wf_params *params, krr_wf **out);
+int krr_wf_destroy(krr_wf *wf);
+int krr_wf_set_params(krr_wf *wf, const krr_wf_params *params);
+/* RenderPass::setScene (integrator.cpp:186-203): uploads the scene and
+ * builds the BVH. */
+int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *scene, void *stream);
+/* RenderPass::resize (integrator.cpp:181-184): reallocates queues. */
+int krr_wf_resize(krr_wf *wf, int32_t width, int32_t height);
+/* RenderPass::beginFrame (integrator.cpp:205-221). frame_index is 1-based. */
+int krr_wf_begin_frame(krr_wf *wf, int64_t frame_index, const krr_camera_desc *camera,
+                       void *stream);
+/* RenderPass::render (integrator.cpp:223-267): writes float4 RGBA per pixel,
+ * row-major, row 0 at the top (the reference's y-flipped surface write). */
+int krr_wf_render(krr_wf *wf, float *d_out_rgba, void *stream);
+
+/* Stage entry points, for stage-level tests and for subclasses in the manner
+ * of PPGPathTracer (src/misc/render/ppg/integrator.h:13). */
+int krr_wf_generate_camera_rays(krr_wf *wf, void *stream);
+int krr_wf_trace_closest(krr_wf *wf, int32_t depth, void *stream);
+int krr_wf_handle_hit(krr_wf *wf, void *stream);
+int krr_wf_handle_miss(krr_wf *wf, void *stream);
+int krr_wf_generate_scatter_rays(krr_wf *wf, int32_t depth, void *stream);
+int krr_wf_trace_shadow(krr_wf *wf, void *stream);
+int krr_wf_sample_medium_interaction(krr_wf *wf, int32_t depth, void *stream);
+int krr_wf_sample_medium_scattering(krr_wf *wf, int32_t depth, void *stream);
+int krr_wf_reset_queues(krr_wf *wf, int32_t depth, void *stream);
+
+enum {
+    KRR_QUEUE_RAY0 = 0, KRR_QUEUE_RAY1 = 1, KRR_QUEUE_MISS = 2, KRR_QUEUE_HIT_LIGHT = 3,
+    KRR_QUEUE_SHADOW = 4, KRR_QUEUE_SCATTER = 5, KRR_QUEUE_MEDIUM_SAMPLE = 6,
+    KRR_QUEUE_MEDIUM_SCATTER = 7, KRR_QUEUE_COUNT = 8
+};
+/* Current item count of a queue (synchronises the stream). */
+int krr_wf_queue_size(krr_wf *wf, int32_t queue, int32_t *out_size, void *stream);
+/* Device pointer to the per-pixel radiance L (float3 per pixel, SoA x/y/z planes). */
+int krr_wf_pixel_radiance(krr_wf *wf, const float **d_L);
+/* Device pointers to planes of the ray queue used at `depth`: float4 per item
+ * (origin.xyz | tmin), (direction.xyz | tmax) and (pu.xyz | pixel id bits);
+ * the item count is krr_wf_queue_size(depth & 1). */
+int krr_wf_ray_queue(krr_wf *wf, int32_t depth, const float **d_origin_tmin,
+                     const float **d_dir_tmax, const float **d_pu_pixel, int32_t *capacity);
+/* Error flags raised by device code since the last call (cleared on read). */
+int krr_wf_device_errors(krr_wf *wf, uint32_t *out_flags, void *stream);
+/* The BVH of the current scene (owned by the pass). */
+int krr_wf_accel(krr_wf *wf, const krr_accel **out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KRR_GB300_H */

@@ -1,0 +1,149 @@
+"""ctypes binding of libkrr_gb300.so (the C ABI declared in include/krr_gb300.h).
+
+There is no fallback: if the shared library is missing or does not load,
+importing the package's GPU entry points raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libkrr_gb300.so"
+
+KRR_OK = 0
+KRR_MISS = 0xFFFFFFFF
+
+MATERIAL_NULL, MATERIAL_DIFFUSE, MATERIAL_DIELECTRIC, MATERIAL_CONDUCTOR = 0, 1, 2, 3
+QUEUES = ["RAY0", "RAY1", "MISS", "HIT_LIGHT", "SHADOW", "SCATTER", "MEDIUM_SAMPLE",
+          "MEDIUM_SCATTER"]
+
+
+class MaterialDesc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("diffuse", C.c_float * 3), ("specular", C.c_float * 3),
+                ("roughness", C.c_float), ("specular_transmission", C.c_float),
+                ("eta", C.c_float), ("anisotropic", C.c_float)]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("h_positions", C.c_void_p), ("h_normals", C.c_void_p),
+                ("h_texcoords", C.c_void_p), ("h_indices", C.c_void_p),
+                ("n_vertices", C.c_int64), ("n_triangles", C.c_int64),
+                ("material", C.c_int32), ("emission", C.c_float * 3),
+                ("medium_inside", C.c_int32), ("medium_outside", C.c_int32)]
+
+
+class InstanceDesc(C.Structure):
+    _fields_ = [("mesh", C.c_int32), ("transform", C.c_float * 12)]
+
+
+class InfiniteLightDesc(C.Structure):
+    _fields_ = [("tint", C.c_float * 3), ("scale", C.c_float), ("rotation", C.c_float * 9),
+                ("h_image", C.c_void_p), ("width", C.c_int32), ("height", C.c_int32)]
+
+
+class MediumDesc(C.Structure):
+    _fields_ = [("h_density", C.c_void_p), ("nx", C.c_int32), ("ny", C.c_int32),
+                ("nz", C.c_int32), ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3),
+                ("sigma_t", C.c_float * 3), ("albedo", C.c_float * 3), ("g", C.c_float),
+                ("scale", C.c_float), ("majorant_res", C.c_int32 * 3)]
+
+
+class CameraDesc(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("rotation", C.c_float * 9),
+                ("film_size", C.c_float * 2), ("focal_length", C.c_float),
+                ("focal_distance", C.c_float), ("lens_radius", C.c_float),
+                ("aspect_ratio", C.c_float), ("shutter_open", C.c_float),
+                ("shutter_time", C.c_float), ("medium", C.c_int32)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("meshes", C.POINTER(MeshDesc)), ("n_meshes", C.c_int32),
+                ("instances", C.POINTER(InstanceDesc)), ("n_instances", C.c_int32),
+                ("materials", C.POINTER(MaterialDesc)), ("n_materials", C.c_int32),
+                ("infinite_lights", C.POINTER(InfiniteLightDesc)), ("n_infinite_lights", C.c_int32),
+                ("media", C.POINTER(MediumDesc)), ("n_media", C.c_int32)]
+
+
+class AccelStats(C.Structure):
+    _fields_ = [("n_triangles", C.c_int64), ("n_nodes", C.c_int64), ("max_depth", C.c_int32),
+                ("reserved", C.c_int32), ("build_ms", C.c_double), ("node_bytes", C.c_double),
+                ("triangle_bytes", C.c_double)]
+
+
+class WfParams(C.Structure):
+    _fields_ = [("nee", C.c_int32), ("enable_medium", C.c_int32), ("max_depth", C.c_int32),
+                ("rr", C.c_float), ("enable_clamp", C.c_int32), ("clamp_max", C.c_float),
+                ("spp", C.c_int32), ("seed", C.c_uint32)]
+
+
+# name -> (restype, argtypes); every function declared in include/krr_gb300.h
+_P = C.c_void_p
+_I = C.c_int
+SIGNATURES = {
+    "krr_last_error": (C.c_char_p, []),
+    "krr_status_string": (C.c_char_p, [_I]),
+    "krr_version": (_I, []),
+    "krr_accel_create_from_triangles": (_I, [_P, C.c_int64, C.POINTER(_P), _P]),
+    "krr_accel_stats_get": (_I, [_P, C.POINTER(AccelStats)]),
+    "krr_accel_destroy": (_I, [_P]),
+    "krr_accel_trace_closest": (_I, [_P, _P, C.c_int64, _P, _P]),
+    "krr_accel_trace_any": (_I, [_P, _P, C.c_int64, _P, _P]),
+    "krr_accel_set_mask": (_I, [_P, _P]),
+    "krr_accel_trace_closest_host": (_I, [_P, _P, C.c_int64, _P, _P]),
+    "krr_accel_trace_stats": (_I, [_P, _P, C.c_int64, C.c_int32, C.POINTER(C.c_ulonglong), _P]),
+    "krr_wf_params_default": (None, [C.POINTER(WfParams)]),
+    "krr_wf_create": (_I, [C.POINTER(WfParams), C.POINTER(_P)]),
+    "krr_wf_destroy": (_I, [_P]),
+    "krr_wf_set_params": (_I, [_P, C.POINTER(WfParams)]),
+    "krr_wf_set_scene": (_I, [_P, C.POINTER(SceneDesc), _P]),
+    "krr_wf_resize": (_I, [_P, C.c_int32, C.c_int32]),
+    "krr_wf_begin_frame": (_I, [_P, C.c_int64, C.POINTER(CameraDesc), _P]),
+    "krr_wf_render": (_I, [_P, _P, _P]),
+    "krr_wf_generate_camera_rays": (_I, [_P, _P]),
+    "krr_wf_trace_closest": (_I, [_P, C.c_int32, _P]),
+    "krr_wf_handle_hit": (_I, [_P, _P]),
+    "krr_wf_handle_miss": (_I, [_P, _P]),
+    "krr_wf_generate_scatter_rays": (_I, [_P, C.c_int32, _P]),
+    "krr_wf_trace_shadow": (_I, [_P, _P]),
+    "krr_wf_sample_medium_interaction": (_I, [_P, C.c_int32, _P]),
+    "krr_wf_sample_medium_scattering": (_I, [_P, C.c_int32, _P]),
+    "krr_wf_reset_queues": (_I, [_P, C.c_int32, _P]),
+    "krr_wf_queue_size": (_I, [_P, C.c_int32, C.POINTER(C.c_int32), _P]),
+    "krr_wf_pixel_radiance": (_I, [_P, C.POINTER(_P)]),
+    "krr_wf_ray_queue": (_I, [_P, C.c_int32, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P),
+                              C.POINTER(C.c_int32)]),
+    "krr_wf_device_errors": (_I, [_P, C.POINTER(C.c_uint32), _P]),
+    "krr_wf_accel": (_I, [_P, C.POINTER(_P)]),
+}
+
+_lib: C.CDLL | None = None
+
+
+class KrrError(RuntimeError):
+    pass
+
+
+def load() -> C.CDLL:
+    """Loads libkrr_gb300.so; raises if it is missing (no CPU fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise KrrError(f"{LIB_PATH.name} is not built; run kiraray_gb300.build.build() first")
+    lib = C.CDLL(str(LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue   # tests/test_abi.py checks that every declared symbol is exported
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status: int, what: str = "") -> None:
+    if status != KRR_OK:
+        lib = load()
+        msg = lib.krr_last_error().decode(errors="replace")
+        kind = lib.krr_status_string(status).decode()
+        raise KrrError(f"{what}: {kind} ({status}): {msg}")

@@ -1,0 +1,102 @@
+"""Acceleration structure: GPU LBVH -> compressed 8-wide BVH, closest-hit and
+any-hit traversal (the reference's OptiX GAS/IAS and its Closest / Shadow
+programs, src/core/device/optix.cpp:143-398, src/render/wavefront/device.cu:43-100).
+
+Rays are float32 [N, 8] device tensors (origin.xyz, tmin, direction.xyz,
+tmax); closest hits come back as float32 [N, 4] (t, b1, b2, triangle id bits)
+with triangle id KRR_MISS = 0xFFFFFFFF for a miss.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+class Accel:
+    def __init__(self, world_triangles: np.ndarray):
+        lib = _lib.load()
+        v = np.ascontiguousarray(world_triangles, dtype=np.float32).reshape(-1, 9)
+        self._h = C.c_void_p()
+        check(lib.krr_accel_create_from_triangles(v.ctypes.data, v.shape[0], C.byref(self._h),
+                                                  _stream()), "krr_accel_create_from_triangles")
+        self.n_triangles = v.shape[0]
+
+    @classmethod
+    def borrowed(cls, handle: int, n_triangles: int) -> "Accel":
+        obj = cls.__new__(cls)
+        obj._h = C.c_void_p(handle)
+        obj.n_triangles = n_triangles
+        obj._borrowed = True
+        return obj
+
+    def stats(self) -> dict:
+        s = _lib.AccelStats()
+        check(_lib.load().krr_accel_stats_get(self._h, C.byref(s)), "krr_accel_stats_get")
+        return {k: getattr(s, k) for k, _ in s._fields_ if k != "reserved"}
+
+    @staticmethod
+    def _rays(rays: torch.Tensor) -> torch.Tensor:
+        if not (rays.is_cuda and rays.dtype == torch.float32 and rays.dim() == 2 and
+                rays.shape[1] == 8):
+            raise ValueError("rays must be a CUDA float32 tensor of shape [N, 8]")
+        return rays.contiguous()
+
+    def trace_closest(self, rays: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        rays = self._rays(rays)
+        n = rays.shape[0]
+        if out is None:
+            out = torch.empty((n, 4), dtype=torch.float32, device=rays.device)
+        check(_lib.load().krr_accel_trace_closest(self._h, rays.data_ptr(), n, out.data_ptr(),
+                                                  _stream()), "krr_accel_trace_closest")
+        return out
+
+    def trace_any(self, rays: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        rays = self._rays(rays)
+        n = rays.shape[0]
+        if out is None:
+            out = torch.empty((n,), dtype=torch.uint8, device=rays.device)
+        check(_lib.load().krr_accel_trace_any(self._h, rays.data_ptr(), n, out.data_ptr(),
+                                              _stream()), "krr_accel_trace_any")
+        return out
+
+    def trace_closest_host(self, rays: np.ndarray | torch.Tensor,
+                           out: np.ndarray | torch.Tensor) -> None:
+        """Host buffers in and out (pinned tensors are fastest)."""
+        n = rays.shape[0]
+        rp = rays.data_ptr() if isinstance(rays, torch.Tensor) else rays.ctypes.data
+        op = out.data_ptr() if isinstance(out, torch.Tensor) else out.ctypes.data
+        check(_lib.load().krr_accel_trace_closest_host(self._h, rp, n, op, _stream()),
+              "krr_accel_trace_closest_host")
+
+    def trace_stats(self, rays: torch.Tensor, any_hit: bool = False) -> tuple[int, int]:
+        rays = self._rays(rays)
+        counts = (C.c_ulonglong * 2)()
+        check(_lib.load().krr_accel_trace_stats(self._h, rays.data_ptr(), rays.shape[0],
+                                                int(any_hit), counts, _stream()),
+              "krr_accel_trace_stats")
+        return int(counts[0]), int(counts[1])
+
+    def set_mask(self, mask: np.ndarray | None) -> None:
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        check(_lib.load().krr_accel_set_mask(self._h, None if m is None else m.ctypes.data),
+              "krr_accel_set_mask")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value and not getattr(self, "_borrowed", False):
+            _lib.load().krr_accel_destroy(self._h)
+        self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,952 @@
+// GPU BVH builder and traversal.
+//
+// Replaces the OptiX acceleration structures of the reference
+// (OptixScene::buildTriangleMeshGAS / buildASFromInputs,
+// src/core/device/optix.cpp:143-250, and the single-level IAS at :357-398)
+// and the closest-hit / any-hit programs (src/render/wavefront/device.cu:43-100).
+// The reference has no software triangle test (OptiX does it in hardware); the
+// test here is the watertight test of Woop, Benthin and Wald (JCGT 2013).
+//
+// Build: per-triangle bounds -> 63-bit Morton codes of centroids -> radix
+// sort -> Karras (HPG 2012) binary radix tree -> bottom-up bounds -> greedy
+// top-down collapse into compressed 8-wide nodes (Ylitie, Karras, Laine,
+// HPG 2017 layout, own collapse heuristic) -> triangles gathered in leaf order.
+//
+// Traversal: persistent warps that refill idle lanes from a global ray
+// counter, one ray per lane, node groups / triangle groups on a per-lane
+// stack, octant-ordered child visits.  Box tests are conservative (children
+// are widened by a margin before quantisation and compared with a small
+// slack), so the hit set equals brute force; ties in t go to the smaller
+// global triangle id, which makes the closest hit independent of the
+// traversal order.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "accel.h"
+#include "kmath.cuh"
+
+namespace krr {
+namespace {
+
+constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr int kBuildThreads = 256;
+constexpr int kRefillBelow = 20;   // refill a warp when fewer lanes are busy
+
+__device__ __forceinline__ void atomic_min_f(float *addr, float v) {
+    if (v >= 0.f) atomicMin(reinterpret_cast<int *>(addr), __float_as_int(v));
+    else atomicMax(reinterpret_cast<unsigned *>(addr), __float_as_uint(v));
+}
+__device__ __forceinline__ void atomic_max_f(float *addr, float v) {
+    if (v >= 0.f) atomicMax(reinterpret_cast<int *>(addr), __float_as_int(v));
+    else atomicMin(reinterpret_cast<unsigned *>(addr), __float_as_uint(v));
+}
+
+__device__ __forceinline__ V3 ld3(const float *p) { return V3{p[0], p[1], p[2]}; }
+
+// ---------------------------------------------------------------- bounds
+// bounds[0..2] = centroid min, [3..5] = centroid max, [6..8] = geometry min,
+// [9..11] = geometry max.
+__global__ void k_scene_bounds(const float *__restrict__ v, int64_t n, float *bounds) {
+    V3 cmin = v3(INFINITY), cmax = v3(-INFINITY), gmin = v3(INFINITY), gmax = v3(-INFINITY);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        V3 a = ld3(v + 9 * i), b = ld3(v + 9 * i + 3), c = ld3(v + 9 * i + 6);
+        V3 lo = vmin(a, vmin(b, c)), hi = vmax(a, vmax(b, c));
+        V3 ce = (lo + hi) * 0.5f;
+        cmin = vmin(cmin, ce); cmax = vmax(cmax, ce);
+        gmin = vmin(gmin, lo); gmax = vmax(gmax, hi);
+    }
+    float vals[12] = {cmin.x, cmin.y, cmin.z, cmax.x, cmax.y, cmax.z,
+                      gmin.x, gmin.y, gmin.z, gmax.x, gmax.y, gmax.z};
+    for (int k = 0; k < 12; ++k) {
+        float x = vals[k];
+        bool is_min = (k % 6) < 3;
+        for (int off = 16; off > 0; off >>= 1) {
+            float y = __shfl_xor_sync(0xffffffffu, x, off);
+            x = is_min ? fminf(x, y) : fmaxf(x, y);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            if (is_min) atomic_min_f(bounds + k, x);
+            else atomic_max_f(bounds + k, x);
+        }
+    }
+}
+
+__device__ __forceinline__ uint64_t spread21(uint32_t x) {
+    uint64_t v = x & 0x1fffffu;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+// Morton codes of centroids and margin-widened leaf boxes.
+__global__ void k_leaf_setup(const float *__restrict__ v, int64_t n, const float *bounds,
+                             float margin, uint64_t *keys, uint32_t *vals, float4 *leaf_lo,
+                             float4 *leaf_hi) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    V3 a = ld3(v + 9 * i), b = ld3(v + 9 * i + 3), c = ld3(v + 9 * i + 6);
+    V3 lo = vmin(a, vmin(b, c)), hi = vmax(a, vmax(b, c));
+    V3 ce = (lo + hi) * 0.5f;
+    V3 cmin = ld3(bounds), cmax = ld3(bounds + 3);
+    V3 ext = cmax - cmin;
+    float q[3];
+    for (int k = 0; k < 3; ++k) {
+        float e = get(ext, k);
+        float t = e > 0.f ? (get(ce, k) - get(cmin, k)) / e : 0.5f;
+        q[k] = fminf(fmaxf(t * 2097152.f, 0.f), 2097151.f);
+    }
+    keys[i] = (spread21((uint32_t)q[0]) << 2) | (spread21((uint32_t)q[1]) << 1) |
+              spread21((uint32_t)q[2]);
+    vals[i] = (uint32_t)i;
+    leaf_lo[i] = make_float4(lo.x - margin, lo.y - margin, lo.z - margin, 0.f);
+    leaf_hi[i] = make_float4(hi.x + margin, hi.y + margin, hi.z + margin, 0.f);
+}
+
+__device__ __forceinline__ int delta_fn(const uint64_t *k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    uint64_t a = k[i], b = k[j];
+    if (a == b) return 64 + __clz((uint32_t)(i ^ j));
+    return __clzll(a ^ b);
+}
+
+// Karras 2012 radix tree: internal node i covers [first, last].
+__global__ void k_karras(const uint64_t *__restrict__ keys, int n, uint32_t *left,
+                         uint32_t *right, int *first, int *last, int *parent_int,
+                         int *parent_leaf) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int d = (delta_fn(keys, n, i, i + 1) - delta_fn(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = delta_fn(keys, n, i, i - d);
+    int lmax = 2;
+    while (delta_fn(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (delta_fn(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = delta_fn(keys, n, i, j);
+    int s = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (delta_fn(keys, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    int gamma = i + s * d + min(d, 0);
+    int lo = min(i, j), hi = max(i, j);
+    first[i] = lo;
+    last[i] = hi;
+    if (lo == gamma) { left[i] = kLeafBit | gamma; parent_leaf[gamma] = i; }
+    else { left[i] = gamma; parent_int[gamma] = i; }
+    if (hi == gamma + 1) { right[i] = kLeafBit | (gamma + 1); parent_leaf[gamma + 1] = i; }
+    else { right[i] = gamma + 1; parent_int[gamma + 1] = i; }
+    if (i == 0) parent_int[0] = -1;
+}
+
+// Leaf boxes are indexed by sorted position; internal boxes by node index.
+__global__ void k_gather_leaf_boxes(const uint32_t *__restrict__ sorted_idx, int n,
+                                    const float4 *__restrict__ lo_in,
+                                    const float4 *__restrict__ hi_in, float4 *lo_out,
+                                    float4 *hi_out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t p = sorted_idx[i];
+    lo_out[i] = lo_in[p];
+    hi_out[i] = hi_in[p];
+}
+
+__global__ void k_bottom_up(int n, const uint32_t *__restrict__ left,
+                            const uint32_t *__restrict__ right, const int *__restrict__ parent_int,
+                            const int *__restrict__ parent_leaf, const float4 *leaf_lo,
+                            const float4 *leaf_hi, float4 *int_lo, float4 *int_hi, int *flags) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int node = parent_leaf[i];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(flags + node, 1) == 0) return;
+        __threadfence();
+        uint32_t l = left[node], r = right[node];
+        float4 llo = (l & kLeafBit) ? leaf_lo[l & ~kLeafBit] : __ldcg(int_lo + l);
+        float4 lhi = (l & kLeafBit) ? leaf_hi[l & ~kLeafBit] : __ldcg(int_hi + l);
+        float4 rlo = (r & kLeafBit) ? leaf_lo[r & ~kLeafBit] : __ldcg(int_lo + r);
+        float4 rhi = (r & kLeafBit) ? leaf_hi[r & ~kLeafBit] : __ldcg(int_hi + r);
+        float4 lo = make_float4(fminf(llo.x, rlo.x), fminf(llo.y, rlo.y), fminf(llo.z, rlo.z), 0.f);
+        float4 hi = make_float4(fmaxf(lhi.x, rhi.x), fmaxf(lhi.y, rhi.y), fmaxf(lhi.z, rhi.z), 0.f);
+        __stcg(int_lo + node, lo);
+        __stcg(int_hi + node, hi);
+        node = parent_int[node];
+    }
+}
+
+// ------------------------------------------------------------- collapse
+struct CollapseItem {
+    uint32_t bref;    // binary node ref (kLeafBit | sorted leaf) or internal index
+    uint32_t wnode;   // destination 8-wide node
+    int depth;
+};
+
+struct BinTree {
+    const uint32_t *left, *right;
+    const int *first, *last;
+    const float4 *int_lo, *int_hi, *leaf_lo, *leaf_hi;
+    const uint32_t *sorted_idx;
+};
+
+__device__ __forceinline__ void ref_info(const BinTree &t, uint32_t ref, V3 &lo, V3 &hi,
+                                         int &first, int &count) {
+    if (ref & kLeafBit) {
+        uint32_t k = ref & ~kLeafBit;
+        lo = f3(t.leaf_lo[k]); hi = f3(t.leaf_hi[k]);
+        first = (int)k; count = 1;
+    } else {
+        lo = f3(t.int_lo[ref]); hi = f3(t.int_hi[ref]);
+        first = t.first[ref]; count = t.last[ref] - t.first[ref] + 1;
+    }
+}
+
+__device__ __forceinline__ float half_area(V3 lo, V3 hi) {
+    V3 e = hi - lo;
+    return e.x * e.y + e.y * e.z + e.z * e.x;
+}
+
+__device__ __forceinline__ int quant_exponent(float ext) {
+    // smallest k with 2^k * 255 >= ext
+    float s = ext * (1.0f + 1.0f / 1048576.f) / 255.f;
+    int e;
+    float m = frexpf(s, &e);   // s = m * 2^e, m in [0.5, 1)
+    int k = (m == 0.5f) ? e - 1 : e;
+    return max(min(k, 127), -126);
+}
+
+__global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const int *n_in,
+                           CollapseItem *out, int *n_out, float4 *nodes, int *node_counter,
+                           uint32_t *leaf_order, int *tri_counter, int *max_depth) {
+    int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= *n_in) return;
+    CollapseItem item = in[w];
+
+    uint32_t ref[8];
+    V3 clo[8], chi[8];
+    int cfirst[8], ccount[8];
+    int nc = 1;
+    ref[0] = item.bref;
+    ref_info(t, ref[0], clo[0], chi[0], cfirst[0], ccount[0]);
+    // Greedily open the largest child that cannot be a leaf (more than three
+    // triangles) or, once all can be leaves, the largest internal one while
+    // slots remain.
+    while (nc < 8) {
+        int best = -1;
+        float best_area = -1.f;
+        bool best_must = false;
+        for (int c = 0; c < nc; ++c) {
+            if (ref[c] & kLeafBit) continue;
+            bool must = ccount[c] > 3;
+            float a = half_area(clo[c], chi[c]);
+            if ((must && !best_must) || (must == best_must && a > best_area)) {
+                best = c; best_area = a; best_must = must;
+            }
+        }
+        if (best < 0 || !best_must) break;
+        uint32_t r = ref[best];
+        ref[best] = t.left[r];
+        ref_info(t, ref[best], clo[best], chi[best], cfirst[best], ccount[best]);
+        ref[nc] = t.right[r];
+        ref_info(t, ref[nc], clo[nc], chi[nc], cfirst[nc], ccount[nc]);
+        ++nc;
+    }
+
+    // Node bounds and quantisation frame.
+    V3 lo = clo[0], hi = chi[0];
+    for (int c = 1; c < nc; ++c) { lo = vmin(lo, clo[c]); hi = vmax(hi, chi[c]); }
+    int ek[3];
+    float escale[3];
+    for (int k = 0; k < 3; ++k) {
+        ek[k] = quant_exponent(get(hi, k) - get(lo, k));
+        escale[k] = ldexpf(1.f, ek[k]);
+    }
+
+    // Octant slot assignment: slot s gets the child nearest for direction
+    // octant s (greedy on dot(child centre - node centre, dir_s)).
+    V3 pc = (lo + hi) * 0.5f;
+    int slot_of[8];
+    int child_in_slot[8];
+    for (int s = 0; s < 8; ++s) child_in_slot[s] = -1;
+    for (int c = 0; c < nc; ++c) slot_of[c] = -1;
+    for (int it = 0; it < nc; ++it) {
+        float best = INFINITY;
+        int bc = -1, bs = -1;
+        for (int c = 0; c < nc; ++c) {
+            if (slot_of[c] >= 0) continue;
+            V3 d = (clo[c] + chi[c]) * 0.5f - pc;
+            for (int s = 0; s < 8; ++s) {
+                if (child_in_slot[s] >= 0) continue;
+                float cost = ((s & 1) ? -d.x : d.x) + ((s & 2) ? -d.y : d.y) + ((s & 4) ? -d.z : d.z);
+                if (cost < best) { best = cost; bc = c; bs = s; }
+            }
+        }
+        if (bc < 0) break;
+        slot_of[bc] = bs;
+        child_in_slot[bs] = bc;
+    }
+
+    // Allocate internal children and leaf triangles.
+    int n_int = 0, n_tri = 0;
+    for (int c = 0; c < nc; ++c) {
+        if (ccount[c] > 3) ++n_int;
+        else n_tri += ccount[c];
+    }
+    int child_base = n_int ? atomicAdd(node_counter, n_int) : 0;
+    int tri_base = n_tri ? atomicAdd(tri_counter, n_tri) : 0;
+    if (n_int) atomicMax(max_depth, item.depth + 1);
+
+    uint32_t meta[2] = {0, 0};
+    uint32_t qlo[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    uint32_t qhi[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    uint32_t imask = 0;
+    int int_rank = 0, tri_off = 0;
+    for (int s = 0; s < 8; ++s) {
+        int c = child_in_slot[s];
+        if (c < 0) continue;
+        for (int k = 0; k < 3; ++k) {
+            float p = get(lo, k), e = escale[k];
+            float a = floorf((get(clo[c], k) - p) / e);
+            float b = ceilf((get(chi[c], k) - p) / e);
+            a = fminf(fmaxf(a, 0.f), 255.f);
+            b = fminf(fmaxf(b, 0.f), 255.f);
+            while (a > 0.f && fmaf(a, e, p) > get(clo[c], k)) a -= 1.f;
+            while (b < 255.f && fmaf(b, e, p) < get(chi[c], k)) b += 1.f;
+            qlo[k][s >> 2] |= (uint32_t)a << (8 * (s & 3));
+            qhi[k][s >> 2] |= (uint32_t)b << (8 * (s & 3));
+        }
+        uint32_t m;
+        if (ccount[c] > 3) {
+            m = 0x80u;
+            imask |= 1u << s;
+        } else {
+            m = ((uint32_t)ccount[c] << 5) | (uint32_t)tri_off;
+            for (int k = 0; k < ccount[c]; ++k)
+                leaf_order[tri_base + tri_off + k] = t.sorted_idx[cfirst[c] + k];
+            tri_off += ccount[c];
+        }
+        meta[s >> 2] |= m << (8 * (s & 3));
+    }
+    // internal children in slot order
+    for (int s = 0; s < 8; ++s) {
+        int c = child_in_slot[s];
+        if (c < 0 || ccount[c] <= 3) continue;
+        int slot = atomicAdd(n_out, 1);
+        out[slot] = CollapseItem{ref[c], (uint32_t)(child_base + int_rank), item.depth + 1};
+        ++int_rank;
+    }
+
+    uint32_t ew = (uint32_t)(ek[0] + 127) | ((uint32_t)(ek[1] + 127) << 8) |
+                  ((uint32_t)(ek[2] + 127) << 16) | (imask << 24);
+    float4 *np = nodes + 5 * (size_t)item.wnode;
+    np[0] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(ew));
+    np[1] = make_float4(__uint_as_float((uint32_t)child_base), __uint_as_float((uint32_t)tri_base),
+                        __uint_as_float(meta[0]), __uint_as_float(meta[1]));
+    np[2] = make_float4(__uint_as_float(qlo[0][0]), __uint_as_float(qlo[0][1]),
+                        __uint_as_float(qlo[1][0]), __uint_as_float(qlo[1][1]));
+    np[3] = make_float4(__uint_as_float(qlo[2][0]), __uint_as_float(qlo[2][1]),
+                        __uint_as_float(qhi[0][0]), __uint_as_float(qhi[0][1]));
+    np[4] = make_float4(__uint_as_float(qhi[1][0]), __uint_as_float(qhi[1][1]),
+                        __uint_as_float(qhi[2][0]), __uint_as_float(qhi[2][1]));
+}
+
+__global__ void k_gather_tris(const float *__restrict__ v, const uint32_t *__restrict__ leaf_order,
+                              int64_t n, float4 *tris, uint32_t *leaf_of_prim) {
+    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t p = leaf_order[k];
+    const float *s = v + 9 * (size_t)p;
+    tris[3 * k + 0] = make_float4(s[0], s[1], s[2], __uint_as_float(p));
+    tris[3 * k + 1] = make_float4(s[3], s[4], s[5], __uint_as_float(1u));
+    tris[3 * k + 2] = make_float4(s[6], s[7], s[8], 0.f);
+    leaf_of_prim[p] = (uint32_t)k;
+}
+
+__global__ void k_set_mask(float4 *tris, const uint32_t *leaf_of_prim, const uint8_t *mask,
+                           int64_t n) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    uint32_t k = leaf_of_prim[p];
+    tris[3 * (size_t)k + 1].w = __uint_as_float(mask ? (uint32_t)(mask[p] != 0) : 1u);
+}
+
+// ------------------------------------------------------------ traversal
+struct RayPre {
+    V3 o, d;
+    float tmin;
+    int kx, ky, kz;
+    float sx, sy, sz;
+};
+
+__device__ __forceinline__ RayPre ray_pre(V3 o, V3 d, float tmin) {
+    RayPre r;
+    r.o = o; r.d = d; r.tmin = tmin;
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    int kx = kz + 1 == 3 ? 0 : kz + 1;
+    int ky = kx + 1 == 3 ? 0 : kx + 1;
+    if (get(d, kz) < 0.f) { int tmp = kx; kx = ky; ky = tmp; }
+    r.kx = kx; r.ky = ky; r.kz = kz;
+    float dz = get(d, kz);
+    r.sx = __fdiv_rn(get(d, kx), dz);
+    r.sy = __fdiv_rn(get(d, ky), dz);
+    r.sz = __fdiv_rn(1.0f, dz);
+    return r;
+}
+
+__device__ __forceinline__ float sel3(float a, float b, float c, int k) {
+    return k == 0 ? a : (k == 1 ? b : c);
+}
+
+// Watertight ray/triangle test; returns t (NaN on a miss, so that a miss fails
+// every comparison including the tie rule at t == tmax == inf) and (b1, b2).
+// Every operation is explicitly rounded so that the CPU restatement of the
+// same steps gives bit-identical results.
+__device__ __forceinline__ float tri_test(const RayPre &r, float4 v0, float4 v1, float4 v2,
+                                          float &b1, float &b2) {
+    float Ax_ = __fsub_rn(v0.x, r.o.x), Ay_ = __fsub_rn(v0.y, r.o.y), Az_ = __fsub_rn(v0.z, r.o.z);
+    float Bx_ = __fsub_rn(v1.x, r.o.x), By_ = __fsub_rn(v1.y, r.o.y), Bz_ = __fsub_rn(v1.z, r.o.z);
+    float Cx_ = __fsub_rn(v2.x, r.o.x), Cy_ = __fsub_rn(v2.y, r.o.y), Cz_ = __fsub_rn(v2.z, r.o.z);
+    float Akx = sel3(Ax_, Ay_, Az_, r.kx), Aky = sel3(Ax_, Ay_, Az_, r.ky), Akz = sel3(Ax_, Ay_, Az_, r.kz);
+    float Bkx = sel3(Bx_, By_, Bz_, r.kx), Bky = sel3(Bx_, By_, Bz_, r.ky), Bkz = sel3(Bx_, By_, Bz_, r.kz);
+    float Ckx = sel3(Cx_, Cy_, Cz_, r.kx), Cky = sel3(Cx_, Cy_, Cz_, r.ky), Ckz = sel3(Cx_, Cy_, Cz_, r.kz);
+    float Ax = __fmaf_rn(-r.sx, Akz, Akx), Ay = __fmaf_rn(-r.sy, Akz, Aky);
+    float Bx = __fmaf_rn(-r.sx, Bkz, Bkx), By = __fmaf_rn(-r.sy, Bkz, Bky);
+    float Cx = __fmaf_rn(-r.sx, Ckz, Ckx), Cy = __fmaf_rn(-r.sy, Ckz, Cky);
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.f || V == 0.f || W == 0.f) {
+        U = (float)__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx));
+        V = (float)__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx));
+        W = (float)__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax));
+    }
+    if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return __int_as_float(0x7fffffff);
+    float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.f) return __int_as_float(0x7fffffff);
+    float Az = __fmul_rn(r.sz, Akz), Bz = __fmul_rn(r.sz, Bkz), Cz = __fmul_rn(r.sz, Ckz);
+    float T = __fmaf_rn(U, Az, __fmaf_rn(V, Bz, __fmul_rn(W, Cz)));
+    float rcp = __frcp_rn(det);
+    float t = __fmul_rn(T, rcp);
+    b1 = __fmul_rn(V, rcp);
+    b2 = __fmul_rn(W, rcp);
+    return t;
+}
+
+__device__ __forceinline__ float byte_to_float(uint32_t w, int k) {
+    return __uint_as_float(0x4B000000u | ((w >> (8 * k)) & 0xffu)) - 8388608.0f;
+}
+
+template <bool ANY, bool STATS>
+__global__ void __launch_bounds__(kTraceThreads)
+k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, TraceLaunch L,
+        unsigned long long *stats) {
+    const int lane = threadIdx.x & 31;
+    const int64_t n = L.d_count ? (int64_t)*L.d_count : L.n;
+    uint2 stack[kTraversalStack];
+    int sp = 0;
+    bool active = false, exhausted = false;
+    int64_t ray_id = 0;
+    RayPre r;
+    V3 inv;
+    int oct = 0;
+    float tmax = 0.f;
+    uint2 ng = make_uint2(0, 0), tg = make_uint2(0, 0);
+    float best_b1 = 0.f, best_b2 = 0.f;
+    uint32_t best_prim = KRR_MISS;
+    unsigned long long n_nodes = 0, n_tris = 0;
+
+    while (true) {
+        unsigned act = __ballot_sync(0xffffffffu, active);
+        if (__popc(act) < kRefillBelow && !exhausted) {
+            unsigned need = ~act;
+            int leader = __ffs(need) - 1;
+            long long base = 0;
+            if (lane == leader) base = atomicAdd(reinterpret_cast<unsigned long long *>(L.counter),
+                                                 (unsigned long long)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (base + __popc(need) >= n) exhausted = true;
+            if (!active) {
+                int64_t idx = base + __popc(need & ((1u << lane) - 1));
+                if (idx < n) {
+                    ray_id = idx;
+                    float4 ro = L.ray_o[idx * L.ray_stride];
+                    float4 rd = L.ray_d[idx * L.ray_stride];
+                    V3 o = f3(ro), d = f3(rd);
+                    r = ray_pre(o, d, ro.w);
+                    tmax = rd.w;
+                    float dx = fabsf(d.x) < 1e-20f ? copysignf(1e-20f, d.x) : d.x;
+                    float dy = fabsf(d.y) < 1e-20f ? copysignf(1e-20f, d.y) : d.y;
+                    float dz = fabsf(d.z) < 1e-20f ? copysignf(1e-20f, d.z) : d.z;
+                    inv = V3{1.f / dx, 1.f / dy, 1.f / dz};
+                    oct = (inv.x < 0.f ? 1 : 0) | (inv.y < 0.f ? 2 : 0) | (inv.z < 0.f ? 4 : 0);
+                    ng = make_uint2(0u, (1u << oct) | (1u << 8));
+                    tg = make_uint2(0u, 0u);
+                    sp = 0;
+                    best_prim = KRR_MISS;
+                    active = true;
+                }
+            }
+            act = __ballot_sync(0xffffffffu, active);
+        }
+        if (act == 0) break;
+        if (!active) continue;
+
+        // ---- one traversal step: optional node visit, its triangles, pop
+        bool done = false;
+        if (ng.y & 0xffu) {
+            int p = __ffs(ng.y & 0xffu) - 1;
+            ng.y &= ~(1u << p);
+            int slot = p ^ oct;
+            uint32_t imask = ng.y >> 8;
+            uint32_t child = ng.x + __popc(imask & ((1u << slot) - 1u));
+            if (ng.y & 0xffu) {
+                if (sp < kTraversalStack) stack[sp++] = ng;
+                else { atomicOr(L.err, (int)kErrStackOverflow); done = true; }
+            }
+            if (STATS) ++n_nodes;
+            const float4 *np = nodes + 5 * (size_t)child;
+            float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3),
+                   q4 = __ldg(np + 4);
+            uint32_t ew = __float_as_uint(q0.w);
+            float ex = __uint_as_float((ew & 0xffu) << 23);
+            float ey = __uint_as_float(((ew >> 8) & 0xffu) << 23);
+            float ez = __uint_as_float(((ew >> 16) & 0xffu) << 23);
+            float adx = ex * inv.x, ady = ey * inv.y, adz = ez * inv.z;
+            float orx = (q0.x - r.o.x) * inv.x, ory = (q0.y - r.o.y) * inv.y,
+                  orz = (q0.z - r.o.z) * inv.z;
+            uint32_t lox0 = __float_as_uint(q2.x), lox1 = __float_as_uint(q2.y);
+            uint32_t loy0 = __float_as_uint(q2.z), loy1 = __float_as_uint(q2.w);
+            uint32_t loz0 = __float_as_uint(q3.x), loz1 = __float_as_uint(q3.y);
+            uint32_t hix0 = __float_as_uint(q3.z), hix1 = __float_as_uint(q3.w);
+            uint32_t hiy0 = __float_as_uint(q4.x), hiy1 = __float_as_uint(q4.y);
+            uint32_t hiz0 = __float_as_uint(q4.z), hiz1 = __float_as_uint(q4.w);
+            uint32_t nx0 = (oct & 1) ? hix0 : lox0, nx1 = (oct & 1) ? hix1 : lox1;
+            uint32_t fx0 = (oct & 1) ? lox0 : hix0, fx1 = (oct & 1) ? lox1 : hix1;
+            uint32_t ny0 = (oct & 2) ? hiy0 : loy0, ny1 = (oct & 2) ? hiy1 : loy1;
+            uint32_t fy0 = (oct & 2) ? loy0 : hiy0, fy1 = (oct & 2) ? loy1 : hiy1;
+            uint32_t nz0 = (oct & 4) ? hiz0 : loz0, nz1 = (oct & 4) ? hiz1 : loz1;
+            uint32_t fz0 = (oct & 4) ? loz0 : hiz0, fz1 = (oct & 4) ? loz1 : hiz1;
+            uint32_t meta0 = __float_as_uint(q1.z), meta1 = __float_as_uint(q1.w);
+            const float tlimit = tmax + fabsf(tmax) * 5e-7f;
+            uint32_t nbits = 0, tbits = 0;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const int k = c & 3;
+                uint32_t m = ((c < 4 ? meta0 : meta1) >> (8 * k)) & 0xffu;
+                float tnx = fmaf(byte_to_float(c < 4 ? nx0 : nx1, k), adx, orx);
+                float tny = fmaf(byte_to_float(c < 4 ? ny0 : ny1, k), ady, ory);
+                float tnz = fmaf(byte_to_float(c < 4 ? nz0 : nz1, k), adz, orz);
+                float tfx = fmaf(byte_to_float(c < 4 ? fx0 : fx1, k), adx, orx);
+                float tfy = fmaf(byte_to_float(c < 4 ? fy0 : fy1, k), ady, ory);
+                float tfz = fmaf(byte_to_float(c < 4 ? fz0 : fz1, k), adz, orz);
+                float t0 = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
+                float t1 = fminf(fminf(tfx, tfy), fminf(tfz, tlimit));
+                bool hit = (m != 0u) && (t0 <= t1);
+                if (hit) {
+                    if (m & 0x80u) nbits |= 1u << (c ^ oct);
+                    else tbits |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+                }
+            }
+            uint32_t cimask = ew >> 24;
+            ng = make_uint2(__float_as_uint(q1.x), nbits | (cimask << 8));
+            tg = make_uint2(__float_as_uint(q1.y), tbits);
+        }
+        while (tg.y && !done) {
+            int b = __ffs(tg.y) - 1;
+            tg.y &= tg.y - 1u;
+            const float4 *tp = tris + 3 * (size_t)(tg.x + b);
+            float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+            if (STATS) ++n_tris;
+            float b1, b2;
+            float t = tri_test(r, v0, v1, v2, b1, b2);
+            uint32_t gid = __float_as_uint(v0.w);
+            if (ANY) {
+                if (t > r.tmin && t <= tmax && __float_as_uint(v1.w) != 0u) {
+                    best_prim = gid;
+                    done = true;
+                }
+            } else {
+                if (t > r.tmin && (t < tmax || (t == tmax && gid < best_prim))) {
+                    tmax = t; best_b1 = b1; best_b2 = b2; best_prim = gid;
+                }
+            }
+        }
+        if (!done && !(ng.y & 0xffu)) {
+            if (sp > 0) ng = stack[--sp];
+            else done = true;
+        }
+        if (done) {
+            if (ANY) {
+                L.occluded[ray_id] = best_prim != KRR_MISS ? 1 : 0;
+            } else {
+                float4 h = best_prim != KRR_MISS
+                               ? make_float4(tmax, best_b1, best_b2, __uint_as_float(best_prim))
+                               : make_float4(INFINITY, 0.f, 0.f, __uint_as_float(KRR_MISS));
+                L.hits[ray_id] = h;
+            }
+            active = false;
+        }
+    }
+    if (STATS) {
+        atomicAdd(stats, n_nodes);
+        atomicAdd(stats + 1, n_tris);
+    }
+}
+
+int g_grid_size = 0;
+
+}  // namespace
+
+int traversal_grid_size() {
+    if (g_grid_size) return g_grid_size;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<false, false>, kTraceThreads, 0);
+    if (per_sm < 1) per_sm = 1;
+    g_grid_size = sms * per_sm;
+    return g_grid_size;
+}
+
+template <bool ANY, bool STATS>
+static int launch_trace(const krr_accel *a, const TraceLaunch &l, cudaStream_t s,
+                        unsigned long long *stats = nullptr) {
+    if (!a || !a->d_nodes) return fail(KRR_ERR_NOT_READY, "acceleration structure not built");
+    KRR_CUDA(cudaMemsetAsync(l.counter, 0, sizeof(unsigned long long), s));
+    if (a->n_tris == 0) return KRR_OK;
+    k_trace<ANY, STATS><<<traversal_grid_size(), kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, l, stats);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+int launch_trace_closest(const krr_accel *a, const TraceLaunch &l, cudaStream_t s) {
+    return launch_trace<false, false>(a, l, s);
+}
+int launch_trace_any(const krr_accel *a, const TraceLaunch &l, cudaStream_t s) {
+    return launch_trace<true, false>(a, l, s);
+}
+int launch_trace_stats(const krr_accel *a, const TraceLaunch &l, bool any,
+                       unsigned long long *d_stats, cudaStream_t s) {
+    return any ? launch_trace<true, true>(a, l, s, d_stats) : launch_trace<false, true>(a, l, s, d_stats);
+}
+
+void accel_free(krr_accel *a) {
+    if (!a) return;
+    cudaFree(a->d_nodes);
+    cudaFree(a->d_tris);
+    cudaFree(a->d_leaf_of_prim);
+    cudaFree(a->d_scratch);
+    a->d_nodes = nullptr;
+    a->d_tris = nullptr;
+    a->d_leaf_of_prim = nullptr;
+    a->d_scratch = nullptr;
+}
+
+namespace {
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    ~DevBuf() { cudaFree(p); }
+    cudaError_t alloc(size_t n) { return cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)); }
+};
+inline unsigned blocks_for(int64_t n, int t = kBuildThreads) { return (unsigned)((n + t - 1) / t); }
+}  // namespace
+
+int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
+    KRR_CHECK_ARG(n >= 0 && n < (int64_t)0x7fffffff, "triangle count out of range");
+    accel_free(a);
+    a->n_tris = n;
+    a->n_nodes = 0;
+    a->max_depth = 0;
+    KRR_CUDA(cudaMalloc(&a->d_scratch, 64));
+    KRR_CUDA(cudaMemsetAsync(a->d_scratch, 0, 64, s));
+    if (n == 0) return KRR_OK;
+
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+
+    // scene bounds
+    DevBuf<float> bounds;
+    KRR_CUDA(bounds.alloc(12));
+    float init[12] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY,
+                      INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    KRR_CUDA(cudaMemcpyAsync(bounds.p, init, sizeof(init), cudaMemcpyHostToDevice, s));
+    k_scene_bounds<<<std::min<unsigned>(blocks_for(n), 4096), kBuildThreads, 0, s>>>(d_v, n, bounds.p);
+    KRR_CUDA(cudaGetLastError());
+    float hb[12];
+    KRR_CUDA(cudaMemcpyAsync(hb, bounds.p, sizeof(hb), cudaMemcpyDeviceToHost, s));
+    KRR_CUDA(cudaStreamSynchronize(s));
+    for (int k = 0; k < 3; ++k) { a->scene_lo[k] = hb[6 + k]; a->scene_hi[k] = hb[9 + k]; }
+    if (!std::isfinite(hb[6]) || !std::isfinite(hb[9]) || !std::isfinite(hb[7]) ||
+        !std::isfinite(hb[10]) || !std::isfinite(hb[8]) || !std::isfinite(hb[11]))
+        return fail(KRR_ERR_INVALID_ARGUMENT, "triangle vertices are not finite");
+    // Margin that keeps quantised boxes conservative: a few float ulps of the
+    // largest coordinate magnitude and of the scene extent.
+    float mag = 0.f, ext = 0.f;
+    for (int k = 0; k < 3; ++k) {
+        mag = std::max(mag, std::max(std::fabs(hb[6 + k]), std::fabs(hb[9 + k])));
+        ext = std::max(ext, hb[9 + k] - hb[6 + k]);
+    }
+    float margin = std::ldexp(mag + ext, -19) + 1e-30f;
+
+    DevBuf<uint64_t> keys, keys2;
+    DevBuf<uint32_t> vals, vals2;
+    DevBuf<float4> tlo, thi, llo, lhi, ilo, ihi;
+    KRR_CUDA(keys.alloc(n)); KRR_CUDA(keys2.alloc(n));
+    KRR_CUDA(vals.alloc(n)); KRR_CUDA(vals2.alloc(n));
+    KRR_CUDA(tlo.alloc(n)); KRR_CUDA(thi.alloc(n));
+    k_leaf_setup<<<blocks_for(n), kBuildThreads, 0, s>>>(d_v, n, bounds.p, margin, keys.p, vals.p,
+                                                          tlo.p, thi.p);
+    KRR_CUDA(cudaGetLastError());
+
+    // sort by Morton code
+    {
+        size_t tmp_bytes = 0;
+        cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys.p, keys2.p, vals.p, vals2.p, (int)n,
+                                        0, 63, s);
+        DevBuf<uint8_t> tmp;
+        KRR_CUDA(tmp.alloc(tmp_bytes));
+        KRR_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys.p, keys2.p, vals.p, vals2.p,
+                                                 (int)n, 0, 63, s));
+    }
+    const uint64_t *skeys = keys2.p;
+    const uint32_t *sidx = vals2.p;
+
+    KRR_CUDA(llo.alloc(n)); KRR_CUDA(lhi.alloc(n));
+    k_gather_leaf_boxes<<<blocks_for(n), kBuildThreads, 0, s>>>(sidx, (int)n, tlo.p, thi.p, llo.p, lhi.p);
+    KRR_CUDA(cudaGetLastError());
+
+    int64_t ni = std::max<int64_t>(n - 1, 1);
+    DevBuf<uint32_t> left, right;
+    DevBuf<int> first, last, par_int, par_leaf, flags;
+    KRR_CUDA(left.alloc(ni)); KRR_CUDA(right.alloc(ni));
+    KRR_CUDA(first.alloc(ni)); KRR_CUDA(last.alloc(ni));
+    KRR_CUDA(par_int.alloc(ni)); KRR_CUDA(par_leaf.alloc(n)); KRR_CUDA(flags.alloc(ni));
+    KRR_CUDA(ilo.alloc(ni)); KRR_CUDA(ihi.alloc(ni));
+    KRR_CUDA(cudaMemsetAsync(flags.p, 0, ni * sizeof(int), s));
+    if (n > 1) {
+        k_karras<<<blocks_for(n - 1), kBuildThreads, 0, s>>>(skeys, (int)n, left.p, right.p, first.p,
+                                                              last.p, par_int.p, par_leaf.p);
+        KRR_CUDA(cudaGetLastError());
+        k_bottom_up<<<blocks_for(n), kBuildThreads, 0, s>>>((int)n, left.p, right.p, par_int.p,
+                                                             par_leaf.p, llo.p, lhi.p, ilo.p, ihi.p,
+                                                             flags.p);
+        KRR_CUDA(cudaGetLastError());
+    }
+
+    // collapse, level by level
+    int64_t max_nodes = std::max<int64_t>(n, 2);
+    DevBuf<float4> nodes_tmp;
+    DevBuf<uint32_t> leaf_order;
+    DevBuf<CollapseItem> qa, qb;
+    DevBuf<int> counters;   // [0] node counter, [1] tri counter, [2] max depth, [3] n_in, [4] n_out
+    KRR_CUDA(nodes_tmp.alloc(5 * max_nodes));
+    KRR_CUDA(leaf_order.alloc(n));
+    KRR_CUDA(qa.alloc(max_nodes)); KRR_CUDA(qb.alloc(max_nodes));
+    KRR_CUDA(counters.alloc(8));
+    int hc[8] = {1, 0, 0, 1, 0, 0, 0, 0};
+    KRR_CUDA(cudaMemcpyAsync(counters.p, hc, sizeof(hc), cudaMemcpyHostToDevice, s));
+    CollapseItem root{n > 1 ? 0u : (kLeafBit | 0u), 0u, 1};
+    KRR_CUDA(cudaMemcpyAsync(qa.p, &root, sizeof(root), cudaMemcpyHostToDevice, s));
+    BinTree bt{left.p, right.p, first.p, last.p, ilo.p, ihi.p, llo.p, lhi.p, sidx};
+    int n_in = 1;
+    CollapseItem *qin = qa.p, *qout = qb.p;
+    int *c_in = counters.p + 3, *c_out = counters.p + 4;
+    int levels = 0;
+    while (n_in > 0) {
+        KRR_CUDA(cudaMemsetAsync(c_out, 0, sizeof(int), s));
+        k_collapse<<<blocks_for(n_in, 128), 128, 0, s>>>(bt, qin, c_in, qout, c_out, nodes_tmp.p,
+                                                         counters.p, leaf_order.p, counters.p + 1,
+                                                         counters.p + 2);
+        KRR_CUDA(cudaGetLastError());
+        KRR_CUDA(cudaMemcpyAsync(&n_in, c_out, sizeof(int), cudaMemcpyDeviceToHost, s));
+        KRR_CUDA(cudaMemcpyAsync(c_in, c_out, sizeof(int), cudaMemcpyDeviceToDevice, s));
+        KRR_CUDA(cudaStreamSynchronize(s));
+        std::swap(qin, qout);
+        if (++levels > 4096) return fail(KRR_ERR_OVERFLOW, "BVH collapse did not terminate");
+    }
+    KRR_CUDA(cudaMemcpyAsync(hc, counters.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    KRR_CUDA(cudaStreamSynchronize(s));
+    a->n_nodes = hc[0];
+    a->max_depth = hc[2];
+    if (hc[1] != n) return fail(KRR_ERR_OVERFLOW, "BVH collapse emitted %d of %lld triangles", hc[1], (long long)n);
+    if (a->max_depth > kTraversalStack)
+        return fail(KRR_ERR_OVERFLOW, "BVH depth %d exceeds the traversal stack (%d)", a->max_depth,
+                    kTraversalStack);
+
+    KRR_CUDA(cudaMalloc(&a->d_nodes, 5 * sizeof(float4) * a->n_nodes));
+    KRR_CUDA(cudaMemcpyAsync(a->d_nodes, nodes_tmp.p, 5 * sizeof(float4) * a->n_nodes,
+                             cudaMemcpyDeviceToDevice, s));
+    KRR_CUDA(cudaMalloc(&a->d_tris, 3 * sizeof(float4) * n));
+    KRR_CUDA(cudaMalloc(&a->d_leaf_of_prim, sizeof(uint32_t) * n));
+    k_gather_tris<<<blocks_for(n), kBuildThreads, 0, s>>>(d_v, leaf_order.p, n, a->d_tris,
+                                                           a->d_leaf_of_prim);
+    KRR_CUDA(cudaGetLastError());
+    cudaEventRecord(e1, s);
+    KRR_CUDA(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    a->build_ms = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return KRR_OK;
+}
+
+int accel_set_mask(krr_accel *a, const uint8_t *d_mask, cudaStream_t s) {
+    if (a->n_tris == 0) return KRR_OK;
+    k_set_mask<<<blocks_for(a->n_tris), kBuildThreads, 0, s>>>(a->d_tris, a->d_leaf_of_prim, d_mask,
+                                                               a->n_tris);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+}  // namespace krr
+
+// ------------------------------------------------------------------ C ABI
+using namespace krr;
+
+extern "C" int krr_accel_create_from_triangles(const float *h_vertices, int64_t n_triangles,
+                                               krr_accel **out, void *stream) {
+    KRR_CHECK_ARG(out != nullptr, "out is NULL");
+    KRR_CHECK_ARG(n_triangles == 0 || h_vertices != nullptr, "vertices are NULL");
+    cudaStream_t s = as_stream(stream);
+    float *d_v = nullptr;
+    size_t bytes = sizeof(float) * 9 * (size_t)n_triangles;
+    KRR_CUDA(cudaMalloc(&d_v, std::max<size_t>(bytes, 4)));
+    cudaError_t e = cudaMemcpyAsync(d_v, h_vertices, bytes, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) { cudaFree(d_v); return cuda_status(e, "cudaMemcpyAsync", __FILE__, __LINE__); }
+    krr_accel *a = new krr_accel();
+    int st = accel_build(a, d_v, n_triangles, s);
+    cudaStreamSynchronize(s);
+    cudaFree(d_v);
+    if (st != KRR_OK) { accel_free(a); delete a; return st; }
+    *out = a;
+    return KRR_OK;
+}
+
+extern "C" int krr_accel_stats_get(const krr_accel *a, krr_accel_stats *out) {
+    KRR_CHECK_ARG(a && out, "NULL argument");
+    out->n_triangles = a->n_tris;
+    out->n_nodes = a->n_nodes;
+    out->max_depth = a->max_depth;
+    out->reserved = 0;
+    out->build_ms = a->build_ms;
+    out->node_bytes = 80.0 * (double)a->n_nodes;
+    out->triangle_bytes = 48.0 * (double)a->n_tris;
+    return KRR_OK;
+}
+
+extern "C" int krr_accel_destroy(krr_accel *a) {
+    if (!a) return KRR_OK;
+    accel_free(a);
+    delete a;
+    return KRR_OK;
+}
+
+extern "C" int krr_accel_set_mask(krr_accel *a, const uint8_t *h_mask) {
+    KRR_CHECK_ARG(a != nullptr, "accel is NULL");
+    if (a->n_tris == 0) return KRR_OK;
+    uint8_t *d = nullptr;
+    if (h_mask) {
+        KRR_CUDA(cudaMalloc(&d, a->n_tris));
+        KRR_CUDA(cudaMemcpy(d, h_mask, a->n_tris, cudaMemcpyHostToDevice));
+    }
+    int st = accel_set_mask(a, d, 0);
+    cudaDeviceSynchronize();
+    cudaFree(d);
+    return st;
+}
+
+static TraceLaunch aos_launch(const krr_accel *a, const krr_ray *d_rays, int64_t n) {
+    TraceLaunch l{};
+    l.ray_o = reinterpret_cast<const float4 *>(d_rays);
+    l.ray_d = reinterpret_cast<const float4 *>(d_rays) + 1;
+    l.ray_stride = 2;
+    l.n = n;
+    l.d_count = nullptr;
+    l.counter = a->d_scratch;
+    l.err = a->d_scratch + 4;
+    return l;
+}
+
+extern "C" int krr_accel_trace_closest(const krr_accel *a, const krr_ray *d_rays, int64_t n,
+                                       krr_hit *d_hits, void *stream) {
+    KRR_CHECK_ARG(a && (n == 0 || (d_rays && d_hits)), "NULL argument");
+    KRR_CHECK_ARG(n >= 0, "negative ray count");
+    if (n == 0) return KRR_OK;
+    TraceLaunch l = aos_launch(a, d_rays, n);
+    l.hits = reinterpret_cast<float4 *>(d_hits);
+    if (a->n_tris == 0) return fail(KRR_ERR_NOT_READY, "empty acceleration structure");
+    return launch_trace_closest(a, l, as_stream(stream));
+}
+
+extern "C" int krr_accel_trace_any(const krr_accel *a, const krr_ray *d_rays, int64_t n,
+                                   uint8_t *d_occluded, void *stream) {
+    KRR_CHECK_ARG(a && (n == 0 || (d_rays && d_occluded)), "NULL argument");
+    KRR_CHECK_ARG(n >= 0, "negative ray count");
+    if (n == 0) return KRR_OK;
+    if (a->n_tris == 0) return fail(KRR_ERR_NOT_READY, "empty acceleration structure");
+    TraceLaunch l = aos_launch(a, d_rays, n);
+    l.occluded = d_occluded;
+    return launch_trace_any(a, l, as_stream(stream));
+}
+
+extern "C" int krr_accel_trace_stats(const krr_accel *a, const krr_ray *d_rays, int64_t n,
+                                     int32_t any_hit, unsigned long long *h_counts, void *stream) {
+    KRR_CHECK_ARG(a && d_rays && h_counts && n > 0, "bad argument");
+    if (a->n_tris == 0) return fail(KRR_ERR_NOT_READY, "empty acceleration structure");
+    cudaStream_t s = as_stream(stream);
+    TraceLaunch l = aos_launch(a, d_rays, n);
+    float4 *hits = nullptr;
+    uint8_t *occ = nullptr;
+    unsigned long long *d_counts = nullptr;
+    KRR_CUDA(cudaMalloc(&d_counts, 2 * sizeof(unsigned long long)));
+    KRR_CUDA(cudaMemsetAsync(d_counts, 0, 2 * sizeof(unsigned long long), s));
+    if (any_hit) { KRR_CUDA(cudaMalloc(&occ, n)); l.occluded = occ; }
+    else { KRR_CUDA(cudaMalloc(&hits, n * sizeof(float4))); l.hits = hits; }
+    int st = launch_trace_stats(a, l, any_hit != 0, d_counts, s);
+    if (st == KRR_OK) {
+        KRR_CUDA(cudaMemcpyAsync(h_counts, d_counts, 2 * sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, s));
+        KRR_CUDA(cudaStreamSynchronize(s));
+    }
+    cudaFree(d_counts);
+    cudaFree(hits);
+    cudaFree(occ);
+    return st;
+}
+
+extern "C" int krr_accel_trace_closest_host(const krr_accel *a, const krr_ray *h_rays, int64_t n,
+                                            krr_hit *h_hits, void *stream) {
+    KRR_CHECK_ARG(a && (n == 0 || (h_rays && h_hits)), "NULL argument");
+    if (n == 0) return KRR_OK;
+    cudaStream_t s = as_stream(stream);
+    krr_ray *d_rays = nullptr;
+    krr_hit *d_hits = nullptr;
+    KRR_CUDA(cudaMallocAsync(&d_rays, n * sizeof(krr_ray), s));
+    KRR_CUDA(cudaMallocAsync(&d_hits, n * sizeof(krr_hit), s));
+    int st = KRR_OK;
+    cudaError_t e = cudaMemcpyAsync(d_rays, h_rays, n * sizeof(krr_ray), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) st = cuda_status(e, "cudaMemcpyAsync", __FILE__, __LINE__);
+    if (st == KRR_OK) st = krr_accel_trace_closest(a, d_rays, n, d_hits, stream);
+    if (st == KRR_OK) {
+        e = cudaMemcpyAsync(h_hits, d_hits, n * sizeof(krr_hit), cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) st = cuda_status(e, "cudaMemcpyAsync", __FILE__, __LINE__);
+    }
+    cudaFreeAsync(d_rays, s);
+    cudaFreeAsync(d_hits, s);
+    e = cudaStreamSynchronize(s);
+    if (st == KRR_OK && e != cudaSuccess) st = cuda_status(e, "cudaStreamSynchronize", __FILE__, __LINE__);
+    return st;
+}

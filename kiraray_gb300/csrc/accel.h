@@ -1,0 +1,63 @@
+// Compressed 8-wide BVH: layout shared by the builder and the traversal.
+//
+// Node (80 bytes = 5 x 16 B, one 16-byte aligned record per node):
+//   q0: origin p.xyz (float) | word: ex | ey<<8 | ez<<16 | imask<<24
+//       (e* = biased float exponent of the per-axis quantisation step)
+//   q1: child_base | tri_base | meta[0..3] | meta[4..7]
+//   q2: qlo_x[0..7] | qlo_y[0..7]      (8-bit quantised child bounds)
+//   q3: qlo_z[0..7] | qhi_x[0..7]
+//   q4: qhi_y[0..7] | qhi_z[0..7]
+// meta byte per child slot: 0 = empty, 0x80 = internal node, otherwise a leaf
+// with (count << 5) | first_triangle_offset (count 1..3, offset 0..23).
+// Internal children are stored contiguously from child_base in slot order;
+// the leaf triangles of all children contiguously from tri_base.
+// Slot s holds the child that is nearest for rays whose direction octant is
+// s (bit i set = negative along axis i), so visiting positions s ^ octant in
+// increasing order is an approximate front-to-back order.
+//
+// Triangle (48 bytes, leaf order): v0.xyz | global id, v1.xyz | any-hit mask,
+// v2.xyz | unused.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "internal.h"
+
+struct krr_accel {
+    int64_t n_tris = 0;
+    int64_t n_nodes = 0;
+    int32_t max_depth = 0;
+    double build_ms = 0.0;
+    float4 *d_nodes = nullptr;   // 5 per node
+    float4 *d_tris = nullptr;    // 3 per triangle
+    uint32_t *d_leaf_of_prim = nullptr;  // global id -> leaf-order slot
+    int *d_scratch = nullptr;    // [0] ray counter, [1] error flags
+    float scene_lo[3] = {0, 0, 0}, scene_hi[3] = {0, 0, 0};
+};
+
+namespace krr {
+
+constexpr int kTraversalStack = 48;
+constexpr int kTraceThreads = 128;
+
+// Build from device world-space vertices (float3 x 3 per triangle).
+int accel_build(krr_accel *a, const float *d_vertices, int64_t n_tris, cudaStream_t stream);
+void accel_free(krr_accel *a);
+
+struct TraceLaunch {
+    const float4 *ray_o;      // origin.xyz, tmin
+    const float4 *ray_d;      // direction.xyz, tmax
+    int ray_stride;           // float4 stride between consecutive rays
+    int64_t n;                // ray count if d_count == nullptr
+    const int *d_count;       // device ray count (queue counter) or nullptr
+    float4 *hits;             // closest: t, b1, b2, prim bits
+    uint8_t *occluded;        // any-hit output
+    int *counter;             // scratch work counter (zeroed by the launcher)
+    int *err;                 // device error flags
+};
+
+int launch_trace_closest(const krr_accel *a, const TraceLaunch &l, cudaStream_t s);
+int launch_trace_any(const krr_accel *a, const TraceLaunch &l, cudaStream_t s);
+int traversal_grid_size();
+
+}  // namespace krr

@@ -1,0 +1,1168 @@
+// Wavefront path tracer: the WavefrontPathTracer render pass of the reference
+// (src/render/wavefront/integrator.{h,cpp}) re-designed for one GB300.
+//
+// Stages per bounce (integrator.cpp:223-267), each one kernel on the caller's
+// stream with queue sizes kept on the device (no host synchronisation inside
+// render):
+//   reset queues -> trace closest (BVH traversal + hit processing, the
+//   reference's __raygen__/__closesthit__/__miss__Closest) -> [medium sample]
+//   -> handle hit -> handle miss -> [medium scatter] -> generate scatter rays
+//   (RR, NEE, BSDF sampling) -> trace shadow rays (any hit + radiance).
+// Queues are SoA planes of float4 (16-byte vector loads and stores); pushes
+// use one atomic per warp.  Consumers run persistent grid-stride loops over
+// the live queue size read from device memory.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "accel.h"
+#include "internal.h"
+#include "shading.cuh"
+#include "wavefront.h"
+
+using namespace krr;
+
+namespace krr {
+int accel_set_mask(krr_accel *a, const uint8_t *d_mask, cudaStream_t s);
+int launch_medium_sample(krr_wf *wf, int depth, cudaStream_t s);
+int launch_medium_scatter(krr_wf *wf, int depth, cudaStream_t s);
+int launch_trace_shadow_tr(krr_wf *wf, cudaStream_t s);
+}
+
+struct DevCamera {
+    float pos[3];
+    float rot[9];
+    float tan_fov;         // tan(atan2(filmSize.y / 2, focalLength)), per frame
+    float aspect;
+    float lens_radius, focal_distance;
+    float shutter_open, shutter_time;
+    int32_t medium;
+};
+
+enum { Q_RAY0 = 0, Q_RAY1 = 1, Q_MISS = 2, Q_HIT_LIGHT = 3, Q_SHADOW = 4, Q_SCATTER = 5,
+       Q_MEDIUM_SAMPLE = 6, Q_MEDIUM_SCATTER = 7, Q_COUNT = 8 };
+static const int kChannels[Q_COUNT] = {kRayCh, kRayCh, kMissCh, kHitLightCh, kShadowCh,
+                                       kScatterCh, kMediumSampleCh, kMediumScatterCh};
+
+struct krr_wf {
+    krr_wf_params params{};
+    int32_t width = 0, height = 0;
+    int64_t n = 0;
+    int64_t frame_index = 0;
+    DevCamera cam{};
+    bool has_scene = false;
+    bool medium = false;        // enable_medium && scene has media
+    DevScene scene{};
+    float scene_radius = 1.f;
+    krr_accel accel{};
+    std::vector<void *> scene_allocs;
+    // queues and pixel state
+    float4 *qbuf[Q_COUNT] = {};
+    int32_t *d_counts = nullptr;   // [0..7] queue sizes, [8] error flags
+    float4 *hits = nullptr;
+    uint8_t *occluded = nullptr;
+    PixelState ps{};
+    int grid = 0;
+
+    Queue q(int k) const { return Queue{qbuf[k], (int32_t)n, d_counts + k}; }
+    uint32_t *err() const { return reinterpret_cast<uint32_t *>(d_counts + 8); }
+    WfConst consts() const {
+        WfConst c;
+        c.width = width; c.height = height;
+        c.nee = params.nee; c.max_depth = params.max_depth;
+        c.enable_medium = medium ? 1 : 0; c.enable_clamp = params.enable_clamp;
+        c.spp = params.spp; c.rr = params.rr; c.clamp_max = params.clamp_max;
+        return c;
+    }
+};
+
+namespace {
+
+constexpr int kThreads = 256;
+
+// ---------------------------------------------------------------- pushes
+__device__ __forceinline__ int push_slot(int32_t *count, int cap, uint32_t *err) {
+    unsigned m = __activemask();
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(m));
+    base = __shfl_sync(m, base, leader);
+    int slot = base + __popc(m & ((1u << lane) - 1u));
+    if (slot >= cap) {
+        atomicOr(err, (uint32_t)kErrQueueOverflow);
+        return -1;
+    }
+    return slot;
+}
+
+__device__ __forceinline__ float fbits(uint32_t u) { return __uint_as_float(u); }
+__device__ __forceinline__ uint32_t ubits(float f) { return __float_as_uint(f); }
+__device__ __forceinline__ float ibits(int32_t i) { return __int_as_float(i); }
+__device__ __forceinline__ int32_t sbits(float f) { return __float_as_int(f); }
+
+__device__ __forceinline__ Pcg load_rng(const PixelState &ps, uint32_t pixel) {
+    ulonglong2 s = ps.rng[pixel];
+    return Pcg{s.x, s.y};
+}
+__device__ __forceinline__ void store_rng(const PixelState &ps, uint32_t pixel, const Pcg &p) {
+    ps.rng[pixel] = make_ulonglong2(p.state, p.inc);
+}
+
+// PixelStateBuffer::addRadiance, workqueue.h:24-26
+__device__ __forceinline__ void add_radiance(const PixelState &ps, uint32_t pixel, V3 v) {
+    float4 l = ps.L[pixel];
+    ps.L[pixel] = make_float4(v.x + l.x, v.y + l.y, v.z + l.z, l.w);
+}
+
+// ----------------------------------------------------------- interaction
+struct Surf {
+    V3 p, wo, n, t, b;
+    float u, v;
+    int32_t material;
+    int32_t mesh;
+    int32_t light;          // light-list index or -1
+    int32_t interface_in, interface_out;   // medium interface (-2 = none)
+};
+
+// prepareSurfaceInteraction, src/render/shading.h:115-226 (no textures).
+__device__ Surf prepare_surface(const DevScene &s, float b1, float b2, uint32_t gid, V3 ray_dir) {
+    Surf o;
+    uint32_t inst = s.tri_instance[gid];
+    const DevInstance &I = s.instances[inst];
+    const DevMesh &M = s.meshes[I.mesh];
+    uint32_t prim = gid - I.prim_offset;
+    float b0 = 1 - b1 - b2;
+    uint32_t i0 = M.idx[3 * prim], i1 = M.idx[3 * prim + 1], i2 = M.idx[3 * prim + 2];
+    V3 wo = -normalize(ray_dir);
+    o.wo = normalize(wo);
+    V3 p0{M.pos[3 * i0], M.pos[3 * i0 + 1], M.pos[3 * i0 + 2]};
+    V3 p1{M.pos[3 * i1], M.pos[3 * i1 + 1], M.pos[3 * i1 + 2]};
+    V3 p2{M.pos[3 * i2], M.pos[3 * i2 + 1], M.pos[3 * i2 + 2]};
+    V3 p = p0 * b0 + p1 * b1 + p2 * b2;
+    V3 n0{M.nrm[3 * i0], M.nrm[3 * i0 + 1], M.nrm[3 * i0 + 2]};
+    V3 n1{M.nrm[3 * i1], M.nrm[3 * i1 + 1], M.nrm[3 * i1 + 2]};
+    V3 n2{M.nrm[3 * i2], M.nrm[3 * i2 + 1], M.nrm[3 * i2 + 2]};
+    V3 n = normalize(n0 * b0 + n1 * b1 + n2 * b2);
+    V3 t = get_perpendicular(n);
+    V3 b = normalize(cross(n, t));
+    o.u = 0.f;
+    o.v = 0.f;
+    if (M.uv) {
+        o.u = M.uv[2 * i0] * b0 + M.uv[2 * i1] * b1 + M.uv[2 * i2] * b2;
+        o.v = M.uv[2 * i0 + 1] * b0 + M.uv[2 * i1 + 1] * b1 + M.uv[2 * i2 + 1] * b2;
+    }
+    o.light = I.light_offset >= 0 ? I.light_offset + (int32_t)prim : -1;
+    o.material = M.material;
+    o.mesh = I.mesh;
+    bool transition = M.medium_inside != M.medium_outside;
+    o.interface_in = transition ? M.medium_inside : -2;
+    o.interface_out = transition ? M.medium_outside : -2;
+    o.p = xform_point(I.xf, p);
+    o.n = normalize(mat3_mul(I.nxf, n));
+    o.t = normalize(mat3_mul(I.nxf, t));
+    o.b = normalize(mat3_mul(I.nxf, b));
+    return o;
+}
+
+// offsetRayOrigin, src/core/raytracing.h:106-111
+__device__ __forceinline__ V3 offset_ray_origin(V3 p, V3 n, V3 w) {
+    V3 off = n * kRayEps;
+    if (dot(n, w) < 0.f) off = -off;
+    return p + off;
+}
+
+// Interaction::getMedium(w), raytracing.h:162-166
+__device__ __forceinline__ int32_t medium_towards(int32_t in, int32_t out, int32_t medium, V3 n,
+                                                  V3 w) {
+    if (in != -2) return dot(w, n) > 0 ? out : in;
+    return medium;
+}
+
+__device__ __forceinline__ ShadingData shading_data(const DevScene &s, int32_t material) {
+    const DevMaterial &m = s.materials[material];
+    ShadingData sd;
+    sd.type = m.type;
+    sd.diffuse = V3{m.diffuse[0], m.diffuse[1], m.diffuse[2]};
+    sd.roughness = 1.f - m.spec_alpha;   // SpecularGlossiness, shading.h:215-220
+    sd.spec_trans = m.spec_trans;
+    sd.ior = m.eta;
+    sd.anisotropic = m.anisotropic;
+    return sd;
+}
+
+// ----------------------------------------------------------------- lights
+__device__ __forceinline__ void light_triangle(const DevScene &s, const DevLight &l, V3 &p0, V3 &p1,
+                                               V3 &p2, uint32_t &i0, uint32_t &i1, uint32_t &i2,
+                                               const DevInstance *&I, const DevMesh *&M) {
+    I = &s.instances[l.index];
+    M = &s.meshes[I->mesh];
+    i0 = M->idx[3 * l.prim];
+    i1 = M->idx[3 * l.prim + 1];
+    i2 = M->idx[3 * l.prim + 2];
+    p0 = V3{M->pos[3 * i0], M->pos[3 * i0 + 1], M->pos[3 * i0 + 2]};
+    p1 = V3{M->pos[3 * i1], M->pos[3 * i1 + 1], M->pos[3 * i1 + 2]};
+    p2 = V3{M->pos[3 * i2], M->pos[3 * i2 + 1], M->pos[3 * i2 + 2]};
+}
+
+// Triangle::area, src/core/shape.h:29-38 (world-space vertices)
+__device__ __forceinline__ float tri_area(const DevInstance &I, V3 p0, V3 p1, V3 p2) {
+    V3 w0 = xform_point(I.xf, p0), w1 = xform_point(I.xf, p1), w2 = xform_point(I.xf, p2);
+    return 0.5f * length(cross(w1 - w0, w2 - w0));
+}
+
+// DiffuseAreaLight::L, src/core/light.h:182-188 (one-sided)
+__device__ __forceinline__ V3 area_L(const DevInstance &I, V3 n, V3 w) {
+    if (dot(n, w) < 0.f) return v3(0.f);
+    return I.le_scale * V3{I.le[0], I.le[1], I.le[2]};
+}
+
+// Triangle::pdf(sample, ctx), src/core/shape.h:114-123
+__device__ __forceinline__ float area_pdf(const DevScene &s, const DevLight &l, V3 sp, V3 sn, V3 cp) {
+    V3 p0, p1, p2;
+    uint32_t i0, i1, i2;
+    const DevInstance *I;
+    const DevMesh *M;
+    light_triangle(s, l, p0, p1, p2, i0, i1, i2, I, M);
+    V3 wi = normalize(sp - cp);
+    float pdf = (1 / tri_area(*I, p0, p1, p2)) / (fabsf(dot(sn, -wi)) / length_sq(cp - sp));
+    if (length(wi) == 0 || isinf(pdf)) pdf = 0;
+    return pdf;
+}
+
+// Bilinear lookup with wrap addressing and normalised coordinates (the
+// reference samples a cudaFilterModeLinear texture, texture.cpp:237-243).
+__device__ __forceinline__ V3 env_lookup(const DevInfinite &e, float u, float v) {
+    float x = u * (float)e.w - 0.5f, y = v * (float)e.h - 0.5f;
+    float fx0 = floorf(x), fy0 = floorf(y);
+    float fx = x - fx0, fy = y - fy0;
+    int x0 = (int)fx0, y0 = (int)fy0;
+    int xa = ((x0 % e.w) + e.w) % e.w, xb = (((x0 + 1) % e.w) + e.w) % e.w;
+    int ya = ((y0 % e.h) + e.h) % e.h, yb = (((y0 + 1) % e.h) + e.h) % e.h;
+    float4 c00 = e.image[(size_t)ya * e.w + xa], c10 = e.image[(size_t)ya * e.w + xb];
+    float4 c01 = e.image[(size_t)yb * e.w + xa], c11 = e.image[(size_t)yb * e.w + xb];
+    V3 top = f3(c00) * (1.f - fx) + f3(c10) * fx;
+    V3 bot = f3(c01) * (1.f - fx) + f3(c11) * fx;
+    return top * (1.f - fy) + bot * fy;
+}
+
+// InfiniteLight::Li, src/core/light.h:242-247
+__device__ __forceinline__ V3 env_Li(const DevInfinite &e, V3 wi) {
+    float u, v;
+    world_to_latlong(mat3_mul_transposed(e.rot, wi), u, v);
+    V3 tint{e.tint[0], e.tint[1], e.tint[2]};
+    V3 L = e.image ? tint * env_lookup(e, u, v) : tint;
+    return e.scale * L;
+}
+
+struct LightSample {
+    V3 p, n;      // n = 0 for the infinite light
+    V3 L;
+    float pdf;
+};
+
+// Light::sampleLi for triangle area lights (light.h:167-180, shape.h:54-108)
+// and the infinite light (light.h:222-231).
+__device__ LightSample sample_li(const DevScene &s, const DevLight &l, float u0, float u1, V3 cp) {
+    LightSample ls;
+    if (l.kind == 1) {
+        const DevInfinite &e = s.infinite[l.index];
+        V3 wi = uniform_sample_sphere(u0, u1);
+        ls.p = cp + wi * 2 * e.scene_radius;
+        ls.n = v3(0.f);
+        ls.L = env_Li(e, wi);
+        ls.pdf = kInv4Pi;
+        return ls;
+    }
+    V3 p0, p1, p2;
+    uint32_t i0, i1, i2;
+    const DevInstance *I;
+    const DevMesh *M;
+    light_triangle(s, l, p0, p1, p2, i0, i1, i2, I, M);
+    V3 n0{M->nrm[3 * i0], M->nrm[3 * i0 + 1], M->nrm[3 * i0 + 2]};
+    V3 n1{M->nrm[3 * i1], M->nrm[3 * i1 + 1], M->nrm[3 * i1 + 2]};
+    V3 n2{M->nrm[3 * i2], M->nrm[3 * i2 + 1], M->nrm[3 * i2 + 2]};
+    V3 b = uniform_sample_triangle(u0, u1);
+    V3 p = p0 * b.x + p1 * b.y + p2 * b.z;
+    V3 n = normalize(cross(p1 - p0, p2 - p0));
+    V3 ns = normalize(n0 * b.x + n1 * b.y + n2 * b.z);
+    if (dot(n, ns) < 0) n = n * -1.f;
+    p = xform_point(I->xf, p);
+    n = normalize(mat3_mul(I->nxf, n));
+    float pdf = 1 / tri_area(*I, p0, p1, p2);
+    V3 wi = normalize(p - cp);
+    pdf = pdf / (fabsf(dot(n, wi)) / length_sq(cp - p));
+    if (length(wi) == 0 || isinf(pdf)) pdf = 0;
+    ls.p = p;
+    ls.n = n;
+    V3 wo = normalize(cp - p);
+    ls.L = area_L(*I, n, wo);
+    ls.pdf = pdf;
+    return ls;
+}
+
+// ---------------------------------------------------------------- kernels
+// beginFrame, integrator.cpp:205-221
+__global__ void k_begin_frame(PixelState ps, int w, int64_t n, uint32_t sample_index) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t x = (uint32_t)(i % w), y = (uint32_t)(i / w);
+        Pcg p;
+        p.set_seed(interleave_32bit(x, y), sample_index);
+        p.advance(256 * i);
+        float u = p.get1d();
+        float lambda0 = (1.f - u) * 360.f + u * 830.f;   // sampleUniform, spectrum.h:47-58
+        ps.L[i] = make_float4(0.f, 0.f, 0.f, lambda0);
+        ps.pixel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        store_rng(ps, (uint32_t)i, p);
+    }
+}
+
+// generateCameraRays + CameraData::getRay, integrator.cpp:166-179, camera.h:32-58
+__global__ void k_camera_rays(PixelState ps, Queue rq, DevCamera cam, int w, int h, int64_t n) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *rq.count = (int32_t)n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        Pcg p = load_rng(ps, (uint32_t)i);
+        float fx = p.get1d(), fy = p.get1d();
+        float lx = p.get1d(), ly = p.get1d();
+        float tm = p.get1d();
+        store_rng(ps, (uint32_t)i, p);
+        (void)lx; (void)ly;
+        float px = (float)(i % w) + 0.5f + fx;
+        float py = (float)(i / w) + 0.5f + fy;
+        float ndcx = (2 * px) / (float)w + (-1.f);
+        float ndcy = (2 * py) / (float)h + (-1.f);
+        V3 fd = normalize(V3{cam.tan_fov * cam.aspect * ndcx, cam.tan_fov * ndcy, -1.f});
+        V3 o = V3{cam.pos[0], cam.pos[1], cam.pos[2]};
+        V3 d = mat3_mul(cam.rot, fd);
+        float time = cam.shutter_open + cam.shutter_time * tm;
+        rq.at(0, i) = f4(o, 0.f);
+        rq.at(1, i) = f4(d, INFINITY);
+        rq.at(2, i) = make_float4(0.f, 0.f, 0.f, ibits(cam.medium));
+        rq.at(3, i) = make_float4(0.f, 0.f, 0.f, fbits(0u));
+        rq.at(4, i) = make_float4(1.f, 1.f, 1.f, fbits(0u));
+        rq.at(5, i) = make_float4(1.f, 1.f, 1.f, fbits((uint32_t)i));
+        rq.at(6, i) = make_float4(1.f, 1.f, 1.f, time);
+    }
+}
+
+__global__ void k_reset_queues(int32_t *counts, int cur, int all) {
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < Q_COUNT; ++k)
+            if (all || k != cur) counts[k] = 0;
+    }
+}
+
+__device__ __forceinline__ void copy_ray_item(const Queue &src, int i, const Queue &dst, int j) {
+    for (int c = 0; c < kRayCh; ++c) dst.at(c, j) = src.at(c, i);
+}
+
+// Routing of a closest hit (__closesthit__/__miss__Closest, device.cu:43-74).
+__global__ void k_hit_process(DevScene s, Queue rq, const float4 *__restrict__ hits, Queue next,
+                              Queue miss, Queue hitl, Queue scat, Queue msq, int enable_medium,
+                              uint32_t *err) {
+    int n = *rq.count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 h = hits[i];
+        uint32_t gid = ubits(h.w);
+        float4 c2 = rq.at(2, i);
+        int32_t ray_medium = sbits(c2.w);
+        bool in_medium = enable_medium && ray_medium >= 0;
+        if (gid == KRR_MISS) {
+            if (in_medium) {
+                int j = push_slot(msq.count, msq.cap, err);
+                if (j >= 0) {
+                    copy_ray_item(rq, i, msq, j);
+                    msq.at(7, j) = make_float4(INFINITY, 0.f, 0.f, fbits(KRR_MISS));
+                }
+            } else {
+                int j = push_slot(miss.count, miss.cap, err);
+                if (j >= 0) copy_ray_item(rq, i, miss, j);
+            }
+            continue;
+        }
+        if (in_medium) {
+            int j = push_slot(msq.count, msq.cap, err);
+            if (j >= 0) {
+                copy_ray_item(rq, i, msq, j);
+                msq.at(7, j) = h;
+            }
+            continue;
+        }
+        float4 c0 = rq.at(0, i), c1 = rq.at(1, i);
+        V3 dir = f3(c1);
+        Surf sf = prepare_surface(s, h.y, h.z, gid, dir);
+        float4 c3 = rq.at(3, i), c4 = rq.at(4, i), c5 = rq.at(5, i), c6 = rq.at(6, i);
+        if (sf.material < 0) {
+            // null material: continue through the interface (device.cu:54-58)
+            int j = push_slot(next.count, next.cap, err);
+            if (j >= 0) {
+                V3 o = offset_ray_origin(sf.p, sf.n, dir);
+                int32_t med = medium_towards(sf.interface_in, sf.interface_out, ray_medium, sf.n, dir);
+                next.at(0, j) = f4(o, 0.f);
+                next.at(1, j) = f4(dir, INFINITY);
+                next.at(2, j) = make_float4(c2.x, c2.y, c2.z, ibits(med));
+                next.at(3, j) = c3;
+                next.at(4, j) = c4;
+                next.at(5, j) = c5;
+                next.at(6, j) = c6;
+            }
+            continue;
+        }
+        (void)c0;
+        V3 thp = f3(c4);
+        if (sf.light >= 0) {
+            int j = push_slot(hitl.count, hitl.cap, err);
+            if (j >= 0) {
+                hitl.at(0, j) = f4(sf.p, ibits(sf.light));
+                hitl.at(1, j) = f4(sf.n, sf.u);
+                hitl.at(2, j) = f4(sf.wo, sf.v);
+                hitl.at(3, j) = make_float4(c2.x, c2.y, c2.z, c3.w);
+                hitl.at(4, j) = make_float4(c3.x, c3.y, c3.z, c4.w);
+                hitl.at(5, j) = make_float4(c4.x, c4.y, c4.z, c5.w);
+                hitl.at(6, j) = c5;
+                hitl.at(7, j) = c6;
+            }
+        }
+        if (any(thp)) {
+            int j = push_slot(scat.count, scat.cap, err);
+            if (j >= 0) {
+                scat.at(0, j) = f4(sf.p, ibits(sf.material));
+                scat.at(1, j) = f4(sf.wo, c4.w);
+                scat.at(2, j) = f4(sf.n, c5.w);
+                scat.at(3, j) = f4(sf.t, ibits(sf.mesh));
+                scat.at(4, j) = f4(sf.b, sf.u);
+                scat.at(5, j) = f4(thp, sf.v);
+                scat.at(6, j) = make_float4(c5.x, c5.y, c5.z, c6.w);
+                scat.at(7, j) = make_float4(ibits(ray_medium), 0.f, 0.f, 0.f);
+            }
+        }
+    }
+}
+
+// handleHit, integrator.cpp:78-90
+__global__ void k_handle_hit(DevScene s, Queue hitl, PixelState ps, int nee) {
+    int n = *hitl.count;
+    float lsel_pdf = 1.f / (float)s.n_lights;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 c0 = hitl.at(0, i), c1 = hitl.at(1, i), c2 = hitl.at(2, i), c3 = hitl.at(3, i);
+        float4 c4 = hitl.at(4, i), c5 = hitl.at(5, i), c6 = hitl.at(6, i), c7 = hitl.at(7, i);
+        const DevLight &l = s.lights[sbits(c0.w)];
+        const DevInstance &I = s.instances[l.index];
+        V3 p = f3(c0), nrm = f3(c1), wo = f3(c2);
+        V3 Le = area_L(I, nrm, wo) * f3(c5);
+        uint32_t bsdf_type = ubits(c3.w), depth = ubits(c4.w), pixel = ubits(c5.w);
+        V3 pu = f3(c6), pl = f3(c7);
+        if (nee && depth && !(bsdf_type & BSDF_DELTA)) {
+            float light_pdf = area_pdf(s, l, p, nrm, f3(c3)) * lsel_pdf;
+            Le = Le / mean(pl * light_pdf + pu);
+        } else {
+            Le = Le / mean(pu);
+        }
+        add_radiance(ps, pixel, Le);
+    }
+}
+
+// handleMiss, integrator.cpp:92-108
+__global__ void k_handle_miss(DevScene s, Queue miss, PixelState ps, int nee) {
+    int n = *miss.count;
+    float lsel_pdf = 1.f / (float)s.n_lights;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 c1 = miss.at(1, i), c3 = miss.at(3, i), c4 = miss.at(4, i), c5 = miss.at(5, i),
+               c6 = miss.at(6, i);
+        V3 dir = f3(c1), pu = f3(c5), pl = f3(c6);
+        uint32_t bsdf_type = ubits(c3.w), depth = ubits(c4.w), pixel = ubits(c5.w);
+        V3 L = v3(0.f);
+        for (int k = 0; k < s.n_infinite; ++k) {
+            const DevInfinite &e = s.infinite[k];
+            if (nee && depth && !(bsdf_type & BSDF_DELTA)) {
+                float light_pdf = kInv4Pi * lsel_pdf;
+                L += env_Li(e, dir) / mean(pu + pl * light_pdf);
+            } else {
+                L += env_Li(e, dir) / mean(pu);
+            }
+        }
+        add_radiance(ps, pixel, f3(c4) * L);
+    }
+}
+
+// generateScatterRays, integrator.cpp:110-164
+__global__ void k_scatter(DevScene s, Queue scat, Queue next, Queue shadow, PixelState ps, int nee,
+                          float rr, uint32_t *err) {
+    int n = *scat.count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 c0 = scat.at(0, i), c1 = scat.at(1, i), c2 = scat.at(2, i), c3 = scat.at(3, i);
+        float4 c4 = scat.at(4, i), c5 = scat.at(5, i), c6 = scat.at(6, i), c7 = scat.at(7, i);
+        uint32_t pixel = ubits(c2.w), depth = ubits(c1.w);
+        Pcg rng = load_rng(ps, pixel);
+        if (rng.get1d() >= rr) {
+            store_rng(ps, pixel, rng);
+            continue;
+        }
+        V3 thp = f3(c5) / rr;
+        V3 p = f3(c0), wo = f3(c1), nrm = f3(c2), tg = f3(c3), bt = f3(c4), pu = f3(c6);
+        float time = c6.w;
+        int32_t material = sbits(c0.w), mesh = sbits(c3.w), ray_medium = sbits(c7.x);
+        const DevMesh &M = s.meshes[mesh];
+        bool transition = M.medium_inside != M.medium_outside;
+        int32_t mi = transition ? M.medium_inside : -2, mo = transition ? M.medium_outside : -2;
+        auto to_local = [&](V3 v) { return V3{dot(tg, v), dot(bt, v), dot(nrm, v)}; };
+        V3 wo_local = to_local(wo);
+        ShadingData sd = shading_data(s, material);
+        uint32_t bsdf_type = bsdf_type_of(sd);
+        Bsdf bsdf = Bsdf::setup(sd);
+        if (nee && (bsdf_type & BSDF_SMOOTH)) {
+            float ul = rng.get1d();
+            uint32_t lid = (uint32_t)(ul * (float)s.n_lights);
+            float sel_pdf = 1.f / (float)s.n_lights;
+            float u0 = rng.get1d(), u1 = rng.get1d();
+            LightSample ls = sample_li(s, s.lights[lid], u0, u1, p);
+            // spawnRayTo(Interaction), raytracing.h:151-160
+            V3 to = offset_ray_origin(ls.p, ls.n, p - ls.p);
+            V3 po = offset_ray_origin(p, nrm, to - p);
+            V3 d = to - po;
+            V3 wi_world = normalize(d);
+            V3 wi_local = to_local(wi_world);
+            float light_pdf = sel_pdf * ls.pdf;
+            V3 fv = bsdf.f(wo_local, wi_local);
+            float bsdf_pdf = bsdf.pdf(wo_local, wi_local);
+            if (light_pdf > 0 && any(fv)) {
+                V3 Ld = ls.L * thp * fv * fabsf(wi_local.z);
+                if (any(Ld)) {
+                    int j = push_slot(shadow.count, shadow.cap, err);
+                    if (j >= 0) {
+                        int32_t med = medium_towards(mi, mo, ray_medium, nrm, d);
+                        shadow.at(0, j) = f4(po, 0.f);
+                        shadow.at(1, j) = f4(d, 1.f);
+                        shadow.at(2, j) = f4(Ld, fbits(pixel));
+                        shadow.at(3, j) = f4(pu * bsdf_pdf, ibits(med));
+                        shadow.at(4, j) = f4(pu * light_pdf, time);
+                    }
+                }
+            }
+        }
+        BsdfSample bs = bsdf.sample(wo_local, [&]() { return rng.get1d(); });
+        store_rng(ps, pixel, rng);
+        if (bs.pdf != 0 && any(bs.f)) {
+            V3 wi_world = tg * bs.wi.x + bt * bs.wi.y + nrm * bs.wi.z;
+            V3 nthp = thp * bs.f * fabsf(bs.wi.z) / bs.pdf;
+            if (any(nthp)) {
+                int j = push_slot(next.count, next.cap, err);
+                if (j >= 0) {
+                    V3 o = offset_ray_origin(p, nrm, wi_world);
+                    int32_t med = medium_towards(mi, mo, ray_medium, nrm, wi_world);
+                    next.at(0, j) = f4(o, 0.f);
+                    next.at(1, j) = f4(wi_world, INFINITY);
+                    next.at(2, j) = f4(p, ibits(med));
+                    next.at(3, j) = f4(nrm, fbits(bs.flags));
+                    next.at(4, j) = f4(nthp, fbits(depth + 1));
+                    next.at(5, j) = f4(pu, fbits(pixel));
+                    next.at(6, j) = f4(pu / bs.pdf, time);
+                }
+            }
+        }
+    }
+}
+
+// Radiance of unoccluded shadow rays (__raygen__Shadow, device.cu:92-100).
+__global__ void k_shadow_resolve(Queue shadow, const uint8_t *__restrict__ occluded, PixelState ps) {
+    int n = *shadow.count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (occluded[i]) continue;
+        float4 c2 = shadow.at(2, i), c3 = shadow.at(3, i), c4 = shadow.at(4, i);
+        add_radiance(ps, ubits(c2.w), f3(c2) / mean(f3(c4) + f3(c3)));
+    }
+}
+
+// pixel += L (integrator.cpp:257-260)
+__global__ void k_accumulate(PixelState ps, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float4 l = ps.L[i], p = ps.pixel[i];
+        ps.pixel[i] = make_float4(p.x + l.x, p.y + l.y, p.z + l.z, 0.f);
+    }
+}
+
+// Final write (integrator.cpp:262-266); rows flipped as the reference's
+// surface write does (src/core/device/cuda.h:33-37).
+__global__ void k_resolve(PixelState ps, float4 *out, int w, int h, float spp, int clamp,
+                          float clamp_max) {
+    int64_t n = (int64_t)w * h;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float4 p = ps.pixel[i];
+        V3 c = V3{p.x, p.y, p.z} / spp;
+        if (clamp) c = vmin(vmax(c, v3(0.f)), v3(clamp_max));
+        int64_t x = i % w, y = i / w;
+        out[(h - 1 - y) * (int64_t)w + x] = f4(c, 1.f);
+    }
+}
+
+// Instance flattening: world-space vertices in instance-major triangle order,
+// each row m0*x + m1*y + m2*z + m3 rounded operation by operation.
+__global__ void k_flatten(const DevScene s, int n_inst, float *out, int64_t n_tris) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n_tris;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t inst = s.tri_instance[g];
+        const DevInstance &I = s.instances[inst];
+        const DevMesh &M = s.meshes[I.mesh];
+        uint32_t prim = (uint32_t)g - I.prim_offset;
+        for (int k = 0; k < 3; ++k) {
+            uint32_t vi = M.idx[3 * prim + k];
+            float x = M.pos[3 * vi], y = M.pos[3 * vi + 1], z = M.pos[3 * vi + 2];
+            for (int r = 0; r < 3; ++r) {
+                const float *m = I.xf + 4 * r;
+                float acc = __fmul_rn(m[0], x);
+                acc = __fadd_rn(acc, __fmul_rn(m[1], y));
+                acc = __fadd_rn(acc, __fmul_rn(m[2], z));
+                out[9 * g + 3 * k + r] = __fadd_rn(acc, m[3]);
+            }
+        }
+    }
+}
+
+__global__ void k_fill_instance_ids(uint32_t *tri_instance, const uint32_t *offsets, int n_inst,
+                                    int64_t n_tris) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n_tris;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        // binary search over instance offsets
+        int lo = 0, hi = n_inst - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (offsets[mid] <= (uint32_t)g) lo = mid;
+            else hi = mid - 1;
+        }
+        tri_instance[g] = (uint32_t)lo;
+    }
+}
+
+__global__ void k_null_mask(const DevScene s, int64_t n_tris, uint8_t *mask) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n_tris;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        const DevInstance &I = s.instances[s.tri_instance[g]];
+        mask[g] = s.meshes[I.mesh].material >= 0 ? 1 : 0;
+    }
+}
+
+}  // namespace
+
+// --------------------------------------------------------------- host side
+namespace {
+
+int grid_for(int64_t n) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    int64_t g = (n + kThreads - 1) / kThreads;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)sms * 8));
+}
+
+template <typename T>
+int dev_upload(krr_wf *wf, T **dst, const T *src, size_t count) {
+    *dst = nullptr;
+    if (count == 0) return KRR_OK;
+    KRR_CUDA(cudaMalloc(dst, count * sizeof(T)));
+    wf->scene_allocs.push_back(*dst);
+    KRR_CUDA(cudaMemcpy(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice));
+    return KRR_OK;
+}
+
+void free_scene(krr_wf *wf) {
+    for (void *p : wf->scene_allocs) cudaFree(p);
+    wf->scene_allocs.clear();
+    accel_free(&wf->accel);
+    wf->scene = DevScene{};
+    wf->has_scene = false;
+}
+
+void free_queues(krr_wf *wf) {
+    for (auto &q : wf->qbuf) { cudaFree(q); q = nullptr; }
+    cudaFree(wf->d_counts); wf->d_counts = nullptr;
+    cudaFree(wf->hits); wf->hits = nullptr;
+    cudaFree(wf->occluded); wf->occluded = nullptr;
+    cudaFree(wf->ps.L); cudaFree(wf->ps.pixel); cudaFree(wf->ps.rng);
+    wf->ps = PixelState{};
+}
+
+// 3x3 inverse-transpose of a row-major 3x4 transform's linear part, in double.
+void inverse_transpose(const float *m, float *out) {
+    double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], h = m[9], i = m[10];
+    double A = e * i - f * h, B = -(d * i - f * g), C = d * h - e * g;
+    double D = -(b * i - c * h), E = a * i - c * g, F = -(a * h - b * g);
+    double G = b * f - c * e, H = -(a * f - c * d), I = a * e - b * d;
+    double det = a * A + b * B + c * C;
+    // inverse = adj^T / det; its transpose = cofactor matrix / det
+    double cof[9] = {A, B, C, D, E, F, G, H, I};
+    for (int k = 0; k < 9; ++k) out[k] = (float)(cof[k] / det);
+}
+
+}  // namespace
+
+extern "C" void krr_wf_params_default(krr_wf_params *p) {
+    if (!p) return;
+    p->nee = 1;
+    p->enable_medium = 1;
+    p->max_depth = 10;
+    p->rr = 0.8f;
+    p->enable_clamp = 0;
+    p->clamp_max = 1e3f;
+    p->spp = 1;
+    p->seed = 0;
+}
+
+extern "C" int krr_wf_create(const krr_wf_params *params, krr_wf **out) {
+    KRR_CHECK_ARG(out != nullptr, "out is NULL");
+    krr_wf *wf = new krr_wf();
+    if (params) wf->params = *params;
+    else krr_wf_params_default(&wf->params);
+    if (wf->params.spp < 1) wf->params.spp = 1;
+    *out = wf;
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_destroy(krr_wf *wf) {
+    if (!wf) return KRR_OK;
+    cudaDeviceSynchronize();
+    free_queues(wf);
+    free_scene(wf);
+    delete wf;
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_set_params(krr_wf *wf, const krr_wf_params *params) {
+    KRR_CHECK_ARG(wf && params, "NULL argument");
+    KRR_CHECK_ARG(params->max_depth >= 0 && params->spp >= 1, "bad parameters");
+    bool was_medium = wf->params.enable_medium;
+    wf->params = *params;
+    wf->medium = wf->params.enable_medium && wf->scene.n_media > 0;
+    (void)was_medium;
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *sd, void *stream) {
+    KRR_CHECK_ARG(wf && sd, "NULL argument");
+    KRR_CHECK_ARG(sd->n_meshes >= 0 && sd->n_instances >= 0 && sd->n_materials >= 0,
+                  "negative counts");
+    cudaStream_t st = as_stream(stream);
+    cudaDeviceSynchronize();
+    free_scene(wf);
+
+    // meshes
+    std::vector<DevMesh> meshes(sd->n_meshes);
+    for (int i = 0; i < sd->n_meshes; ++i) {
+        const krr_mesh_desc &m = sd->meshes[i];
+        KRR_CHECK_ARG(m.h_positions && m.h_normals && m.h_indices, "mesh arrays missing (normals are required)");
+        KRR_CHECK_ARG(m.material < sd->n_materials, "mesh material out of range");
+        KRR_CHECK_ARG(m.medium_inside < sd->n_media && m.medium_outside < sd->n_media,
+                      "mesh medium out of range");
+        // meshes that share arrays (same host pointers) share device copies
+        int shared = -1;
+        for (int j = 0; j < i; ++j)
+            if (sd->meshes[j].h_positions == m.h_positions && sd->meshes[j].h_indices == m.h_indices &&
+                sd->meshes[j].n_vertices == m.n_vertices && sd->meshes[j].n_triangles == m.n_triangles &&
+                sd->meshes[j].h_normals == m.h_normals && sd->meshes[j].h_texcoords == m.h_texcoords) {
+                shared = j;
+                break;
+            }
+        DevMesh d{};
+        if (shared >= 0) {
+            d = meshes[shared];
+        } else {
+            for (int64_t k = 0; k < 3 * m.n_triangles; ++k)
+                KRR_CHECK_ARG(m.h_indices[k] < (uint64_t)m.n_vertices, "mesh index out of range");
+            KRR_TRY(dev_upload(wf, const_cast<float **>(&d.pos), m.h_positions, 3 * m.n_vertices));
+            KRR_TRY(dev_upload(wf, const_cast<float **>(&d.nrm), m.h_normals, 3 * m.n_vertices));
+            if (m.h_texcoords) KRR_TRY(dev_upload(wf, const_cast<float **>(&d.uv), m.h_texcoords, 2 * m.n_vertices));
+            KRR_TRY(dev_upload(wf, const_cast<uint32_t **>(&d.idx), m.h_indices, 3 * m.n_triangles));
+        }
+        d.material = m.material;
+        d.medium_inside = m.medium_inside;
+        d.medium_outside = m.medium_outside;
+        meshes[i] = d;
+    }
+    // materials (src/scene/krrscene.cpp:208-227: specular alpha = 1 - roughness)
+    std::vector<DevMaterial> mats(std::max(1, sd->n_materials));
+    for (int i = 0; i < sd->n_materials; ++i) {
+        const krr_material_desc &m = sd->materials[i];
+        KRR_CHECK_ARG(m.type >= 0 && m.type <= 3, "unknown material type");
+        DevMaterial d{};
+        d.type = m.type;
+        for (int k = 0; k < 3; ++k) d.diffuse[k] = m.diffuse[k];
+        d.spec_alpha = 1.f - m.roughness;
+        d.spec_trans = m.specular_transmission;
+        d.eta = m.eta;
+        d.anisotropic = m.anisotropic;
+        mats[i] = d;
+    }
+    // instances, triangle offsets and the light list (src/core/device/scene.cpp:93-132)
+    std::vector<DevInstance> insts(sd->n_instances);
+    std::vector<DevLight> lights;
+    std::vector<uint32_t> offsets(std::max(1, sd->n_instances));
+    uint64_t n_tris = 0;
+    for (int i = 0; i < sd->n_instances; ++i) {
+        const krr_instance_desc &in = sd->instances[i];
+        KRR_CHECK_ARG(in.mesh >= 0 && in.mesh < sd->n_meshes, "instance mesh out of range");
+        const krr_mesh_desc &m = sd->meshes[in.mesh];
+        DevInstance d{};
+        std::memcpy(d.xf, in.transform, sizeof(d.xf));
+        inverse_transpose(in.transform, d.nxf);
+        d.mesh = in.mesh;
+        d.prim_offset = (uint32_t)n_tris;
+        offsets[i] = (uint32_t)n_tris;
+        d.light_offset = -1;
+        float le[3] = {m.emission[0], m.emission[1], m.emission[2]};
+        if (le[0] > 0.f || le[1] > 0.f || le[2] > 0.f) {
+            float scale = std::max(le[0], std::max(le[1], le[2]));   // mesh.cpp:47-48
+            for (int k = 0; k < 3; ++k) d.le[k] = le[k] / scale;
+            d.le_scale = scale;
+            d.light_offset = (int32_t)lights.size();
+            for (int64_t t = 0; t < m.n_triangles; ++t) lights.push_back(DevLight{0, i, (uint32_t)t, 0});
+        }
+        insts[i] = d;
+        n_tris += (uint64_t)m.n_triangles;
+        KRR_CHECK_ARG(n_tris < 0x7fffffffull, "too many triangles");
+    }
+    // infinite lights follow the mesh lights
+    std::vector<DevInfinite> infs(std::max(0, sd->n_infinite_lights));
+    for (int i = 0; i < sd->n_infinite_lights; ++i) {
+        const krr_infinite_light_desc &l = sd->infinite_lights[i];
+        DevInfinite d{};
+        for (int k = 0; k < 3; ++k) d.tint[k] = l.tint[k];
+        d.scale = l.scale;
+        std::memcpy(d.rot, l.rotation, sizeof(d.rot));
+        if (l.h_image) {
+            KRR_CHECK_ARG(l.width > 0 && l.height > 0, "environment image size");
+            float4 *img = nullptr;
+            KRR_TRY(dev_upload(wf, &img, reinterpret_cast<const float4 *>(l.h_image),
+                               (size_t)l.width * l.height));
+            d.image = img;
+            d.w = l.width;
+            d.h = l.height;
+        }
+        infs[i] = d;
+        lights.push_back(DevLight{1, i, 0, 0});
+    }
+    KRR_CHECK_ARG(!lights.empty(), "the scene has no light");
+
+    DevScene s{};
+    KRR_TRY(dev_upload(wf, const_cast<DevMesh **>(&s.meshes), meshes.data(), meshes.size()));
+    KRR_TRY(dev_upload(wf, const_cast<DevMaterial **>(&s.materials), mats.data(), mats.size()));
+    KRR_TRY(dev_upload(wf, const_cast<DevInstance **>(&s.instances), insts.data(), insts.size()));
+    KRR_TRY(dev_upload(wf, const_cast<DevLight **>(&s.lights), lights.data(), lights.size()));
+    s.n_lights = (int32_t)lights.size();
+    uint32_t *d_offsets = nullptr;
+    KRR_TRY(dev_upload(wf, &d_offsets, offsets.data(), offsets.size()));
+    uint32_t *tri_inst = nullptr;
+    KRR_CUDA(cudaMalloc(&tri_inst, std::max<uint64_t>(n_tris, 1) * sizeof(uint32_t)));
+    wf->scene_allocs.push_back(tri_inst);
+    if (n_tris)
+        k_fill_instance_ids<<<grid_for(n_tris), kThreads, 0, st>>>(tri_inst, d_offsets,
+                                                                   sd->n_instances, n_tris);
+    KRR_CUDA(cudaGetLastError());
+    s.tri_instance = tri_inst;
+
+    // world-space triangles and the BVH
+    float *d_world = nullptr;
+    KRR_CUDA(cudaMalloc(&d_world, std::max<uint64_t>(n_tris, 1) * 9 * sizeof(float)));
+    if (n_tris) k_flatten<<<grid_for(n_tris), kThreads, 0, st>>>(s, sd->n_instances, d_world, n_tris);
+    KRR_CUDA(cudaGetLastError());
+    int stat = accel_build(&wf->accel, d_world, (int64_t)n_tris, st);
+    cudaFree(d_world);
+    if (stat != KRR_OK) return stat;
+    // null-material triangles never block shadow rays (device.cu:83-88)
+    if (n_tris) {
+        uint8_t *mask = nullptr;
+        KRR_CUDA(cudaMalloc(&mask, n_tris));
+        k_null_mask<<<grid_for(n_tris), kThreads, 0, st>>>(s, (int64_t)n_tris, mask);
+        KRR_CUDA(cudaGetLastError());
+        KRR_TRY(accel_set_mask(&wf->accel, mask, st));
+        KRR_CUDA(cudaStreamSynchronize(st));
+        cudaFree(mask);
+    }
+    // scene radius = length of the bounding-box diagonal (scene.cpp:108)
+    float dx = wf->accel.scene_hi[0] - wf->accel.scene_lo[0];
+    float dy = wf->accel.scene_hi[1] - wf->accel.scene_lo[1];
+    float dz = wf->accel.scene_hi[2] - wf->accel.scene_lo[2];
+    wf->scene_radius = std::sqrt(dx * dx + dy * dy + dz * dz);
+    for (auto &d : infs) d.scene_radius = wf->scene_radius;
+    KRR_TRY(dev_upload(wf, const_cast<DevInfinite **>(&s.infinite), infs.data(), infs.size()));
+    s.n_infinite = (int32_t)infs.size();
+
+    // media
+    std::vector<DevMedium> media(sd->n_media);
+    for (int i = 0; i < sd->n_media; ++i) {
+        const krr_medium_desc &m = sd->media[i];
+        DevMedium d{};
+        d.nx = m.nx; d.ny = m.ny; d.nz = m.nz;
+        for (int k = 0; k < 3; ++k) {
+            d.lo[k] = m.bounds_min[k]; d.hi[k] = m.bounds_max[k];
+            d.sigma_t[k] = m.sigma_t[k]; d.albedo[k] = m.albedo[k];
+            d.mres[k] = std::max(1, m.majorant_res[k]);
+        }
+        d.g = m.g;
+        d.scale = m.scale;
+        if (m.h_density) {
+            KRR_CHECK_ARG(m.nx > 0 && m.ny > 0 && m.nz > 0, "density grid size");
+            uint16_t *g = nullptr;
+            KRR_TRY(dev_upload(wf, &g, m.h_density, (size_t)m.nx * m.ny * m.nz));
+            d.density = g;
+        }
+        media[i] = d;
+    }
+    KRR_TRY(dev_upload(wf, const_cast<DevMedium **>(&s.media), media.data(), media.size()));
+    s.n_media = sd->n_media;
+    wf->scene = s;
+    wf->has_scene = true;
+    wf->medium = wf->params.enable_medium && s.n_media > 0;
+    KRR_CUDA(cudaStreamSynchronize(st));
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_resize(krr_wf *wf, int32_t width, int32_t height) {
+    KRR_CHECK_ARG(wf && width > 0 && height > 0, "bad frame size");
+    KRR_CHECK_ARG((int64_t)width * height < (1ll << 30), "frame too large");
+    cudaDeviceSynchronize();
+    free_queues(wf);
+    wf->width = width;
+    wf->height = height;
+    wf->n = (int64_t)width * height;
+    for (int k = 0; k < Q_COUNT; ++k)
+        KRR_CUDA(cudaMalloc(&wf->qbuf[k], (size_t)kChannels[k] * wf->n * sizeof(float4)));
+    KRR_CUDA(cudaMalloc(&wf->d_counts, 16 * sizeof(int32_t)));
+    KRR_CUDA(cudaMemset(wf->d_counts, 0, 16 * sizeof(int32_t)));
+    KRR_CUDA(cudaMalloc(&wf->hits, wf->n * sizeof(float4)));
+    KRR_CUDA(cudaMalloc(&wf->occluded, wf->n));
+    KRR_CUDA(cudaMalloc(&wf->ps.L, wf->n * sizeof(float4)));
+    KRR_CUDA(cudaMalloc(&wf->ps.pixel, wf->n * sizeof(float4)));
+    KRR_CUDA(cudaMalloc(&wf->ps.rng, wf->n * sizeof(ulonglong2)));
+    wf->grid = grid_for(wf->n);
+    return KRR_OK;
+}
+
+static int ready(krr_wf *wf) {
+    if (!wf) return fail(KRR_ERR_INVALID_ARGUMENT, "pass is NULL");
+    if (!wf->has_scene) return fail(KRR_ERR_NOT_READY, "set_scene has not been called");
+    if (!wf->n) return fail(KRR_ERR_NOT_READY, "resize has not been called");
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_begin_frame(krr_wf *wf, int64_t frame_index, const krr_camera_desc *c,
+                                  void *stream) {
+    KRR_TRY(ready(wf));
+    KRR_CHECK_ARG(c != nullptr, "camera is NULL");
+    KRR_CHECK_ARG(c->lens_radius <= 1e-5f, "thin-lens cameras are not supported");
+    cudaStream_t st = as_stream(stream);
+    DevCamera d{};
+    for (int k = 0; k < 3; ++k) d.pos[k] = c->position[k];
+    for (int k = 0; k < 9; ++k) d.rot[k] = c->rotation[k];
+    float fov = std::atan2(c->film_size[1] * 0.5f, c->focal_length);
+    d.tan_fov = std::tan(fov);
+    d.aspect = c->aspect_ratio;
+    d.lens_radius = c->lens_radius;
+    d.focal_distance = c->focal_distance;
+    d.shutter_open = c->shutter_open;
+    d.shutter_time = c->shutter_time;
+    d.medium = c->medium;
+    wf->cam = d;
+    wf->frame_index = frame_index;
+    uint32_t sample_index = (uint32_t)(frame_index * wf->params.spp + wf->params.seed);
+    k_begin_frame<<<wf->grid, kThreads, 0, st>>>(wf->ps, wf->width, wf->n, sample_index);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_generate_camera_rays(krr_wf *wf, void *stream) {
+    KRR_TRY(ready(wf));
+    cudaStream_t st = as_stream(stream);
+    k_camera_rays<<<wf->grid, kThreads, 0, st>>>(wf->ps, wf->q(Q_RAY0), wf->cam, wf->width,
+                                                  wf->height, wf->n);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_reset_queues(krr_wf *wf, int32_t depth, void *stream) {
+    KRR_TRY(ready(wf));
+    k_reset_queues<<<1, 32, 0, as_stream(stream)>>>(wf->d_counts, depth & 1, depth < 0 ? 1 : 0);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_trace_closest(krr_wf *wf, int32_t depth, void *stream) {
+    KRR_TRY(ready(wf));
+    cudaStream_t st = as_stream(stream);
+    int cur = depth & 1;
+    Queue rq = wf->q(cur);
+    TraceLaunch l{};
+    l.ray_o = rq.base;
+    l.ray_d = rq.base + wf->n;
+    l.ray_stride = 1;
+    l.d_count = rq.count;
+    l.hits = wf->hits;
+    l.counter = wf->accel.d_scratch;
+    l.err = wf->accel.d_scratch + 4;
+    KRR_TRY(launch_trace_closest(&wf->accel, l, st));
+    k_hit_process<<<wf->grid, kThreads, 0, st>>>(wf->scene, rq, wf->hits, wf->q(cur ^ 1),
+                                                  wf->q(Q_MISS), wf->q(Q_HIT_LIGHT), wf->q(Q_SCATTER),
+                                                  wf->q(Q_MEDIUM_SAMPLE), wf->medium ? 1 : 0, wf->err());
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_handle_hit(krr_wf *wf, void *stream) {
+    KRR_TRY(ready(wf));
+    k_handle_hit<<<wf->grid, kThreads, 0, as_stream(stream)>>>(wf->scene, wf->q(Q_HIT_LIGHT), wf->ps,
+                                                               wf->params.nee);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_handle_miss(krr_wf *wf, void *stream) {
+    KRR_TRY(ready(wf));
+    if (wf->scene.n_infinite == 0) return KRR_OK;
+    k_handle_miss<<<wf->grid, kThreads, 0, as_stream(stream)>>>(wf->scene, wf->q(Q_MISS), wf->ps,
+                                                                wf->params.nee);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_generate_scatter_rays(krr_wf *wf, int32_t depth, void *stream) {
+    KRR_TRY(ready(wf));
+    int cur = depth & 1;
+    k_scatter<<<wf->grid, kThreads, 0, as_stream(stream)>>>(wf->scene, wf->q(Q_SCATTER),
+                                                            wf->q(cur ^ 1), wf->q(Q_SHADOW), wf->ps,
+                                                            wf->params.nee, wf->params.rr, wf->err());
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_trace_shadow(krr_wf *wf, void *stream) {
+    KRR_TRY(ready(wf));
+    cudaStream_t st = as_stream(stream);
+    if (wf->medium) return launch_trace_shadow_tr(wf, st);
+    Queue sq = wf->q(Q_SHADOW);
+    TraceLaunch l{};
+    l.ray_o = sq.base;
+    l.ray_d = sq.base + wf->n;
+    l.ray_stride = 1;
+    l.d_count = sq.count;
+    l.occluded = wf->occluded;
+    l.counter = wf->accel.d_scratch;
+    l.err = wf->accel.d_scratch + 4;
+    KRR_TRY(launch_trace_any(&wf->accel, l, st));
+    k_shadow_resolve<<<wf->grid, kThreads, 0, st>>>(sq, wf->occluded, wf->ps);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_sample_medium_interaction(krr_wf *wf, int32_t depth, void *stream) {
+    KRR_TRY(ready(wf));
+    if (!wf->medium) return KRR_OK;
+    return launch_medium_sample(wf, depth, as_stream(stream));
+}
+
+extern "C" int krr_wf_sample_medium_scattering(krr_wf *wf, int32_t depth, void *stream) {
+    KRR_TRY(ready(wf));
+    if (!wf->medium) return KRR_OK;
+    return launch_medium_scatter(wf, depth, as_stream(stream));
+}
+
+extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
+    KRR_TRY(ready(wf));
+    KRR_CHECK_ARG(d_out != nullptr, "output is NULL");
+    cudaStream_t st = as_stream(stream);
+    for (int s = 0; s < wf->params.spp; ++s) {
+        KRR_TRY(krr_wf_reset_queues(wf, -1, stream));
+        KRR_TRY(krr_wf_generate_camera_rays(wf, stream));
+        for (int depth = 0;; ++depth) {
+            KRR_TRY(krr_wf_reset_queues(wf, depth, stream));
+            KRR_TRY(krr_wf_trace_closest(wf, depth, stream));
+            if (wf->medium) KRR_TRY(krr_wf_sample_medium_interaction(wf, depth, stream));
+            KRR_TRY(krr_wf_handle_hit(wf, stream));
+            KRR_TRY(krr_wf_handle_miss(wf, stream));
+            if (depth == wf->params.max_depth) break;
+            if (wf->medium) KRR_TRY(krr_wf_sample_medium_scattering(wf, depth, stream));
+            KRR_TRY(krr_wf_generate_scatter_rays(wf, depth, stream));
+            if (wf->params.nee) KRR_TRY(krr_wf_trace_shadow(wf, stream));
+        }
+        k_accumulate<<<wf->grid, kThreads, 0, st>>>(wf->ps, wf->n);
+        KRR_CUDA(cudaGetLastError());
+    }
+    k_resolve<<<wf->grid, kThreads, 0, st>>>(wf->ps, reinterpret_cast<float4 *>(d_out), wf->width,
+                                              wf->height, (float)wf->params.spp,
+                                              wf->params.enable_clamp, wf->params.clamp_max);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_queue_size(krr_wf *wf, int32_t queue, int32_t *out, void *stream) {
+    KRR_TRY(ready(wf));
+    KRR_CHECK_ARG(queue >= 0 && queue < Q_COUNT && out, "bad queue");
+    KRR_CUDA(cudaMemcpyAsync(out, wf->d_counts + queue, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                             as_stream(stream)));
+    KRR_CUDA(cudaStreamSynchronize(as_stream(stream)));
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_pixel_radiance(krr_wf *wf, const float **d_L) {
+    KRR_TRY(ready(wf));
+    KRR_CHECK_ARG(d_L != nullptr, "NULL argument");
+    *d_L = reinterpret_cast<const float *>(wf->ps.L);
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_ray_queue(krr_wf *wf, int32_t depth, const float **d_origin_tmin,
+                                const float **d_dir_tmax, const float **d_pu_pixel,
+                                int32_t *capacity) {
+    KRR_TRY(ready(wf));
+    KRR_CHECK_ARG(d_origin_tmin && d_dir_tmax, "NULL argument");
+    const float4 *b = wf->qbuf[depth & 1];
+    *d_origin_tmin = reinterpret_cast<const float *>(b);
+    *d_dir_tmax = reinterpret_cast<const float *>(b + wf->n);
+    if (d_pu_pixel) *d_pu_pixel = reinterpret_cast<const float *>(b + 5 * wf->n);
+    if (capacity) *capacity = (int32_t)wf->n;
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_device_errors(krr_wf *wf, uint32_t *out, void *stream) {
+    KRR_CHECK_ARG(wf && out, "NULL argument");
+    uint32_t flags[2] = {0, 0};
+    cudaStream_t st = as_stream(stream);
+    if (wf->d_counts) {
+        KRR_CUDA(cudaMemcpyAsync(&flags[0], wf->d_counts + 8, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        KRR_CUDA(cudaMemsetAsync(wf->d_counts + 8, 0, sizeof(uint32_t), st));
+    }
+    if (wf->accel.d_scratch) {
+        KRR_CUDA(cudaMemcpyAsync(&flags[1], wf->accel.d_scratch + 4, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        KRR_CUDA(cudaMemsetAsync(wf->accel.d_scratch + 4, 0, sizeof(uint32_t), st));
+    }
+    KRR_CUDA(cudaStreamSynchronize(st));
+    *out = flags[0] | flags[1];
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_accel(krr_wf *wf, const krr_accel **out) {
+    KRR_TRY(ready(wf));
+    KRR_CHECK_ARG(out != nullptr, "NULL argument");
+    *out = &wf->accel;
+    return KRR_OK;
+}
+
+// Medium stages are added with the medium kernels; until then a scene with
+// media renders without them only when enable_medium is off.
+namespace krr {
+int launch_medium_sample(krr_wf *, int, cudaStream_t) {
+    return fail(KRR_ERR_NOT_READY, "participating media are not built in this library");
+}
+int launch_medium_scatter(krr_wf *, int, cudaStream_t) {
+    return fail(KRR_ERR_NOT_READY, "participating media are not built in this library");
+}
+int launch_trace_shadow_tr(krr_wf *, cudaStream_t) {
+    return fail(KRR_ERR_NOT_READY, "participating media are not built in this library");
+}
+}  // namespace krr

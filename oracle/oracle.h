@@ -1,0 +1,57 @@
+/*
+ * oracle.h — CPU restatement of the WavefrontPathTracer hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA path
+ * in kiraray_gb300/: only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline legs may load it.  The product never links or calls it.
+ *
+ * Parity status: the reference cannot be built here (OptiX, Eigen, NanoVDB
+ * and the Vulkan stack are absent and the build is Windows-only), and it has
+ * no tests or golden vectors.  Shading, sampling, light and medium code follow
+ * the cited reference files line by line; ray/triangle intersection restates
+ * the published watertight test of Woop, Benthin and Wald (JCGT 2013) because
+ * the reference delegates it to OptiX (closed).  Parity is therefore
+ * UNPINNED against reference outputs; it is pinned against known answers
+ * (PCG32 published sequence, analytic furnace / Fresnel / transmittance
+ * values) in tests/.
+ *
+ * Built with -ffp-contract=off so that every float operation rounds exactly
+ * as written.
+ */
+#ifndef KRR_ORACLE_H
+#define KRR_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_bvh oracle_bvh;
+
+/* Binned-SAH binary BVH over world-space triangles (float3 x 3 per triangle). */
+int oracle_bvh_build(const float *vertices, int64_t n_tris, int threads, oracle_bvh **out);
+void oracle_bvh_free(oracle_bvh *bvh);
+/* Triangles whose mask byte is 0 are ignored by any-hit queries. */
+void oracle_bvh_set_mask(oracle_bvh *bvh, const uint8_t *mask);
+
+/* rays: 8 floats each (o.xyz, tmin, d.xyz, tmax); hits: (t, b1, b2, prim bits). */
+int oracle_trace_closest(const oracle_bvh *bvh, const float *rays, int64_t n, float *hits,
+                         int threads);
+int oracle_trace_any(const oracle_bvh *bvh, const float *rays, int64_t n, uint8_t *occluded,
+                     int threads);
+/* Brute force over all triangles (small scenes). */
+int oracle_trace_closest_brute(const float *vertices, int64_t n_tris, const float *rays,
+                               int64_t n, float *hits);
+
+/* PCG sampler (src/core/sampler.h:13-91): `count` floats drawn after
+ * setPixelSample(pixel, sample_index) and advance(advance_by). */
+void oracle_pcg_floats(uint32_t px, uint32_t py, uint32_t sample_index, int64_t advance_by,
+                       int count, float *out);
+/* Raw PCG32 outputs after setSeed(initstate, initseq). */
+void oracle_pcg_u32(uint64_t initstate, uint64_t initseq, int count, uint32_t *out);
+uint32_t oracle_interleave_32bit(uint32_t x, uint32_t y);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

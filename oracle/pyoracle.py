@@ -1,0 +1,104 @@
+"""ctypes loader of oracle/liboracle.so (test infrastructure only)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    deps = list(HERE.glob("*.cpp")) + list(HERE.glob("*.h"))
+    if force or not LIB.exists() or any(p.stat().st_mtime > LIB.stat().st_mtime for p in deps):
+        jobs = str(min(16, os.cpu_count() or 4))
+        subprocess.run(["make", "-s", "-j", jobs, "-C", str(HERE)], check=True)
+    return LIB
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(str(LIB))
+        P, I64 = C.c_void_p, C.c_int64
+        sig = {
+            "oracle_bvh_build": (C.c_int, [P, I64, C.c_int, C.POINTER(P)]),
+            "oracle_bvh_free": (None, [P]),
+            "oracle_bvh_set_mask": (None, [P, P]),
+            "oracle_trace_closest": (C.c_int, [P, P, I64, P, C.c_int]),
+            "oracle_trace_any": (C.c_int, [P, P, I64, P, C.c_int]),
+            "oracle_trace_closest_brute": (C.c_int, [P, I64, P, I64, P]),
+            "oracle_pcg_floats": (None, [C.c_uint32, C.c_uint32, C.c_uint32, I64, C.c_int, P]),
+            "oracle_pcg_u32": (None, [C.c_uint64, C.c_uint64, C.c_int, P]),
+            "oracle_interleave_32bit": (C.c_uint32, [C.c_uint32, C.c_uint32]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def threads() -> int:
+    return max(1, os.cpu_count() or 1)
+
+
+class Bvh:
+    def __init__(self, tris: np.ndarray):
+        self.tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 9)
+        self._h = C.c_void_p()
+        load().oracle_bvh_build(self.tris.ctypes.data, self.tris.shape[0], threads(),
+                                C.byref(self._h))
+
+    def set_mask(self, mask):
+        self._mask = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+        load().oracle_bvh_set_mask(self._h, None if self._mask is None else self._mask.ctypes.data)
+
+    def closest(self, rays: np.ndarray, nthreads: int | None = None) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        out = np.empty((rays.shape[0], 4), np.float32)
+        load().oracle_trace_closest(self._h, rays.ctypes.data, rays.shape[0], out.ctypes.data,
+                                    nthreads or threads())
+        return out
+
+    def any(self, rays: np.ndarray, nthreads: int | None = None) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        out = np.empty((rays.shape[0],), np.uint8)
+        load().oracle_trace_any(self._h, rays.ctypes.data, rays.shape[0], out.ctypes.data,
+                                nthreads or threads())
+        return out
+
+    def __del__(self):
+        try:
+            if self._h:
+                load().oracle_bvh_free(self._h)
+        except Exception:
+            pass
+
+
+def closest_brute(tris: np.ndarray, rays: np.ndarray) -> np.ndarray:
+    tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 9)
+    rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+    out = np.empty((rays.shape[0], 4), np.float32)
+    load().oracle_trace_closest_brute(tris.ctypes.data, tris.shape[0], rays.ctypes.data,
+                                      rays.shape[0], out.ctypes.data)
+    return out
+
+
+def pcg_floats(px: int, py: int, sample_index: int, advance: int, count: int) -> np.ndarray:
+    out = np.empty(count, np.float32)
+    load().oracle_pcg_floats(px, py, sample_index, advance, count, out.ctypes.data)
+    return out
+
+
+def pcg_u32(initstate: int, initseq: int, count: int) -> np.ndarray:
+    out = np.empty(count, np.uint32)
+    load().oracle_pcg_u32(initstate, initseq, count, out.ctypes.data)
+    return out

@@ -1,0 +1,118 @@
+"""Ray-set generators shared by the tests (numpy, float32)."""
+from __future__ import annotations
+
+import numpy as np
+
+
+def pinhole_rays(scene, width=None, height=None, jitter_seed=None) -> np.ndarray:
+    """Camera rays of the scene's pinhole camera through pixel centres (or
+    jittered), float32 [H*W, 8]."""
+    cam = scene.camera
+    w = width or scene.width
+    h = height or scene.height
+    ys, xs = np.meshgrid(np.arange(h), np.arange(w), indexing="ij")
+    px = xs.reshape(-1).astype(np.float64) + 0.5
+    py = ys.reshape(-1).astype(np.float64) + 0.5
+    if jitter_seed is not None:
+        rng = np.random.default_rng(jitter_seed)
+        px += rng.random(px.shape) - 0.5
+        py += rng.random(py.shape) - 0.5
+    ndcx = 2 * px / w - 1
+    ndcy = 1 - 2 * py / h
+    tanf = (cam.film_size[1] * 0.5) / cam.focal_length
+    d = np.stack([tanf * cam.aspect_ratio * ndcx, tanf * ndcy, -np.ones_like(ndcx)], -1)
+    d /= np.linalg.norm(d, axis=-1, keepdims=True)
+    R = np.asarray(cam.rotation, np.float64)
+    d = d @ R.T
+    out = np.zeros((d.shape[0], 8), np.float32)
+    out[:, :3] = cam.position
+    out[:, 3] = 0.0
+    out[:, 4:7] = d
+    out[:, 7] = np.inf
+    return out
+
+
+def bounce_rays(tris: np.ndarray, rays: np.ndarray, hits: np.ndarray, seed: int) -> np.ndarray:
+    """Cosine-weighted rays from the primary hit points around the geometric
+    normal facing the incoming ray (first-bounce diffuse set)."""
+    prim = hits[:, 3].view(np.uint32)
+    ok = prim != 0xFFFFFFFF
+    t = hits[ok, 0:1].astype(np.float64)
+    o = rays[ok, 0:3].astype(np.float64) + t * rays[ok, 4:7]
+    v = tris[prim[ok]].reshape(-1, 3, 3).astype(np.float64)
+    n = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
+    n /= np.linalg.norm(n, axis=-1, keepdims=True) + 1e-30
+    flip = np.sum(n * rays[ok, 4:7], -1) > 0
+    n[flip] *= -1
+    rng = np.random.default_rng(seed)
+    u1, u2 = rng.random(n.shape[0]), rng.random(n.shape[0])
+    r, phi = np.sqrt(u1), 2 * np.pi * u2
+    local = np.stack([r * np.cos(phi), r * np.sin(phi), np.sqrt(np.maximum(0, 1 - u1))], -1)
+    a = np.where(np.abs(n[:, :1]) > 0.9, np.array([[0, 1, 0]]), np.array([[1, 0, 0]]))
+    tt = np.cross(a, n)
+    tt /= np.linalg.norm(tt, axis=-1, keepdims=True)
+    bb = np.cross(n, tt)
+    d = local[:, :1] * tt + local[:, 1:2] * bb + local[:, 2:3] * n
+    out = np.zeros((n.shape[0], 8), np.float32)
+    out[:, :3] = o + n * 1e-4
+    out[:, 4:7] = d
+    out[:, 7] = np.inf
+    return out
+
+
+def random_soup(n: int, seed: int, size: float = 0.2) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    c = rng.random((n, 1, 3)) * 2 - 1
+    return (c + (rng.random((n, 3, 3)) - 0.5) * size).reshape(n, 9).astype(np.float32)
+
+
+def random_rays(n: int, seed: int, box: float = 1.5) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    o = (rng.random((n, 3)) * 2 - 1) * box
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=-1, keepdims=True)
+    out = np.zeros((n, 8), np.float32)
+    out[:, :3] = o
+    out[:, 4:7] = d
+    out[:, 7] = np.inf
+    return out
+
+
+def grid_mesh(n: int) -> np.ndarray:
+    """n x n unit quads in the z=0 plane as 2n^2 triangles (shared edges)."""
+    tris = []
+    for j in range(n):
+        for i in range(n):
+            a, b, c, d = (i, j, 0), (i + 1, j, 0), (i + 1, j + 1, 0), (i, j + 1, 0)
+            tris.append([*a, *b, *c])
+            tris.append([*a, *c, *d])
+    return (np.array(tris, np.float32) / n).astype(np.float32)
+
+
+def vertex_edge_rays(n: int, seed: int) -> np.ndarray:
+    """Rays through the shared vertices and edge midpoints of grid_mesh(n),
+    from random origins above the plane."""
+    rng = np.random.default_rng(seed)
+    pts = []
+    for j in range(n + 1):
+        for i in range(n + 1):
+            pts.append((i / n, j / n))
+            if i < n:
+                pts.append(((i + 0.5) / n, j / n))
+            if j < n:
+                pts.append((i / n, (j + 0.5) / n))
+            if i < n and j < n:
+                pts.append(((i + 0.5) / n, (j + 0.5) / n))   # on the diagonal
+    pts = np.array(pts, np.float64)
+    # keep strictly interior targets so that every ray must hit
+    inner = (pts[:, 0] > 0) & (pts[:, 0] < 1) & (pts[:, 1] > 0) & (pts[:, 1] < 1)
+    pts = pts[inner]
+    o = np.concatenate([rng.random((pts.shape[0], 2)) * 2 - 0.5,
+                        rng.random((pts.shape[0], 1)) * 2 + 0.5], 1)
+    tgt = np.concatenate([pts, np.zeros((pts.shape[0], 1))], 1)
+    d = tgt - o
+    out = np.zeros((pts.shape[0], 8), np.float32)
+    out[:, :3] = o
+    out[:, 4:7] = d
+    out[:, 7] = np.inf
+    return out

@@ -1,0 +1,162 @@
+"""GPU closest-hit / any-hit parity against the CPU oracle (bit-exact).
+
+The hit record (t, b1, b2, triangle id) of the CUDA traversal must equal the
+oracle's bit for bit: both run the same watertight test with the same
+rounding, and ties in t go to the smaller triangle id on both sides."""
+import numpy as np
+import pytest
+import torch
+
+from kiraray_gb300 import scenes
+from kiraray_gb300.accel import Accel
+from oracle import pyoracle as O
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_closest(acc, rays):
+    out = acc.trace_closest(torch.from_numpy(rays).cuda())
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def _assert_bits_equal(a, b, what):
+    ua, ub = a.view(np.uint32), b.view(np.uint32)
+    bad = np.where(~np.all(ua == ub, axis=1))[0]
+    assert bad.size == 0, f"{what}: {bad.size} of {a.shape[0]} hits differ, first {bad[:5]}: " \
+                          f"gpu {a[bad[:3]]} oracle {b[bad[:3]]}"
+
+
+def test_cornell_box_camera_rays(krr_lib, cuda):
+    sc = scenes.cornell_box()
+    tris = sc.world_triangles()
+    rays = H.pinhole_rays(sc)
+    acc = Accel(tris)
+    got = _gpu_closest(acc, rays)
+    want = O.Bvh(tris).closest(rays)
+    _assert_bits_equal(got, want, "cornell camera rays")
+    assert (got[:, 3].view(np.uint32) != 0xFFFFFFFF).mean() > 0.9
+
+
+@pytest.mark.parametrize("n_tris,seed", [(1, 0), (2, 1), (3, 2), (4, 3), (5, 9), (100, 4),
+                                         (5000, 5), (60000, 6)])
+def test_random_soup_vs_brute_force(krr_lib, cuda, n_tris, seed):
+    tris = H.random_soup(n_tris, seed, size=0.2 if n_tris > 100 else 1.0)
+    rays = H.random_rays(3000, seed + 50)
+    acc = Accel(tris)
+    got = _gpu_closest(acc, rays)
+    want = O.closest_brute(tris, rays) if n_tris <= 5000 else O.Bvh(tris).closest(rays)
+    _assert_bits_equal(got, want, f"soup {n_tris}")
+
+
+def test_shared_vertices_and_edges_do_not_leak(krr_lib, cuda):
+    tris = H.grid_mesh(16)
+    rays = H.vertex_edge_rays(16, 7)
+    acc = Accel(tris)
+    got = _gpu_closest(acc, rays)
+    assert np.all(got[:, 3].view(np.uint32) != 0xFFFFFFFF)
+    _assert_bits_equal(got, O.closest_brute(tris, rays), "grid vertex/edge rays")
+
+
+def test_closed_mesh_from_inside(krr_lib, cuda):
+    m = scenes.icosphere(4)
+    tris = m.positions[m.indices].reshape(-1, 9).astype(np.float32)
+    rays = H.random_rays(50000, 11, box=0.0)
+    got = _gpu_closest(Accel(tris), rays)
+    assert np.all(got[:, 3].view(np.uint32) != 0xFFFFFFFF)
+
+
+def test_axis_aligned_and_degenerate_directions(krr_lib, cuda):
+    sc = scenes.cornell_box()
+    tris = sc.world_triangles()
+    rng = np.random.default_rng(3)
+    dirs = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1],
+                     [0, 0, 0], [1e-30, 0, 1], [-0.0, 1, 0]], np.float32)
+    o = rng.random((400, 3)).astype(np.float32) * 0.9 + 0.05
+    rays = np.zeros((400 * len(dirs), 8), np.float32)
+    rays[:, :3] = np.repeat(o, len(dirs), 0)
+    rays[:, 4:7] = np.tile(dirs, (400, 1))
+    rays[:, 7] = np.inf
+    got = _gpu_closest(Accel(tris), rays)
+    _assert_bits_equal(got, O.closest_brute(tris, rays), "axis-aligned rays")
+
+
+def test_tmin_tmax_and_ties(krr_lib, cuda):
+    t = np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32)
+    tris = np.concatenate([t, t, t, t + np.array([0, 0, -1] * 3, np.float32)])
+    rays = np.array([[0.2, 0.2, 1, 0, 0, 0, -1, np.inf],
+                     [0.2, 0.2, 1, 1.5, 0, 0, -1, np.inf],
+                     [0.2, 0.2, 1, 0, 0, 0, -1, 0.5],
+                     [0.2, 0.2, 1, 0, 0, 0, -1, 1.0]], np.float32)
+    got = _gpu_closest(Accel(tris), rays)
+    assert list(got[:, 3].view(np.uint32)) == [0, 3, 0xFFFFFFFF, 0]
+    _assert_bits_equal(got, O.closest_brute(tris, rays), "windows")
+
+
+def test_any_hit_and_mask(krr_lib, cuda):
+    sc = scenes.cornell_box()
+    tris = sc.world_triangles()
+    rng = np.random.default_rng(8)
+    n = 20000
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, :3] = rng.random((n, 3)) * 0.9 + 0.05
+    rays[:, 4:7] = (rng.random((n, 3)) * 0.9 + 0.05) - rays[:, :3]   # segments, tmax = 1
+    rays[:, 7] = 1.0
+    acc = Accel(tris)
+    occ = acc.trace_any(torch.from_numpy(rays).cuda()).cpu().numpy()
+    ob = O.Bvh(tris)
+    assert np.array_equal(occ, ob.any(rays))
+    mask = np.ones(tris.shape[0], np.uint8)
+    mask[10:22] = 0   # the short box does not block
+    acc.set_mask(mask)
+    ob.set_mask(mask)
+    occ2 = acc.trace_any(torch.from_numpy(rays).cuda()).cpu().numpy()
+    assert np.array_equal(occ2, ob.any(rays))
+    assert occ2.sum() < occ.sum()
+
+
+def test_empty_ray_batch(krr_lib, cuda):
+    acc = Accel(H.random_soup(10, 1))
+    out = acc.trace_closest(torch.empty((0, 8), device="cuda"))
+    assert out.shape == (0, 4)
+
+
+def test_host_buffer_entry_point(krr_lib, cuda):
+    sc = scenes.cornell_box(64, 64)
+    tris = sc.world_triangles()
+    rays = H.pinhole_rays(sc)
+    acc = Accel(tris)
+    out = np.zeros((rays.shape[0], 4), np.float32)
+    acc.trace_closest_host(rays, out)
+    _assert_bits_equal(out, O.Bvh(tris).closest(rays), "host entry point")
+
+
+def test_large_scene_reduced(krr_lib, cuda):
+    sc = scenes.large_scene(width=320, height=180, grid=512, n_spheres=100, sky_size=(64, 32))
+    tris = sc.world_triangles()
+    rays = H.pinhole_rays(sc)
+    acc = Accel(tris)
+    ob = O.Bvh(tris)
+    got = _gpu_closest(acc, rays)
+    want = ob.closest(rays)
+    _assert_bits_equal(got, want, "large scene camera rays")
+    b = H.bounce_rays(tris, rays, want, 5)
+    _assert_bits_equal(_gpu_closest(acc, b), ob.closest(b), "large scene bounce rays")
+    st = acc.stats()
+    assert st["n_triangles"] == tris.shape[0] and st["max_depth"] <= 48
+
+
+@pytest.mark.slow
+def test_full_size_scene_sampled(krr_lib, cuda):
+    """10.9M triangles: GPU hits on a 1-in-64 sample of the 1920x1080 camera
+    rays and of their first bounce equal the oracle's."""
+    sc = scenes.large_scene(sky_size=(64, 32))
+    tris = sc.world_triangles()
+    rays = H.pinhole_rays(sc)[::64].copy()
+    acc = Accel(tris)
+    ob = O.Bvh(tris)
+    want = ob.closest(rays)
+    _assert_bits_equal(_gpu_closest(acc, rays), want, "10M camera rays")
+    b = H.bounce_rays(tris, rays, want, 6)
+    _assert_bits_equal(_gpu_closest(acc, b), ob.closest(b), "10M bounce rays")
