@@ -183,6 +183,23 @@ int krr_accel_set_mask(krr_accel *accel, const uint8_t *h_mask);
 int krr_accel_trace_stats(const krr_accel *accel, const krr_ray *d_rays, int64_t n,
                           int32_t any_hit, unsigned long long *h_counts, void *stream);
 
+/* No-allocation variant of krr_accel_trace_stats (this entry point has no
+ * counterpart in the reference).  For callers that must not allocate device
+ * memory during their work, such as render loops with a fixed per-frame
+ * memory budget (cudaMalloc/cudaFree can synchronise the device and stall the
+ * frame) or hosts whose pool allocator owns all device memory.  Its scratch
+ * (per-ray hit records and counters) lives in one static device array of
+ * KRR_NOALLOC_MAX_RAYS rays (about 1 MiB), resident on every GPU that loads
+ * the library until exit; n must be 1..KRR_NOALLOC_MAX_RAYS or the call
+ * returns KRR_ERR_INVALID_ARGUMENT.  The first call on each device looks up
+ * the array's device address (make it before any stream capture).  All calls
+ * share the array, so calls that overlap on the GPU race; counters are
+ * cleared at the start of each call.  Calls no cudaMalloc, cudaFree or other
+ * allocating routine. */
+#define KRR_NOALLOC_MAX_RAYS 65536
+int krr_accel_trace_stats_noalloc(const krr_accel *accel, const krr_ray *d_rays, int64_t n,
+                                  int32_t any_hit, unsigned long long *h_counts, void *stream);
+
 /* Same as krr_accel_trace_closest, with host buffers: copies the rays in and
  * the hits out inside the call (pinned host memory is fastest). */
 int krr_accel_trace_closest_host(const krr_accel *accel, const krr_ray *h_rays, int64_t n,

@@ -12,6 +12,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libkrr_gb300.so"
 
 KRR_OK = 0
 KRR_MISS = 0xFFFFFFFF
+NOALLOC_MAX_RAYS = 65536
 
 MATERIAL_NULL, MATERIAL_DIFFUSE, MATERIAL_DIELECTRIC, MATERIAL_CONDUCTOR = 0, 1, 2, 3
 QUEUES = ["RAY0", "RAY1", "MISS", "HIT_LIGHT", "SHADOW", "SCATTER", "MEDIUM_SAMPLE",
@@ -91,6 +92,8 @@ SIGNATURES = {
     "krr_accel_set_mask": (_I, [_P, _P]),
     "krr_accel_trace_closest_host": (_I, [_P, _P, C.c_int64, _P, _P]),
     "krr_accel_trace_stats": (_I, [_P, _P, C.c_int64, C.c_int32, C.POINTER(C.c_ulonglong), _P]),
+    "krr_accel_trace_stats_noalloc": (_I, [_P, _P, C.c_int64, C.c_int32,
+                                           C.POINTER(C.c_ulonglong), _P]),
     "krr_wf_params_default": (None, [C.POINTER(WfParams)]),
     "krr_wf_create": (_I, [C.POINTER(WfParams), C.POINTER(_P)]),
     "krr_wf_destroy": (_I, [_P]),
