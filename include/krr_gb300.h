@@ -257,8 +257,11 @@ enum {
 };
 /* Current item count of a queue (synchronises the stream). */
 int krr_wf_queue_size(krr_wf *wf, int32_t queue, int32_t *out_size, void *stream);
-/* Device pointer to the per-pixel radiance L (float3 per pixel, SoA x/y/z planes). */
+/* Device pointer to the per-pixel radiance: float4 per pixel (L.xyz,
+ * lambda[0]), the reference's PixelState::L (workqueue.h:15-26). */
 int krr_wf_pixel_radiance(krr_wf *wf, const float **d_L);
+/* Copies the per-pixel radiance (float4 per pixel) into d_dst on the stream. */
+int krr_wf_read_radiance(krr_wf *wf, float *d_dst, void *stream);
 /* Device pointers to planes of the ray queue used at `depth`: float4 per item
  * (origin.xyz | tmin), (direction.xyz | tmax) and (pu.xyz | pixel id bits);
  * the item count is krr_wf_queue_size(depth & 1). */

@@ -113,6 +113,7 @@ SIGNATURES = {
     "krr_wf_reset_queues": (_I, [_P, C.c_int32, _P]),
     "krr_wf_queue_size": (_I, [_P, C.c_int32, C.POINTER(C.c_int32), _P]),
     "krr_wf_pixel_radiance": (_I, [_P, C.POINTER(_P)]),
+    "krr_wf_read_radiance": (_I, [_P, _P, _P]),
     "krr_wf_ray_queue": (_I, [_P, C.c_int32, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P),
                               C.POINTER(C.c_int32)]),
     "krr_wf_device_errors": (_I, [_P, C.POINTER(C.c_uint32), _P]),

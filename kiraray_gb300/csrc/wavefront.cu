@@ -1116,6 +1116,14 @@ extern "C" int krr_wf_pixel_radiance(krr_wf *wf, const float **d_L) {
     return KRR_OK;
 }
 
+extern "C" int krr_wf_read_radiance(krr_wf *wf, float *d_dst, void *stream) {
+    KRR_TRY(ready(wf));
+    KRR_CHECK_ARG(d_dst != nullptr, "NULL argument");
+    KRR_CUDA(cudaMemcpyAsync(d_dst, wf->ps.L, wf->n * sizeof(float4), cudaMemcpyDeviceToDevice,
+                             as_stream(stream)));
+    return KRR_OK;
+}
+
 extern "C" int krr_wf_ray_queue(krr_wf *wf, int32_t depth, const float **d_origin_tmin,
                                 const float **d_dir_tmax, const float **d_pu_pixel,
                                 int32_t *capacity) {

@@ -1,0 +1,131 @@
+"""Host-side mirror of the reference's WavefrontPathTracer render pass
+(src/render/wavefront/integrator.h:24-104) over the C ABI.
+
+    pt = WavefrontPathTracer({"max_depth": 5, "rr": 0.8, "nee": True})
+    pt.set_scene(scene)          # RenderPass::setScene
+    pt.resize(w, h)              # RenderPass::resize
+    pt.begin_frame(1, camera)    # RenderPass::beginFrame (frame index is 1-based)
+    img = pt.render()            # RenderPass::render -> float32 [H, W, 4] on the GPU
+
+Stage methods keep the reference's names for PPG-style subclasses.  Device
+buffers are torch CUDA tensors; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _lib
+from ._lib import check
+
+PARAM_NAMES = ("nee", "enable_medium", "max_depth", "rr", "enable_clamp", "clamp_max")
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+class WavefrontPathTracer:
+    def __init__(self, params: dict | None = None, spp: int = 1, seed: int = 0):
+        self.lib = _lib.load()
+        self.params = _lib.WfParams()
+        self.lib.krr_wf_params_default(C.byref(self.params))
+        self.params.spp = spp
+        self.params.seed = seed
+        self._apply(params or {})
+        self._h = C.c_void_p()
+        check(self.lib.krr_wf_create(C.byref(self.params), C.byref(self._h)), "krr_wf_create")
+        self.width = self.height = 0
+        self._keep = None
+        self.scene = None
+
+    # from_json, integrator.h:94-103
+    def _apply(self, params: dict):
+        for k, v in params.items():
+            if k not in PARAM_NAMES + ("spp", "seed"):
+                raise KeyError(f"unknown parameter {k!r}")
+            setattr(self.params, k, type(getattr(self.params, k))(v))
+
+    def set_params(self, params: dict):
+        self._apply(params)
+        check(self.lib.krr_wf_set_params(self._h, C.byref(self.params)), "krr_wf_set_params")
+
+    def get_name(self) -> str:
+        return "WavefrontPathTracer"
+
+    def set_scene(self, scene):
+        desc, keep = scene.desc()
+        check(self.lib.krr_wf_set_scene(self._h, C.byref(desc), _stream()), "krr_wf_set_scene")
+        self._keep = (desc, keep)
+        self.scene = scene
+
+    def resize(self, width: int, height: int):
+        check(self.lib.krr_wf_resize(self._h, width, height), "krr_wf_resize")
+        self.width, self.height = width, height
+
+    def begin_frame(self, frame_index: int, camera):
+        self._cam = camera.desc()
+        check(self.lib.krr_wf_begin_frame(self._h, frame_index, C.byref(self._cam), _stream()),
+              "krr_wf_begin_frame")
+
+    def render(self, out: torch.Tensor | None = None) -> torch.Tensor:
+        if out is None:
+            out = torch.empty((self.height, self.width, 4), dtype=torch.float32, device="cuda")
+        check(self.lib.krr_wf_render(self._h, out.data_ptr(), _stream()), "krr_wf_render")
+        return out
+
+    # stage methods (integrator.cpp:50-179)
+    def generate_camera_rays(self):
+        check(self.lib.krr_wf_generate_camera_rays(self._h, _stream()), "generate_camera_rays")
+
+    def reset_queues(self, depth: int):
+        check(self.lib.krr_wf_reset_queues(self._h, depth, _stream()), "reset_queues")
+
+    def trace_closest(self, depth: int):
+        check(self.lib.krr_wf_trace_closest(self._h, depth, _stream()), "trace_closest")
+
+    def handle_hit(self):
+        check(self.lib.krr_wf_handle_hit(self._h, _stream()), "handle_hit")
+
+    def handle_miss(self):
+        check(self.lib.krr_wf_handle_miss(self._h, _stream()), "handle_miss")
+
+    def generate_scatter_rays(self, depth: int):
+        check(self.lib.krr_wf_generate_scatter_rays(self._h, depth, _stream()), "scatter")
+
+    def trace_shadow(self):
+        check(self.lib.krr_wf_trace_shadow(self._h, _stream()), "trace_shadow")
+
+    def sample_medium_interaction(self, depth: int):
+        check(self.lib.krr_wf_sample_medium_interaction(self._h, depth, _stream()), "medium")
+
+    def sample_medium_scattering(self, depth: int):
+        check(self.lib.krr_wf_sample_medium_scattering(self._h, depth, _stream()), "medium")
+
+    def queue_size(self, queue: int) -> int:
+        v = C.c_int32()
+        check(self.lib.krr_wf_queue_size(self._h, queue, C.byref(v), _stream()), "queue_size")
+        return v.value
+
+    def radiance(self) -> torch.Tensor:
+        """Per-pixel L (the reference's PixelState::L) as float32 [H*W, 4]."""
+        out = torch.empty((self.width * self.height, 4), dtype=torch.float32, device="cuda")
+        check(self.lib.krr_wf_read_radiance(self._h, out.data_ptr(), _stream()), "read_radiance")
+        return out
+
+    def device_errors(self) -> int:
+        v = C.c_uint32()
+        check(self.lib.krr_wf_device_errors(self._h, C.byref(v), _stream()), "device_errors")
+        return v.value
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self.lib.krr_wf_destroy(self._h)
+        self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

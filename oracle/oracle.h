@@ -51,6 +51,20 @@ void oracle_pcg_floats(uint32_t px, uint32_t py, uint32_t sample_index, int64_t 
 void oracle_pcg_u32(uint64_t initstate, uint64_t initseq, int count, uint32_t *out);
 uint32_t oracle_interleave_32bit(uint32_t x, uint32_t y);
 
+/* Path tracer restatement: scene in the C-ABI description (include/krr_gb300.h). */
+struct krr_scene_desc;
+struct krr_wf_params;
+struct krr_camera_desc;
+typedef struct oracle_pt oracle_pt;
+int oracle_pt_create(const struct krr_scene_desc *scene, int threads, oracle_pt **out);
+void oracle_pt_free(oracle_pt *pt);
+/* Renders pixels [px_begin, px_end) of one frame; out_L / out_pixel get 3
+ * floats per pixel (L after the frame, and the accumulated pixel). */
+int oracle_pt_render(const oracle_pt *pt, const struct krr_wf_params *params,
+                     const struct krr_camera_desc *camera, int32_t width, int32_t height,
+                     int64_t frame_index, int64_t px_begin, int64_t px_end, float *out_L,
+                     float *out_pixel, int threads);
+
 #ifdef __cplusplus
 }
 #endif

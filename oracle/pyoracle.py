@@ -102,3 +102,49 @@ def pcg_u32(initstate: int, initseq: int, count: int) -> np.ndarray:
     out = np.empty(count, np.uint32)
     load().oracle_pcg_u32(initstate, initseq, count, out.ctypes.data)
     return out
+
+
+class PathTracer:
+    """CPU restatement of the wavefront path tracer (oracle/pathtracer.cpp)."""
+
+    def __init__(self, scene):
+        from kiraray_gb300 import _lib as L
+        lib = load()
+        lib.oracle_pt_create.restype = C.c_int
+        lib.oracle_pt_create.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
+        lib.oracle_pt_free.argtypes = [C.c_void_p]
+        lib.oracle_pt_render.restype = C.c_int
+        lib.oracle_pt_render.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
+                                         C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
+                                         C.c_int]
+        self._L = L
+        self.scene = scene
+        self._desc, self._keep = scene.desc()
+        self._h = C.c_void_p()
+        lib.oracle_pt_create(C.byref(self._desc), threads(), C.byref(self._h))
+
+    def render(self, params: dict, frame_index: int, px_begin: int = 0, px_end: int | None = None,
+               spp: int = 1, seed: int = 0, camera=None):
+        L = self._L
+        p = L.WfParams()
+        p.nee, p.enable_medium, p.max_depth, p.rr = 1, 1, 10, 0.8
+        p.enable_clamp, p.clamp_max, p.spp, p.seed = 0, 1e3, spp, seed
+        for k, v in params.items():
+            setattr(p, k, type(getattr(p, k))(v))
+        sc = self.scene
+        cam = (camera or sc.camera).desc()
+        n_total = sc.width * sc.height
+        px_end = n_total if px_end is None else px_end
+        n = px_end - px_begin
+        out_L = np.zeros((n, 3), np.float32)
+        out_px = np.zeros((n, 3), np.float32)
+        load().oracle_pt_render(self._h, C.byref(p), C.byref(cam), sc.width, sc.height,
+                                frame_index, px_begin, px_end, out_L.ctypes.data,
+                                out_px.ctypes.data, threads())
+        return out_L, out_px
+
+    def __del__(self):
+        try:
+            load().oracle_pt_free(self._h)
+        except Exception:
+            pass

@@ -1,0 +1,129 @@
+"""Wavefront path tracer on the GPU against the CPU restatement (per pixel).
+
+Tolerance: per pixel and channel |gpu - oracle| <= 1e-4 * |oracle| + 1e-6.
+The shading code rounds every float operation as written on both sides, so
+differences come only from CUDA's vs glibc's transcendental functions
+(<= 2 ulp); a pixel whose path takes another branch because of such an ulp
+is an outlier, and at most 0.2% of pixels may be outliers."""
+import numpy as np
+import pytest
+import torch
+
+from kiraray_gb300 import scenes
+from kiraray_gb300.wavefront import WavefrontPathTracer
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+RTOL, ATOL, MAX_OUTLIERS = 1e-4, 1e-6, 0.002
+
+
+def compare(gpu_L, ora_L, what):
+    g = gpu_L.astype(np.float64)
+    o = ora_L.astype(np.float64)
+    bad = np.abs(g - o) > RTOL * np.abs(o) + ATOL
+    bad_px = bad.any(axis=1)
+    frac = bad_px.mean()
+    assert np.isfinite(g).all(), f"{what}: non-finite radiance"
+    assert frac <= MAX_OUTLIERS, (f"{what}: {bad_px.sum()} of {bad_px.size} pixels differ "
+                                  f"(first {np.where(bad_px)[0][:5]}, gpu {g[bad_px][:3]}, "
+                                  f"oracle {o[bad_px][:3]})")
+    return frac
+
+
+def gpu_frame(pt, sc, frame):
+    pt.begin_frame(frame, sc.camera)
+    img = pt.render()
+    L = pt.radiance()
+    torch.cuda.synchronize()
+    return L.cpu().numpy(), img.cpu().numpy()
+
+
+@pytest.mark.parametrize("frame", [1, 2, 7])
+def test_cornell_box_per_pixel(krr_lib, cuda, frame):
+    sc = scenes.cornell_box(128, 128, max_depth=5)
+    pt = WavefrontPathTracer({"max_depth": 5})
+    pt.set_scene(sc)
+    pt.resize(sc.width, sc.height)
+    L, img = gpu_frame(pt, sc, frame)
+    oL, opx = O.PathTracer(sc).render({"max_depth": 5}, frame)
+    compare(L[:, :3], oL, f"cornell frame {frame}")
+    # render() output: pixel / spp, row 0 at the top
+    want = opx.reshape(sc.height, sc.width, 3)[::-1]
+    got = img[..., :3]
+    assert np.mean(np.abs(got - want) > RTOL * np.abs(want) + ATOL) < 3 * MAX_OUTLIERS
+    assert np.all(img[..., 3] == 1.0)
+    assert pt.device_errors() == 0
+    assert (L[:, :3].sum(1) > 0).mean() > 0.4
+
+
+def test_cornell_box_no_nee_and_clamp(krr_lib, cuda):
+    sc = scenes.cornell_box(96, 96, max_depth=4)
+    params = {"max_depth": 4, "nee": False, "enable_clamp": True, "clamp_max": 2.0}
+    pt = WavefrontPathTracer(params)
+    pt.set_scene(sc)
+    pt.resize(sc.width, sc.height)
+    L, img = gpu_frame(pt, sc, 3)
+    oL, _ = O.PathTracer(sc).render(params, 3)
+    compare(L[:, :3], oL, "cornell without NEE")
+    assert img[..., :3].max() <= 2.0
+
+
+def test_large_scene_materials_and_environment(krr_lib, cuda):
+    sc = scenes.large_scene(width=192, height=108, grid=192, n_spheres=60, sky_size=(256, 128),
+                            max_depth=8)
+    pt = WavefrontPathTracer({"max_depth": 8})
+    pt.set_scene(sc)
+    pt.resize(sc.width, sc.height)
+    L, _ = gpu_frame(pt, sc, 1)
+    oL, _ = O.PathTracer(sc).render({"max_depth": 8}, 1)
+    compare(L[:, :3], oL, "large scene")
+    assert pt.device_errors() == 0
+
+
+def test_spp_and_seed(krr_lib, cuda):
+    sc = scenes.cornell_box(64, 64, max_depth=3)
+    pt = WavefrontPathTracer({"max_depth": 3}, spp=3, seed=11)
+    pt.set_scene(sc)
+    pt.resize(sc.width, sc.height)
+    pt.begin_frame(2, sc.camera)
+    img = pt.render().cpu().numpy()
+    _, opx = O.PathTracer(sc).render({"max_depth": 3}, 2, spp=3, seed=11)
+    want = (opx / 3.0).reshape(64, 64, 3)[::-1]
+    bad = np.abs(img[..., :3] - want) > RTOL * np.abs(want) + ATOL
+    assert bad.any(axis=2).mean() <= MAX_OUTLIERS
+
+
+def test_stage_api_and_queue_sizes(krr_lib, cuda):
+    sc = scenes.cornell_box(32, 32)
+    pt = WavefrontPathTracer({"max_depth": 5})
+    pt.set_scene(sc)
+    pt.resize(32, 32)
+    pt.begin_frame(1, sc.camera)
+    pt.reset_queues(-1)
+    pt.generate_camera_rays()
+    assert pt.queue_size(0) == 32 * 32
+    pt.reset_queues(0)
+    pt.trace_closest(0)
+    n_scatter, n_miss = pt.queue_size(5), pt.queue_size(2)
+    assert n_scatter + n_miss <= 32 * 32 and n_scatter > 0
+    pt.handle_hit()
+    pt.handle_miss()
+    pt.generate_scatter_rays(0)
+    assert pt.queue_size(1) <= n_scatter
+    pt.trace_shadow()
+    assert pt.device_errors() == 0
+
+
+def test_resize_and_rescene(krr_lib, cuda):
+    pt = WavefrontPathTracer({"max_depth": 2})
+    sc = scenes.cornell_box(40, 30)
+    pt.set_scene(sc)
+    for w, h in ((40, 30), (17, 23)):
+        pt.resize(w, h)
+        pt.begin_frame(1, sc.camera)
+        img = pt.render()
+        assert img.shape == (h, w, 4) and torch.isfinite(img).all()
+    pt.set_scene(scenes.cornell_box(17, 23))
+    pt.begin_frame(2, sc.camera)
+    assert torch.isfinite(pt.render()).all()
