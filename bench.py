@@ -225,6 +225,7 @@ def run_ours(args, rank, world, local):
     alg_bytes = 48.0 * n_per_step + 80.0 * node_visits + 48.0 * tri_tests
 
     stream = torch.cuda.current_stream()
+    clk = ClockSampler(local).__enter__()
     for _ in range(args.warmup):
         for r, h in sets:
             acc.trace_closest(r, h)
@@ -235,17 +236,17 @@ def run_ours(args, rank, world, local):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        start.record(stream)
-        k = 0
-        for _ in range(args.steps):
-            for r, h in sets:
-                ev[k][0].record(stream)
-                acc.trace_closest(r, h)
-                ev[k][1].record(stream)
-                k += 1
-        end.record(stream)
-        torch.cuda.synchronize()
+    start.record(stream)
+    k = 0
+    for _ in range(args.steps):
+        for r, h in sets:
+            ev[k][0].record(stream)
+            acc.trace_closest(r, h)
+            ev[k][1].record(stream)
+            k += 1
+    end.record(stream)
+    torch.cuda.synchronize()
+    clk.__exit__(None, None, None)
     if world > 1:
         torch.distributed.barrier()
     total_ms = start.elapsed_time(end)
@@ -281,7 +282,8 @@ def run_ours(args, rank, world, local):
     traffic = profile_traffic()
     if rank != 0:
         return
-    cpu = cpu_baseline(tris, [rays_np, bounce_np], args.cpu_seconds, os.cpu_count() or 1)
+    cpu = (cpu_baseline(tris, [rays_np, bounce_np], args.cpu_seconds, os.cpu_count() or 1)
+           if args.cpu_seconds > 0 else None)
     clocks = clk.summary()
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world,

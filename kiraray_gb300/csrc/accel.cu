@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "accel.h"
+#include "accel_device.cuh"
 #include "kmath.cuh"
 
 namespace krr {
@@ -378,73 +379,6 @@ __global__ void k_set_mask(float4 *tris, const uint32_t *leaf_of_prim, const uin
     tris[3 * (size_t)k + 1].w = __uint_as_float(mask ? (uint32_t)(mask[p] != 0) : 1u);
 }
 
-// ------------------------------------------------------------ traversal
-struct RayPre {
-    V3 o, d;
-    float tmin;
-    int kx, ky, kz;
-    float sx, sy, sz;
-};
-
-__device__ __forceinline__ RayPre ray_pre(V3 o, V3 d, float tmin) {
-    RayPre r;
-    r.o = o; r.d = d; r.tmin = tmin;
-    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
-    int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
-    int kx = kz + 1 == 3 ? 0 : kz + 1;
-    int ky = kx + 1 == 3 ? 0 : kx + 1;
-    if (get(d, kz) < 0.f) { int tmp = kx; kx = ky; ky = tmp; }
-    r.kx = kx; r.ky = ky; r.kz = kz;
-    float dz = get(d, kz);
-    r.sx = __fdiv_rn(get(d, kx), dz);
-    r.sy = __fdiv_rn(get(d, ky), dz);
-    r.sz = __fdiv_rn(1.0f, dz);
-    return r;
-}
-
-__device__ __forceinline__ float sel3(float a, float b, float c, int k) {
-    return k == 0 ? a : (k == 1 ? b : c);
-}
-
-// Watertight ray/triangle test; returns t (NaN on a miss, so that a miss fails
-// every comparison including the tie rule at t == tmax == inf) and (b1, b2).
-// Every operation is explicitly rounded so that the CPU restatement of the
-// same steps gives bit-identical results.
-__device__ __forceinline__ float tri_test(const RayPre &r, float4 v0, float4 v1, float4 v2,
-                                          float &b1, float &b2) {
-    float Ax_ = __fsub_rn(v0.x, r.o.x), Ay_ = __fsub_rn(v0.y, r.o.y), Az_ = __fsub_rn(v0.z, r.o.z);
-    float Bx_ = __fsub_rn(v1.x, r.o.x), By_ = __fsub_rn(v1.y, r.o.y), Bz_ = __fsub_rn(v1.z, r.o.z);
-    float Cx_ = __fsub_rn(v2.x, r.o.x), Cy_ = __fsub_rn(v2.y, r.o.y), Cz_ = __fsub_rn(v2.z, r.o.z);
-    float Akx = sel3(Ax_, Ay_, Az_, r.kx), Aky = sel3(Ax_, Ay_, Az_, r.ky), Akz = sel3(Ax_, Ay_, Az_, r.kz);
-    float Bkx = sel3(Bx_, By_, Bz_, r.kx), Bky = sel3(Bx_, By_, Bz_, r.ky), Bkz = sel3(Bx_, By_, Bz_, r.kz);
-    float Ckx = sel3(Cx_, Cy_, Cz_, r.kx), Cky = sel3(Cx_, Cy_, Cz_, r.ky), Ckz = sel3(Cx_, Cy_, Cz_, r.kz);
-    float Ax = __fmaf_rn(-r.sx, Akz, Akx), Ay = __fmaf_rn(-r.sy, Akz, Aky);
-    float Bx = __fmaf_rn(-r.sx, Bkz, Bkx), By = __fmaf_rn(-r.sy, Bkz, Bky);
-    float Cx = __fmaf_rn(-r.sx, Ckz, Ckx), Cy = __fmaf_rn(-r.sy, Ckz, Cky);
-    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
-    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
-    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
-    if (U == 0.f || V == 0.f || W == 0.f) {
-        U = (float)__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx));
-        V = (float)__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx));
-        W = (float)__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax));
-    }
-    if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return __int_as_float(0x7fffffff);
-    float det = __fadd_rn(__fadd_rn(U, V), W);
-    if (det == 0.f) return __int_as_float(0x7fffffff);
-    float Az = __fmul_rn(r.sz, Akz), Bz = __fmul_rn(r.sz, Bkz), Cz = __fmul_rn(r.sz, Ckz);
-    float T = __fmaf_rn(U, Az, __fmaf_rn(V, Bz, __fmul_rn(W, Cz)));
-    float rcp = __frcp_rn(det);
-    float t = __fmul_rn(T, rcp);
-    b1 = __fmul_rn(V, rcp);
-    b2 = __fmul_rn(W, rcp);
-    return t;
-}
-
-__device__ __forceinline__ float byte_to_float(uint32_t w, int k) {
-    return __uint_as_float(0x4B000000u | ((w >> (8 * k)) & 0xffu)) - 8388608.0f;
-}
-
 template <bool ANY, bool STATS>
 __global__ void __launch_bounds__(kTraceThreads)
 k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, TraceLaunch L,
@@ -483,10 +417,7 @@ k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, Trace
                     V3 o = f3(ro), d = f3(rd);
                     r = ray_pre(o, d, ro.w);
                     tmax = rd.w;
-                    float dx = fabsf(d.x) < 1e-20f ? copysignf(1e-20f, d.x) : d.x;
-                    float dy = fabsf(d.y) < 1e-20f ? copysignf(1e-20f, d.y) : d.y;
-                    float dz = fabsf(d.z) < 1e-20f ? copysignf(1e-20f, d.z) : d.z;
-                    inv = V3{1.f / dx, 1.f / dy, 1.f / dz};
+                    inv = box_inverse(d);
                     oct = (inv.x < 0.f ? 1 : 0) | (inv.y < 0.f ? 2 : 0) | (inv.z < 0.f ? 4 : 0);
                     ng = make_uint2(0u, (1u << oct) | (1u << 8));
                     tg = make_uint2(0u, 0u);
@@ -513,52 +444,7 @@ k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, Trace
                 else { atomicOr(L.err, (int)kErrStackOverflow); done = true; }
             }
             if (STATS) ++n_nodes;
-            const float4 *np = nodes + 5 * (size_t)child;
-            float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3),
-                   q4 = __ldg(np + 4);
-            uint32_t ew = __float_as_uint(q0.w);
-            float ex = __uint_as_float((ew & 0xffu) << 23);
-            float ey = __uint_as_float(((ew >> 8) & 0xffu) << 23);
-            float ez = __uint_as_float(((ew >> 16) & 0xffu) << 23);
-            float adx = ex * inv.x, ady = ey * inv.y, adz = ez * inv.z;
-            float orx = (q0.x - r.o.x) * inv.x, ory = (q0.y - r.o.y) * inv.y,
-                  orz = (q0.z - r.o.z) * inv.z;
-            uint32_t lox0 = __float_as_uint(q2.x), lox1 = __float_as_uint(q2.y);
-            uint32_t loy0 = __float_as_uint(q2.z), loy1 = __float_as_uint(q2.w);
-            uint32_t loz0 = __float_as_uint(q3.x), loz1 = __float_as_uint(q3.y);
-            uint32_t hix0 = __float_as_uint(q3.z), hix1 = __float_as_uint(q3.w);
-            uint32_t hiy0 = __float_as_uint(q4.x), hiy1 = __float_as_uint(q4.y);
-            uint32_t hiz0 = __float_as_uint(q4.z), hiz1 = __float_as_uint(q4.w);
-            uint32_t nx0 = (oct & 1) ? hix0 : lox0, nx1 = (oct & 1) ? hix1 : lox1;
-            uint32_t fx0 = (oct & 1) ? lox0 : hix0, fx1 = (oct & 1) ? lox1 : hix1;
-            uint32_t ny0 = (oct & 2) ? hiy0 : loy0, ny1 = (oct & 2) ? hiy1 : loy1;
-            uint32_t fy0 = (oct & 2) ? loy0 : hiy0, fy1 = (oct & 2) ? loy1 : hiy1;
-            uint32_t nz0 = (oct & 4) ? hiz0 : loz0, nz1 = (oct & 4) ? hiz1 : loz1;
-            uint32_t fz0 = (oct & 4) ? loz0 : hiz0, fz1 = (oct & 4) ? loz1 : hiz1;
-            uint32_t meta0 = __float_as_uint(q1.z), meta1 = __float_as_uint(q1.w);
-            const float tlimit = tmax + fabsf(tmax) * 5e-7f;
-            uint32_t nbits = 0, tbits = 0;
-#pragma unroll
-            for (int c = 0; c < 8; ++c) {
-                const int k = c & 3;
-                uint32_t m = ((c < 4 ? meta0 : meta1) >> (8 * k)) & 0xffu;
-                float tnx = fmaf(byte_to_float(c < 4 ? nx0 : nx1, k), adx, orx);
-                float tny = fmaf(byte_to_float(c < 4 ? ny0 : ny1, k), ady, ory);
-                float tnz = fmaf(byte_to_float(c < 4 ? nz0 : nz1, k), adz, orz);
-                float tfx = fmaf(byte_to_float(c < 4 ? fx0 : fx1, k), adx, orx);
-                float tfy = fmaf(byte_to_float(c < 4 ? fy0 : fy1, k), ady, ory);
-                float tfz = fmaf(byte_to_float(c < 4 ? fz0 : fz1, k), adz, orz);
-                float t0 = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
-                float t1 = fminf(fminf(tfx, tfy), fminf(tfz, tlimit));
-                bool hit = (m != 0u) && (t0 <= t1);
-                if (hit) {
-                    if (m & 0x80u) nbits |= 1u << (c ^ oct);
-                    else tbits |= ((1u << (m >> 5)) - 1u) << (m & 31u);
-                }
-            }
-            uint32_t cimask = ew >> 24;
-            ng = make_uint2(__float_as_uint(q1.x), nbits | (cimask << 8));
-            tg = make_uint2(__float_as_uint(q1.y), tbits);
+            visit_node(nodes, child, r, inv, oct, tmax, ng, tg);
         }
         while (tg.y && !done) {
             int b = __ffs(tg.y) - 1;
