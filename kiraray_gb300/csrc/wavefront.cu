@@ -20,6 +20,8 @@
 #include "internal.h"
 #include "shading.cuh"
 #include "wavefront.h"
+#include "accel_device.cuh"
+#include <cuda_fp16.h>
 
 using namespace krr;
 
@@ -302,6 +304,10 @@ __device__ LightSample sample_li(const DevScene &s, const DevLight &l, float u0,
     return ls;
 }
 
+}  // namespace
+#include "media.cuh"
+namespace {
+
 // ---------------------------------------------------------------- kernels
 // beginFrame, integrator.cpp:205-221
 __global__ void k_begin_frame(PixelState ps, int w, int64_t n, uint32_t sample_index) {
@@ -573,6 +579,257 @@ __global__ void k_shadow_resolve(Queue shadow, const uint8_t *__restrict__ occlu
         if (occluded[i]) continue;
         float4 c2 = shadow.at(2, i), c3 = shadow.at(3, i), c4 = shadow.at(4, i);
         add_radiance(ps, ubits(c2.w), f3(c2) / mean(f3(c4) + f3(c3)));
+    }
+}
+
+// sampleMediumInteraction, medium.cpp:13-103 (the medium has no emission).
+__global__ void k_medium_sample(DevScene s, Queue msq, Queue next, Queue miss, Queue hitl,
+                                Queue scat, Queue mscat, PixelState ps, int max_depth,
+                                uint32_t *err) {
+    int n = *msq.count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 c0 = msq.at(0, i), c1 = msq.at(1, i), c2 = msq.at(2, i), c3 = msq.at(3, i);
+        float4 c4 = msq.at(4, i), c5 = msq.at(5, i), c6 = msq.at(6, i), h = msq.at(7, i);
+        V3 o = f3(c0), dir = f3(c1);
+        V3 thp = f3(c4), pu = f3(c5), pl = f3(c6);
+        uint32_t depth = ubits(c4.w), pixel = ubits(c5.w);
+        int32_t medium = sbits(c2.w);
+        float time = c6.w;
+        float tmax_hit = h.x;
+        Pcg rng = load_rng(ps, pixel);
+        int ch = main_index(ps.L[pixel].w);
+        const DevMedium &m = s.media[medium];
+        bool scattered = false;
+        bool aborted;
+        V3 T_maj = sample_t_maj(m, o, dir, tmax_hit, rng, ch, err, aborted,
+            [&](V3 p, const MediumProps &mp, V3 sigma_maj, V3 Tm) -> bool {
+                float p_absorb = get(mp.sigma_a, ch) / get(sigma_maj, ch);
+                float p_scatter = get(mp.sigma_s, ch) / get(sigma_maj, ch);
+                float p_null = fmaxf(0.f, 1.f - p_absorb - p_scatter);
+                int mode = sample_discrete3(p_absorb, p_scatter, p_null, rng.get1d());
+                if (mode == 0) {
+                    thp = v3(0.f);
+                    return false;
+                }
+                if (mode == 1) {
+                    float pr = get(Tm, ch) * get(mp.sigma_s, ch);
+                    thp *= Tm * mp.sigma_s / pr;
+                    pu *= Tm * mp.sigma_s / pr;
+                    if (any(thp) && any(pu)) {
+                        int j = push_slot(mscat.count, mscat.cap, err);
+                        if (j >= 0) {
+                            mscat.at(0, j) = f4(p, ibits(medium));
+                            mscat.at(1, j) = f4(-dir, fbits(depth));
+                            mscat.at(2, j) = f4(thp, fbits(pixel));
+                            mscat.at(3, j) = f4(pu, time);
+                        }
+                    }
+                    scattered = true;
+                    return false;
+                }
+                V3 sigma_n = vmax(sigma_maj - mp.sigma_a - mp.sigma_s, v3(0.f));
+                float pr = get(Tm, ch) * get(sigma_n, ch);
+                thp *= Tm * sigma_n / pr;
+                if (pr == 0) thp = v3(0.f);
+                pu *= Tm * sigma_n / pr;
+                pl *= Tm * sigma_maj / pr;
+                return any(thp) && any(pu);
+            });
+        if (aborted) thp = v3(0.f);
+        store_rng(ps, pixel, rng);
+        if (!scattered && any(thp)) {
+            V3 r = T_maj / get(T_maj, ch);
+            thp *= r;
+            pu *= r;
+            pl *= r;
+        }
+        if (scattered || !any(thp) || !any(pu) || (int)depth == max_depth) continue;
+        if (isinf(tmax_hit)) {
+            int j = push_slot(miss.count, miss.cap, err);
+            if (j >= 0) {
+                miss.at(0, j) = c0; miss.at(1, j) = c1; miss.at(2, j) = c2; miss.at(3, j) = c3;
+                miss.at(4, j) = f4(thp, c4.w); miss.at(5, j) = f4(pu, c5.w); miss.at(6, j) = f4(pl, c6.w);
+            }
+            continue;
+        }
+        uint32_t gid = ubits(h.w);
+        Surf sf = prepare_surface(s, h.y, h.z, gid, dir);
+        if (sf.material < 0) {
+            int j = push_slot(next.count, next.cap, err);
+            if (j >= 0) {
+                V3 no = offset_ray_origin(sf.p, sf.n, dir);
+                int32_t med = medium_towards(sf.interface_in, sf.interface_out, medium, sf.n, dir);
+                next.at(0, j) = f4(no, 0.f);
+                next.at(1, j) = f4(dir, INFINITY);
+                next.at(2, j) = make_float4(c2.x, c2.y, c2.z, ibits(med));
+                next.at(3, j) = c3;
+                next.at(4, j) = f4(thp, c4.w);
+                next.at(5, j) = f4(pu, c5.w);
+                next.at(6, j) = f4(pl, c6.w);
+            }
+            continue;
+        }
+        if (sf.light >= 0) {
+            int j = push_slot(hitl.count, hitl.cap, err);
+            if (j >= 0) {
+                hitl.at(0, j) = f4(sf.p, ibits(sf.light));
+                hitl.at(1, j) = f4(sf.n, sf.u);
+                hitl.at(2, j) = f4(sf.wo, sf.v);
+                hitl.at(3, j) = make_float4(c2.x, c2.y, c2.z, c3.w);
+                hitl.at(4, j) = make_float4(c3.x, c3.y, c3.z, c4.w);
+                hitl.at(5, j) = f4(thp, c5.w);
+                hitl.at(6, j) = f4(pu, c5.w);
+                hitl.at(7, j) = f4(pl, c6.w);
+            }
+        }
+        int j = push_slot(scat.count, scat.cap, err);
+        if (j >= 0) {
+            scat.at(0, j) = f4(sf.p, ibits(sf.material));
+            scat.at(1, j) = f4(sf.wo, c4.w);
+            scat.at(2, j) = f4(sf.n, c5.w);
+            scat.at(3, j) = f4(sf.t, ibits(sf.mesh));
+            scat.at(4, j) = f4(sf.b, sf.u);
+            scat.at(5, j) = f4(thp, sf.v);
+            scat.at(6, j) = f4(pu, time);
+            scat.at(7, j) = make_float4(ibits(medium), 0.f, 0.f, 0.f);
+        }
+    }
+}
+
+// sampleMediumScattering, medium.cpp:105-153
+__global__ void k_medium_scatter(DevScene s, Queue mscat, Queue next, Queue shadow, PixelState ps,
+                                 int nee, uint32_t *err) {
+    int n = *mscat.count;
+    float sel_pdf = 1.f / (float)s.n_lights;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 c0 = mscat.at(0, i), c1 = mscat.at(1, i), c2 = mscat.at(2, i), c3 = mscat.at(3, i);
+        V3 p = f3(c0), wo = f3(c1), wthp = f3(c2), wpu = f3(c3);
+        int32_t medium = sbits(c0.w);
+        uint32_t depth = ubits(c1.w), pixel = ubits(c2.w);
+        float time = c3.w;
+        float g = s.media[medium].g;
+        Pcg rng = load_rng(ps, pixel);
+        if (nee) {
+            float ul = rng.get1d();
+            uint32_t lid = (uint32_t)(ul * (float)s.n_lights);
+            float u0 = rng.get1d(), u1 = rng.get1d();
+            LightSample ls = sample_li(s, s.lights[lid], u0, u1, p);
+            V3 to = offset_ray_origin(ls.p, ls.n, p - ls.p);
+            V3 d = to - p;
+            V3 wi = normalize(d);
+            V3 thp = wthp * hg_p(g, wo, wi);
+            float light_pdf = sel_pdf * ls.pdf;
+            float phase_pdf = hg_p(g, wo, wi);
+            V3 Ld = thp * ls.L;
+            if (any(Ld) && light_pdf > 0) {
+                int j = push_slot(shadow.count, shadow.cap, err);
+                if (j >= 0) {
+                    shadow.at(0, j) = f4(p, 0.f);
+                    shadow.at(1, j) = f4(d, 1.f);
+                    shadow.at(2, j) = f4(Ld, fbits(pixel));
+                    shadow.at(3, j) = f4(wpu * phase_pdf, ibits(medium));
+                    shadow.at(4, j) = f4(wpu * light_pdf, time);
+                }
+            }
+        }
+        float u0 = rng.get1d(), u1 = rng.get1d();
+        float pdf;
+        V3 wi = hg_sample(g, wo, u0, u1, pdf);
+        float pp = pdf;   // PhaseFunctionSample{wi, p, pdf} with p == pdf
+        V3 thp = wthp * pp / pdf;
+        float rr = max_coeff(thp / mean(wpu));
+        bool killed = false;
+        if (depth >= 1 && rr < 1) {
+            if (rng.get1d() >= rr) killed = true;
+            else thp /= rr;
+        }
+        store_rng(ps, pixel, rng);
+        if (killed) continue;
+        bool has_nan = isnan(thp.x) || isnan(thp.y) || isnan(thp.z);
+        if (!is_zero(thp) && !has_nan) {
+            int j = push_slot(next.count, next.cap, err);
+            if (j >= 0) {
+                next.at(0, j) = f4(p, 0.f);
+                next.at(1, j) = f4(wi, INFINITY);
+                next.at(2, j) = f4(p, ibits(medium));
+                next.at(3, j) = make_float4(0.f, 0.f, 0.f, fbits(BSDF_SMOOTH));
+                next.at(4, j) = f4(thp, fbits(depth + 1));
+                next.at(5, j) = f4(wpu, fbits(pixel));
+                next.at(6, j) = f4(wpu / pdf, time);
+            }
+        }
+    }
+}
+
+// traceTransmittance (wavefront.h:80-139) for every shadow ray when media
+// are enabled: closest hits through null-material interfaces with ratio
+// tracking inside media.
+__global__ void k_shadow_tr(DevScene s, const float4 *__restrict__ nodes,
+                            const float4 *__restrict__ tris, Queue shadow, PixelState ps,
+                            uint32_t *err, int *trace_err) {
+    int n = *shadow.count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 c0 = shadow.at(0, i), c1 = shadow.at(1, i), c2 = shadow.at(2, i), c3 = shadow.at(3, i),
+               c4 = shadow.at(4, i);
+        V3 o = f3(c0), d = f3(c1);
+        float tmax = c1.w;
+        uint32_t pixel = ubits(c2.w);
+        int32_t medium = sbits(c3.w);
+        V3 p_light = o + d * tmax;
+        Pcg rng = load_rng(ps, pixel);
+        int ch = main_index(ps.L[pixel].w);
+        V3 T_ray = v3(1.f), pu = v3(1.f), pl = v3(1.f);
+        int crossings = 0;
+        while (fabsf(d.x) > kRayEps * 2 || fabsf(d.y) > kRayEps * 2 || fabsf(d.z) > kRayEps * 2) {
+            float4 h = traverse_ray<false>(nodes, tris, o, d, 0.f, tmax, trace_err);
+            bool visible = ubits(h.w) == KRR_MISS;
+            Surf sf;
+            if (!visible) {
+                sf = prepare_surface(s, h.y, h.z, ubits(h.w), d);
+                if (sf.material >= 0) {
+                    T_ray = v3(0.f);
+                    break;
+                }
+            }
+            if (medium >= 0) {
+                float t_end = visible ? tmax : length(sf.p - o) / length(d);
+                bool aborted;
+                V3 T_maj = sample_t_maj(s.media[medium], o, d, t_end, rng, ch, err, aborted,
+                    [&](V3, const MediumProps &mp, V3 sigma_maj, V3 Tm) -> bool {
+                        V3 sigma_n = vmax(sigma_maj - mp.sigma_a - mp.sigma_s, v3(0.f));
+                        float pr = get(Tm, ch) * get(sigma_maj, ch);
+                        T_ray *= Tm * sigma_n / pr;
+                        pl *= Tm * sigma_maj / pr;
+                        pu *= Tm * sigma_n / pr;
+                        V3 Tr = T_ray / mean(pu + pl);
+                        if (max_coeff(Tr) < 0.05f) {
+                            if (rng.get1d() < 0.75f) T_ray = v3(0.f);
+                            else T_ray /= 0.25f;
+                        }
+                        return any(T_ray);
+                    });
+                if (aborted) T_ray = v3(0.f);
+                V3 r = T_maj / get(T_maj, ch);
+                T_ray *= r;
+                pu *= r;
+                pl *= r;
+            }
+            if (visible || is_zero(T_ray)) break;
+            // Interaction::spawnRayTo(pLight) from the null surface
+            V3 po = offset_ray_origin(sf.p, sf.n, p_light - sf.p);
+            V3 nd = p_light - po;
+            medium = medium_towards(sf.interface_in, sf.interface_out, medium, sf.n, nd);
+            o = po;
+            d = nd;
+            if (++crossings > kMaxInterfaceCrossings) {
+                atomicOr(err, (uint32_t)kErrLoopLimit);
+                T_ray = v3(0.f);
+                break;
+            }
+        }
+        store_rng(ps, pixel, rng);
+        if (any(T_ray))
+            add_radiance(ps, pixel, f3(c2) * T_ray / mean(f3(c3) * pu + f3(c4) * pl));
     }
 }
 
@@ -912,6 +1169,13 @@ extern "C" int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *sd, void *stre
             uint16_t *g = nullptr;
             KRR_TRY(dev_upload(wf, &g, m.h_density, (size_t)m.nx * m.ny * m.nz));
             d.density = g;
+            float *maj = nullptr;
+            size_t nm = (size_t)d.mres[0] * d.mres[1] * d.mres[2];
+            KRR_CUDA(cudaMalloc(&maj, nm * sizeof(float)));
+            wf->scene_allocs.push_back(maj);
+            k_build_majorant<<<grid_for((int64_t)nm), kThreads, 0, st>>>(d, maj);
+            KRR_CUDA(cudaGetLastError());
+            d.majorant = maj;
         }
         media[i] = d;
     }
@@ -1161,16 +1425,28 @@ extern "C" int krr_wf_accel(krr_wf *wf, const krr_accel **out) {
     return KRR_OK;
 }
 
-// Medium stages are added with the medium kernels; until then a scene with
-// media renders without them only when enable_medium is off.
 namespace krr {
-int launch_medium_sample(krr_wf *, int, cudaStream_t) {
-    return fail(KRR_ERR_NOT_READY, "participating media are not built in this library");
+int launch_medium_sample(krr_wf *wf, int depth, cudaStream_t st) {
+    k_medium_sample<<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->q(Q_MEDIUM_SAMPLE),
+                                                    wf->q((depth & 1) ^ 1), wf->q(Q_MISS),
+                                                    wf->q(Q_HIT_LIGHT), wf->q(Q_SCATTER),
+                                                    wf->q(Q_MEDIUM_SCATTER), wf->ps,
+                                                    wf->params.max_depth, wf->err());
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
 }
-int launch_medium_scatter(krr_wf *, int, cudaStream_t) {
-    return fail(KRR_ERR_NOT_READY, "participating media are not built in this library");
+int launch_medium_scatter(krr_wf *wf, int depth, cudaStream_t st) {
+    k_medium_scatter<<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->q(Q_MEDIUM_SCATTER),
+                                                     wf->q((depth & 1) ^ 1), wf->q(Q_SHADOW), wf->ps,
+                                                     wf->params.nee, wf->err());
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
 }
-int launch_trace_shadow_tr(krr_wf *, cudaStream_t) {
-    return fail(KRR_ERR_NOT_READY, "participating media are not built in this library");
+int launch_trace_shadow_tr(krr_wf *wf, cudaStream_t st) {
+    k_shadow_tr<<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris,
+                                                wf->q(Q_SHADOW), wf->ps, wf->err(),
+                                                wf->accel.d_scratch + 4);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
 }
 }  // namespace krr

@@ -65,6 +65,9 @@ int oracle_pt_render(const oracle_pt *pt, const struct krr_wf_params *params,
                      int64_t frame_index, int64_t px_begin, int64_t px_end, float *out_L,
                      float *out_pixel, int threads);
 
+double oracle_medium_transmittance(const oracle_pt *pt, const float *o, const float *d, float tmax,
+                                   int n, uint32_t seed);
+
 #ifdef __cplusplus
 }
 #endif
