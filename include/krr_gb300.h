@@ -39,7 +39,8 @@ int krr_version(void);
 /* ------------------------------------------------------------ ray records */
 /* One ray, 32 bytes: origin.xyz + tmin, direction.xyz + tmax.  The
  * direction need not be normalised (the reference's shadow rays are not:
- * src/core/raytracing.h:151-160). */
+ * src/core/raytracing.h:151-160).  tmin below zero acts as zero (OptiX also
+ * requires tmin >= 0). */
 typedef struct krr_ray {
     float ox, oy, oz, tmin;
     float dx, dy, dz, tmax;

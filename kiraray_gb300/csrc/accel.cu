@@ -326,10 +326,10 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
         }
         uint32_t m;
         if (ccount[c] > 3) {
-            m = 0x80u;
+            m = 0x20u | (24u + (uint32_t)s);
             imask |= 1u << s;
         } else {
-            m = ((uint32_t)ccount[c] << 5) | (uint32_t)tri_off;
+            m = (((1u << ccount[c]) - 1u) << 5) | (uint32_t)tri_off;
             for (int k = 0; k < ccount[c]; ++k)
                 leaf_order[tri_base + tri_off + k] = t.sorted_idx[cfirst[c] + k];
             tri_off += ccount[c];

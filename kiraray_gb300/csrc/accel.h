@@ -7,8 +7,12 @@
 //   q2: qlo_x[0..7] | qlo_y[0..7]      (8-bit quantised child bounds)
 //   q3: qlo_z[0..7] | qhi_x[0..7]
 //   q4: qhi_y[0..7] | qhi_z[0..7]
-// meta byte per child slot: 0 = empty, 0x80 = internal node, otherwise a leaf
-// with (count << 5) | first_triangle_offset (count 1..3, offset 0..23).
+// meta byte per child slot: 0 = empty; otherwise (unary count << 5) | bit,
+// where an internal child in slot s has count 1 and bit 24 + s, and a leaf
+// has count 1..3 (unary 001/011/111) and bit = its first triangle's offset
+// (0..23).  A hit child contributes (m >> 5) << (m & 31) to a 32-bit hit mask:
+// triangles in bits 0..23, internal children in bits 24..31 (the traversal
+// XORs the slot of internal children with the ray octant).
 // Internal children are stored contiguously from child_base in slot order;
 // the leaf triangles of all children contiguously from tri_base.
 // Slot s holds the child that is nearest for rays whose direction octant is

@@ -18,7 +18,8 @@ struct RayPre {
 
 __device__ __forceinline__ RayPre ray_pre(V3 o, V3 d, float tmin) {
     RayPre r;
-    r.o = o; r.d = d; r.tmin = tmin;
+    r.o = o; r.d = d;
+    r.tmin = tmin > 0.f ? tmin : 0.f;   // negative (and -0) tmin act as +0
     float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
     int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
     int kx = kz + 1 == 3 ? 0 : kz + 1;
@@ -76,8 +77,18 @@ __device__ __forceinline__ float byte_to_float(uint32_t w, int k) {
 }
 
 
+// 8-bit quantised plane k of a packed word as a float (exact): one byte
+// permute into 0x4B0000xx (2^23 + q) and one subtraction.
+__device__ __forceinline__ float plane(uint32_t w, int k) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u + (uint32_t)k)) - 8388608.0f;
+}
+
 // Visits one 8-wide node: returns the next node group (child base, hit
 // positions | internal mask << 8) and the triangle group (base, bits).
+// Entry/exit distances are compared as integers: with tmin >= +0 the
+// maximum of the entry distances is a non-negative float, and the ordering
+// of non-negative floats is the ordering of their bit patterns; a negative
+// exit distance is a negative integer and fails the test, as it should.
 __device__ __forceinline__ void visit_node(const float4 *__restrict__ nodes, uint32_t child,
                                            const RayPre &r, V3 inv, int oct, float tmax,
                                            uint2 &ng, uint2 &tg) {
@@ -102,30 +113,31 @@ __device__ __forceinline__ void visit_node(const float4 *__restrict__ nodes, uin
     uint32_t fy0 = (oct & 2) ? loy0 : hiy0, fy1 = (oct & 2) ? loy1 : hiy1;
     uint32_t nz0 = (oct & 4) ? hiz0 : loz0, nz1 = (oct & 4) ? hiz1 : loz1;
     uint32_t fz0 = (oct & 4) ? loz0 : hiz0, fz1 = (oct & 4) ? loz1 : hiz1;
+    // internal children: XOR the ray octant into their bit index (24 + slot)
     uint32_t meta0 = __float_as_uint(q1.z), meta1 = __float_as_uint(q1.w);
+    meta0 ^= ((meta0 & (meta0 << 1) & 0x10101010u) >> 4) * (uint32_t)oct;
+    meta1 ^= ((meta1 & (meta1 << 1) & 0x10101010u) >> 4) * (uint32_t)oct;
     const float tlimit = tmax + fabsf(tmax) * 5e-7f;
-    uint32_t nbits = 0, tbits = 0;
+    const int tmin_i = __float_as_int(r.tmin), tlim_i = __float_as_int(tlimit);
+    uint32_t hitmask = 0;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         const int k = c & 3;
-        uint32_t m = ((c < 4 ? meta0 : meta1) >> (8 * k)) & 0xffu;
-        float tnx = fmaf(byte_to_float(c < 4 ? nx0 : nx1, k), adx, orx);
-        float tny = fmaf(byte_to_float(c < 4 ? ny0 : ny1, k), ady, ory);
-        float tnz = fmaf(byte_to_float(c < 4 ? nz0 : nz1, k), adz, orz);
-        float tfx = fmaf(byte_to_float(c < 4 ? fx0 : fx1, k), adx, orx);
-        float tfy = fmaf(byte_to_float(c < 4 ? fy0 : fy1, k), ady, ory);
-        float tfz = fmaf(byte_to_float(c < 4 ? fz0 : fz1, k), adz, orz);
-        float t0 = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
-        float t1 = fminf(fminf(tfx, tfy), fminf(tfz, tlimit));
-        bool hit = (m != 0u) && (t0 <= t1);
-        if (hit) {
-            if (m & 0x80u) nbits |= 1u << (c ^ oct);
-            else tbits |= ((1u << (m >> 5)) - 1u) << (m & 31u);
-        }
+        uint32_t m = __byte_perm(c < 4 ? meta0 : meta1, 0u, 0x4440u + (uint32_t)k);
+        int tnx = __float_as_int(fmaf(plane(c < 4 ? nx0 : nx1, k), adx, orx));
+        int tny = __float_as_int(fmaf(plane(c < 4 ? ny0 : ny1, k), ady, ory));
+        int tnz = __float_as_int(fmaf(plane(c < 4 ? nz0 : nz1, k), adz, orz));
+        int tfx = __float_as_int(fmaf(plane(c < 4 ? fx0 : fx1, k), adx, orx));
+        int tfy = __float_as_int(fmaf(plane(c < 4 ? fy0 : fy1, k), ady, ory));
+        int tfz = __float_as_int(fmaf(plane(c < 4 ? fz0 : fz1, k), adz, orz));
+        int t0 = __vimax3_s32(tnx, tny, max(tnz, tmin_i));
+        int t1 = __vimin3_s32(tfx, tfy, min(tfz, tlim_i));
+        uint32_t bits = (m >> 5) << (m & 31u);
+        hitmask |= (t0 <= t1) ? bits : 0u;
     }
     uint32_t cimask = ew >> 24;
-    ng = make_uint2(__float_as_uint(q1.x), nbits | (cimask << 8));
-    tg = make_uint2(__float_as_uint(q1.y), tbits);
+    ng = make_uint2(__float_as_uint(q1.x), (hitmask >> 24) | (cimask << 8));
+    tg = make_uint2(__float_as_uint(q1.y), hitmask & 0x00ffffffu);
 }
 
 __device__ __forceinline__ V3 box_inverse(V3 d) {

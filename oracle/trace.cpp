@@ -31,7 +31,7 @@ struct RayPre {
 RayPre make_ray(const float *r) {
     RayPre p;
     for (int k = 0; k < 3; ++k) { p.o[k] = r[k]; p.d[k] = r[4 + k]; }
-    p.tmin = r[3];
+    p.tmin = r[3] > 0.f ? r[3] : 0.f;   // negative (and -0) tmin act as +0
     p.tmax = r[7];
     float ax = std::fabs(p.d[0]), ay = std::fabs(p.d[1]), az = std::fabs(p.d[2]);
     int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
