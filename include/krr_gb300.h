@@ -273,6 +273,73 @@ int krr_wf_device_errors(krr_wf *wf, uint32_t *out_flags, void *stream);
 /* The BVH of the current scene (owned by the pass). */
 int krr_wf_accel(krr_wf *wf, const krr_accel **out);
 
+/* ------------------------------------------------- neural radiance cache */
+/* Online-trained radiance cache (no counterpart in the reference; it plugs
+ * into the pass the way PPGPathTracer records per-vertex radiance,
+ * src/misc/render/ppg/guideditem.h:119-166).  Query/training records are
+ * float[10]: position (world), shading normal, roughness, albedo. */
+typedef struct krr_nrc krr_nrc;
+
+typedef struct krr_nrc_config {
+    int32_t n_levels;            /* hash-grid levels (16)                    */
+    int32_t features_per_level;  /* 2                                        */
+    int32_t log2_table_size;     /* entries per hashed level, log2 (19)      */
+    int32_t base_resolution;     /* 16                                       */
+    int32_t max_resolution;      /* 2048                                     */
+    int32_t hidden_layers;       /* width-64 ReLU layers (5)                 */
+    float learning_rate;         /* Adam (1e-2)                              */
+    float beta1, beta2, epsilon; /* 0.9, 0.99, 1e-15                         */
+    float loss_scale;            /* backward-pass loss scale (128)           */
+    int32_t batch_size;          /* training records per frame (65536)       */
+    int32_t train_pixel_stride;  /* 1 of this many pixels trains (16)        */
+    uint32_t seed;
+    float scene_lo[3], scene_hi[3];   /* box mapped to the unit cube         */
+} krr_nrc_config;
+
+typedef struct krr_nrc_info_t {
+    int64_t n_params_mlp;
+    int64_t n_table_entries;
+    int32_t n_levels;
+    int32_t resolution[16];
+    uint32_t level_offset[16];
+    uint32_t level_size[16];
+    int64_t step;
+} krr_nrc_info_t;
+
+void krr_nrc_config_default(krr_nrc_config *config);
+int krr_nrc_create(const krr_nrc_config *config, krr_nrc **out);
+int krr_nrc_destroy(krr_nrc *nrc);
+int krr_nrc_info(const krr_nrc *nrc, krr_nrc_info_t *info);
+/* d_out[3*i..] = predicted RGB radiance of record i. */
+int krr_nrc_query(krr_nrc *nrc, const float *d_inputs, int64_t count, float *d_out, void *stream);
+/* One Adam step on (inputs, RGB targets); h_loss (optional) gets the loss. */
+int krr_nrc_train_step(krr_nrc *nrc, const float *d_inputs, const float *d_targets, int64_t count,
+                       float *h_loss, void *stream);
+/* Gradients of the loss for one batch without updating (host arrays sized
+ * as krr_nrc_get_params); synchronises the device. */
+int krr_nrc_gradients(krr_nrc *nrc, const float *d_inputs, const float *d_targets, int64_t count,
+                      float *h_grad_mlp, float *h_grad_table, float *h_loss);
+/* which: 0 = MLP weights [layer][out rows][64], 1 = hash table [entry][2]. */
+int krr_nrc_get_params(const krr_nrc *nrc, int32_t which, float *h_dst, int64_t count);
+int krr_nrc_set_params(krr_nrc *nrc, int32_t which, const float *h_src, int64_t count);
+/* Attaches a cache to the pass (NULL detaches: the plain tracer).  With a
+ * cache, paths of 1 in train_pixel_stride pixels run unbiased and record
+ * training targets; the others stop at the vertex after their first
+ * non-specular bounce and add throughput x cache(vertex). */
+int krr_wf_set_nrc(krr_wf *wf, krr_nrc *nrc, int32_t train);
+
+/* ------------------------------------------------ accumulation and error */
+/* d_accum (double RGB per pixel) += d_rgba.rgb (float4 per pixel): the
+ * reference's AccumulatePass in "double" precision
+ * (src/render/passes/accumulate/accumulate.cu:30-79). */
+int krr_accumulate_f64(const float *d_rgba, double *d_accum, int64_t n_pixels, void *stream);
+/* Error of the image scale * d_accum against d_ref_rgba (float4 per pixel):
+ * metric 0 = relMSE, 1 = MSE, per pixel clamped at 100 and averaged, as the
+ * reference's ErrorMeasurePass (src/render/passes/errormeasure/metrics.cu:
+ * 64-128), reduced in FP64.  Synchronises the stream. */
+int krr_image_error(const double *d_accum, double scale, const float *d_ref_rgba,
+                    int64_t n_pixels, int32_t metric, double *h_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -71,6 +71,23 @@ class AccelStats(C.Structure):
                 ("triangle_bytes", C.c_double)]
 
 
+class NrcConfig(C.Structure):
+    _fields_ = [("n_levels", C.c_int32), ("features_per_level", C.c_int32),
+                ("log2_table_size", C.c_int32), ("base_resolution", C.c_int32),
+                ("max_resolution", C.c_int32), ("hidden_layers", C.c_int32),
+                ("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float),
+                ("epsilon", C.c_float), ("loss_scale", C.c_float), ("batch_size", C.c_int32),
+                ("train_pixel_stride", C.c_int32), ("seed", C.c_uint32),
+                ("scene_lo", C.c_float * 3), ("scene_hi", C.c_float * 3)]
+
+
+class NrcInfo(C.Structure):
+    _fields_ = [("n_params_mlp", C.c_int64), ("n_table_entries", C.c_int64),
+                ("n_levels", C.c_int32), ("resolution", C.c_int32 * 16),
+                ("level_offset", C.c_uint32 * 16), ("level_size", C.c_uint32 * 16),
+                ("step", C.c_int64)]
+
+
 class WfParams(C.Structure):
     _fields_ = [("nee", C.c_int32), ("enable_medium", C.c_int32), ("max_depth", C.c_int32),
                 ("rr", C.c_float), ("enable_clamp", C.c_int32), ("clamp_max", C.c_float),
@@ -118,6 +135,19 @@ SIGNATURES = {
                               C.POINTER(C.c_int32)]),
     "krr_wf_device_errors": (_I, [_P, C.POINTER(C.c_uint32), _P]),
     "krr_wf_accel": (_I, [_P, C.POINTER(_P)]),
+    "krr_accumulate_f64": (_I, [_P, _P, C.c_int64, _P]),
+    "krr_nrc_config_default": (None, [C.POINTER(NrcConfig)]),
+    "krr_nrc_create": (_I, [C.POINTER(NrcConfig), C.POINTER(_P)]),
+    "krr_nrc_destroy": (_I, [_P]),
+    "krr_nrc_info": (_I, [_P, C.POINTER(NrcInfo)]),
+    "krr_nrc_query": (_I, [_P, _P, C.c_int64, _P, _P]),
+    "krr_nrc_train_step": (_I, [_P, _P, _P, C.c_int64, C.POINTER(C.c_float), _P]),
+    "krr_nrc_gradients": (_I, [_P, _P, _P, C.c_int64, _P, _P, C.POINTER(C.c_float)]),
+    "krr_nrc_get_params": (_I, [_P, C.c_int32, _P, C.c_int64]),
+    "krr_nrc_set_params": (_I, [_P, C.c_int32, _P, C.c_int64]),
+    "krr_wf_set_nrc": (_I, [_P, _P, C.c_int32]),
+    "krr_image_error": (_I, [_P, C.c_double, _P, C.c_int64, C.c_int32, C.POINTER(C.c_double),
+                             _P]),
 }
 
 _lib: C.CDLL | None = None

@@ -1,0 +1,96 @@
+"""Convergence measurement: FP64 accumulation and relMSE against a reference
+image, in the manner of the reference's AccumulatePass ("double" precision,
+src/render/passes/accumulate/accumulate.cu:30-79) and ErrorMeasurePass
+(src/render/passes/errormeasure/errormeasure.cpp:17-57, metrics.cu:64-128),
+which logs a curve {timesteps, timepoints, data}.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import torch
+
+from . import _lib
+from ._lib import check
+
+RELMSE, MSE = 0, 1
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+class Accumulator:
+    """FP64 running sum of float4 RGBA frames (device resident)."""
+
+    def __init__(self, width: int, height: int):
+        self.n = width * height
+        self.sum = torch.zeros((self.n, 3), dtype=torch.float64, device="cuda")
+        self.frames = 0
+
+    def add(self, rgba: torch.Tensor):
+        check(_lib.load().krr_accumulate_f64(rgba.data_ptr(), self.sum.data_ptr(), self.n,
+                                             _stream()), "krr_accumulate_f64")
+        self.frames += 1
+
+    def image(self) -> torch.Tensor:
+        """float32 [n, 4] mean image."""
+        out = torch.ones((self.n, 4), dtype=torch.float32, device="cuda")
+        out[:, :3] = (self.sum / max(self.frames, 1)).float()
+        return out
+
+    def error(self, ref_rgba: torch.Tensor, metric: int = RELMSE) -> float:
+        v = C.c_double()
+        check(_lib.load().krr_image_error(self.sum.data_ptr(), 1.0 / max(self.frames, 1),
+                                          ref_rgba.data_ptr(), self.n, metric, C.byref(v),
+                                          _stream()), "krr_image_error")
+        return v.value
+
+
+def render_reference(pt, scene, frames: int, first_frame: int = 1_000_000) -> torch.Tensor:
+    """Mean of `frames` 1-spp frames accumulated in FP64 (float32 [n, 4])."""
+    acc = Accumulator(scene.width, scene.height)
+    out = torch.empty((scene.height, scene.width, 4), dtype=torch.float32, device="cuda")
+    for f in range(frames):
+        pt.begin_frame(first_frame + f, scene.camera)
+        pt.render(out)
+        acc.add(out)
+    return acc.image()
+
+
+def time_to_error(pt, scene, ref_rgba: torch.Tensor, target: float = 0.01, max_frames: int = 4096,
+                  check_every: int = 4, metric: int = RELMSE, on_frame=None) -> dict:
+    """Renders 1-spp frames until the running mean reaches `target` error.
+
+    Only the device time of rendering (and of on_frame, e.g. cache training)
+    counts; error evaluation is excluded.  Returns the curve
+    {timesteps, timepoints, data} and the time at which the target was met
+    (None if it was not within max_frames)."""
+    acc = Accumulator(scene.width, scene.height)
+    out = torch.empty((scene.height, scene.width, 4), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    t_ms = 0.0
+    curve = {"timesteps": [], "timepoints": [], "data": []}
+    reached = None
+    for f in range(1, max_frames + 1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        pt.begin_frame(f, scene.camera)
+        pt.render(out)
+        if on_frame is not None:
+            on_frame(f, out)
+        acc.add(out)
+        e1.record(stream)
+        e1.synchronize()
+        t_ms += e0.elapsed_time(e1)
+        if f % check_every == 0 or f == max_frames:
+            err = acc.error(ref_rgba, metric)
+            curve["timesteps"].append(f)
+            curve["timepoints"].append(t_ms / 1e3)
+            curve["data"].append(err)
+            if err <= target:
+                reached = t_ms / 1e3
+                break
+    return {"seconds": reached, "frames": acc.frames, "curve": curve,
+            "final_error": curve["data"][-1] if curve["data"] else None}

@@ -1,0 +1,677 @@
+// Neural radiance cache (no counterpart in the reference; its learned-method
+// hook is PPG's per-vertex radiance records, src/misc/render/ppg/
+// guideditem.h:119-166).
+//
+// Encoding: multiresolution hash grid (16 levels x 2 features, 2^19 entries
+// per hashed level, resolutions 16..2048 in a geometric series; coarse
+// levels that fit are indexed densely), trilinear interpolation, features
+// stored in BF16.  Inputs of the MLP: the 32 grid features, the normal
+// mapped to [0,1], roughness and albedo, zero-padded to 64.  MLP: 5 hidden
+// layers of width 64 with ReLU and a linear RGB output.  Activations and
+// weights are rounded to BF16 at every layer input, products accumulate in
+// FP32.  Loss: relative L2, (y - t)^2 / (sg(y)^2 + 0.01), scaled by a
+// constant loss scale during the backward pass.  Optimiser: Adam on FP32
+// master copies of the weights and of the hash table.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "nrc.h"
+
+using namespace krr;
+
+struct krr_nrc {
+    krr_nrc_config cfg{};
+    NrcGrid grid{};
+    NrcMlp mlp{};
+    uint32_t n_entries = 0;                  // total table entries
+    // parameters: FP32 master, BF16 copy, Adam moments, gradient
+    float *table_master = nullptr, *table_m = nullptr, *table_v = nullptr, *table_grad = nullptr;
+    __nv_bfloat16 *table = nullptr;
+    float *w_master = nullptr, *w_m = nullptr, *w_v = nullptr, *w_grad = nullptr;
+    __nv_bfloat16 *weights = nullptr;
+    int64_t step = 0;
+    // activation buffers: [layers][cap][64] bf16, gradients float
+    int64_t cap = 0;
+    __nv_bfloat16 *act = nullptr;
+    float *out = nullptr;                    // [cap][16]
+    float *dA = nullptr, *dB = nullptr;      // [cap][64]
+    float *loss = nullptr;                   // device loss accumulator
+    int32_t *count_buf = nullptr;
+};
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ float bf(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+// Level-l grid index of integer corner (x, y, z).
+__device__ __forceinline__ uint32_t grid_index(const NrcGrid &g, int l, uint32_t x, uint32_t y,
+                                               uint32_t z) {
+    uint32_t n1 = (uint32_t)g.res[l] + 1u;
+    if (g.dense_mask & (1u << l)) return x + n1 * (y + n1 * z);
+    return (x ^ (y * 2654435761u) ^ (z * 805459861u)) & (g.table_size - 1u);
+}
+
+struct Corner {
+    uint32_t idx[8];
+    float w[8];
+};
+
+__device__ __forceinline__ void corners(const NrcGrid &g, int l, const float p[3], Corner &c) {
+    float fr[3];
+    uint32_t base[3];
+    for (int a = 0; a < 3; ++a) {
+        float s = p[a] * (float)g.res[l];
+        float fl = floorf(s);
+        fl = fminf(fmaxf(fl, 0.f), (float)(g.res[l] - 1));
+        base[a] = (uint32_t)fl;
+        fr[a] = fminf(fmaxf(s - fl, 0.f), 1.f);
+    }
+    for (int k = 0; k < 8; ++k) {
+        uint32_t x = base[0] + (k & 1), y = base[1] + ((k >> 1) & 1), z = base[2] + ((k >> 2) & 1);
+        c.idx[k] = g.offset[l] + grid_index(g, l, x, y, z);
+        c.w[k] = ((k & 1) ? fr[0] : 1.f - fr[0]) * (((k >> 1) & 1) ? fr[1] : 1.f - fr[1]) *
+                 (((k >> 2) & 1) ? fr[2] : 1.f - fr[2]);
+    }
+}
+
+__device__ __forceinline__ void normalise_position(const NrcGrid &g, const float *in, float p[3]) {
+    for (int a = 0; a < 3; ++a) p[a] = fminf(fmaxf((in[a] - g.lo[a]) * g.inv_extent[a], 0.f), 1.f);
+}
+
+__device__ __forceinline__ int64_t live_count(const int32_t *d_count, int64_t cap) {
+    return d_count ? min((int64_t)*d_count, cap) : cap;
+}
+
+// Encoded MLP input (bf16 values) for each query.
+__global__ void k_encode(NrcGrid g, const float *__restrict__ in, const int32_t *d_count,
+                         int64_t cap, const __nv_bfloat16 *__restrict__ table,
+                         __nv_bfloat16 *__restrict__ X) {
+    int64_t n = live_count(d_count, cap);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float *q = in + kNrcInputs * i;
+        float p[3];
+        normalise_position(g, q, p);
+        __nv_bfloat16 *x = X + kNrcIn * i;
+        for (int l = 0; l < g.levels; ++l) {
+            Corner c;
+            corners(g, l, p, c);
+            float f0 = 0.f, f1 = 0.f;
+            for (int k = 0; k < 8; ++k) {
+                __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162 *>(table + 2 * (size_t)c.idx[k]);
+                f0 += c.w[k] * __bfloat162float(v.x);
+                f1 += c.w[k] * __bfloat162float(v.y);
+            }
+            x[2 * l] = __float2bfloat16_rn(f0);
+            x[2 * l + 1] = __float2bfloat16_rn(f1);
+        }
+        int o = 2 * g.levels;
+        for (int a = 0; a < 3; ++a) x[o + a] = __float2bfloat16_rn((q[3 + a] + 1.f) * 0.5f);
+        x[o + 3] = __float2bfloat16_rn(q[6]);
+        for (int a = 0; a < 3; ++a) x[o + 4 + a] = __float2bfloat16_rn(q[7 + a]);
+        for (int k = o + 7; k < kNrcIn; ++k) x[k] = __float2bfloat16_rn(0.f);
+    }
+}
+
+// Y[i][0..N) = act(X[i] . W[j]) for 128-row tiles; W is [N][64].
+template <int N, bool RELU, bool OUT_F32>
+__global__ void __launch_bounds__(kThreads)
+k_dense_fwd(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__restrict__ W,
+            const int32_t *d_count, int64_t cap, __nv_bfloat16 *__restrict__ Yb,
+            float *__restrict__ Yf) {
+    __shared__ float Ws[kNrcIn][N + 1];
+    __shared__ float Xs[128][kNrcIn + 1];
+    for (int e = threadIdx.x; e < N * kNrcIn; e += blockDim.x)
+        Ws[e % kNrcIn][e / kNrcIn] = __bfloat162float(W[e]);
+    int64_t n = live_count(d_count, cap);
+    constexpr int kCols = N * 128 / kThreads;   // outputs per thread
+    constexpr int kThreadsPerRow = N / kCols;
+    for (int64_t t0 = (int64_t)blockIdx.x * 128; t0 < n; t0 += (int64_t)gridDim.x * 128) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < 128 * kNrcIn; e += blockDim.x) {
+            int64_t r = t0 + e / kNrcIn;
+            Xs[e / kNrcIn][e % kNrcIn] = r < n ? __bfloat162float(X[r * kNrcIn + e % kNrcIn]) : 0.f;
+        }
+        __syncthreads();
+        int row = threadIdx.x / kThreadsPerRow;
+        int c0 = (threadIdx.x % kThreadsPerRow) * kCols;
+        float acc[kCols];
+#pragma unroll
+        for (int j = 0; j < kCols; ++j) acc[j] = 0.f;
+        for (int k = 0; k < kNrcIn; ++k) {
+            float x = Xs[row][k];
+#pragma unroll
+            for (int j = 0; j < kCols; ++j) acc[j] = fmaf(x, Ws[k][c0 + j], acc[j]);
+        }
+        int64_t r = t0 + row;
+        if (r < n) {
+#pragma unroll
+            for (int j = 0; j < kCols; ++j) {
+                float v = RELU ? fmaxf(acc[j], 0.f) : acc[j];
+                if (OUT_F32) Yf[r * N + c0 + j] = v;
+                else Yb[r * N + c0 + j] = __float2bfloat16_rn(v);
+            }
+        }
+    }
+}
+
+// dX[i][k] = sum_j dY[i][j] W[j][k], masked by the ReLU of the layer input
+// (X > 0) when MASK; dY is [n][N] float, W is [N][64].
+template <int N, bool MASK>
+__global__ void __launch_bounds__(kThreads)
+k_dense_bwd(const float *__restrict__ dY, const __nv_bfloat16 *__restrict__ W,
+            const __nv_bfloat16 *__restrict__ Xin, const int32_t *d_count, int64_t cap,
+            float *__restrict__ dX) {
+    __shared__ float Ws[N][kNrcIn + 1];
+    __shared__ float Ds[128][N + 1];
+    for (int e = threadIdx.x; e < N * kNrcIn; e += blockDim.x)
+        Ws[e / kNrcIn][e % kNrcIn] = __bfloat162float(W[e]);
+    int64_t n = live_count(d_count, cap);
+    constexpr int kCols = kNrcIn * 128 / kThreads;
+    constexpr int kThreadsPerRow = kNrcIn / kCols;
+    for (int64_t t0 = (int64_t)blockIdx.x * 128; t0 < n; t0 += (int64_t)gridDim.x * 128) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < 128 * N; e += blockDim.x) {
+            int64_t r = t0 + e / N;
+            Ds[e / N][e % N] = r < n ? bf(dY[r * N + e % N]) : 0.f;
+        }
+        __syncthreads();
+        int row = threadIdx.x / kThreadsPerRow;
+        int c0 = (threadIdx.x % kThreadsPerRow) * kCols;
+        float acc[kCols];
+#pragma unroll
+        for (int j = 0; j < kCols; ++j) acc[j] = 0.f;
+        for (int k = 0; k < N; ++k) {
+            float d = Ds[row][k];
+#pragma unroll
+            for (int j = 0; j < kCols; ++j) acc[j] = fmaf(d, Ws[k][c0 + j], acc[j]);
+        }
+        int64_t r = t0 + row;
+        if (r < n) {
+#pragma unroll
+            for (int j = 0; j < kCols; ++j) {
+                float v = acc[j];
+                if (MASK && !(__bfloat162float(Xin[r * kNrcIn + c0 + j]) > 0.f)) v = 0.f;
+                dX[r * kNrcIn + c0 + j] = v;
+            }
+        }
+    }
+}
+
+// dW[j][k] += sum_i dY[i][j] X[i][k] over a chunk of rows per block.
+template <int N>
+__global__ void __launch_bounds__(kThreads)
+k_dense_wgrad(const float *__restrict__ dY, const __nv_bfloat16 *__restrict__ X,
+              const int32_t *d_count, int64_t cap, float *__restrict__ dW) {
+    constexpr int kRows = 64;
+    __shared__ float Ds[kRows][N + 1];
+    __shared__ float Xs[kRows][kNrcIn + 1];
+    constexpr int kOut = N * kNrcIn / kThreads;   // outputs per thread
+    int64_t n = live_count(d_count, cap);
+    float acc[kOut];
+#pragma unroll
+    for (int j = 0; j < kOut; ++j) acc[j] = 0.f;
+    int o0 = threadIdx.x * kOut;
+    for (int64_t t0 = (int64_t)blockIdx.x * kRows; t0 < n; t0 += (int64_t)gridDim.x * kRows) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < kRows * N; e += blockDim.x) {
+            int64_t r = t0 + e / N;
+            Ds[e / N][e % N] = r < n ? bf(dY[r * N + e % N]) : 0.f;
+        }
+        for (int e = threadIdx.x; e < kRows * kNrcIn; e += blockDim.x) {
+            int64_t r = t0 + e / kNrcIn;
+            Xs[e / kNrcIn][e % kNrcIn] = r < n ? __bfloat162float(X[r * kNrcIn + e % kNrcIn]) : 0.f;
+        }
+        __syncthreads();
+        for (int r = 0; r < kRows; ++r) {
+#pragma unroll
+            for (int j = 0; j < kOut; ++j) {
+                int o = o0 + j;
+                acc[j] = fmaf(Ds[r][o / kNrcIn], Xs[r][o % kNrcIn], acc[j]);
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < kOut; ++j) atomicAdd(dW + o0 + j, acc[j]);
+}
+
+// Relative L2 loss gradient (scaled) and loss sum.
+__global__ void k_loss(const float *__restrict__ Y, const float *__restrict__ T, const int32_t *d_count,
+                       int64_t cap, float scale, float *__restrict__ dY, float *loss) {
+    int64_t n = live_count(d_count, cap);
+    float inv = 1.f / (float)(max(n, (int64_t)1) * 3);
+    float lsum = 0.f;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        for (int c = 0; c < kNrcOutPad; ++c) {
+            float g = 0.f;
+            if (c < 3) {
+                float y = Y[i * kNrcOutPad + c], t = T[3 * i + c];
+                float den = y * y + 0.01f;
+                lsum += (y - t) * (y - t) / den;
+                g = 2.f * (y - t) / den * inv * scale;
+            }
+            dY[i * kNrcOutPad + c] = g;
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, lsum * inv);
+}
+
+// Scatter the gradient of the 32 grid features into the table gradient.
+__global__ void k_encode_bwd(NrcGrid g, const float *__restrict__ in, const float *__restrict__ dX,
+                             const int32_t *d_count, int64_t cap, float *__restrict__ tgrad) {
+    int64_t n = live_count(d_count, cap);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float p[3];
+        normalise_position(g, in + kNrcInputs * i, p);
+        for (int l = 0; l < g.levels; ++l) {
+            float d0 = dX[i * kNrcIn + 2 * l], d1 = dX[i * kNrcIn + 2 * l + 1];
+            if (d0 == 0.f && d1 == 0.f) continue;
+            Corner c;
+            corners(g, l, p, c);
+            for (int k = 0; k < 8; ++k) {
+                atomicAdd(tgrad + 2 * (size_t)c.idx[k], c.w[k] * d0);
+                atomicAdd(tgrad + 2 * (size_t)c.idx[k] + 1, c.w[k] * d1);
+            }
+        }
+    }
+}
+
+// Adam on an FP32 master array; writes the BF16 copy and clears the gradient.
+__global__ void k_adam(float *__restrict__ w, float *__restrict__ m, float *__restrict__ v,
+                       float *__restrict__ grad, __nv_bfloat16 *__restrict__ wb, int64_t n, float lr,
+                       float b1, float b2, float eps, float grad_scale, float bc1, float bc2,
+                       const uint8_t *__restrict__ frozen) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float gr = grad[i] * grad_scale;
+        grad[i] = 0.f;
+        if (frozen && frozen[i]) continue;
+        if (!isfinite(gr)) continue;
+        float mi = b1 * m[i] + (1.f - b1) * gr;
+        float vi = b2 * v[i] + (1.f - b2) * gr * gr;
+        m[i] = mi;
+        v[i] = vi;
+        float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+        w[i] = wi;
+        wb[i] = __float2bfloat16_rn(wi);
+    }
+}
+
+__global__ void k_to_bf16(const float *__restrict__ a, __nv_bfloat16 *__restrict__ b, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = __float2bfloat16_rn(a[i]);
+}
+
+int grid_for(int64_t n, int per = kThreads) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int64_t g = (n + per - 1) / per;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)std::max(sms, 1) * 8));
+}
+
+// Deterministic parameter initialisation (splitmix64).
+struct Rng {
+    uint64_t s;
+    uint64_t next() {
+        uint64_t z = (s += 0x9e3779b97f4a7c15ULL);
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+        return z ^ (z >> 31);
+    }
+    float uniform() { return (float)((next() >> 40) * (1.0 / 16777216.0)); }
+};
+
+int ensure_capacity(krr_nrc *n, int64_t cap) {
+    if (cap <= n->cap) return KRR_OK;
+    cudaFree(n->act); cudaFree(n->out); cudaFree(n->dA); cudaFree(n->dB);
+    n->act = nullptr; n->out = nullptr; n->dA = nullptr; n->dB = nullptr;
+    int layers = n->mlp.layers;   // inputs of every layer: encoding + hidden outputs
+    KRR_CUDA(cudaMalloc(&n->act, (size_t)layers * cap * kNrcIn * sizeof(__nv_bfloat16)));
+    KRR_CUDA(cudaMalloc(&n->out, (size_t)cap * kNrcOutPad * sizeof(float)));
+    KRR_CUDA(cudaMalloc(&n->dA, (size_t)cap * kNrcIn * sizeof(float)));
+    KRR_CUDA(cudaMalloc(&n->dB, (size_t)cap * kNrcIn * sizeof(float)));
+    n->cap = cap;
+    return KRR_OK;
+}
+
+// Forward pass over `cap` rows (live count on the device); leaves the layer
+// inputs in n->act and the output in n->out.
+int forward(krr_nrc *n, const float *d_inputs, const int32_t *d_count, int64_t cap, cudaStream_t s) {
+    KRR_TRY(ensure_capacity(n, cap));
+    __nv_bfloat16 *A = n->act;
+    k_encode<<<grid_for(cap), kThreads, 0, s>>>(n->grid, d_inputs, d_count, cap, n->table, A);
+    KRR_CUDA(cudaGetLastError());
+    int blocks = grid_for(cap, 128);
+    for (int l = 0; l < n->mlp.layers; ++l) {
+        const __nv_bfloat16 *X = A + (size_t)l * cap * kNrcIn;
+        const __nv_bfloat16 *W = n->weights + n->mlp.w_offset[l];
+        if (l + 1 < n->mlp.layers) {
+            __nv_bfloat16 *Y = A + (size_t)(l + 1) * cap * kNrcIn;
+            k_dense_fwd<kNrcWidth, true, false><<<blocks, kThreads, 0, s>>>(X, W, d_count, cap, Y, nullptr);
+        } else {
+            k_dense_fwd<kNrcOutPad, false, true><<<blocks, kThreads, 0, s>>>(X, W, d_count, cap, nullptr, n->out);
+        }
+        KRR_CUDA(cudaGetLastError());
+    }
+    return KRR_OK;
+}
+
+__global__ void k_write_rgb(const float *__restrict__ out, const int32_t *d_count, int64_t cap,
+                            float *__restrict__ dst) {
+    int64_t n = live_count(d_count, cap);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        for (int c = 0; c < 3; ++c) dst[3 * i + c] = out[i * kNrcOutPad + c];
+}
+
+}  // namespace
+
+namespace krr {
+
+NrcView nrc_view(const krr_nrc *n) { return NrcView{n->grid, n->mlp, n->table, n->weights}; }
+int64_t nrc_batch_size(const krr_nrc *n) { return n->cfg.batch_size; }
+int32_t nrc_train_stride(const krr_nrc *n) { return n->cfg.train_pixel_stride; }
+
+int nrc_query_device(krr_nrc *n, const float *d_inputs, const int32_t *d_count, int64_t cap,
+                     float *d_out, cudaStream_t s) {
+    if (cap <= 0) return KRR_OK;
+    KRR_TRY(forward(n, d_inputs, d_count, cap, s));
+    k_write_rgb<<<grid_for(cap), kThreads, 0, s>>>(n->out, d_count, cap, d_out);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+int nrc_train_device(krr_nrc *n, const float *d_inputs, const float *d_targets,
+                     const int32_t *d_count, int64_t cap, cudaStream_t s) {
+    if (cap <= 0) return KRR_OK;
+    KRR_TRY(forward(n, d_inputs, d_count, cap, s));
+    const float scale = n->cfg.loss_scale;
+    int blocks = grid_for(cap, 128);
+    KRR_CUDA(cudaMemsetAsync(n->loss, 0, sizeof(float), s));
+    k_loss<<<grid_for(cap), kThreads, 0, s>>>(n->out, d_targets, d_count, cap, scale, n->dA, n->loss);
+    KRR_CUDA(cudaGetLastError());
+    // backward through the layers: dA holds dY of layer l (width N_l)
+    float *dY = n->dA, *dX = n->dB;
+    int wblocks = grid_for(cap, 64);
+    for (int l = n->mlp.layers - 1; l >= 0; --l) {
+        const __nv_bfloat16 *X = n->act + (size_t)l * cap * kNrcIn;
+        const __nv_bfloat16 *W = n->weights + n->mlp.w_offset[l];
+        float *dW = n->w_grad + n->mlp.w_offset[l];
+        bool out_layer = l + 1 == n->mlp.layers;
+        if (out_layer) k_dense_wgrad<kNrcOutPad><<<wblocks, kThreads, 0, s>>>(dY, X, d_count, cap, dW);
+        else k_dense_wgrad<kNrcWidth><<<wblocks, kThreads, 0, s>>>(dY, X, d_count, cap, dW);
+        KRR_CUDA(cudaGetLastError());
+        if (l > 0) {
+            if (out_layer) k_dense_bwd<kNrcOutPad, true><<<blocks, kThreads, 0, s>>>(dY, W, X, d_count, cap, dX);
+            else k_dense_bwd<kNrcWidth, true><<<blocks, kThreads, 0, s>>>(dY, W, X, d_count, cap, dX);
+        } else {
+            if (out_layer) k_dense_bwd<kNrcOutPad, false><<<blocks, kThreads, 0, s>>>(dY, W, X, d_count, cap, dX);
+            else k_dense_bwd<kNrcWidth, false><<<blocks, kThreads, 0, s>>>(dY, W, X, d_count, cap, dX);
+        }
+        KRR_CUDA(cudaGetLastError());
+        std::swap(dY, dX);
+    }
+    // dY now holds the gradient of the encoded input
+    k_encode_bwd<<<grid_for(cap), kThreads, 0, s>>>(n->grid, d_inputs, dY, d_count, cap, n->table_grad);
+    KRR_CUDA(cudaGetLastError());
+    // Adam
+    n->step += 1;
+    const krr_nrc_config &c = n->cfg;
+    float bc1 = 1.f - std::pow(c.beta1, (float)n->step), bc2 = 1.f - std::pow(c.beta2, (float)n->step);
+    k_adam<<<grid_for(n->mlp.n_params), kThreads, 0, s>>>(n->w_master, n->w_m, n->w_v, n->w_grad,
+                                                           n->weights, n->mlp.n_params, c.learning_rate,
+                                                           c.beta1, c.beta2, c.epsilon, 1.f / scale,
+                                                           bc1, bc2, nullptr);
+    int64_t tn = (int64_t)n->n_entries * n->grid.features;
+    k_adam<<<grid_for(tn), kThreads, 0, s>>>(n->table_master, n->table_m, n->table_v, n->table_grad,
+                                             n->table, tn, c.learning_rate, c.beta1, c.beta2,
+                                             c.epsilon, 1.f / scale, bc1, bc2, nullptr);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+}  // namespace krr
+
+// ------------------------------------------------------------------ C ABI
+extern "C" void krr_nrc_config_default(krr_nrc_config *c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->n_levels = 16;
+    c->features_per_level = 2;
+    c->log2_table_size = 19;
+    c->base_resolution = 16;
+    c->max_resolution = 2048;
+    c->hidden_layers = 5;
+    c->learning_rate = 1e-2f;
+    c->beta1 = 0.9f;
+    c->beta2 = 0.99f;
+    c->epsilon = 1e-15f;
+    c->loss_scale = 128.f;
+    c->batch_size = 65536;
+    c->train_pixel_stride = 16;
+    c->seed = 3;
+    for (int k = 0; k < 3; ++k) { c->scene_lo[k] = 0.f; c->scene_hi[k] = 1.f; }
+}
+
+extern "C" int krr_nrc_create(const krr_nrc_config *cfg, krr_nrc **out) {
+    KRR_CHECK_ARG(cfg && out, "NULL argument");
+    KRR_CHECK_ARG(cfg->n_levels >= 1 && cfg->n_levels <= kNrcMaxLevels, "n_levels must be 1..16");
+    KRR_CHECK_ARG(cfg->features_per_level == 2, "features_per_level must be 2");
+    KRR_CHECK_ARG(2 * cfg->n_levels + 7 <= kNrcIn, "encoded input wider than 64");
+    KRR_CHECK_ARG(cfg->log2_table_size >= 8 && cfg->log2_table_size <= 24, "log2_table_size 8..24");
+    KRR_CHECK_ARG(cfg->hidden_layers >= 1 && cfg->hidden_layers <= 7, "hidden_layers 1..7");
+    KRR_CHECK_ARG(cfg->base_resolution >= 2 && cfg->max_resolution >= cfg->base_resolution,
+                  "bad resolutions");
+    KRR_CHECK_ARG(cfg->batch_size > 0, "batch_size must be positive");
+    krr_nrc *n = new krr_nrc();
+    n->cfg = *cfg;
+    if (n->cfg.train_pixel_stride < 1) n->cfg.train_pixel_stride = 1;
+    NrcGrid &g = n->grid;
+    g.levels = cfg->n_levels;
+    g.features = 2;
+    g.table_size = 1u << cfg->log2_table_size;
+    double b = cfg->n_levels > 1 ? std::exp((std::log((double)cfg->max_resolution) -
+                                             std::log((double)cfg->base_resolution)) / (cfg->n_levels - 1))
+                                 : 1.0;
+    uint32_t off = 0;
+    for (int l = 0; l < g.levels; ++l) {
+        g.res[l] = (int)std::floor(cfg->base_resolution * std::pow(b, l) + 1e-6);
+        uint64_t n1 = (uint64_t)g.res[l] + 1;
+        uint64_t dense = n1 * n1 * n1;
+        g.size[l] = dense <= g.table_size ? (uint32_t)dense : g.table_size;
+        if (dense <= g.table_size) g.dense_mask |= 1u << l;
+        g.offset[l] = off;
+        off += g.size[l];
+    }
+    n->n_entries = off;
+    for (int a = 0; a < 3; ++a) {
+        g.lo[a] = cfg->scene_lo[a];
+        float e = cfg->scene_hi[a] - cfg->scene_lo[a];
+        g.inv_extent[a] = e > 0.f ? 1.f / e : 1.f;
+    }
+    NrcMlp &m = n->mlp;
+    m.layers = cfg->hidden_layers + 1;
+    int o = 0;
+    for (int l = 0; l < m.layers; ++l) {
+        m.w_offset[l] = o;
+        o += (l + 1 < m.layers ? kNrcWidth : kNrcOutPad) * kNrcIn;
+    }
+    m.n_params = o;
+    // host initialisation
+    Rng rng{0x6a09e667f3bcc908ULL ^ (uint64_t)cfg->seed};
+    std::vector<float> w(m.n_params, 0.f);
+    for (int l = 0; l < m.layers; ++l) {
+        int rows = l + 1 < m.layers ? kNrcWidth : 3;
+        int fan_in = l == 0 ? 2 * g.levels + 7 : kNrcWidth;
+        float a = std::sqrt(6.f / (float)(fan_in + rows));
+        for (int r = 0; r < rows; ++r)
+            for (int k = 0; k < fan_in; ++k) w[m.w_offset[l] + r * kNrcIn + k] = (2.f * rng.uniform() - 1.f) * a;
+    }
+    size_t tn = (size_t)n->n_entries * 2;
+    std::vector<float> t(tn);
+    for (auto &x : t) x = (2.f * rng.uniform() - 1.f) * 1e-4f;
+    int st = KRR_OK;
+    auto alloc = [&](void **p, size_t bytes) {
+        if (st != KRR_OK) return;
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e == cudaSuccess) e = cudaMemset(*p, 0, bytes);
+        if (e != cudaSuccess) st = cuda_status(e, "cudaMalloc", __FILE__, __LINE__);
+    };
+    alloc((void **)&n->w_master, m.n_params * 4);
+    alloc((void **)&n->w_m, m.n_params * 4);
+    alloc((void **)&n->w_v, m.n_params * 4);
+    alloc((void **)&n->w_grad, m.n_params * 4);
+    alloc((void **)&n->weights, m.n_params * 2);
+    alloc((void **)&n->table_master, tn * 4);
+    alloc((void **)&n->table_m, tn * 4);
+    alloc((void **)&n->table_v, tn * 4);
+    alloc((void **)&n->table_grad, tn * 4);
+    alloc((void **)&n->table, tn * 2);
+    alloc((void **)&n->loss, 16);
+    if (st == KRR_OK) {
+        cudaMemcpy(n->w_master, w.data(), m.n_params * 4, cudaMemcpyHostToDevice);
+        cudaMemcpy(n->table_master, t.data(), tn * 4, cudaMemcpyHostToDevice);
+        k_to_bf16<<<grid_for(m.n_params), kThreads>>>(n->w_master, n->weights, m.n_params);
+        k_to_bf16<<<grid_for((int64_t)tn), kThreads>>>(n->table_master, n->table, (int64_t)tn);
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) st = cuda_status(e, "krr_nrc_create", __FILE__, __LINE__);
+    }
+    if (st != KRR_OK) {
+        krr_nrc_destroy(n);
+        return st;
+    }
+    *out = n;
+    return KRR_OK;
+}
+
+extern "C" int krr_nrc_destroy(krr_nrc *n) {
+    if (!n) return KRR_OK;
+    cudaDeviceSynchronize();
+    for (void *p : {(void *)n->table_master, (void *)n->table_m, (void *)n->table_v,
+                    (void *)n->table_grad, (void *)n->table, (void *)n->w_master, (void *)n->w_m,
+                    (void *)n->w_v, (void *)n->w_grad, (void *)n->weights, (void *)n->act,
+                    (void *)n->out, (void *)n->dA, (void *)n->dB, (void *)n->loss})
+        cudaFree(p);
+    delete n;
+    return KRR_OK;
+}
+
+extern "C" int krr_nrc_query(krr_nrc *n, const float *d_inputs, int64_t count, float *d_out,
+                             void *stream) {
+    KRR_CHECK_ARG(n && (count == 0 || (d_inputs && d_out)) && count >= 0, "bad argument");
+    return nrc_query_device(n, d_inputs, nullptr, count, d_out, as_stream(stream));
+}
+
+extern "C" int krr_nrc_train_step(krr_nrc *n, const float *d_inputs, const float *d_targets,
+                                  int64_t count, float *h_loss, void *stream) {
+    KRR_CHECK_ARG(n && (count == 0 || (d_inputs && d_targets)) && count >= 0, "bad argument");
+    cudaStream_t s = as_stream(stream);
+    KRR_TRY(nrc_train_device(n, d_inputs, d_targets, nullptr, count, s));
+    if (h_loss) {
+        KRR_CUDA(cudaMemcpyAsync(h_loss, n->loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+        KRR_CUDA(cudaStreamSynchronize(s));
+    }
+    return KRR_OK;
+}
+
+extern "C" int krr_nrc_info(const krr_nrc *n, krr_nrc_info_t *info) {
+    KRR_CHECK_ARG(n && info, "NULL argument");
+    info->n_params_mlp = n->mlp.n_params;
+    info->n_table_entries = (int64_t)n->n_entries;
+    info->n_levels = n->grid.levels;
+    for (int l = 0; l < n->grid.levels; ++l) {
+        info->resolution[l] = n->grid.res[l];
+        info->level_offset[l] = n->grid.offset[l];
+        info->level_size[l] = n->grid.size[l];
+    }
+    info->step = n->step;
+    return KRR_OK;
+}
+
+// Parameter access for tests and checkpoints: which = 0 MLP weights (FP32
+// master, [layer][out][64]), 1 hash table (FP32 master, [entry][2]).
+extern "C" int krr_nrc_get_params(const krr_nrc *n, int32_t which, float *h_dst, int64_t count) {
+    KRR_CHECK_ARG(n && h_dst, "NULL argument");
+    int64_t total = which == 0 ? n->mlp.n_params : (int64_t)n->n_entries * 2;
+    KRR_CHECK_ARG(count == total, "count does not match the parameter array");
+    KRR_CUDA(cudaDeviceSynchronize());
+    KRR_CUDA(cudaMemcpy(h_dst, which == 0 ? n->w_master : n->table_master, total * 4,
+                        cudaMemcpyDeviceToHost));
+    return KRR_OK;
+}
+
+extern "C" int krr_nrc_set_params(krr_nrc *n, int32_t which, const float *h_src, int64_t count) {
+    KRR_CHECK_ARG(n && h_src, "NULL argument");
+    int64_t total = which == 0 ? n->mlp.n_params : (int64_t)n->n_entries * 2;
+    KRR_CHECK_ARG(count == total, "count does not match the parameter array");
+    float *dst = which == 0 ? n->w_master : n->table_master;
+    __nv_bfloat16 *bdst = which == 0 ? n->weights : n->table;
+    KRR_CUDA(cudaDeviceSynchronize());
+    KRR_CUDA(cudaMemcpy(dst, h_src, total * 4, cudaMemcpyHostToDevice));
+    k_to_bf16<<<grid_for(total), kThreads>>>(dst, bdst, total);
+    KRR_CUDA(cudaDeviceSynchronize());
+    return KRR_OK;
+}
+
+// Gradients of the last train step before Adam consumed them are not kept;
+// this computes them for one batch without updating (loss-scaled units are
+// removed): which = 0 MLP, 1 table.
+extern "C" int krr_nrc_gradients(krr_nrc *n, const float *d_inputs, const float *d_targets,
+                                 int64_t count, float *h_grad_mlp, float *h_grad_table,
+                                 float *h_loss) {
+    KRR_CHECK_ARG(n && d_inputs && d_targets && count > 0, "bad argument");
+    cudaStream_t s = 0;
+    KRR_TRY(forward(n, d_inputs, nullptr, count, s));
+    // reuse the training path but stop before Adam
+    float scale = n->cfg.loss_scale;
+    int blocks = grid_for(count, 128);
+    KRR_CUDA(cudaMemset(n->loss, 0, sizeof(float)));
+    KRR_CUDA(cudaMemset(n->w_grad, 0, n->mlp.n_params * 4));
+    KRR_CUDA(cudaMemset(n->table_grad, 0, (size_t)n->n_entries * 2 * 4));
+    k_loss<<<grid_for(count), kThreads, 0, s>>>(n->out, d_targets, nullptr, count, scale, n->dA, n->loss);
+    float *dY = n->dA, *dX = n->dB;
+    int wblocks = grid_for(count, 64);
+    for (int l = n->mlp.layers - 1; l >= 0; --l) {
+        const __nv_bfloat16 *X = n->act + (size_t)l * count * kNrcIn;
+        const __nv_bfloat16 *W = n->weights + n->mlp.w_offset[l];
+        float *dW = n->w_grad + n->mlp.w_offset[l];
+        bool out_layer = l + 1 == n->mlp.layers;
+        if (out_layer) k_dense_wgrad<kNrcOutPad><<<wblocks, kThreads, 0, s>>>(dY, X, nullptr, count, dW);
+        else k_dense_wgrad<kNrcWidth><<<wblocks, kThreads, 0, s>>>(dY, X, nullptr, count, dW);
+        if (l > 0) {
+            if (out_layer) k_dense_bwd<kNrcOutPad, true><<<blocks, kThreads, 0, s>>>(dY, W, X, nullptr, count, dX);
+            else k_dense_bwd<kNrcWidth, true><<<blocks, kThreads, 0, s>>>(dY, W, X, nullptr, count, dX);
+        } else {
+            if (out_layer) k_dense_bwd<kNrcOutPad, false><<<blocks, kThreads, 0, s>>>(dY, W, X, nullptr, count, dX);
+            else k_dense_bwd<kNrcWidth, false><<<blocks, kThreads, 0, s>>>(dY, W, X, nullptr, count, dX);
+        }
+        std::swap(dY, dX);
+    }
+    k_encode_bwd<<<grid_for(count), kThreads, 0, s>>>(n->grid, d_inputs, dY, nullptr, count, n->table_grad);
+    KRR_CUDA(cudaGetLastError());
+    KRR_CUDA(cudaDeviceSynchronize());
+    std::vector<float> tmp;
+    if (h_grad_mlp) {
+        KRR_CUDA(cudaMemcpy(h_grad_mlp, n->w_grad, n->mlp.n_params * 4, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < n->mlp.n_params; ++i) h_grad_mlp[i] /= scale;
+    }
+    if (h_grad_table) {
+        size_t tn = (size_t)n->n_entries * 2;
+        KRR_CUDA(cudaMemcpy(h_grad_table, n->table_grad, tn * 4, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < tn; ++i) h_grad_table[i] /= scale;
+    }
+    if (h_loss) KRR_CUDA(cudaMemcpy(h_loss, n->loss, 4, cudaMemcpyDeviceToHost));
+    KRR_CUDA(cudaMemset(n->w_grad, 0, n->mlp.n_params * 4));
+    KRR_CUDA(cudaMemset(n->table_grad, 0, (size_t)n->n_entries * 2 * 4));
+    return KRR_OK;
+}

@@ -1,0 +1,56 @@
+// Neural radiance cache: device layout shared by nrc.cu and the wavefront
+// integration (wavefront.cu).
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "internal.h"
+
+namespace krr {
+
+constexpr int kNrcMaxLevels = 16;
+constexpr int kNrcIn = 64;       // padded MLP input width
+constexpr int kNrcWidth = 64;    // hidden width
+constexpr int kNrcOutPad = 16;   // padded output rows (3 used)
+constexpr int kNrcInputs = 10;   // query record: position 3, normal 3, roughness 1, albedo 3
+
+// Hash-grid description passed by value to kernels.
+struct NrcGrid {
+    int32_t levels, features;         // features per level (2)
+    uint32_t table_size;              // entries per hashed level (power of two)
+    uint32_t dense_mask;              // bit l set: level l is indexed densely
+    int32_t res[kNrcMaxLevels];       // cells per axis
+    uint32_t offset[kNrcMaxLevels];   // first entry of each level
+    uint32_t size[kNrcMaxLevels];     // entries of each level
+    float lo[3], inv_extent[3];       // scene box -> [0,1]^3
+};
+
+// One MLP: layer l maps rows_in[l] -> rows_out[l]; weights row-major
+// [out][in] at w_offset[l].
+struct NrcMlp {
+    int32_t layers;                   // hidden layers + output layer
+    int32_t w_offset[8];
+    int32_t n_params;
+};
+
+}  // namespace krr
+
+struct krr_nrc;
+
+namespace krr {
+// Device views used by the wavefront hooks.
+struct NrcView {
+    NrcGrid grid;
+    NrcMlp mlp;
+    const __nv_bfloat16 *table;       // bf16 features, [entries][features]
+    const __nv_bfloat16 *weights;     // bf16 weights
+};
+NrcView nrc_view(const krr_nrc *n);
+int nrc_query_device(krr_nrc *n, const float *d_inputs, const int32_t *d_count, int64_t capacity,
+                     float *d_out, cudaStream_t s);
+int nrc_train_device(krr_nrc *n, const float *d_inputs, const float *d_targets,
+                     const int32_t *d_count, int64_t capacity, cudaStream_t s);
+int64_t nrc_batch_size(const krr_nrc *n);
+int32_t nrc_train_stride(const krr_nrc *n);
+}  // namespace krr

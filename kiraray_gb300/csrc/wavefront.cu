@@ -18,6 +18,7 @@
 
 #include "accel.h"
 #include "internal.h"
+#include "nrc.h"
 #include "shading.cuh"
 #include "wavefront.h"
 #include "accel_device.cuh"
@@ -66,8 +67,21 @@ struct krr_wf {
     uint8_t *occluded = nullptr;
     PixelState ps{};
     int grid = 0;
+    // neural radiance cache hooks
+    krr_nrc *nrc = nullptr;
+    bool nrc_train = false;
+    float *nrc_q_in = nullptr;       // [n][10] query records
+    float4 *nrc_q_meta = nullptr;    // [n] throughput | pixel
+    float *nrc_q_out = nullptr;      // [n][3]
+    float *nrc_rec = nullptr;        // [slots][max_rec][16] training vertices
+    int32_t *nrc_rec_count = nullptr;
+    int32_t nrc_rec_max = 0;
+    int64_t nrc_slots = 0;
+    float *nrc_b_in = nullptr, *nrc_b_t = nullptr;   // training batch
 
     Queue q(int k) const { return Queue{qbuf[k], (int32_t)n, d_counts + k}; }
+    int32_t *nrc_q_count() const { return d_counts + 9; }
+    int32_t *nrc_b_count() const { return d_counts + 10; }
     uint32_t *err() const { return reinterpret_cast<uint32_t *>(d_counts + 8); }
     WfConst consts() const {
         WfConst c;
@@ -365,10 +379,107 @@ __device__ __forceinline__ void copy_ray_item(const Queue &src, int i, const Que
     for (int c = 0; c < kRayCh; ++c) dst.at(c, j) = src.at(c, i);
 }
 
+
+// Cache hooks of the closest-hit stage.  mode 0: off; 1: on.  A pixel is a
+// training pixel when (pixel + offset) % stride == 0; its slot is
+// pixel / stride.
+struct NrcHook {
+    int32_t mode;
+    int32_t stride, offset;
+    float *q_in;
+    float4 *q_meta;
+    int32_t *q_count;
+    int32_t q_cap;
+    float *rec;
+    int32_t *rec_count;
+    int32_t rec_max;
+};
+
+__device__ __forceinline__ void nrc_features(const DevScene &s, const Surf &sf, float *dst) {
+    const DevMaterial &m = s.materials[sf.material];
+    dst[0] = sf.p.x; dst[1] = sf.p.y; dst[2] = sf.p.z;
+    dst[3] = sf.n.x; dst[4] = sf.n.y; dst[5] = sf.n.z;
+    dst[6] = 1.f - m.spec_alpha;
+    dst[7] = m.diffuse[0]; dst[8] = m.diffuse[1]; dst[9] = m.diffuse[2];
+}
+
+// Returns true when the path stops here and the cache answers for it.
+__device__ __forceinline__ bool nrc_vertex(const NrcHook &h, const DevScene &s, const Surf &sf,
+                                           const PixelState &ps, uint32_t pixel, uint32_t depth,
+                                           uint32_t bsdf_type, V3 thp, uint32_t *err) {
+    if (!h.mode || depth < 1 || !(bsdf_type & BSDF_SMOOTH)) return false;
+    if ((pixel + (uint32_t)h.offset) % (uint32_t)h.stride == 0u) {
+        if (!h.rec) return false;
+        uint32_t slot = pixel / (uint32_t)h.stride;
+        int k = h.rec_count[slot];
+        if (k < h.rec_max) {
+            float *r = h.rec + ((size_t)slot * h.rec_max + k) * 16;
+            nrc_features(s, sf, r);
+            float4 l = ps.L[pixel];
+            r[10] = thp.x; r[11] = thp.y; r[12] = thp.z;
+            r[13] = l.x; r[14] = l.y; r[15] = l.z;
+            h.rec_count[slot] = k + 1;
+        }
+        return false;
+    }
+    int j = push_slot(h.q_count, h.q_cap, err);
+    if (j >= 0) {
+        nrc_features(s, sf, h.q_in + (size_t)kNrcInputs * j);
+        h.q_meta[j] = make_float4(thp.x, thp.y, thp.z, __uint_as_float(pixel));
+    }
+    return true;
+}
+
+// L[pixel] += throughput x max(cache, 0)
+__global__ void k_nrc_apply(const float *__restrict__ out, const float4 *__restrict__ meta,
+                            const int32_t *count, PixelState ps) {
+    int n = *count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 m = meta[i];
+        V3 c{fmaxf(out[3 * i], 0.f), fmaxf(out[3 * i + 1], 0.f), fmaxf(out[3 * i + 2], 0.f)};
+        add_radiance(ps, __float_as_uint(m.w), V3{m.x, m.y, m.z} * c);
+    }
+}
+
+// Training targets (L_final - L_at_vertex) / throughput of every recorded
+// vertex, appended to the batch up to its capacity.
+__global__ void k_nrc_targets(const float *__restrict__ rec, const int32_t *__restrict__ rec_count,
+                              int64_t slots, int rec_max, int stride, int offset, int64_t n_pixels,
+                              PixelState ps, float *b_in, float *b_t, int32_t *b_count, int b_cap) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < slots;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        int k_n = rec_count[s];
+        if (k_n == 0) continue;
+        int64_t pixel = s * stride + ((stride - offset % stride) % stride);
+        if (pixel >= n_pixels) continue;
+        float4 lf = ps.L[pixel];
+        for (int k = 0; k < k_n; ++k) {
+            const float *r = rec + ((size_t)s * rec_max + k) * 16;
+            float t[3];
+            float lfin[3] = {lf.x, lf.y, lf.z};
+            bool ok = true;
+            for (int c = 0; c < 3; ++c) {
+                float thp = r[10 + c];
+                t[c] = thp > 0.f ? (lfin[c] - r[13 + c]) / thp : 0.f;
+                ok = ok && isfinite(t[c]);
+            }
+            if (!ok) continue;
+            int j = atomicAdd(b_count, 1);
+            if (j >= b_cap) return;
+            for (int q = 0; q < kNrcInputs; ++q) b_in[(size_t)kNrcInputs * j + q] = r[q];
+            for (int c = 0; c < 3; ++c) b_t[3 * (size_t)j + c] = fmaxf(t[c], 0.f);
+        }
+    }
+}
+
+__global__ void k_clamp_count(int32_t *count, int cap) {
+    if (threadIdx.x == 0 && *count > cap) *count = cap;
+}
+
 // Routing of a closest hit (__closesthit__/__miss__Closest, device.cu:43-74).
 __global__ void k_hit_process(DevScene s, Queue rq, const float4 *__restrict__ hits, Queue next,
                               Queue miss, Queue hitl, Queue scat, Queue msq, int enable_medium,
-                              uint32_t *err) {
+                              uint32_t *err, NrcHook hook, PixelState ps) {
     int n = *rq.count;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 h = hits[i];
@@ -419,6 +530,7 @@ __global__ void k_hit_process(DevScene s, Queue rq, const float4 *__restrict__ h
         }
         (void)c0;
         V3 thp = f3(c4);
+        if (nrc_vertex(hook, s, sf, ps, ubits(c5.w), ubits(c4.w), ubits(c3.w), thp, err)) continue;
         if (sf.light >= 0) {
             int j = push_slot(hitl.count, hitl.cap, err);
             if (j >= 0) {
@@ -961,6 +1073,58 @@ void inverse_transpose(const float *m, float *out) {
 
 }  // namespace
 
+
+static void free_nrc_buffers(krr_wf *wf) {
+    for (void *p : {(void *)wf->nrc_q_in, (void *)wf->nrc_q_meta, (void *)wf->nrc_q_out,
+                    (void *)wf->nrc_rec, (void *)wf->nrc_rec_count, (void *)wf->nrc_b_in,
+                    (void *)wf->nrc_b_t})
+        cudaFree(p);
+    wf->nrc_q_in = nullptr; wf->nrc_q_meta = nullptr; wf->nrc_q_out = nullptr;
+    wf->nrc_rec = nullptr; wf->nrc_rec_count = nullptr; wf->nrc_b_in = nullptr; wf->nrc_b_t = nullptr;
+    wf->nrc_slots = 0;
+}
+
+static int alloc_nrc_buffers(krr_wf *wf) {
+    free_nrc_buffers(wf);
+    if (!wf->nrc || !wf->n) return KRR_OK;
+    int stride = nrc_train_stride(wf->nrc);
+    wf->nrc_slots = (wf->n + stride - 1) / stride;
+    wf->nrc_rec_max = std::min(16, std::max(1, wf->params.max_depth + 1));
+    int64_t batch = nrc_batch_size(wf->nrc);
+    KRR_CUDA(cudaMalloc(&wf->nrc_q_in, (size_t)wf->n * kNrcInputs * sizeof(float)));
+    KRR_CUDA(cudaMalloc(&wf->nrc_q_meta, (size_t)wf->n * sizeof(float4)));
+    KRR_CUDA(cudaMalloc(&wf->nrc_q_out, (size_t)wf->n * 3 * sizeof(float)));
+    KRR_CUDA(cudaMalloc(&wf->nrc_rec, (size_t)wf->nrc_slots * wf->nrc_rec_max * 16 * sizeof(float)));
+    KRR_CUDA(cudaMalloc(&wf->nrc_rec_count, (size_t)wf->nrc_slots * sizeof(int32_t)));
+    KRR_CUDA(cudaMemset(wf->nrc_rec_count, 0, (size_t)wf->nrc_slots * sizeof(int32_t)));
+    KRR_CUDA(cudaMalloc(&wf->nrc_b_in, (size_t)batch * kNrcInputs * sizeof(float)));
+    KRR_CUDA(cudaMalloc(&wf->nrc_b_t, (size_t)batch * 3 * sizeof(float)));
+    return KRR_OK;
+}
+
+// End of a frame with training: build the batch from the recorded vertices
+// and take one optimiser step.
+static int nrc_train_frame(krr_wf *wf, cudaStream_t st) {
+    int stride = nrc_train_stride(wf->nrc);
+    int offset = (int)(wf->frame_index % stride);
+    int64_t batch = nrc_batch_size(wf->nrc);
+    KRR_CUDA(cudaMemsetAsync(wf->nrc_b_count(), 0, sizeof(int32_t), st));
+    k_nrc_targets<<<grid_for(wf->nrc_slots), kThreads, 0, st>>>(
+        wf->nrc_rec, wf->nrc_rec_count, wf->nrc_slots, wf->nrc_rec_max, stride, offset, wf->n, wf->ps,
+        wf->nrc_b_in, wf->nrc_b_t, wf->nrc_b_count(), (int)batch);
+    k_clamp_count<<<1, 32, 0, st>>>(wf->nrc_b_count(), (int)batch);
+    KRR_CUDA(cudaGetLastError());
+    return nrc_train_device(wf->nrc, wf->nrc_b_in, wf->nrc_b_t, wf->nrc_b_count(), batch, st);
+}
+
+extern "C" int krr_wf_set_nrc(krr_wf *wf, krr_nrc *nrc, int32_t train) {
+    KRR_CHECK_ARG(wf != nullptr, "pass is NULL");
+    cudaDeviceSynchronize();
+    wf->nrc = nrc;
+    wf->nrc_train = nrc && train;
+    return alloc_nrc_buffers(wf);
+}
+
 extern "C" void krr_wf_params_default(krr_wf_params *p) {
     if (!p) return;
     p->nee = 1;
@@ -988,6 +1152,7 @@ extern "C" int krr_wf_destroy(krr_wf *wf) {
     cudaDeviceSynchronize();
     free_queues(wf);
     free_scene(wf);
+    free_nrc_buffers(wf);
     delete wf;
     return KRR_OK;
 }
@@ -1206,7 +1371,7 @@ extern "C" int krr_wf_resize(krr_wf *wf, int32_t width, int32_t height) {
     KRR_CUDA(cudaMalloc(&wf->ps.pixel, wf->n * sizeof(float4)));
     KRR_CUDA(cudaMalloc(&wf->ps.rng, wf->n * sizeof(ulonglong2)));
     wf->grid = grid_for(wf->n);
-    return KRR_OK;
+    return alloc_nrc_buffers(wf);
 }
 
 static int ready(krr_wf *wf) {
@@ -1238,6 +1403,8 @@ extern "C" int krr_wf_begin_frame(krr_wf *wf, int64_t frame_index, const krr_cam
     uint32_t sample_index = (uint32_t)(frame_index * wf->params.spp + wf->params.seed);
     k_begin_frame<<<wf->grid, kThreads, 0, st>>>(wf->ps, wf->width, wf->n, sample_index);
     KRR_CUDA(cudaGetLastError());
+    if (wf->nrc && wf->nrc_rec_count)
+        KRR_CUDA(cudaMemsetAsync(wf->nrc_rec_count, 0, wf->nrc_slots * sizeof(int32_t), st));
     return KRR_OK;
 }
 
@@ -1271,10 +1438,30 @@ extern "C" int krr_wf_trace_closest(krr_wf *wf, int32_t depth, void *stream) {
     l.counter = wf->accel.d_scratch;
     l.err = wf->accel.d_scratch + 4;
     KRR_TRY(launch_trace_closest(&wf->accel, l, st));
+    NrcHook hook{};
+    if (wf->nrc) {
+        hook.mode = 1;
+        hook.stride = nrc_train_stride(wf->nrc);
+        hook.offset = (int32_t)(wf->frame_index % hook.stride);
+        hook.q_in = wf->nrc_q_in;
+        hook.q_meta = wf->nrc_q_meta;
+        hook.q_count = wf->nrc_q_count();
+        hook.q_cap = (int32_t)wf->n;
+        hook.rec = wf->nrc_train ? wf->nrc_rec : nullptr;
+        hook.rec_count = wf->nrc_rec_count;
+        hook.rec_max = wf->nrc_rec_max;
+        KRR_CUDA(cudaMemsetAsync(wf->nrc_q_count(), 0, sizeof(int32_t), st));
+    }
     k_hit_process<<<wf->grid, kThreads, 0, st>>>(wf->scene, rq, wf->hits, wf->q(cur ^ 1),
                                                   wf->q(Q_MISS), wf->q(Q_HIT_LIGHT), wf->q(Q_SCATTER),
-                                                  wf->q(Q_MEDIUM_SAMPLE), wf->medium ? 1 : 0, wf->err());
+                                                  wf->q(Q_MEDIUM_SAMPLE), wf->medium ? 1 : 0, wf->err(),
+                                                  hook, wf->ps);
     KRR_CUDA(cudaGetLastError());
+    if (wf->nrc) {
+        KRR_TRY(nrc_query_device(wf->nrc, wf->nrc_q_in, wf->nrc_q_count(), wf->n, wf->nrc_q_out, st));
+        k_nrc_apply<<<wf->grid, kThreads, 0, st>>>(wf->nrc_q_out, wf->nrc_q_meta, wf->nrc_q_count(), wf->ps);
+        KRR_CUDA(cudaGetLastError());
+    }
     return KRR_OK;
 }
 
@@ -1354,6 +1541,7 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
             KRR_TRY(krr_wf_generate_scatter_rays(wf, depth, stream));
             if (wf->params.nee) KRR_TRY(krr_wf_trace_shadow(wf, stream));
         }
+        if (wf->nrc && wf->nrc_train) KRR_TRY(nrc_train_frame(wf, st));
         k_accumulate<<<wf->grid, kThreads, 0, st>>>(wf->ps, wf->n);
         KRR_CUDA(cudaGetLastError());
     }

@@ -60,6 +60,12 @@ class WavefrontPathTracer:
         self._keep = (desc, keep)
         self.scene = scene
 
+    def set_nrc(self, cache, train: bool = True):
+        """Attaches a NeuralRadianceCache (None detaches: the plain tracer)."""
+        self._nrc = cache
+        check(self.lib.krr_wf_set_nrc(self._h, cache._h if cache is not None else None,
+                                      int(bool(train))), "krr_wf_set_nrc")
+
     def resize(self, width: int, height: int):
         check(self.lib.krr_wf_resize(self._h, width, height), "krr_wf_resize")
         self.width, self.height = width, height

@@ -1,0 +1,37 @@
+"""FP64 accumulation and relMSE/MSE on the GPU against numpy float64."""
+import numpy as np
+import pytest
+import torch
+
+from kiraray_gb300.convergence import MSE, RELMSE, Accumulator
+
+pytestmark = pytest.mark.gpu
+
+
+def _numpy_error(mean_rgb, ref_rgb, metric):
+    d = np.abs(mean_rgb - ref_rgb)
+    if metric == RELMSE:
+        with np.errstate(divide="ignore", invalid="ignore"):
+            e = np.where(ref_rgb == 0, 0.0, (d / ref_rgb) ** 2)
+    else:
+        e = d ** 2
+    return np.minimum(e.mean(1), 100.0).mean()
+
+
+@pytest.mark.parametrize("metric", [RELMSE, MSE])
+def test_accumulate_and_error(krr_lib, cuda, metric):
+    rng = np.random.default_rng(3)
+    n = 50000
+    ref = np.ones((n, 4), np.float32)
+    ref[:, :3] = rng.random((n, 3)).astype(np.float32)
+    ref[::7, 1] = 0.0                       # zero reference channels contribute 0
+    frames = [rng.random((n, 4)).astype(np.float32) * 2 for _ in range(5)]
+    frames[2][::11, 0] = 1e6                # outliers are clamped at 100 per pixel
+    acc = Accumulator(n, 1)
+    for f in frames:
+        acc.add(torch.from_numpy(f).cuda())
+    got = acc.error(torch.from_numpy(ref).cuda(), metric)
+    mean = np.sum([f[:, :3].astype(np.float64) for f in frames], 0) / 5
+    want = _numpy_error(mean, ref[:, :3].astype(np.float64), metric)
+    assert abs(got - want) <= 1e-12 * max(1.0, abs(want))
+    assert np.allclose(acc.sum.cpu().numpy(), np.sum([f[:, :3].astype(np.float64) for f in frames], 0))

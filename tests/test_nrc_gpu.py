@@ -1,0 +1,119 @@
+"""Neural radiance cache on the GPU: predictions and gradients against the
+numpy restatement (same BF16 rounding points), training, and the cache in
+the wavefront pass."""
+import numpy as np
+import pytest
+import torch
+
+from kiraray_gb300 import scenes
+from kiraray_gb300.nrc import NeuralRadianceCache
+from kiraray_gb300.wavefront import WavefrontPathTracer
+from oracle import nrc_ref as R
+
+pytestmark = pytest.mark.gpu
+
+SMALL = dict(n_levels=8, log2_table_size=14, base_resolution=4, max_resolution=128)
+
+
+def _records(n, seed):
+    rng = np.random.default_rng(seed)
+    r = np.zeros((n, 10), np.float32)
+    r[:, :3] = rng.random((n, 3)) * 2 - 1
+    nrm = rng.normal(size=(n, 3))
+    r[:, 3:6] = nrm / np.linalg.norm(nrm, axis=1, keepdims=True)
+    r[:, 6] = rng.random(n)
+    r[:, 7:10] = rng.random((n, 3))
+    return r
+
+
+def _targets(rec):
+    p = rec[:, :3].astype(np.float64)
+    return np.stack([1 + np.sin(3 * p[:, 0]), 1 + np.cos(2 * p[:, 1]) * p[:, 2],
+                     0.5 + rec[:, 7]], 1).astype(np.float32)
+
+
+def _oracle(cache, lo, hi):
+    info = cache.info()
+    grid = R.Grid(info, lo, hi, 1 << cache.cfg.log2_table_size)
+    mlp = R.Mlp(cache.params(0).astype(np.float64), cache.cfg.hidden_layers + 1)
+    return grid, mlp, cache.params(1).astype(np.float64), info
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+
+
+def test_forward_matches_oracle(krr_lib, cuda):
+    lo, hi = (-1, -1, -1), (1, 1, 1)
+    cache = NeuralRadianceCache(lo, hi, **SMALL)
+    rec = _records(3000, 1)
+    # train a few steps so that the prediction is not near zero
+    for s in range(20):
+        cache.train_step(torch.from_numpy(rec).cuda(), torch.from_numpy(_targets(rec)).cuda())
+    got = cache.query(torch.from_numpy(rec).cuda()).cpu().numpy()
+    grid, mlp, table, _ = _oracle(cache, lo, hi)
+    X0, _ = R.encode(grid, table, rec)
+    want, _ = R.forward(mlp, X0)
+    assert _rel(got, want) < 2e-2
+    assert np.median(np.abs(got - want) / (np.abs(want) + 1e-3)) < 5e-3
+
+
+def test_gradients_match_oracle(krr_lib, cuda):
+    lo, hi = (-1, -1, -1), (1, 1, 1)
+    cache = NeuralRadianceCache(lo, hi, **SMALL)
+    rec = _records(4096, 2)
+    tgt = _targets(rec)
+    for s in range(5):
+        cache.train_step(torch.from_numpy(rec).cuda(), torch.from_numpy(tgt).cuda())
+    gm, gt, loss = cache.gradients(torch.from_numpy(rec).cuda(), torch.from_numpy(tgt).cuda())
+    grid, mlp, table, info = _oracle(cache, lo, hi)
+    X0, cs = R.encode(grid, table, rec)
+    y, acts = R.forward(mlp, X0)
+    want_loss, dy = R.loss_and_grad(y, tgt.astype(np.float64))
+    gW, dX0 = R.backward(mlp, acts, dy, loss_scale=cache.cfg.loss_scale)
+    gT = R.table_grad(grid, cs, dX0, info.n_table_entries)
+    assert abs(loss - want_loss) < 1e-2 * want_loss
+    o = 0
+    for l in range(mlp.layers):
+        rows = R.WIDTH if l + 1 < mlp.layers else R.OUT_PAD
+        g = gm[o:o + rows * R.IN].reshape(rows, R.IN)
+        o += rows * R.IN
+        assert _rel(g, gW[l]) < 3e-2, f"layer {l}"
+    assert _rel(gt, gT) < 3e-2
+
+
+def test_training_reduces_loss(krr_lib, cuda):
+    cache = NeuralRadianceCache((-1, -1, -1), (1, 1, 1), **SMALL)
+    rec = torch.from_numpy(_records(16384, 3)).cuda()
+    tgt = torch.from_numpy(_targets(rec.cpu().numpy())).cuda()
+    losses = [cache.train_step(rec, tgt) for _ in range(300)]
+    assert np.isfinite(losses).all()
+    assert np.mean(losses[-10:]) < 0.1 * np.mean(losses[:3])
+
+
+def test_cache_in_the_pass(krr_lib, cuda):
+    sc = scenes.cornell_box(96, 96, max_depth=5)
+    lo, hi = (0, 0, 0), (1, 1, 1)
+    plain = WavefrontPathTracer({"max_depth": 5})
+    plain.set_scene(sc)
+    plain.resize(96, 96)
+    pt = WavefrontPathTracer({"max_depth": 5})
+    pt.set_scene(sc)
+    pt.resize(96, 96)
+    cache = NeuralRadianceCache(lo, hi, batch_size=8192)
+    pt.set_nrc(cache, train=True)
+    acc_p = torch.zeros((96, 96, 4), device="cuda")
+    acc_n = torch.zeros((96, 96, 4), device="cuda")
+    for f in range(1, 121):
+        plain.begin_frame(f, sc.camera)
+        acc_p += plain.render()
+        pt.begin_frame(f, sc.camera)
+        img = pt.render()
+        if f > 60:
+            acc_n += img
+    assert pt.device_errors() == 0
+    assert cache.info().step == 120
+    mp = (acc_p / 120)[..., :3].mean().item()
+    mn = (acc_n / 60)[..., :3].mean().item()
+    assert torch.isfinite(acc_n).all()
+    assert abs(mn - mp) < 0.15 * mp, (mn, mp)
