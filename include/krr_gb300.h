@@ -294,6 +294,8 @@ typedef struct krr_nrc_config {
     int32_t train_pixel_stride;  /* 1 of this many pixels trains (16)        */
     uint32_t seed;
     float scene_lo[3], scene_hi[3];   /* box mapped to the unit cube         */
+    int32_t tensor_cores;        /* 1: forward passes on tcgen05 (default);
+                                    0: CUDA-core kernels (reference path) */
 } krr_nrc_config;
 
 typedef struct krr_nrc_info_t {

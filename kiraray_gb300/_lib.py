@@ -78,7 +78,8 @@ class NrcConfig(C.Structure):
                 ("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float),
                 ("epsilon", C.c_float), ("loss_scale", C.c_float), ("batch_size", C.c_int32),
                 ("train_pixel_stride", C.c_int32), ("seed", C.c_uint32),
-                ("scene_lo", C.c_float * 3), ("scene_hi", C.c_float * 3)]
+                ("scene_lo", C.c_float * 3), ("scene_hi", C.c_float * 3),
+                ("tensor_cores", C.c_int32)]
 
 
 class NrcInfo(C.Structure):

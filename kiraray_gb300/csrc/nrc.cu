@@ -40,6 +40,8 @@ struct krr_nrc {
     float *dA = nullptr, *dB = nullptr;      // [cap][64]
     float *loss = nullptr;                   // device loss accumulator
     int32_t *count_buf = nullptr;
+    uint8_t *packed = nullptr;               // weights in tcgen05 canonical tiles
+    uint32_t *err = nullptr;                 // device error flags
 };
 
 namespace {
@@ -346,9 +348,13 @@ int ensure_capacity(krr_nrc *n, int64_t cap) {
 
 // Forward pass over `cap` rows (live count on the device); leaves the layer
 // inputs in n->act and the output in n->out.
-int forward(krr_nrc *n, const float *d_inputs, const int32_t *d_count, int64_t cap, cudaStream_t s) {
+int forward(krr_nrc *n, const float *d_inputs, const int32_t *d_count, int64_t cap, cudaStream_t s,
+            bool keep_acts = true) {
     KRR_TRY(ensure_capacity(n, cap));
     __nv_bfloat16 *A = n->act;
+    if (n->cfg.tensor_cores)
+        return nrc_forward_tc(n->grid, n->mlp, d_inputs, d_count, cap, n->table, n->packed, n->out,
+                              keep_acts ? A : nullptr, n->err, s);
     k_encode<<<grid_for(cap), kThreads, 0, s>>>(n->grid, d_inputs, d_count, cap, n->table, A);
     KRR_CUDA(cudaGetLastError());
     int blocks = grid_for(cap, 128);
@@ -385,7 +391,7 @@ int32_t nrc_train_stride(const krr_nrc *n) { return n->cfg.train_pixel_stride; }
 int nrc_query_device(krr_nrc *n, const float *d_inputs, const int32_t *d_count, int64_t cap,
                      float *d_out, cudaStream_t s) {
     if (cap <= 0) return KRR_OK;
-    KRR_TRY(forward(n, d_inputs, d_count, cap, s));
+    KRR_TRY(forward(n, d_inputs, d_count, cap, s, false));
     k_write_rgb<<<grid_for(cap), kThreads, 0, s>>>(n->out, d_count, cap, d_out);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
@@ -437,6 +443,7 @@ int nrc_train_device(krr_nrc *n, const float *d_inputs, const float *d_targets,
                                              n->table, tn, c.learning_rate, c.beta1, c.beta2,
                                              c.epsilon, 1.f / scale, bc1, bc2, nullptr);
     KRR_CUDA(cudaGetLastError());
+    if (n->cfg.tensor_cores) KRR_TRY(nrc_pack_weights(n->weights, n->mlp, n->packed, s));
     return KRR_OK;
 }
 
@@ -460,6 +467,7 @@ extern "C" void krr_nrc_config_default(krr_nrc_config *c) {
     c->batch_size = 65536;
     c->train_pixel_stride = 16;
     c->seed = 3;
+    c->tensor_cores = 1;
     for (int k = 0; k < 3; ++k) { c->scene_lo[k] = 0.f; c->scene_hi[k] = 1.f; }
 }
 
@@ -538,11 +546,14 @@ extern "C" int krr_nrc_create(const krr_nrc_config *cfg, krr_nrc **out) {
     alloc((void **)&n->table_grad, tn * 4);
     alloc((void **)&n->table, tn * 2);
     alloc((void **)&n->loss, 16);
+    alloc((void **)&n->packed, (size_t)(m.layers - 1) * kNrcWidth * kNrcIn * 2 + kNrcOutPad * kNrcIn * 2);
+    alloc((void **)&n->err, 16);
     if (st == KRR_OK) {
         cudaMemcpy(n->w_master, w.data(), m.n_params * 4, cudaMemcpyHostToDevice);
         cudaMemcpy(n->table_master, t.data(), tn * 4, cudaMemcpyHostToDevice);
         k_to_bf16<<<grid_for(m.n_params), kThreads>>>(n->w_master, n->weights, m.n_params);
         k_to_bf16<<<grid_for((int64_t)tn), kThreads>>>(n->table_master, n->table, (int64_t)tn);
+        if (cfg->tensor_cores) nrc_pack_weights(n->weights, n->mlp, n->packed, 0);
         cudaError_t e = cudaDeviceSynchronize();
         if (e != cudaSuccess) st = cuda_status(e, "krr_nrc_create", __FILE__, __LINE__);
     }
@@ -560,7 +571,8 @@ extern "C" int krr_nrc_destroy(krr_nrc *n) {
     for (void *p : {(void *)n->table_master, (void *)n->table_m, (void *)n->table_v,
                     (void *)n->table_grad, (void *)n->table, (void *)n->w_master, (void *)n->w_m,
                     (void *)n->w_v, (void *)n->w_grad, (void *)n->weights, (void *)n->act,
-                    (void *)n->out, (void *)n->dA, (void *)n->dB, (void *)n->loss})
+                    (void *)n->out, (void *)n->dA, (void *)n->dB, (void *)n->loss,
+                    (void *)n->packed, (void *)n->err})
         cudaFree(p);
     delete n;
     return KRR_OK;
@@ -619,6 +631,7 @@ extern "C" int krr_nrc_set_params(krr_nrc *n, int32_t which, const float *h_src,
     KRR_CUDA(cudaDeviceSynchronize());
     KRR_CUDA(cudaMemcpy(dst, h_src, total * 4, cudaMemcpyHostToDevice));
     k_to_bf16<<<grid_for(total), kThreads>>>(dst, bdst, total);
+    if (which == 0 && n->cfg.tensor_cores) KRR_TRY(nrc_pack_weights(n->weights, n->mlp, n->packed, 0));
     KRR_CUDA(cudaDeviceSynchronize());
     return KRR_OK;
 }

@@ -52,5 +52,11 @@ int nrc_query_device(krr_nrc *n, const float *d_inputs, const int32_t *d_count, 
 int nrc_train_device(krr_nrc *n, const float *d_inputs, const float *d_targets,
                      const int32_t *d_count, int64_t capacity, cudaStream_t s);
 int64_t nrc_batch_size(const krr_nrc *n);
+// tcgen05 forward (nrc_tc.cu)
+size_t nrc_tc_smem_bytes(int layers);
+int nrc_pack_weights(const __nv_bfloat16 *w, const NrcMlp &mlp, uint8_t *packed, cudaStream_t s);
+int nrc_forward_tc(const NrcGrid &g, const NrcMlp &mlp, const float *d_in, const int32_t *d_count,
+                   int64_t cap, const __nv_bfloat16 *table, const uint8_t *packed, float *d_out,
+                   __nv_bfloat16 *acts, uint32_t *err, cudaStream_t s);
 int32_t nrc_train_stride(const krr_nrc *n);
 }  // namespace krr

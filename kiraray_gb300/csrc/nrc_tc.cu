@@ -1,0 +1,335 @@
+// Fused neural-radiance-cache forward pass on the 5th-generation tensor
+// cores (tcgen05), one 128-row tile of queries at a time per CTA.
+//
+// Per tile: the 128 threads encode their query (hash grid, trilinear) into
+// a 128x64 BF16 activation tile in shared memory; then for each of the six
+// layers one elected thread issues four tcgen05.mma.kind::f16 (M=128,
+// N=64 or 16, K=16, BF16 x BF16 -> FP32 in tensor memory), commits them to
+// an mbarrier, and all threads read the accumulator rows back with
+// tcgen05.ld, apply ReLU, round to BF16 and write the next activation tile
+// (or the RGB output).  All weights (43 KB, BF16) stay resident in shared
+// memory for the CTA's lifetime.  Waits on the mbarrier are bounded: a wait
+// that gives up sets an error flag and the CTA frees its tensor memory and
+// returns.
+//
+// Shared-memory operands use the canonical K-major layout without swizzle:
+// 8x8-element core matrices of 128 contiguous bytes, core (i, j) of a tile
+// with 64 columns at byte ((i * 8) + j) * 128, so the leading-dimension
+// byte offset (next core along K) is 128 and the stride-dimension byte
+// offset (next 8-row group) is 1024.
+#include <algorithm>
+
+#include "nrc.h"
+
+namespace krr {
+
+constexpr int kTcRows = 128;
+constexpr int kTcThreads = 128;
+constexpr uint32_t kTcCols = 64;                 // tensor-memory columns per CTA
+constexpr int kLayerBytes = kNrcWidth * kNrcIn * 2;     // 8 KB
+constexpr int kOutBytes = kNrcOutPad * kNrcIn * 2;      // 2 KB
+constexpr uint32_t kWaitLimit = 1u << 26;
+
+namespace {
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor (tcgen05): start address, leading and
+// stride byte offsets (all >> 4), descriptor version 1 at bit 46, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo & 0x3FFFFu) >> 4) << 16) |
+           ((uint64_t)((sbo & 0x3FFFFu) >> 4) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator (bits 4-5 = 1), A and
+// B BF16 (bits 7-9 and 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4
+// at bit 24.
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+           ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                       uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ uint32_t mbar_try_wait(uint32_t mbar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    return ok;
+}
+
+__device__ __forceinline__ void fence_before_sync() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after_sync() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+        "%11, %12, %13, %14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_wait_ld() {
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Byte offset of element (r, k) in a canonical K-major tile of 64 columns.
+__host__ __device__ __forceinline__ uint32_t canon(uint32_t r, uint32_t k) {
+    return (((r >> 3) * 8u + (k >> 3)) * 128u) + (r & 7u) * 16u + (k & 7u) * 2u;
+}
+
+// Writes one row (64 values) of a canonical tile as eight 16-byte chunks.
+__device__ __forceinline__ void store_row(uint8_t *tile, uint32_t r, const float *v) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        __nv_bfloat162 p0 = __floats2bfloat162_rn(v[8 * j + 0], v[8 * j + 1]);
+        __nv_bfloat162 p1 = __floats2bfloat162_rn(v[8 * j + 2], v[8 * j + 3]);
+        __nv_bfloat162 p2 = __floats2bfloat162_rn(v[8 * j + 4], v[8 * j + 5]);
+        __nv_bfloat162 p3 = __floats2bfloat162_rn(v[8 * j + 6], v[8 * j + 7]);
+        uint4 q;
+        q.x = *reinterpret_cast<uint32_t *>(&p0);
+        q.y = *reinterpret_cast<uint32_t *>(&p1);
+        q.z = *reinterpret_cast<uint32_t *>(&p2);
+        q.w = *reinterpret_cast<uint32_t *>(&p3);
+        *reinterpret_cast<uint4 *>(tile + canon(r, 8 * j)) = q;
+    }
+}
+
+// Packs the BF16 weights [layer][out][64] into canonical tiles.
+__global__ void k_pack_weights(const __nv_bfloat16 *__restrict__ w, NrcMlp mlp, uint8_t *packed) {
+    int total = mlp.n_params;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        int l = 0;
+        while (l + 1 < mlp.layers && e >= mlp.w_offset[l + 1]) ++l;
+        int local = e - mlp.w_offset[l];
+        int r = local / kNrcIn, k = local % kNrcIn;
+        *reinterpret_cast<__nv_bfloat16 *>(packed + (size_t)l * kLayerBytes + canon(r, k)) = w[e];
+    }
+}
+
+__device__ __forceinline__ void encode_row(const NrcGrid &g, const float *q,
+                                           const __nv_bfloat16 *__restrict__ table, float *x) {
+    float p[3];
+    for (int a = 0; a < 3; ++a) p[a] = fminf(fmaxf((q[a] - g.lo[a]) * g.inv_extent[a], 0.f), 1.f);
+    for (int l = 0; l < kNrcMaxLevels; ++l) {
+        if (l >= g.levels) break;
+        float fr[3];
+        uint32_t base[3];
+        for (int a = 0; a < 3; ++a) {
+            float s = p[a] * (float)g.res[l];
+            float fl = fminf(fmaxf(floorf(s), 0.f), (float)(g.res[l] - 1));
+            base[a] = (uint32_t)fl;
+            fr[a] = fminf(fmaxf(s - fl, 0.f), 1.f);
+        }
+        uint32_t n1 = (uint32_t)g.res[l] + 1u;
+        bool dense = g.dense_mask & (1u << l);
+        float f0 = 0.f, f1 = 0.f;
+        for (int k = 0; k < 8; ++k) {
+            uint32_t xx = base[0] + (k & 1), yy = base[1] + ((k >> 1) & 1), zz = base[2] + ((k >> 2) & 1);
+            uint32_t idx = dense ? xx + n1 * (yy + n1 * zz)
+                                 : (xx ^ (yy * 2654435761u) ^ (zz * 805459861u)) & (g.table_size - 1u);
+            idx += g.offset[l];
+            float w = ((k & 1) ? fr[0] : 1.f - fr[0]) * (((k >> 1) & 1) ? fr[1] : 1.f - fr[1]) *
+                      (((k >> 2) & 1) ? fr[2] : 1.f - fr[2]);
+            __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162 *>(table + 2 * (size_t)idx);
+            f0 += w * __bfloat162float(v.x);
+            f1 += w * __bfloat162float(v.y);
+        }
+        x[2 * l] = f0;
+        x[2 * l + 1] = f1;
+    }
+    int o = 2 * g.levels;
+    for (int a = 0; a < 3; ++a) x[o + a] = (q[3 + a] + 1.f) * 0.5f;
+    x[o + 3] = q[6];
+    for (int a = 0; a < 3; ++a) x[o + 4 + a] = q[7 + a];
+    for (int k = o + 7; k < kNrcIn; ++k) x[k] = 0.f;
+}
+
+// out[i][0..3) for i < *count (or cap); optional per-layer activation dump
+// (bf16 [layers][cap][64], row-major) for the training backward pass.
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_nrc_forward_tc(NrcGrid g, int layers, const float *__restrict__ in, const int32_t *d_count,
+                 int64_t cap, const __nv_bfloat16 *__restrict__ table,
+                 const uint8_t *__restrict__ packed_w, float *__restrict__ out,
+                 __nv_bfloat16 *__restrict__ acts, uint32_t *err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *sw = smem;                                              // weights
+    uint8_t *sa = smem + (layers - 1) * kLayerBytes + kOutBytes;     // activation tile
+    sa = reinterpret_cast<uint8_t *>(((uintptr_t)sa + 1023) & ~(uintptr_t)1023);
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(sa + kTcRows * kNrcIn * 2);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
+    uint32_t *fail_flag = tmem_slot + 1;
+    const int tid = threadIdx.x, warp = tid >> 5;
+
+    // weights -> shared memory (16-byte copies)
+    int wbytes = (layers - 1) * kLayerBytes + kOutBytes;
+    for (int e = tid; e < wbytes / 16; e += blockDim.x)
+        reinterpret_cast<uint4 *>(sw)[e] = reinterpret_cast<const uint4 *>(packed_w)[e];
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tmem_slot)),
+                     "r"(kTcCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        mbar_init(smem_u32(mbar), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t my_lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+
+    int64_t n = d_count ? min((int64_t)*d_count, cap) : cap;
+    int64_t tiles = (n + kTcRows - 1) / kTcRows;
+    uint32_t phase = 0;
+    bool failed = false;
+    float x[kNrcIn];
+    for (int64_t t = blockIdx.x; t < tiles && !failed; t += gridDim.x) {
+        int64_t row = t * kTcRows + tid;
+        if (row < n) encode_row(g, in + kNrcInputs * row, table, x);
+        else
+            for (int k = 0; k < kNrcIn; ++k) x[k] = 0.f;
+        store_row(sa, (uint32_t)tid, x);
+        if (acts && row < n) {
+            for (int k = 0; k < kNrcIn; ++k) acts[row * kNrcIn + k] = __float2bfloat16_rn(x[k]);
+        }
+        fence_proxy_async();
+        fence_before_sync();
+        __syncthreads();
+        for (int l = 0; l < layers; ++l) {
+            const bool last = l + 1 == layers;
+            const int nrows = last ? kNrcOutPad : kNrcWidth;
+            if (tid == 0) {
+                fence_after_sync();
+                const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sw + l * kLayerBytes);
+                const uint32_t idesc = idesc_bf16(kTcRows, nrows);
+#pragma unroll
+                for (int kk = 0; kk < kNrcIn / 16; ++kk)
+                    tc_mma(tmem, smem_desc(a0 + 256u * kk, 128u, 1024u),
+                           smem_desc(b0 + 256u * kk, 128u, 1024u), idesc, kk > 0 ? 1u : 0u);
+                tc_commit(smem_u32(mbar));
+            }
+            // thread 0 waits for the accumulator (bounded) and tells the
+            // others; the decision to stop is uniform across the CTA
+            if (tid == 0) {
+                uint32_t spins = 0, ok = 0;
+                while (!(ok = mbar_try_wait(smem_u32(mbar), phase)) && ++spins < kWaitLimit) {
+                }
+                *fail_flag = ok ? 0u : 1u;
+                if (!ok) atomicOr(err, (uint32_t)kErrLoopLimit);
+            }
+            __syncthreads();
+            if (*fail_flag) {
+                failed = true;
+                break;
+            }
+            {
+                uint32_t spins = 0;   // already complete: returns at once
+                while (!mbar_try_wait(smem_u32(mbar), phase) && ++spins < kWaitLimit) {
+                }
+            }
+            phase ^= 1u;
+            fence_after_sync();
+            float v[kNrcIn];
+            tmem_ld16(my_lane_addr + 0, v);
+            if (!last) {
+                tmem_ld16(my_lane_addr + 16, v + 16);
+                tmem_ld16(my_lane_addr + 32, v + 32);
+                tmem_ld16(my_lane_addr + 48, v + 48);
+            }
+            tmem_wait_ld();
+            if (!last) {
+                for (int k = 0; k < kNrcIn; ++k) v[k] = fmaxf(v[k], 0.f);
+                store_row(sa, (uint32_t)tid, v);
+                if (acts && row < n) {
+                    __nv_bfloat16 *dst = acts + ((size_t)(l + 1) * cap + row) * kNrcIn;
+                    for (int k = 0; k < kNrcIn; ++k) dst[k] = __float2bfloat16_rn(v[k]);
+                }
+                fence_proxy_async();
+            } else if (row < n) {
+                out[row * kNrcOutPad + 0] = v[0];
+                out[row * kNrcOutPad + 1] = v[1];
+                out[row * kNrcOutPad + 2] = v[2];
+            }
+            fence_before_sync();
+            __syncthreads();
+        }
+    }
+    fence_after_sync();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols));
+}
+
+}  // namespace
+
+size_t nrc_tc_smem_bytes(int layers) {
+    size_t w = (size_t)(layers - 1) * kLayerBytes + kOutBytes;
+    size_t a = ((w + 1023) & ~(size_t)1023) + kTcRows * kNrcIn * 2;
+    return a + 64 + 1024;   // mbarrier, tensor-memory slot, alignment slack
+}
+
+int nrc_pack_weights(const __nv_bfloat16 *w, const NrcMlp &mlp, uint8_t *packed, cudaStream_t s) {
+    cudaMemsetAsync(packed, 0, (size_t)(mlp.layers - 1) * kLayerBytes + kOutBytes, s);
+    k_pack_weights<<<64, 256, 0, s>>>(w, mlp, packed);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+int nrc_forward_tc(const NrcGrid &g, const NrcMlp &mlp, const float *d_in, const int32_t *d_count,
+                   int64_t cap, const __nv_bfloat16 *table, const uint8_t *packed, float *d_out,
+                   __nv_bfloat16 *acts, uint32_t *err, cudaStream_t s) {
+    static bool configured = false;
+    size_t smem = nrc_tc_smem_bytes(mlp.layers);
+    if (!configured) {
+        KRR_CUDA(cudaFuncSetAttribute(k_nrc_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+        configured = true;
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int64_t tiles = (cap + kTcRows - 1) / kTcRows;
+    int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sms * 2));
+    k_nrc_forward_tc<<<grid, kTcThreads, smem, s>>>(g, mlp.layers, d_in, d_count, cap, table, packed,
+                                                    d_out, acts, err);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+}  // namespace krr

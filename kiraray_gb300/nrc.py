@@ -17,7 +17,7 @@ from ._lib import check
 
 CONFIG_KEYS = ("n_levels", "features_per_level", "log2_table_size", "base_resolution",
                "max_resolution", "hidden_layers", "learning_rate", "beta1", "beta2", "epsilon",
-               "loss_scale", "batch_size", "train_pixel_stride", "seed")
+               "loss_scale", "batch_size", "train_pixel_stride", "seed", "tensor_cores")
 
 
 def _stream() -> int:

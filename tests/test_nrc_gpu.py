@@ -82,6 +82,30 @@ def test_gradients_match_oracle(krr_lib, cuda):
     assert _rel(gt, gT) < 3e-2
 
 
+def test_tensor_core_forward_matches_cuda_core_kernels(krr_lib, cuda):
+    """tcgen05 BF16 MMAs (FP32 accumulation in tensor memory) against the
+    CUDA-core kernels with the same BF16 rounding points."""
+    lo, hi = (-1, -1, -1), (1, 1, 1)
+    tc = NeuralRadianceCache(lo, hi, tensor_cores=1, **SMALL)
+    ref = NeuralRadianceCache(lo, hi, tensor_cores=0, **SMALL)
+    rec = _records(10000, 5)
+    for _ in range(30):
+        tc.train_step(torch.from_numpy(rec[:4096]).cuda(),
+                      torch.from_numpy(_targets(rec[:4096])).cuda())
+    ref.set_params(0, tc.params(0))
+    ref.set_params(1, tc.params(1))
+    q = torch.from_numpy(rec).cuda()
+    a = tc.query(q).cpu().numpy()
+    b = ref.query(q).cpu().numpy()
+    assert np.isfinite(a).all()
+    assert _rel(a, b) < 1e-2
+    assert np.median(np.abs(a - b) / (np.abs(b) + 1e-3)) < 2e-3
+    # tile edges: counts that are not multiples of 128 rows
+    for n in (1, 127, 129, 1000):
+        aa = tc.query(q[:n].contiguous()).cpu().numpy()
+        assert np.allclose(aa, a[:n], rtol=0, atol=1e-6)
+
+
 def test_training_reduces_loss(krr_lib, cuda):
     cache = NeuralRadianceCache((-1, -1, -1), (1, 1, 1), **SMALL)
     rec = torch.from_numpy(_records(16384, 3)).cuda()
