@@ -216,6 +216,9 @@ def run_ours(args, rank, world, local):
     sets = [(rays0, hits0), (rays1, hits1)]
     n_per_step = rays0.shape[0] + rays1.shape[0]
 
+    # autotuner: traversal settings for this workload (outside the timed region)
+    tuning = acc.autotune(rays0, repeats=2)
+
     # algorithmic bytes per ray from a counter-instrumented replay
     node_visits = tri_tests = 0
     for r, _ in sets:
@@ -298,6 +301,8 @@ def run_ours(args, rank, world, local):
                    "bvh_build_ms": stats["build_ms"], "bvh_nodes": int(stats["n_nodes"]),
                    "bvh_depth": int(stats["max_depth"]),
                    "nodes_per_ray": node_visits / n_per_step, "tris_per_ray": tri_tests / n_per_step,
+                   "tuning": {"refill_below": tuning["refill_below"],
+                              "postpone_pct": tuning["postpone_pct"]},
                    "parallelism": f"replicas{world}"},
         "e2e": e2e,
         "gpu_launches": args.steps * len(sets),

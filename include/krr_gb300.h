@@ -201,6 +201,16 @@ int krr_accel_trace_stats(const krr_accel *accel, const krr_ray *d_rays, int64_t
 int krr_accel_trace_stats_noalloc(const krr_accel *accel, const krr_ray *d_rays, int64_t n,
                                   int32_t any_hit, unsigned long long *h_counts, void *stream);
 
+/* Traversal tuning: refill a warp's idle lanes from the ray counter when
+ * fewer than refill_below (1..32) lanes are busy; postpone a node's
+ * triangles while fewer than postpone_pct % of the busy lanes have
+ * triangles (0 = never).  Defaults 20 and 0.  Results do not depend on it. */
+int krr_accel_set_tuning(krr_accel *accel, int32_t refill_below, int32_t postpone_pct);
+/* Autotuner: times closest-hit traversal of the given rays for a grid of
+ * tuning settings (repeats launches each) and keeps the fastest. */
+int krr_accel_autotune(krr_accel *accel, const krr_ray *d_rays, int64_t n, int32_t repeats,
+                       int32_t *out_refill, int32_t *out_postpone, float *out_ms, void *stream);
+
 /* Same as krr_accel_trace_closest, with host buffers: copies the rays in and
  * the hits out inside the call (pinned host memory is fastest). */
 int krr_accel_trace_closest_host(const krr_accel *accel, const krr_ray *h_rays, int64_t n,

@@ -109,6 +109,9 @@ SIGNATURES = {
     "krr_accel_trace_any": (_I, [_P, _P, C.c_int64, _P, _P]),
     "krr_accel_set_mask": (_I, [_P, _P]),
     "krr_accel_trace_closest_host": (_I, [_P, _P, C.c_int64, _P, _P]),
+    "krr_accel_set_tuning": (_I, [_P, C.c_int32, C.c_int32]),
+    "krr_accel_autotune": (_I, [_P, _P, C.c_int64, C.c_int32, C.POINTER(C.c_int32),
+                                C.POINTER(C.c_int32), C.POINTER(C.c_float), _P]),
     "krr_accel_trace_stats": (_I, [_P, _P, C.c_int64, C.c_int32, C.POINTER(C.c_ulonglong), _P]),
     "krr_accel_trace_stats_noalloc": (_I, [_P, _P, C.c_int64, C.c_int32,
                                            C.POINTER(C.c_ulonglong), _P]),

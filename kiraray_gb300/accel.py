@@ -85,6 +85,18 @@ class Accel:
               "krr_accel_trace_stats")
         return int(counts[0]), int(counts[1])
 
+    def set_tuning(self, refill_below: int = 20, postpone_pct: int = 0) -> None:
+        check(_lib.load().krr_accel_set_tuning(self._h, refill_below, postpone_pct), "set_tuning")
+
+    def autotune(self, rays: torch.Tensor, repeats: int = 3) -> dict:
+        """Picks the fastest traversal tuning for these rays (autotuner)."""
+        rays = self._rays(rays)
+        rf, pp, ms = C.c_int32(), C.c_int32(), C.c_float()
+        check(_lib.load().krr_accel_autotune(self._h, rays.data_ptr(), rays.shape[0], repeats,
+                                             C.byref(rf), C.byref(pp), C.byref(ms), _stream()),
+              "krr_accel_autotune")
+        return {"refill_below": rf.value, "postpone_pct": pp.value, "ms": ms.value}
+
     def set_mask(self, mask: np.ndarray | None) -> None:
         m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
         check(_lib.load().krr_accel_set_mask(self._h, None if m is None else m.ctypes.data),

@@ -34,7 +34,6 @@ namespace {
 
 constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr int kBuildThreads = 256;
-constexpr int kRefillBelow = 20;   // refill a warp when fewer lanes are busy
 
 __device__ __forceinline__ void atomic_min_f(float *addr, float v) {
     if (v >= 0.f) atomicMin(reinterpret_cast<int *>(addr), __float_as_int(v));
@@ -400,7 +399,7 @@ k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, Trace
 
     while (true) {
         unsigned act = __ballot_sync(0xffffffffu, active);
-        if (__popc(act) < kRefillBelow && !exhausted) {
+        if (__popc(act) < L.refill_below && !exhausted) {
             unsigned need = ~act;
             int leader = __ffs(need) - 1;
             long long base = 0;
@@ -429,11 +428,11 @@ k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, Trace
             act = __ballot_sync(0xffffffffu, active);
         }
         if (act == 0) break;
-        if (!active) continue;
 
-        // ---- one traversal step: optional node visit, its triangles, pop
-        bool done = false;
-        if (ng.y & 0xffu) {
+        // ---- one traversal step, all lanes together: optional node visit,
+        // triangles (possibly postponed), pop
+        bool done = false, fresh = false;
+        if (active && (ng.y & 0xffu)) {
             int p = __ffs(ng.y & 0xffu) - 1;
             ng.y &= ~(1u << p);
             int slot = p ^ oct;
@@ -445,8 +444,19 @@ k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, Trace
             }
             if (STATS) ++n_nodes;
             visit_node(nodes, child, r, inv, oct, tmax, ng, tg);
+            fresh = true;
         }
-        while (tg.y && !done) {
+        // Postpone a fresh triangle group onto the stack while too few lanes
+        // of the warp have triangles to test (keeps the warp on node work).
+        if (L.postpone_pct > 0) {
+            unsigned tri_lanes = __ballot_sync(0xffffffffu, active && tg.y != 0u);
+            if (active && fresh && tg.y && __popc(tri_lanes) * 100 < L.postpone_pct * __popc(act) &&
+                (ng.y & 0xffu) && sp < kTraversalStack) {
+                stack[sp++] = make_uint2(tg.x, tg.y | 0x80000000u);
+                tg.y = 0;
+            }
+        }
+        while (active && tg.y && !done) {
             int b = __ffs(tg.y) - 1;
             tg.y &= tg.y - 1u;
             const float4 *tp = tris + 3 * (size_t)(tg.x + b);
@@ -466,10 +476,16 @@ k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, Trace
                 }
             }
         }
-        if (!done && !(ng.y & 0xffu)) {
-            if (sp > 0) ng = stack[--sp];
-            else done = true;
+        if (active && !done && !(ng.y & 0xffu) && tg.y == 0u) {
+            if (sp > 0) {
+                uint2 e = stack[--sp];
+                if (e.y & 0x80000000u) tg = make_uint2(e.x, e.y & 0x00ffffffu);
+                else ng = e;
+            } else {
+                done = true;
+            }
         }
+        if (!active) continue;
         if (done) {
             if (ANY) {
                 L.occluded[ray_id] = best_prim != KRR_MISS ? 1 : 0;
@@ -509,7 +525,10 @@ static int launch_trace(const krr_accel *a, const TraceLaunch &l, cudaStream_t s
     if (!a || !a->d_nodes) return fail(KRR_ERR_NOT_READY, "acceleration structure not built");
     KRR_CUDA(cudaMemsetAsync(l.counter, 0, sizeof(unsigned long long), s));
     if (a->n_tris == 0) return KRR_OK;
-    k_trace<ANY, STATS><<<traversal_grid_size(), kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, l, stats);
+    TraceLaunch lt = l;
+    lt.refill_below = a->refill_below;
+    lt.postpone_pct = a->postpone_pct;
+    k_trace<ANY, STATS><<<traversal_grid_size(), kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, lt, stats);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }
@@ -834,5 +853,62 @@ extern "C" int krr_accel_trace_closest_host(const krr_accel *a, const krr_ray *h
     cudaFreeAsync(d_hits, s);
     e = cudaStreamSynchronize(s);
     if (st == KRR_OK && e != cudaSuccess) st = cuda_status(e, "cudaStreamSynchronize", __FILE__, __LINE__);
+    return st;
+}
+
+extern "C" int krr_accel_set_tuning(krr_accel *a, int32_t refill_below, int32_t postpone_pct) {
+    KRR_CHECK_ARG(a != nullptr, "accel is NULL");
+    KRR_CHECK_ARG(refill_below >= 1 && refill_below <= 32, "refill_below must be 1..32");
+    KRR_CHECK_ARG(postpone_pct >= 0 && postpone_pct <= 100, "postpone_pct must be 0..100");
+    a->refill_below = refill_below;
+    a->postpone_pct = postpone_pct;
+    return KRR_OK;
+}
+
+// Times the closest-hit kernel on the given rays for each candidate setting
+// (refill threshold x triangle-postponing threshold) and keeps the fastest.
+extern "C" int krr_accel_autotune(krr_accel *a, const krr_ray *d_rays, int64_t n, int32_t repeats,
+                                  int32_t *out_refill, int32_t *out_postpone, float *out_ms,
+                                  void *stream) {
+    KRR_CHECK_ARG(a && d_rays && n > 0, "bad argument");
+    if (a->n_tris == 0) return fail(KRR_ERR_NOT_READY, "empty acceleration structure");
+    cudaStream_t s = as_stream(stream);
+    float4 *hits = nullptr;
+    KRR_CUDA(cudaMalloc(&hits, n * sizeof(float4)));
+    TraceLaunch l = aos_launch(a, d_rays, n);
+    l.hits = hits;
+    const int refills[] = {12, 16, 20, 24, 28};
+    const int postpones[] = {0, 10, 20, 35};
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    int br = a->refill_below, bp = a->postpone_pct;
+    int st = KRR_OK;
+    for (int rf : refills) {
+        for (int pp : postpones) {
+            a->refill_below = rf;
+            a->postpone_pct = pp;
+            st = launch_trace_closest(a, l, s);   // warm-up
+            if (st != KRR_OK) break;
+            cudaEventRecord(e0, s);
+            for (int k = 0; k < std::max(1, repeats); ++k) st = launch_trace_closest(a, l, s);
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            ms /= std::max(1, repeats);
+            if (ms < best) { best = ms; br = rf; bp = pp; }
+        }
+        if (st != KRR_OK) break;
+    }
+    a->refill_below = br;
+    a->postpone_pct = bp;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(hits);
+    if (out_refill) *out_refill = br;
+    if (out_postpone) *out_postpone = bp;
+    if (out_ms) *out_ms = best;
     return st;
 }

@@ -37,6 +37,8 @@ struct krr_accel {
     uint32_t *d_leaf_of_prim = nullptr;  // global id -> leaf-order slot
     int *d_scratch = nullptr;    // [0] ray counter, [1] error flags
     float scene_lo[3] = {0, 0, 0}, scene_hi[3] = {0, 0, 0};
+    int refill_below = 20;       // traversal tuning (krr_accel_set_tuning)
+    int postpone_pct = 0;
 };
 
 namespace krr {
@@ -58,6 +60,8 @@ struct TraceLaunch {
     uint8_t *occluded;        // any-hit output
     int *counter;             // scratch work counter (zeroed by the launcher)
     int *err;                 // device error flags
+    int refill_below;         // refill a warp's idle lanes when fewer lanes are busy
+    int postpone_pct;         // postpone triangles when fewer % of busy lanes have some
 };
 
 int launch_trace_closest(const krr_accel *a, const TraceLaunch &l, cudaStream_t s);

@@ -160,3 +160,26 @@ def test_full_size_scene_sampled(krr_lib, cuda):
     _assert_bits_equal(_gpu_closest(acc, rays), want, "10M camera rays")
     b = H.bounce_rays(tris, rays, want, 6)
     _assert_bits_equal(_gpu_closest(acc, b), ob.closest(b), "10M bounce rays")
+
+
+@pytest.mark.parametrize("refill,postpone", [(12, 0), (28, 0), (20, 20), (24, 50)])
+def test_tuning_settings_keep_hits_identical(krr_lib, cuda, refill, postpone):
+    sc = scenes.large_scene(width=160, height=90, grid=384, n_spheres=80, sky_size=(64, 32))
+    tris = sc.world_triangles()
+    rays = H.pinhole_rays(sc, jitter_seed=3)
+    acc = Accel(tris)
+    acc.set_tuning(refill, postpone)
+    ob = O.Bvh(tris)
+    want = ob.closest(rays)
+    _assert_bits_equal(_gpu_closest(acc, rays), want, f"tuning {refill}/{postpone}")
+    b = H.bounce_rays(tris, rays, want, 8)
+    _assert_bits_equal(_gpu_closest(acc, b), ob.closest(b), f"tuning {refill}/{postpone} bounce")
+    occ = acc.trace_any(torch.from_numpy(b).cuda()).cpu().numpy()
+    assert np.array_equal(occ, ob.any(b))
+
+
+def test_autotune_picks_a_setting(krr_lib, cuda):
+    sc = scenes.large_scene(width=160, height=90, grid=256, n_spheres=20, sky_size=(64, 32))
+    acc = Accel(sc.world_triangles())
+    res = acc.autotune(torch.from_numpy(H.pinhole_rays(sc)).cuda(), repeats=1)
+    assert 1 <= res["refill_below"] <= 32 and 0 <= res["postpone_pct"] <= 100 and res["ms"] > 0
