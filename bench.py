@@ -38,6 +38,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--nrc-res", default="480x270",
+                    help="resolution of the time-to-relMSE comparison (0 = skip)")
+    ap.add_argument("--nrc-ref-frames", type=int, default=8192)
+    ap.add_argument("--nrc-max-frames", type=int, default=1024)
     return ap.parse_args()
 
 
@@ -156,6 +160,64 @@ def cpu_baseline(tris, ray_sets, seconds: float, threads: int):
     return {"value": n / el / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
             "sample": f"{n} rays (1-in-16 sample of the camera + first-bounce sets, cycled) in "
                       f"{el:.1f} s; oracle BVH build {build_s:.1f} s not included"}
+
+
+def time_to_relmse(args):
+    """Time to relMSE 0.01 of the plain tracer and of the neural-cache tracer
+    on the large scene (configs: max depth 8, 1 spp per frame), against an
+    FP64-accumulated reference rendered by the plain tracer."""
+    if args.nrc_res in ("0", "", "none"):
+        return None
+    import torch
+    from kiraray_gb300 import scenes
+    from kiraray_gb300.convergence import render_reference, time_to_error
+    from kiraray_gb300.nrc import NeuralRadianceCache
+    from kiraray_gb300.wavefront import WavefrontPathTracer
+
+    w, h = (int(x) for x in args.nrc_res.split("x"))
+    sc = scenes.large_scene(width=w, height=h, seed=3)
+    params = {"max_depth": 8}
+    plain = WavefrontPathTracer(params, seed=3)
+    plain.set_scene(sc)
+    plain.resize(w, h)
+    t0 = time.perf_counter()
+    ref = render_reference(plain, sc, args.nrc_ref_frames)
+    torch.cuda.synchronize()
+    ref_s = time.perf_counter() - t0
+    res_plain = time_to_error(plain, sc, ref, target=0.01, max_frames=args.nrc_max_frames,
+                              check_every=8)
+    tris = sc.world_triangles().reshape(-1, 3, 3)
+    lo, hi = tris.reshape(-1, 3).min(0), tris.reshape(-1, 3).max(0)
+    pt = WavefrontPathTracer(params, seed=3)
+    pt.set_scene(sc)
+    pt.resize(w, h)
+    cache = NeuralRadianceCache(lo, hi, seed=3)
+    pt.set_nrc(cache, train=True)
+    res_nrc = time_to_error(pt, sc, ref, target=0.01, max_frames=args.nrc_max_frames,
+                            check_every=8)
+    def extrapolated(res):
+        # unbiased estimator: relMSE ~ 1/frames, so t(0.01) ~ t_final * err / 0.01
+        c = res["curve"]
+        if res["seconds"] or not c["data"]:
+            return res["seconds"]
+        return c["timepoints"][-1] * c["data"][-1] / 0.01
+
+    out = {"resolution": f"{w}x{h}", "reference_frames": args.nrc_ref_frames,
+           "reference_seconds": round(ref_s, 2), "target_relmse": 0.01,
+           "plain_seconds": res_plain["seconds"], "plain_frames": res_plain["frames"],
+           "plain_final_relmse": res_plain["final_error"],
+           "nrc_seconds": res_nrc["seconds"], "nrc_frames": res_nrc["frames"],
+           "nrc_final_relmse": res_nrc["final_error"]}
+    if not res_plain["seconds"]:
+        out["plain_seconds_extrapolated"] = extrapolated(res_plain)
+    if res_nrc["seconds"]:
+        out["nrc_time_fraction"] = res_nrc["seconds"] / (res_plain["seconds"] or
+                                                         extrapolated(res_plain))
+    out["plain_curve_tail"] = list(zip(res_plain["curve"]["timesteps"][-3:],
+                                       [round(x, 5) for x in res_plain["curve"]["data"][-3:]]))
+    out["nrc_curve_tail"] = list(zip(res_nrc["curve"]["timesteps"][-3:],
+                                     [round(x, 5) for x in res_nrc["curve"]["data"][-3:]]))
+    return out
 
 
 def run_reference(args, rank):
@@ -288,6 +350,7 @@ def run_ours(args, rank, world, local):
     cpu = (cpu_baseline(tris, [rays_np, bounce_np], args.cpu_seconds, os.cpu_count() or 1)
            if args.cpu_seconds > 0 else None)
     clocks = clk.summary()
+    nrc = time_to_relmse(args)
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
@@ -314,6 +377,7 @@ def run_ours(args, rank, world, local):
                              "so the fraction is against the measured HBM copy bandwidth"},
         "cpu_baseline": cpu,
         "clocks": clocks,
+        "time_to_relmse": nrc,
     }
     print(json.dumps(line))
 

@@ -249,6 +249,27 @@ int krr_wf_begin_frame(krr_wf *wf, int64_t frame_index, const krr_camera_desc *c
  * row-major, row 0 at the top (the reference's y-flipped surface write). */
 int krr_wf_render(krr_wf *wf, float *d_out_rgba, void *stream);
 
+/* Batched views: many cameras of different sizes in one wavefront (one
+ * launch per stage per bounce).  krr_wf_resize_views replaces resize; each
+ * frame krr_wf_begin_frame_views gives the cameras (sizes must match) and
+ * per-view seeds (sample index = frame_index * spp + seed); render writes
+ * the views one after another, each row-major with row 0 at the top. */
+typedef struct krr_view {
+    krr_camera_desc camera;
+    int32_t width, height;
+    uint32_t seed;
+} krr_view;
+int krr_wf_resize_views(krr_wf *wf, const krr_view *views, int32_t n_views);
+int krr_wf_begin_frame_views(krr_wf *wf, int64_t frame_index, const krr_view *views,
+                             int32_t n_views, void *stream);
+/* Captures one whole frame (constants upload, beginFrame, render into
+ * d_out) into a CUDA graph on a non-default stream; krr_wf_launch_frame
+ * replays it for a new frame index (views NULL keeps the cameras).  Run one
+ * ordinary frame first so that every lazily sized buffer exists. */
+int krr_wf_capture_frame(krr_wf *wf, float *d_out, void *stream);
+int krr_wf_launch_frame(krr_wf *wf, int64_t frame_index, const krr_view *views, int32_t n_views,
+                        void *stream);
+
 /* Stage entry points, for stage-level tests and for subclasses in the manner
  * of PPGPathTracer (src/misc/render/ppg/integrator.h:13). */
 int krr_wf_generate_camera_rays(krr_wf *wf, void *stream);

@@ -57,6 +57,11 @@ class CameraDesc(C.Structure):
                 ("shutter_time", C.c_float), ("medium", C.c_int32)]
 
 
+class ViewDesc(C.Structure):
+    _fields_ = [("camera", CameraDesc), ("width", C.c_int32), ("height", C.c_int32),
+                ("seed", C.c_uint32)]
+
+
 class SceneDesc(C.Structure):
     _fields_ = [("meshes", C.POINTER(MeshDesc)), ("n_meshes", C.c_int32),
                 ("instances", C.POINTER(InstanceDesc)), ("n_instances", C.c_int32),
@@ -124,6 +129,10 @@ SIGNATURES = {
     "krr_wf_begin_frame": (_I, [_P, C.c_int64, C.POINTER(CameraDesc), _P]),
     "krr_wf_render": (_I, [_P, _P, _P]),
     "krr_wf_generate_camera_rays": (_I, [_P, _P]),
+    "krr_wf_resize_views": (_I, [_P, C.POINTER(ViewDesc), C.c_int32]),
+    "krr_wf_begin_frame_views": (_I, [_P, C.c_int64, C.POINTER(ViewDesc), C.c_int32, _P]),
+    "krr_wf_capture_frame": (_I, [_P, _P, _P]),
+    "krr_wf_launch_frame": (_I, [_P, C.c_int64, C.POINTER(ViewDesc), C.c_int32, _P]),
     "krr_wf_trace_closest": (_I, [_P, C.c_int32, _P]),
     "krr_wf_handle_hit": (_I, [_P, _P]),
     "krr_wf_handle_miss": (_I, [_P, _P]),

@@ -43,6 +43,26 @@ struct DevCamera {
     int32_t medium;
 };
 
+// One camera view of a batch: its pixels occupy [offset, offset + w*h) of
+// the pass's pixel state (row-major per view).
+struct DevView {
+    DevCamera cam;
+    int32_t w, h;
+    int64_t offset;
+    uint32_t sample_index;   // frame_index * spp + seed of the view
+    int32_t pad;
+};
+
+// Per-frame constants read by kernels from device memory (so that a frame
+// captured in a CUDA graph can be replayed with new values).
+struct FrameConst {
+    int32_t n_views;
+    int32_t nrc_offset;      // training pixels: (pixel + offset) % stride == 0
+    int64_t frame_index;
+};
+
+constexpr int kMaxViews = 256;
+
 enum { Q_RAY0 = 0, Q_RAY1 = 1, Q_MISS = 2, Q_HIT_LIGHT = 3, Q_SHADOW = 4, Q_SCATTER = 5,
        Q_MEDIUM_SAMPLE = 6, Q_MEDIUM_SCATTER = 7, Q_COUNT = 8 };
 static const int kChannels[Q_COUNT] = {kRayCh, kRayCh, kMissCh, kHitLightCh, kShadowCh,
@@ -67,6 +87,12 @@ struct krr_wf {
     uint8_t *occluded = nullptr;
     PixelState ps{};
     int grid = 0;
+    // view table (pinned host copy, device copy) and per-frame constants
+    DevView *h_views = nullptr, *d_views = nullptr;
+    FrameConst *h_frame = nullptr, *d_frame = nullptr;
+    int32_t n_views = 1;
+    std::vector<DevView> layout;           // views of the current layout (w, h, offset)
+    cudaGraphExec_t graph = nullptr;       // captured frame (krr_wf_capture_frame)
     // neural radiance cache hooks
     krr_nrc *nrc = nullptr;
     bool nrc_train = false;
@@ -323,48 +349,69 @@ __device__ LightSample sample_li(const DevScene &s, const DevLight &l, float u0,
 namespace {
 
 // ---------------------------------------------------------------- kernels
-// beginFrame, integrator.cpp:205-221
-__global__ void k_begin_frame(PixelState ps, int w, int64_t n, uint32_t sample_index) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        uint32_t x = (uint32_t)(i % w), y = (uint32_t)(i / w);
+// View owning global pixel g (binary search over view offsets).
+__device__ __forceinline__ int view_of(const DevView *__restrict__ v, int n_views, int64_t g) {
+    int lo = 0, hi = n_views - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (v[mid].offset <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// beginFrame, integrator.cpp:205-221 (per view: pixel coordinates and the
+// advance(256 * pixelId) are view-local)
+__global__ void k_begin_frame(PixelState ps, const DevView *__restrict__ views,
+                              const FrameConst *__restrict__ fc, int64_t n) {
+    const int nv = fc->n_views;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        const DevView &v = views[view_of(views, nv, g)];
+        int64_t i = g - v.offset;
+        uint32_t x = (uint32_t)(i % v.w), y = (uint32_t)(i / v.w);
         Pcg p;
-        p.set_seed(interleave_32bit(x, y), sample_index);
+        p.set_seed(interleave_32bit(x, y), v.sample_index);
         p.advance(256 * i);
         float u = p.get1d();
         float lambda0 = (1.f - u) * 360.f + u * 830.f;   // sampleUniform, spectrum.h:47-58
-        ps.L[i] = make_float4(0.f, 0.f, 0.f, lambda0);
-        ps.pixel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        store_rng(ps, (uint32_t)i, p);
+        ps.L[g] = make_float4(0.f, 0.f, 0.f, lambda0);
+        ps.pixel[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+        store_rng(ps, (uint32_t)g, p);
     }
 }
 
 // generateCameraRays + CameraData::getRay, integrator.cpp:166-179, camera.h:32-58
-__global__ void k_camera_rays(PixelState ps, Queue rq, DevCamera cam, int w, int h, int64_t n) {
+__global__ void k_camera_rays(PixelState ps, Queue rq, const DevView *__restrict__ views,
+                              const FrameConst *__restrict__ fc, int64_t n) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *rq.count = (int32_t)n;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        Pcg p = load_rng(ps, (uint32_t)i);
+    const int nv = fc->n_views;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        const DevView &v = views[view_of(views, nv, g)];
+        const DevCamera &cam = v.cam;
+        int64_t i = g - v.offset;
+        Pcg p = load_rng(ps, (uint32_t)g);
         float fx = p.get1d(), fy = p.get1d();
         float lx = p.get1d(), ly = p.get1d();
         float tm = p.get1d();
-        store_rng(ps, (uint32_t)i, p);
+        store_rng(ps, (uint32_t)g, p);
         (void)lx; (void)ly;
-        float px = (float)(i % w) + 0.5f + fx;
-        float py = (float)(i / w) + 0.5f + fy;
-        float ndcx = (2 * px) / (float)w + (-1.f);
-        float ndcy = (2 * py) / (float)h + (-1.f);
+        float px = (float)(i % v.w) + 0.5f + fx;
+        float py = (float)(i / v.w) + 0.5f + fy;
+        float ndcx = (2 * px) / (float)v.w + (-1.f);
+        float ndcy = (2 * py) / (float)v.h + (-1.f);
         V3 fd = normalize(V3{cam.tan_fov * cam.aspect * ndcx, cam.tan_fov * ndcy, -1.f});
         V3 o = V3{cam.pos[0], cam.pos[1], cam.pos[2]};
         V3 d = mat3_mul(cam.rot, fd);
         float time = cam.shutter_open + cam.shutter_time * tm;
-        rq.at(0, i) = f4(o, 0.f);
-        rq.at(1, i) = f4(d, INFINITY);
-        rq.at(2, i) = make_float4(0.f, 0.f, 0.f, ibits(cam.medium));
-        rq.at(3, i) = make_float4(0.f, 0.f, 0.f, fbits(0u));
-        rq.at(4, i) = make_float4(1.f, 1.f, 1.f, fbits(0u));
-        rq.at(5, i) = make_float4(1.f, 1.f, 1.f, fbits((uint32_t)i));
-        rq.at(6, i) = make_float4(1.f, 1.f, 1.f, time);
+        rq.at(0, g) = f4(o, 0.f);
+        rq.at(1, g) = f4(d, INFINITY);
+        rq.at(2, g) = make_float4(0.f, 0.f, 0.f, ibits(cam.medium));
+        rq.at(3, g) = make_float4(0.f, 0.f, 0.f, fbits(0u));
+        rq.at(4, g) = make_float4(1.f, 1.f, 1.f, fbits(0u));
+        rq.at(5, g) = make_float4(1.f, 1.f, 1.f, fbits((uint32_t)g));
+        rq.at(6, g) = make_float4(1.f, 1.f, 1.f, time);
     }
 }
 
@@ -385,7 +432,8 @@ __device__ __forceinline__ void copy_ray_item(const Queue &src, int i, const Que
 // pixel / stride.
 struct NrcHook {
     int32_t mode;
-    int32_t stride, offset;
+    int32_t stride;
+    const FrameConst *frame;   // offset = frame->nrc_offset
     float *q_in;
     float4 *q_meta;
     int32_t *q_count;
@@ -408,7 +456,7 @@ __device__ __forceinline__ bool nrc_vertex(const NrcHook &h, const DevScene &s, 
                                            const PixelState &ps, uint32_t pixel, uint32_t depth,
                                            uint32_t bsdf_type, V3 thp, uint32_t *err) {
     if (!h.mode || depth < 1 || !(bsdf_type & BSDF_SMOOTH)) return false;
-    if ((pixel + (uint32_t)h.offset) % (uint32_t)h.stride == 0u) {
+    if ((pixel + (uint32_t)h.frame->nrc_offset) % (uint32_t)h.stride == 0u) {
         if (!h.rec) return false;
         uint32_t slot = pixel / (uint32_t)h.stride;
         int k = h.rec_count[slot];
@@ -444,8 +492,10 @@ __global__ void k_nrc_apply(const float *__restrict__ out, const float4 *__restr
 // Training targets (L_final - L_at_vertex) / throughput of every recorded
 // vertex, appended to the batch up to its capacity.
 __global__ void k_nrc_targets(const float *__restrict__ rec, const int32_t *__restrict__ rec_count,
-                              int64_t slots, int rec_max, int stride, int offset, int64_t n_pixels,
-                              PixelState ps, float *b_in, float *b_t, int32_t *b_count, int b_cap) {
+                              int64_t slots, int rec_max, int stride, const FrameConst *fc,
+                              int64_t n_pixels, PixelState ps, float *b_in, float *b_t,
+                              int32_t *b_count, int b_cap) {
+    const int offset = fc->nrc_offset;
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < slots;
          s += (int64_t)gridDim.x * blockDim.x) {
         int k_n = rec_count[s];
@@ -955,17 +1005,20 @@ __global__ void k_accumulate(PixelState ps, int64_t n) {
 }
 
 // Final write (integrator.cpp:262-266); rows flipped as the reference's
-// surface write does (src/core/device/cuda.h:33-37).
-__global__ void k_resolve(PixelState ps, float4 *out, int w, int h, float spp, int clamp,
+// surface write does (src/core/device/cuda.h:33-37), per view.
+__global__ void k_resolve(PixelState ps, float4 *out, const DevView *__restrict__ views,
+                          const FrameConst *__restrict__ fc, int64_t n, float spp, int clamp,
                           float clamp_max) {
-    int64_t n = (int64_t)w * h;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        float4 p = ps.pixel[i];
+    const int nv = fc->n_views;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        const DevView &v = views[view_of(views, nv, g)];
+        int64_t i = g - v.offset;
+        float4 p = ps.pixel[g];
         V3 c = V3{p.x, p.y, p.z} / spp;
         if (clamp) c = vmin(vmax(c, v3(0.f)), v3(clamp_max));
-        int64_t x = i % w, y = i / w;
-        out[(h - 1 - y) * (int64_t)w + x] = f4(c, 1.f);
+        int64_t x = i % v.w, y = i / v.w;
+        out[v.offset + (v.h - 1 - y) * (int64_t)v.w + x] = f4(c, 1.f);
     }
 }
 
@@ -1106,11 +1159,10 @@ static int alloc_nrc_buffers(krr_wf *wf) {
 // and take one optimiser step.
 static int nrc_train_frame(krr_wf *wf, cudaStream_t st) {
     int stride = nrc_train_stride(wf->nrc);
-    int offset = (int)(wf->frame_index % stride);
     int64_t batch = nrc_batch_size(wf->nrc);
     KRR_CUDA(cudaMemsetAsync(wf->nrc_b_count(), 0, sizeof(int32_t), st));
     k_nrc_targets<<<grid_for(wf->nrc_slots), kThreads, 0, st>>>(
-        wf->nrc_rec, wf->nrc_rec_count, wf->nrc_slots, wf->nrc_rec_max, stride, offset, wf->n, wf->ps,
+        wf->nrc_rec, wf->nrc_rec_count, wf->nrc_slots, wf->nrc_rec_max, stride, wf->d_frame, wf->n, wf->ps,
         wf->nrc_b_in, wf->nrc_b_t, wf->nrc_b_count(), (int)batch);
     k_clamp_count<<<1, 32, 0, st>>>(wf->nrc_b_count(), (int)batch);
     KRR_CUDA(cudaGetLastError());
@@ -1153,6 +1205,11 @@ extern "C" int krr_wf_destroy(krr_wf *wf) {
     free_queues(wf);
     free_scene(wf);
     free_nrc_buffers(wf);
+    if (wf->graph) cudaGraphExecDestroy(wf->graph);
+    cudaFreeHost(wf->h_views);
+    cudaFreeHost(wf->h_frame);
+    cudaFree(wf->d_views);
+    cudaFree(wf->d_frame);
     delete wf;
     return KRR_OK;
 }
@@ -1353,14 +1410,30 @@ extern "C" int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *sd, void *stre
     return KRR_OK;
 }
 
-extern "C" int krr_wf_resize(krr_wf *wf, int32_t width, int32_t height) {
-    KRR_CHECK_ARG(wf && width > 0 && height > 0, "bad frame size");
-    KRR_CHECK_ARG((int64_t)width * height < (1ll << 30), "frame too large");
+// Allocates queues and pixel state for the views of `layout` (offsets set).
+static int set_layout(krr_wf *wf, std::vector<DevView> layout) {
+    int64_t n = 0;
+    for (auto &v : layout) {
+        KRR_CHECK_ARG(v.w > 0 && v.h > 0, "bad view size");
+        v.offset = n;
+        n += (int64_t)v.w * v.h;
+    }
+    KRR_CHECK_ARG(n > 0 && n < (1ll << 30), "frame too large");
+    KRR_CHECK_ARG(layout.size() <= (size_t)kMaxViews, "too many views");
     cudaDeviceSynchronize();
+    if (wf->graph) { cudaGraphExecDestroy(wf->graph); wf->graph = nullptr; }
     free_queues(wf);
-    wf->width = width;
-    wf->height = height;
-    wf->n = (int64_t)width * height;
+    if (!wf->h_views) {
+        KRR_CUDA(cudaMallocHost(&wf->h_views, kMaxViews * sizeof(DevView)));
+        KRR_CUDA(cudaMalloc(&wf->d_views, kMaxViews * sizeof(DevView)));
+        KRR_CUDA(cudaMallocHost(&wf->h_frame, sizeof(FrameConst)));
+        KRR_CUDA(cudaMalloc(&wf->d_frame, sizeof(FrameConst)));
+    }
+    wf->layout = layout;
+    wf->n_views = (int32_t)layout.size();
+    wf->width = layout.size() == 1 ? layout[0].w : 0;
+    wf->height = layout.size() == 1 ? layout[0].h : 0;
+    wf->n = n;
     for (int k = 0; k < Q_COUNT; ++k)
         KRR_CUDA(cudaMalloc(&wf->qbuf[k], (size_t)kChannels[k] * wf->n * sizeof(float4)));
     KRR_CUDA(cudaMalloc(&wf->d_counts, 16 * sizeof(int32_t)));
@@ -1374,6 +1447,25 @@ extern "C" int krr_wf_resize(krr_wf *wf, int32_t width, int32_t height) {
     return alloc_nrc_buffers(wf);
 }
 
+extern "C" int krr_wf_resize(krr_wf *wf, int32_t width, int32_t height) {
+    KRR_CHECK_ARG(wf && width > 0 && height > 0, "bad frame size");
+    DevView v{};
+    v.w = width;
+    v.h = height;
+    return set_layout(wf, {v});
+}
+
+extern "C" int krr_wf_resize_views(krr_wf *wf, const krr_view *views, int32_t n_views) {
+    KRR_CHECK_ARG(wf && views && n_views >= 1, "bad views");
+    std::vector<DevView> layout(n_views);
+    for (int i = 0; i < n_views; ++i) {
+        layout[i] = DevView{};
+        layout[i].w = views[i].width;
+        layout[i].h = views[i].height;
+    }
+    return set_layout(wf, layout);
+}
+
 static int ready(krr_wf *wf) {
     if (!wf) return fail(KRR_ERR_INVALID_ARGUMENT, "pass is NULL");
     if (!wf->has_scene) return fail(KRR_ERR_NOT_READY, "set_scene has not been called");
@@ -1381,13 +1473,10 @@ static int ready(krr_wf *wf) {
     return KRR_OK;
 }
 
-extern "C" int krr_wf_begin_frame(krr_wf *wf, int64_t frame_index, const krr_camera_desc *c,
-                                  void *stream) {
-    KRR_TRY(ready(wf));
+static int make_camera(const krr_camera_desc *c, DevCamera &d) {
     KRR_CHECK_ARG(c != nullptr, "camera is NULL");
     KRR_CHECK_ARG(c->lens_radius <= 1e-5f, "thin-lens cameras are not supported");
-    cudaStream_t st = as_stream(stream);
-    DevCamera d{};
+    d = DevCamera{};
     for (int k = 0; k < 3; ++k) d.pos[k] = c->position[k];
     for (int k = 0; k < 9; ++k) d.rot[k] = c->rotation[k];
     float fov = std::atan2(c->film_size[1] * 0.5f, c->focal_length);
@@ -1398,21 +1487,77 @@ extern "C" int krr_wf_begin_frame(krr_wf *wf, int64_t frame_index, const krr_cam
     d.shutter_open = c->shutter_open;
     d.shutter_time = c->shutter_time;
     d.medium = c->medium;
-    wf->cam = d;
+    return KRR_OK;
+}
+
+// Fills the view table and frame constants of frame `frame_index` into the
+// given host arrays (cameras == nullptr keeps the current cameras).
+static int fill_frame(krr_wf *wf, int64_t frame_index, const krr_camera_desc *single,
+                      const krr_view *views, int32_t n_views, DevView *dv, FrameConst *fc) {
+    if (single) {
+        KRR_CHECK_ARG(wf->n_views == 1, "the pass has a multi-view layout: use begin_frame_views");
+        DevView v = wf->layout[0];
+        KRR_TRY(make_camera(single, v.cam));
+        v.sample_index = (uint32_t)(frame_index * wf->params.spp + wf->params.seed);
+        wf->layout[0] = v;
+    } else if (views) {
+        KRR_CHECK_ARG(n_views == wf->n_views, "view count differs from the layout");
+        for (int i = 0; i < n_views; ++i) {
+            KRR_CHECK_ARG(views[i].width == wf->layout[i].w && views[i].height == wf->layout[i].h,
+                          "view size differs from the layout");
+            KRR_TRY(make_camera(&views[i].camera, wf->layout[i].cam));
+            wf->layout[i].sample_index = (uint32_t)(frame_index * wf->params.spp + views[i].seed);
+        }
+    }
+    for (int i = 0; i < wf->n_views; ++i) dv[i] = wf->layout[i];
+    fc->n_views = wf->n_views;
+    fc->frame_index = frame_index;
+    fc->nrc_offset = wf->nrc ? (int32_t)(frame_index % nrc_train_stride(wf->nrc)) : 0;
+    wf->cam = wf->layout[0].cam;
     wf->frame_index = frame_index;
-    uint32_t sample_index = (uint32_t)(frame_index * wf->params.spp + wf->params.seed);
-    k_begin_frame<<<wf->grid, kThreads, 0, st>>>(wf->ps, wf->width, wf->n, sample_index);
+    return KRR_OK;
+}
+
+static int launch_begin_frame(krr_wf *wf, cudaStream_t st) {
+    k_begin_frame<<<wf->grid, kThreads, 0, st>>>(wf->ps, wf->d_views, wf->d_frame, wf->n);
     KRR_CUDA(cudaGetLastError());
     if (wf->nrc && wf->nrc_rec_count)
         KRR_CUDA(cudaMemsetAsync(wf->nrc_rec_count, 0, wf->nrc_slots * sizeof(int32_t), st));
     return KRR_OK;
 }
 
+static int begin_frame_common(krr_wf *wf, int64_t frame_index, const krr_camera_desc *single,
+                              const krr_view *views, int32_t n_views, cudaStream_t st) {
+    // pageable staging: the copies below take the values before returning
+    std::vector<DevView> dv(wf->n_views);
+    FrameConst fc{};
+    KRR_TRY(fill_frame(wf, frame_index, single, views, n_views, dv.data(), &fc));
+    KRR_CUDA(cudaMemcpyAsync(wf->d_views, dv.data(), dv.size() * sizeof(DevView),
+                             cudaMemcpyHostToDevice, st));
+    KRR_CUDA(cudaMemcpyAsync(wf->d_frame, &fc, sizeof(FrameConst), cudaMemcpyHostToDevice, st));
+    KRR_CUDA(cudaStreamSynchronize(st));
+    return launch_begin_frame(wf, st);
+}
+
+extern "C" int krr_wf_begin_frame(krr_wf *wf, int64_t frame_index, const krr_camera_desc *c,
+                                  void *stream) {
+    KRR_TRY(ready(wf));
+    KRR_CHECK_ARG(c != nullptr, "camera is NULL");
+    return begin_frame_common(wf, frame_index, c, nullptr, 0, as_stream(stream));
+}
+
+extern "C" int krr_wf_begin_frame_views(krr_wf *wf, int64_t frame_index, const krr_view *views,
+                                        int32_t n_views, void *stream) {
+    KRR_TRY(ready(wf));
+    KRR_CHECK_ARG(views != nullptr, "views are NULL");
+    return begin_frame_common(wf, frame_index, nullptr, views, n_views, as_stream(stream));
+}
+
 extern "C" int krr_wf_generate_camera_rays(krr_wf *wf, void *stream) {
     KRR_TRY(ready(wf));
     cudaStream_t st = as_stream(stream);
-    k_camera_rays<<<wf->grid, kThreads, 0, st>>>(wf->ps, wf->q(Q_RAY0), wf->cam, wf->width,
-                                                  wf->height, wf->n);
+    k_camera_rays<<<wf->grid, kThreads, 0, st>>>(wf->ps, wf->q(Q_RAY0), wf->d_views, wf->d_frame,
+                                                  wf->n);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }
@@ -1442,7 +1587,7 @@ extern "C" int krr_wf_trace_closest(krr_wf *wf, int32_t depth, void *stream) {
     if (wf->nrc) {
         hook.mode = 1;
         hook.stride = nrc_train_stride(wf->nrc);
-        hook.offset = (int32_t)(wf->frame_index % hook.stride);
+        hook.frame = wf->d_frame;
         hook.q_in = wf->nrc_q_in;
         hook.q_meta = wf->nrc_q_meta;
         hook.q_count = wf->nrc_q_count();
@@ -1545,8 +1690,8 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
         k_accumulate<<<wf->grid, kThreads, 0, st>>>(wf->ps, wf->n);
         KRR_CUDA(cudaGetLastError());
     }
-    k_resolve<<<wf->grid, kThreads, 0, st>>>(wf->ps, reinterpret_cast<float4 *>(d_out), wf->width,
-                                              wf->height, (float)wf->params.spp,
+    k_resolve<<<wf->grid, kThreads, 0, st>>>(wf->ps, reinterpret_cast<float4 *>(d_out), wf->d_views,
+                                              wf->d_frame, wf->n, (float)wf->params.spp,
                                               wf->params.enable_clamp, wf->params.clamp_max);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
@@ -1610,6 +1755,47 @@ extern "C" int krr_wf_accel(krr_wf *wf, const krr_accel **out) {
     KRR_TRY(ready(wf));
     KRR_CHECK_ARG(out != nullptr, "NULL argument");
     *out = &wf->accel;
+    return KRR_OK;
+}
+
+// A whole frame (view table upload, beginFrame, render) captured into a CUDA
+// graph; replays read the per-frame constants from pinned host memory.
+extern "C" int krr_wf_capture_frame(krr_wf *wf, float *d_out, void *stream) {
+    KRR_TRY(ready(wf));
+    KRR_CHECK_ARG(d_out != nullptr, "output is NULL");
+    cudaStream_t st = as_stream(stream);
+    KRR_CHECK_ARG(st != nullptr, "capture needs a non-default stream");
+    if (wf->graph) { cudaGraphExecDestroy(wf->graph); wf->graph = nullptr; }
+    for (int i = 0; i < wf->n_views; ++i) wf->h_views[i] = wf->layout[i];
+    KRR_CUDA(cudaStreamSynchronize(st));
+    KRR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int status = KRR_OK;
+    cudaError_t e = cudaMemcpyAsync(wf->d_views, wf->h_views, wf->n_views * sizeof(DevView),
+                                    cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(wf->d_frame, wf->h_frame, sizeof(FrameConst), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) status = cuda_status(e, "capture copies", __FILE__, __LINE__);
+    if (status == KRR_OK) status = launch_begin_frame(wf, st);
+    if (status == KRR_OK) status = krr_wf_render(wf, d_out, stream);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(st, &g);
+    if (status != KRR_OK) { if (g) cudaGraphDestroy(g); return status; }
+    if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+    e = cudaGraphInstantiate(&wf->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_launch_frame(krr_wf *wf, int64_t frame_index, const krr_view *views,
+                                   int32_t n_views, void *stream) {
+    KRR_TRY(ready(wf));
+    if (!wf->graph) return fail(KRR_ERR_NOT_READY, "no captured frame: call krr_wf_capture_frame");
+    cudaStream_t st = as_stream(stream);
+    // the previous replay must have read the pinned constants before they change
+    KRR_CUDA(cudaStreamSynchronize(st));
+    KRR_TRY(fill_frame(wf, frame_index, nullptr, views, n_views, wf->h_views, wf->h_frame));
+    KRR_CUDA(cudaGraphLaunch(wf->graph, st));
     return KRR_OK;
 }
 

@@ -69,6 +69,48 @@ class WavefrontPathTracer:
     def resize(self, width: int, height: int):
         check(self.lib.krr_wf_resize(self._h, width, height), "krr_wf_resize")
         self.width, self.height = width, height
+        self.n_pixels = width * height
+        self._views = None
+
+    def resize_views(self, views):
+        """Batched views: list of (camera, width, height, seed)."""
+        arr = (_lib.ViewDesc * len(views))()
+        for i, (cam, w, h, seed) in enumerate(views):
+            arr[i].camera = cam.desc()
+            arr[i].width, arr[i].height, arr[i].seed = w, h, seed
+        check(self.lib.krr_wf_resize_views(self._h, arr, len(views)), "krr_wf_resize_views")
+        self._views = arr
+        self.width = self.height = 0
+        self.n_pixels = sum(w * h for _, w, h, _ in views)
+
+    def begin_frame_views(self, frame_index: int, views=None):
+        if views is not None:
+            arr = (_lib.ViewDesc * len(views))()
+            for i, (cam, w, h, seed) in enumerate(views):
+                arr[i].camera = cam.desc()
+                arr[i].width, arr[i].height, arr[i].seed = w, h, seed
+            self._views = arr
+        check(self.lib.krr_wf_begin_frame_views(self._h, frame_index, self._views,
+                                                len(self._views), _stream()),
+              "krr_wf_begin_frame_views")
+
+    def render_flat(self, out: torch.Tensor | None = None) -> torch.Tensor:
+        """render() for a batched layout: float32 [total pixels, 4]."""
+        if out is None:
+            out = torch.empty((self.n_pixels, 4), dtype=torch.float32, device="cuda")
+        check(self.lib.krr_wf_render(self._h, out.data_ptr(), _stream()), "krr_wf_render")
+        return out
+
+    def capture_frame(self, out: torch.Tensor):
+        """Captures beginFrame + render into a CUDA graph writing `out`."""
+        check(self.lib.krr_wf_capture_frame(self._h, out.data_ptr(), _stream()),
+              "krr_wf_capture_frame")
+
+    def launch_frame(self, frame_index: int):
+        views = getattr(self, "_views", None)
+        check(self.lib.krr_wf_launch_frame(self._h, frame_index, views,
+                                           len(views) if views is not None else 0, _stream()),
+              "krr_wf_launch_frame")
 
     def begin_frame(self, frame_index: int, camera):
         self._cam = camera.desc()
@@ -115,8 +157,8 @@ class WavefrontPathTracer:
         return v.value
 
     def radiance(self) -> torch.Tensor:
-        """Per-pixel L (the reference's PixelState::L) as float32 [H*W, 4]."""
-        out = torch.empty((self.width * self.height, 4), dtype=torch.float32, device="cuda")
+        """Per-pixel L (the reference's PixelState::L) as float32 [pixels, 4]."""
+        out = torch.empty((self.n_pixels, 4), dtype=torch.float32, device="cuda")
         check(self.lib.krr_wf_read_radiance(self._h, out.data_ptr(), _stream()), "read_radiance")
         return out
 
