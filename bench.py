@@ -38,6 +38,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--node-format", default="0", choices=["auto", "0", "1"],
+                    help="BVH node format: 0 compressed 80 B (default), 1 float 224 B, auto = "
+                         "the faster after autotuning both (outside the timed region)")
     ap.add_argument("--nrc-res", default="480x270",
                     help="resolution of the time-to-relMSE comparison (0 = skip)")
     ap.add_argument("--nrc-ref-frames", type=int, default=8192)
@@ -267,9 +270,20 @@ def run_ours(args, rank, world, local):
 
     build()
     sc, tris, rays_np, H = make_workload(seed_offset=rank)
-    acc = Accel(tris)
-    stats = acc.stats()
     rays0 = torch.from_numpy(rays_np).to(dev)
+    # node format and traversal settings for this workload (outside the timed region)
+    formats = [0, 1] if args.node_format == "auto" else [int(args.node_format)]
+    acc, tuning, tried = None, None, {}
+    for fmt in formats:
+        cand = Accel(tris, node_format=fmt)
+        t = cand.autotune(rays0, repeats=2)
+        tried[fmt] = t["ms"]
+        if tuning is None or t["ms"] < tuning["ms"]:
+            acc, tuning = cand, t
+        else:
+            del cand
+    torch.cuda.synchronize()
+    stats = acc.stats()
     hits0 = acc.trace_closest(rays0)
     torch.cuda.synchronize()
     bounce_np = H.bounce_rays(tris, rays_np, hits0.cpu().numpy(), 2 + rank)
@@ -278,16 +292,14 @@ def run_ours(args, rank, world, local):
     sets = [(rays0, hits0), (rays1, hits1)]
     n_per_step = rays0.shape[0] + rays1.shape[0]
 
-    # autotuner: traversal settings for this workload (outside the timed region)
-    tuning = acc.autotune(rays0, repeats=2)
-
     # algorithmic bytes per ray from a counter-instrumented replay
     node_visits = tri_tests = 0
     for r, _ in sets:
         nn, nt = acc.trace_stats(r)
         node_visits += nn
         tri_tests += nt
-    alg_bytes = 48.0 * n_per_step + 80.0 * node_visits + 48.0 * tri_tests
+    node_size = stats["node_bytes"] / stats["n_nodes"]
+    alg_bytes = 48.0 * n_per_step + node_size * node_visits + 48.0 * tri_tests
 
     stream = torch.cuda.current_stream()
     clk = ClockSampler(local).__enter__()
@@ -365,14 +377,16 @@ def run_ours(args, rank, world, local):
                    "bvh_depth": int(stats["max_depth"]),
                    "nodes_per_ray": node_visits / n_per_step, "tris_per_ray": tri_tests / n_per_step,
                    "tuning": {"refill_below": tuning["refill_below"],
-                              "postpone_pct": tuning["postpone_pct"]},
+                              "postpone_pct": tuning["postpone_pct"],
+                              "node_format": stats["node_format"],
+                              "primary_ms_by_format": tried},
                    "parallelism": f"replicas{world}"},
         "e2e": e2e,
         "gpu_launches": args.steps * len(sets),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_kind": peak_kind,
-                     "note": "algorithmic bytes = 48 B ray+hit + 80 B per 8-wide node visit + "
+                     "note": f"algorithmic bytes = 48 B ray+hit + {node_size:.0f} B per 8-wide node visit + "
                              "48 B per triangle test, per launch; they are served mostly by L2, "
                              "so the fraction is against the measured HBM copy bandwidth"},
         "cpu_baseline": cpu,

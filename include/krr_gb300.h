@@ -159,6 +159,12 @@ typedef struct krr_accel_stats {
     double triangle_bytes;    /* bytes of the leaf-ordered triangle array   */
 } krr_accel_stats;
 
+/* Node format of the BVHs built from now on, process-wide: 0 = compressed
+ * 8-wide nodes (80 B, 8-bit quantised child boxes; default), 1 = float
+ * 8-wide nodes (224 B, fewer instructions per box test).  Hits are the
+ * same with either.  krr_accel_stats.reserved reports a build's format. */
+int krr_set_bvh_node_format(int32_t format);
+
 /* Build from host arrays of world-space triangles: h_vertices float3[3*n]. */
 int krr_accel_create_from_triangles(const float *h_vertices, int64_t n_triangles,
                                     krr_accel **out, void *stream);

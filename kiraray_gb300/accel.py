@@ -21,9 +21,16 @@ def _stream() -> int:
     return torch.cuda.current_stream().cuda_stream
 
 
+def set_node_format(fmt: int) -> None:
+    """0 = compressed 80-byte nodes (default), 1 = float 224-byte nodes."""
+    check(_lib.load().krr_set_bvh_node_format(fmt), "krr_set_bvh_node_format")
+
+
 class Accel:
-    def __init__(self, world_triangles: np.ndarray):
+    def __init__(self, world_triangles: np.ndarray, node_format: int | None = None):
         lib = _lib.load()
+        if node_format is not None:
+            set_node_format(node_format)
         v = np.ascontiguousarray(world_triangles, dtype=np.float32).reshape(-1, 9)
         self._h = C.c_void_p()
         check(lib.krr_accel_create_from_triangles(v.ctypes.data, v.shape[0], C.byref(self._h),
@@ -41,7 +48,9 @@ class Accel:
     def stats(self) -> dict:
         s = _lib.AccelStats()
         check(_lib.load().krr_accel_stats_get(self._h, C.byref(s)), "krr_accel_stats_get")
-        return {k: getattr(s, k) for k, _ in s._fields_ if k != "reserved"}
+        d = {k: getattr(s, k) for k, _ in s._fields_ if k != "reserved"}
+        d["node_format"] = s.reserved
+        return d
 
     @staticmethod
     def _rays(rays: torch.Tensor) -> torch.Tensor:

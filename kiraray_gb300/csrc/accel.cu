@@ -225,7 +225,7 @@ __device__ __forceinline__ int quant_exponent(float ext) {
 
 __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const int *n_in,
                            CollapseItem *out, int *n_out, float4 *nodes, int *node_counter,
-                           uint32_t *leaf_order, int *tri_counter, int *max_depth) {
+                           uint32_t *leaf_order, int *tri_counter, int *max_depth, int format) {
     int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= *n_in) return;
     CollapseItem item = in[w];
@@ -346,6 +346,25 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
 
     uint32_t ew = (uint32_t)(ek[0] + 127) | ((uint32_t)(ek[1] + 127) << 8) |
                   ((uint32_t)(ek[2] + 127) << 16) | (imask << 24);
+    if (format == 1) {
+        float4 *np = nodes + 14 * (size_t)item.wnode;
+        float b[6][8];
+        for (int s2 = 0; s2 < 8; ++s2) {
+            int c = child_in_slot[s2];
+            for (int k = 0; k < 3; ++k) {
+                b[2 * k][s2] = c >= 0 ? get(clo[c], k) : INFINITY;
+                b[2 * k + 1][s2] = c >= 0 ? get(chi[c], k) : -INFINITY;
+            }
+        }
+        for (int q = 0; q < 6; ++q) {
+            np[2 * q] = make_float4(b[q][0], b[q][1], b[q][2], b[q][3]);
+            np[2 * q + 1] = make_float4(b[q][4], b[q][5], b[q][6], b[q][7]);
+        }
+        np[12] = make_float4(__uint_as_float((uint32_t)child_base), __uint_as_float((uint32_t)tri_base),
+                             __uint_as_float(meta[0]), __uint_as_float(meta[1]));
+        np[13] = make_float4(__uint_as_float(imask), 0.f, 0.f, 0.f);
+        return;
+    }
     float4 *np = nodes + 5 * (size_t)item.wnode;
     np[0] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(ew));
     np[1] = make_float4(__uint_as_float((uint32_t)child_base), __uint_as_float((uint32_t)tri_base),
@@ -378,7 +397,7 @@ __global__ void k_set_mask(float4 *tris, const uint32_t *leaf_of_prim, const uin
     tris[3 * (size_t)k + 1].w = __uint_as_float(mask ? (uint32_t)(mask[p] != 0) : 1u);
 }
 
-template <bool ANY, bool STATS>
+template <bool ANY, bool STATS, int FMT>
 __global__ void __launch_bounds__(kTraceThreads)
 k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, TraceLaunch L,
         unsigned long long *stats) {
@@ -389,7 +408,7 @@ k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, Trace
     bool active = false, exhausted = false;
     int64_t ray_id = 0;
     RayPre r;
-    V3 inv;
+    V3 inv, oinv;
     int oct = 0;
     float tmax = 0.f;
     uint2 ng = make_uint2(0, 0), tg = make_uint2(0, 0);
@@ -417,6 +436,7 @@ k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, Trace
                     r = ray_pre(o, d, ro.w);
                     tmax = rd.w;
                     inv = box_inverse(d);
+                    oinv = V3{-o.x * inv.x, -o.y * inv.y, -o.z * inv.z};
                     oct = (inv.x < 0.f ? 1 : 0) | (inv.y < 0.f ? 2 : 0) | (inv.z < 0.f ? 4 : 0);
                     ng = make_uint2(0u, (1u << oct) | (1u << 8));
                     tg = make_uint2(0u, 0u);
@@ -443,7 +463,7 @@ k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, Trace
                 else { atomicOr(L.err, (int)kErrStackOverflow); done = true; }
             }
             if (STATS) ++n_nodes;
-            visit_node(nodes, child, r, inv, oct, tmax, ng, tg);
+            visit<FMT>(nodes, child, r, inv, oinv, oct, tmax, ng, tg);
             fresh = true;
         }
         // Postpone a fresh triangle group onto the stack while too few lanes
@@ -513,7 +533,7 @@ int traversal_grid_size() {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<false, false>, kTraceThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<false, false, 0>, kTraceThreads, 0);
     if (per_sm < 1) per_sm = 1;
     g_grid_size = sms * per_sm;
     return g_grid_size;
@@ -528,7 +548,10 @@ static int launch_trace(const krr_accel *a, const TraceLaunch &l, cudaStream_t s
     TraceLaunch lt = l;
     lt.refill_below = a->refill_below;
     lt.postpone_pct = a->postpone_pct;
-    k_trace<ANY, STATS><<<traversal_grid_size(), kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, lt, stats);
+    if (a->node_format == 1)
+        k_trace<ANY, STATS, 1><<<traversal_grid_size(), kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, lt, stats);
+    else
+        k_trace<ANY, STATS, 0><<<traversal_grid_size(), kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, lt, stats);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }
@@ -569,6 +592,7 @@ inline unsigned blocks_for(int64_t n, int t = kBuildThreads) { return (unsigned)
 int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     KRR_CHECK_ARG(n >= 0 && n < (int64_t)0x7fffffff, "triangle count out of range");
     accel_free(a);
+    a->node_format = default_node_format();
     a->n_tris = n;
     a->n_nodes = 0;
     a->max_depth = 0;
@@ -656,7 +680,9 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     DevBuf<uint32_t> leaf_order;
     DevBuf<CollapseItem> qa, qb;
     DevBuf<int> counters;   // [0] node counter, [1] tri counter, [2] max depth, [3] n_in, [4] n_out
-    KRR_CUDA(nodes_tmp.alloc(5 * max_nodes));
+    const int fmt = a->node_format;
+    const int quads = kNodeQuads[fmt];
+    KRR_CUDA(nodes_tmp.alloc(quads * max_nodes));
     KRR_CUDA(leaf_order.alloc(n));
     KRR_CUDA(qa.alloc(max_nodes)); KRR_CUDA(qb.alloc(max_nodes));
     KRR_CUDA(counters.alloc(8));
@@ -673,7 +699,7 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
         KRR_CUDA(cudaMemsetAsync(c_out, 0, sizeof(int), s));
         k_collapse<<<blocks_for(n_in, 128), 128, 0, s>>>(bt, qin, c_in, qout, c_out, nodes_tmp.p,
                                                          counters.p, leaf_order.p, counters.p + 1,
-                                                         counters.p + 2);
+                                                         counters.p + 2, fmt);
         KRR_CUDA(cudaGetLastError());
         KRR_CUDA(cudaMemcpyAsync(&n_in, c_out, sizeof(int), cudaMemcpyDeviceToHost, s));
         KRR_CUDA(cudaMemcpyAsync(c_in, c_out, sizeof(int), cudaMemcpyDeviceToDevice, s));
@@ -690,8 +716,8 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
         return fail(KRR_ERR_OVERFLOW, "BVH depth %d exceeds the traversal stack (%d)", a->max_depth,
                     kTraversalStack);
 
-    KRR_CUDA(cudaMalloc(&a->d_nodes, 5 * sizeof(float4) * a->n_nodes));
-    KRR_CUDA(cudaMemcpyAsync(a->d_nodes, nodes_tmp.p, 5 * sizeof(float4) * a->n_nodes,
+    KRR_CUDA(cudaMalloc(&a->d_nodes, quads * sizeof(float4) * a->n_nodes));
+    KRR_CUDA(cudaMemcpyAsync(a->d_nodes, nodes_tmp.p, quads * sizeof(float4) * a->n_nodes,
                              cudaMemcpyDeviceToDevice, s));
     KRR_CUDA(cudaMalloc(&a->d_tris, 3 * sizeof(float4) * n));
     KRR_CUDA(cudaMalloc(&a->d_leaf_of_prim, sizeof(uint32_t) * n));
@@ -740,14 +766,23 @@ extern "C" int krr_accel_create_from_triangles(const float *h_vertices, int64_t 
     return KRR_OK;
 }
 
+static int g_node_format = 0;
+int krr::default_node_format() { return g_node_format; }
+
+extern "C" int krr_set_bvh_node_format(int32_t format) {
+    KRR_CHECK_ARG(format == 0 || format == 1, "node format must be 0 (compressed) or 1 (float)");
+    g_node_format = format;
+    return KRR_OK;
+}
+
 extern "C" int krr_accel_stats_get(const krr_accel *a, krr_accel_stats *out) {
     KRR_CHECK_ARG(a && out, "NULL argument");
     out->n_triangles = a->n_tris;
     out->n_nodes = a->n_nodes;
     out->max_depth = a->max_depth;
-    out->reserved = 0;
     out->build_ms = a->build_ms;
-    out->node_bytes = 80.0 * (double)a->n_nodes;
+    out->node_bytes = 16.0 * kNodeQuads[a->node_format] * (double)a->n_nodes;
+    out->reserved = a->node_format;
     out->triangle_bytes = 48.0 * (double)a->n_tris;
     return KRR_OK;
 }

@@ -19,6 +19,12 @@
 // s (bit i set = negative along axis i), so visiting positions s ^ octant in
 // increasing order is an approximate front-to-back order.
 //
+// Float node format (224 bytes = 14 x 16 B), the same tree without
+// quantisation: q0..q1 lo_x[0..7], q2..q3 hi_x, q4..q5 lo_y, q6..q7 hi_y,
+// q8..q9 lo_z, q10..q11 hi_z (empty slots: lo = +inf, hi = -inf),
+// q12: child_base | tri_base | meta[0..3] | meta[4..7], q13: imask | 0 | 0 | 0.
+// It spends 2.8x the node bytes to drop the per-plane byte extraction.
+//
 // Triangle (48 bytes, leaf order): v0.xyz | global id, v1.xyz | any-hit mask,
 // v2.xyz | unused.
 #pragma once
@@ -39,11 +45,15 @@ struct krr_accel {
     float scene_lo[3] = {0, 0, 0}, scene_hi[3] = {0, 0, 0};
     int refill_below = 20;       // traversal tuning (krr_accel_set_tuning)
     int postpone_pct = 0;
+    int node_format = 0;         // 0 compressed (80 B), 1 float (224 B)
 };
 
 namespace krr {
 
 constexpr int kTraversalStack = 48;
+constexpr int kNodeQuads[2] = {5, 14};   // float4 per node, by node format
+// Process-wide node format used by builds (krr_set_bvh_node_format).
+int default_node_format();
 constexpr int kTraceThreads = 128;
 
 // Build from device world-space vertices (float3 x 3 per triangle).

@@ -140,6 +140,59 @@ __device__ __forceinline__ void visit_node(const float4 *__restrict__ nodes, uin
     tg = make_uint2(__float_as_uint(q1.y), hitmask & 0x00ffffffu);
 }
 
+// Float node format: near/far planes are picked per ray by address (no
+// per-child selects); t = b * inv + (-o * inv) with one FMA per plane.
+__device__ __forceinline__ void visit_node_f(const float4 *__restrict__ nodes, uint32_t child,
+                                             const RayPre &r, V3 inv, V3 oinv, int oct, float tmax,
+                                             uint2 &ng, uint2 &tg) {
+    const float4 *np = nodes + 14 * (size_t)child;
+    const int nxo = (oct & 1) ? 2 : 0, nyo = (oct & 2) ? 6 : 4, nzo = (oct & 4) ? 10 : 8;
+    const float4 nxa = __ldg(np + nxo), nxb = __ldg(np + nxo + 1);
+    const float4 fxa = __ldg(np + (nxo ^ 2)), fxb = __ldg(np + (nxo ^ 2) + 1);
+    const float4 nya = __ldg(np + nyo), nyb = __ldg(np + nyo + 1);
+    const float4 fya = __ldg(np + (nyo ^ 2)), fyb = __ldg(np + (nyo ^ 2) + 1);
+    const float4 nza = __ldg(np + nzo), nzb = __ldg(np + nzo + 1);
+    const float4 fza = __ldg(np + (nzo ^ 2)), fzb = __ldg(np + (nzo ^ 2) + 1);
+    const float4 q12 = __ldg(np + 12), q13 = __ldg(np + 13);
+    uint32_t meta0 = __float_as_uint(q12.z), meta1 = __float_as_uint(q12.w);
+    meta0 ^= ((meta0 & (meta0 << 1) & 0x10101010u) >> 4) * (uint32_t)oct;
+    meta1 ^= ((meta1 & (meta1 << 1) & 0x10101010u) >> 4) * (uint32_t)oct;
+    const float tlimit = tmax + fabsf(tmax) * 5e-7f;
+    const int tmin_i = __float_as_int(r.tmin), tlim_i = __float_as_int(tlimit);
+    const float nx[8] = {nxa.x, nxa.y, nxa.z, nxa.w, nxb.x, nxb.y, nxb.z, nxb.w};
+    const float fx[8] = {fxa.x, fxa.y, fxa.z, fxa.w, fxb.x, fxb.y, fxb.z, fxb.w};
+    const float ny[8] = {nya.x, nya.y, nya.z, nya.w, nyb.x, nyb.y, nyb.z, nyb.w};
+    const float fy[8] = {fya.x, fya.y, fya.z, fya.w, fyb.x, fyb.y, fyb.z, fyb.w};
+    const float nz[8] = {nza.x, nza.y, nza.z, nza.w, nzb.x, nzb.y, nzb.z, nzb.w};
+    const float fz[8] = {fza.x, fza.y, fza.z, fza.w, fzb.x, fzb.y, fzb.z, fzb.w};
+    uint32_t hitmask = 0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        uint32_t m = __byte_perm(c < 4 ? meta0 : meta1, 0u, 0x4440u + (uint32_t)(c & 3));
+        int tnx = __float_as_int(fmaf(nx[c], inv.x, oinv.x));
+        int tny = __float_as_int(fmaf(ny[c], inv.y, oinv.y));
+        int tnz = __float_as_int(fmaf(nz[c], inv.z, oinv.z));
+        int tfx = __float_as_int(fmaf(fx[c], inv.x, oinv.x));
+        int tfy = __float_as_int(fmaf(fy[c], inv.y, oinv.y));
+        int tfz = __float_as_int(fmaf(fz[c], inv.z, oinv.z));
+        int t0 = __vimax3_s32(tnx, tny, max(tnz, tmin_i));
+        int t1 = __vimin3_s32(tfx, tfy, min(tfz, tlim_i));
+        uint32_t bits = (m >> 5) << (m & 31u);
+        hitmask |= (t0 <= t1) ? bits : 0u;
+    }
+    uint32_t cimask = __float_as_uint(q13.x);
+    ng = make_uint2(__float_as_uint(q12.x), (hitmask >> 24) | (cimask << 8));
+    tg = make_uint2(__float_as_uint(q12.y), hitmask & 0x00ffffffu);
+}
+
+template <int FMT>
+__device__ __forceinline__ void visit(const float4 *__restrict__ nodes, uint32_t child,
+                                      const RayPre &r, V3 inv, V3 oinv, int oct, float tmax,
+                                      uint2 &ng, uint2 &tg) {
+    if (FMT == 1) visit_node_f(nodes, child, r, inv, oinv, oct, tmax, ng, tg);
+    else visit_node(nodes, child, r, inv, oct, tmax, ng, tg);
+}
+
 __device__ __forceinline__ V3 box_inverse(V3 d) {
     float dx = fabsf(d.x) < 1e-20f ? copysignf(1e-20f, d.x) : d.x;
     float dy = fabsf(d.y) < 1e-20f ? copysignf(1e-20f, d.y) : d.y;
@@ -151,11 +204,12 @@ __device__ __forceinline__ V3 box_inverse(V3 d) {
 // Closest hit: returns (t, b1, b2, id bits) or id KRR_MISS; any hit: the id
 // of some blocking triangle (mask != 0) or KRR_MISS.  Same hit as the
 // persistent kernel (the result does not depend on traversal order).
-template <bool ANY>
+template <bool ANY, int FMT>
 __device__ float4 traverse_ray(const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
                                V3 o, V3 d, float tmin, float tmax, int *err) {
     RayPre r = ray_pre(o, d, tmin);
     V3 inv = box_inverse(d);
+    V3 oinv = V3{-o.x * inv.x, -o.y * inv.y, -o.z * inv.z};
     int oct = (inv.x < 0.f ? 1 : 0) | (inv.y < 0.f ? 2 : 0) | (inv.z < 0.f ? 4 : 0);
     uint2 stack[kTraversalStack];
     int sp = 0;
@@ -173,7 +227,7 @@ __device__ float4 traverse_ray(const float4 *__restrict__ nodes, const float4 *_
                 if (sp < kTraversalStack) stack[sp++] = ng;
                 else { atomicOr(err, (int)kErrStackOverflow); break; }
             }
-            visit_node(nodes, child, r, inv, oct, tmax, ng, tg);
+            visit<FMT>(nodes, child, r, inv, oinv, oct, tmax, ng, tg);
         }
         while (tg.y) {
             int b = __ffs(tg.y) - 1;

@@ -32,7 +32,10 @@ struct krr_nrc {
     __nv_bfloat16 *table = nullptr;
     float *w_master = nullptr, *w_m = nullptr, *w_v = nullptr, *w_grad = nullptr;
     __nv_bfloat16 *weights = nullptr;
-    int64_t step = 0;
+    // Adam step counter and bias corrections live on the device so that a
+    // captured frame graph advances them on every replay: {int64 step,
+    // float 1 - beta1^step, float 1 - beta2^step}.
+    int64_t *step = nullptr;
     // activation buffers: [layers][cap][64] bf16, gradients float
     int64_t cap = 0;
     __nv_bfloat16 *act = nullptr;
@@ -287,10 +290,21 @@ __global__ void k_encode_bwd(NrcGrid g, const float *__restrict__ in, const floa
 }
 
 // Adam on an FP32 master array; writes the BF16 copy and clears the gradient.
+// Advances the device step counter and stores the bias corrections.
+__global__ void k_adam_step(int64_t *step, double b1, double b2) {
+    int64_t t = *step + 1;
+    *step = t;
+    float *bc = reinterpret_cast<float *>(step + 1);
+    bc[0] = (float)(1.0 - pow(b1, (double)t));
+    bc[1] = (float)(1.0 - pow(b2, (double)t));
+}
+
 __global__ void k_adam(float *__restrict__ w, float *__restrict__ m, float *__restrict__ v,
                        float *__restrict__ grad, __nv_bfloat16 *__restrict__ wb, int64_t n, float lr,
-                       float b1, float b2, float eps, float grad_scale, float bc1, float bc2,
+                       float b1, float b2, float eps, float grad_scale, const int64_t *__restrict__ step,
                        const uint8_t *__restrict__ frozen) {
+    const float bc1 = reinterpret_cast<const float *>(step + 1)[0];
+    const float bc2 = reinterpret_cast<const float *>(step + 1)[1];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         float gr = grad[i] * grad_scale;
@@ -431,17 +445,16 @@ int nrc_train_device(krr_nrc *n, const float *d_inputs, const float *d_targets,
     k_encode_bwd<<<grid_for(cap), kThreads, 0, s>>>(n->grid, d_inputs, dY, d_count, cap, n->table_grad);
     KRR_CUDA(cudaGetLastError());
     // Adam
-    n->step += 1;
     const krr_nrc_config &c = n->cfg;
-    float bc1 = 1.f - std::pow(c.beta1, (float)n->step), bc2 = 1.f - std::pow(c.beta2, (float)n->step);
+    k_adam_step<<<1, 1, 0, s>>>(n->step, (double)c.beta1, (double)c.beta2);
     k_adam<<<grid_for(n->mlp.n_params), kThreads, 0, s>>>(n->w_master, n->w_m, n->w_v, n->w_grad,
                                                            n->weights, n->mlp.n_params, c.learning_rate,
                                                            c.beta1, c.beta2, c.epsilon, 1.f / scale,
-                                                           bc1, bc2, nullptr);
+                                                           n->step, nullptr);
     int64_t tn = (int64_t)n->n_entries * n->grid.features;
     k_adam<<<grid_for(tn), kThreads, 0, s>>>(n->table_master, n->table_m, n->table_v, n->table_grad,
                                              n->table, tn, c.learning_rate, c.beta1, c.beta2,
-                                             c.epsilon, 1.f / scale, bc1, bc2, nullptr);
+                                             c.epsilon, 1.f / scale, n->step, nullptr);
     KRR_CUDA(cudaGetLastError());
     if (n->cfg.tensor_cores) KRR_TRY(nrc_pack_weights(n->weights, n->mlp, n->packed, s));
     return KRR_OK;
@@ -548,6 +561,7 @@ extern "C" int krr_nrc_create(const krr_nrc_config *cfg, krr_nrc **out) {
     alloc((void **)&n->loss, 16);
     alloc((void **)&n->packed, (size_t)(m.layers - 1) * kNrcWidth * kNrcIn * 2 + kNrcOutPad * kNrcIn * 2);
     alloc((void **)&n->err, 16);
+    alloc((void **)&n->step, 16);
     if (st == KRR_OK) {
         cudaMemcpy(n->w_master, w.data(), m.n_params * 4, cudaMemcpyHostToDevice);
         cudaMemcpy(n->table_master, t.data(), tn * 4, cudaMemcpyHostToDevice);
@@ -572,7 +586,7 @@ extern "C" int krr_nrc_destroy(krr_nrc *n) {
                     (void *)n->table_grad, (void *)n->table, (void *)n->w_master, (void *)n->w_m,
                     (void *)n->w_v, (void *)n->w_grad, (void *)n->weights, (void *)n->act,
                     (void *)n->out, (void *)n->dA, (void *)n->dB, (void *)n->loss,
-                    (void *)n->packed, (void *)n->err})
+                    (void *)n->packed, (void *)n->err, (void *)n->step})
         cudaFree(p);
     delete n;
     return KRR_OK;
@@ -606,7 +620,10 @@ extern "C" int krr_nrc_info(const krr_nrc *n, krr_nrc_info_t *info) {
         info->level_offset[l] = n->grid.offset[l];
         info->level_size[l] = n->grid.size[l];
     }
-    info->step = n->step;
+    int64_t step = 0;
+    KRR_CUDA(cudaDeviceSynchronize());
+    KRR_CUDA(cudaMemcpy(&step, n->step, sizeof(step), cudaMemcpyDeviceToHost));
+    info->step = step;
     return KRR_OK;
 }
 

@@ -926,6 +926,7 @@ __global__ void k_medium_scatter(DevScene s, Queue mscat, Queue next, Queue shad
 // traceTransmittance (wavefront.h:80-139) for every shadow ray when media
 // are enabled: closest hits through null-material interfaces with ratio
 // tracking inside media.
+template <int FMT>
 __global__ void k_shadow_tr(DevScene s, const float4 *__restrict__ nodes,
                             const float4 *__restrict__ tris, Queue shadow, PixelState ps,
                             uint32_t *err, int *trace_err) {
@@ -943,7 +944,7 @@ __global__ void k_shadow_tr(DevScene s, const float4 *__restrict__ nodes,
         V3 T_ray = v3(1.f), pu = v3(1.f), pl = v3(1.f);
         int crossings = 0;
         while (fabsf(d.x) > kRayEps * 2 || fabsf(d.y) > kRayEps * 2 || fabsf(d.z) > kRayEps * 2) {
-            float4 h = traverse_ray<false>(nodes, tris, o, d, 0.f, tmax, trace_err);
+            float4 h = traverse_ray<false, FMT>(nodes, tris, o, d, 0.f, tmax, trace_err);
             bool visible = ubits(h.w) == KRR_MISS;
             Surf sf;
             if (!visible) {
@@ -1817,9 +1818,14 @@ int launch_medium_scatter(krr_wf *wf, int depth, cudaStream_t st) {
     return KRR_OK;
 }
 int launch_trace_shadow_tr(krr_wf *wf, cudaStream_t st) {
-    k_shadow_tr<<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris,
-                                                wf->q(Q_SHADOW), wf->ps, wf->err(),
-                                                wf->accel.d_scratch + 4);
+    if (wf->accel.node_format == 1)
+        k_shadow_tr<1><<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris,
+                                                       wf->q(Q_SHADOW), wf->ps, wf->err(),
+                                                       wf->accel.d_scratch + 4);
+    else
+        k_shadow_tr<0><<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris,
+                                                       wf->q(Q_SHADOW), wf->ps, wf->err(),
+                                                       wf->accel.d_scratch + 4);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }

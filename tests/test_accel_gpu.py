@@ -183,3 +183,53 @@ def test_autotune_picks_a_setting(krr_lib, cuda):
     acc = Accel(sc.world_triangles())
     res = acc.autotune(torch.from_numpy(H.pinhole_rays(sc)).cuda(), repeats=1)
     assert 1 <= res["refill_below"] <= 32 and 0 <= res["postpone_pct"] <= 100 and res["ms"] > 0
+
+
+@pytest.fixture
+def float_nodes():
+    from kiraray_gb300.accel import set_node_format
+    set_node_format(1)
+    yield
+    set_node_format(0)
+
+
+@pytest.mark.parametrize("n_tris,seed", [(1, 0), (3, 2), (5, 9), (100, 4), (5000, 5), (60000, 6)])
+def test_float_nodes_soup_vs_brute_force(krr_lib, cuda, float_nodes, n_tris, seed):
+    tris = H.random_soup(n_tris, seed, size=0.2 if n_tris > 100 else 1.0)
+    rays = H.random_rays(3000, seed + 50)
+    acc = Accel(tris)
+    assert acc.stats()["node_format"] == 1
+    want = O.closest_brute(tris, rays) if n_tris <= 5000 else O.Bvh(tris).closest(rays)
+    _assert_bits_equal(_gpu_closest(acc, rays), want, f"float nodes soup {n_tris}")
+
+
+def test_float_nodes_large_scene_and_edges(krr_lib, cuda, float_nodes):
+    sc = scenes.large_scene(width=160, height=90, grid=384, n_spheres=80, sky_size=(64, 32))
+    tris = sc.world_triangles()
+    rays = H.pinhole_rays(sc, jitter_seed=5)
+    acc = Accel(tris)
+    acc.set_tuning(20, 20)
+    ob = O.Bvh(tris)
+    want = ob.closest(rays)
+    _assert_bits_equal(_gpu_closest(acc, rays), want, "float nodes camera rays")
+    b = H.bounce_rays(tris, rays, want, 9)
+    _assert_bits_equal(_gpu_closest(acc, b), ob.closest(b), "float nodes bounce rays")
+    occ = acc.trace_any(torch.from_numpy(b).cuda()).cpu().numpy()
+    assert np.array_equal(occ, ob.any(b))
+    g = H.grid_mesh(16)
+    r = H.vertex_edge_rays(16, 7)
+    _assert_bits_equal(_gpu_closest(Accel(g), r), O.closest_brute(g, r), "float nodes grid edges")
+
+
+def test_float_nodes_in_wavefront_frame(krr_lib, cuda, float_nodes):
+    from kiraray_gb300.wavefront import WavefrontPathTracer
+    sc = scenes.cornell_box(32, 32, max_depth=4)
+    pt = WavefrontPathTracer({"max_depth": 4})
+    pt.set_scene(sc)
+    pt.resize(32, 32)
+    pt.begin_frame(1, sc.camera)
+    pt.render()
+    L = pt.radiance().cpu().numpy()[:, :3]
+    oL, _ = O.PathTracer(sc).render({"max_depth": 4}, 1)
+    bad = (np.abs(L - oL) > 1e-4 * np.abs(oL) + 1e-6).any(1).mean()
+    assert bad <= 0.01 and not pt.device_errors()
