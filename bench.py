@@ -43,8 +43,12 @@ def parse():
                          "the faster after autotuning both (outside the timed region)")
     ap.add_argument("--nrc-res", default="480x270",
                     help="resolution of the time-to-relMSE comparison (0 = skip)")
-    ap.add_argument("--nrc-ref-frames", type=int, default=8192)
-    ap.add_argument("--nrc-max-frames", type=int, default=1024)
+    ap.add_argument("--nrc-copies", type=int, default=8,
+                    help="camera replicas traced per launch in the time-to-relMSE runs")
+    ap.add_argument("--nrc-ref-spp", type=int, default=65536)
+    ap.add_argument("--nrc-max-spp", type=int, default=65536)
+    ap.add_argument("--nrc-max-seconds", type=float, default=40.0,
+                    help="device-time cap per tracer in the time-to-relMSE runs")
     return ap.parse_args()
 
 
@@ -167,55 +171,67 @@ def cpu_baseline(tris, ray_sets, seconds: float, threads: int):
 
 def time_to_relmse(args):
     """Time to relMSE 0.01 of the plain tracer and of the neural-cache tracer
-    on the large scene (configs: max depth 8, 1 spp per frame), against an
-    FP64-accumulated reference rendered by the plain tracer."""
+    on the large scene (max depth 8), against an FP64-accumulated reference
+    of --nrc-ref-spp samples per pixel rendered by the plain tracer.  Each
+    launch traces --nrc-copies replicas of the camera (batched views, frames
+    replayed from a captured graph), so a frame adds that many samples."""
     if args.nrc_res in ("0", "", "none"):
         return None
     import torch
     from kiraray_gb300 import scenes
-    from kiraray_gb300.convergence import render_reference, time_to_error
+    from kiraray_gb300.convergence import render_reference_views, time_to_error_views
     from kiraray_gb300.nrc import NeuralRadianceCache
     from kiraray_gb300.wavefront import WavefrontPathTracer
 
     w, h = (int(x) for x in args.nrc_res.split("x"))
+    copies = args.nrc_copies
     sc = scenes.large_scene(width=w, height=h, seed=3)
     params = {"max_depth": 8}
     plain = WavefrontPathTracer(params, seed=3)
     plain.set_scene(sc)
-    plain.resize(w, h)
     t0 = time.perf_counter()
-    ref = render_reference(plain, sc, args.nrc_ref_frames)
+    ref = render_reference_views(plain, sc, copies, max(1, args.nrc_ref_spp // copies))
     torch.cuda.synchronize()
     ref_s = time.perf_counter() - t0
-    res_plain = time_to_error(plain, sc, ref, target=0.01, max_frames=args.nrc_max_frames,
-                              check_every=8)
-    tris = sc.world_triangles().reshape(-1, 3, 3)
-    lo, hi = tris.reshape(-1, 3).min(0), tris.reshape(-1, 3).max(0)
+    max_frames = max(1, args.nrc_max_spp // copies)
+    res_plain = time_to_error_views(plain, sc, ref, copies, target=0.01, max_frames=max_frames,
+                                    check_every=8, max_seconds=args.nrc_max_seconds)
+    tris = sc.world_triangles().reshape(-1, 3)
     pt = WavefrontPathTracer(params, seed=3)
     pt.set_scene(sc)
-    pt.resize(w, h)
-    cache = NeuralRadianceCache(lo, hi, seed=3)
+    cache = NeuralRadianceCache(tris.min(0), tris.max(0), seed=3)
     pt.set_nrc(cache, train=True)
-    res_nrc = time_to_error(pt, sc, ref, target=0.01, max_frames=args.nrc_max_frames,
-                            check_every=8)
+    res_nrc = time_to_error_views(pt, sc, ref, copies, target=0.01, max_frames=max_frames,
+                                  check_every=8, max_seconds=args.nrc_max_seconds)
+
     def extrapolated(res):
-        # unbiased estimator: relMSE ~ 1/frames, so t(0.01) ~ t_final * err / 0.01
+        # unbiased estimator: relMSE ~ 1/samples, so t(0.01) ~ t_final * err / 0.01
         c = res["curve"]
         if res["seconds"] or not c["data"]:
             return res["seconds"]
         return c["timepoints"][-1] * c["data"][-1] / 0.01
 
-    out = {"resolution": f"{w}x{h}", "reference_frames": args.nrc_ref_frames,
+    out = {"resolution": f"{w}x{h}", "views_per_launch": copies,
+           "reference_spp": max(1, args.nrc_ref_spp // copies) * copies,
            "reference_seconds": round(ref_s, 2), "target_relmse": 0.01,
-           "plain_seconds": res_plain["seconds"], "plain_frames": res_plain["frames"],
+           "plain_seconds": res_plain["seconds"], "plain_spp": res_plain["spp"],
+           "plain_ms_per_frame": round(res_plain["ms_per_frame"], 3),
            "plain_final_relmse": res_plain["final_error"],
-           "nrc_seconds": res_nrc["seconds"], "nrc_frames": res_nrc["frames"],
+           "nrc_seconds": res_nrc["seconds"], "nrc_spp": res_nrc["spp"],
+           "nrc_ms_per_frame": round(res_nrc["ms_per_frame"], 3),
            "nrc_final_relmse": res_nrc["final_error"]}
     if not res_plain["seconds"]:
         out["plain_seconds_extrapolated"] = extrapolated(res_plain)
     if res_nrc["seconds"]:
         out["nrc_time_fraction"] = res_nrc["seconds"] / (res_plain["seconds"] or
                                                          extrapolated(res_plain))
+    # equal-time comparison: error of each tracer at the plain run's last time point
+    tp = res_plain["curve"]["timepoints"][-1]
+    nrc_at = [e for t, e in zip(res_nrc["curve"]["timepoints"], res_nrc["curve"]["data"]) if t <= tp]
+    if nrc_at:
+        out["equal_time_seconds"] = round(tp, 3)
+        out["equal_time_relmse"] = {"plain": round(res_plain["curve"]["data"][-1], 5),
+                                    "nrc": round(nrc_at[-1], 5)}
     out["plain_curve_tail"] = list(zip(res_plain["curve"]["timesteps"][-3:],
                                        [round(x, 5) for x in res_plain["curve"]["data"][-3:]]))
     out["nrc_curve_tail"] = list(zip(res_nrc["curve"]["timesteps"][-3:],

@@ -236,6 +236,12 @@ typedef struct krr_wf_params {
     float clamp_max;          /* "clamp_max", default 1e3    */
     int32_t spp;              /* samples per pixel per frame */
     uint32_t seed;            /* added to the per-pixel sample index */
+    /* 0 (default): as the reference, the path radiance L is not cleared
+     * between the samples of one frame, so with spp > 1 the pixel sums
+     * running totals (integrator.cpp:205-221 clears L once per frame,
+     * :255-258 adds L after every sample).  1: L is cleared before every
+     * sample, so the frame is the plain mean of spp independent samples. */
+    int32_t independent_samples;
 } krr_wf_params;
 
 void krr_wf_params_default(krr_wf_params *p);
@@ -314,7 +320,8 @@ int krr_wf_accel(krr_wf *wf, const krr_accel **out);
 /* Online-trained radiance cache (no counterpart in the reference; it plugs
  * into the pass the way PPGPathTracer records per-vertex radiance,
  * src/misc/render/ppg/guideditem.h:119-166).  Query/training records are
- * float[10]: position (world), shading normal, roughness, albedo. */
+ * float[13]: position (world), shading normal, roughness, albedo, outgoing
+ * direction wo (unit, towards the previous path vertex). */
 typedef struct krr_nrc krr_nrc;
 
 typedef struct krr_nrc_config {
@@ -333,6 +340,10 @@ typedef struct krr_nrc_config {
     float scene_lo[3], scene_hi[3];   /* box mapped to the unit cube         */
     int32_t tensor_cores;        /* 1: forward passes on tcgen05 (default);
                                     0: CUDA-core kernels (reference path) */
+    float termination_spread;    /* in a pass: a path stops at a vertex
+                                    and takes the cache's answer once its
+                                    spread a(x1..xn) exceeds this fraction
+                                    of a0 (0.01; 0 = at the first bounce) */
 } krr_nrc_config;
 
 typedef struct krr_nrc_info_t {

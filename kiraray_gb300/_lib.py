@@ -84,7 +84,7 @@ class NrcConfig(C.Structure):
                 ("epsilon", C.c_float), ("loss_scale", C.c_float), ("batch_size", C.c_int32),
                 ("train_pixel_stride", C.c_int32), ("seed", C.c_uint32),
                 ("scene_lo", C.c_float * 3), ("scene_hi", C.c_float * 3),
-                ("tensor_cores", C.c_int32)]
+                ("tensor_cores", C.c_int32), ("termination_spread", C.c_float)]
 
 
 class NrcInfo(C.Structure):
@@ -97,7 +97,7 @@ class NrcInfo(C.Structure):
 class WfParams(C.Structure):
     _fields_ = [("nee", C.c_int32), ("enable_medium", C.c_int32), ("max_depth", C.c_int32),
                 ("rr", C.c_float), ("enable_clamp", C.c_int32), ("clamp_max", C.c_float),
-                ("spp", C.c_int32), ("seed", C.c_uint32)]
+                ("spp", C.c_int32), ("seed", C.c_uint32), ("independent_samples", C.c_int32)]
 
 
 # name -> (restype, argtypes); every function declared in include/krr_gb300.h

@@ -48,6 +48,91 @@ class Accumulator:
         return v.value
 
 
+def replica_views(scene, copies: int, seed_base: int = 0) -> list:
+    """`copies` views of the scene's camera whose seeds are 2^24 apart, so
+    that frame f of view k (sample index f + seed) never repeats another
+    view's sample index while f < 2^24."""
+    return [(scene.camera, scene.width, scene.height, seed_base + (k << 24)) for k in range(copies)]
+
+
+def _add_views(acc: "Accumulator", flat: torch.Tensor, copies: int):
+    n = acc.n
+    for k in range(copies):
+        acc.add(flat[k * n:(k + 1) * n])
+
+
+def render_reference_views(pt, scene, copies: int, frames: int,
+                           first_frame: int = 1 << 22) -> torch.Tensor:
+    """FP64 mean of frames x copies samples per pixel: `copies` replicas of
+    the camera traced together in each launch (a captured frame graph
+    replayed `frames` times).  Frame indices start at `first_frame`, away
+    from those of a measured run.  Returns float32 [n, 4]."""
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        pt.resize_views(replica_views(scene, copies))
+        acc = Accumulator(scene.width, scene.height)
+        out = torch.empty((copies * acc.n, 4), dtype=torch.float32, device="cuda")
+        pt.begin_frame_views(first_frame)
+        pt.render_flat(out)
+        _add_views(acc, out, copies)
+        pt.capture_frame(out)
+        for f in range(1, frames):
+            pt.launch_frame(first_frame + f)
+            _add_views(acc, out, copies)
+        img = acc.image()
+    stream.synchronize()
+    return img
+
+
+def time_to_error_views(pt, scene, ref_rgba: torch.Tensor, copies: int, target: float = 0.01,
+                        max_frames: int = 4096, check_every: int = 16, metric: int = RELMSE,
+                        max_seconds: float | None = None) -> dict:
+    """time_to_error with `copies` replicas of the camera per launch (so each
+    frame adds `copies` samples per pixel) and frames replayed from a
+    captured graph.  Device time of rendering and accumulation counts;
+    error evaluation does not.  Curve timesteps are samples per pixel."""
+    stream = torch.cuda.Stream()
+    curve = {"timesteps": [], "timepoints": [], "data": []}
+    reached = None
+    with torch.cuda.stream(stream):
+        pt.resize_views(replica_views(scene, copies))
+        acc = Accumulator(scene.width, scene.height)
+        out = torch.empty((copies * acc.n, 4), dtype=torch.float32, device="cuda")
+        t_ms = 0.0
+        pending = []
+        for f in range(1, max_frames + 1):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            if f == 1:
+                pt.begin_frame_views(1)
+                pt.render_flat(out)
+            else:
+                pt.launch_frame(f)
+            _add_views(acc, out, copies)
+            e1.record(stream)
+            pending.append((e0, e1))
+            if f == 1:
+                stream.synchronize()
+                pt.capture_frame(out)
+            if f % check_every == 0 or f == max_frames:
+                stream.synchronize()
+                t_ms += sum(a.elapsed_time(b) for a, b in pending)
+                pending = []
+                err = acc.error(ref_rgba, metric)
+                curve["timesteps"].append(acc.frames)
+                curve["timepoints"].append(t_ms / 1e3)
+                curve["data"].append(err)
+                if err <= target:
+                    reached = t_ms / 1e3
+                    break
+                if max_seconds is not None and t_ms / 1e3 >= max_seconds:
+                    break
+    stream.synchronize()
+    return {"seconds": reached, "spp": acc.frames, "frames": acc.frames // copies,
+            "curve": curve, "ms_per_frame": t_ms / max(1, acc.frames // copies),
+            "final_error": curve["data"][-1] if curve["data"] else None}
+
+
 def render_reference(pt, scene, frames: int, first_frame: int = 1_000_000) -> torch.Tensor:
     """Mean of `frames` 1-spp frames accumulated in FP64 (float32 [n, 4])."""
     acc = Accumulator(scene.width, scene.height)

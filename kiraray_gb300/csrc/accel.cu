@@ -397,12 +397,15 @@ __global__ void k_set_mask(float4 *tris, const uint32_t *leaf_of_prim, const uin
     tris[3 * (size_t)k + 1].w = __uint_as_float(mask ? (uint32_t)(mask[p] != 0) : 1u);
 }
 
-template <bool ANY, bool STATS, int FMT>
-__global__ void __launch_bounds__(kTraceThreads)
-k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, TraceLaunch L,
-        unsigned long long *stats) {
+// MODE 0: closest hit, 1: any hit, 2: mixed (any-hit set, then closest set).
+template <int MODE, bool STATS, int FMT>
+__device__ __forceinline__ void trace_body(const float4 *__restrict__ nodes,
+                                           const float4 *__restrict__ tris, const TraceLaunch &L,
+                                           unsigned long long *stats) {
     const int lane = threadIdx.x & 31;
-    const int64_t n = L.d_count ? (int64_t)*L.d_count : L.n;
+    const int64_t n_any = MODE == 2 ? (int64_t)*L.d_any_count : 0;
+    const int64_t n = (L.d_count ? (int64_t)*L.d_count : L.n) + n_any;
+    bool any_ray = MODE == 1;
     uint2 stack[kTraversalStack];
     int sp = 0;
     bool active = false, exhausted = false;
@@ -429,9 +432,15 @@ k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, Trace
             if (!active) {
                 int64_t idx = base + __popc(need & ((1u << lane) - 1));
                 if (idx < n) {
+                    const float4 *po = L.ray_o, *pd = L.ray_d;
+                    if (MODE == 2) {
+                        any_ray = idx < n_any;
+                        if (any_ray) { po = L.any_o; pd = L.any_d; }
+                        else idx -= n_any;
+                    }
                     ray_id = idx;
-                    float4 ro = L.ray_o[idx * L.ray_stride];
-                    float4 rd = L.ray_d[idx * L.ray_stride];
+                    float4 ro = po[idx * L.ray_stride];
+                    float4 rd = pd[idx * L.ray_stride];
                     V3 o = f3(ro), d = f3(rd);
                     r = ray_pre(o, d, ro.w);
                     tmax = rd.w;
@@ -485,7 +494,7 @@ k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, Trace
             float b1, b2;
             float t = tri_test(r, v0, v1, v2, b1, b2);
             uint32_t gid = __float_as_uint(v0.w);
-            if (ANY) {
+            if (any_ray) {
                 if (t > r.tmin && t <= tmax && __float_as_uint(v1.w) != 0u) {
                     best_prim = gid;
                     done = true;
@@ -507,7 +516,7 @@ k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, Trace
         }
         if (!active) continue;
         if (done) {
-            if (ANY) {
+            if (any_ray) {
                 L.occluded[ray_id] = best_prim != KRR_MISS ? 1 : 0;
             } else {
                 float4 h = best_prim != KRR_MISS
@@ -524,6 +533,21 @@ k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, Trace
     }
 }
 
+template <int MODE, bool STATS, int FMT>
+__global__ void __launch_bounds__(kTraceThreads)
+k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, TraceLaunch L,
+        unsigned long long *stats) {
+    trace_body<MODE, STATS, FMT>(nodes, tris, L, stats);
+}
+
+// The mixed launch is held to the closest-hit kernel's 8 blocks per SM (the
+// grid is sized for that occupancy).
+template <int FMT>
+__global__ void __launch_bounds__(kTraceThreads, FMT == 0 ? 8 : 1)
+k_trace_mixed(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, TraceLaunch L) {
+    trace_body<2, false, FMT>(nodes, tris, L, nullptr);
+}
+
 int g_grid_size = 0;
 
 }  // namespace
@@ -533,13 +557,13 @@ int traversal_grid_size() {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<false, false, 0>, kTraceThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<0, false, 0>, kTraceThreads, 0);
     if (per_sm < 1) per_sm = 1;
     g_grid_size = sms * per_sm;
     return g_grid_size;
 }
 
-template <bool ANY, bool STATS>
+template <int MODE, bool STATS>
 static int launch_trace(const krr_accel *a, const TraceLaunch &l, cudaStream_t s,
                         unsigned long long *stats = nullptr) {
     if (!a || !a->d_nodes) return fail(KRR_ERR_NOT_READY, "acceleration structure not built");
@@ -548,23 +572,34 @@ static int launch_trace(const krr_accel *a, const TraceLaunch &l, cudaStream_t s
     TraceLaunch lt = l;
     lt.refill_below = a->refill_below;
     lt.postpone_pct = a->postpone_pct;
-    if (a->node_format == 1)
-        k_trace<ANY, STATS, 1><<<traversal_grid_size(), kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, lt, stats);
-    else
-        k_trace<ANY, STATS, 0><<<traversal_grid_size(), kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, lt, stats);
+    const int grid = traversal_grid_size();
+    if constexpr (MODE == 2) {
+        if (a->node_format == 1)
+            k_trace_mixed<1><<<grid, kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, lt);
+        else
+            k_trace_mixed<0><<<grid, kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, lt);
+    } else {
+        if (a->node_format == 1)
+            k_trace<MODE, STATS, 1><<<grid, kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, lt, stats);
+        else
+            k_trace<MODE, STATS, 0><<<grid, kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, lt, stats);
+    }
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }
 
 int launch_trace_closest(const krr_accel *a, const TraceLaunch &l, cudaStream_t s) {
-    return launch_trace<false, false>(a, l, s);
+    return launch_trace<0, false>(a, l, s);
 }
 int launch_trace_any(const krr_accel *a, const TraceLaunch &l, cudaStream_t s) {
-    return launch_trace<true, false>(a, l, s);
+    return launch_trace<1, false>(a, l, s);
+}
+int launch_trace_mixed(const krr_accel *a, const TraceLaunch &l, cudaStream_t s) {
+    return launch_trace<2, false>(a, l, s);
 }
 int launch_trace_stats(const krr_accel *a, const TraceLaunch &l, bool any,
                        unsigned long long *d_stats, cudaStream_t s) {
-    return any ? launch_trace<true, true>(a, l, s, d_stats) : launch_trace<false, true>(a, l, s, d_stats);
+    return any ? launch_trace<1, true>(a, l, s, d_stats) : launch_trace<0, true>(a, l, s, d_stats);
 }
 
 void accel_free(krr_accel *a) {

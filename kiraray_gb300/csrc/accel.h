@@ -72,10 +72,20 @@ struct TraceLaunch {
     int *err;                 // device error flags
     int refill_below;         // refill a warp's idle lanes when fewer lanes are busy
     int postpone_pct;         // postpone triangles when fewer % of busy lanes have some
+    // Mixed launches only: an any-hit ray set traced in the same launch as
+    // the closest-hit set above (same stride); its rays take indices
+    // [0, *d_any_count) of the shared work counter.
+    const float4 *any_o;
+    const float4 *any_d;
+    const int *d_any_count;
 };
 
 int launch_trace_closest(const krr_accel *a, const TraceLaunch &l, cudaStream_t s);
 int launch_trace_any(const krr_accel *a, const TraceLaunch &l, cudaStream_t s);
+// One launch for an any-hit set (any_o/any_d -> occluded) and a closest-hit
+// set (ray_o/ray_d -> hits): the two sets share one persistent grid, so the
+// latency tail of the longest ray is paid once.
+int launch_trace_mixed(const krr_accel *a, const TraceLaunch &l, cudaStream_t s);
 int traversal_grid_size();
 
 }  // namespace krr

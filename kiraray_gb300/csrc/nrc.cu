@@ -119,7 +119,8 @@ __global__ void k_encode(NrcGrid g, const float *__restrict__ in, const int32_t 
         for (int a = 0; a < 3; ++a) x[o + a] = __float2bfloat16_rn((q[3 + a] + 1.f) * 0.5f);
         x[o + 3] = __float2bfloat16_rn(q[6]);
         for (int a = 0; a < 3; ++a) x[o + 4 + a] = __float2bfloat16_rn(q[7 + a]);
-        for (int k = o + 7; k < kNrcIn; ++k) x[k] = __float2bfloat16_rn(0.f);
+        for (int a = 0; a < 3; ++a) x[o + 7 + a] = __float2bfloat16_rn((q[10 + a] + 1.f) * 0.5f);
+        for (int k = o + 10; k < kNrcIn; ++k) x[k] = __float2bfloat16_rn(0.f);
     }
 }
 
@@ -401,6 +402,7 @@ namespace krr {
 NrcView nrc_view(const krr_nrc *n) { return NrcView{n->grid, n->mlp, n->table, n->weights}; }
 int64_t nrc_batch_size(const krr_nrc *n) { return n->cfg.batch_size; }
 int32_t nrc_train_stride(const krr_nrc *n) { return n->cfg.train_pixel_stride; }
+float nrc_termination_spread(const krr_nrc *n) { return n->cfg.termination_spread; }
 
 int nrc_query_device(krr_nrc *n, const float *d_inputs, const int32_t *d_count, int64_t cap,
                      float *d_out, cudaStream_t s) {
@@ -481,6 +483,7 @@ extern "C" void krr_nrc_config_default(krr_nrc_config *c) {
     c->train_pixel_stride = 16;
     c->seed = 3;
     c->tensor_cores = 1;
+    c->termination_spread = 0.01f;
     for (int k = 0; k < 3; ++k) { c->scene_lo[k] = 0.f; c->scene_hi[k] = 1.f; }
 }
 

@@ -13,7 +13,8 @@ constexpr int kNrcMaxLevels = 16;
 constexpr int kNrcIn = 64;       // padded MLP input width
 constexpr int kNrcWidth = 64;    // hidden width
 constexpr int kNrcOutPad = 16;   // padded output rows (3 used)
-constexpr int kNrcInputs = 10;   // query record: position 3, normal 3, roughness 1, albedo 3
+constexpr int kNrcInputs = 13;   // query record: position 3, normal 3, roughness 1, albedo 3,
+                                 // outgoing direction 3
 
 // Hash-grid description passed by value to kernels.
 struct NrcGrid {
@@ -59,4 +60,6 @@ int nrc_forward_tc(const NrcGrid &g, const NrcMlp &mlp, const float *d_in, const
                    int64_t cap, const __nv_bfloat16 *table, const uint8_t *packed, float *d_out,
                    __nv_bfloat16 *acts, uint32_t *err, cudaStream_t s);
 int32_t nrc_train_stride(const krr_nrc *n);
+float nrc_termination_spread(const krr_nrc *n);
+constexpr int kNrcRecFloats = 20;   // training vertex: record 13 | throughput 3 | L 3 | pad
 }  // namespace krr

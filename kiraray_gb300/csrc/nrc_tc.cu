@@ -175,7 +175,8 @@ __device__ __forceinline__ void encode_row(const NrcGrid &g, const float *q,
     for (int a = 0; a < 3; ++a) x[o + a] = (q[3 + a] + 1.f) * 0.5f;
     x[o + 3] = q[6];
     for (int a = 0; a < 3; ++a) x[o + 4 + a] = q[7 + a];
-    for (int k = o + 7; k < kNrcIn; ++k) x[k] = 0.f;
+    for (int a = 0; a < 3; ++a) x[o + 7 + a] = (q[10 + a] + 1.f) * 0.5f;
+    for (int k = o + 10; k < kNrcIn; ++k) x[k] = 0.f;
 }
 
 // out[i][0..3) for i < *count (or cap); optional per-layer activation dump

@@ -50,7 +50,7 @@ struct DevView {
     int32_t w, h;
     int64_t offset;
     uint32_t sample_index;   // frame_index * spp + seed of the view
-    int32_t pad;
+    uint32_t seed;           // seed of the view (kept for replays without new views)
 };
 
 // Per-frame constants read by kernels from device memory (so that a frame
@@ -104,6 +104,7 @@ struct krr_wf {
     int32_t nrc_rec_max = 0;
     int64_t nrc_slots = 0;
     float *nrc_b_in = nullptr, *nrc_b_t = nullptr;   // training batch
+    float2 *nrc_spread = nullptr;    // [n] path spread (a0, sum of sqrt spreads)
 
     Queue q(int k) const { return Queue{qbuf[k], (int32_t)n, d_counts + k}; }
     int32_t *nrc_q_count() const { return d_counts + 9; }
@@ -441,6 +442,8 @@ struct NrcHook {
     float *rec;
     int32_t *rec_count;
     int32_t rec_max;
+    float2 *spread;            // per pixel: a0, running sum of sqrt spreads
+    float spread_c;            // termination threshold c of a(x1..xn) > c a0
 };
 
 __device__ __forceinline__ void nrc_features(const DevScene &s, const Surf &sf, float *dst) {
@@ -449,23 +452,44 @@ __device__ __forceinline__ void nrc_features(const DevScene &s, const Surf &sf, 
     dst[3] = sf.n.x; dst[4] = sf.n.y; dst[5] = sf.n.z;
     dst[6] = 1.f - m.spec_alpha;
     dst[7] = m.diffuse[0]; dst[8] = m.diffuse[1]; dst[9] = m.diffuse[2];
+    dst[10] = sf.wo.x; dst[11] = sf.wo.y; dst[12] = sf.wo.z;
 }
 
 // Returns true when the path stops here and the cache answers for it.
+// Termination follows the path-spread rule of neural radiance caching
+// (Mueller et al. 2021): with a0 = t0^2 / (4 pi |cos theta1|) at the primary
+// vertex and a(x1..xn) = (sum_i sqrt(t_{i-1}^2 / (p_i |cos theta_i|)))^2,
+// the path stops at the first non-delta vertex where a > c a0.  Specular
+// samples add no spread.  Training pixels record instead of stopping.
 __device__ __forceinline__ bool nrc_vertex(const NrcHook &h, const DevScene &s, const Surf &sf,
                                            const PixelState &ps, uint32_t pixel, uint32_t depth,
-                                           uint32_t bsdf_type, V3 thp, uint32_t *err) {
-    if (!h.mode || depth < 1 || !(bsdf_type & BSDF_SMOOTH)) return false;
+                                           uint32_t prev_flags, V3 thp, float t, V3 dir, V3 pu,
+                                           V3 pl, uint32_t *err) {
+    if (!h.mode) return false;
+    const float cosv = fmaxf(fabsf(dot(sf.n, dir)), 1e-4f);
+    if (depth == 0) {
+        h.spread[pixel] = make_float2(t * t / (4.f * kPi * cosv), 0.f);
+        return false;
+    }
+    float2 sp = h.spread[pixel];
+    if (!(prev_flags & BSDF_SPECULAR) && pl.x > 0.f) {
+        const float pdf = pu.x / pl.x;   // pl = pu / pdf (generateScatterRays)
+        if (pdf > 0.f) sp.y += sqrtf(t * t / (pdf * cosv));
+    }
+    h.spread[pixel] = sp;
+    const DevMaterial &m = s.materials[sf.material];
+    if (m.type != MAT_DIFFUSE && 1.f - m.spec_alpha <= 1e-3f) return false;   // delta BSDF
+    if (sp.y * sp.y <= h.spread_c * sp.x) return false;
     if ((pixel + (uint32_t)h.frame->nrc_offset) % (uint32_t)h.stride == 0u) {
         if (!h.rec) return false;
         uint32_t slot = pixel / (uint32_t)h.stride;
         int k = h.rec_count[slot];
         if (k < h.rec_max) {
-            float *r = h.rec + ((size_t)slot * h.rec_max + k) * 16;
+            float *r = h.rec + ((size_t)slot * h.rec_max + k) * kNrcRecFloats;
             nrc_features(s, sf, r);
             float4 l = ps.L[pixel];
-            r[10] = thp.x; r[11] = thp.y; r[12] = thp.z;
-            r[13] = l.x; r[14] = l.y; r[15] = l.z;
+            r[kNrcInputs + 0] = thp.x; r[kNrcInputs + 1] = thp.y; r[kNrcInputs + 2] = thp.z;
+            r[kNrcInputs + 3] = l.x; r[kNrcInputs + 4] = l.y; r[kNrcInputs + 5] = l.z;
             h.rec_count[slot] = k + 1;
         }
         return false;
@@ -504,13 +528,13 @@ __global__ void k_nrc_targets(const float *__restrict__ rec, const int32_t *__re
         if (pixel >= n_pixels) continue;
         float4 lf = ps.L[pixel];
         for (int k = 0; k < k_n; ++k) {
-            const float *r = rec + ((size_t)s * rec_max + k) * 16;
+            const float *r = rec + ((size_t)s * rec_max + k) * kNrcRecFloats;
             float t[3];
             float lfin[3] = {lf.x, lf.y, lf.z};
             bool ok = true;
             for (int c = 0; c < 3; ++c) {
-                float thp = r[10 + c];
-                t[c] = thp > 0.f ? (lfin[c] - r[13 + c]) / thp : 0.f;
+                float thp = r[kNrcInputs + c];
+                t[c] = thp > 0.f ? (lfin[c] - r[kNrcInputs + 3 + c]) / thp : 0.f;
                 ok = ok && isfinite(t[c]);
             }
             if (!ok) continue;
@@ -580,7 +604,9 @@ __global__ void k_hit_process(DevScene s, Queue rq, const float4 *__restrict__ h
         }
         (void)c0;
         V3 thp = f3(c4);
-        if (nrc_vertex(hook, s, sf, ps, ubits(c5.w), ubits(c4.w), ubits(c3.w), thp, err)) continue;
+        if (hook.mode && nrc_vertex(hook, s, sf, ps, ubits(c5.w), ubits(c4.w), ubits(c3.w), thp, h.x,
+                                    dir, f3(c5), f3(c6), err))
+            continue;
         if (sf.light >= 0) {
             int j = push_slot(hitl.count, hitl.cap, err);
             if (j >= 0) {
@@ -997,11 +1023,14 @@ __global__ void k_shadow_tr(DevScene s, const float4 *__restrict__ nodes,
 }
 
 // pixel += L (integrator.cpp:257-260)
-__global__ void k_accumulate(PixelState ps, int64_t n) {
+// pixel += L after each sample (integrator.cpp:255-258); with `clear` the
+// next sample starts from L = 0 (the reference keeps L for the whole frame).
+__global__ void k_accumulate(PixelState ps, int64_t n, int clear) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         float4 l = ps.L[i], p = ps.pixel[i];
         ps.pixel[i] = make_float4(p.x + l.x, p.y + l.y, p.z + l.z, 0.f);
+        if (clear) ps.L[i] = make_float4(0.f, 0.f, 0.f, l.w);
     }
 }
 
@@ -1131,10 +1160,11 @@ void inverse_transpose(const float *m, float *out) {
 static void free_nrc_buffers(krr_wf *wf) {
     for (void *p : {(void *)wf->nrc_q_in, (void *)wf->nrc_q_meta, (void *)wf->nrc_q_out,
                     (void *)wf->nrc_rec, (void *)wf->nrc_rec_count, (void *)wf->nrc_b_in,
-                    (void *)wf->nrc_b_t})
+                    (void *)wf->nrc_b_t, (void *)wf->nrc_spread})
         cudaFree(p);
     wf->nrc_q_in = nullptr; wf->nrc_q_meta = nullptr; wf->nrc_q_out = nullptr;
     wf->nrc_rec = nullptr; wf->nrc_rec_count = nullptr; wf->nrc_b_in = nullptr; wf->nrc_b_t = nullptr;
+    wf->nrc_spread = nullptr;
     wf->nrc_slots = 0;
 }
 
@@ -1148,7 +1178,8 @@ static int alloc_nrc_buffers(krr_wf *wf) {
     KRR_CUDA(cudaMalloc(&wf->nrc_q_in, (size_t)wf->n * kNrcInputs * sizeof(float)));
     KRR_CUDA(cudaMalloc(&wf->nrc_q_meta, (size_t)wf->n * sizeof(float4)));
     KRR_CUDA(cudaMalloc(&wf->nrc_q_out, (size_t)wf->n * 3 * sizeof(float)));
-    KRR_CUDA(cudaMalloc(&wf->nrc_rec, (size_t)wf->nrc_slots * wf->nrc_rec_max * 16 * sizeof(float)));
+    KRR_CUDA(cudaMalloc(&wf->nrc_rec, (size_t)wf->nrc_slots * wf->nrc_rec_max * kNrcRecFloats * sizeof(float)));
+    KRR_CUDA(cudaMalloc(&wf->nrc_spread, (size_t)wf->n * sizeof(float2)));
     KRR_CUDA(cudaMalloc(&wf->nrc_rec_count, (size_t)wf->nrc_slots * sizeof(int32_t)));
     KRR_CUDA(cudaMemset(wf->nrc_rec_count, 0, (size_t)wf->nrc_slots * sizeof(int32_t)));
     KRR_CUDA(cudaMalloc(&wf->nrc_b_in, (size_t)batch * kNrcInputs * sizeof(float)));
@@ -1188,6 +1219,7 @@ extern "C" void krr_wf_params_default(krr_wf_params *p) {
     p->clamp_max = 1e3f;
     p->spp = 1;
     p->seed = 0;
+    p->independent_samples = 0;
 }
 
 extern "C" int krr_wf_create(const krr_wf_params *params, krr_wf **out) {
@@ -1463,6 +1495,7 @@ extern "C" int krr_wf_resize_views(krr_wf *wf, const krr_view *views, int32_t n_
         layout[i] = DevView{};
         layout[i].w = views[i].width;
         layout[i].h = views[i].height;
+        layout[i].seed = (uint32_t)views[i].seed;
     }
     return set_layout(wf, layout);
 }
@@ -1499,7 +1532,8 @@ static int fill_frame(krr_wf *wf, int64_t frame_index, const krr_camera_desc *si
         KRR_CHECK_ARG(wf->n_views == 1, "the pass has a multi-view layout: use begin_frame_views");
         DevView v = wf->layout[0];
         KRR_TRY(make_camera(single, v.cam));
-        v.sample_index = (uint32_t)(frame_index * wf->params.spp + wf->params.seed);
+        v.seed = (uint32_t)wf->params.seed;
+        v.sample_index = (uint32_t)(frame_index * wf->params.spp + v.seed);
         wf->layout[0] = v;
     } else if (views) {
         KRR_CHECK_ARG(n_views == wf->n_views, "view count differs from the layout");
@@ -1507,8 +1541,13 @@ static int fill_frame(krr_wf *wf, int64_t frame_index, const krr_camera_desc *si
             KRR_CHECK_ARG(views[i].width == wf->layout[i].w && views[i].height == wf->layout[i].h,
                           "view size differs from the layout");
             KRR_TRY(make_camera(&views[i].camera, wf->layout[i].cam));
+            wf->layout[i].seed = (uint32_t)views[i].seed;
             wf->layout[i].sample_index = (uint32_t)(frame_index * wf->params.spp + views[i].seed);
         }
+    } else {
+        // same cameras, next frame
+        for (int i = 0; i < wf->n_views; ++i)
+            wf->layout[i].sample_index = (uint32_t)(frame_index * wf->params.spp + wf->layout[i].seed);
     }
     for (int i = 0; i < wf->n_views; ++i) dv[i] = wf->layout[i];
     fc->n_views = wf->n_views;
@@ -1570,11 +1609,8 @@ extern "C" int krr_wf_reset_queues(krr_wf *wf, int32_t depth, void *stream) {
     return KRR_OK;
 }
 
-extern "C" int krr_wf_trace_closest(krr_wf *wf, int32_t depth, void *stream) {
-    KRR_TRY(ready(wf));
-    cudaStream_t st = as_stream(stream);
-    int cur = depth & 1;
-    Queue rq = wf->q(cur);
+static TraceLaunch closest_launch(krr_wf *wf, int depth) {
+    Queue rq = wf->q(depth & 1);
     TraceLaunch l{};
     l.ray_o = rq.base;
     l.ray_d = rq.base + wf->n;
@@ -1583,7 +1619,15 @@ extern "C" int krr_wf_trace_closest(krr_wf *wf, int32_t depth, void *stream) {
     l.hits = wf->hits;
     l.counter = wf->accel.d_scratch;
     l.err = wf->accel.d_scratch + 4;
-    KRR_TRY(launch_trace_closest(&wf->accel, l, st));
+    return l;
+}
+
+// Routing of the closest hits of ray queue `depth` (already traced into
+// wf->hits when `traced`).
+static int closest_stage(krr_wf *wf, int depth, cudaStream_t st, bool traced) {
+    int cur = depth & 1;
+    Queue rq = wf->q(cur);
+    if (!traced) KRR_TRY(launch_trace_closest(&wf->accel, closest_launch(wf, depth), st));
     NrcHook hook{};
     if (wf->nrc) {
         hook.mode = 1;
@@ -1596,6 +1640,8 @@ extern "C" int krr_wf_trace_closest(krr_wf *wf, int32_t depth, void *stream) {
         hook.rec = wf->nrc_train ? wf->nrc_rec : nullptr;
         hook.rec_count = wf->nrc_rec_count;
         hook.rec_max = wf->nrc_rec_max;
+        hook.spread = wf->nrc_spread;
+        hook.spread_c = nrc_termination_spread(wf->nrc);
         KRR_CUDA(cudaMemsetAsync(wf->nrc_q_count(), 0, sizeof(int32_t), st));
     }
     k_hit_process<<<wf->grid, kThreads, 0, st>>>(wf->scene, rq, wf->hits, wf->q(cur ^ 1),
@@ -1608,6 +1654,28 @@ extern "C" int krr_wf_trace_closest(krr_wf *wf, int32_t depth, void *stream) {
         k_nrc_apply<<<wf->grid, kThreads, 0, st>>>(wf->nrc_q_out, wf->nrc_q_meta, wf->nrc_q_count(), wf->ps);
         KRR_CUDA(cudaGetLastError());
     }
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_trace_closest(krr_wf *wf, int32_t depth, void *stream) {
+    KRR_TRY(ready(wf));
+    return closest_stage(wf, depth, as_stream(stream), false);
+}
+
+// Shadow rays of bounce `depth` and the closest-hit rays of bounce depth+1
+// in one traversal launch (surfaces only: with media the shadow rays need
+// transmittance tracking).  The shadow results are resolved right away, as
+// traceShadow does; the hits wait in wf->hits for closest_stage(depth + 1).
+static int trace_shadow_and_next(krr_wf *wf, int depth, cudaStream_t st) {
+    Queue sq = wf->q(Q_SHADOW);
+    TraceLaunch l = closest_launch(wf, depth + 1);
+    l.any_o = sq.base;
+    l.any_d = sq.base + wf->n;
+    l.d_any_count = sq.count;
+    l.occluded = wf->occluded;
+    KRR_TRY(launch_trace_mixed(&wf->accel, l, st));
+    k_shadow_resolve<<<wf->grid, kThreads, 0, st>>>(sq, wf->occluded, wf->ps);
+    KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }
 
@@ -1673,22 +1741,30 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
     KRR_TRY(ready(wf));
     KRR_CHECK_ARG(d_out != nullptr, "output is NULL");
     cudaStream_t st = as_stream(stream);
+    // Without media, the shadow rays of a bounce and the next bounce's rays
+    // are traced in one launch; results and their order of use are those of
+    // the stage-by-stage loop (integrator.cpp:223-254).
+    const bool fuse = wf->params.nee && !wf->medium;
     for (int s = 0; s < wf->params.spp; ++s) {
         KRR_TRY(krr_wf_reset_queues(wf, -1, stream));
         KRR_TRY(krr_wf_generate_camera_rays(wf, stream));
+        bool traced = false;
         for (int depth = 0;; ++depth) {
             KRR_TRY(krr_wf_reset_queues(wf, depth, stream));
-            KRR_TRY(krr_wf_trace_closest(wf, depth, stream));
+            KRR_TRY(closest_stage(wf, depth, st, traced));
             if (wf->medium) KRR_TRY(krr_wf_sample_medium_interaction(wf, depth, stream));
             KRR_TRY(krr_wf_handle_hit(wf, stream));
             KRR_TRY(krr_wf_handle_miss(wf, stream));
             if (depth == wf->params.max_depth) break;
             if (wf->medium) KRR_TRY(krr_wf_sample_medium_scattering(wf, depth, stream));
             KRR_TRY(krr_wf_generate_scatter_rays(wf, depth, stream));
-            if (wf->params.nee) KRR_TRY(krr_wf_trace_shadow(wf, stream));
+            traced = fuse;
+            if (fuse) KRR_TRY(trace_shadow_and_next(wf, depth, st));
+            else if (wf->params.nee) KRR_TRY(krr_wf_trace_shadow(wf, stream));
         }
         if (wf->nrc && wf->nrc_train) KRR_TRY(nrc_train_frame(wf, st));
-        k_accumulate<<<wf->grid, kThreads, 0, st>>>(wf->ps, wf->n);
+        k_accumulate<<<wf->grid, kThreads, 0, st>>>(wf->ps, wf->n,
+                                                     wf->params.independent_samples && s + 1 < wf->params.spp);
         KRR_CUDA(cudaGetLastError());
     }
     k_resolve<<<wf->grid, kThreads, 0, st>>>(wf->ps, reinterpret_cast<float4 *>(d_out), wf->d_views,

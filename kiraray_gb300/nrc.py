@@ -1,7 +1,7 @@
 """Neural radiance cache (hash grid + MLP) over the C ABI.
 
     cache = NeuralRadianceCache(scene_lo, scene_hi)
-    pred = cache.query(records)            # float32 [n, 10] CUDA -> [n, 3]
+    pred = cache.query(records)            # float32 [n, 13] CUDA -> [n, 3]
     loss = cache.train_step(records, targets)
     pass_.set_nrc(cache, train=True)       # attach to a WavefrontPathTracer
 """
@@ -17,11 +17,21 @@ from ._lib import check
 
 CONFIG_KEYS = ("n_levels", "features_per_level", "log2_table_size", "base_resolution",
                "max_resolution", "hidden_layers", "learning_rate", "beta1", "beta2", "epsilon",
-               "loss_scale", "batch_size", "train_pixel_stride", "seed", "tensor_cores")
+               "loss_scale", "batch_size", "train_pixel_stride", "seed", "tensor_cores",
+               "termination_spread")
+
+
+RECORD_FLOATS = 13   # position 3, normal 3, roughness 1, albedo 3, outgoing direction 3
 
 
 def _stream() -> int:
     return torch.cuda.current_stream().cuda_stream
+
+
+def _check_records(records: torch.Tensor) -> None:
+    if records.dim() != 2 or records.shape[1] != RECORD_FLOATS or records.dtype != torch.float32:
+        raise ValueError(f"records must be float32 [n, {RECORD_FLOATS}], got "
+                         f"{records.dtype} {tuple(records.shape)}")
 
 
 class NeuralRadianceCache:
@@ -44,6 +54,7 @@ class NeuralRadianceCache:
         return i
 
     def query(self, records: torch.Tensor) -> torch.Tensor:
+        _check_records(records)
         records = records.contiguous()
         out = torch.empty((records.shape[0], 3), dtype=torch.float32, device="cuda")
         check(self.lib.krr_nrc_query(self._h, records.data_ptr(), records.shape[0], out.data_ptr(),
@@ -51,6 +62,7 @@ class NeuralRadianceCache:
         return out
 
     def train_step(self, records: torch.Tensor, targets: torch.Tensor) -> float:
+        _check_records(records)
         loss = C.c_float()
         check(self.lib.krr_nrc_train_step(self._h, records.contiguous().data_ptr(),
                                           targets.contiguous().data_ptr(), records.shape[0],

@@ -43,7 +43,7 @@ class WavefrontPathTracer:
     # from_json, integrator.h:94-103
     def _apply(self, params: dict):
         for k, v in params.items():
-            if k not in PARAM_NAMES + ("spp", "seed"):
+            if k not in PARAM_NAMES + ("spp", "seed", "independent_samples"):
                 raise KeyError(f"unknown parameter {k!r}")
             setattr(self.params, k, type(getattr(self.params, k))(v))
 

@@ -89,6 +89,7 @@ def encode(grid: Grid, table: np.ndarray, inputs: np.ndarray, rounding=True):
     X[:, o:o + 3] = (inputs[:, 3:6].astype(np.float64) + 1) * 0.5
     X[:, o + 3] = inputs[:, 6]
     X[:, o + 4:o + 7] = inputs[:, 7:10]
+    X[:, o + 7:o + 10] = (inputs[:, 10:13].astype(np.float64) + 1) * 0.5
     if rounding:
         X = bf16(X)
     return X, cs

@@ -892,6 +892,9 @@ void render_pixel(const oracle_pt &s, const krr_wf_params &prm, const Camera &ca
             ps = next;
         }
         pixel = pixel + L;
+        // the reference keeps L across the samples of a frame
+        // (integrator.cpp:205-221, 255-258); independent_samples clears it
+        if (prm.independent_samples && spp + 1 < prm.spp) L = v3(0.f);
     }
     L_out = L;
     pixel_out = pixel;

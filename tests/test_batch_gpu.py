@@ -89,3 +89,31 @@ def test_graph_replay_with_cache_training(krr_lib, cuda):
     assert cache.info().step == 11
     assert torch.isfinite(out).all()
     assert pt.device_errors() == 0
+
+
+def test_single_view_graph_replay_advances_samples(krr_lib, cuda):
+    """resize() + begin_frame(camera) + capture; replays without new cameras
+    keep the camera and seed and move to the frame's sample index."""
+    sc = scenes.cornell_box(24, 16, max_depth=4)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        pt = WavefrontPathTracer({"max_depth": 4}, seed=7)
+        pt.set_scene(sc)
+        pt.resize(24, 16)
+        out = torch.empty((16, 24, 4), device="cuda")
+        pt.begin_frame(1, sc.camera)
+        pt.render(out)
+        pt.capture_frame(out)
+        got = {}
+        for f in (5, 6):
+            pt.launch_frame(f)
+            s.synchronize()
+            got[f] = out.cpu().numpy().copy()
+        ref = WavefrontPathTracer({"max_depth": 4}, seed=7)
+        ref.set_scene(sc)
+        ref.resize(24, 16)
+        for f in (5, 6):
+            ref.begin_frame(f, sc.camera)
+            want = ref.render().cpu().numpy()
+            assert np.array_equal(got[f].view(np.uint32), want.view(np.uint32)), f
+    assert not np.array_equal(got[5], got[6])

@@ -17,12 +17,14 @@ SMALL = dict(n_levels=8, log2_table_size=14, base_resolution=4, max_resolution=1
 
 def _records(n, seed):
     rng = np.random.default_rng(seed)
-    r = np.zeros((n, 10), np.float32)
+    r = np.zeros((n, 13), np.float32)
     r[:, :3] = rng.random((n, 3)) * 2 - 1
     nrm = rng.normal(size=(n, 3))
     r[:, 3:6] = nrm / np.linalg.norm(nrm, axis=1, keepdims=True)
     r[:, 6] = rng.random(n)
     r[:, 7:10] = rng.random((n, 3))
+    wo = rng.normal(size=(n, 3))
+    r[:, 10:13] = wo / np.linalg.norm(wo, axis=1, keepdims=True)
     return r
 
 
@@ -141,3 +143,27 @@ def test_cache_in_the_pass(krr_lib, cuda):
     mn = (acc_n / 60)[..., :3].mean().item()
     assert torch.isfinite(acc_n).all()
     assert abs(mn - mp) < 0.15 * mp, (mn, mp)
+
+
+def test_spread_threshold_controls_termination(krr_lib, cuda):
+    """With an unreachable spread threshold no path stops at the cache, so the
+    pass draws the same samples as the plain tracer and the frame is equal
+    bit for bit; with threshold 0 paths stop at their first rough vertex."""
+    sc = scenes.cornell_box(48, 48, max_depth=5)
+    plain = WavefrontPathTracer({"max_depth": 5})
+    plain.set_scene(sc)
+    plain.resize(48, 48)
+    plain.begin_frame(3, sc.camera)
+    want = plain.render().cpu().numpy()
+    imgs = {}
+    for c in (1e30, 0.0):
+        pt = WavefrontPathTracer({"max_depth": 5})
+        pt.set_scene(sc)
+        pt.resize(48, 48)
+        cache = NeuralRadianceCache((0, 0, 0), (1, 1, 1), batch_size=4096, termination_spread=c)
+        pt.set_nrc(cache, train=False)
+        pt.begin_frame(3, sc.camera)
+        imgs[c] = pt.render().cpu().numpy()
+        assert pt.device_errors() == 0
+    assert np.array_equal(imgs[1e30].view(np.uint32), want.view(np.uint32))
+    assert not np.array_equal(imgs[0.0], want)

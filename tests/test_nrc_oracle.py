@@ -17,7 +17,7 @@ def _tiny(seed=0):
     w = np.zeros(2 * R.WIDTH * R.IN + R.OUT_PAD * R.IN)
     w[:] = rng.normal(size=w.size) * 0.2
     mlp = R.Mlp(w, layers)
-    inp = rng.random((6, 10))
+    inp = rng.random((6, 13))
     inp[:, 3:6] = inp[:, 3:6] * 2 - 1
     t = rng.random((6, 3))
     return grid, table, mlp, inp, t, n_entries

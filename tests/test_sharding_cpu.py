@@ -80,7 +80,7 @@ def _grad_shards(rank, world):
     grid = R.Grid(info, [0, 0, 0], [1, 1, 1], table_size=64)
     table = rng.normal(size=91 * 2) * 0.2
     mlp = R.Mlp(rng.normal(size=2 * R.WIDTH * R.IN + R.OUT_PAD * R.IN) * 0.2, 3)
-    inp = rng.random((64, 10))
+    inp = rng.random((64, 13))
     t = rng.random((64, 3))
     shard = slice(rank * 32, rank * 32 + 32)
 

@@ -94,6 +94,27 @@ def test_spp_and_seed(krr_lib, cuda):
     assert bad.any(axis=2).mean() <= MAX_OUTLIERS
 
 
+def test_independent_samples(krr_lib, cuda):
+    """independent_samples=1: L cleared between the samples of a frame; the
+    default keeps the reference's running sum, so the two frames differ."""
+    sc = scenes.cornell_box(48, 48, max_depth=3)
+    imgs = {}
+    for ind in (0, 1):
+        pt = WavefrontPathTracer({"max_depth": 3, "independent_samples": ind}, spp=4, seed=5)
+        pt.set_scene(sc)
+        pt.resize(sc.width, sc.height)
+        pt.begin_frame(3, sc.camera)
+        imgs[ind] = pt.render().cpu().numpy()
+        _, opx = O.PathTracer(sc).render({"max_depth": 3, "independent_samples": ind}, 3,
+                                         spp=4, seed=5)
+        want = (opx / 4.0).reshape(48, 48, 3)[::-1]
+        bad = np.abs(imgs[ind][..., :3] - want) > RTOL * np.abs(want) + ATOL
+        assert bad.any(axis=2).mean() <= MAX_OUTLIERS
+    # running sums weigh the first sample 4x: the mean is ~2.5x the independent one
+    ratio = imgs[0][..., :3].mean() / imgs[1][..., :3].mean()
+    assert 1.8 < ratio < 3.2
+
+
 def test_stage_api_and_queue_sizes(krr_lib, cuda):
     sc = scenes.cornell_box(32, 32)
     pt = WavefrontPathTracer({"max_depth": 5})
@@ -112,6 +133,35 @@ def test_stage_api_and_queue_sizes(krr_lib, cuda):
     pt.generate_scatter_rays(0)
     assert pt.queue_size(1) <= n_scatter
     pt.trace_shadow()
+    assert pt.device_errors() == 0
+
+
+def test_render_equals_stage_loop(krr_lib, cuda):
+    """render() traces each bounce's shadow rays together with the next
+    bounce's rays; the radiance must equal the stage-by-stage loop of
+    integrator.cpp:223-254 bit for bit."""
+    sc = scenes.large_scene(width=96, height=64, grid=256, n_spheres=40, sky_size=(64, 32))
+    depth_max = 6
+    pt = WavefrontPathTracer({"max_depth": depth_max}, seed=4)
+    pt.set_scene(sc)
+    pt.resize(96, 64)
+    pt.begin_frame(2, sc.camera)
+    pt.render()
+    fused = pt.radiance().cpu().numpy()
+    pt.begin_frame(2, sc.camera)
+    pt.reset_queues(-1)
+    pt.generate_camera_rays()
+    for d in range(depth_max + 1):
+        pt.reset_queues(d)
+        pt.trace_closest(d)
+        pt.handle_hit()
+        pt.handle_miss()
+        if d == depth_max:
+            break
+        pt.generate_scatter_rays(d)
+        pt.trace_shadow()
+    staged = pt.radiance().cpu().numpy()
+    assert np.array_equal(fused.view(np.uint32), staged.view(np.uint32))
     assert pt.device_errors() == 0
 
 
