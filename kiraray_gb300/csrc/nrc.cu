@@ -44,6 +44,7 @@ struct krr_nrc {
     float *loss = nullptr;                   // device loss accumulator
     int32_t *count_buf = nullptr;
     uint8_t *packed = nullptr;               // weights in tcgen05 canonical tiles
+    uint8_t *packed_t = nullptr;             // transposed weights (backward)
     uint32_t *err = nullptr;                 // device error flags
 };
 
@@ -300,25 +301,56 @@ __global__ void k_adam_step(int64_t *step, double b1, double b2) {
     bc[1] = (float)(1.0 - pow(b2, (double)t));
 }
 
+struct AdamArgs {
+    float lr, b1, b2, eps, grad_scale, bc1, bc2;
+};
+
+// One Adam update; a non-finite gradient leaves the parameter and its moments
+// unchanged.  Returns the new FP32 master weight.
+__device__ __forceinline__ float adam_one(const AdamArgs &a, float g, float &m, float &v, float w) {
+    float gr = g * a.grad_scale;
+    if (!isfinite(gr)) return w;
+    m = a.b1 * m + (1.f - a.b1) * gr;
+    v = a.b2 * v + (1.f - a.b2) * gr * gr;
+    return w - a.lr * (m / a.bc1) / (sqrtf(v / a.bc2) + a.eps);
+}
+
+// Adam over n parameters (FP32 masters w, moments m and v, gradient grad which
+// is cleared, BF16 copy wb).  Streams four parameters per thread and step with
+// 16-byte accesses and every load issued before the arithmetic (the kernel is
+// bound by HBM bandwidth: 34 bytes per parameter).
 __global__ void k_adam(float *__restrict__ w, float *__restrict__ m, float *__restrict__ v,
                        float *__restrict__ grad, __nv_bfloat16 *__restrict__ wb, int64_t n, float lr,
-                       float b1, float b2, float eps, float grad_scale, const int64_t *__restrict__ step,
-                       const uint8_t *__restrict__ frozen) {
-    const float bc1 = reinterpret_cast<const float *>(step + 1)[0];
-    const float bc2 = reinterpret_cast<const float *>(step + 1)[1];
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        float gr = grad[i] * grad_scale;
+                       float b1, float b2, float eps, float grad_scale, const int64_t *__restrict__ step) {
+    AdamArgs a{lr, b1, b2, eps, grad_scale, reinterpret_cast<const float *>(step + 1)[0],
+               reinterpret_cast<const float *>(step + 1)[1]};
+    const int64_t n4 = n >> 2;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += stride) {
+        float4 g = reinterpret_cast<const float4 *>(grad)[i];
+        float4 mm = reinterpret_cast<const float4 *>(m)[i];
+        float4 vv = reinterpret_cast<const float4 *>(v)[i];
+        float4 ww = reinterpret_cast<const float4 *>(w)[i];
+        reinterpret_cast<float4 *>(grad)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        ww.x = adam_one(a, g.x, mm.x, vv.x, ww.x);
+        ww.y = adam_one(a, g.y, mm.y, vv.y, ww.y);
+        ww.z = adam_one(a, g.z, mm.z, vv.z, ww.z);
+        ww.w = adam_one(a, g.w, mm.w, vv.w, ww.w);
+        reinterpret_cast<float4 *>(m)[i] = mm;
+        reinterpret_cast<float4 *>(v)[i] = vv;
+        reinterpret_cast<float4 *>(w)[i] = ww;
+        __nv_bfloat162 lo = __floats2bfloat162_rn(ww.x, ww.y), hi = __floats2bfloat162_rn(ww.z, ww.w);
+        uint2 packed = make_uint2(*reinterpret_cast<uint32_t *>(&lo), *reinterpret_cast<uint32_t *>(&hi));
+        reinterpret_cast<uint2 *>(wb)[i] = packed;
+    }
+    for (int64_t i = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        float g = grad[i], mm = m[i], vv = v[i];
         grad[i] = 0.f;
-        if (frozen && frozen[i]) continue;
-        if (!isfinite(gr)) continue;
-        float mi = b1 * m[i] + (1.f - b1) * gr;
-        float vi = b2 * v[i] + (1.f - b2) * gr * gr;
-        m[i] = mi;
-        v[i] = vi;
-        float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
-        w[i] = wi;
-        wb[i] = __float2bfloat16_rn(wi);
+        float ww = adam_one(a, g, mm, vv, w[i]);
+        m[i] = mm;
+        v[i] = vv;
+        w[i] = ww;
+        wb[i] = __float2bfloat16_rn(ww);
     }
 }
 
@@ -413,53 +445,75 @@ int nrc_query_device(krr_nrc *n, const float *d_inputs, const int32_t *d_count, 
     return KRR_OK;
 }
 
-int nrc_train_device(krr_nrc *n, const float *d_inputs, const float *d_targets,
-                     const int32_t *d_count, int64_t cap, cudaStream_t s) {
-    if (cap <= 0) return KRR_OK;
-    KRR_TRY(forward(n, d_inputs, d_count, cap, s));
+// Loss, MLP backward and hash-grid backward of the last forward pass (its
+// activations in n->act): w_grad and table_grad receive the scaled gradients.
+int backward(krr_nrc *n, const float *d_inputs, const float *d_targets, const int32_t *d_count,
+             int64_t cap, cudaStream_t s) {
     const float scale = n->cfg.loss_scale;
-    int blocks = grid_for(cap, 128);
     KRR_CUDA(cudaMemsetAsync(n->loss, 0, sizeof(float), s));
     k_loss<<<grid_for(cap), kThreads, 0, s>>>(n->out, d_targets, d_count, cap, scale, n->dA, n->loss);
     KRR_CUDA(cudaGetLastError());
-    // backward through the layers: dA holds dY of layer l (width N_l)
     float *dY = n->dA, *dX = n->dB;
-    int wblocks = grid_for(cap, 64);
-    for (int l = n->mlp.layers - 1; l >= 0; --l) {
-        const __nv_bfloat16 *X = n->act + (size_t)l * cap * kNrcIn;
-        const __nv_bfloat16 *W = n->weights + n->mlp.w_offset[l];
-        float *dW = n->w_grad + n->mlp.w_offset[l];
-        bool out_layer = l + 1 == n->mlp.layers;
-        if (out_layer) k_dense_wgrad<kNrcOutPad><<<wblocks, kThreads, 0, s>>>(dY, X, d_count, cap, dW);
-        else k_dense_wgrad<kNrcWidth><<<wblocks, kThreads, 0, s>>>(dY, X, d_count, cap, dW);
-        KRR_CUDA(cudaGetLastError());
-        if (l > 0) {
-            if (out_layer) k_dense_bwd<kNrcOutPad, true><<<blocks, kThreads, 0, s>>>(dY, W, X, d_count, cap, dX);
-            else k_dense_bwd<kNrcWidth, true><<<blocks, kThreads, 0, s>>>(dY, W, X, d_count, cap, dX);
-        } else {
-            if (out_layer) k_dense_bwd<kNrcOutPad, false><<<blocks, kThreads, 0, s>>>(dY, W, X, d_count, cap, dX);
-            else k_dense_bwd<kNrcWidth, false><<<blocks, kThreads, 0, s>>>(dY, W, X, d_count, cap, dX);
+    if (n->cfg.tensor_cores) {
+        // dX0 -> dB, dW += on the tensor cores
+        KRR_TRY(nrc_backward_tc(n->mlp, n->dA, n->act, d_count, cap, n->packed_t, n->dB, n->w_grad,
+                                n->err, s));
+        dY = n->dB;
+    } else {
+        // backward through the layers: dY holds the gradient of layer l's output
+        int blocks = grid_for(cap, 128);
+        int wblocks = grid_for(cap, 64);
+        for (int l = n->mlp.layers - 1; l >= 0; --l) {
+            const __nv_bfloat16 *X = n->act + (size_t)l * cap * kNrcIn;
+            const __nv_bfloat16 *W = n->weights + n->mlp.w_offset[l];
+            float *dW = n->w_grad + n->mlp.w_offset[l];
+            bool out_layer = l + 1 == n->mlp.layers;
+            if (out_layer) k_dense_wgrad<kNrcOutPad><<<wblocks, kThreads, 0, s>>>(dY, X, d_count, cap, dW);
+            else k_dense_wgrad<kNrcWidth><<<wblocks, kThreads, 0, s>>>(dY, X, d_count, cap, dW);
+            KRR_CUDA(cudaGetLastError());
+            if (l > 0) {
+                if (out_layer) k_dense_bwd<kNrcOutPad, true><<<blocks, kThreads, 0, s>>>(dY, W, X, d_count, cap, dX);
+                else k_dense_bwd<kNrcWidth, true><<<blocks, kThreads, 0, s>>>(dY, W, X, d_count, cap, dX);
+            } else {
+                if (out_layer) k_dense_bwd<kNrcOutPad, false><<<blocks, kThreads, 0, s>>>(dY, W, X, d_count, cap, dX);
+                else k_dense_bwd<kNrcWidth, false><<<blocks, kThreads, 0, s>>>(dY, W, X, d_count, cap, dX);
+            }
+            KRR_CUDA(cudaGetLastError());
+            std::swap(dY, dX);
         }
-        KRR_CUDA(cudaGetLastError());
-        std::swap(dY, dX);
     }
     // dY now holds the gradient of the encoded input
     k_encode_bwd<<<grid_for(cap), kThreads, 0, s>>>(n->grid, d_inputs, dY, d_count, cap, n->table_grad);
     KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+// Both weight layouts of the tensor-core kernels, from the BF16 weights.
+int pack_weights(krr_nrc *n, cudaStream_t s) {
+    if (!n->cfg.tensor_cores) return KRR_OK;
+    KRR_TRY(nrc_pack_weights(n->weights, n->mlp, n->packed, s));
+    return nrc_pack_weights_t(n->weights, n->mlp, n->packed_t, s);
+}
+
+int nrc_train_device(krr_nrc *n, const float *d_inputs, const float *d_targets,
+                     const int32_t *d_count, int64_t cap, cudaStream_t s) {
+    if (cap <= 0) return KRR_OK;
+    KRR_TRY(forward(n, d_inputs, d_count, cap, s));
+    KRR_TRY(backward(n, d_inputs, d_targets, d_count, cap, s));
+    const float scale = n->cfg.loss_scale;
     // Adam
     const krr_nrc_config &c = n->cfg;
     k_adam_step<<<1, 1, 0, s>>>(n->step, (double)c.beta1, (double)c.beta2);
     k_adam<<<grid_for(n->mlp.n_params), kThreads, 0, s>>>(n->w_master, n->w_m, n->w_v, n->w_grad,
                                                            n->weights, n->mlp.n_params, c.learning_rate,
                                                            c.beta1, c.beta2, c.epsilon, 1.f / scale,
-                                                           n->step, nullptr);
+                                                           n->step);
     int64_t tn = (int64_t)n->n_entries * n->grid.features;
     k_adam<<<grid_for(tn), kThreads, 0, s>>>(n->table_master, n->table_m, n->table_v, n->table_grad,
                                              n->table, tn, c.learning_rate, c.beta1, c.beta2,
-                                             c.epsilon, 1.f / scale, n->step, nullptr);
+                                             c.epsilon, 1.f / scale, n->step);
     KRR_CUDA(cudaGetLastError());
-    if (n->cfg.tensor_cores) KRR_TRY(nrc_pack_weights(n->weights, n->mlp, n->packed, s));
-    return KRR_OK;
+    return pack_weights(n, s);
 }
 
 }  // namespace krr
@@ -563,6 +617,7 @@ extern "C" int krr_nrc_create(const krr_nrc_config *cfg, krr_nrc **out) {
     alloc((void **)&n->table, tn * 2);
     alloc((void **)&n->loss, 16);
     alloc((void **)&n->packed, (size_t)(m.layers - 1) * kNrcWidth * kNrcIn * 2 + kNrcOutPad * kNrcIn * 2);
+    alloc((void **)&n->packed_t, (size_t)(m.layers - 1) * kNrcWidth * kNrcIn * 2 + kNrcIn * kNrcOutPad * 2);
     alloc((void **)&n->err, 16);
     alloc((void **)&n->step, 16);
     if (st == KRR_OK) {
@@ -570,7 +625,7 @@ extern "C" int krr_nrc_create(const krr_nrc_config *cfg, krr_nrc **out) {
         cudaMemcpy(n->table_master, t.data(), tn * 4, cudaMemcpyHostToDevice);
         k_to_bf16<<<grid_for(m.n_params), kThreads>>>(n->w_master, n->weights, m.n_params);
         k_to_bf16<<<grid_for((int64_t)tn), kThreads>>>(n->table_master, n->table, (int64_t)tn);
-        if (cfg->tensor_cores) nrc_pack_weights(n->weights, n->mlp, n->packed, 0);
+        pack_weights(n, 0);
         cudaError_t e = cudaDeviceSynchronize();
         if (e != cudaSuccess) st = cuda_status(e, "krr_nrc_create", __FILE__, __LINE__);
     }
@@ -589,7 +644,7 @@ extern "C" int krr_nrc_destroy(krr_nrc *n) {
                     (void *)n->table_grad, (void *)n->table, (void *)n->w_master, (void *)n->w_m,
                     (void *)n->w_v, (void *)n->w_grad, (void *)n->weights, (void *)n->act,
                     (void *)n->out, (void *)n->dA, (void *)n->dB, (void *)n->loss,
-                    (void *)n->packed, (void *)n->err, (void *)n->step})
+                    (void *)n->packed, (void *)n->packed_t, (void *)n->err, (void *)n->step})
         cudaFree(p);
     delete n;
     return KRR_OK;
@@ -651,7 +706,7 @@ extern "C" int krr_nrc_set_params(krr_nrc *n, int32_t which, const float *h_src,
     KRR_CUDA(cudaDeviceSynchronize());
     KRR_CUDA(cudaMemcpy(dst, h_src, total * 4, cudaMemcpyHostToDevice));
     k_to_bf16<<<grid_for(total), kThreads>>>(dst, bdst, total);
-    if (which == 0 && n->cfg.tensor_cores) KRR_TRY(nrc_pack_weights(n->weights, n->mlp, n->packed, 0));
+    if (which == 0) KRR_TRY(pack_weights(n, 0));
     KRR_CUDA(cudaDeviceSynchronize());
     return KRR_OK;
 }
@@ -665,33 +720,11 @@ extern "C" int krr_nrc_gradients(krr_nrc *n, const float *d_inputs, const float 
     KRR_CHECK_ARG(n && d_inputs && d_targets && count > 0, "bad argument");
     cudaStream_t s = 0;
     KRR_TRY(forward(n, d_inputs, nullptr, count, s));
-    // reuse the training path but stop before Adam
+    // the training path, stopped before Adam
     float scale = n->cfg.loss_scale;
-    int blocks = grid_for(count, 128);
-    KRR_CUDA(cudaMemset(n->loss, 0, sizeof(float)));
     KRR_CUDA(cudaMemset(n->w_grad, 0, n->mlp.n_params * 4));
     KRR_CUDA(cudaMemset(n->table_grad, 0, (size_t)n->n_entries * 2 * 4));
-    k_loss<<<grid_for(count), kThreads, 0, s>>>(n->out, d_targets, nullptr, count, scale, n->dA, n->loss);
-    float *dY = n->dA, *dX = n->dB;
-    int wblocks = grid_for(count, 64);
-    for (int l = n->mlp.layers - 1; l >= 0; --l) {
-        const __nv_bfloat16 *X = n->act + (size_t)l * count * kNrcIn;
-        const __nv_bfloat16 *W = n->weights + n->mlp.w_offset[l];
-        float *dW = n->w_grad + n->mlp.w_offset[l];
-        bool out_layer = l + 1 == n->mlp.layers;
-        if (out_layer) k_dense_wgrad<kNrcOutPad><<<wblocks, kThreads, 0, s>>>(dY, X, nullptr, count, dW);
-        else k_dense_wgrad<kNrcWidth><<<wblocks, kThreads, 0, s>>>(dY, X, nullptr, count, dW);
-        if (l > 0) {
-            if (out_layer) k_dense_bwd<kNrcOutPad, true><<<blocks, kThreads, 0, s>>>(dY, W, X, nullptr, count, dX);
-            else k_dense_bwd<kNrcWidth, true><<<blocks, kThreads, 0, s>>>(dY, W, X, nullptr, count, dX);
-        } else {
-            if (out_layer) k_dense_bwd<kNrcOutPad, false><<<blocks, kThreads, 0, s>>>(dY, W, X, nullptr, count, dX);
-            else k_dense_bwd<kNrcWidth, false><<<blocks, kThreads, 0, s>>>(dY, W, X, nullptr, count, dX);
-        }
-        std::swap(dY, dX);
-    }
-    k_encode_bwd<<<grid_for(count), kThreads, 0, s>>>(n->grid, d_inputs, dY, nullptr, count, n->table_grad);
-    KRR_CUDA(cudaGetLastError());
+    KRR_TRY(backward(n, d_inputs, d_targets, nullptr, count, s));
     KRR_CUDA(cudaDeviceSynchronize());
     std::vector<float> tmp;
     if (h_grad_mlp) {

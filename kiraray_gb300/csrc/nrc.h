@@ -56,6 +56,12 @@ int64_t nrc_batch_size(const krr_nrc *n);
 // tcgen05 forward (nrc_tc.cu)
 size_t nrc_tc_smem_bytes(int layers);
 int nrc_pack_weights(const __nv_bfloat16 *w, const NrcMlp &mlp, uint8_t *packed, cudaStream_t s);
+// tcgen05 backward (nrc_tc.cu): transposed weight tiles, then dX0 and dW.
+size_t nrc_tc_bwd_smem_bytes(int layers);
+int nrc_pack_weights_t(const __nv_bfloat16 *w, const NrcMlp &mlp, uint8_t *packed, cudaStream_t s);
+int nrc_backward_tc(const NrcMlp &mlp, const float *d_dy_out, const __nv_bfloat16 *acts,
+                    const int32_t *d_count, int64_t cap, const uint8_t *packed_wt, float *d_dx0,
+                    float *d_dw, uint32_t *err, cudaStream_t s);
 int nrc_forward_tc(const NrcGrid &g, const NrcMlp &mlp, const float *d_in, const int32_t *d_count,
                    int64_t cap, const __nv_bfloat16 *table, const uint8_t *packed, float *d_out,
                    __nv_bfloat16 *acts, uint32_t *err, cudaStream_t s);

@@ -297,6 +297,221 @@ k_nrc_forward_tc(NrcGrid g, int layers, const float *__restrict__ in, const int3
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols));
 }
 
+// ------------------------------------------------------------------ backward
+//
+// Per 128-row tile, from the output layer down: dX_l = dY_l . W_l (M=128,
+// N=64, K=64 or 16) and dW_l += dY_l^T . X_l (M=128 with rows 64..127 of the
+// A operand zero, N=64, K=128 rows of the tile).  The dX accumulator (64
+// columns) is read back each layer, masked by ReLU'(X_l), rounded to BF16
+// and becomes the next layer's dY tile (row-major and transposed copies);
+// the dW_l accumulators (64 columns each) stay in tensor memory for all of
+// the CTA's tiles and are added to the FP32 gradient once at the end.
+// Operand rounding points match the CUDA-core kernels: dY, W and X in BF16,
+// FP32 accumulation.
+
+constexpr uint32_t kBwCols = 512;
+constexpr int kT128Bytes = 128 * 128 * 2;   // [128][128] canonical tile, 32 KB
+constexpr int kXtBytes = 64 * 128 * 2;      // [64][128], 16 KB
+constexpr int kA64Bytes = 128 * 64 * 2;     // [128][64], 16 KB
+constexpr int kA16Bytes = 128 * 16 * 2;     // [128][16], 4 KB
+constexpr int kWtOutBytes = 64 * 16 * 2;    // W_out^T [64][16], 2 KB
+
+// Byte offset of element (r, k) in a canonical K-major tile of `cols` columns.
+__host__ __device__ __forceinline__ uint32_t canon_c(uint32_t r, uint32_t k, uint32_t cols) {
+    return (((r >> 3) * (cols >> 3) + (k >> 3)) * 128u) + (r & 7u) * 16u + (k & 7u) * 2u;
+}
+
+// Transposed weights: hidden layer l as W_l^T [64 in][64 out] at l * 8 KB,
+// the output layer as W^T [64 in][16 out] after them.
+__global__ void k_pack_weights_t(const __nv_bfloat16 *__restrict__ w, NrcMlp mlp, uint8_t *packed) {
+    int total = mlp.n_params;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        int l = 0;
+        while (l + 1 < mlp.layers && e >= mlp.w_offset[l + 1]) ++l;
+        int local = e - mlp.w_offset[l];
+        int r = local / kNrcIn, k = local % kNrcIn;   // W_l[r][k]
+        size_t off = l + 1 < mlp.layers ? (size_t)l * kLayerBytes + canon_c(k, r, 64)
+                                        : (size_t)l * kLayerBytes + canon_c(k, r, 16);
+        *reinterpret_cast<__nv_bfloat16 *>(packed + off) = w[e];
+    }
+}
+
+__device__ __forceinline__ void store_bf16(uint8_t *tile, uint32_t off, float v) {
+    *reinterpret_cast<__nv_bfloat16 *>(tile + off) = __float2bfloat16_rn(v);
+}
+
+// Bounded wait on the CTA's mbarrier by thread 0, decision shared through
+// shared memory; returns false (all threads) when the wait gave up.
+__device__ __forceinline__ bool cta_wait(uint32_t mbar, uint32_t phase, uint32_t *fail_flag,
+                                         uint32_t *err) {
+    if (threadIdx.x == 0) {
+        uint32_t spins = 0, ok = 0;
+        while (!(ok = mbar_try_wait(mbar, phase)) && ++spins < kWaitLimit) {
+        }
+        *fail_flag = ok ? 0u : 1u;
+        if (!ok) atomicOr(err, (uint32_t)kErrLoopLimit);
+    }
+    __syncthreads();
+    if (*fail_flag) return false;
+    uint32_t spins = 0;   // already complete: returns at once
+    while (!mbar_try_wait(mbar, phase) && ++spins < kWaitLimit) {
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_nrc_backward_tc(int layers, const float *__restrict__ dy_out, const __nv_bfloat16 *__restrict__ acts,
+                  const int32_t *d_count, int64_t cap, const uint8_t *__restrict__ packed_wt,
+                  float *__restrict__ dx0, float *__restrict__ dw, NrcMlp mlp, uint32_t *err) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    const int wt_bytes = (layers - 1) * kLayerBytes + kWtOutBytes;
+    uint8_t *swt = smem;
+    uint8_t *at = smem + ((wt_bytes + 1023) & ~1023);   // dY_l^T, rows 64..127 zero
+    uint8_t *at16 = at + kT128Bytes;                     // dY_out^T, rows 16..127 zero
+    uint8_t *xt = at16 + kT128Bytes;                     // X_l^T
+    uint8_t *a64 = xt + kXtBytes;                        // dY_l
+    uint8_t *a16 = a64 + kA64Bytes;                      // dY_out
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(a16 + kA16Bytes);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
+    uint32_t *fail_flag = tmem_slot + 1;
+    const int tid = threadIdx.x, warp = tid >> 5;
+
+    for (int e = tid; e < wt_bytes / 16; e += blockDim.x)
+        reinterpret_cast<uint4 *>(swt)[e] = reinterpret_cast<const uint4 *>(packed_wt)[e];
+    for (int e = tid; e < 2 * kT128Bytes / 16; e += blockDim.x)
+        reinterpret_cast<uint4 *>(at)[e] = make_uint4(0u, 0u, 0u, 0u);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tmem_slot)),
+                     "r"(kBwCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        mbar_init(smem_u32(mbar), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t my_lanes = (uint32_t)(warp * 32) << 16;
+
+    const int64_t n = d_count ? min((int64_t)*d_count, cap) : cap;
+    const int64_t tiles = (n + kTcRows - 1) / kTcRows;
+    uint32_t phase = 0;
+    bool failed = false, any_tile = false;
+    for (int64_t t = blockIdx.x; t < tiles && !failed; t += gridDim.x) {
+        const int64_t row = t * kTcRows + tid;
+        const bool live = row < n;
+        // dY of the output layer: row-major [128][16] and transposed [16 of 128][128]
+        {
+            float d[kNrcOutPad];
+            for (int c = 0; c < kNrcOutPad; ++c) d[c] = live ? dy_out[row * kNrcOutPad + c] : 0.f;
+            for (int c = 0; c < kNrcOutPad; ++c) {
+                store_bf16(a16, canon_c((uint32_t)tid, (uint32_t)c, 16), d[c]);
+                store_bf16(at16, canon_c((uint32_t)c, (uint32_t)tid, 128), d[c]);
+            }
+        }
+        for (int l = layers - 1; l >= 0 && !failed; --l) {
+            const bool out_layer = l == layers - 1;
+            // X_l^T and the ReLU mask of X_l
+            uint64_t mask = 0;
+            {
+                const uint4 *src = reinterpret_cast<const uint4 *>(acts + ((size_t)l * cap + row) * kNrcIn);
+                for (int j = 0; j < 8; ++j) {
+                    uint4 q = live ? src[j] : make_uint4(0u, 0u, 0u, 0u);
+                    const __nv_bfloat16 *h = reinterpret_cast<const __nv_bfloat16 *>(&q);
+                    for (int i = 0; i < 8; ++i) {
+                        const int k = 8 * j + i;
+                        *reinterpret_cast<__nv_bfloat16 *>(xt + canon_c((uint32_t)k, (uint32_t)tid, 128)) = h[i];
+                        if (__bfloat162float(h[i]) > 0.f) mask |= 1ull << k;
+                    }
+                }
+            }
+            fence_proxy_async();
+            fence_before_sync();
+            __syncthreads();
+            if (tid == 0) {
+                fence_after_sync();
+                // dW_l += dY_l^T . X_l   (K = the tile's 128 rows)
+                const uint32_t a0 = smem_u32(out_layer ? at16 : at), b0 = smem_u32(xt);
+                const uint32_t dcol = tmem + 64u + 64u * (uint32_t)l;
+                const uint32_t idw = idesc_bf16(kTcRows, 64);
+#pragma unroll
+                for (int kk = 0; kk < 8; ++kk)
+                    tc_mma(dcol, smem_desc(a0 + 256u * kk, 128u, 2048u), smem_desc(b0 + 256u * kk, 128u, 2048u),
+                           idw, (any_tile || kk > 0) ? 1u : 0u);
+                // dX = dY_l . W_l  (K = 16 for the output layer, 64 otherwise)
+                const uint32_t wt = smem_u32(swt + l * kLayerBytes);
+                if (out_layer) {
+                    tc_mma(tmem, smem_desc(smem_u32(a16), 128u, 256u), smem_desc(wt, 128u, 256u),
+                           idesc_bf16(kTcRows, 64), 0u);
+                } else {
+                    const uint32_t a1 = smem_u32(a64);
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk)
+                        tc_mma(tmem, smem_desc(a1 + 256u * kk, 128u, 1024u), smem_desc(wt + 256u * kk, 128u, 1024u),
+                               idesc_bf16(kTcRows, 64), kk > 0 ? 1u : 0u);
+                }
+                tc_commit(smem_u32(mbar));
+            }
+            if (!cta_wait(smem_u32(mbar), phase, fail_flag, err)) {
+                failed = true;
+                break;
+            }
+            phase ^= 1u;
+            fence_after_sync();
+            float v[kNrcIn];
+            tmem_ld16(tmem + my_lanes + 0, v);
+            tmem_ld16(tmem + my_lanes + 16, v + 16);
+            tmem_ld16(tmem + my_lanes + 32, v + 32);
+            tmem_ld16(tmem + my_lanes + 48, v + 48);
+            tmem_wait_ld();
+            if (l > 0) {
+                for (int k = 0; k < kNrcIn; ++k) {
+                    const float d = ((mask >> k) & 1ull) ? v[k] : 0.f;
+                    v[k] = d;
+                    store_bf16(at, canon_c((uint32_t)k, (uint32_t)tid, 128), d);
+                }
+                store_row(a64, (uint32_t)tid, v);
+                fence_proxy_async();
+            } else if (live) {
+                float4 *dst = reinterpret_cast<float4 *>(dx0 + row * kNrcIn);
+                for (int k = 0; k < kNrcIn / 4; ++k)
+                    dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+            }
+            fence_before_sync();
+            __syncthreads();
+        }
+        any_tile = true;
+    }
+    // dW accumulators: rows 0..63 (out features) live in the lanes of warps 0-1
+    if (!failed && any_tile && warp < 2) {
+        fence_after_sync();
+        const int m = tid;   // out-feature row of dW_l
+        for (int l = 0; l < layers; ++l) {
+            const int rows = l + 1 == layers ? kNrcOutPad : kNrcWidth;
+            float v[kNrcIn];
+            const uint32_t base = tmem + my_lanes + 64u + 64u * (uint32_t)l;
+            tmem_ld16(base + 0, v);
+            tmem_ld16(base + 16, v + 16);
+            tmem_ld16(base + 32, v + 32);
+            tmem_ld16(base + 48, v + 48);
+            tmem_wait_ld();
+            if (m < rows) {
+                float *dst = dw + mlp.w_offset[l] + (size_t)m * kNrcIn;
+                for (int k = 0; k < kNrcIn; ++k) atomicAdd(dst + k, v[k]);
+            }
+        }
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kBwCols));
+}
+
 }  // namespace
 
 size_t nrc_tc_smem_bytes(int layers) {
@@ -308,6 +523,39 @@ size_t nrc_tc_smem_bytes(int layers) {
 int nrc_pack_weights(const __nv_bfloat16 *w, const NrcMlp &mlp, uint8_t *packed, cudaStream_t s) {
     cudaMemsetAsync(packed, 0, (size_t)(mlp.layers - 1) * kLayerBytes + kOutBytes, s);
     k_pack_weights<<<64, 256, 0, s>>>(w, mlp, packed);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+size_t nrc_tc_bwd_smem_bytes(int layers) {
+    size_t w = (size_t)(layers - 1) * kLayerBytes + kWtOutBytes;
+    return ((w + 1023) & ~(size_t)1023) + 2 * kT128Bytes + kXtBytes + kA64Bytes + kA16Bytes + 64 + 1024;
+}
+
+int nrc_pack_weights_t(const __nv_bfloat16 *w, const NrcMlp &mlp, uint8_t *packed, cudaStream_t s) {
+    cudaMemsetAsync(packed, 0, (size_t)(mlp.layers - 1) * kLayerBytes + kWtOutBytes, s);
+    k_pack_weights_t<<<64, 256, 0, s>>>(w, mlp, packed);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+int nrc_backward_tc(const NrcMlp &mlp, const float *d_dy_out, const __nv_bfloat16 *acts,
+                    const int32_t *d_count, int64_t cap, const uint8_t *packed_wt, float *d_dx0,
+                    float *d_dw, uint32_t *err, cudaStream_t s) {
+    static bool configured = false;
+    size_t smem = nrc_tc_bwd_smem_bytes(mlp.layers);
+    if (!configured) {
+        KRR_CUDA(cudaFuncSetAttribute(k_nrc_backward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+        configured = true;
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int64_t tiles = (cap + kTcRows - 1) / kTcRows;
+    int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sms));
+    k_nrc_backward_tc<<<grid, kTcThreads, smem, s>>>(mlp.layers, d_dy_out, acts, d_count, cap, packed_wt,
+                                                     d_dx0, d_dw, mlp, err);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }

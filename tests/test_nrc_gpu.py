@@ -167,3 +167,26 @@ def test_spread_threshold_controls_termination(krr_lib, cuda):
         assert pt.device_errors() == 0
     assert np.array_equal(imgs[1e30].view(np.uint32), want.view(np.uint32))
     assert not np.array_equal(imgs[0.0], want)
+
+
+@pytest.mark.parametrize("n", [1, 100, 128, 1000, 4096])
+def test_tensor_core_backward_matches_cuda_core_kernels(krr_lib, cuda, n):
+    """tcgen05 backward (dX chain and per-layer dW accumulated in tensor
+    memory) against the CUDA-core kernels with the same BF16 operands."""
+    lo, hi = (-1, -1, -1), (1, 1, 1)
+    tc = NeuralRadianceCache(lo, hi, tensor_cores=1, **SMALL)
+    ref = NeuralRadianceCache(lo, hi, tensor_cores=0, **SMALL)
+    rec = _records(4096, 8)
+    for _ in range(10):
+        tc.train_step(torch.from_numpy(rec).cuda(), torch.from_numpy(_targets(rec)).cuda())
+    ref.set_params(0, tc.params(0))
+    ref.set_params(1, tc.params(1))
+    q = torch.from_numpy(rec[:n]).cuda()
+    t = torch.from_numpy(_targets(rec[:n])).cuda()
+    gm_a, gt_a, la = tc.gradients(q, t)
+    gm_b, gt_b, lb = ref.gradients(q, t)
+    assert np.isfinite(gm_a).all() and np.isfinite(gt_a).all()
+    assert abs(la - lb) <= 5e-3 * abs(lb) + 1e-7
+    assert _rel(gm_a, gm_b) < 2e-2
+    assert _rel(gt_a, gt_b) < 2e-2
+    assert tc.info().step == 10
