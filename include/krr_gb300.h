@@ -311,6 +311,14 @@ int krr_wf_read_radiance(krr_wf *wf, float *d_dst, void *stream);
  * the item count is krr_wf_queue_size(depth & 1). */
 int krr_wf_ray_queue(krr_wf *wf, int32_t depth, const float **d_origin_tmin,
                      const float **d_dir_tmax, const float **d_pu_pixel, int32_t *capacity);
+/* SoA view of any queue (the reference's queue pointers that stage-level
+ * subclasses read, workqueue.h:159-359): `channels` planes of float4, plane
+ * c of item i at d_base + 4 * (c * capacity + i) floats; the layouts per
+ * queue are those of the pass (Ray/Miss: o|tmin, d|tmax, ctx.p|medium,
+ * ctx.n|bsdfType, thp|depth, pu|pixel, pl|time; Shadow: o|tmin, d|tmax,
+ * Ld|pixel, pu|medium, pl|time; ...).  Valid until the next resize. */
+int krr_wf_queue_view(krr_wf *wf, int32_t queue, const float **d_base, int32_t *channels,
+                      int32_t *capacity);
 /* Error flags raised by device code since the last call (cleared on read). */
 int krr_wf_device_errors(krr_wf *wf, uint32_t *out_flags, void *stream);
 /* The BVH of the current scene (owned by the pass). */

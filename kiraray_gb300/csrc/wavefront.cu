@@ -1811,6 +1811,16 @@ extern "C" int krr_wf_ray_queue(krr_wf *wf, int32_t depth, const float **d_origi
     return KRR_OK;
 }
 
+extern "C" int krr_wf_queue_view(krr_wf *wf, int32_t queue, const float **d_base, int32_t *channels,
+                                 int32_t *capacity) {
+    KRR_TRY(ready(wf));
+    KRR_CHECK_ARG(queue >= 0 && queue < Q_COUNT && d_base, "bad queue");
+    *d_base = reinterpret_cast<const float *>(wf->qbuf[queue]);
+    if (channels) *channels = kChannels[queue];
+    if (capacity) *capacity = (int32_t)wf->n;
+    return KRR_OK;
+}
+
 extern "C" int krr_wf_device_errors(krr_wf *wf, uint32_t *out, void *stream) {
     KRR_CHECK_ARG(wf && out, "NULL argument");
     uint32_t flags[2] = {0, 0};

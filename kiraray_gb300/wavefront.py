@@ -26,6 +26,15 @@ def _stream() -> int:
     return torch.cuda.current_stream().cuda_stream
 
 
+class _DeviceArray:
+    """float32 device memory owned by the pass, seen through the CUDA array
+    interface (no copy)."""
+
+    def __init__(self, ptr: int, shape: tuple):
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": "<f4", "data": (ptr, False),
+                                         "version": 3, "strides": None}
+
+
 class WavefrontPathTracer:
     def __init__(self, params: dict | None = None, spp: int = 1, seed: int = 0):
         self.lib = _lib.load()
@@ -155,6 +164,15 @@ class WavefrontPathTracer:
         v = C.c_int32()
         check(self.lib.krr_wf_queue_size(self._h, queue, C.byref(v), _stream()), "queue_size")
         return v.value
+
+    def queue_items(self, queue: int) -> torch.Tensor:
+        """Copy of a queue's live items: float32 [count, channels, 4]."""
+        base, ch, cap = C.c_void_p(), C.c_int32(), C.c_int32()
+        check(self.lib.krr_wf_queue_view(self._h, queue, C.byref(base), C.byref(ch), C.byref(cap)),
+              "queue_view")
+        n = self.queue_size(queue)
+        planes = torch.as_tensor(_DeviceArray(base.value, (ch.value, cap.value, 4)), device="cuda")
+        return planes[:, :n, :].permute(1, 0, 2).contiguous()
 
     def radiance(self) -> torch.Tensor:
         """Per-pixel L (the reference's PixelState::L) as float32 [pixels, 4]."""

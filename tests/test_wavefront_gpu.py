@@ -132,6 +132,11 @@ def test_stage_api_and_queue_sizes(krr_lib, cuda):
     pt.handle_miss()
     pt.generate_scatter_rays(0)
     assert pt.queue_size(1) <= n_scatter
+    shadow = pt.queue_items(4)
+    assert shadow.shape[1:] == (5, 4) and shadow.shape[0] == pt.queue_size(4)
+    if shadow.shape[0]:
+        # shadow rays end on the light sample: tMax = 1 (spawnRayTo)
+        assert torch.all(shadow[:, 1, 3] == 1.0)
     pt.trace_shadow()
     assert pt.device_errors() == 0
 
