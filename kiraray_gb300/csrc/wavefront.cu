@@ -682,81 +682,130 @@ __global__ void k_handle_miss(DevScene s, Queue miss, PixelState ps, int nee) {
     }
 }
 
-// generateScatterRays, integrator.cpp:110-164
-__global__ void k_scatter(DevScene s, Queue scat, Queue next, Queue shadow, PixelState ps, int nee,
-                          float rr, uint32_t *err) {
-    int n = *scat.count;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 c0 = scat.at(0, i), c1 = scat.at(1, i), c2 = scat.at(2, i), c3 = scat.at(3, i);
-        float4 c4 = scat.at(4, i), c5 = scat.at(5, i), c6 = scat.at(6, i), c7 = scat.at(7, i);
-        uint32_t pixel = ubits(c2.w), depth = ubits(c1.w);
-        Pcg rng = load_rng(ps, pixel);
-        if (rng.get1d() >= rr) {
-            store_rng(ps, pixel, rng);
-            continue;
-        }
-        V3 thp = f3(c5) / rr;
-        V3 p = f3(c0), wo = f3(c1), nrm = f3(c2), tg = f3(c3), bt = f3(c4), pu = f3(c6);
-        float time = c6.w;
-        int32_t material = sbits(c0.w), mesh = sbits(c3.w), ray_medium = sbits(c7.x);
-        const DevMesh &M = s.meshes[mesh];
-        bool transition = M.medium_inside != M.medium_outside;
-        int32_t mi = transition ? M.medium_inside : -2, mo = transition ? M.medium_outside : -2;
-        auto to_local = [&](V3 v) { return V3{dot(tg, v), dot(bt, v), dot(nrm, v)}; };
-        V3 wo_local = to_local(wo);
-        ShadingData sd = shading_data(s, material);
-        uint32_t bsdf_type = bsdf_type_of(sd);
-        Bsdf bsdf = Bsdf::setup(sd);
-        if (nee && (bsdf_type & BSDF_SMOOTH)) {
-            float ul = rng.get1d();
-            uint32_t lid = (uint32_t)(ul * (float)s.n_lights);
-            float sel_pdf = 1.f / (float)s.n_lights;
-            float u0 = rng.get1d(), u1 = rng.get1d();
-            LightSample ls = sample_li(s, s.lights[lid], u0, u1, p);
-            // spawnRayTo(Interaction), raytracing.h:151-160
-            V3 to = offset_ray_origin(ls.p, ls.n, p - ls.p);
-            V3 po = offset_ray_origin(p, nrm, to - p);
-            V3 d = to - po;
-            V3 wi_world = normalize(d);
-            V3 wi_local = to_local(wi_world);
-            float light_pdf = sel_pdf * ls.pdf;
-            V3 fv = bsdf.f(wo_local, wi_local);
-            float bsdf_pdf = bsdf.pdf(wo_local, wi_local);
-            if (light_pdf > 0 && any(fv)) {
-                V3 Ld = ls.L * thp * fv * fabsf(wi_local.z);
-                if (any(Ld)) {
-                    int j = push_slot(shadow.count, shadow.cap, err);
-                    if (j >= 0) {
-                        int32_t med = medium_towards(mi, mo, ray_medium, nrm, d);
-                        shadow.at(0, j) = f4(po, 0.f);
-                        shadow.at(1, j) = f4(d, 1.f);
-                        shadow.at(2, j) = f4(Ld, fbits(pixel));
-                        shadow.at(3, j) = f4(pu * bsdf_pdf, ibits(med));
-                        shadow.at(4, j) = f4(pu * light_pdf, time);
-                    }
-                }
-            }
-        }
-        BsdfSample bs = bsdf.sample(wo_local, [&]() { return rng.get1d(); });
-        store_rng(ps, pixel, rng);
-        if (bs.pdf != 0 && any(bs.f)) {
-            V3 wi_world = tg * bs.wi.x + bt * bs.wi.y + nrm * bs.wi.z;
-            V3 nthp = thp * bs.f * fabsf(bs.wi.z) / bs.pdf;
-            if (any(nthp)) {
-                int j = push_slot(next.count, next.cap, err);
+// generateScatterRays (integrator.cpp:110-164) for one item whose Russian
+// roulette draw has survived; `rng` is the pixel's sampler after that draw.
+__device__ __forceinline__ void scatter_item(const DevScene &s, const Queue &scat, int i, Pcg rng,
+                                             const Queue &next, const Queue &shadow,
+                                             const PixelState &ps, int nee, float rr, uint32_t *err) {
+    float4 c0 = scat.at(0, i), c1 = scat.at(1, i), c2 = scat.at(2, i), c3 = scat.at(3, i);
+    float4 c4 = scat.at(4, i), c5 = scat.at(5, i), c6 = scat.at(6, i), c7 = scat.at(7, i);
+    uint32_t pixel = ubits(c2.w), depth = ubits(c1.w);
+    V3 thp = f3(c5) / rr;
+    V3 p = f3(c0), wo = f3(c1), nrm = f3(c2), tg = f3(c3), bt = f3(c4), pu = f3(c6);
+    float time = c6.w;
+    int32_t material = sbits(c0.w), mesh = sbits(c3.w), ray_medium = sbits(c7.x);
+    const DevMesh &M = s.meshes[mesh];
+    bool transition = M.medium_inside != M.medium_outside;
+    int32_t mi = transition ? M.medium_inside : -2, mo = transition ? M.medium_outside : -2;
+    auto to_local = [&](V3 v) { return V3{dot(tg, v), dot(bt, v), dot(nrm, v)}; };
+    V3 wo_local = to_local(wo);
+    ShadingData sd = shading_data(s, material);
+    uint32_t bsdf_type = bsdf_type_of(sd);
+    Bsdf bsdf = Bsdf::setup(sd);
+    if (nee && (bsdf_type & BSDF_SMOOTH)) {
+        float ul = rng.get1d();
+        uint32_t lid = (uint32_t)(ul * (float)s.n_lights);
+        float sel_pdf = 1.f / (float)s.n_lights;
+        float u0 = rng.get1d(), u1 = rng.get1d();
+        LightSample ls = sample_li(s, s.lights[lid], u0, u1, p);
+        // spawnRayTo(Interaction), raytracing.h:151-160
+        V3 to = offset_ray_origin(ls.p, ls.n, p - ls.p);
+        V3 po = offset_ray_origin(p, nrm, to - p);
+        V3 d = to - po;
+        V3 wi_world = normalize(d);
+        V3 wi_local = to_local(wi_world);
+        float light_pdf = sel_pdf * ls.pdf;
+        V3 fv = bsdf.f(wo_local, wi_local);
+        float bsdf_pdf = bsdf.pdf(wo_local, wi_local);
+        if (light_pdf > 0 && any(fv)) {
+            V3 Ld = ls.L * thp * fv * fabsf(wi_local.z);
+            if (any(Ld)) {
+                int j = push_slot(shadow.count, shadow.cap, err);
                 if (j >= 0) {
-                    V3 o = offset_ray_origin(p, nrm, wi_world);
-                    int32_t med = medium_towards(mi, mo, ray_medium, nrm, wi_world);
-                    next.at(0, j) = f4(o, 0.f);
-                    next.at(1, j) = f4(wi_world, INFINITY);
-                    next.at(2, j) = f4(p, ibits(med));
-                    next.at(3, j) = f4(nrm, fbits(bs.flags));
-                    next.at(4, j) = f4(nthp, fbits(depth + 1));
-                    next.at(5, j) = f4(pu, fbits(pixel));
-                    next.at(6, j) = f4(pu / bs.pdf, time);
+                    int32_t med = medium_towards(mi, mo, ray_medium, nrm, d);
+                    shadow.at(0, j) = f4(po, 0.f);
+                    shadow.at(1, j) = f4(d, 1.f);
+                    shadow.at(2, j) = f4(Ld, fbits(pixel));
+                    shadow.at(3, j) = f4(pu * bsdf_pdf, ibits(med));
+                    shadow.at(4, j) = f4(pu * light_pdf, time);
                 }
             }
         }
+    }
+    BsdfSample bs = bsdf.sample(wo_local, [&]() { return rng.get1d(); });
+    store_rng(ps, pixel, rng);
+    if (bs.pdf != 0 && any(bs.f)) {
+        V3 wi_world = tg * bs.wi.x + bt * bs.wi.y + nrm * bs.wi.z;
+        V3 nthp = thp * bs.f * fabsf(bs.wi.z) / bs.pdf;
+        if (any(nthp)) {
+            int j = push_slot(next.count, next.cap, err);
+            if (j >= 0) {
+                V3 o = offset_ray_origin(p, nrm, wi_world);
+                int32_t med = medium_towards(mi, mo, ray_medium, nrm, wi_world);
+                next.at(0, j) = f4(o, 0.f);
+                next.at(1, j) = f4(wi_world, INFINITY);
+                next.at(2, j) = f4(p, ibits(med));
+                next.at(3, j) = f4(nrm, fbits(bs.flags));
+                next.at(4, j) = f4(nthp, fbits(depth + 1));
+                next.at(5, j) = f4(pu, fbits(pixel));
+                next.at(6, j) = f4(pu / bs.pdf, time);
+            }
+        }
+    }
+}
+
+constexpr int kScatterThreads = 256;
+
+// generateScatterRays, integrator.cpp:110-164.  Each block takes a tile of
+// 256 items, draws their Russian roulette, and regroups the survivors by
+// material type in shared memory before shading, so that a warp runs one
+// BSDF.  Every item is computed exactly as alone (its sampler stream is its
+// pixel's); only the order of the queue pushes changes.
+__global__ void __launch_bounds__(kScatterThreads, 4)
+k_scatter(DevScene s, Queue scat, Queue next, Queue shadow, PixelState ps, int nee, float rr,
+          uint32_t *err) {
+    __shared__ int sh_count[5];                  // material types 0..3, 4 = ended by RR
+    __shared__ int sh_base[5];
+    __shared__ uint16_t sh_item[kScatterThreads];
+    __shared__ ulonglong2 sh_rng[kScatterThreads];
+    const int n = *scat.count;
+    const int t = threadIdx.x;
+    for (int base = blockIdx.x * kScatterThreads; base < n; base += gridDim.x * kScatterThreads) {
+        if (t < 5) sh_count[t] = 0;
+        __syncthreads();
+        const int i = base + t;
+        int cls = -1;
+        Pcg rng{0, 0};
+        if (i < n) {
+            uint32_t pixel = ubits(scat.at(2, i).w);
+            rng = load_rng(ps, pixel);
+            if (rng.get1d() >= rr) {
+                store_rng(ps, pixel, rng);
+                cls = 4;
+            } else {
+                cls = min(max(s.materials[sbits(scat.at(0, i).w)].type, 0), 3);
+            }
+        }
+        const int rank = cls >= 0 ? atomicAdd(&sh_count[cls], 1) : 0;
+        __syncthreads();
+        if (t == 0) {
+            int acc = 0;
+            for (int k = 0; k < 5; ++k) {
+                sh_base[k] = acc;
+                acc += sh_count[k];
+            }
+        }
+        __syncthreads();
+        if (cls >= 0 && cls < 4) {
+            const int slot = sh_base[cls] + rank;
+            sh_item[slot] = (uint16_t)t;
+            sh_rng[slot] = make_ulonglong2(rng.state, rng.inc);
+        }
+        __syncthreads();
+        if (t < sh_base[4])
+            scatter_item(s, scat, base + sh_item[t], Pcg{sh_rng[t].x, sh_rng[t].y}, next, shadow, ps,
+                         nee, rr, err);
+        __syncthreads();
     }
 }
 

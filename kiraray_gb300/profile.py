@@ -1,0 +1,84 @@
+"""Fixed workloads for profiling the pass under a profiler (ncu launch lists
+and single-kernel captures); prints the device time of each repetition.
+
+    python -m kiraray_gb300.profile trace [--reps 4]
+        closest hits of the 1920x1080 camera rays of the 10.9M-triangle scene
+    python -m kiraray_gb300.profile frame [--res 480x270] [--views 8] [--nrc] [--frames 3]
+        frames of the wavefront pass on the same scene (max depth 8), the
+        camera replicated into `views` batched views, optionally with the
+        neural radiance cache attached and training
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+import torch
+
+
+def _timed(fn) -> float:
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    fn()
+    e1.record(s)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def trace(reps: int) -> dict:
+    from . import scenes
+    from .accel import Accel
+
+    sc = scenes.large_scene()
+    acc = Accel(sc.world_triangles())
+    rays = torch.from_numpy(scenes.pinhole_rays(sc)).cuda()
+    ms = [_timed(lambda: acc.trace_closest(rays)) for _ in range(reps)]
+    return {"workload": "trace", "rays": int(rays.shape[0]), "ms": ms}
+
+
+def frame(res: str, views: int, nrc: bool, frames: int) -> dict:
+    from . import scenes
+    from .convergence import replica_views
+    from .nrc import NeuralRadianceCache
+    from .wavefront import WavefrontPathTracer
+
+    w, h = (int(x) for x in res.split("x"))
+    sc = scenes.large_scene(width=w, height=h, seed=3)
+    pt = WavefrontPathTracer({"max_depth": sc.max_depth}, seed=3)
+    pt.set_scene(sc)
+    if nrc:
+        tris = sc.world_triangles().reshape(-1, 3)
+        cache = NeuralRadianceCache(tris.min(0), tris.max(0), seed=3)
+        pt.set_nrc(cache, train=True)
+    pt.resize_views(replica_views(sc, views))
+    out = torch.empty((pt.n_pixels, 4), device="cuda")
+
+    def one(f):
+        pt.begin_frame_views(f)
+        pt.render_flat(out)
+
+    ms = [_timed(lambda: one(f)) for f in range(1, frames + 1)]
+    return {"workload": "frame", "res": res, "views": views, "nrc": nrc, "ms": ms,
+            "device_errors": pt.device_errors()}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    t = sub.add_parser("trace")
+    t.add_argument("--reps", type=int, default=4)
+    f = sub.add_parser("frame")
+    f.add_argument("--res", default="480x270")
+    f.add_argument("--views", type=int, default=8)
+    f.add_argument("--nrc", action="store_true")
+    f.add_argument("--frames", type=int, default=3)
+    a = ap.parse_args()
+    from .build import build
+    build()
+    r = trace(a.reps) if a.cmd == "trace" else frame(a.res, a.views, a.nrc, a.frames)
+    print(json.dumps(r))
+
+
+if __name__ == "__main__":
+    main()

@@ -3,33 +3,7 @@ from __future__ import annotations
 
 import numpy as np
 
-
-def pinhole_rays(scene, width=None, height=None, jitter_seed=None) -> np.ndarray:
-    """Camera rays of the scene's pinhole camera through pixel centres (or
-    jittered), float32 [H*W, 8]."""
-    cam = scene.camera
-    w = width or scene.width
-    h = height or scene.height
-    ys, xs = np.meshgrid(np.arange(h), np.arange(w), indexing="ij")
-    px = xs.reshape(-1).astype(np.float64) + 0.5
-    py = ys.reshape(-1).astype(np.float64) + 0.5
-    if jitter_seed is not None:
-        rng = np.random.default_rng(jitter_seed)
-        px += rng.random(px.shape) - 0.5
-        py += rng.random(py.shape) - 0.5
-    ndcx = 2 * px / w - 1
-    ndcy = 1 - 2 * py / h
-    tanf = (cam.film_size[1] * 0.5) / cam.focal_length
-    d = np.stack([tanf * cam.aspect_ratio * ndcx, tanf * ndcy, -np.ones_like(ndcx)], -1)
-    d /= np.linalg.norm(d, axis=-1, keepdims=True)
-    R = np.asarray(cam.rotation, np.float64)
-    d = d @ R.T
-    out = np.zeros((d.shape[0], 8), np.float32)
-    out[:, :3] = cam.position
-    out[:, 3] = 0.0
-    out[:, 4:7] = d
-    out[:, 7] = np.inf
-    return out
+from kiraray_gb300.scenes import pinhole_rays  # noqa: F401  (camera ray sets)
 
 
 def bounce_rays(tris: np.ndarray, rays: np.ndarray, hits: np.ndarray, seed: int) -> np.ndarray:
