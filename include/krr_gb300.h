@@ -261,6 +261,15 @@ int krr_wf_begin_frame(krr_wf *wf, int64_t frame_index, const krr_camera_desc *c
  * row-major, row 0 at the top (the reference's y-flipped surface write). */
 int krr_wf_render(krr_wf *wf, float *d_out_rgba, void *stream);
 
+/* The same frame as krr_wf_render computed by one persistent kernel, one
+ * thread per pixel path (no queues): equal to krr_wf_render bit for bit, for
+ * an A/B of queue traffic against register pressure.  Counterpart of the
+ * reference's MegakernelPathTracer pass (src/render/megakernel/device.cu:
+ * 148-195) in structure, with the wavefront pass's sampling.  Surfaces only:
+ * returns KRR_ERR_INVALID_ARGUMENT for scenes with media or with a cache
+ * attached. */
+int krr_wf_render_megakernel(krr_wf *wf, float *d_out_rgba, void *stream);
+
 /* Batched views: many cameras of different sizes in one wavefront (one
  * launch per stage per bounce).  krr_wf_resize_views replaces resize; each
  * frame krr_wf_begin_frame_views gives the cameras (sizes must match) and

@@ -1101,6 +1101,169 @@ __global__ void k_resolve(PixelState ps, float4 *out, const DevView *__restrict_
     }
 }
 
+// ---------------------------------------------------------------- megakernel
+// The stage loop of integrator.cpp:223-266 run as one kernel, one thread per
+// pixel: each bounce's closest hit, emission or environment, NEE shadow ray
+// and BSDF sample are taken in registers in the stages' order, with the same
+// device functions, so a pixel's radiance equals the wavefront pass's bit for
+// bit.  It is the queue-free side of an A/B against the wavefront (the
+// reference's MegakernelPathTracer, src/render/megakernel/device.cu:148-195,
+// has the same structure but its own sampling and MIS).  Surfaces only: no
+// media and no cache hooks.
+template <int FMT>
+__global__ void __launch_bounds__(128)
+k_megakernel(DevScene s, const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
+             const DevView *__restrict__ views, const FrameConst *__restrict__ fc, PixelState ps,
+             WfConst c, int independent, int64_t n, float4 *__restrict__ out, uint32_t *err,
+             int *trace_err) {
+    const int nv = fc->n_views;
+    const float lsel_pdf = 1.f / (float)s.n_lights;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        const DevView &v = views[view_of(views, nv, g)];
+        const DevCamera &cam = v.cam;
+        const int64_t i = g - v.offset;
+        const uint32_t pixel = (uint32_t)g;
+        Pcg rng = load_rng(ps, pixel);
+        const float4 l0 = ps.L[g], p0 = ps.pixel[g];
+        V3 L = f3(l0), acc = f3(p0);
+        for (int sample = 0; sample < c.spp; ++sample) {
+            // generateCameraRays
+            float fx = rng.get1d(), fy = rng.get1d();
+            float lx = rng.get1d(), ly = rng.get1d();
+            float tm = rng.get1d();
+            (void)lx; (void)ly;
+            float px = (float)(i % v.w) + 0.5f + fx;
+            float py = (float)(i / v.w) + 0.5f + fy;
+            float ndcx = (2 * px) / (float)v.w + (-1.f);
+            float ndcy = (2 * py) / (float)v.h + (-1.f);
+            V3 fd = normalize(V3{cam.tan_fov * cam.aspect * ndcx, cam.tan_fov * ndcy, -1.f});
+            V3 ro = V3{cam.pos[0], cam.pos[1], cam.pos[2]};
+            V3 rd = mat3_mul(cam.rot, fd);
+            const float time = cam.shutter_open + cam.shutter_time * tm;
+            V3 ctx_p = v3(0.f), ctx_n = v3(0.f), thp = v3(1.f), pu = v3(1.f), pl = v3(1.f);
+            uint32_t flags = 0u, depth = 0u;
+            int32_t medium = cam.medium;
+            for (int iter = 0;; ++iter) {
+                const float4 h = traverse_ray<false, FMT>(nodes, tris, ro, rd, 0.f, INFINITY, trace_err);
+                const uint32_t gid = ubits(h.w);
+                bool next = false, scatter = false;
+                Surf sf;
+                if (gid == KRR_MISS) {
+                    // handleMiss
+                    if (s.n_infinite > 0) {
+                        V3 Lm = v3(0.f);
+                        for (int k = 0; k < s.n_infinite; ++k) {
+                            const DevInfinite &e = s.infinite[k];
+                            if (c.nee && depth && !(flags & BSDF_DELTA)) {
+                                float light_pdf = kInv4Pi * lsel_pdf;
+                                Lm += env_Li(e, rd) / mean(pu + pl * light_pdf);
+                            } else {
+                                Lm += env_Li(e, rd) / mean(pu);
+                            }
+                        }
+                        V3 add = thp * Lm;
+                        L = add + L;
+                    }
+                } else {
+                    sf = prepare_surface(s, h.y, h.z, gid, rd);
+                    if (sf.material < 0) {
+                        // null material: the same ray continues from the interface
+                        ro = offset_ray_origin(sf.p, sf.n, rd);
+                        medium = medium_towards(sf.interface_in, sf.interface_out, medium, sf.n, rd);
+                        next = true;
+                    } else {
+                        if (sf.light >= 0) {
+                            // handleHit
+                            const DevLight &l = s.lights[sf.light];
+                            const DevInstance &I = s.instances[l.index];
+                            V3 Le = area_L(I, sf.n, sf.wo) * thp;
+                            if (c.nee && depth && !(flags & BSDF_DELTA)) {
+                                float light_pdf = area_pdf(s, l, sf.p, sf.n, ctx_p) * lsel_pdf;
+                                Le = Le / mean(pl * light_pdf + pu);
+                            } else {
+                                Le = Le / mean(pu);
+                            }
+                            L = Le + L;
+                        }
+                        scatter = any(thp);
+                    }
+                }
+                if (iter == c.max_depth) break;
+                if (scatter) {
+                    // generateScatterRays
+                    if (rng.get1d() >= c.rr) break;
+                    V3 sthp = thp / c.rr;
+                    const DevMesh &M = s.meshes[sf.mesh];
+                    bool transition = M.medium_inside != M.medium_outside;
+                    int32_t mi = transition ? M.medium_inside : -2, mo = transition ? M.medium_outside : -2;
+                    const V3 tg = sf.t, bt = sf.b, nrm = sf.n, p = sf.p;
+                    auto to_local = [&](V3 w) { return V3{dot(tg, w), dot(bt, w), dot(nrm, w)}; };
+                    V3 wo_local = to_local(sf.wo);
+                    ShadingData sd = shading_data(s, sf.material);
+                    uint32_t bsdf_type = bsdf_type_of(sd);
+                    Bsdf bsdf = Bsdf::setup(sd);
+                    if (c.nee && (bsdf_type & BSDF_SMOOTH)) {
+                        float ul = rng.get1d();
+                        uint32_t lid = (uint32_t)(ul * (float)s.n_lights);
+                        float sel_pdf = 1.f / (float)s.n_lights;
+                        float u0 = rng.get1d(), u1 = rng.get1d();
+                        LightSample ls = sample_li(s, s.lights[lid], u0, u1, p);
+                        V3 to = offset_ray_origin(ls.p, ls.n, p - ls.p);
+                        V3 po = offset_ray_origin(p, nrm, to - p);
+                        V3 d = to - po;
+                        V3 wi_world = normalize(d);
+                        V3 wi_local = to_local(wi_world);
+                        float light_pdf = sel_pdf * ls.pdf;
+                        V3 fv = bsdf.f(wo_local, wi_local);
+                        float bsdf_pdf = bsdf.pdf(wo_local, wi_local);
+                        if (light_pdf > 0 && any(fv)) {
+                            V3 Ld = ls.L * sthp * fv * fabsf(wi_local.z);
+                            if (any(Ld)) {
+                                // traceShadow + resolve
+                                float4 sh = traverse_ray<true, FMT>(nodes, tris, po, d, 0.f, 1.f, trace_err);
+                                if (ubits(sh.w) == KRR_MISS) {
+                                    V3 add = Ld / mean(pu * light_pdf + pu * bsdf_pdf);
+                                    L = add + L;
+                                }
+                            }
+                        }
+                    }
+                    BsdfSample bs = bsdf.sample(wo_local, [&]() { return rng.get1d(); });
+                    if (bs.pdf != 0 && any(bs.f)) {
+                        V3 wi_world = tg * bs.wi.x + bt * bs.wi.y + nrm * bs.wi.z;
+                        V3 nthp = sthp * bs.f * fabsf(bs.wi.z) / bs.pdf;
+                        if (any(nthp)) {
+                            ro = offset_ray_origin(p, nrm, wi_world);
+                            medium = medium_towards(mi, mo, medium, nrm, wi_world);
+                            rd = wi_world;
+                            ctx_p = p;
+                            ctx_n = nrm;
+                            flags = bs.flags;
+                            thp = nthp;
+                            depth = depth + 1;
+                            pl = pu / bs.pdf;
+                            next = true;
+                        }
+                    }
+                }
+                if (!next) break;
+            }
+            (void)ctx_n;
+            (void)time;
+            acc = V3{acc.x + L.x, acc.y + L.y, acc.z + L.z};
+            if (independent && sample + 1 < c.spp) L = v3(0.f);
+        }
+        store_rng(ps, pixel, rng);
+        ps.L[g] = make_float4(L.x, L.y, L.z, l0.w);
+        ps.pixel[g] = make_float4(acc.x, acc.y, acc.z, 0.f);
+        V3 col = acc / (float)c.spp;
+        if (c.enable_clamp) col = vmin(vmax(col, v3(0.f)), v3(c.clamp_max));
+        const int64_t x = i % v.w, y = i / v.w;
+        out[v.offset + (v.h - 1 - y) * (int64_t)v.w + x] = f4(col, 1.f);
+    }
+}
+
 // Instance flattening: world-space vertices in instance-major triangle order,
 // each row m0*x + m1*y + m2*z + m3 rounded operation by operation.
 __global__ void k_flatten(const DevScene s, int n_inst, float *out, int64_t n_tris) {
@@ -1299,10 +1462,8 @@ extern "C" int krr_wf_destroy(krr_wf *wf) {
 extern "C" int krr_wf_set_params(krr_wf *wf, const krr_wf_params *params) {
     KRR_CHECK_ARG(wf && params, "NULL argument");
     KRR_CHECK_ARG(params->max_depth >= 0 && params->spp >= 1, "bad parameters");
-    bool was_medium = wf->params.enable_medium;
     wf->params = *params;
     wf->medium = wf->params.enable_medium && wf->scene.n_media > 0;
-    (void)was_medium;
     return KRR_OK;
 }
 
@@ -1819,6 +1980,38 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
     k_resolve<<<wf->grid, kThreads, 0, st>>>(wf->ps, reinterpret_cast<float4 *>(d_out), wf->d_views,
                                               wf->d_frame, wf->n, (float)wf->params.spp,
                                               wf->params.enable_clamp, wf->params.clamp_max);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_render_megakernel(krr_wf *wf, float *d_out, void *stream) {
+    KRR_TRY(ready(wf));
+    KRR_CHECK_ARG(d_out != nullptr, "output is NULL");
+    KRR_CHECK_ARG(!wf->medium, "the megakernel pass traces surfaces only; the scene has media");
+    KRR_CHECK_ARG(!wf->nrc, "the megakernel pass has no cache hooks; detach the cache first");
+    cudaStream_t st = as_stream(stream);
+    static int grid[2] = {0, 0};
+    const int fmt = wf->accel.node_format;
+    if (!grid[fmt]) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (fmt == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_megakernel<1>, 128, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_megakernel<0>, 128, 0);
+        grid[fmt] = std::max(1, sms) * std::max(1, per_sm);
+    }
+    const int blocks = (int)std::min<int64_t>(grid[fmt], (wf->n + 127) / 128);
+    WfConst c = wf->consts();
+    if (fmt == 1)
+        k_megakernel<1><<<blocks, 128, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, wf->d_views,
+                                                 wf->d_frame, wf->ps, c, wf->params.independent_samples,
+                                                 wf->n, reinterpret_cast<float4 *>(d_out), wf->err(),
+                                                 wf->accel.d_scratch + 4);
+    else
+        k_megakernel<0><<<blocks, 128, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, wf->d_views,
+                                                 wf->d_frame, wf->ps, c, wf->params.independent_samples,
+                                                 wf->n, reinterpret_cast<float4 *>(d_out), wf->err(),
+                                                 wf->accel.d_scratch + 4);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }

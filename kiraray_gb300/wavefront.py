@@ -132,6 +132,14 @@ class WavefrontPathTracer:
         check(self.lib.krr_wf_render(self._h, out.data_ptr(), _stream()), "krr_wf_render")
         return out
 
+    def render_megakernel(self, out: torch.Tensor | None = None) -> torch.Tensor:
+        """The same frame as render() from one persistent kernel (surfaces only)."""
+        if out is None:
+            out = torch.empty((self.height, self.width, 4), dtype=torch.float32, device="cuda")
+        check(self.lib.krr_wf_render_megakernel(self._h, out.data_ptr(), _stream()),
+              "krr_wf_render_megakernel")
+        return out
+
     # stage methods (integrator.cpp:50-179)
     def generate_camera_rays(self):
         check(self.lib.krr_wf_generate_camera_rays(self._h, _stream()), "generate_camera_rays")

@@ -182,3 +182,49 @@ def test_resize_and_rescene(krr_lib, cuda):
     pt.set_scene(scenes.cornell_box(17, 23))
     pt.begin_frame(2, sc.camera)
     assert torch.isfinite(pt.render()).all()
+
+
+@pytest.mark.parametrize("params,spp", [({"max_depth": 5}, 1), ({"max_depth": 3, "nee": False}, 1),
+                                        ({"max_depth": 4, "enable_clamp": True, "clamp_max": 1.5}, 2),
+                                        ({"max_depth": 4, "independent_samples": 1}, 3)])
+def test_megakernel_equals_wavefront_cornell(krr_lib, cuda, params, spp):
+    sc = scenes.cornell_box(64, 48, max_depth=params["max_depth"])
+    pt = WavefrontPathTracer(params, spp=spp, seed=9)
+    pt.set_scene(sc)
+    pt.resize(64, 48)
+    pt.begin_frame(4, sc.camera)
+    a = pt.render().cpu().numpy()
+    La = pt.radiance().cpu().numpy()
+    pt.begin_frame(4, sc.camera)
+    b = pt.render_megakernel().cpu().numpy()
+    Lb = pt.radiance().cpu().numpy()
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert np.array_equal(La.view(np.uint32), Lb.view(np.uint32))
+    assert pt.device_errors() == 0
+
+
+def test_megakernel_equals_wavefront_large_scene_views(krr_lib, cuda):
+    """Conductors, dielectrics, the environment and two batched views."""
+    sc = scenes.large_scene(width=96, height=64, grid=256, n_spheres=40, sky_size=(64, 32))
+    views = [(sc.camera, 96, 64, 3), (sc.camera, 40, 30, 1 << 24)]
+    pt = WavefrontPathTracer({"max_depth": 8})
+    pt.set_scene(sc)
+    pt.resize_views(views)
+    pt.begin_frame_views(2)
+    a = pt.render_flat().cpu().numpy()
+    out = torch.empty((pt.n_pixels, 4), device="cuda")
+    pt.begin_frame_views(2)
+    pt.render_megakernel(out)
+    b = out.cpu().numpy()
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_megakernel_rejects_media(krr_lib, cuda):
+    from kiraray_gb300._lib import KrrError
+    sc = scenes.volume_box(16, 16)
+    pt = WavefrontPathTracer({"max_depth": 3})
+    pt.set_scene(sc)
+    pt.resize(16, 16)
+    pt.begin_frame(1, sc.camera)
+    with pytest.raises(KrrError):
+        pt.render_megakernel()
