@@ -252,6 +252,13 @@ int krr_wf_set_params(krr_wf *wf, const krr_wf_params *params);
 /* RenderPass::setScene (integrator.cpp:186-203): uploads the scene and
  * builds the BVH. */
 int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *scene, void *stream);
+/* Scene::update for animated instances (src/core/scene.cpp:17-31,
+ * src/core/device/optix.cpp:618-642): instance h_indices[k] gets the
+ * row-major 3x4 transform h_transforms[12k..12k+11]; the world-space
+ * triangles and the BVH are rebuilt (about 8 ms for 10.9M triangles).
+ * Drops a captured frame graph (capture again). */
+int krr_wf_update_instances(krr_wf *wf, int32_t n, const int32_t *h_indices,
+                            const float *h_transforms, void *stream);
 /* RenderPass::resize (integrator.cpp:181-184): reallocates queues. */
 int krr_wf_resize(krr_wf *wf, int32_t width, int32_t height);
 /* RenderPass::beginFrame (integrator.cpp:205-221). frame_index is 1-based. */
@@ -406,6 +413,12 @@ int krr_accumulate_f64(const float *d_rgba, double *d_accum, int64_t n_pixels, v
  * 64-128), reduced in FP64.  Synchronises the stream. */
 int krr_image_error(const double *d_accum, double scale, const float *d_ref_rgba,
                     int64_t n_pixels, int32_t metric, double *h_out, void *stream);
+/* ToneMappingPass (src/render/passes/tonemapping/tonemapping.cu:60-88): per
+ * pixel color * exposure, then operator op (0 linear, 1 reinhard, 2 aces,
+ * 3 uncharted2, 4 hejihable; the pass's JSON "operator"), then pow(1/2.2)
+ * when gamma is set; alpha 1.  In place when d_out == d_in. */
+int krr_tonemap(const float *d_in_rgba, float *d_out_rgba, int64_t n_pixels, int32_t op,
+                float exposure, int32_t gamma, void *stream);
 
 #ifdef __cplusplus
 }

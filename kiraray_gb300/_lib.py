@@ -109,6 +109,8 @@ SIGNATURES = {
     "krr_version": (_I, []),
     "krr_accel_create_from_triangles": (_I, [_P, C.c_int64, C.POINTER(_P), _P]),
     "krr_set_bvh_node_format": (_I, [C.c_int32]),
+    "krr_wf_update_instances": (_I, [_P, C.c_int32, _P, _P, _P]),
+    "krr_tonemap": (_I, [_P, _P, C.c_int64, C.c_int32, C.c_float, C.c_int32, _P]),
     "krr_wf_render_megakernel": (_I, [_P, _P, _P]),
     "krr_wf_queue_view": (_I, [_P, C.c_int32, C.POINTER(_P), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "krr_accel_stats_get": (_I, [_P, C.POINTER(AccelStats)]),

@@ -1,8 +1,9 @@
-"""Convergence measurement: FP64 accumulation and relMSE against a reference
-image, in the manner of the reference's AccumulatePass ("double" precision,
-src/render/passes/accumulate/accumulate.cu:30-79) and ErrorMeasurePass
-(src/render/passes/errormeasure/errormeasure.cpp:17-57, metrics.cu:64-128),
-which logs a curve {timesteps, timepoints, data}.
+"""Image passes after the path tracer: FP64 accumulation and relMSE against a
+reference image, in the manner of the reference's AccumulatePass ("double"
+precision, src/render/passes/accumulate/accumulate.cu:30-79) and
+ErrorMeasurePass (src/render/passes/errormeasure/errormeasure.cpp:17-57,
+metrics.cu:64-128), which logs a curve {timesteps, timepoints, data}; and
+the ToneMappingPass (src/render/passes/tonemapping/tonemapping.cu:60-88).
 """
 from __future__ import annotations
 
@@ -46,6 +47,23 @@ class Accumulator:
                                           ref_rgba.data_ptr(), self.n, metric, C.byref(v),
                                           _stream()), "krr_image_error")
         return v.value
+
+
+TONEMAP_OPERATORS = ("linear", "reinhard", "aces", "uncharted2", "hejihable")
+
+
+def tonemap(rgba: torch.Tensor, operator: str = "linear", exposure: float = 1.0, gamma: bool = True,
+            out: torch.Tensor | None = None) -> torch.Tensor:
+    """The reference's ToneMappingPass with its JSON parameters ("operator",
+    "exposure", "gamma"; tonemapping.h:40-51) on a float4 RGBA image."""
+    if not (rgba.is_cuda and rgba.dtype == torch.float32 and rgba.shape[-1] == 4):
+        raise ValueError("rgba must be a CUDA float32 tensor with 4 channels last")
+    rgba = rgba.contiguous()
+    out = torch.empty_like(rgba) if out is None else out
+    check(_lib.load().krr_tonemap(rgba.data_ptr(), out.data_ptr(), rgba.numel() // 4,
+                                  TONEMAP_OPERATORS.index(operator), float(exposure), int(bool(gamma)),
+                                  _stream()), "krr_tonemap")
+    return out
 
 
 def replica_views(scene, copies: int, seed_base: int = 0) -> list:

@@ -1,4 +1,4 @@
-// Image accumulation in FP64 and error metrics on the GPU.
+// Image passes on the GPU: accumulation in FP64, error metrics, tone mapping.
 //
 // The reference accumulates frames in its AccumulatePass with a "double"
 // precision mode (src/render/passes/accumulate/accumulate.cu:30-79) and
@@ -69,6 +69,53 @@ __global__ void k_sum_partials(const double *partial, int n, double *out) {
     if (threadIdx.x == 0) *out = sh[0];
 }
 
+// ToneMappingPass::render (src/render/passes/tonemapping/tonemapping.cu:
+// 60-88): exposure scale, operator, optional gamma 1/2.2, alpha 1.
+__device__ __forceinline__ float tm_lum(float r, float g, float b) {
+    return r * 0.299f + g * 0.587f + b * 0.114f;   // luminance(), spectrum.h:545-547
+}
+
+__device__ __forceinline__ float tm_aces(float c) {   // toneMapAces, tonemapping.cu:11-20
+    c *= 0.6f;
+    const float a = 2.51f, b = 0.03f, cc = 2.43f, d = 0.59f, e = 0.14f;
+    float v = (c * (a * c + b)) / (c * (cc * c + d) + e);
+    return fminf(fmaxf(v, 0.f), 1.f);
+}
+
+__device__ __forceinline__ float tm_uc2(float c) {    // toneMapUC2, tonemapping.cu:28-37
+    const float A = 0.22f, B = 0.3f, C = 0.1f, D = 0.2f, E = 0.01f, F = 0.3f;
+    return ((c * (A * c + C * B) + D * E) / (c * (A * c + B) + D * F)) - (E / F);
+}
+
+__device__ __forceinline__ float tm_heji(float c) {   // toneMapHejiHableAlu, tonemapping.cu:39-44
+    c = fmaxf(c - 0.004f, 0.f);
+    c = (c * (6.2f * c + 0.5f)) / (c * (6.2f * c + 1.7f) + 0.06f);
+    return powf(c, 2.2f);
+}
+
+__global__ void k_tonemap(const float4 *__restrict__ in, float4 *__restrict__ out, int64_t n, int op,
+                          float exposure, int gamma) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float4 p = in[i];
+        float c[3] = {p.x * exposure, p.y * exposure, p.z * exposure};
+        if (op == 1) {   // Reinhard on luminance
+            float lum = tm_lum(c[0], c[1], c[2]);
+            float r = lum / (lum + 1.f);
+            for (int k = 0; k < 3; ++k) c[k] = lum == 0.f ? 0.f : (c[k] * r) / lum;
+        } else if (op == 2) {
+            for (int k = 0; k < 3; ++k) c[k] = tm_aces(c[k]);
+        } else if (op == 3) {
+            for (int k = 0; k < 3; ++k) c[k] = tm_uc2(c[k]);
+        } else if (op == 4) {
+            for (int k = 0; k < 3; ++k) c[k] = tm_heji(c[k]);
+        }
+        if (gamma)
+            for (int k = 0; k < 3; ++k) c[k] = powf(c[k], 0.45454545f);
+        out[i] = make_float4(c[0], c[1], c[2], 1.f);
+    }
+}
+
 int grid_for(int64_t n) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -87,6 +134,18 @@ extern "C" int krr_accumulate_f64(const float *d_rgba, double *d_accum, int64_t 
     if (n_pixels == 0) return KRR_OK;
     k_accumulate_f64<<<grid_for(n_pixels), kThreads, 0, as_stream(stream)>>>(
         reinterpret_cast<const float4 *>(d_rgba), d_accum, n_pixels);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+extern "C" int krr_tonemap(const float *d_in_rgba, float *d_out_rgba, int64_t n_pixels, int32_t op,
+                           float exposure, int32_t gamma, void *stream) {
+    KRR_CHECK_ARG(d_in_rgba && d_out_rgba && n_pixels >= 0, "bad argument");
+    KRR_CHECK_ARG(op >= 0 && op <= 4, "operator must be 0 linear, 1 reinhard, 2 aces, 3 uncharted2, 4 hejihable");
+    if (n_pixels == 0) return KRR_OK;
+    k_tonemap<<<grid_for(n_pixels), kThreads, 0, as_stream(stream)>>>(
+        reinterpret_cast<const float4 *>(d_in_rgba), reinterpret_cast<float4 *>(d_out_rgba), n_pixels, op,
+        exposure, gamma);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }

@@ -80,6 +80,10 @@ struct krr_wf {
     float scene_radius = 1.f;
     krr_accel accel{};
     std::vector<void *> scene_allocs;
+    std::vector<DevInstance> h_instances;     // host copies for instance updates
+    std::vector<DevInfinite> h_infinite;
+    int32_t n_instances = 0;
+    uint64_t n_tris = 0;
     // queues and pixel state
     float4 *qbuf[Q_COUNT] = {};
     int32_t *d_counts = nullptr;   // [0..7] queue sizes, [8] error flags
@@ -1467,6 +1471,41 @@ extern "C" int krr_wf_set_params(krr_wf *wf, const krr_wf_params *params) {
     return KRR_OK;
 }
 
+// Flattens the instances to world space and builds the BVH over them, with
+// the null-material any-hit mask; sets the scene radius (the length of the
+// bounding-box diagonal, src/core/device/scene.cpp:108).
+static int rebuild_bvh(krr_wf *wf, cudaStream_t st) {
+    const uint64_t n_tris = wf->n_tris;
+    DevScene &s = wf->scene;
+    float *d_world = nullptr;
+    KRR_CUDA(cudaMalloc(&d_world, std::max<uint64_t>(n_tris, 1) * 9 * sizeof(float)));
+    if (n_tris) k_flatten<<<grid_for(n_tris), kThreads, 0, st>>>(s, wf->n_instances, d_world, n_tris);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        cudaFree(d_world);
+        return cuda_status(e, "k_flatten", __FILE__, __LINE__);
+    }
+    int stat = accel_build(&wf->accel, d_world, (int64_t)n_tris, st);
+    cudaFree(d_world);
+    if (stat != KRR_OK) return stat;
+    // null-material triangles never block shadow rays (device.cu:83-88)
+    if (n_tris) {
+        uint8_t *mask = nullptr;
+        KRR_CUDA(cudaMalloc(&mask, n_tris));
+        k_null_mask<<<grid_for(n_tris), kThreads, 0, st>>>(s, (int64_t)n_tris, mask);
+        stat = cuda_status(cudaGetLastError(), "k_null_mask", __FILE__, __LINE__);
+        if (stat == KRR_OK) stat = accel_set_mask(&wf->accel, mask, st);
+        if (stat == KRR_OK) stat = cuda_status(cudaStreamSynchronize(st), "mask", __FILE__, __LINE__);
+        cudaFree(mask);
+        if (stat != KRR_OK) return stat;
+    }
+    float dx = wf->accel.scene_hi[0] - wf->accel.scene_lo[0];
+    float dy = wf->accel.scene_hi[1] - wf->accel.scene_lo[1];
+    float dz = wf->accel.scene_hi[2] - wf->accel.scene_lo[2];
+    wf->scene_radius = std::sqrt(dx * dx + dy * dy + dz * dz);
+    return KRR_OK;
+}
+
 extern "C" int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *sd, void *stream) {
     KRR_CHECK_ARG(wf && sd, "NULL argument");
     KRR_CHECK_ARG(sd->n_meshes >= 0 && sd->n_instances >= 0 && sd->n_materials >= 0,
@@ -1590,31 +1629,15 @@ extern "C" int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *sd, void *stre
     s.tri_instance = tri_inst;
 
     // world-space triangles and the BVH
-    float *d_world = nullptr;
-    KRR_CUDA(cudaMalloc(&d_world, std::max<uint64_t>(n_tris, 1) * 9 * sizeof(float)));
-    if (n_tris) k_flatten<<<grid_for(n_tris), kThreads, 0, st>>>(s, sd->n_instances, d_world, n_tris);
-    KRR_CUDA(cudaGetLastError());
-    int stat = accel_build(&wf->accel, d_world, (int64_t)n_tris, st);
-    cudaFree(d_world);
-    if (stat != KRR_OK) return stat;
-    // null-material triangles never block shadow rays (device.cu:83-88)
-    if (n_tris) {
-        uint8_t *mask = nullptr;
-        KRR_CUDA(cudaMalloc(&mask, n_tris));
-        k_null_mask<<<grid_for(n_tris), kThreads, 0, st>>>(s, (int64_t)n_tris, mask);
-        KRR_CUDA(cudaGetLastError());
-        KRR_TRY(accel_set_mask(&wf->accel, mask, st));
-        KRR_CUDA(cudaStreamSynchronize(st));
-        cudaFree(mask);
-    }
-    // scene radius = length of the bounding-box diagonal (scene.cpp:108)
-    float dx = wf->accel.scene_hi[0] - wf->accel.scene_lo[0];
-    float dy = wf->accel.scene_hi[1] - wf->accel.scene_lo[1];
-    float dz = wf->accel.scene_hi[2] - wf->accel.scene_lo[2];
-    wf->scene_radius = std::sqrt(dx * dx + dy * dy + dz * dz);
+    wf->n_instances = sd->n_instances;
+    wf->n_tris = n_tris;
+    wf->h_instances = insts;
+    wf->scene = s;   // rebuild_bvh reads the uploaded instances
+    KRR_TRY(rebuild_bvh(wf, st));
     for (auto &d : infs) d.scene_radius = wf->scene_radius;
     KRR_TRY(dev_upload(wf, const_cast<DevInfinite **>(&s.infinite), infs.data(), infs.size()));
     s.n_infinite = (int32_t)infs.size();
+    wf->h_infinite = infs;
 
     // media
     std::vector<DevMedium> media(sd->n_media);
@@ -1688,6 +1711,41 @@ static int set_layout(krr_wf *wf, std::vector<DevView> layout) {
     KRR_CUDA(cudaMalloc(&wf->ps.rng, wf->n * sizeof(ulonglong2)));
     wf->grid = grid_for(wf->n);
     return alloc_nrc_buffers(wf);
+}
+
+// Scene::update for animated instances (src/core/scene.cpp:17-31,
+// OptixSceneSingleLevel::updateAccelStructure, src/core/device/optix.cpp:
+// 618-642): new 3x4 transforms for some instances, then the world-space
+// triangles and the BVH are rebuilt (the reference rebuilds its instance
+// level; here instances are flattened into one BVH).  A captured frame graph
+// refers to the old BVH and is dropped.
+extern "C" int krr_wf_update_instances(krr_wf *wf, int32_t n, const int32_t *h_indices,
+                                       const float *h_transforms, void *stream) {
+    KRR_CHECK_ARG(wf && wf->has_scene, "no scene");
+    KRR_CHECK_ARG(n >= 0 && (n == 0 || (h_indices && h_transforms)), "bad argument");
+    for (int k = 0; k < n; ++k)
+        KRR_CHECK_ARG(h_indices[k] >= 0 && h_indices[k] < wf->n_instances, "instance index out of range");
+    if (n == 0) return KRR_OK;
+    cudaStream_t st = as_stream(stream);
+    for (int k = 0; k < n; ++k) {
+        DevInstance &d = wf->h_instances[h_indices[k]];
+        std::memcpy(d.xf, h_transforms + 12 * k, sizeof(d.xf));
+        inverse_transpose(h_transforms + 12 * k, d.nxf);
+    }
+    KRR_CUDA(cudaStreamSynchronize(st));
+    KRR_CUDA(cudaMemcpy(const_cast<DevInstance *>(wf->scene.instances), wf->h_instances.data(),
+                        wf->h_instances.size() * sizeof(DevInstance), cudaMemcpyHostToDevice));
+    if (wf->graph) {
+        cudaGraphExecDestroy(wf->graph);
+        wf->graph = nullptr;
+    }
+    KRR_TRY(rebuild_bvh(wf, st));
+    if (!wf->h_infinite.empty()) {
+        for (auto &d : wf->h_infinite) d.scene_radius = wf->scene_radius;
+        KRR_CUDA(cudaMemcpy(const_cast<DevInfinite *>(wf->scene.infinite), wf->h_infinite.data(),
+                            wf->h_infinite.size() * sizeof(DevInfinite), cudaMemcpyHostToDevice));
+    }
+    return KRR_OK;
 }
 
 extern "C" int krr_wf_resize(krr_wf *wf, int32_t width, int32_t height) {

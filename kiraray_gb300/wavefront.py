@@ -14,6 +14,7 @@ from __future__ import annotations
 
 import ctypes as C
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -68,6 +69,16 @@ class WavefrontPathTracer:
         check(self.lib.krr_wf_set_scene(self._h, C.byref(desc), _stream()), "krr_wf_set_scene")
         self._keep = (desc, keep)
         self.scene = scene
+
+    def update_instances(self, indices, transforms) -> None:
+        """New 3x4 transforms (float32 [n, 3, 4] or [n, 12]) for the given
+        instances; rebuilds the BVH (Scene::update with animation)."""
+        idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int32))
+        xf = np.ascontiguousarray(np.asarray(transforms, dtype=np.float32).reshape(-1, 12))
+        if xf.shape[0] != idx.shape[0]:
+            raise ValueError("one transform per instance index")
+        check(self.lib.krr_wf_update_instances(self._h, int(idx.shape[0]), idx.ctypes.data,
+                                               xf.ctypes.data, _stream()), "update_instances")
 
     def set_nrc(self, cache, train: bool = True):
         """Attaches a NeuralRadianceCache (None detaches: the plain tracer)."""

@@ -35,3 +35,18 @@ def test_accumulate_and_error(krr_lib, cuda, metric):
     want = _numpy_error(mean, ref[:, :3].astype(np.float64), metric)
     assert abs(got - want) <= 1e-12 * max(1.0, abs(want))
     assert np.allclose(acc.sum.cpu().numpy(), np.sum([f[:, :3].astype(np.float64) for f in frames], 0))
+
+
+@pytest.mark.parametrize("op", range(5))
+@pytest.mark.parametrize("gamma", [False, True])
+def test_tonemap_matches_oracle(krr_lib, cuda, op, gamma):
+    from kiraray_gb300.convergence import TONEMAP_OPERATORS, tonemap
+    from oracle.imagepasses import tonemap as tonemap_ref
+    rng = np.random.default_rng(op)
+    img = np.zeros((37, 53, 4), np.float32)
+    img[..., :3] = rng.exponential(0.8, (37, 53, 3)).astype(np.float32)
+    img[0, :5, :3] = 0.0          # black pixels (Reinhard's 0/0 guard)
+    got = tonemap(torch.from_numpy(img).cuda(), TONEMAP_OPERATORS[op], 1.7, gamma).cpu().numpy()
+    want = tonemap_ref(img, op, 1.7, gamma)
+    assert np.all(got[..., 3] == 1.0)
+    np.testing.assert_allclose(got, want, rtol=2e-6, atol=2e-7)
