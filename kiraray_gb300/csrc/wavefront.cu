@@ -759,38 +759,51 @@ __device__ __forceinline__ void scatter_item(const DevScene &s, const Queue &sca
 }
 
 constexpr int kScatterThreads = 256;
+constexpr int kScatterPerThread = 4;
+constexpr int kScatterTile = kScatterThreads * kScatterPerThread;
 
 // generateScatterRays, integrator.cpp:110-164.  Each block takes a tile of
-// 256 items, draws their Russian roulette, and regroups the survivors by
+// 1024 items, draws their Russian roulette, and regroups the survivors by
 // material type in shared memory before shading, so that a warp runs one
-// BSDF.  Every item is computed exactly as alone (its sampler stream is its
-// pixel's); only the order of the queue pushes changes.
+// BSDF; warps take the sorted tile in 32-item chunks interleaved across the
+// tile (warp w: chunks w, w + 8, ...) so that every warp gets a similar mix of
+// cheap and expensive materials between two block barriers.  Every item is
+// computed exactly as alone (its sampler stream is its pixel's); only the
+// order of the queue pushes changes.
 __global__ void __launch_bounds__(kScatterThreads, 4)
 k_scatter(DevScene s, Queue scat, Queue next, Queue shadow, PixelState ps, int nee, float rr,
           uint32_t *err) {
     __shared__ int sh_count[5];                  // material types 0..3, 4 = ended by RR
     __shared__ int sh_base[5];
-    __shared__ uint16_t sh_item[kScatterThreads];
-    __shared__ ulonglong2 sh_rng[kScatterThreads];
+    __shared__ uint16_t sh_item[kScatterTile];
     const int n = *scat.count;
-    const int t = threadIdx.x;
-    for (int base = blockIdx.x * kScatterThreads; base < n; base += gridDim.x * kScatterThreads) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    // items per thread and tile: up to 4, fewer when the queue is short so
+    // that every block still gets work
+    const int64_t span = (int64_t)gridDim.x * kScatterThreads;
+    const int64_t want = (n + span - 1) / span;
+    const int per = want < 1 ? 1 : (want > kScatterPerThread ? kScatterPerThread : (int)want);
+    const int tile = per * kScatterThreads;
+    for (int base = blockIdx.x * tile; base < n; base += gridDim.x * tile) {
         if (t < 5) sh_count[t] = 0;
         __syncthreads();
-        const int i = base + t;
-        int cls = -1;
-        Pcg rng{0, 0};
-        if (i < n) {
-            uint32_t pixel = ubits(scat.at(2, i).w);
-            rng = load_rng(ps, pixel);
-            if (rng.get1d() >= rr) {
-                store_rng(ps, pixel, rng);
-                cls = 4;
-            } else {
-                cls = min(max(s.materials[sbits(scat.at(0, i).w)].type, 0), 3);
+        int cls[kScatterPerThread], rank[kScatterPerThread];
+#pragma unroll
+        for (int k = 0; k < kScatterPerThread; ++k) {
+            const int i = base + k * kScatterThreads + t;
+            cls[k] = -1;
+            if (k < per && i < n) {
+                const uint32_t pixel = ubits(scat.at(2, i).w);
+                Pcg rng = load_rng(ps, pixel);
+                if (rng.get1d() >= rr) {
+                    store_rng(ps, pixel, rng);   // the path ends here
+                    cls[k] = 4;
+                } else {
+                    cls[k] = min(max(s.materials[sbits(scat.at(0, i).w)].type, 0), 3);
+                }
             }
+            rank[k] = cls[k] >= 0 ? atomicAdd(&sh_count[cls[k]], 1) : 0;
         }
-        const int rank = cls >= 0 ? atomicAdd(&sh_count[cls], 1) : 0;
         __syncthreads();
         if (t == 0) {
             int acc = 0;
@@ -800,15 +813,20 @@ k_scatter(DevScene s, Queue scat, Queue next, Queue shadow, PixelState ps, int n
             }
         }
         __syncthreads();
-        if (cls >= 0 && cls < 4) {
-            const int slot = sh_base[cls] + rank;
-            sh_item[slot] = (uint16_t)t;
-            sh_rng[slot] = make_ulonglong2(rng.state, rng.inc);
-        }
+#pragma unroll
+        for (int k = 0; k < kScatterPerThread; ++k)
+            if (cls[k] >= 0 && cls[k] < 4) sh_item[sh_base[cls[k]] + rank[k]] = (uint16_t)(k * kScatterThreads + t);
         __syncthreads();
-        if (t < sh_base[4])
-            scatter_item(s, scat, base + sh_item[t], Pcg{sh_rng[t].x, sh_rng[t].y}, next, shadow, ps,
-                         nee, rr, err);
+        const int live = sh_base[4];
+        for (int c = warp; c * 32 < live; c += kScatterThreads / 32) {
+            const int slot = c * 32 + lane;
+            if (slot < live) {
+                const int i = base + sh_item[slot];
+                Pcg rng = load_rng(ps, ubits(scat.at(2, i).w));
+                rng.get1d();   // the roulette draw taken above
+                scatter_item(s, scat, i, rng, next, shadow, ps, nee, rr, err);
+            }
+        }
         __syncthreads();
     }
 }
