@@ -43,6 +43,9 @@ def parse():
                          "the faster after autotuning both (outside the timed region)")
     ap.add_argument("--nrc-res", default="480x270",
                     help="resolution of the time-to-relMSE comparison (0 = skip)")
+    ap.add_argument("--views", type=int, default=64,
+                    help="batched-views run: number of views (0 = skip)")
+    ap.add_argument("--view-frames", type=int, default=5)
     ap.add_argument("--frame", type=int, default=1,
                     help="1: also time a 1920x1080 wavefront frame and its stages")
     ap.add_argument("--nrc-copies", type=int, default=8,
@@ -287,6 +290,85 @@ def wavefront_frame(sc, acc, peak, frames: int = 5):
                     "each bounce's shadow rays with the next bounce's rays in one launch"}
 
 
+def batched_views(args):
+    """64 views, sides log-uniform in [256, 1024] (view i seeded 100 + i),
+    even views on the large scene and odd views on the volume box, the
+    neural radiance cache attached to both passes; the two passes run as one
+    CUDA graph with a branch per pass.  Reports device time per frame (all
+    views) and the same frames run pass after pass."""
+    if args.views <= 0:
+        return None
+    import math
+
+    import torch
+    from kiraray_gb300 import scenes
+    from kiraray_gb300.nrc import NeuralRadianceCache
+    from kiraray_gb300.wavefront import FrameGroup, WavefrontPathTracer
+
+    big = scenes.large_scene(width=64, height=64, seed=1)
+    vol = scenes.volume_box(64, 64)
+    views = ([], [])
+    total = 0
+    for i in range(args.views):
+        rng = np.random.default_rng(100 + i)
+        w = int(round(math.exp(rng.uniform(math.log(256), math.log(1024)))))
+        h = int(round(math.exp(rng.uniform(math.log(256), math.log(1024)))))
+        a = math.radians(rng.uniform(-10, 10))
+        if i % 2 == 0:
+            pos = (62.0 * math.sin(a), 22.0, -62.0 * math.cos(a))
+            cam = scenes._camera(pos, (0.0, 2.0, 0.0), 45.0, w, h)
+        else:
+            pos = (0.5 + 1.9 * math.sin(a), 0.5, 0.5 - 1.9 * math.cos(a))
+            cam = scenes._camera(pos, (0.5, 0.5, 0.0), 40.0, w, h)
+        views[i % 2].append((cam, w, h, 100 + i))
+        total += w * h
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        passes, outs = [], []
+        for sc, vs in ((big, views[0]), (vol, views[1])):
+            pt = WavefrontPathTracer({"max_depth": sc.max_depth}, seed=0)
+            pt.set_scene(sc)
+            tris = sc.world_triangles().reshape(-1, 3)
+            pt.set_nrc(NeuralRadianceCache(tris.min(0), tris.max(0), seed=3), train=True)
+            pt.resize_views(vs)
+            out = torch.empty((pt.n_pixels, 4), device="cuda")
+            pt.begin_frame_views(1)
+            pt.render_flat(out)
+            passes.append(pt)
+            outs.append(out)
+        group = FrameGroup(passes, outs)
+        group.capture()
+        for p, o in zip(passes, outs):
+            p.capture_frame(o)
+
+        def timed(fn, frames):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ms = []
+            for f in frames:
+                e0.record(stream)
+                fn(f)
+                e1.record(stream)
+                e1.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            return sorted(ms)[len(ms) // 2]
+
+        for f in range(2, 5):
+            group.launch(f)
+        stream.synchronize()
+        grouped = timed(group.launch, range(5, 5 + args.view_frames))
+
+        def one_after_other(f):
+            for p in passes:
+                p.launch_frame(f)
+        sequential = timed(one_after_other, range(5 + args.view_frames, 5 + 2 * args.view_frames))
+        errors = sum(p.device_errors() for p in passes)
+        group.close()
+    return {"views": args.views, "pixels_per_frame": total, "scenes": ["large_scene", "volume_box"],
+            "nrc": True, "frame_ms_group_graph": round(grouped, 3),
+            "frame_ms_pass_after_pass": round(sequential, 3),
+            "mpaths_per_s": round(total / grouped / 1e3, 1), "device_errors": errors}
+
+
 NRC_TUNED = {"learning_rate": 3e-3, "batch_size": 16384, "termination_spread": 0.05}
 
 
@@ -518,6 +600,7 @@ def run_ours(args, rank, world, local):
            if args.cpu_seconds > 0 else None)
     clocks = clk.summary()
     frame = wavefront_frame(sc, acc, peak) if args.frame else None
+    batched = batched_views(args)
     nrc = time_to_relmse(args)
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world,
@@ -549,6 +632,7 @@ def run_ours(args, rank, world, local):
         "clocks": clocks,
         "ray_sets_mrays_s": dict(set_mrays, **({"shadow": frame["shadow_mrays_s"]} if frame else {})),
         "wavefront_frame": frame,
+        "batched_views": batched,
         "time_to_relmse": nrc,
     }
     print(json.dumps(line))

@@ -298,6 +298,18 @@ int krr_wf_capture_frame(krr_wf *wf, float *d_out, void *stream);
 int krr_wf_launch_frame(krr_wf *wf, int64_t frame_index, const krr_view *views, int32_t n_views,
                         void *stream);
 
+/* Frame groups: several passes (for instance two scenes, each with its own
+ * batched views) captured as one CUDA graph whose branches run the passes'
+ * frames concurrently.  Each pass must have rendered one ordinary frame
+ * before krr_wf_group_capture; krr_wf_group_launch renders frame
+ * `frame_index` of every pass with its current cameras into its d_outs[i].
+ * A pass's results equal the pass rendered alone. */
+typedef struct krr_wf_group krr_wf_group;
+int krr_wf_group_create(krr_wf *const *passes, float *const *d_outs, int32_t n, krr_wf_group **out);
+int krr_wf_group_capture(krr_wf_group *group, void *stream);
+int krr_wf_group_launch(krr_wf_group *group, int64_t frame_index, void *stream);
+int krr_wf_group_destroy(krr_wf_group *group);
+
 /* Stage entry points, for stage-level tests and for subclasses in the manner
  * of PPGPathTracer (src/misc/render/ppg/integrator.h:13). */
 int krr_wf_generate_camera_rays(krr_wf *wf, void *stream);

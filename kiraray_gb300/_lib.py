@@ -109,6 +109,10 @@ SIGNATURES = {
     "krr_version": (_I, []),
     "krr_accel_create_from_triangles": (_I, [_P, C.c_int64, C.POINTER(_P), _P]),
     "krr_set_bvh_node_format": (_I, [C.c_int32]),
+    "krr_wf_group_create": (_I, [C.POINTER(_P), C.POINTER(_P), C.c_int32, C.POINTER(_P)]),
+    "krr_wf_group_capture": (_I, [_P, _P]),
+    "krr_wf_group_launch": (_I, [_P, C.c_int64, _P]),
+    "krr_wf_group_destroy": (_I, [_P]),
     "krr_wf_update_instances": (_I, [_P, C.c_int32, _P, _P, _P]),
     "krr_tonemap": (_I, [_P, _P, C.c_int64, C.c_int32, C.c_float, C.c_int32, _P]),
     "krr_wf_render_megakernel": (_I, [_P, _P, _P]),

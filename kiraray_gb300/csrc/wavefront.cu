@@ -2204,6 +2204,115 @@ extern "C" int krr_wf_launch_frame(krr_wf *wf, int64_t frame_index, const krr_vi
     return KRR_OK;
 }
 
+// Several passes (different scenes, each with its batched views) rendered
+// as one CUDA graph: the graph forks one branch per pass, each branch runs
+// that pass's whole frame, and the branches join, so the passes' launches
+// overlap on the GPU and the tail of one pass's bounces is filled by the
+// others.
+struct krr_wf_group {
+    std::vector<krr_wf *> passes;
+    std::vector<float *> outs;
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> events;    // fork + one join per pass
+    cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" int krr_wf_group_create(krr_wf *const *passes, float *const *d_outs, int32_t n,
+                                   krr_wf_group **out) {
+    KRR_CHECK_ARG(passes && d_outs && out && n >= 1 && n <= 64, "bad group");
+    for (int i = 0; i < n; ++i) {
+        KRR_CHECK_ARG(passes[i] && d_outs[i], "NULL pass or output");
+        KRR_TRY(ready(passes[i]));
+        for (int j = 0; j < i; ++j) KRR_CHECK_ARG(passes[j] != passes[i], "a pass appears twice");
+    }
+    krr_wf_group *g = new krr_wf_group();
+    g->passes.assign(passes, passes + n);
+    g->outs.assign(d_outs, d_outs + n);
+    int status = KRR_OK;
+    for (int i = 0; i < n && status == KRR_OK; ++i) {
+        cudaStream_t s = nullptr;
+        cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e != cudaSuccess) status = cuda_status(e, "cudaStreamCreate", __FILE__, __LINE__);
+        else g->streams.push_back(s);
+    }
+    for (int i = 0; i <= n && status == KRR_OK; ++i) {
+        cudaEvent_t ev = nullptr;
+        cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) status = cuda_status(e, "cudaEventCreate", __FILE__, __LINE__);
+        else g->events.push_back(ev);
+    }
+    if (status != KRR_OK) {
+        krr_wf_group_destroy(g);
+        return status;
+    }
+    *out = g;
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_group_destroy(krr_wf_group *g) {
+    if (!g) return KRR_OK;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    for (cudaStream_t s : g->streams) {
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+    }
+    for (cudaEvent_t e : g->events) cudaEventDestroy(e);
+    delete g;
+    return KRR_OK;
+}
+
+// Captures the group's frame on `stream` (non-default).  Each pass must have
+// rendered one ordinary frame first (lazily sized buffers exist).
+extern "C" int krr_wf_group_capture(krr_wf_group *g, void *stream) {
+    KRR_CHECK_ARG(g != nullptr, "NULL group");
+    cudaStream_t st = as_stream(stream);
+    KRR_CHECK_ARG(st != nullptr, "capture needs a non-default stream");
+    if (g->exec) { cudaGraphExecDestroy(g->exec); g->exec = nullptr; }
+    for (krr_wf *wf : g->passes)
+        for (int i = 0; i < wf->n_views; ++i) wf->h_views[i] = wf->layout[i];
+    KRR_CUDA(cudaStreamSynchronize(st));
+    KRR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int status = KRR_OK;
+    cudaError_t e = cudaEventRecord(g->events[0], st);
+    const int n = (int)g->passes.size();
+    for (int i = 0; i < n && e == cudaSuccess && status == KRR_OK; ++i) {
+        krr_wf *wf = g->passes[i];
+        cudaStream_t si = g->streams[i];
+        e = cudaStreamWaitEvent(si, g->events[0], 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(wf->d_views, wf->h_views, wf->n_views * sizeof(DevView),
+                                cudaMemcpyHostToDevice, si);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(wf->d_frame, wf->h_frame, sizeof(FrameConst), cudaMemcpyHostToDevice, si);
+        if (e != cudaSuccess) break;
+        status = launch_begin_frame(wf, si);
+        if (status == KRR_OK) status = krr_wf_render(wf, g->outs[i], si);
+        if (status == KRR_OK) e = cudaEventRecord(g->events[1 + i], si);
+        if (status == KRR_OK && e == cudaSuccess) e = cudaStreamWaitEvent(st, g->events[1 + i], 0);
+    }
+    if (e != cudaSuccess && status == KRR_OK) status = cuda_status(e, "group capture", __FILE__, __LINE__);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(st, &graph);
+    if (status != KRR_OK) { if (graph) cudaGraphDestroy(graph); return status; }
+    if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+    e = cudaGraphInstantiate(&g->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+    return KRR_OK;
+}
+
+// One frame of every pass of the group: same cameras, frame `frame_index`.
+extern "C" int krr_wf_group_launch(krr_wf_group *g, int64_t frame_index, void *stream) {
+    KRR_CHECK_ARG(g != nullptr, "NULL group");
+    if (!g->exec) return fail(KRR_ERR_NOT_READY, "no captured group frame: call krr_wf_group_capture");
+    cudaStream_t st = as_stream(stream);
+    KRR_CUDA(cudaStreamSynchronize(st));
+    for (krr_wf *wf : g->passes)
+        KRR_TRY(fill_frame(wf, frame_index, nullptr, nullptr, 0, wf->h_views, wf->h_frame));
+    KRR_CUDA(cudaGraphLaunch(g->exec, st));
+    return KRR_OK;
+}
+
 namespace krr {
 int launch_medium_sample(krr_wf *wf, int depth, cudaStream_t st) {
     k_medium_sample<<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->q(Q_MEDIUM_SAMPLE),

@@ -214,3 +214,36 @@ class WavefrontPathTracer:
             self.close()
         except Exception:
             pass
+
+
+class FrameGroup:
+    """Several passes rendered as one CUDA graph with one branch per pass
+    (e.g. two scenes with their batched views); see krr_wf_group_*."""
+
+    def __init__(self, passes, outs):
+        if len(passes) != len(outs):
+            raise ValueError("one output per pass")
+        self.lib = _lib.load()
+        self.passes, self.outs = list(passes), list(outs)
+        n = len(self.passes)
+        hp = (C.c_void_p * n)(*[p._h.value for p in self.passes])
+        ho = (C.c_void_p * n)(*[o.data_ptr() for o in self.outs])
+        self._h = C.c_void_p()
+        check(self.lib.krr_wf_group_create(hp, ho, n, C.byref(self._h)), "krr_wf_group_create")
+
+    def capture(self):
+        check(self.lib.krr_wf_group_capture(self._h, _stream()), "krr_wf_group_capture")
+
+    def launch(self, frame_index: int):
+        check(self.lib.krr_wf_group_launch(self._h, frame_index, _stream()), "krr_wf_group_launch")
+
+    def close(self):
+        if self._h:
+            self.lib.krr_wf_group_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -117,3 +117,42 @@ def test_single_view_graph_replay_advances_samples(krr_lib, cuda):
             want = ref.render().cpu().numpy()
             assert np.array_equal(got[f].view(np.uint32), want.view(np.uint32)), f
     assert not np.array_equal(got[5], got[6])
+
+
+def test_frame_group_equals_passes_alone(krr_lib, cuda):
+    """Two scenes (surfaces with views, volume box with views) captured as one
+    graph with a branch per pass; each output equals its pass rendered alone."""
+    from kiraray_gb300.wavefront import FrameGroup
+    sc_a, views_a = _views()
+    sc_b = scenes.volume_box(8, 8, grid=32)
+    views_b = [(sc_b.camera, 24, 24, 7), (sc_b.camera, 16, 12, 1 << 24)]
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        pa = WavefrontPathTracer({"max_depth": 5})
+        pa.set_scene(sc_a)
+        pa.resize_views(views_a)
+        pb = WavefrontPathTracer({"max_depth": 6})
+        pb.set_scene(sc_b)
+        pb.resize_views(views_b)
+        oa = torch.empty((pa.n_pixels, 4), device="cuda")
+        ob = torch.empty((pb.n_pixels, 4), device="cuda")
+        for p, o in ((pa, oa), (pb, ob)):
+            p.begin_frame_views(1)
+            p.render_flat(o)
+        grp = FrameGroup([pa, pb], [oa, ob])
+        grp.capture()
+        got = {}
+        for f in (3, 4):
+            grp.launch(f)
+            s.synchronize()
+            got[f] = (oa.cpu().numpy().copy(), ob.cpu().numpy().copy())
+        for f in (3, 4):
+            for k, (p, sc, views) in enumerate(((pa, sc_a, views_a), (pb, sc_b, views_b))):
+                ref = WavefrontPathTracer({"max_depth": 5 if k == 0 else 6})
+                ref.set_scene(sc)
+                ref.resize_views(views)
+                ref.begin_frame_views(f)
+                want = ref.render_flat().cpu().numpy()
+                assert np.array_equal(got[f][k].view(np.uint32), want.view(np.uint32)), (f, k)
+        grp.close()
+    assert pa.device_errors() == 0 and pb.device_errors() == 0
