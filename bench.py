@@ -290,6 +290,52 @@ def wavefront_frame(sc, acc, peak, frames: int = 5):
                     "each bounce's shadow rays with the next bounce's rays in one launch"}
 
 
+def config_frames(args):
+    """Frame time of the Cornell box (512x512, max depth 5) and the volume
+    box (1024x1024, max depth 16) on the GPU, and the CPU restatement's time
+    for the same frame estimated from a band of rows in the middle of the
+    image (all host cores)."""
+    if not args.frame:
+        return None
+    import torch
+    from kiraray_gb300 import scenes
+    from kiraray_gb300.wavefront import WavefrontPathTracer
+    from oracle import pyoracle as O
+
+    out = {}
+    for name, sc, frac in (("cornell_box_512", scenes.cornell_box(512, 512, max_depth=5), 4),
+                           ("volume_box_1024", scenes.volume_box(1024, 1024), 16)):
+        params = {"max_depth": sc.max_depth}
+        pt = WavefrontPathTracer(params, seed=sc.seed)
+        pt.set_scene(sc)
+        pt.resize(sc.width, sc.height)
+        img = torch.empty((sc.height, sc.width, 4), device="cuda")
+        s = torch.cuda.current_stream()
+        ms = []
+        for f in range(1, 9):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            pt.begin_frame(f, sc.camera)
+            e0.record(s)
+            pt.render(img)
+            e1.record(s)
+            e1.synchronize()
+            if f > 3:
+                ms.append(e0.elapsed_time(e1))
+        gpu_ms = sorted(ms)[len(ms) // 2]
+        n = sc.width * sc.height
+        band = n // frac
+        lo = (n - band) // 2 // sc.width * sc.width
+        ora = O.PathTracer(sc)
+        t0 = time.perf_counter()
+        ora.render(params, 4, lo, lo + band)
+        cpu_ms = (time.perf_counter() - t0) * 1e3 * n / band
+        out[name] = {"gpu_frame_ms": round(gpu_ms, 3), "gpu_mpaths_s": round(n / gpu_ms / 1e3, 1),
+                     "cpu_frame_ms_est": round(cpu_ms, 1), "cpu_cores": os.cpu_count() or 1,
+                     "cpu_sample": f"rows {lo // sc.width}..{(lo + band) // sc.width} (1/{frac} of the pixels)",
+                     "device_errors": pt.device_errors()}
+    return out
+
+
 def batched_views(args):
     """64 views, sides log-uniform in [256, 1024] (view i seeded 100 + i),
     even views on the large scene and odd views on the volume box, the
@@ -601,6 +647,7 @@ def run_ours(args, rank, world, local):
     clocks = clk.summary()
     frame = wavefront_frame(sc, acc, peak) if args.frame else None
     batched = batched_views(args)
+    frames = config_frames(args)
     nrc = time_to_relmse(args)
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world,
@@ -633,6 +680,7 @@ def run_ours(args, rank, world, local):
         "ray_sets_mrays_s": dict(set_mrays, **({"shadow": frame["shadow_mrays_s"]} if frame else {})),
         "wavefront_frame": frame,
         "batched_views": batched,
+        "config_frames": frames,
         "time_to_relmse": nrc,
     }
     print(json.dumps(line))
