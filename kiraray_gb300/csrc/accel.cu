@@ -902,27 +902,58 @@ extern "C" int krr_accel_trace_stats(const krr_accel *a, const krr_ray *d_rays, 
     return st;
 }
 
+// Host buffers in and out.  The rays go in chunks over two streams (the
+// caller's and a helper), so that the copies of one chunk overlap the
+// traversal of another; each stream has its own work counter in the scratch
+// block (ints 0-1 and 8-9).
 extern "C" int krr_accel_trace_closest_host(const krr_accel *a, const krr_ray *h_rays, int64_t n,
                                             krr_hit *h_hits, void *stream) {
     KRR_CHECK_ARG(a && (n == 0 || (h_rays && h_hits)), "NULL argument");
+    KRR_CHECK_ARG(n >= 0, "negative ray count");
     if (n == 0) return KRR_OK;
+    if (!a->d_nodes) return fail(KRR_ERR_NOT_READY, "acceleration structure not built");
     cudaStream_t s = as_stream(stream);
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_done = nullptr;
     krr_ray *d_rays = nullptr;
     krr_hit *d_hits = nullptr;
-    KRR_CUDA(cudaMallocAsync(&d_rays, n * sizeof(krr_ray), s));
-    KRR_CUDA(cudaMallocAsync(&d_hits, n * sizeof(krr_hit), s));
     int st = KRR_OK;
-    cudaError_t e = cudaMemcpyAsync(d_rays, h_rays, n * sizeof(krr_ray), cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) st = cuda_status(e, "cudaMemcpyAsync", __FILE__, __LINE__);
-    if (st == KRR_OK) st = krr_accel_trace_closest(a, d_rays, n, d_hits, stream);
-    if (st == KRR_OK) {
-        e = cudaMemcpyAsync(h_hits, d_hits, n * sizeof(krr_hit), cudaMemcpyDeviceToHost, s);
-        if (e != cudaSuccess) st = cuda_status(e, "cudaMemcpyAsync", __FILE__, __LINE__);
+    auto check = [&](cudaError_t e, const char *what) {
+        if (st == KRR_OK && e != cudaSuccess) st = cuda_status(e, what, __FILE__, __LINE__);
+    };
+    check(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking), "cudaStreamCreate");
+    check(cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming), "cudaEventCreate");
+    check(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming), "cudaEventCreate");
+    check(cudaMallocAsync(&d_rays, n * sizeof(krr_ray), s), "cudaMallocAsync");
+    check(cudaMallocAsync(&d_hits, n * sizeof(krr_hit), s), "cudaMallocAsync");
+    check(cudaEventRecord(ev_start, s), "cudaEventRecord");
+    check(cudaStreamWaitEvent(aux, ev_start, 0), "cudaStreamWaitEvent");
+    const int64_t chunk = std::max<int64_t>(int64_t(1) << 18, (n + 3) / 4);
+    int k = 0;
+    for (int64_t off = 0; off < n && st == KRR_OK; off += chunk, ++k) {
+        const int64_t m = std::min(chunk, n - off);
+        cudaStream_t sk = (k & 1) ? aux : s;
+        check(cudaMemcpyAsync(d_rays + off, h_rays + off, m * sizeof(krr_ray), cudaMemcpyHostToDevice, sk),
+              "cudaMemcpyAsync");
+        if (st != KRR_OK) break;
+        TraceLaunch l = aos_launch(a, d_rays + off, m);
+        l.hits = reinterpret_cast<float4 *>(d_hits + off);
+        l.counter = a->d_scratch + ((k & 1) ? 8 : 0);
+        st = launch_trace_closest(a, l, sk);
+        if (st != KRR_OK) break;
+        check(cudaMemcpyAsync(h_hits + off, d_hits + off, m * sizeof(krr_hit), cudaMemcpyDeviceToHost, sk),
+              "cudaMemcpyAsync");
     }
-    cudaFreeAsync(d_rays, s);
-    cudaFreeAsync(d_hits, s);
-    e = cudaStreamSynchronize(s);
-    if (st == KRR_OK && e != cudaSuccess) st = cuda_status(e, "cudaStreamSynchronize", __FILE__, __LINE__);
+    if (ev_done && aux) {
+        cudaEventRecord(ev_done, aux);
+        cudaStreamWaitEvent(s, ev_done, 0);
+    }
+    if (d_rays) cudaFreeAsync(d_rays, s);
+    if (d_hits) cudaFreeAsync(d_hits, s);
+    check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    if (aux) cudaStreamDestroy(aux);
+    if (ev_start) cudaEventDestroy(ev_start);
+    if (ev_done) cudaEventDestroy(ev_done);
     return st;
 }
 

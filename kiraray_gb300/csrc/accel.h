@@ -41,7 +41,7 @@ struct krr_accel {
     float4 *d_nodes = nullptr;   // 5 per node
     float4 *d_tris = nullptr;    // 3 per triangle
     uint32_t *d_leaf_of_prim = nullptr;  // global id -> leaf-order slot
-    int *d_scratch = nullptr;    // [0] ray counter, [1] error flags
+    int *d_scratch = nullptr;    // 64 B: ints 0-1 ray counter, 4 error flags, 8-9 second counter
     float scene_lo[3] = {0, 0, 0}, scene_hi[3] = {0, 0, 0};
     int refill_below = 20;       // traversal tuning (krr_accel_set_tuning)
     int postpone_pct = 0;

@@ -233,3 +233,16 @@ def test_float_nodes_in_wavefront_frame(krr_lib, cuda, float_nodes):
     oL, _ = O.PathTracer(sc).render({"max_depth": 4}, 1)
     bad = (np.abs(L - oL) > 1e-4 * np.abs(oL) + 1e-6).any(1).mean()
     assert bad <= 0.01 and not pt.device_errors()
+
+
+def test_host_entry_point_in_chunks(krr_lib, cuda):
+    """More than four chunks of host rays over the two streams: the hits
+    equal the device-buffer entry point's."""
+    sc = scenes.large_scene(width=160, height=90, grid=256, n_spheres=30, sky_size=(64, 32))
+    tris = sc.world_triangles()
+    acc = Accel(tris)
+    rays = H.random_rays(1_300_000, 77, box=60.0)
+    want = _gpu_closest(acc, rays)
+    got = torch.empty((rays.shape[0], 4), dtype=torch.float32).pin_memory()
+    acc.trace_closest_host(torch.from_numpy(rays).pin_memory(), got)
+    _assert_bits_equal(got.numpy(), want, "host entry point, chunked")
