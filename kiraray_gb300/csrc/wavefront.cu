@@ -1093,7 +1093,6 @@ __global__ void k_shadow_tr(DevScene s, const float4 *__restrict__ nodes,
     }
 }
 
-// pixel += L (integrator.cpp:257-260)
 // pixel += L after each sample (integrator.cpp:255-258); with `clear` the
 // next sample starts from L = 0 (the reference keeps L for the whole frame).
 __global__ void k_accumulate(PixelState ps, int64_t n, int clear) {

@@ -3,10 +3,12 @@ and single-kernel captures); prints the device time of each repetition.
 
     python -m kiraray_gb300.profile trace [--reps 4]
         closest hits of the 1920x1080 camera rays of the 10.9M-triangle scene
-    python -m kiraray_gb300.profile frame [--res 480x270] [--views 8] [--nrc] [--frames 3]
-        frames of the wavefront pass on the same scene (max depth 8), the
-        camera replicated into `views` batched views, optionally with the
-        neural radiance cache attached and training
+    python -m kiraray_gb300.profile frame [--scene large] [--res 480x270] [--views 8] [--nrc]
+                                          [--frames 3]
+        frames of the wavefront pass on the large scene (max depth 8), the
+        Cornell box (5) or the volume box (16), the camera replicated into
+        `views` batched views, optionally with the neural radiance cache
+        attached and training
 """
 from __future__ import annotations
 
@@ -37,14 +39,19 @@ def trace(reps: int) -> dict:
     return {"workload": "trace", "rays": int(rays.shape[0]), "ms": ms}
 
 
-def frame(res: str, views: int, nrc: bool, frames: int) -> dict:
+def frame(res: str, views: int, nrc: bool, frames: int, scene: str = "large") -> dict:
     from . import scenes
     from .convergence import replica_views
     from .nrc import NeuralRadianceCache
     from .wavefront import WavefrontPathTracer
 
     w, h = (int(x) for x in res.split("x"))
-    sc = scenes.large_scene(width=w, height=h, seed=3)
+    if scene == "large":
+        sc = scenes.large_scene(width=w, height=h, seed=3)
+    elif scene == "cornell":
+        sc = scenes.cornell_box(w, h)
+    else:
+        sc = scenes.volume_box(w, h)
     pt = WavefrontPathTracer({"max_depth": sc.max_depth}, seed=3)
     pt.set_scene(sc)
     if nrc:
@@ -59,7 +66,7 @@ def frame(res: str, views: int, nrc: bool, frames: int) -> dict:
         pt.render_flat(out)
 
     ms = [_timed(lambda: one(f)) for f in range(1, frames + 1)]
-    return {"workload": "frame", "res": res, "views": views, "nrc": nrc, "ms": ms,
+    return {"workload": "frame", "scene": scene, "res": res, "views": views, "nrc": nrc, "ms": ms,
             "device_errors": pt.device_errors()}
 
 
@@ -69,6 +76,7 @@ def main() -> None:
     t = sub.add_parser("trace")
     t.add_argument("--reps", type=int, default=4)
     f = sub.add_parser("frame")
+    f.add_argument("--scene", default="large", choices=["large", "cornell", "volume"])
     f.add_argument("--res", default="480x270")
     f.add_argument("--views", type=int, default=8)
     f.add_argument("--nrc", action="store_true")
@@ -76,7 +84,7 @@ def main() -> None:
     a = ap.parse_args()
     from .build import build
     build()
-    r = trace(a.reps) if a.cmd == "trace" else frame(a.res, a.views, a.nrc, a.frames)
+    r = trace(a.reps) if a.cmd == "trace" else frame(a.res, a.views, a.nrc, a.frames, a.scene)
     print(json.dumps(r))
 
 
