@@ -117,11 +117,10 @@ __global__ void k_encode(NrcGrid g, const float *__restrict__ in, const int32_t 
             x[2 * l + 1] = __float2bfloat16_rn(f1);
         }
         int o = 2 * g.levels;
-        for (int a = 0; a < 3; ++a) x[o + a] = __float2bfloat16_rn((q[3 + a] + 1.f) * 0.5f);
-        x[o + 3] = __float2bfloat16_rn(q[6]);
-        for (int a = 0; a < 3; ++a) x[o + 4 + a] = __float2bfloat16_rn(q[7 + a]);
-        for (int a = 0; a < 3; ++a) x[o + 7 + a] = __float2bfloat16_rn((q[10 + a] + 1.f) * 0.5f);
-        for (int k = o + 10; k < kNrcIn; ++k) x[k] = __float2bfloat16_rn(0.f);
+        float e[kNrcExtra];
+        nrc_encode_extras(q, e);
+        for (int a = 0; a < kNrcExtra; ++a) x[o + a] = __float2bfloat16_rn(e[a]);
+        for (int k = o + kNrcExtra; k < kNrcIn; ++k) x[k] = __float2bfloat16_rn(0.f);
     }
 }
 
@@ -590,7 +589,7 @@ extern "C" int krr_nrc_create(const krr_nrc_config *cfg, krr_nrc **out) {
     std::vector<float> w(m.n_params, 0.f);
     for (int l = 0; l < m.layers; ++l) {
         int rows = l + 1 < m.layers ? kNrcWidth : 3;
-        int fan_in = l == 0 ? 2 * g.levels + 7 : kNrcWidth;
+        int fan_in = l == 0 ? 2 * g.levels + kNrcExtra : kNrcWidth;
         float a = std::sqrt(6.f / (float)(fan_in + rows));
         for (int r = 0; r < rows; ++r)
             for (int k = 0; k < fan_in; ++k) w[m.w_offset[l] + r * kNrcIn + k] = (2.f * rng.uniform() - 1.f) * a;

@@ -16,6 +16,41 @@ constexpr int kNrcOutPad = 16;   // padded output rows (3 used)
 constexpr int kNrcInputs = 13;   // query record: position 3, normal 3, roughness 1, albedo 3,
                                  // outgoing direction 3
 
+// Inputs after the hash-grid features (the encoding of neural radiance
+// caching, Mueller et al. 2021): normal and outgoing direction as spherical
+// angles, and roughness as 1 - exp(-r), each in a one-blob encoding of 4
+// bins (Gaussian bumps of width 1/4 centred at (i + 0.5)/4); albedo as is.
+constexpr int kNrcBlobBins = 4;
+constexpr int kNrcExtra = 5 * kNrcBlobBins + 3;
+
+__host__ __device__ inline void nrc_one_blob(float s, float *x) {
+    for (int i = 0; i < kNrcBlobBins; ++i) {
+        float d = (s - ((float)i + 0.5f) / (float)kNrcBlobBins) * (float)kNrcBlobBins;
+        x[i] = expf(-0.5f * d * d);
+    }
+}
+
+__host__ __device__ inline void nrc_spherical(float x, float y, float z, float &theta, float &phi) {
+    theta = acosf(fminf(fmaxf(z, -1.f), 1.f)) * 0.318309886183790672f;        // / pi
+    phi = atan2f(y, x) * 0.159154943091895336f + 0.5f;                          // / (2 pi) + 1/2
+}
+
+// q: query record (position 3, normal 3, roughness 1, albedo 3, wo 3);
+// writes kNrcExtra values.
+__host__ __device__ inline void nrc_encode_extras(const float *q, float *x) {
+    float t, p;
+    nrc_spherical(q[3], q[4], q[5], t, p);
+    nrc_one_blob(t, x);
+    nrc_one_blob(p, x + kNrcBlobBins);
+    nrc_spherical(q[10], q[11], q[12], t, p);
+    nrc_one_blob(t, x + 2 * kNrcBlobBins);
+    nrc_one_blob(p, x + 3 * kNrcBlobBins);
+    nrc_one_blob(1.f - expf(-q[6]), x + 4 * kNrcBlobBins);
+    x[5 * kNrcBlobBins + 0] = q[7];
+    x[5 * kNrcBlobBins + 1] = q[8];
+    x[5 * kNrcBlobBins + 2] = q[9];
+}
+
 // Hash-grid description passed by value to kernels.
 struct NrcGrid {
     int32_t levels, features;         // features per level (2)

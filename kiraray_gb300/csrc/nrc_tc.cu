@@ -172,11 +172,8 @@ __device__ __forceinline__ void encode_row(const NrcGrid &g, const float *q,
         x[2 * l + 1] = f1;
     }
     int o = 2 * g.levels;
-    for (int a = 0; a < 3; ++a) x[o + a] = (q[3 + a] + 1.f) * 0.5f;
-    x[o + 3] = q[6];
-    for (int a = 0; a < 3; ++a) x[o + 4 + a] = q[7 + a];
-    for (int a = 0; a < 3; ++a) x[o + 7 + a] = (q[10 + a] + 1.f) * 0.5f;
-    for (int k = o + 10; k < kNrcIn; ++k) x[k] = 0.f;
+    nrc_encode_extras(q, x + o);
+    for (int k = o + kNrcExtra; k < kNrcIn; ++k) x[k] = 0.f;
 }
 
 // out[i][0..3) for i < *count (or cap); optional per-layer activation dump

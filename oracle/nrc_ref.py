@@ -74,6 +74,34 @@ class Mlp:
             o += rows * IN
 
 
+BLOB_BINS = 4
+EXTRA = 5 * BLOB_BINS + 3
+
+
+def one_blob(s: np.ndarray) -> np.ndarray:
+    c = (np.arange(BLOB_BINS) + 0.5) / BLOB_BINS
+    d = (s[:, None] - c[None, :]) * BLOB_BINS
+    return np.exp(-0.5 * d * d)
+
+
+def spherical(v: np.ndarray):
+    theta = np.arccos(np.clip(v[:, 2], -1, 1)) / np.pi
+    phi = np.arctan2(v[:, 1], v[:, 0]) / (2 * np.pi) + 0.5
+    return theta, phi
+
+
+def encode_extras(inputs: np.ndarray) -> np.ndarray:
+    """Normal and outgoing direction (spherical angles) and 1 - exp(-roughness)
+    in one-blob encodings of 4 bins, albedo as is (the neural radiance
+    caching input encoding)."""
+    q = inputs.astype(np.float64)
+    tn, pn = spherical(q[:, 3:6])
+    tw, pw = spherical(q[:, 10:13])
+    parts = [one_blob(tn), one_blob(pn), one_blob(tw), one_blob(pw), one_blob(1 - np.exp(-q[:, 6])),
+             q[:, 7:10]]
+    return np.concatenate(parts, axis=1)
+
+
 def encode(grid: Grid, table: np.ndarray, inputs: np.ndarray, rounding=True):
     """Encoded inputs X0 [n, 64] and the corner data for the backward pass."""
     n = inputs.shape[0]
@@ -86,10 +114,7 @@ def encode(grid: Grid, table: np.ndarray, inputs: np.ndarray, rounding=True):
         X[:, 2 * l] = (w * tab[idx, 0]).sum(1)
         X[:, 2 * l + 1] = (w * tab[idx, 1]).sum(1)
     o = 2 * grid.levels
-    X[:, o:o + 3] = (inputs[:, 3:6].astype(np.float64) + 1) * 0.5
-    X[:, o + 3] = inputs[:, 6]
-    X[:, o + 4:o + 7] = inputs[:, 7:10]
-    X[:, o + 7:o + 10] = (inputs[:, 10:13].astype(np.float64) + 1) * 0.5
+    X[:, o:o + EXTRA] = encode_extras(inputs)
     if rounding:
         X = bf16(X)
     return X, cs
