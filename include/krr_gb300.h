@@ -164,6 +164,11 @@ typedef struct krr_accel_stats {
  * 8-wide nodes (224 B, fewer instructions per box test).  Hits are the
  * same with either.  krr_accel_stats.reserved reports a build's format. */
 int krr_set_bvh_node_format(int32_t format);
+/* Largest leaf child of the BVHs built from now on, in triangles (1..3,
+ * default 1): smaller leaves test fewer triangles per ray for a few more
+ * node visits (a triangle test costs several node-child tests).  Hits are
+ * the same with any setting. */
+int krr_set_bvh_max_leaf(int32_t triangles);
 
 /* Build from host arrays of world-space triangles: h_vertices float3[3*n]. */
 int krr_accel_create_from_triangles(const float *h_vertices, int64_t n_triangles,

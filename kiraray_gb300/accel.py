@@ -26,6 +26,11 @@ def set_node_format(fmt: int) -> None:
     check(_lib.load().krr_set_bvh_node_format(fmt), "krr_set_bvh_node_format")
 
 
+def set_max_leaf(triangles: int) -> None:
+    """Largest leaf (1..3 triangles) of the BVHs built from now on."""
+    check(_lib.load().krr_set_bvh_max_leaf(triangles), "krr_set_bvh_max_leaf")
+
+
 class Accel:
     def __init__(self, world_triangles: np.ndarray, node_format: int | None = None):
         lib = _lib.load()

@@ -225,7 +225,8 @@ __device__ __forceinline__ int quant_exponent(float ext) {
 
 __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const int *n_in,
                            CollapseItem *out, int *n_out, float4 *nodes, int *node_counter,
-                           uint32_t *leaf_order, int *tri_counter, int *max_depth, int format) {
+                           uint32_t *leaf_order, int *tri_counter, int *max_depth, int format,
+                           int max_leaf) {
     int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= *n_in) return;
     CollapseItem item = in[w];
@@ -245,7 +246,7 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
         bool best_must = false;
         for (int c = 0; c < nc; ++c) {
             if (ref[c] & kLeafBit) continue;
-            bool must = ccount[c] > 3;
+            bool must = ccount[c] > max_leaf;
             float a = half_area(clo[c], chi[c]);
             if ((must && !best_must) || (must == best_must && a > best_area)) {
                 best = c; best_area = a; best_must = must;
@@ -297,7 +298,7 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
     // Allocate internal children and leaf triangles.
     int n_int = 0, n_tri = 0;
     for (int c = 0; c < nc; ++c) {
-        if (ccount[c] > 3) ++n_int;
+        if (ccount[c] > max_leaf) ++n_int;
         else n_tri += ccount[c];
     }
     int child_base = n_int ? atomicAdd(node_counter, n_int) : 0;
@@ -324,7 +325,7 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
             qhi[k][s >> 2] |= (uint32_t)b << (8 * (s & 3));
         }
         uint32_t m;
-        if (ccount[c] > 3) {
+        if (ccount[c] > max_leaf) {
             m = 0x20u | (24u + (uint32_t)s);
             imask |= 1u << s;
         } else {
@@ -338,7 +339,7 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
     // internal children in slot order
     for (int s = 0; s < 8; ++s) {
         int c = child_in_slot[s];
-        if (c < 0 || ccount[c] <= 3) continue;
+        if (c < 0 || ccount[c] <= max_leaf) continue;
         int slot = atomicAdd(n_out, 1);
         out[slot] = CollapseItem{ref[c], (uint32_t)(child_base + int_rank), item.depth + 1};
         ++int_rank;
@@ -628,6 +629,7 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     KRR_CHECK_ARG(n >= 0 && n < (int64_t)0x7fffffff, "triangle count out of range");
     accel_free(a);
     a->node_format = default_node_format();
+    a->max_leaf = default_max_leaf();
     a->n_tris = n;
     a->n_nodes = 0;
     a->max_depth = 0;
@@ -734,7 +736,7 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
         KRR_CUDA(cudaMemsetAsync(c_out, 0, sizeof(int), s));
         k_collapse<<<blocks_for(n_in, 128), 128, 0, s>>>(bt, qin, c_in, qout, c_out, nodes_tmp.p,
                                                          counters.p, leaf_order.p, counters.p + 1,
-                                                         counters.p + 2, fmt);
+                                                         counters.p + 2, fmt, a->max_leaf);
         KRR_CUDA(cudaGetLastError());
         KRR_CUDA(cudaMemcpyAsync(&n_in, c_out, sizeof(int), cudaMemcpyDeviceToHost, s));
         KRR_CUDA(cudaMemcpyAsync(c_in, c_out, sizeof(int), cudaMemcpyDeviceToDevice, s));
@@ -802,7 +804,15 @@ extern "C" int krr_accel_create_from_triangles(const float *h_vertices, int64_t 
 }
 
 static int g_node_format = 0;
+static int g_max_leaf = 1;
 int krr::default_node_format() { return g_node_format; }
+int krr::default_max_leaf() { return g_max_leaf; }
+
+extern "C" int krr_set_bvh_max_leaf(int32_t triangles) {
+    KRR_CHECK_ARG(triangles >= 1 && triangles <= 3, "leaf size must be 1, 2 or 3 triangles");
+    g_max_leaf = triangles;
+    return KRR_OK;
+}
 
 extern "C" int krr_set_bvh_node_format(int32_t format) {
     KRR_CHECK_ARG(format == 0 || format == 1, "node format must be 0 (compressed) or 1 (float)");

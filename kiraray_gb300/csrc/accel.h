@@ -46,6 +46,7 @@ struct krr_accel {
     int refill_below = 20;       // traversal tuning (krr_accel_set_tuning)
     int postpone_pct = 0;
     int node_format = 0;         // 0 compressed (80 B), 1 float (224 B)
+    int max_leaf = 1;            // triangles per leaf child (1..3)
 };
 
 namespace krr {
@@ -54,6 +55,7 @@ constexpr int kTraversalStack = 48;
 constexpr int kNodeQuads[2] = {5, 14};   // float4 per node, by node format
 // Process-wide node format used by builds (krr_set_bvh_node_format).
 int default_node_format();
+int default_max_leaf();   // krr_set_bvh_max_leaf
 constexpr int kTraceThreads = 128;
 
 // Build from device world-space vertices (float3 x 3 per triangle).

@@ -246,3 +246,31 @@ def test_host_entry_point_in_chunks(krr_lib, cuda):
     got = torch.empty((rays.shape[0], 4), dtype=torch.float32).pin_memory()
     acc.trace_closest_host(torch.from_numpy(rays).pin_memory(), got)
     _assert_bits_equal(got.numpy(), want, "host entry point, chunked")
+
+
+@pytest.mark.parametrize("leaf", [1, 2, 3])
+def test_leaf_sizes_keep_hits_identical(krr_lib, cuda, leaf):
+    from kiraray_gb300.accel import set_max_leaf
+    sc = scenes.large_scene(width=160, height=90, grid=256, n_spheres=40, sky_size=(64, 32))
+    tris = sc.world_triangles()
+    rays = H.pinhole_rays(sc, jitter_seed=11)
+    set_max_leaf(leaf)
+    try:
+        acc = Accel(tris)
+    finally:
+        set_max_leaf(1)
+    ob = O.Bvh(tris)
+    want = ob.closest(rays)
+    _assert_bits_equal(_gpu_closest(acc, rays), want, f"leaf {leaf}")
+    b = H.bounce_rays(tris, rays, want, 12)
+    _assert_bits_equal(_gpu_closest(acc, b), ob.closest(b), f"leaf {leaf} bounce")
+    occ = acc.trace_any(torch.from_numpy(b).cuda()).cpu().numpy()
+    assert np.array_equal(occ, ob.any(b))
+    g = H.grid_mesh(12)
+    r = H.vertex_edge_rays(12, 3)
+    set_max_leaf(leaf)
+    try:
+        ga = Accel(g)
+    finally:
+        set_max_leaf(1)
+    _assert_bits_equal(_gpu_closest(ga, r), O.closest_brute(g, r), f"leaf {leaf} edges")
