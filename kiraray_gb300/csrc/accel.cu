@@ -551,6 +551,18 @@ k_trace_mixed(const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
 
 int g_grid_size = 0;
 
+// An empty scene: every ray misses (MODE as k_trace).
+__global__ void k_all_miss(TraceLaunch L, int mode) {
+    const int64_t n_any = mode == 2 ? (int64_t)*L.d_any_count : 0;
+    const int64_t n = (L.d_count ? (int64_t)*L.d_count : L.n) + n_any;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const bool any = mode == 1 || (mode == 2 && i < n_any);
+        if (any) L.occluded[i] = 0;
+        else L.hits[mode == 2 ? i - n_any : i] = make_float4(INFINITY, 0.f, 0.f, __uint_as_float(KRR_MISS));
+    }
+}
+
 }  // namespace
 
 int traversal_grid_size() {
@@ -567,9 +579,13 @@ int traversal_grid_size() {
 template <int MODE, bool STATS>
 static int launch_trace(const krr_accel *a, const TraceLaunch &l, cudaStream_t s,
                         unsigned long long *stats = nullptr) {
-    if (!a || !a->d_nodes) return fail(KRR_ERR_NOT_READY, "acceleration structure not built");
+    if (!a || !a->d_scratch) return fail(KRR_ERR_NOT_READY, "acceleration structure not built");
     KRR_CUDA(cudaMemsetAsync(l.counter, 0, sizeof(unsigned long long), s));
-    if (a->n_tris == 0) return KRR_OK;
+    if (a->n_tris == 0) {
+        k_all_miss<<<traversal_grid_size(), kTraceThreads, 0, s>>>(l, MODE);
+        KRR_CUDA(cudaGetLastError());
+        return KRR_OK;
+    }
     TraceLaunch lt = l;
     lt.refill_below = a->refill_below;
     lt.postpone_pct = a->postpone_pct;
@@ -872,8 +888,7 @@ extern "C" int krr_accel_trace_closest(const krr_accel *a, const krr_ray *d_rays
     if (n == 0) return KRR_OK;
     TraceLaunch l = aos_launch(a, d_rays, n);
     l.hits = reinterpret_cast<float4 *>(d_hits);
-    if (a->n_tris == 0) return fail(KRR_ERR_NOT_READY, "empty acceleration structure");
-    return launch_trace_closest(a, l, as_stream(stream));
+    return launch_trace_closest(a, l, as_stream(stream));   // no triangles: every ray misses
 }
 
 extern "C" int krr_accel_trace_any(const krr_accel *a, const krr_ray *d_rays, int64_t n,
@@ -881,7 +896,6 @@ extern "C" int krr_accel_trace_any(const krr_accel *a, const krr_ray *d_rays, in
     KRR_CHECK_ARG(a && (n == 0 || (d_rays && d_occluded)), "NULL argument");
     KRR_CHECK_ARG(n >= 0, "negative ray count");
     if (n == 0) return KRR_OK;
-    if (a->n_tris == 0) return fail(KRR_ERR_NOT_READY, "empty acceleration structure");
     TraceLaunch l = aos_launch(a, d_rays, n);
     l.occluded = d_occluded;
     return launch_trace_any(a, l, as_stream(stream));
@@ -921,7 +935,7 @@ extern "C" int krr_accel_trace_closest_host(const krr_accel *a, const krr_ray *h
     KRR_CHECK_ARG(a && (n == 0 || (h_rays && h_hits)), "NULL argument");
     KRR_CHECK_ARG(n >= 0, "negative ray count");
     if (n == 0) return KRR_OK;
-    if (!a->d_nodes) return fail(KRR_ERR_NOT_READY, "acceleration structure not built");
+    if (!a->d_scratch) return fail(KRR_ERR_NOT_READY, "acceleration structure not built");
     cudaStream_t s = as_stream(stream);
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_start = nullptr, ev_done = nullptr;

@@ -706,7 +706,9 @@ __device__ __forceinline__ void scatter_item(const DevScene &s, const Queue &sca
     ShadingData sd = shading_data(s, material);
     uint32_t bsdf_type = bsdf_type_of(sd);
     Bsdf bsdf = Bsdf::setup(sd);
-    if (nee && (bsdf_type & BSDF_SMOOTH)) {
+    // a scene without emitters has nothing to sample (the reference indexes an
+    // empty light list there); NEE and its draws are skipped
+    if (nee && (bsdf_type & BSDF_SMOOTH) && s.n_lights > 0) {
         float ul = rng.get1d();
         uint32_t lid = (uint32_t)(ul * (float)s.n_lights);
         float sel_pdf = 1.f / (float)s.n_lights;
@@ -968,7 +970,7 @@ __global__ void k_medium_scatter(DevScene s, Queue mscat, Queue next, Queue shad
         float time = c3.w;
         float g = s.media[medium].g;
         Pcg rng = load_rng(ps, pixel);
-        if (nee) {
+        if (nee && s.n_lights > 0) {
             float ul = rng.get1d();
             uint32_t lid = (uint32_t)(ul * (float)s.n_lights);
             float u0 = rng.get1d(), u1 = rng.get1d();
@@ -1224,7 +1226,7 @@ k_megakernel(DevScene s, const float4 *__restrict__ nodes, const float4 *__restr
                     ShadingData sd = shading_data(s, sf.material);
                     uint32_t bsdf_type = bsdf_type_of(sd);
                     Bsdf bsdf = Bsdf::setup(sd);
-                    if (c.nee && (bsdf_type & BSDF_SMOOTH)) {
+                    if (c.nee && (bsdf_type & BSDF_SMOOTH) && s.n_lights > 0) {
                         float ul = rng.get1d();
                         uint32_t lid = (uint32_t)(ul * (float)s.n_lights);
                         float sel_pdf = 1.f / (float)s.n_lights;
@@ -1626,7 +1628,8 @@ extern "C" int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *sd, void *stre
         infs[i] = d;
         lights.push_back(DevLight{1, i, 0, 0});
     }
-    KRR_CHECK_ARG(!lights.empty(), "the scene has no light");
+    // A scene without lights is accepted: light sampling is skipped (every
+    // NEE site tests n_lights) and the frame is black.
 
     DevScene s{};
     KRR_TRY(dev_upload(wf, const_cast<DevMesh **>(&s.meshes), meshes.data(), meshes.size()));

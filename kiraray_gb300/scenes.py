@@ -162,6 +162,8 @@ class Scene:
                 acc = (acc + (m[r, 2] * p[:, 2]).astype(np.float32)).astype(np.float32)
                 w[:, r] = (acc + m[r, 3]).astype(np.float32)
             out.append(w[mesh.indices.astype(np.int64)].reshape(-1, 9))
+        if not out:
+            return np.zeros((0, 9), np.float32)
         return np.ascontiguousarray(np.concatenate(out, 0), dtype=np.float32)
 
     def desc(self):

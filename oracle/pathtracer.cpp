@@ -777,7 +777,7 @@ void render_pixel(const oracle_pt &s, const krr_wf_params &prm, const Camera &ca
             if (has_mscatter) {
                 // sampleMediumScattering
                 float g = s.media[msc_medium].g;
-                if (prm.nee) {
+                if (prm.nee && !s.lights.empty()) {
                     float u = rng.get1d();
                     uint32_t lid = (uint32_t)(u * (float)s.lights.size());
                     float u0 = rng.get1d();
@@ -834,7 +834,7 @@ void render_pixel(const oracle_pt &s, const krr_wf_params &prm, const Camera &ca
                     ShadingData sd = shading_data(s, sf.material);
                     uint32_t bt = bsdf_type_of(sd);
                     Bsdf bsdf = Bsdf::setup(sd);
-                    if (prm.nee && (bt & BSDF_SMOOTH)) {
+                    if (prm.nee && (bt & BSDF_SMOOTH) && !s.lights.empty()) {
                         float u = rng.get1d();
                         uint32_t lid = (uint32_t)(u * (float)s.lights.size());
                         float u0 = rng.get1d();

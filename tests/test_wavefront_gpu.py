@@ -257,3 +257,51 @@ def test_update_instances_equals_fresh_scene(krr_lib, cuda):
     b = fresh.render().cpu().numpy()
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
     assert pt.device_errors() == 0
+
+
+def test_scene_without_emitters_and_tiny_frames(krr_lib, cuda):
+    """No area or infinite light: NEE has nothing to sample and the frame is
+    black; frames of 1x1 and 3x1 pixels; both match the oracle."""
+    from kiraray_gb300.scenes import Material
+    dark = scenes.cornell_box(8, 8, max_depth=4)
+    for m in dark.meshes:
+        m.emission = (0.0, 0.0, 0.0)
+    dark.infinite_lights = []
+    pt = WavefrontPathTracer({"max_depth": 4})
+    pt.set_scene(dark)
+    for w, h in ((8, 8), (1, 1), (3, 1)):
+        pt.resize(w, h)
+        pt.begin_frame(2, dark.camera)
+        img = pt.render().cpu().numpy()
+        assert img.shape == (h, w, 4) and np.all(img[..., :3] == 0.0)
+        b = pt.render_megakernel().cpu().numpy()
+        assert np.all(b[..., :3] == 0.0)
+    assert pt.device_errors() == 0
+    lit = scenes.cornell_box(3, 1, max_depth=4)
+    pt.set_scene(lit)
+    pt.resize(3, 1)
+    L, _ = gpu_frame(pt, lit, 5)
+    oL, _ = O.PathTracer(lit).render({"max_depth": 4}, 5)
+    compare(L[:, :3], oL, "3x1 frame")
+
+
+def test_empty_geometry(krr_lib, cuda):
+    """No triangles: every ray misses; the frame is the environment."""
+    from kiraray_gb300.accel import Accel
+    from kiraray_gb300.scenes import InfiniteLight, Material, Scene
+    acc = Accel(np.zeros((0, 9), np.float32))
+    one = np.array([[0, 0, 0, 0, 0, 0, 1, np.inf]], np.float32)
+    rays = torch.from_numpy(np.tile(one, (100, 1))).cuda()
+    hits = acc.trace_closest(rays).cpu().numpy()
+    assert np.all(hits[:, 3].view(np.uint32) == 0xFFFFFFFF) and np.all(np.isinf(hits[:, 0]))
+    assert not acc.trace_any(rays).cpu().numpy().any()
+    cam = scenes.cornell_box(16, 12).camera
+    sc = Scene([], [], [Material()], cam, 16, 12,
+               infinite_lights=[InfiniteLight(tint=(0.2, 0.3, 0.5), scale=2.0)], max_depth=3)
+    pt = WavefrontPathTracer({"max_depth": 3})
+    pt.set_scene(sc)
+    pt.resize(16, 12)
+    pt.begin_frame(1, cam)
+    img = pt.render().cpu().numpy()
+    assert np.allclose(img[..., :3], np.array([0.4, 0.6, 1.0], np.float32), rtol=1e-6)
+    assert pt.device_errors() == 0
