@@ -202,9 +202,10 @@ __device__ __forceinline__ V3 box_inverse(V3 d) {
 
 // Single-ray traversal for kernels that trace inside their own loops.
 // Closest hit: returns (t, b1, b2, id bits) or id KRR_MISS; any hit: the id
-// of some blocking triangle (mask != 0) or KRR_MISS.  Same hit as the
-// persistent kernel (the result does not depend on traversal order).
-template <bool ANY, int FMT>
+// of some blocking triangle (mask != 0, or any triangle when !MASKED) or
+// KRR_MISS.  Same hit as the persistent kernel (the result does not depend
+// on traversal order).
+template <bool ANY, int FMT, bool MASKED = true>
 __device__ float4 traverse_ray(const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
                                V3 o, V3 d, float tmin, float tmax, int *err) {
     RayPre r = ray_pre(o, d, tmin);
@@ -238,7 +239,8 @@ __device__ float4 traverse_ray(const float4 *__restrict__ nodes, const float4 *_
             float t = tri_test(r, v0, v1, v2, b1, b2);
             uint32_t gid = __float_as_uint(v0.w);
             if (ANY) {
-                if (t > r.tmin && t <= tmax && __float_as_uint(v1.w) != 0u) return make_float4(t, b1, b2, __uint_as_float(gid));
+                if (t > r.tmin && t <= tmax && (!MASKED || __float_as_uint(v1.w) != 0u))
+                    return make_float4(t, b1, b2, __uint_as_float(gid));
             } else if (t > r.tmin && (t < tmax || (t == tmax && gid < best))) {
                 tmax = t; b1b = b1; b2b = b2; best = gid;
             }

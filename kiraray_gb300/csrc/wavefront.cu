@@ -86,7 +86,8 @@ struct krr_wf {
     uint64_t n_tris = 0;
     // queues and pixel state
     float4 *qbuf[Q_COUNT] = {};
-    int32_t *d_counts = nullptr;   // [0..7] queue sizes, [8] error flags
+    int32_t *d_counts = nullptr;   // [0..7] queue sizes, [8] error flags, [9-10] cache
+                                   // batches, [11] ratio-tracked shadow rays
     float4 *hits = nullptr;
     uint8_t *occluded = nullptr;
     PixelState ps{};
@@ -113,6 +114,7 @@ struct krr_wf {
     Queue q(int k) const { return Queue{qbuf[k], (int32_t)n, d_counts + k}; }
     int32_t *nrc_q_count() const { return d_counts + 9; }
     int32_t *nrc_b_count() const { return d_counts + 10; }
+    int32_t *shadow_tracked_count() const { return d_counts + 11; }
     uint32_t *err() const { return reinterpret_cast<uint32_t *>(d_counts + 8); }
     WfConst consts() const {
         WfConst c;
@@ -555,9 +557,11 @@ __global__ void k_clamp_count(int32_t *count, int cap) {
 }
 
 // Routing of a closest hit (__closesthit__/__miss__Closest, device.cu:43-74).
-__global__ void k_hit_process(DevScene s, Queue rq, const float4 *__restrict__ hits, Queue next,
-                              Queue miss, Queue hitl, Queue scat, Queue msq, int enable_medium,
-                              uint32_t *err, NrcHook hook, PixelState ps) {
+// Four blocks per SM (64 registers): the mesh gathers are latency-bound.
+__global__ void __launch_bounds__(kThreads, 4)
+k_hit_process(DevScene s, Queue rq, const float4 *__restrict__ hits, Queue next, Queue miss,
+              Queue hitl, Queue scat, Queue msq, int enable_medium, uint32_t *err, NrcHook hook,
+              PixelState ps) {
     int n = *rq.count;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 h = hits[i];
@@ -844,9 +848,11 @@ __global__ void k_shadow_resolve(Queue shadow, const uint8_t *__restrict__ occlu
 }
 
 // sampleMediumInteraction, medium.cpp:13-103 (the medium has no emission).
-__global__ void k_medium_sample(DevScene s, Queue msq, Queue next, Queue miss, Queue hitl,
-                                Queue scat, Queue mscat, PixelState ps, int max_depth,
-                                uint32_t *err) {
+// Three blocks of 256 per SM (at most 80 registers): the tracking loops are
+// latency-bound, and the extra warps outweigh a few spilled registers.
+__global__ void __launch_bounds__(kThreads, 3)
+k_medium_sample(DevScene s, Queue msq, Queue next, Queue miss, Queue hitl, Queue scat,
+                Queue mscat, PixelState ps, int max_depth, uint32_t *err) {
     int n = *msq.count;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 c0 = msq.at(0, i), c1 = msq.at(1, i), c2 = msq.at(2, i), c3 = msq.at(3, i);
@@ -1025,10 +1031,11 @@ __global__ void k_medium_scatter(DevScene s, Queue mscat, Queue next, Queue shad
 // traceTransmittance (wavefront.h:80-139) for every shadow ray when media
 // are enabled: closest hits through null-material interfaces with ratio
 // tracking inside media.
+// Three blocks per SM, as k_medium_sample.
 template <int FMT>
-__global__ void k_shadow_tr(DevScene s, const float4 *__restrict__ nodes,
-                            const float4 *__restrict__ tris, Queue shadow, PixelState ps,
-                            uint32_t *err, int *trace_err) {
+__global__ void __launch_bounds__(kThreads, 3)
+k_shadow_tr(DevScene s, const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
+            Queue shadow, PixelState ps, uint32_t *err, int *trace_err) {
     int n = *shadow.count;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 c0 = shadow.at(0, i), c1 = shadow.at(1, i), c2 = shadow.at(2, i), c3 = shadow.at(3, i),
@@ -1092,6 +1099,37 @@ __global__ void k_shadow_tr(DevScene s, const float4 *__restrict__ nodes,
         store_rng(ps, pixel, rng);
         if (any(T_ray))
             add_radiance(ps, pixel, f3(c2) * T_ray / mean(f3(c3) * pu + f3(c4) * pl));
+    }
+}
+
+// First pass of the transmittance shadow stage.  A shadow ray that starts
+// outside every medium and crosses no triangle at all (null-material
+// interfaces included) is the reference loop's first iteration ending with
+// `visible` and T_ray = pu = pl = 1, no sampler draw: its radiance is added
+// here with the same expression.  Every other ray (one that starts in a
+// medium, meets a surface or has a zero-length direction) is copied to
+// `tracked` for k_shadow_tr, so that the tracker's warps hold only the long
+// ratio-tracking loops.
+template <int FMT>
+__global__ void k_shadow_split(const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
+                               Queue shadow, Queue tracked, PixelState ps, uint32_t *err,
+                               int *trace_err) {
+    int n = *shadow.count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 c0 = shadow.at(0, i), c1 = shadow.at(1, i), c3 = shadow.at(3, i);
+        V3 d = f3(c1);
+        bool moving = fabsf(d.x) > kRayEps * 2 || fabsf(d.y) > kRayEps * 2 || fabsf(d.z) > kRayEps * 2;
+        if (sbits(c3.w) < 0 && moving) {
+            float4 h = traverse_ray<true, FMT, false>(nodes, tris, f3(c0), d, 0.f, c1.w, trace_err);
+            if (ubits(h.w) == KRR_MISS) {
+                float4 c2 = shadow.at(2, i), c4 = shadow.at(4, i);
+                add_radiance(ps, ubits(c2.w), f3(c2) * v3(1.f) / mean(f3(c3) * v3(1.f) + f3(c4) * v3(1.f)));
+                continue;
+            }
+        }
+        int j = push_slot(tracked.count, tracked.cap, err);
+        if (j < 0) continue;
+        for (int c = 0; c < kShadowCh; ++c) tracked.at(c, j) = shadow.at(c, i);
     }
 }
 
@@ -2332,15 +2370,26 @@ int launch_medium_scatter(krr_wf *wf, int depth, cudaStream_t st) {
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }
+// traceShadow with media (device.cu:102-128): unoccluded rays outside the
+// media are finished by k_shadow_split; the rest are staged in the
+// medium-sample queue's storage (consumed earlier in the bounce) with their
+// own counter and ratio-tracked by k_shadow_tr.
 int launch_trace_shadow_tr(krr_wf *wf, cudaStream_t st) {
-    if (wf->accel.node_format == 1)
+    static_assert(kMediumSampleCh >= kShadowCh, "tracked shadow rays need five planes");
+    Queue tracked{wf->qbuf[Q_MEDIUM_SAMPLE], (int32_t)wf->n, wf->shadow_tracked_count()};
+    KRR_CUDA(cudaMemsetAsync(tracked.count, 0, sizeof(int32_t), st));
+    int *terr = wf->accel.d_scratch + 4;
+    if (wf->accel.node_format == 1) {
+        k_shadow_split<1><<<wf->grid, kThreads, 0, st>>>(wf->accel.d_nodes, wf->accel.d_tris,
+                                                          wf->q(Q_SHADOW), tracked, wf->ps, wf->err(), terr);
         k_shadow_tr<1><<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris,
-                                                       wf->q(Q_SHADOW), wf->ps, wf->err(),
-                                                       wf->accel.d_scratch + 4);
-    else
+                                                       tracked, wf->ps, wf->err(), terr);
+    } else {
+        k_shadow_split<0><<<wf->grid, kThreads, 0, st>>>(wf->accel.d_nodes, wf->accel.d_tris,
+                                                          wf->q(Q_SHADOW), tracked, wf->ps, wf->err(), terr);
         k_shadow_tr<0><<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris,
-                                                       wf->q(Q_SHADOW), wf->ps, wf->err(),
-                                                       wf->accel.d_scratch + 4);
+                                                       tracked, wf->ps, wf->err(), terr);
+    }
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }
