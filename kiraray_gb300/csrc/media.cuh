@@ -29,11 +29,12 @@ __device__ __forceinline__ float half_to_float(uint16_t h) {
 
 // Density at world point p: trilinear interpolation with voxel centres at
 // integer index coordinates, zero outside the grid (NanoVDB's
-// SampleFromVoxels<1> on the index-space point worldToIndexF(p)).
+// SampleFromVoxels<1> on the index-space point worldToIndexF(p), an affine
+// map: offset, then a multiply by the voxels per unit length).
 __device__ __forceinline__ float density_at(const DevMedium &m, V3 p) {
-    float fx = (p.x - m.lo[0]) / (m.hi[0] - m.lo[0]) * (float)m.nx - 0.5f;
-    float fy = (p.y - m.lo[1]) / (m.hi[1] - m.lo[1]) * (float)m.ny - 0.5f;
-    float fz = (p.z - m.lo[2]) / (m.hi[2] - m.lo[2]) * (float)m.nz - 0.5f;
+    float fx = (p.x - m.lo[0]) * m.idx_scale[0] - 0.5f;
+    float fy = (p.y - m.lo[1]) * m.idx_scale[1] - 0.5f;
+    float fz = (p.z - m.lo[2]) * m.idx_scale[2] - 0.5f;
     float ix = floorf(fx), iy = floorf(fy), iz = floorf(fz);
     float u = fx - ix, v = fy - iy, w = fz - iz;
     int x0 = (int)ix, y0 = (int)iy, z0 = (int)iz;
@@ -51,6 +52,27 @@ __device__ __forceinline__ float density_at(const DevMedium &m, V3 p) {
     auto lerp = [](float a, float b, float t) { return a + t * (b - a); };
     return lerp(lerp(lerp(c[0][0][0], c[0][0][1], w), lerp(c[0][1][0], c[0][1][1], w), v),
                 lerp(lerp(c[1][0][0], c[1][0][1], w), lerp(c[1][1][0], c[1][1][1], w), v), u);
+}
+
+// Spectra of a grey medium keep three equal channels through the tracking
+// loops; an operation on such a spectrum is done once and broadcast, which
+// gives the same bits as three per-channel operations.
+__device__ __forceinline__ bool grey(V3 a) {
+    return __float_as_uint(a.x) == __float_as_uint(a.y) && __float_as_uint(a.y) == __float_as_uint(a.z);
+}
+__device__ __forceinline__ V3 div_g(V3 a, float b) {
+    if (grey(a)) {
+        float q = a.x / b;
+        return V3{q, q, q};
+    }
+    return a / b;
+}
+__device__ __forceinline__ V3 exp_g(V3 a) {
+    if (grey(a)) {
+        float e = expf(a.x);
+        return V3{e, e, e};
+    }
+    return vexp(a);
 }
 
 // Medium::samplePoint (media.h:121-126 homogeneous, :161-172 grid)
@@ -225,7 +247,7 @@ __device__ V3 sample_t_maj(const DevMedium &m, V3 o, V3 d, float tmax, Pcg &rng,
         if (get(seg.sigma_maj, ch) == 0.f) {
             float dt = seg.tmax - seg.tmin;
             if (isinf(dt)) dt = 3.402823466e38f;
-            T_maj *= vexp(-dt * seg.sigma_maj);
+            T_maj *= exp_g(-dt * seg.sigma_maj);
             continue;
         }
         float tmin = seg.tmin;
@@ -238,7 +260,7 @@ __device__ V3 sample_t_maj(const DevMedium &m, V3 o, V3 d, float tmax, Pcg &rng,
             float u = rng.get1d();
             float t = tmin + (-logf(1 - u) / get(seg.sigma_maj, ch));
             if (t < seg.tmax) {
-                T_maj *= vexp(-(t - tmin) * seg.sigma_maj);
+                T_maj *= exp_g(-(t - tmin) * seg.sigma_maj);
                 V3 p = o + d * t;
                 MediumProps mp = sample_point(m, p);
                 if (!cb(p, mp, seg.sigma_maj, T_maj)) return v3(1.f);
@@ -247,7 +269,7 @@ __device__ V3 sample_t_maj(const DevMedium &m, V3 o, V3 d, float tmax, Pcg &rng,
             } else {
                 float dt = seg.tmax - tmin;
                 if (isinf(dt)) dt = 3.402823466e38f;
-                T_maj *= vexp(-dt * seg.sigma_maj);
+                T_maj *= exp_g(-dt * seg.sigma_maj);
                 break;
             }
         }

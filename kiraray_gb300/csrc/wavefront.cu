@@ -880,8 +880,9 @@ k_medium_sample(DevScene s, Queue msq, Queue next, Queue miss, Queue hitl, Queue
                 }
                 if (mode == 1) {
                     float pr = get(Tm, ch) * get(mp.sigma_s, ch);
-                    thp *= Tm * mp.sigma_s / pr;
-                    pu *= Tm * mp.sigma_s / pr;
+                    V3 q = div_g(Tm * mp.sigma_s, pr);
+                    thp *= q;
+                    pu *= q;
                     if (any(thp) && any(pu)) {
                         int j = push_slot(mscat.count, mscat.cap, err);
                         if (j >= 0) {
@@ -896,16 +897,17 @@ k_medium_sample(DevScene s, Queue msq, Queue next, Queue miss, Queue hitl, Queue
                 }
                 V3 sigma_n = vmax(sigma_maj - mp.sigma_a - mp.sigma_s, v3(0.f));
                 float pr = get(Tm, ch) * get(sigma_n, ch);
-                thp *= Tm * sigma_n / pr;
+                V3 qn = div_g(Tm * sigma_n, pr);
+                thp *= qn;
                 if (pr == 0) thp = v3(0.f);
-                pu *= Tm * sigma_n / pr;
-                pl *= Tm * sigma_maj / pr;
+                pu *= qn;
+                pl *= div_g(Tm * sigma_maj, pr);
                 return any(thp) && any(pu);
             });
         if (aborted) thp = v3(0.f);
         store_rng(ps, pixel, rng);
         if (!scattered && any(thp)) {
-            V3 r = T_maj / get(T_maj, ch);
+            V3 r = div_g(T_maj, get(T_maj, ch));
             thp *= r;
             pu *= r;
             pl *= r;
@@ -1067,10 +1069,11 @@ k_shadow_tr(DevScene s, const float4 *__restrict__ nodes, const float4 *__restri
                     [&](V3, const MediumProps &mp, V3 sigma_maj, V3 Tm) -> bool {
                         V3 sigma_n = vmax(sigma_maj - mp.sigma_a - mp.sigma_s, v3(0.f));
                         float pr = get(Tm, ch) * get(sigma_maj, ch);
-                        T_ray *= Tm * sigma_n / pr;
-                        pl *= Tm * sigma_maj / pr;
-                        pu *= Tm * sigma_n / pr;
-                        V3 Tr = T_ray / mean(pu + pl);
+                        V3 qn = div_g(Tm * sigma_n, pr);
+                        T_ray *= qn;
+                        pl *= div_g(Tm * sigma_maj, pr);
+                        pu *= qn;
+                        V3 Tr = div_g(T_ray, mean(pu + pl));
                         if (max_coeff(Tr) < 0.05f) {
                             if (rng.get1d() < 0.75f) T_ray = v3(0.f);
                             else T_ray /= 0.25f;
@@ -1078,7 +1081,7 @@ k_shadow_tr(DevScene s, const float4 *__restrict__ nodes, const float4 *__restri
                         return any(T_ray);
                     });
                 if (aborted) T_ray = v3(0.f);
-                V3 r = T_maj / get(T_maj, ch);
+                V3 r = div_g(T_maj, get(T_maj, ch));
                 T_ray *= r;
                 pu *= r;
                 pl *= r;
@@ -1707,6 +1710,7 @@ extern "C" int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *sd, void *stre
             d.lo[k] = m.bounds_min[k]; d.hi[k] = m.bounds_max[k];
             d.sigma_t[k] = m.sigma_t[k]; d.albedo[k] = m.albedo[k];
             d.mres[k] = std::max(1, m.majorant_res[k]);
+            d.idx_scale[k] = (float)(k == 0 ? m.nx : k == 1 ? m.ny : m.nz) / (d.hi[k] - d.lo[k]);
         }
         d.g = m.g;
         d.scale = m.scale;

@@ -63,6 +63,7 @@ struct DevMedium {
     float scale;
     int32_t mres[3];
     const float *majorant;     // [mz][my][mx]
+    float idx_scale[3];        // n / (hi - lo) per axis: world to voxel index
 };
 
 struct DevScene {

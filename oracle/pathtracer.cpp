@@ -315,10 +315,12 @@ float half_to_float(uint16_t h) {
     return f;
 }
 
+// Index-space point: offset, then a multiply by the voxels per unit length
+// (an affine world-to-index map, as NanoVDB's worldToIndexF).
 float density_at(const Medium &m, V3 p) {
-    float fx = (p.x - m.lo[0]) / (m.hi[0] - m.lo[0]) * (float)m.nx - 0.5f;
-    float fy = (p.y - m.lo[1]) / (m.hi[1] - m.lo[1]) * (float)m.ny - 0.5f;
-    float fz = (p.z - m.lo[2]) / (m.hi[2] - m.lo[2]) * (float)m.nz - 0.5f;
+    float fx = (p.x - m.lo[0]) * ((float)m.nx / (m.hi[0] - m.lo[0])) - 0.5f;
+    float fy = (p.y - m.lo[1]) * ((float)m.ny / (m.hi[1] - m.lo[1])) - 0.5f;
+    float fz = (p.z - m.lo[2]) * ((float)m.nz / (m.hi[2] - m.lo[2])) - 0.5f;
     float ix = std::floor(fx), iy = std::floor(fy), iz = std::floor(fz);
     float u = fx - ix, v = fy - iy, w = fz - iz;
     int x0 = (int)ix, y0 = (int)iy, z0 = (int)iz;
