@@ -140,36 +140,60 @@ __global__ void k_pack_weights(const __nv_bfloat16 *__restrict__ w, NrcMlp mlp, 
     }
 }
 
+// Hash-grid encoding of one query row.  The table gathers are the latency
+// of the whole kernel, so the levels go in groups of four: the 32 corner
+// loads of a group are issued before any of them is used (levels at or
+// beyond g.levels load entry 0 and are discarded), which turns sixteen
+// dependent round trips into four.  Per level the corner weights and the
+// accumulation order are those of the CUDA-core encoder (nrc.cu).
+constexpr int kEncGroup = 4;
+
 __device__ __forceinline__ void encode_row(const NrcGrid &g, const float *q,
                                            const __nv_bfloat16 *__restrict__ table, float *x) {
     float p[3];
     for (int a = 0; a < 3; ++a) p[a] = fminf(fmaxf((q[a] - g.lo[a]) * g.inv_extent[a], 0.f), 1.f);
-    for (int l = 0; l < kNrcMaxLevels; ++l) {
-        if (l >= g.levels) break;
-        float fr[3];
-        uint32_t base[3];
-        for (int a = 0; a < 3; ++a) {
-            float s = p[a] * (float)g.res[l];
-            float fl = fminf(fmaxf(floorf(s), 0.f), (float)(g.res[l] - 1));
-            base[a] = (uint32_t)fl;
-            fr[a] = fminf(fmaxf(s - fl, 0.f), 1.f);
+#pragma unroll 1
+    for (int l0 = 0; l0 < kNrcMaxLevels; l0 += kEncGroup) {
+        if (l0 >= g.levels) break;
+        __nv_bfloat162 v[kEncGroup][8];
+        float fr[kEncGroup][3];
+#pragma unroll
+        for (int j = 0; j < kEncGroup; ++j) {
+            const int l = l0 + j;
+            const bool valid = l < g.levels;
+            uint32_t base[3];
+            for (int a = 0; a < 3; ++a) {
+                float s = p[a] * (float)g.res[l];
+                float fl = fminf(fmaxf(floorf(s), 0.f), (float)(g.res[l] - 1));
+                base[a] = (uint32_t)fl;
+                fr[j][a] = fminf(fmaxf(s - fl, 0.f), 1.f);
+            }
+            uint32_t n1 = (uint32_t)g.res[l] + 1u;
+            bool dense = g.dense_mask & (1u << l);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                uint32_t xx = base[0] + (k & 1), yy = base[1] + ((k >> 1) & 1), zz = base[2] + ((k >> 2) & 1);
+                uint32_t idx = dense ? xx + n1 * (yy + n1 * zz)
+                                     : (xx ^ (yy * 2654435761u) ^ (zz * 805459861u)) & (g.table_size - 1u);
+                idx = valid ? idx + g.offset[l] : 0u;
+                v[j][k] = *reinterpret_cast<const __nv_bfloat162 *>(table + 2 * (size_t)idx);
+            }
         }
-        uint32_t n1 = (uint32_t)g.res[l] + 1u;
-        bool dense = g.dense_mask & (1u << l);
-        float f0 = 0.f, f1 = 0.f;
-        for (int k = 0; k < 8; ++k) {
-            uint32_t xx = base[0] + (k & 1), yy = base[1] + ((k >> 1) & 1), zz = base[2] + ((k >> 2) & 1);
-            uint32_t idx = dense ? xx + n1 * (yy + n1 * zz)
-                                 : (xx ^ (yy * 2654435761u) ^ (zz * 805459861u)) & (g.table_size - 1u);
-            idx += g.offset[l];
-            float w = ((k & 1) ? fr[0] : 1.f - fr[0]) * (((k >> 1) & 1) ? fr[1] : 1.f - fr[1]) *
-                      (((k >> 2) & 1) ? fr[2] : 1.f - fr[2]);
-            __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162 *>(table + 2 * (size_t)idx);
-            f0 += w * __bfloat162float(v.x);
-            f1 += w * __bfloat162float(v.y);
+#pragma unroll
+        for (int j = 0; j < kEncGroup; ++j) {
+            if (l0 + j >= g.levels) break;
+            float f0 = 0.f, f1 = 0.f;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                float w = ((k & 1) ? fr[j][0] : 1.f - fr[j][0]) *
+                          (((k >> 1) & 1) ? fr[j][1] : 1.f - fr[j][1]) *
+                          (((k >> 2) & 1) ? fr[j][2] : 1.f - fr[j][2]);
+                f0 += w * __bfloat162float(v[j][k].x);
+                f1 += w * __bfloat162float(v[j][k].y);
+            }
+            x[2 * (l0 + j)] = f0;
+            x[2 * (l0 + j) + 1] = f1;
         }
-        x[2 * l] = f0;
-        x[2 * l + 1] = f1;
     }
     int o = 2 * g.levels;
     nrc_encode_extras(q, x + o);
