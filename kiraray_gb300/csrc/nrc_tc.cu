@@ -594,8 +594,16 @@ int nrc_forward_tc(const NrcGrid &g, const NrcMlp &mlp, const float *d_in, const
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // as many CTAs as fit on an SM (registers and shared memory allow three;
+    // their 3 x 64 tensor-memory columns fit in 512): the hash gathers of one
+    // CTA's tile overlap the MMA chains of the others
+    static int per_sm = 0;
+    if (!per_sm) {
+        KRR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_nrc_forward_tc, kTcThreads, smem));
+        per_sm = std::max(1, std::min(per_sm, (int)(512 / kTcCols)));
+    }
     int64_t tiles = (cap + kTcRows - 1) / kTcRows;
-    int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sms * 2));
+    int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sms * per_sm));
     k_nrc_forward_tc<<<grid, kTcThreads, smem, s>>>(g, mlp.layers, d_in, d_count, cap, table, packed,
                                                     d_out, acts, err);
     KRR_CUDA(cudaGetLastError());
