@@ -183,7 +183,7 @@ STAGE_BYTES = {
     "trace_closest": 112 + 16 + 16 + 128,   # ray read, hit write+read, one push (BVH bytes apart)
     "handle_hit": 128 + 32,                 # hit-light item, L RMW
     "handle_miss": 112 + 32,                # miss item, L RMW
-    "scatter": 128 + 32 + 80 + 112,         # scatter item, sampler RMW, shadow + ray push
+    "scatter": 128 + 32 + 80 + 112 + 8,     # scatter item, sampler RMW, shadow + ray push, index list
     "trace_shadow": 80 + 1 + 80 + 1 + 32,   # any-hit read/write, resolve read, L RMW
 }
 

@@ -87,9 +87,11 @@ struct krr_wf {
     // queues and pixel state
     float4 *qbuf[Q_COUNT] = {};
     int32_t *d_counts = nullptr;   // [0..7] queue sizes, [8] error flags, [9-10] cache
-                                   // batches, [11] ratio-tracked shadow rays
+                                   // batches, [11] ratio-tracked shadow rays, [12-15]
+                                   // scatter items per material class
     float4 *hits = nullptr;
     uint8_t *occluded = nullptr;
+    int32_t *scatter_lists = nullptr;   // [2][n] scatter items by material class
     PixelState ps{};
     int grid = 0;
     // view table (pinned host copy, device copy) and per-frame constants
@@ -115,6 +117,7 @@ struct krr_wf {
     int32_t *nrc_q_count() const { return d_counts + 9; }
     int32_t *nrc_b_count() const { return d_counts + 10; }
     int32_t *shadow_tracked_count() const { return d_counts + 11; }
+    int32_t *scatter_class_counts() const { return d_counts + 12; }
     uint32_t *err() const { return reinterpret_cast<uint32_t *>(d_counts + 8); }
     WfConst consts() const {
         WfConst c;
@@ -764,76 +767,51 @@ __device__ __forceinline__ void scatter_item(const DevScene &s, const Queue &sca
     }
 }
 
-constexpr int kScatterThreads = 256;
-constexpr int kScatterPerThread = 4;
-constexpr int kScatterTile = kScatterThreads * kScatterPerThread;
+// generateScatterRays (integrator.cpp:110-164) as two launches over the whole
+// queue.  The first draws every item's Russian roulette (integrator.cpp:
+// 116-118; an ended path stores its sampler and stops) and appends each
+// survivor to the index list of its material class, warp-aggregated: classes
+// 0 and 1 fill `lists[0..n)` from the front and from the back, classes 2 and
+// 3 fill `lists[n..2n)` likewise.  The second walks the four lists in class
+// order with no block barrier, so that a warp runs one BSDF except at the
+// three class boundaries.  Every item is computed exactly as alone (its
+// sampler stream is its pixel's); only the order of the queue pushes changes.
+__global__ void k_scatter_classify(DevScene s, Queue scat, PixelState ps, float rr,
+                                   int32_t *__restrict__ lists, int32_t *__restrict__ counts) {
+    const int cap = scat.cap, n = min(*scat.count, cap);
+    const int lane = threadIdx.x & 31;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t pixel = ubits(scat.at(2, i).w);
+        Pcg rng = load_rng(ps, pixel);
+        if (rng.get1d() >= rr) {
+            store_rng(ps, pixel, rng);   // the path ends here
+            continue;
+        }
+        const int cls = min(max(s.materials[sbits(scat.at(0, i).w)].type, 0), 3);
+        const unsigned peers = __match_any_sync(__activemask(), cls);
+        const int leader = __ffs(peers) - 1;
+        int slot = 0;
+        if (lane == leader) slot = atomicAdd(&counts[cls], __popc(peers));
+        slot = __shfl_sync(peers, slot, leader) + __popc(peers & ((1u << lane) - 1u));
+        int32_t *list = lists + (cls >> 1) * (size_t)cap;
+        list[(cls & 1) ? cap - 1 - slot : slot] = i;
+    }
+}
 
-// generateScatterRays, integrator.cpp:110-164.  Each block takes a tile of
-// 1024 items, draws their Russian roulette, and regroups the survivors by
-// material type in shared memory before shading, so that a warp runs one
-// BSDF; warps take the sorted tile in 32-item chunks interleaved across the
-// tile (warp w: chunks w, w + 8, ...) so that every warp gets a similar mix of
-// cheap and expensive materials between two block barriers.  Every item is
-// computed exactly as alone (its sampler stream is its pixel's); only the
-// order of the queue pushes changes.
-__global__ void __launch_bounds__(kScatterThreads, 4)
-k_scatter(DevScene s, Queue scat, Queue next, Queue shadow, PixelState ps, int nee, float rr,
-          uint32_t *err) {
-    __shared__ int sh_count[5];                  // material types 0..3, 4 = ended by RR
-    __shared__ int sh_base[5];
-    __shared__ uint16_t sh_item[kScatterTile];
-    const int n = *scat.count;
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    // items per thread and tile: up to 4, fewer when the queue is short so
-    // that every block still gets work
-    const int64_t span = (int64_t)gridDim.x * kScatterThreads;
-    const int64_t want = (n + span - 1) / span;
-    const int per = want < 1 ? 1 : (want > kScatterPerThread ? kScatterPerThread : (int)want);
-    const int tile = per * kScatterThreads;
-    for (int base = blockIdx.x * tile; base < n; base += gridDim.x * tile) {
-        if (t < 5) sh_count[t] = 0;
-        __syncthreads();
-        int cls[kScatterPerThread], rank[kScatterPerThread];
-#pragma unroll
-        for (int k = 0; k < kScatterPerThread; ++k) {
-            const int i = base + k * kScatterThreads + t;
-            cls[k] = -1;
-            if (k < per && i < n) {
-                const uint32_t pixel = ubits(scat.at(2, i).w);
-                Pcg rng = load_rng(ps, pixel);
-                if (rng.get1d() >= rr) {
-                    store_rng(ps, pixel, rng);   // the path ends here
-                    cls[k] = 4;
-                } else {
-                    cls[k] = min(max(s.materials[sbits(scat.at(0, i).w)].type, 0), 3);
-                }
-            }
-            rank[k] = cls[k] >= 0 ? atomicAdd(&sh_count[cls[k]], 1) : 0;
-        }
-        __syncthreads();
-        if (t == 0) {
-            int acc = 0;
-            for (int k = 0; k < 5; ++k) {
-                sh_base[k] = acc;
-                acc += sh_count[k];
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < kScatterPerThread; ++k)
-            if (cls[k] >= 0 && cls[k] < 4) sh_item[sh_base[cls[k]] + rank[k]] = (uint16_t)(k * kScatterThreads + t);
-        __syncthreads();
-        const int live = sh_base[4];
-        for (int c = warp; c * 32 < live; c += kScatterThreads / 32) {
-            const int slot = c * 32 + lane;
-            if (slot < live) {
-                const int i = base + sh_item[slot];
-                Pcg rng = load_rng(ps, ubits(scat.at(2, i).w));
-                rng.get1d();   // the roulette draw taken above
-                scatter_item(s, scat, i, rng, next, shadow, ps, nee, rr, err);
-            }
-        }
-        __syncthreads();
+__global__ void __launch_bounds__(kThreads, 4)
+k_scatter_process(DevScene s, Queue scat, const int32_t *__restrict__ lists,
+                  const int32_t *__restrict__ counts, Queue next, Queue shadow, PixelState ps,
+                  int nee, float rr, uint32_t *err) {
+    const int cap = scat.cap;
+    const int c0 = counts[0], c01 = c0 + counts[1], c012 = c01 + counts[2], total = c012 + counts[3];
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const int i = g < c0 ? lists[g]
+                    : g < c01 ? lists[cap - 1 - (g - c0)]
+                    : g < c012 ? lists[cap + (g - c01)]
+                    : lists[2 * (size_t)cap - 1 - (g - c012)];
+        Pcg rng = load_rng(ps, ubits(scat.at(2, i).w));
+        rng.get1d();   // the roulette draw taken by k_scatter_classify
+        scatter_item(s, scat, i, rng, next, shadow, ps, nee, rr, err);
     }
 }
 
@@ -1414,6 +1392,7 @@ void free_queues(krr_wf *wf) {
     cudaFree(wf->d_counts); wf->d_counts = nullptr;
     cudaFree(wf->hits); wf->hits = nullptr;
     cudaFree(wf->occluded); wf->occluded = nullptr;
+    cudaFree(wf->scatter_lists); wf->scatter_lists = nullptr;
     cudaFree(wf->ps.L); cudaFree(wf->ps.pixel); cudaFree(wf->ps.rng);
     wf->ps = PixelState{};
 }
@@ -1768,6 +1747,7 @@ static int set_layout(krr_wf *wf, std::vector<DevView> layout) {
     KRR_CUDA(cudaMemset(wf->d_counts, 0, 16 * sizeof(int32_t)));
     KRR_CUDA(cudaMalloc(&wf->hits, wf->n * sizeof(float4)));
     KRR_CUDA(cudaMalloc(&wf->occluded, wf->n));
+    KRR_CUDA(cudaMalloc(&wf->scatter_lists, 2 * wf->n * sizeof(int32_t)));
     KRR_CUDA(cudaMalloc(&wf->ps.L, wf->n * sizeof(float4)));
     KRR_CUDA(cudaMalloc(&wf->ps.pixel, wf->n * sizeof(float4)));
     KRR_CUDA(cudaMalloc(&wf->ps.rng, wf->n * sizeof(ulonglong2)));
@@ -2029,9 +2009,15 @@ extern "C" int krr_wf_handle_miss(krr_wf *wf, void *stream) {
 extern "C" int krr_wf_generate_scatter_rays(krr_wf *wf, int32_t depth, void *stream) {
     KRR_TRY(ready(wf));
     int cur = depth & 1;
-    k_scatter<<<wf->grid, kThreads, 0, as_stream(stream)>>>(wf->scene, wf->q(Q_SCATTER),
-                                                            wf->q(cur ^ 1), wf->q(Q_SHADOW), wf->ps,
-                                                            wf->params.nee, wf->params.rr, wf->err());
+    cudaStream_t st = as_stream(stream);
+    KRR_CUDA(cudaMemsetAsync(wf->scatter_class_counts(), 0, 4 * sizeof(int32_t), st));
+    k_scatter_classify<<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->q(Q_SCATTER), wf->ps,
+                                                      wf->params.rr, wf->scatter_lists,
+                                                      wf->scatter_class_counts());
+    k_scatter_process<<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->q(Q_SCATTER), wf->scatter_lists,
+                                                     wf->scatter_class_counts(), wf->q(cur ^ 1),
+                                                     wf->q(Q_SHADOW), wf->ps, wf->params.nee,
+                                                     wf->params.rr, wf->err());
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }
