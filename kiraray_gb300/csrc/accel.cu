@@ -625,10 +625,19 @@ void accel_free(krr_accel *a) {
     cudaFree(a->d_tris);
     cudaFree(a->d_leaf_of_prim);
     cudaFree(a->d_scratch);
+    cudaFree(a->stage_rays);
+    cudaFree(a->stage_hits);
+    if (a->stage_aux) cudaStreamDestroy(a->stage_aux);
+    for (cudaEvent_t &e : a->stage_ev)
+        if (e) cudaEventDestroy(e);
     a->d_nodes = nullptr;
     a->d_tris = nullptr;
     a->d_leaf_of_prim = nullptr;
     a->d_scratch = nullptr;
+    a->stage_rays = a->stage_hits = nullptr;
+    a->stage_cap = 0;
+    a->stage_aux = nullptr;
+    a->stage_ev[0] = a->stage_ev[1] = nullptr;
 }
 
 namespace {
@@ -936,48 +945,56 @@ extern "C" int krr_accel_trace_closest_host(const krr_accel *a, const krr_ray *h
     KRR_CHECK_ARG(n >= 0, "negative ray count");
     if (n == 0) return KRR_OK;
     if (!a->d_scratch) return fail(KRR_ERR_NOT_READY, "acceleration structure not built");
+    // the staging buffers, stream and events are cached on the handle (the
+    // handle is not const in storage; callers already may not trace on one
+    // handle from two threads at once, since the work counters are shared)
+    krr_accel *m = const_cast<krr_accel *>(a);
     cudaStream_t s = as_stream(stream);
-    cudaStream_t aux = nullptr;
-    cudaEvent_t ev_start = nullptr, ev_done = nullptr;
-    krr_ray *d_rays = nullptr;
-    krr_hit *d_hits = nullptr;
+    if (!m->stage_aux) {
+        KRR_CUDA(cudaStreamCreateWithFlags(&m->stage_aux, cudaStreamNonBlocking));
+        KRR_CUDA(cudaEventCreateWithFlags(&m->stage_ev[0], cudaEventDisableTiming));
+        KRR_CUDA(cudaEventCreateWithFlags(&m->stage_ev[1], cudaEventDisableTiming));
+    }
+    if (m->stage_cap < n) {
+        KRR_CUDA(cudaStreamSynchronize(s));
+        cudaFree(m->stage_rays);
+        cudaFree(m->stage_hits);
+        m->stage_rays = m->stage_hits = nullptr;
+        m->stage_cap = 0;
+        KRR_CUDA(cudaMalloc(&m->stage_rays, (size_t)n * sizeof(krr_ray)));
+        KRR_CUDA(cudaMalloc(&m->stage_hits, (size_t)n * sizeof(krr_hit)));
+        m->stage_cap = n;
+    }
+    static_assert(sizeof(krr_ray) == 2 * sizeof(float4) && sizeof(krr_hit) == sizeof(float4),
+                  "ray and hit records");
+    krr_ray *d_rays = reinterpret_cast<krr_ray *>(m->stage_rays);
+    krr_hit *d_hits = reinterpret_cast<krr_hit *>(m->stage_hits);
+    cudaStream_t aux = m->stage_aux;
     int st = KRR_OK;
     auto check = [&](cudaError_t e, const char *what) {
         if (st == KRR_OK && e != cudaSuccess) st = cuda_status(e, what, __FILE__, __LINE__);
     };
-    check(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking), "cudaStreamCreate");
-    check(cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming), "cudaEventCreate");
-    check(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming), "cudaEventCreate");
-    check(cudaMallocAsync(&d_rays, n * sizeof(krr_ray), s), "cudaMallocAsync");
-    check(cudaMallocAsync(&d_hits, n * sizeof(krr_hit), s), "cudaMallocAsync");
-    check(cudaEventRecord(ev_start, s), "cudaEventRecord");
-    check(cudaStreamWaitEvent(aux, ev_start, 0), "cudaStreamWaitEvent");
+    check(cudaEventRecord(m->stage_ev[0], s), "cudaEventRecord");
+    check(cudaStreamWaitEvent(aux, m->stage_ev[0], 0), "cudaStreamWaitEvent");
     const int64_t chunk = std::max<int64_t>(int64_t(1) << 18, (n + 3) / 4);
     int k = 0;
     for (int64_t off = 0; off < n && st == KRR_OK; off += chunk, ++k) {
-        const int64_t m = std::min(chunk, n - off);
+        const int64_t c = std::min(chunk, n - off);
         cudaStream_t sk = (k & 1) ? aux : s;
-        check(cudaMemcpyAsync(d_rays + off, h_rays + off, m * sizeof(krr_ray), cudaMemcpyHostToDevice, sk),
+        check(cudaMemcpyAsync(d_rays + off, h_rays + off, c * sizeof(krr_ray), cudaMemcpyHostToDevice, sk),
               "cudaMemcpyAsync");
         if (st != KRR_OK) break;
-        TraceLaunch l = aos_launch(a, d_rays + off, m);
+        TraceLaunch l = aos_launch(a, d_rays + off, c);
         l.hits = reinterpret_cast<float4 *>(d_hits + off);
         l.counter = a->d_scratch + ((k & 1) ? 8 : 0);
         st = launch_trace_closest(a, l, sk);
         if (st != KRR_OK) break;
-        check(cudaMemcpyAsync(h_hits + off, d_hits + off, m * sizeof(krr_hit), cudaMemcpyDeviceToHost, sk),
+        check(cudaMemcpyAsync(h_hits + off, d_hits + off, c * sizeof(krr_hit), cudaMemcpyDeviceToHost, sk),
               "cudaMemcpyAsync");
     }
-    if (ev_done && aux) {
-        cudaEventRecord(ev_done, aux);
-        cudaStreamWaitEvent(s, ev_done, 0);
-    }
-    if (d_rays) cudaFreeAsync(d_rays, s);
-    if (d_hits) cudaFreeAsync(d_hits, s);
+    cudaEventRecord(m->stage_ev[1], aux);
+    cudaStreamWaitEvent(s, m->stage_ev[1], 0);
     check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
-    if (aux) cudaStreamDestroy(aux);
-    if (ev_start) cudaEventDestroy(ev_start);
-    if (ev_done) cudaEventDestroy(ev_done);
     return st;
 }
 

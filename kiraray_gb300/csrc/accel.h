@@ -47,6 +47,14 @@ struct krr_accel {
     int postpone_pct = 0;
     int node_format = 0;         // 0 compressed (80 B), 1 float (224 B)
     int max_leaf = 1;            // triangles per leaf child (1..3)
+    // host-buffer entry point (krr_accel_trace_closest_host): device staging
+    // for rays (2 float4 each) and hits, grown on demand, and a second stream
+    // with two events, kept across calls so that a call allocates nothing
+    float4 *stage_rays = nullptr;
+    float4 *stage_hits = nullptr;
+    int64_t stage_cap = 0;
+    cudaStream_t stage_aux = nullptr;
+    cudaEvent_t stage_ev[2] = {nullptr, nullptr};
 };
 
 namespace krr {
