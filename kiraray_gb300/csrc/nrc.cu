@@ -315,9 +315,28 @@ __device__ __forceinline__ float adam_one(const AdamArgs &a, float g, float &m, 
 }
 
 // Adam over n parameters (FP32 masters w, moments m and v, gradient grad which
-// is cleared, BF16 copy wb).  Streams four parameters per thread and step with
-// 16-byte accesses and every load issued before the arithmetic (the kernel is
-// bound by HBM bandwidth: 34 bytes per parameter).
+// is cleared, BF16 copy wb).  A thread streams two groups of four parameters
+// per step (16-byte accesses, all eight loads issued before the arithmetic):
+// the kernel is bound by HBM bandwidth, 34 bytes per parameter.
+__device__ __forceinline__ void adam4(const AdamArgs &a, float4 g, float4 &mm, float4 &vv, float4 &ww) {
+    ww.x = adam_one(a, g.x, mm.x, vv.x, ww.x);
+    ww.y = adam_one(a, g.y, mm.y, vv.y, ww.y);
+    ww.z = adam_one(a, g.z, mm.z, vv.z, ww.z);
+    ww.w = adam_one(a, g.w, mm.w, vv.w, ww.w);
+}
+
+__device__ __forceinline__ void adam_store4(float *m, float *v, float *w, float *grad,
+                                            __nv_bfloat16 *wb, int64_t i, float4 mm, float4 vv,
+                                            float4 ww) {
+    reinterpret_cast<float4 *>(grad)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    reinterpret_cast<float4 *>(m)[i] = mm;
+    reinterpret_cast<float4 *>(v)[i] = vv;
+    reinterpret_cast<float4 *>(w)[i] = ww;
+    __nv_bfloat162 lo = __floats2bfloat162_rn(ww.x, ww.y), hi = __floats2bfloat162_rn(ww.z, ww.w);
+    reinterpret_cast<uint2 *>(wb)[i] =
+        make_uint2(*reinterpret_cast<uint32_t *>(&lo), *reinterpret_cast<uint32_t *>(&hi));
+}
+
 __global__ void k_adam(float *__restrict__ w, float *__restrict__ m, float *__restrict__ v,
                        float *__restrict__ grad, __nv_bfloat16 *__restrict__ wb, int64_t n, float lr,
                        float b1, float b2, float eps, float grad_scale, const int64_t *__restrict__ step) {
@@ -325,22 +344,26 @@ __global__ void k_adam(float *__restrict__ w, float *__restrict__ m, float *__re
                reinterpret_cast<const float *>(step + 1)[1]};
     const int64_t n4 = n >> 2;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += stride) {
-        float4 g = reinterpret_cast<const float4 *>(grad)[i];
-        float4 mm = reinterpret_cast<const float4 *>(m)[i];
-        float4 vv = reinterpret_cast<const float4 *>(v)[i];
-        float4 ww = reinterpret_cast<const float4 *>(w)[i];
-        reinterpret_cast<float4 *>(grad)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        ww.x = adam_one(a, g.x, mm.x, vv.x, ww.x);
-        ww.y = adam_one(a, g.y, mm.y, vv.y, ww.y);
-        ww.z = adam_one(a, g.z, mm.z, vv.z, ww.z);
-        ww.w = adam_one(a, g.w, mm.w, vv.w, ww.w);
-        reinterpret_cast<float4 *>(m)[i] = mm;
-        reinterpret_cast<float4 *>(v)[i] = vv;
-        reinterpret_cast<float4 *>(w)[i] = ww;
-        __nv_bfloat162 lo = __floats2bfloat162_rn(ww.x, ww.y), hi = __floats2bfloat162_rn(ww.z, ww.w);
-        uint2 packed = make_uint2(*reinterpret_cast<uint32_t *>(&lo), *reinterpret_cast<uint32_t *>(&hi));
-        reinterpret_cast<uint2 *>(wb)[i] = packed;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += 2 * stride) {
+        const int64_t j = i + stride;
+        const bool two = j < n4;
+        float4 g0 = reinterpret_cast<const float4 *>(grad)[i];
+        float4 m0 = reinterpret_cast<const float4 *>(m)[i];
+        float4 v0 = reinterpret_cast<const float4 *>(v)[i];
+        float4 w0 = reinterpret_cast<const float4 *>(w)[i];
+        float4 g1{}, m1{}, v1{}, w1{};
+        if (two) {
+            g1 = reinterpret_cast<const float4 *>(grad)[j];
+            m1 = reinterpret_cast<const float4 *>(m)[j];
+            v1 = reinterpret_cast<const float4 *>(v)[j];
+            w1 = reinterpret_cast<const float4 *>(w)[j];
+        }
+        adam4(a, g0, m0, v0, w0);
+        adam_store4(m, v, w, grad, wb, i, m0, v0, w0);
+        if (two) {
+            adam4(a, g1, m1, v1, w1);
+            adam_store4(m, v, w, grad, wb, j, m1, v1, w1);
+        }
     }
     for (int64_t i = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
         float g = grad[i], mm = m[i], vv = v[i];
