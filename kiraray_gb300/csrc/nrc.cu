@@ -282,10 +282,10 @@ __global__ void k_encode_bwd(NrcGrid g, const float *__restrict__ in, const floa
             if (d0 == 0.f && d1 == 0.f) continue;
             Corner c;
             corners(g, l, p, c);
-            for (int k = 0; k < 8; ++k) {
-                atomicAdd(tgrad + 2 * (size_t)c.idx[k], c.w[k] * d0);
-                atomicAdd(tgrad + 2 * (size_t)c.idx[k] + 1, c.w[k] * d1);
-            }
+            // one 8-byte vector atomic per corner (both features of the entry)
+            for (int k = 0; k < 8; ++k)
+                atomicAdd(reinterpret_cast<float2 *>(tgrad) + c.idx[k],
+                          make_float2(c.w[k] * d0, c.w[k] * d1));
         }
     }
 }
