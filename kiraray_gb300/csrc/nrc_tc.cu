@@ -128,6 +128,19 @@ __device__ __forceinline__ void store_row(uint8_t *tile, uint32_t r, const float
     }
 }
 
+// Copies the rows < n of a canonical 128x64 BF16 tile to a row-major global
+// array (16-byte chunks; eight consecutive threads write one 128-byte row, so
+// a warp writes four whole rows per instruction).
+__device__ __forceinline__ void dump_tile(const uint8_t *tile, __nv_bfloat16 *dst, int64_t row0,
+                                          int64_t n) {
+    for (int c = threadIdx.x; c < kTcRows * 8; c += blockDim.x) {
+        const int r = c >> 3, j = c & 7;
+        if (row0 + r < n)
+            reinterpret_cast<uint4 *>(dst + (row0 + r) * kNrcIn)[j] =
+                *reinterpret_cast<const uint4 *>(tile + canon((uint32_t)r, (uint32_t)(8 * j)));
+    }
+}
+
 // Packs the BF16 weights [layer][out][64] into canonical tiles.
 __global__ void k_pack_weights(const __nv_bfloat16 *__restrict__ w, NrcMlp mlp, uint8_t *packed) {
     int total = mlp.n_params;
@@ -247,15 +260,16 @@ k_nrc_forward_tc(NrcGrid g, int layers, const float *__restrict__ in, const int3
         else
             for (int k = 0; k < kNrcIn; ++k) x[k] = 0.f;
         store_row(sa, (uint32_t)tid, x);
-        if (acts && row < n) {
-            for (int k = 0; k < kNrcIn; ++k) acts[row * kNrcIn + k] = __float2bfloat16_rn(x[k]);
-        }
         fence_proxy_async();
         fence_before_sync();
         __syncthreads();
         for (int l = 0; l < layers; ++l) {
             const bool last = l + 1 == layers;
             const int nrows = last ? kNrcOutPad : kNrcWidth;
+            // the tile holds this layer's input X_l, complete since the last
+            // barrier: dump it for the backward pass while the MMAs read it
+            // (it is overwritten only after the accumulator wait's barrier)
+            if (acts) dump_tile(sa, acts + (size_t)l * cap * kNrcIn, t * kTcRows, n);
             if (tid == 0) {
                 fence_after_sync();
                 const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sw + l * kLayerBytes);
@@ -298,10 +312,6 @@ k_nrc_forward_tc(NrcGrid g, int layers, const float *__restrict__ in, const int3
             if (!last) {
                 for (int k = 0; k < kNrcIn; ++k) v[k] = fmaxf(v[k], 0.f);
                 store_row(sa, (uint32_t)tid, v);
-                if (acts && row < n) {
-                    __nv_bfloat16 *dst = acts + ((size_t)(l + 1) * cap + row) * kNrcIn;
-                    for (int k = 0; k < kNrcIn; ++k) dst[k] = __float2bfloat16_rn(v[k]);
-                }
                 fence_proxy_async();
             } else if (row < n) {
                 out[row * kNrcOutPad + 0] = v[0];
