@@ -1933,8 +1933,19 @@ static TraceLaunch closest_launch(krr_wf *wf, int depth) {
 }
 
 // Routing of the closest hits of ray queue `depth` (already traced into
-// wf->hits when `traced`).
-static int closest_stage(krr_wf *wf, int depth, cudaStream_t st, bool traced) {
+// wf->hits when `traced`).  With a cache attached, the paths that stop at it
+// are evaluated and their radiance added here, or, with `defer_cache`, left in
+// the query buffer for one evaluation at the end of the sample (render()).
+// L[pixel] += throughput x cache(query) for the queued cache queries.
+static int nrc_evaluate_queries(krr_wf *wf, cudaStream_t st) {
+    KRR_TRY(nrc_query_device(wf->nrc, wf->nrc_q_in, wf->nrc_q_count(), wf->n, wf->nrc_q_out, st));
+    k_nrc_apply<<<wf->grid, kThreads, 0, st>>>(wf->nrc_q_out, wf->nrc_q_meta, wf->nrc_q_count(), wf->ps);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
+}
+
+static int closest_stage(krr_wf *wf, int depth, cudaStream_t st, bool traced,
+                         bool defer_cache = false) {
     int cur = depth & 1;
     Queue rq = wf->q(cur);
     if (!traced) KRR_TRY(launch_trace_closest(&wf->accel, closest_launch(wf, depth), st));
@@ -1952,18 +1963,14 @@ static int closest_stage(krr_wf *wf, int depth, cudaStream_t st, bool traced) {
         hook.rec_max = wf->nrc_rec_max;
         hook.spread = wf->nrc_spread;
         hook.spread_c = nrc_termination_spread(wf->nrc);
-        KRR_CUDA(cudaMemsetAsync(wf->nrc_q_count(), 0, sizeof(int32_t), st));
+        if (!defer_cache) KRR_CUDA(cudaMemsetAsync(wf->nrc_q_count(), 0, sizeof(int32_t), st));
     }
     k_hit_process<<<wf->grid, kThreads, 0, st>>>(wf->scene, rq, wf->hits, wf->q(cur ^ 1),
                                                   wf->q(Q_MISS), wf->q(Q_HIT_LIGHT), wf->q(Q_SCATTER),
                                                   wf->q(Q_MEDIUM_SAMPLE), wf->medium ? 1 : 0, wf->err(),
                                                   hook, wf->ps);
     KRR_CUDA(cudaGetLastError());
-    if (wf->nrc) {
-        KRR_TRY(nrc_query_device(wf->nrc, wf->nrc_q_in, wf->nrc_q_count(), wf->n, wf->nrc_q_out, st));
-        k_nrc_apply<<<wf->grid, kThreads, 0, st>>>(wf->nrc_q_out, wf->nrc_q_meta, wf->nrc_q_count(), wf->ps);
-        KRR_CUDA(cudaGetLastError());
-    }
+    if (wf->nrc && !defer_cache) KRR_TRY(nrc_evaluate_queries(wf, st));
     return KRR_OK;
 }
 
@@ -2060,14 +2067,19 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
     // Without media, the shadow rays of a bounce and the next bounce's rays
     // are traced in one launch; results and their order of use are those of
     // the stage-by-stage loop (integrator.cpp:223-254).
+    // With a cache attached, the paths that stop at it (at any depth) are
+    // evaluated in one launch at the end of the sample: a stopped path gets no
+    // other radiance afterwards, so each pixel's sum is the same, in the same
+    // order, as with one evaluation per depth.
     const bool fuse = wf->params.nee && !wf->medium;
     for (int s = 0; s < wf->params.spp; ++s) {
         KRR_TRY(krr_wf_reset_queues(wf, -1, stream));
         KRR_TRY(krr_wf_generate_camera_rays(wf, stream));
+        if (wf->nrc) KRR_CUDA(cudaMemsetAsync(wf->nrc_q_count(), 0, sizeof(int32_t), st));
         bool traced = false;
         for (int depth = 0;; ++depth) {
             KRR_TRY(krr_wf_reset_queues(wf, depth, stream));
-            KRR_TRY(closest_stage(wf, depth, st, traced));
+            KRR_TRY(closest_stage(wf, depth, st, traced, true));
             if (wf->medium) KRR_TRY(krr_wf_sample_medium_interaction(wf, depth, stream));
             KRR_TRY(krr_wf_handle_hit(wf, stream));
             KRR_TRY(krr_wf_handle_miss(wf, stream));
@@ -2078,6 +2090,7 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
             if (fuse) KRR_TRY(trace_shadow_and_next(wf, depth, st));
             else if (wf->params.nee) KRR_TRY(krr_wf_trace_shadow(wf, stream));
         }
+        if (wf->nrc) KRR_TRY(nrc_evaluate_queries(wf, st));
         if (wf->nrc && wf->nrc_train) KRR_TRY(nrc_train_frame(wf, st));
         k_accumulate<<<wf->grid, kThreads, 0, st>>>(wf->ps, wf->n,
                                                      wf->params.independent_samples && s + 1 < wf->params.spp);

@@ -169,6 +169,41 @@ def test_spread_threshold_controls_termination(krr_lib, cuda):
     assert not np.array_equal(imgs[0.0], want)
 
 
+def test_cache_queries_of_a_sample_evaluated_at_its_end(krr_lib, cuda):
+    """render() evaluates the cache once per sample for the paths that stopped
+    at it at any depth; the stage-by-stage loop evaluates it after each
+    closest-hit stage.  A stopped path gets no radiance afterwards, so the
+    two are equal bit for bit (with a spread threshold of 0, most paths stop
+    at their first rough vertex)."""
+    sc = scenes.cornell_box(64, 48, max_depth=5)
+    cache = NeuralRadianceCache((0, 0, 0), (1, 1, 1), batch_size=4096, termination_spread=0.0, seed=5)
+    rec = _records(4096, 3)
+    for _ in range(5):   # weights away from their initial values
+        cache.train_step(torch.from_numpy(rec).cuda(), torch.from_numpy(_targets(rec)).cuda())
+    pt = WavefrontPathTracer({"max_depth": 5}, seed=6)
+    pt.set_scene(sc)
+    pt.resize(64, 48)
+    pt.set_nrc(cache, train=False)
+    pt.begin_frame(4, sc.camera)
+    pt.render()
+    fused = pt.radiance().cpu().numpy()
+    pt.begin_frame(4, sc.camera)
+    pt.reset_queues(-1)
+    pt.generate_camera_rays()
+    for d in range(6):
+        pt.reset_queues(d)
+        pt.trace_closest(d)
+        pt.handle_hit()
+        pt.handle_miss()
+        if d == 5:
+            break
+        pt.generate_scatter_rays(d)
+        pt.trace_shadow()
+    staged = pt.radiance().cpu().numpy()
+    assert np.array_equal(fused.view(np.uint32), staged.view(np.uint32))
+    assert pt.device_errors() == 0
+
+
 @pytest.mark.parametrize("n", [1, 100, 128, 1000, 4096])
 def test_tensor_core_backward_matches_cuda_core_kernels(krr_lib, cuda, n):
     """tcgen05 backward (dX chain and per-layer dW accumulated in tensor
