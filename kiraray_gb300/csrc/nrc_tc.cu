@@ -530,9 +530,10 @@ k_nrc_backward_tc(int layers, const float *__restrict__ dy_out, const __nv_bfloa
             tmem_ld16(base + 32, v + 32);
             tmem_ld16(base + 48, v + 48);
             tmem_wait_ld();
-            if (m < rows) {
-                float *dst = dw + mlp.w_offset[l] + (size_t)m * kNrcIn;
-                for (int k = 0; k < kNrcIn; ++k) atomicAdd(dst + k, v[k]);
+            if (m < rows) {   // 16-byte vector atomics (the row offsets are multiples of 64 floats)
+                float4 *dst = reinterpret_cast<float4 *>(dw + mlp.w_offset[l] + (size_t)m * kNrcIn);
+                for (int k = 0; k < kNrcIn / 4; ++k)
+                    atomicAdd(dst + k, make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]));
             }
         }
     }
