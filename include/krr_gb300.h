@@ -169,6 +169,11 @@ int krr_set_bvh_node_format(int32_t format);
  * node visits (a triangle test costs several node-child tests).  Hits are
  * the same with any setting. */
 int krr_set_bvh_max_leaf(int32_t triangles);
+/* Largest leaf child of a full node (eight children) of the BVHs built from
+ * now on, in triangles (max leaf..3, default 1): a child of a full node that
+ * covers at most this many triangles becomes a leaf instead of a node of
+ * its own with two or three children.  Hits are the same with any setting. */
+int krr_set_bvh_full_node_leaf(int32_t triangles);
 
 /* Build from host arrays of world-space triangles: h_vertices float3[3*n]. */
 int krr_accel_create_from_triangles(const float *h_vertices, int64_t n_triangles,

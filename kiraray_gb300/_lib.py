@@ -110,6 +110,7 @@ SIGNATURES = {
     "krr_accel_create_from_triangles": (_I, [_P, C.c_int64, C.POINTER(_P), _P]),
     "krr_set_bvh_node_format": (_I, [C.c_int32]),
     "krr_set_bvh_max_leaf": (_I, [C.c_int32]),
+    "krr_set_bvh_full_node_leaf": (_I, [C.c_int32]),
     "krr_wf_group_create": (_I, [C.POINTER(_P), C.POINTER(_P), C.c_int32, C.POINTER(_P)]),
     "krr_wf_group_capture": (_I, [_P, _P]),
     "krr_wf_group_launch": (_I, [_P, C.c_int64, _P]),

@@ -31,6 +31,11 @@ def set_max_leaf(triangles: int) -> None:
     check(_lib.load().krr_set_bvh_max_leaf(triangles), "krr_set_bvh_max_leaf")
 
 
+def set_full_node_leaf(triangles: int) -> None:
+    """Largest leaf (1..3 triangles) among the children of a full node."""
+    check(_lib.load().krr_set_bvh_full_node_leaf(triangles), "krr_set_bvh_full_node_leaf")
+
+
 class Accel:
     def __init__(self, world_triangles: np.ndarray, node_format: int | None = None):
         lib = _lib.load()

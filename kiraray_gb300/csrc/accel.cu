@@ -226,7 +226,7 @@ __device__ __forceinline__ int quant_exponent(float ext) {
 __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const int *n_in,
                            CollapseItem *out, int *n_out, float4 *nodes, int *node_counter,
                            uint32_t *leaf_order, int *tri_counter, int *max_depth, int format,
-                           int max_leaf) {
+                           int max_leaf, int full_leaf) {
     int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= *n_in) return;
     CollapseItem item = in[w];
@@ -260,6 +260,12 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
         ref_info(t, ref[nc], clo[nc], chi[nc], cfirst[nc], ccount[nc]);
         ++nc;
     }
+    // A child that stays internal becomes a node of its own; in a full node a
+    // child of at most `full_leaf` triangles becomes a leaf instead (eight
+    // leaves of three triangles still fit the 24-bit triangle mask).
+    bool internal[8];
+    const int leaf_max = nc == 8 ? full_leaf : max_leaf;
+    for (int c = 0; c < nc; ++c) internal[c] = ccount[c] > leaf_max;
 
     // Node bounds and quantisation frame.
     V3 lo = clo[0], hi = chi[0];
@@ -298,7 +304,7 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
     // Allocate internal children and leaf triangles.
     int n_int = 0, n_tri = 0;
     for (int c = 0; c < nc; ++c) {
-        if (ccount[c] > max_leaf) ++n_int;
+        if (internal[c]) ++n_int;
         else n_tri += ccount[c];
     }
     int child_base = n_int ? atomicAdd(node_counter, n_int) : 0;
@@ -325,7 +331,7 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
             qhi[k][s >> 2] |= (uint32_t)b << (8 * (s & 3));
         }
         uint32_t m;
-        if (ccount[c] > max_leaf) {
+        if (internal[c]) {
             m = 0x20u | (24u + (uint32_t)s);
             imask |= 1u << s;
         } else {
@@ -339,7 +345,7 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
     // internal children in slot order
     for (int s = 0; s < 8; ++s) {
         int c = child_in_slot[s];
-        if (c < 0 || ccount[c] <= max_leaf) continue;
+        if (c < 0 || !internal[c]) continue;
         int slot = atomicAdd(n_out, 1);
         out[slot] = CollapseItem{ref[c], (uint32_t)(child_base + int_rank), item.depth + 1};
         ++int_rank;
@@ -655,6 +661,7 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     accel_free(a);
     a->node_format = default_node_format();
     a->max_leaf = default_max_leaf();
+    a->full_leaf = std::max(a->max_leaf, default_full_leaf());
     a->n_tris = n;
     a->n_nodes = 0;
     a->max_depth = 0;
@@ -761,7 +768,7 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
         KRR_CUDA(cudaMemsetAsync(c_out, 0, sizeof(int), s));
         k_collapse<<<blocks_for(n_in, 128), 128, 0, s>>>(bt, qin, c_in, qout, c_out, nodes_tmp.p,
                                                          counters.p, leaf_order.p, counters.p + 1,
-                                                         counters.p + 2, fmt, a->max_leaf);
+                                                         counters.p + 2, fmt, a->max_leaf, a->full_leaf);
         KRR_CUDA(cudaGetLastError());
         KRR_CUDA(cudaMemcpyAsync(&n_in, c_out, sizeof(int), cudaMemcpyDeviceToHost, s));
         KRR_CUDA(cudaMemcpyAsync(c_in, c_out, sizeof(int), cudaMemcpyDeviceToDevice, s));
@@ -836,6 +843,15 @@ int krr::default_max_leaf() { return g_max_leaf; }
 extern "C" int krr_set_bvh_max_leaf(int32_t triangles) {
     KRR_CHECK_ARG(triangles >= 1 && triangles <= 3, "leaf size must be 1, 2 or 3 triangles");
     g_max_leaf = triangles;
+    return KRR_OK;
+}
+
+static int g_full_leaf = 1;
+int krr::default_full_leaf() { return g_full_leaf; }
+
+extern "C" int krr_set_bvh_full_node_leaf(int32_t triangles) {
+    KRR_CHECK_ARG(triangles >= 1 && triangles <= 3, "leaf size must be 1, 2 or 3 triangles");
+    g_full_leaf = triangles;
     return KRR_OK;
 }
 

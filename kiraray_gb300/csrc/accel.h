@@ -47,6 +47,7 @@ struct krr_accel {
     int postpone_pct = 0;
     int node_format = 0;         // 0 compressed (80 B), 1 float (224 B)
     int max_leaf = 1;            // triangles per leaf child (1..3)
+    int full_leaf = 1;           // triangles per leaf child of a full node (max_leaf..3)
     // host-buffer entry point (krr_accel_trace_closest_host): device staging
     // for rays (2 float4 each) and hits, grown on demand, and a second stream
     // with two events, kept across calls so that a call allocates nothing
@@ -64,6 +65,7 @@ constexpr int kNodeQuads[2] = {5, 14};   // float4 per node, by node format
 // Process-wide node format used by builds (krr_set_bvh_node_format).
 int default_node_format();
 int default_max_leaf();   // krr_set_bvh_max_leaf
+int default_full_leaf();  // krr_set_bvh_full_node_leaf
 constexpr int kTraceThreads = 128;
 
 // Build from device world-space vertices (float3 x 3 per triangle).

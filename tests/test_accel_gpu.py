@@ -248,29 +248,34 @@ def test_host_entry_point_in_chunks(krr_lib, cuda):
     _assert_bits_equal(got.numpy(), want, "host entry point, chunked")
 
 
-@pytest.mark.parametrize("leaf", [1, 2, 3])
-def test_leaf_sizes_keep_hits_identical(krr_lib, cuda, leaf):
-    from kiraray_gb300.accel import set_max_leaf
+@pytest.mark.parametrize("leaf,full_leaf", [(1, 1), (2, 2), (3, 3), (1, 2), (1, 3)])
+def test_leaf_sizes_keep_hits_identical(krr_lib, cuda, leaf, full_leaf):
+    """Leaf children of 1-3 triangles, everywhere or only in full nodes: the
+    hits are those of the oracle bit for bit."""
+    from kiraray_gb300.accel import set_full_node_leaf, set_max_leaf
+
+    def build(t):
+        set_max_leaf(leaf)
+        set_full_node_leaf(full_leaf)
+        try:
+            return Accel(t)
+        finally:
+            set_max_leaf(1)
+            set_full_node_leaf(1)
+
     sc = scenes.large_scene(width=160, height=90, grid=256, n_spheres=40, sky_size=(64, 32))
     tris = sc.world_triangles()
     rays = H.pinhole_rays(sc, jitter_seed=11)
-    set_max_leaf(leaf)
-    try:
-        acc = Accel(tris)
-    finally:
-        set_max_leaf(1)
+    acc = build(tris)
+    tag = f"leaf {leaf}/{full_leaf}"
     ob = O.Bvh(tris)
     want = ob.closest(rays)
-    _assert_bits_equal(_gpu_closest(acc, rays), want, f"leaf {leaf}")
+    _assert_bits_equal(_gpu_closest(acc, rays), want, tag)
     b = H.bounce_rays(tris, rays, want, 12)
-    _assert_bits_equal(_gpu_closest(acc, b), ob.closest(b), f"leaf {leaf} bounce")
+    _assert_bits_equal(_gpu_closest(acc, b), ob.closest(b), f"{tag} bounce")
     occ = acc.trace_any(torch.from_numpy(b).cuda()).cpu().numpy()
     assert np.array_equal(occ, ob.any(b))
     g = H.grid_mesh(12)
     r = H.vertex_edge_rays(12, 3)
-    set_max_leaf(leaf)
-    try:
-        ga = Accel(g)
-    finally:
-        set_max_leaf(1)
-    _assert_bits_equal(_gpu_closest(ga, r), O.closest_brute(g, r), f"leaf {leaf} edges")
+    ga = build(g)
+    _assert_bits_equal(_gpu_closest(ga, r), O.closest_brute(g, r), f"{tag} edges")
