@@ -227,8 +227,11 @@ int krr_accel_set_tuning(krr_accel *accel, int32_t refill_below, int32_t postpon
 int krr_accel_autotune(krr_accel *accel, const krr_ray *d_rays, int64_t n, int32_t repeats,
                        int32_t *out_refill, int32_t *out_postpone, float *out_ms, void *stream);
 
-/* Same as krr_accel_trace_closest, with host buffers: copies the rays in and
- * the hits out inside the call (pinned host memory is fastest). */
+/* Same as krr_accel_trace_closest, with host buffers; returns when the hits
+ * are in h_hits.  Page-locked buffers on a coherently linked host (Grace
+ * NVLink-C2C) are read and written in place by the traversal kernel;
+ * otherwise the rays are copied in and the hits out in chunks over two
+ * streams.  Not reentrant per handle (staging and counters are shared). */
 int krr_accel_trace_closest_host(const krr_accel *accel, const krr_ray *h_rays, int64_t n,
                                  krr_hit *h_hits, void *stream);
 

@@ -966,6 +966,35 @@ extern "C" int krr_accel_trace_closest_host(const krr_accel *a, const krr_ray *h
     // handle from two threads at once, since the work counters are shared)
     krr_accel *m = const_cast<krr_accel *>(a);
     cudaStream_t s = as_stream(stream);
+    // Page-locked host buffers on a GPU that reaches host memory coherently
+    // through the host's page tables (Grace's NVLink-C2C): the persistent
+    // kernel reads the rays and writes the hits in host memory directly, so
+    // the transfers overlap the traversal with no staging and no chunking.
+    {
+        static int coherent = -1;
+        if (coherent < 0) {
+            int dev = 0, v = 0;
+            cudaGetDevice(&dev);
+            coherent = cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) ==
+                               cudaSuccess && v ? 1 : 0;
+            cudaGetLastError();
+        }
+        cudaPointerAttributes pr{}, ph{};
+        const bool ok = coherent && cudaPointerGetAttributes(&pr, h_rays) == cudaSuccess &&
+                        cudaPointerGetAttributes(&ph, h_hits) == cudaSuccess;
+        cudaGetLastError();
+        if (ok && pr.type == cudaMemoryTypeHost && ph.type == cudaMemoryTypeHost && pr.devicePointer &&
+            ph.devicePointer && ((uintptr_t)pr.devicePointer & 15u) == 0 &&
+            ((uintptr_t)ph.devicePointer & 15u) == 0) {
+            TraceLaunch l = aos_launch(a, reinterpret_cast<const krr_ray *>(pr.devicePointer), n);
+            l.hits = reinterpret_cast<float4 *>(ph.devicePointer);
+            KRR_TRY(launch_trace_closest(a, l, s));
+            KRR_CUDA(cudaStreamSynchronize(s));
+            return KRR_OK;
+        }
+    }
+    // Otherwise (pageable memory, or no coherent link): chunks of rays are
+    // copied in, traced and copied out over two streams.
     if (!m->stage_aux) {
         KRR_CUDA(cudaStreamCreateWithFlags(&m->stage_aux, cudaStreamNonBlocking));
         KRR_CUDA(cudaEventCreateWithFlags(&m->stage_ev[0], cudaEventDisableTiming));

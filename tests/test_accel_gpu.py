@@ -235,9 +235,10 @@ def test_float_nodes_in_wavefront_frame(krr_lib, cuda, float_nodes):
     assert bad <= 0.01 and not pt.device_errors()
 
 
-def test_host_entry_point_in_chunks(krr_lib, cuda):
-    """More than four chunks of host rays over the two streams: the hits
-    equal the device-buffer entry point's."""
+def test_host_entry_point_pinned_and_pageable(krr_lib, cuda):
+    """1.3M host rays from page-locked buffers (traced in place on a coherent
+    link, else in chunks) and from pageable arrays (more than four chunks over
+    the two streams): the hits equal the device-buffer entry point's."""
     sc = scenes.large_scene(width=160, height=90, grid=256, n_spheres=30, sky_size=(64, 32))
     tris = sc.world_triangles()
     acc = Accel(tris)
@@ -245,7 +246,14 @@ def test_host_entry_point_in_chunks(krr_lib, cuda):
     want = _gpu_closest(acc, rays)
     got = torch.empty((rays.shape[0], 4), dtype=torch.float32).pin_memory()
     acc.trace_closest_host(torch.from_numpy(rays).pin_memory(), got)
-    _assert_bits_equal(got.numpy(), want, "host entry point, chunked")
+    _assert_bits_equal(got.numpy(), want, "host entry point, page-locked")
+    out = np.zeros((rays.shape[0], 4), np.float32)
+    acc.trace_closest_host(np.ascontiguousarray(rays), out)
+    _assert_bits_equal(out, want, "host entry point, pageable")
+    # mixed: page-locked rays, pageable hits
+    out2 = np.zeros((rays.shape[0], 4), np.float32)
+    acc.trace_closest_host(torch.from_numpy(rays).pin_memory(), out2)
+    _assert_bits_equal(out2, want, "host entry point, mixed")
 
 
 @pytest.mark.parametrize("leaf,full_leaf", [(1, 1), (2, 2), (3, 3), (1, 2), (1, 3)])
