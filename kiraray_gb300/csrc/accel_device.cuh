@@ -72,15 +72,11 @@ __device__ __forceinline__ float tri_test(const RayPre &r, float4 v0, float4 v1,
     return t;
 }
 
-__device__ __forceinline__ float byte_to_float(uint32_t w, int k) {
-    return __uint_as_float(0x4B000000u | ((w >> (8 * k)) & 0xffu)) - 8388608.0f;
-}
 
-
-// 8-bit quantised plane k of a packed word as a float (exact): one byte
-// permute into 0x4B0000xx (2^23 + q) and one subtraction.
-__device__ __forceinline__ float plane(uint32_t w, int k) {
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u + (uint32_t)k)) - 8388608.0f;
+// 8-bit quantised plane k of a packed word as the float 2^23 + 256 q
+// (exact): one byte permute into 0x4B00qq00.
+__device__ __forceinline__ float plane256(uint32_t w, int k) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7404u | ((uint32_t)k << 4)));
 }
 
 // Visits one 8-wide node: returns the next node group (child base, hit
@@ -101,6 +97,16 @@ __device__ __forceinline__ void visit_node(const float4 *__restrict__ nodes, uin
     float ez = __uint_as_float(((ew >> 16) & 0xffu) << 23);
     float adx = ex * inv.x, ady = ey * inv.y, adz = ez * inv.z;
     float orx = (q0.x - r.o.x) * inv.x, ory = (q0.y - r.o.y) * inv.y, orz = (q0.z - r.o.z) * inv.z;
+    // A plane at q steps is t = q ad + or = (2^23 + 256 q) (ad / 256) + (or - 2^15 ad): one FMA
+    // on the permuted byte.  Rounding the offset or - 2^15 ad errs by at most 2^-9 |ad| (half an
+    // ulp of 2^15 |ad|) plus half an ulp of or; entry planes are moved down and exit planes up
+    // by |ad| / 64 (1/64 of a quantisation step), which covers that with room to spare, so the
+    // test stays conservative.
+    const float dx = adx * 0.00390625f, dy = ady * 0.00390625f, dz = adz * 0.00390625f;
+    const float cx = fmaf(-32768.f, adx, orx), cy = fmaf(-32768.f, ady, ory), cz = fmaf(-32768.f, adz, orz);
+    const float sx = fabsf(adx) * 0.015625f, sy = fabsf(ady) * 0.015625f, sz = fabsf(adz) * 0.015625f;
+    const float nox = cx - sx, noy = cy - sy, noz = cz - sz;
+    const float fox = cx + sx, foy = cy + sy, foz = cz + sz;
     uint32_t lox0 = __float_as_uint(q2.x), lox1 = __float_as_uint(q2.y);
     uint32_t loy0 = __float_as_uint(q2.z), loy1 = __float_as_uint(q2.w);
     uint32_t loz0 = __float_as_uint(q3.x), loz1 = __float_as_uint(q3.y);
@@ -124,12 +130,12 @@ __device__ __forceinline__ void visit_node(const float4 *__restrict__ nodes, uin
     for (int c = 0; c < 8; ++c) {
         const int k = c & 3;
         uint32_t m = __byte_perm(c < 4 ? meta0 : meta1, 0u, 0x4440u + (uint32_t)k);
-        int tnx = __float_as_int(fmaf(plane(c < 4 ? nx0 : nx1, k), adx, orx));
-        int tny = __float_as_int(fmaf(plane(c < 4 ? ny0 : ny1, k), ady, ory));
-        int tnz = __float_as_int(fmaf(plane(c < 4 ? nz0 : nz1, k), adz, orz));
-        int tfx = __float_as_int(fmaf(plane(c < 4 ? fx0 : fx1, k), adx, orx));
-        int tfy = __float_as_int(fmaf(plane(c < 4 ? fy0 : fy1, k), ady, ory));
-        int tfz = __float_as_int(fmaf(plane(c < 4 ? fz0 : fz1, k), adz, orz));
+        int tnx = __float_as_int(fmaf(plane256(c < 4 ? nx0 : nx1, k), dx, nox));
+        int tny = __float_as_int(fmaf(plane256(c < 4 ? ny0 : ny1, k), dy, noy));
+        int tnz = __float_as_int(fmaf(plane256(c < 4 ? nz0 : nz1, k), dz, noz));
+        int tfx = __float_as_int(fmaf(plane256(c < 4 ? fx0 : fx1, k), dx, fox));
+        int tfy = __float_as_int(fmaf(plane256(c < 4 ? fy0 : fy1, k), dy, foy));
+        int tfz = __float_as_int(fmaf(plane256(c < 4 ? fz0 : fz1, k), dz, foz));
         int t0 = __vimax3_s32(tnx, tny, max(tnz, tmin_i));
         int t1 = __vimin3_s32(tfx, tfy, min(tfz, tlim_i));
         uint32_t bits = (m >> 5) << (m & 31u);
