@@ -540,8 +540,10 @@ __device__ __forceinline__ void trace_body(const float4 *__restrict__ nodes,
     }
 }
 
+// Compressed nodes: eight blocks per SM (64 registers, no spills); the float
+// node format keeps the compiler's register choice.
 template <int MODE, bool STATS, int FMT>
-__global__ void __launch_bounds__(kTraceThreads)
+__global__ void __launch_bounds__(kTraceThreads, FMT == 0 ? 8 : 1)
 k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, TraceLaunch L,
         unsigned long long *stats) {
     trace_body<MODE, STATS, FMT>(nodes, tris, L, stats);
