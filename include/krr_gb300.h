@@ -180,6 +180,14 @@ int krr_accel_create_from_triangles(const float *h_vertices, int64_t n_triangles
                                     krr_accel **out, void *stream);
 int krr_accel_stats_get(const krr_accel *accel, krr_accel_stats *out);
 int krr_accel_destroy(krr_accel *accel);
+/* New positions for the triangles of a built structure (same count and order,
+ * h_vertices float3[3*n]): the boxes are refitted bottom-up over the existing
+ * tree (about 1/10 of a build), the device buffers keep their addresses and
+ * hits stay exact; the tree's quality follows the motion, so a caller
+ * rebuilds after large changes.  The update path of an OptiX AS (used by
+ * OptixSceneSingleLevel::updateAccelStructure, optix.cpp:618-642). */
+int krr_accel_refit_triangles(krr_accel *accel, const float *h_vertices, int64_t n_triangles,
+                              void *stream);
 
 /* Closest hit for n rays (the reference's __raygen__Closest +
  * __closesthit__Closest, src/render/wavefront/device.cu:43-81, without the
@@ -268,10 +276,15 @@ int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *scene, void *stream);
 /* Scene::update for animated instances (src/core/scene.cpp:17-31,
  * src/core/device/optix.cpp:618-642): instance h_indices[k] gets the
  * row-major 3x4 transform h_transforms[12k..12k+11]; the world-space
- * triangles and the BVH are rebuilt (about 8 ms for 10.9M triangles).
- * Drops a captured frame graph (capture again). */
+ * triangles are re-flattened and the BVH's boxes refitted over its tree
+ * (krr_accel_refit_triangles).  Device buffers stay in place: a captured
+ * frame graph stays valid.  Frames equal those of a fresh scene. */
 int krr_wf_update_instances(krr_wf *wf, int32_t n, const int32_t *h_indices,
                             const float *h_transforms, void *stream);
+/* Full BVH build over the current instance transforms (restores the tree's
+ * quality after large motion; about 9 ms for 10.9M triangles).  Drops a
+ * captured frame graph (capture again). */
+int krr_wf_rebuild_bvh(krr_wf *wf, void *stream);
 /* RenderPass::resize (integrator.cpp:181-184): reallocates queues. */
 int krr_wf_resize(krr_wf *wf, int32_t width, int32_t height);
 /* RenderPass::beginFrame (integrator.cpp:205-221). frame_index is 1-based. */

@@ -116,11 +116,13 @@ SIGNATURES = {
     "krr_wf_group_launch": (_I, [_P, C.c_int64, _P]),
     "krr_wf_group_destroy": (_I, [_P]),
     "krr_wf_update_instances": (_I, [_P, C.c_int32, _P, _P, _P]),
+    "krr_wf_rebuild_bvh": (_I, [_P, _P]),
     "krr_tonemap": (_I, [_P, _P, C.c_int64, C.c_int32, C.c_float, C.c_int32, _P]),
     "krr_wf_render_megakernel": (_I, [_P, _P, _P]),
     "krr_wf_queue_view": (_I, [_P, C.c_int32, C.POINTER(_P), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "krr_accel_stats_get": (_I, [_P, C.POINTER(AccelStats)]),
     "krr_accel_destroy": (_I, [_P]),
+    "krr_accel_refit_triangles": (_I, [_P, _P, C.c_int64, _P]),
     "krr_accel_trace_closest": (_I, [_P, _P, C.c_int64, _P, _P]),
     "krr_accel_trace_any": (_I, [_P, _P, C.c_int64, _P, _P]),
     "krr_accel_set_mask": (_I, [_P, _P]),

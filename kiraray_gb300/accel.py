@@ -55,6 +55,13 @@ class Accel:
         obj._borrowed = True
         return obj
 
+    def refit(self, world_triangles: np.ndarray) -> None:
+        """New positions for the same triangles (count and order kept): the
+        boxes are refitted over the existing tree."""
+        v = np.ascontiguousarray(world_triangles, dtype=np.float32).reshape(-1, 9)
+        check(_lib.load().krr_accel_refit_triangles(self._h, v.ctypes.data, v.shape[0], _stream()),
+              "krr_accel_refit_triangles")
+
     def stats(self) -> dict:
         s = _lib.AccelStats()
         check(_lib.load().krr_accel_stats_get(self._h, C.byref(s)), "krr_accel_stats_get")

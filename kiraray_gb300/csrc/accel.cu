@@ -223,6 +223,67 @@ __device__ __forceinline__ int quant_exponent(float ext) {
     return max(min(k, 127), -126);
 }
 
+// Child boxes of one 8-wide node, by slot (empty slots have slot_box_lo.x =
+// +inf): writes the quantisation frame and the quantised boxes (format 0:
+// node quads 0 and 2-4, quad 1 left to the caller; format 1: the float planes,
+// quads 0-11) and returns the node's bounds.  Used by the collapse and by the
+// refit, so that both quantise alike: every quantised box contains its child
+// box (floor/ceil, then stepped outwards while rounding left it inside).
+__device__ void write_node_boxes(float4 *np, int format, const V3 *slo, const V3 *shi, uint32_t imask,
+                                 V3 &out_lo, V3 &out_hi) {
+    V3 lo = v3(INFINITY), hi = v3(-INFINITY);
+    for (int s = 0; s < 8; ++s)
+        if (slo[s].x != INFINITY) { lo = vmin(lo, slo[s]); hi = vmax(hi, shi[s]); }
+    out_lo = lo;
+    out_hi = hi;
+    if (format == 1) {
+        for (int k = 0; k < 3; ++k) {
+            float b0[8], b1[8];
+            for (int s = 0; s < 8; ++s) {
+                const bool used = slo[s].x != INFINITY;
+                b0[s] = used ? get(slo[s], k) : INFINITY;
+                b1[s] = used ? get(shi[s], k) : -INFINITY;
+            }
+            np[4 * k + 0] = make_float4(b0[0], b0[1], b0[2], b0[3]);
+            np[4 * k + 1] = make_float4(b0[4], b0[5], b0[6], b0[7]);
+            np[4 * k + 2] = make_float4(b1[0], b1[1], b1[2], b1[3]);
+            np[4 * k + 3] = make_float4(b1[4], b1[5], b1[6], b1[7]);
+        }
+        return;
+    }
+    int ek[3];
+    float escale[3];
+    for (int k = 0; k < 3; ++k) {
+        ek[k] = quant_exponent(get(hi, k) - get(lo, k));
+        escale[k] = ldexpf(1.f, ek[k]);
+    }
+    uint32_t qlo[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    uint32_t qhi[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    for (int s = 0; s < 8; ++s) {
+        if (slo[s].x == INFINITY) continue;
+        for (int k = 0; k < 3; ++k) {
+            float p = get(lo, k), e = escale[k];
+            float a = floorf((get(slo[s], k) - p) / e);
+            float b = ceilf((get(shi[s], k) - p) / e);
+            a = fminf(fmaxf(a, 0.f), 255.f);
+            b = fminf(fmaxf(b, 0.f), 255.f);
+            while (a > 0.f && fmaf(a, e, p) > get(slo[s], k)) a -= 1.f;
+            while (b < 255.f && fmaf(b, e, p) < get(shi[s], k)) b += 1.f;
+            qlo[k][s >> 2] |= (uint32_t)a << (8 * (s & 3));
+            qhi[k][s >> 2] |= (uint32_t)b << (8 * (s & 3));
+        }
+    }
+    uint32_t ew = (uint32_t)(ek[0] + 127) | ((uint32_t)(ek[1] + 127) << 8) |
+                  ((uint32_t)(ek[2] + 127) << 16) | (imask << 24);
+    np[0] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(ew));
+    np[2] = make_float4(__uint_as_float(qlo[0][0]), __uint_as_float(qlo[0][1]),
+                        __uint_as_float(qlo[1][0]), __uint_as_float(qlo[1][1]));
+    np[3] = make_float4(__uint_as_float(qlo[2][0]), __uint_as_float(qlo[2][1]),
+                        __uint_as_float(qhi[0][0]), __uint_as_float(qhi[0][1]));
+    np[4] = make_float4(__uint_as_float(qhi[1][0]), __uint_as_float(qhi[1][1]),
+                        __uint_as_float(qhi[2][0]), __uint_as_float(qhi[2][1]));
+}
+
 __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const int *n_in,
                            CollapseItem *out, int *n_out, float4 *nodes, int *node_counter,
                            uint32_t *leaf_order, int *tri_counter, int *max_depth, int format,
@@ -267,15 +328,9 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
     const int leaf_max = nc == 8 ? full_leaf : max_leaf;
     for (int c = 0; c < nc; ++c) internal[c] = ccount[c] > leaf_max;
 
-    // Node bounds and quantisation frame.
+    // Node bounds.
     V3 lo = clo[0], hi = chi[0];
     for (int c = 1; c < nc; ++c) { lo = vmin(lo, clo[c]); hi = vmax(hi, chi[c]); }
-    int ek[3];
-    float escale[3];
-    for (int k = 0; k < 3; ++k) {
-        ek[k] = quant_exponent(get(hi, k) - get(lo, k));
-        escale[k] = ldexpf(1.f, ek[k]);
-    }
 
     // Octant slot assignment: slot s gets the child nearest for direction
     // octant s (greedy on dot(child centre - node centre, dir_s)).
@@ -312,24 +367,14 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
     if (n_int) atomicMax(max_depth, item.depth + 1);
 
     uint32_t meta[2] = {0, 0};
-    uint32_t qlo[3][2] = {{0, 0}, {0, 0}, {0, 0}};
-    uint32_t qhi[3][2] = {{0, 0}, {0, 0}, {0, 0}};
     uint32_t imask = 0;
     int int_rank = 0, tri_off = 0;
+    V3 slo[8], shi[8];
     for (int s = 0; s < 8; ++s) {
         int c = child_in_slot[s];
+        slo[s] = c >= 0 ? clo[c] : v3(INFINITY);
+        shi[s] = c >= 0 ? chi[c] : v3(-INFINITY);
         if (c < 0) continue;
-        for (int k = 0; k < 3; ++k) {
-            float p = get(lo, k), e = escale[k];
-            float a = floorf((get(clo[c], k) - p) / e);
-            float b = ceilf((get(chi[c], k) - p) / e);
-            a = fminf(fmaxf(a, 0.f), 255.f);
-            b = fminf(fmaxf(b, 0.f), 255.f);
-            while (a > 0.f && fmaf(a, e, p) > get(clo[c], k)) a -= 1.f;
-            while (b < 255.f && fmaf(b, e, p) < get(chi[c], k)) b += 1.f;
-            qlo[k][s >> 2] |= (uint32_t)a << (8 * (s & 3));
-            qhi[k][s >> 2] |= (uint32_t)b << (8 * (s & 3));
-        }
         uint32_t m;
         if (internal[c]) {
             m = 0x20u | (24u + (uint32_t)s);
@@ -351,37 +396,19 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
         ++int_rank;
     }
 
-    uint32_t ew = (uint32_t)(ek[0] + 127) | ((uint32_t)(ek[1] + 127) << 8) |
-                  ((uint32_t)(ek[2] + 127) << 16) | (imask << 24);
+    V3 blo, bhi;
     if (format == 1) {
         float4 *np = nodes + 14 * (size_t)item.wnode;
-        float b[6][8];
-        for (int s2 = 0; s2 < 8; ++s2) {
-            int c = child_in_slot[s2];
-            for (int k = 0; k < 3; ++k) {
-                b[2 * k][s2] = c >= 0 ? get(clo[c], k) : INFINITY;
-                b[2 * k + 1][s2] = c >= 0 ? get(chi[c], k) : -INFINITY;
-            }
-        }
-        for (int q = 0; q < 6; ++q) {
-            np[2 * q] = make_float4(b[q][0], b[q][1], b[q][2], b[q][3]);
-            np[2 * q + 1] = make_float4(b[q][4], b[q][5], b[q][6], b[q][7]);
-        }
+        write_node_boxes(np, 1, slo, shi, imask, blo, bhi);
         np[12] = make_float4(__uint_as_float((uint32_t)child_base), __uint_as_float((uint32_t)tri_base),
                              __uint_as_float(meta[0]), __uint_as_float(meta[1]));
         np[13] = make_float4(__uint_as_float(imask), 0.f, 0.f, 0.f);
         return;
     }
     float4 *np = nodes + 5 * (size_t)item.wnode;
-    np[0] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(ew));
+    write_node_boxes(np, 0, slo, shi, imask, blo, bhi);
     np[1] = make_float4(__uint_as_float((uint32_t)child_base), __uint_as_float((uint32_t)tri_base),
                         __uint_as_float(meta[0]), __uint_as_float(meta[1]));
-    np[2] = make_float4(__uint_as_float(qlo[0][0]), __uint_as_float(qlo[0][1]),
-                        __uint_as_float(qlo[1][0]), __uint_as_float(qlo[1][1]));
-    np[3] = make_float4(__uint_as_float(qlo[2][0]), __uint_as_float(qlo[2][1]),
-                        __uint_as_float(qhi[0][0]), __uint_as_float(qhi[0][1]));
-    np[4] = make_float4(__uint_as_float(qhi[1][0]), __uint_as_float(qhi[1][1]),
-                        __uint_as_float(qhi[2][0]), __uint_as_float(qhi[2][1]));
 }
 
 __global__ void k_gather_tris(const float *__restrict__ v, const uint32_t *__restrict__ leaf_order,
@@ -635,6 +662,9 @@ void accel_free(krr_accel *a) {
     cudaFree(a->d_scratch);
     cudaFree(a->stage_rays);
     cudaFree(a->stage_hits);
+    cudaFree(a->d_node_bounds);
+    a->d_node_bounds = nullptr;
+    a->level_first.clear();
     if (a->stage_aux) cudaStreamDestroy(a->stage_aux);
     for (cudaEvent_t &e : a->stage_ev)
         if (e) cudaEventDestroy(e);
@@ -658,6 +688,127 @@ struct DevBuf {
 inline unsigned blocks_for(int64_t n, int t = kBuildThreads) { return (unsigned)((n + t - 1) / t); }
 }  // namespace
 
+// New vertex positions into the leaf-ordered triangle records (the id and
+// mask words are kept).
+__global__ void k_refit_tris(const float *__restrict__ v, int64_t n,
+                             const uint32_t *__restrict__ leaf_of_prim, float4 *tris) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const float *s = v + 9 * (size_t)p;
+    float4 *t = tris + 3 * (size_t)leaf_of_prim[p];
+    for (int j = 0; j < 3; ++j) {
+        float4 q = t[j];
+        q.x = s[3 * j]; q.y = s[3 * j + 1]; q.z = s[3 * j + 2];
+        t[j] = q;
+    }
+}
+
+// Refit of the nodes [first, first + count) of one tree level, children
+// refitted before: a leaf child's box is the box of its triangles widened by
+// `margin` (as the build's leaf boxes), an internal child's box the bounds of
+// its node; quantised by write_node_boxes as the build does.  Topology,
+// slots and child/triangle offsets are kept.
+template <int FMT>
+__global__ void k_refit_level(float4 *nodes, const float4 *__restrict__ tris, float4 *bounds,
+                              int first, int count, float margin) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const int w = first + i;
+    float4 *np = nodes + (FMT == 1 ? 14 : 5) * (size_t)w;
+    uint32_t child_base, tri_base, meta0, meta1, imask;
+    if (FMT == 1) {
+        const float4 q12 = np[12], q13 = np[13];
+        child_base = __float_as_uint(q12.x); tri_base = __float_as_uint(q12.y);
+        meta0 = __float_as_uint(q12.z); meta1 = __float_as_uint(q12.w);
+        imask = __float_as_uint(q13.x);
+    } else {
+        const float4 q0 = np[0], q1 = np[1];
+        child_base = __float_as_uint(q1.x); tri_base = __float_as_uint(q1.y);
+        meta0 = __float_as_uint(q1.z); meta1 = __float_as_uint(q1.w);
+        imask = __float_as_uint(q0.w) >> 24;
+    }
+    V3 slo[8], shi[8];
+    for (int s = 0; s < 8; ++s) {
+        const uint32_t m = ((s < 4 ? meta0 : meta1) >> (8 * (s & 3))) & 0xffu;
+        slo[s] = v3(INFINITY);
+        shi[s] = v3(-INFINITY);
+        if (imask & (1u << s)) {
+            const uint32_t c = child_base + __popc(imask & ((1u << s) - 1u));
+            slo[s] = f3(bounds[2 * (size_t)c]);
+            shi[s] = f3(bounds[2 * (size_t)c + 1]);
+        } else if (m) {
+            const uint32_t cnt = __popc(m >> 5), off = m & 31u;
+            V3 lo = v3(INFINITY), hi = v3(-INFINITY);
+            for (uint32_t k = 0; k < cnt; ++k) {
+                const float4 *t = tris + 3 * (size_t)(tri_base + off + k);
+                for (int j = 0; j < 3; ++j) {
+                    V3 p = f3(t[j]);
+                    lo = vmin(lo, p);
+                    hi = vmax(hi, p);
+                }
+            }
+            slo[s] = lo - v3(margin);
+            shi[s] = hi + v3(margin);
+        }
+    }
+    V3 lo, hi;
+    write_node_boxes(np, FMT, slo, shi, imask, lo, hi);
+    bounds[2 * (size_t)w] = make_float4(lo.x, lo.y, lo.z, 0.f);
+    bounds[2 * (size_t)w + 1] = make_float4(hi.x, hi.y, hi.z, 0.f);
+}
+
+// Scene bounds of device vertices (into a->scene_lo/hi) and the margin that
+// keeps quantised boxes conservative: a few float ulps of the largest
+// coordinate magnitude and of the scene extent.
+static int scene_bounds_margin(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s,
+                               DevBuf<float> &bounds, float *margin) {
+    KRR_CUDA(bounds.alloc(12));
+    float init[12] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY,
+                      INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    KRR_CUDA(cudaMemcpyAsync(bounds.p, init, sizeof(init), cudaMemcpyHostToDevice, s));
+    k_scene_bounds<<<std::min<unsigned>(blocks_for(n), 4096), kBuildThreads, 0, s>>>(d_v, n, bounds.p);
+    KRR_CUDA(cudaGetLastError());
+    float hb[12];
+    KRR_CUDA(cudaMemcpyAsync(hb, bounds.p, sizeof(hb), cudaMemcpyDeviceToHost, s));
+    KRR_CUDA(cudaStreamSynchronize(s));
+    for (int k = 0; k < 3; ++k) { a->scene_lo[k] = hb[6 + k]; a->scene_hi[k] = hb[9 + k]; }
+    for (int k = 6; k < 12; ++k)
+        if (!std::isfinite(hb[k])) return fail(KRR_ERR_INVALID_ARGUMENT, "triangle vertices are not finite");
+    float mag = 0.f, ext = 0.f;
+    for (int k = 0; k < 3; ++k) {
+        mag = std::max(mag, std::max(std::fabs(hb[6 + k]), std::fabs(hb[9 + k])));
+        ext = std::max(ext, hb[9 + k] - hb[6 + k]);
+    }
+    *margin = std::ldexp(mag + ext, -19) + 1e-30f;
+    return KRR_OK;
+}
+
+int accel_refit(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
+    KRR_CHECK_ARG(a && a->d_scratch, "acceleration structure not built");
+    KRR_CHECK_ARG(n == a->n_tris, "a refit keeps the triangle count of the build");
+    if (n == 0) return KRR_OK;
+    KRR_CHECK_ARG(d_v != nullptr, "vertices are NULL");
+    float margin = 0.f;
+    DevBuf<float> bounds;
+    KRR_TRY(scene_bounds_margin(a, d_v, n, s, bounds, &margin));
+    if (!a->d_node_bounds) KRR_CUDA(cudaMalloc(&a->d_node_bounds, 2 * sizeof(float4) * a->n_nodes));
+    k_refit_tris<<<blocks_for(n), kBuildThreads, 0, s>>>(d_v, n, a->d_leaf_of_prim, a->d_tris);
+    KRR_CUDA(cudaGetLastError());
+    const std::vector<int32_t> &lf = a->level_first;
+    for (int L = (int)lf.size() - 1; L >= 1; --L) {
+        const int first = lf[L - 1], count = lf[L] - lf[L - 1];
+        if (count <= 0) continue;
+        if (a->node_format == 1)
+            k_refit_level<1><<<blocks_for(count, 128), 128, 0, s>>>(a->d_nodes, a->d_tris, a->d_node_bounds,
+                                                                     first, count, margin);
+        else
+            k_refit_level<0><<<blocks_for(count, 128), 128, 0, s>>>(a->d_nodes, a->d_tris, a->d_node_bounds,
+                                                                     first, count, margin);
+        KRR_CUDA(cudaGetLastError());
+    }
+    return KRR_OK;
+}
+
 int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     KRR_CHECK_ARG(n >= 0 && n < (int64_t)0x7fffffff, "triangle count out of range");
     accel_free(a);
@@ -676,29 +827,11 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
 
-    // scene bounds
+    // scene bounds (centroid bounds first, for the Morton codes) and the
+    // conservative-box margin
+    float margin = 0.f;
     DevBuf<float> bounds;
-    KRR_CUDA(bounds.alloc(12));
-    float init[12] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY,
-                      INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
-    KRR_CUDA(cudaMemcpyAsync(bounds.p, init, sizeof(init), cudaMemcpyHostToDevice, s));
-    k_scene_bounds<<<std::min<unsigned>(blocks_for(n), 4096), kBuildThreads, 0, s>>>(d_v, n, bounds.p);
-    KRR_CUDA(cudaGetLastError());
-    float hb[12];
-    KRR_CUDA(cudaMemcpyAsync(hb, bounds.p, sizeof(hb), cudaMemcpyDeviceToHost, s));
-    KRR_CUDA(cudaStreamSynchronize(s));
-    for (int k = 0; k < 3; ++k) { a->scene_lo[k] = hb[6 + k]; a->scene_hi[k] = hb[9 + k]; }
-    if (!std::isfinite(hb[6]) || !std::isfinite(hb[9]) || !std::isfinite(hb[7]) ||
-        !std::isfinite(hb[10]) || !std::isfinite(hb[8]) || !std::isfinite(hb[11]))
-        return fail(KRR_ERR_INVALID_ARGUMENT, "triangle vertices are not finite");
-    // Margin that keeps quantised boxes conservative: a few float ulps of the
-    // largest coordinate magnitude and of the scene extent.
-    float mag = 0.f, ext = 0.f;
-    for (int k = 0; k < 3; ++k) {
-        mag = std::max(mag, std::max(std::fabs(hb[6 + k]), std::fabs(hb[9 + k])));
-        ext = std::max(ext, hb[9 + k] - hb[6 + k]);
-    }
-    float margin = std::ldexp(mag + ext, -19) + 1e-30f;
+    KRR_TRY(scene_bounds_margin(a, d_v, n, s, bounds, &margin));
 
     DevBuf<uint64_t> keys, keys2;
     DevBuf<uint32_t> vals, vals2;
@@ -763,6 +896,7 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     KRR_CUDA(cudaMemcpyAsync(qa.p, &root, sizeof(root), cudaMemcpyHostToDevice, s));
     BinTree bt{left.p, right.p, first.p, last.p, ilo.p, ihi.p, llo.p, lhi.p, sidx};
     int n_in = 1;
+    a->level_first.assign({0, 1});
     CollapseItem *qin = qa.p, *qout = qb.p;
     int *c_in = counters.p + 3, *c_out = counters.p + 4;
     int levels = 0;
@@ -772,9 +906,12 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
                                                          counters.p, leaf_order.p, counters.p + 1,
                                                          counters.p + 2, fmt, a->max_leaf, a->full_leaf);
         KRR_CUDA(cudaGetLastError());
+        int allocated = 0;
         KRR_CUDA(cudaMemcpyAsync(&n_in, c_out, sizeof(int), cudaMemcpyDeviceToHost, s));
+        KRR_CUDA(cudaMemcpyAsync(&allocated, counters.p, sizeof(int), cudaMemcpyDeviceToHost, s));
         KRR_CUDA(cudaMemcpyAsync(c_in, c_out, sizeof(int), cudaMemcpyDeviceToDevice, s));
         KRR_CUDA(cudaStreamSynchronize(s));
+        if (n_in > 0) a->level_first.push_back(allocated);   // the next level's nodes end here
         std::swap(qin, qout);
         if (++levels > 4096) return fail(KRR_ERR_OVERFLOW, "BVH collapse did not terminate");
     }
@@ -835,6 +972,23 @@ extern "C" int krr_accel_create_from_triangles(const float *h_vertices, int64_t 
     if (st != KRR_OK) { accel_free(a); delete a; return st; }
     *out = a;
     return KRR_OK;
+}
+
+extern "C" int krr_accel_refit_triangles(krr_accel *a, const float *h_vertices, int64_t n_triangles,
+                                         void *stream) {
+    KRR_CHECK_ARG(a != nullptr, "accel is NULL");
+    KRR_CHECK_ARG(n_triangles == 0 || h_vertices != nullptr, "vertices are NULL");
+    KRR_CHECK_ARG(n_triangles == a->n_tris, "a refit keeps the triangle count of the build");
+    if (n_triangles == 0) return KRR_OK;
+    cudaStream_t s = as_stream(stream);
+    DevBuf<float> d_v;
+    const size_t bytes = sizeof(float) * 9 * (size_t)n_triangles;
+    KRR_CUDA(d_v.alloc(9 * (size_t)n_triangles));
+    KRR_CUDA(cudaMemcpyAsync(d_v.p, h_vertices, bytes, cudaMemcpyHostToDevice, s));
+    int st = accel_refit(a, d_v.p, n_triangles, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (st != KRR_OK) return st;
+    return cuda_status(e, "cudaStreamSynchronize", __FILE__, __LINE__);
 }
 
 static int g_node_format = 0;

@@ -29,6 +29,7 @@
 // v2.xyz | unused.
 #pragma once
 #include <cuda_runtime.h>
+#include <vector>
 #include <stdint.h>
 
 #include "internal.h"
@@ -51,6 +52,10 @@ struct krr_accel {
     // host-buffer entry point (krr_accel_trace_closest_host): device staging
     // for rays (2 float4 each) and hits, grown on demand, and a second stream
     // with two events, kept across calls so that a call allocates nothing
+    // refit (krr_accel_refit): first node of each tree level (level L holds
+    // nodes [level_first[L-1], level_first[L])) and the refitted node bounds
+    std::vector<int32_t> level_first;
+    float4 *d_node_bounds = nullptr;   // 2 per node: lo, hi
     float4 *stage_rays = nullptr;
     float4 *stage_hits = nullptr;
     int64_t stage_cap = 0;
@@ -70,6 +75,9 @@ constexpr int kTraceThreads = 128;
 
 // Build from device world-space vertices (float3 x 3 per triangle).
 int accel_build(krr_accel *a, const float *d_vertices, int64_t n_tris, cudaStream_t stream);
+// New positions for the same triangles (same count and order): boxes refitted
+// bottom-up over the existing tree; the buffers keep their addresses.
+int accel_refit(krr_accel *a, const float *d_vertices, int64_t n_tris, cudaStream_t stream);
 void accel_free(krr_accel *a);
 
 struct TraceLaunch {

@@ -81,6 +81,7 @@ struct krr_wf {
     krr_accel accel{};
     std::vector<void *> scene_allocs;
     std::vector<DevInstance> h_instances;     // host copies for instance updates
+    float *d_world = nullptr;                 // flattened triangles, kept for refits
     std::vector<DevInfinite> h_infinite;
     int32_t n_instances = 0;
     uint64_t n_tris = 0;
@@ -1380,6 +1381,8 @@ int dev_upload(krr_wf *wf, T **dst, const T *src, size_t count) {
 }
 
 void free_scene(krr_wf *wf) {
+    cudaFree(wf->d_world);
+    wf->d_world = nullptr;
     for (void *p : wf->scene_allocs) cudaFree(p);
     wf->scene_allocs.clear();
     accel_free(&wf->accel);
@@ -1513,22 +1516,29 @@ extern "C" int krr_wf_set_params(krr_wf *wf, const krr_wf_params *params) {
 // Flattens the instances to world space and builds the BVH over them, with
 // the null-material any-hit mask; sets the scene radius (the length of the
 // bounding-box diagonal, src/core/device/scene.cpp:108).
-static int rebuild_bvh(krr_wf *wf, cudaStream_t st) {
+// World-space triangles of the instances into the BVH: a full build, or with
+// `refit` new boxes over the existing tree (same triangles, moved).
+static int rebuild_bvh(krr_wf *wf, cudaStream_t st, bool refit = false) {
     const uint64_t n_tris = wf->n_tris;
     DevScene &s = wf->scene;
-    float *d_world = nullptr;
-    KRR_CUDA(cudaMalloc(&d_world, std::max<uint64_t>(n_tris, 1) * 9 * sizeof(float)));
+    // the flattened triangles: kept after a refit (the next update refits
+    // again), freed after a build (a scene that never moves does not hold them)
+    if (!wf->d_world)
+        KRR_CUDA(cudaMalloc(&wf->d_world, std::max<uint64_t>(n_tris, 1) * 9 * sizeof(float)));
+    float *d_world = wf->d_world;
     if (n_tris) k_flatten<<<grid_for(n_tris), kThreads, 0, st>>>(s, wf->n_instances, d_world, n_tris);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) {
-        cudaFree(d_world);
-        return cuda_status(e, "k_flatten", __FILE__, __LINE__);
+    KRR_CUDA(cudaGetLastError());
+    int stat = refit ? accel_refit(&wf->accel, d_world, (int64_t)n_tris, st)
+                     : accel_build(&wf->accel, d_world, (int64_t)n_tris, st);
+    if (stat == KRR_OK) stat = cuda_status(cudaStreamSynchronize(st), "BVH", __FILE__, __LINE__);
+    if (!refit || stat != KRR_OK) {
+        cudaFree(wf->d_world);
+        wf->d_world = nullptr;
     }
-    int stat = accel_build(&wf->accel, d_world, (int64_t)n_tris, st);
-    cudaFree(d_world);
     if (stat != KRR_OK) return stat;
-    // null-material triangles never block shadow rays (device.cu:83-88)
-    if (n_tris) {
+    // null-material triangles never block shadow rays (device.cu:83-88); a
+    // refit keeps the mask words of the triangle records
+    if (n_tris && !refit) {
         uint8_t *mask = nullptr;
         KRR_CUDA(cudaMalloc(&mask, n_tris));
         k_null_mask<<<grid_for(n_tris), kThreads, 0, st>>>(s, (int64_t)n_tris, mask);
@@ -1758,9 +1768,28 @@ static int set_layout(krr_wf *wf, std::vector<DevView> layout) {
 // Scene::update for animated instances (src/core/scene.cpp:17-31,
 // OptixSceneSingleLevel::updateAccelStructure, src/core/device/optix.cpp:
 // 618-642): new 3x4 transforms for some instances, then the world-space
-// triangles and the BVH are rebuilt (the reference rebuilds its instance
-// level; here instances are flattened into one BVH).  A captured frame graph
-// refers to the old BVH and is dropped.
+// triangles are re-flattened and the BVH's boxes refitted over its existing
+// tree (the reference rebuilds its instance level over static mesh
+// structures; here instances are flattened into one BVH).  Every device
+// buffer stays in place, so a captured frame graph stays valid.
+// krr_wf_rebuild_bvh restores the tree's quality after large motion.
+extern "C" int krr_wf_rebuild_bvh(krr_wf *wf, void *stream) {
+    KRR_CHECK_ARG(wf && wf->has_scene, "no scene");
+    cudaStream_t st = as_stream(stream);
+    KRR_CUDA(cudaStreamSynchronize(st));
+    if (wf->graph) {   // the rebuilt BVH lives in new buffers
+        cudaGraphExecDestroy(wf->graph);
+        wf->graph = nullptr;
+    }
+    KRR_TRY(rebuild_bvh(wf, st));
+    if (!wf->h_infinite.empty()) {
+        for (auto &d : wf->h_infinite) d.scene_radius = wf->scene_radius;
+        KRR_CUDA(cudaMemcpy(const_cast<DevInfinite *>(wf->scene.infinite), wf->h_infinite.data(),
+                            wf->h_infinite.size() * sizeof(DevInfinite), cudaMemcpyHostToDevice));
+    }
+    return KRR_OK;
+}
+
 extern "C" int krr_wf_update_instances(krr_wf *wf, int32_t n, const int32_t *h_indices,
                                        const float *h_transforms, void *stream) {
     KRR_CHECK_ARG(wf && wf->has_scene, "no scene");
@@ -1777,11 +1806,8 @@ extern "C" int krr_wf_update_instances(krr_wf *wf, int32_t n, const int32_t *h_i
     KRR_CUDA(cudaStreamSynchronize(st));
     KRR_CUDA(cudaMemcpy(const_cast<DevInstance *>(wf->scene.instances), wf->h_instances.data(),
                         wf->h_instances.size() * sizeof(DevInstance), cudaMemcpyHostToDevice));
-    if (wf->graph) {
-        cudaGraphExecDestroy(wf->graph);
-        wf->graph = nullptr;
-    }
-    KRR_TRY(rebuild_bvh(wf, st));
+    // a refit keeps every device buffer in place, so a captured frame stays valid
+    KRR_TRY(rebuild_bvh(wf, st, true));
     if (!wf->h_infinite.empty()) {
         for (auto &d : wf->h_infinite) d.scene_radius = wf->scene_radius;
         KRR_CUDA(cudaMemcpy(const_cast<DevInfinite *>(wf->scene.infinite), wf->h_infinite.data(),

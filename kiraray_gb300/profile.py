@@ -3,6 +3,9 @@ and single-kernel captures); prints the device time of each repetition.
 
     python -m kiraray_gb300.profile trace [--reps 4]
         closest hits of the 1920x1080 camera rays of the 10.9M-triangle scene
+    python -m kiraray_gb300.profile update [--reps 5]
+        an instance update of the large scene (re-flatten + BVH refit) against
+        a full BVH rebuild, host wall time per call
     python -m kiraray_gb300.profile frame [--scene large] [--res 480x270] [--views 8] [--nrc]
                                           [--frames 3] [--seed 3]
         frames of the wavefront pass on the large scene (max depth 8), the
@@ -37,6 +40,35 @@ def trace(reps: int) -> dict:
     rays = torch.from_numpy(scenes.pinhole_rays(sc)).cuda()
     ms = [_timed(lambda: acc.trace_closest(rays)) for _ in range(reps)]
     return {"workload": "trace", "rays": int(rays.shape[0]), "ms": ms}
+
+
+def update(reps: int) -> dict:
+    import time
+
+    import numpy as np
+
+    from . import scenes
+    from .wavefront import WavefrontPathTracer
+
+    sc = scenes.large_scene()
+    pt = WavefrontPathTracer({"max_depth": sc.max_depth})
+    pt.set_scene(sc)
+    pt.resize(64, 64)
+    k = len(sc.instances) - 2   # a sphere
+    xf = np.array(sc.instances[k][1], np.float32)
+    out = {"workload": "update", "triangles": int(sc.world_triangles().shape[0])}
+    for name, fn in (("refit_ms", lambda: pt.update_instances([k], xf[None])),
+                     ("rebuild_ms", pt.rebuild_bvh)):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append((time.perf_counter() - t0) * 1e3)
+        out[name] = sorted(ts)[len(ts) // 2]
+    return out
 
 
 def frame(res: str, views: int, nrc: bool, frames: int, scene: str = "large", seed: int = 3) -> dict:
@@ -75,6 +107,8 @@ def main() -> None:
     sub = ap.add_subparsers(dest="cmd", required=True)
     t = sub.add_parser("trace")
     t.add_argument("--reps", type=int, default=4)
+    u = sub.add_parser("update")
+    u.add_argument("--reps", type=int, default=5)
     f = sub.add_parser("frame")
     f.add_argument("--scene", default="large", choices=["large", "cornell", "volume"])
     f.add_argument("--res", default="480x270")
@@ -85,7 +119,12 @@ def main() -> None:
     a = ap.parse_args()
     from .build import build
     build()
-    r = trace(a.reps) if a.cmd == "trace" else frame(a.res, a.views, a.nrc, a.frames, a.scene, a.seed)
+    if a.cmd == "trace":
+        r = trace(a.reps)
+    elif a.cmd == "update":
+        r = update(a.reps)
+    else:
+        r = frame(a.res, a.views, a.nrc, a.frames, a.scene, a.seed)
     print(json.dumps(r))
 
 

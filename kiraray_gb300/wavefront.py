@@ -72,13 +72,18 @@ class WavefrontPathTracer:
 
     def update_instances(self, indices, transforms) -> None:
         """New 3x4 transforms (float32 [n, 3, 4] or [n, 12]) for the given
-        instances; rebuilds the BVH (Scene::update with animation)."""
+        instances; refits the BVH's boxes over its tree (Scene::update with
+        animation).  A captured frame stays valid."""
         idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int32))
         xf = np.ascontiguousarray(np.asarray(transforms, dtype=np.float32).reshape(-1, 12))
         if xf.shape[0] != idx.shape[0]:
             raise ValueError("one transform per instance index")
         check(self.lib.krr_wf_update_instances(self._h, int(idx.shape[0]), idx.ctypes.data,
                                                xf.ctypes.data, _stream()), "update_instances")
+
+    def rebuild_bvh(self) -> None:
+        """Full BVH build over the current instance transforms."""
+        check(self.lib.krr_wf_rebuild_bvh(self._h, _stream()), "rebuild_bvh")
 
     def set_nrc(self, cache, train: bool = True):
         """Attaches a NeuralRadianceCache (None detaches: the plain tracer)."""

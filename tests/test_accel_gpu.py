@@ -256,6 +256,47 @@ def test_host_entry_point_pinned_and_pageable(krr_lib, cuda):
     _assert_bits_equal(out2, want, "host entry point, mixed")
 
 
+@pytest.mark.parametrize("node_format", [0, 1])
+def test_refit_keeps_hits_exact(krr_lib, cuda, node_format):
+    """Boxes refitted over the tree of other positions: hits equal the
+    oracle's on the new positions (camera, bounce and shadow rays, shared
+    edges); a refit with the same positions changes nothing; a refit with
+    another triangle count is refused."""
+    from kiraray_gb300._lib import KrrError
+    from kiraray_gb300.accel import set_node_format
+    sc = scenes.large_scene(width=160, height=90, grid=256, n_spheres=40, sky_size=(64, 32))
+    tris = sc.world_triangles()
+    rng = np.random.default_rng(8)
+    moved = tris.reshape(-1, 3, 3).copy()
+    # a global shear, some triangles moved far (across the tree), all jittered
+    moved[..., 0] += 0.15 * moved[..., 1]
+    far = rng.choice(moved.shape[0], moved.shape[0] // 50, replace=False)
+    moved[far] += rng.normal(0.0, 20.0, (far.size, 1, 3)).astype(np.float32)
+    moved += rng.normal(0.0, 1e-3, moved.shape).astype(np.float32)
+    moved = moved.reshape(-1, 9).astype(np.float32)
+    acc = Accel(tris, node_format=node_format)
+    set_node_format(0)
+    rays = H.pinhole_rays(sc, jitter_seed=21)
+    before = _gpu_closest(acc, rays)
+    acc.refit(tris)
+    _assert_bits_equal(_gpu_closest(acc, rays), before, "same positions")
+    acc.refit(moved)
+    ob = O.Bvh(moved)
+    want = ob.closest(rays)
+    _assert_bits_equal(_gpu_closest(acc, rays), want, "refit camera")
+    b = H.bounce_rays(moved, rays, want, 5)
+    _assert_bits_equal(_gpu_closest(acc, b), ob.closest(b), "refit bounce")
+    assert np.array_equal(acc.trace_any(torch.from_numpy(b).cuda()).cpu().numpy(), ob.any(b))
+    g = H.grid_mesh(12)
+    r = H.vertex_edge_rays(12, 3)
+    ga = Accel(g + 0.5, node_format=node_format)
+    set_node_format(0)
+    ga.refit(g)
+    _assert_bits_equal(_gpu_closest(ga, r), O.closest_brute(g, r), "refit edges")
+    with pytest.raises(KrrError):
+        acc.refit(moved[:-1])
+
+
 @pytest.mark.parametrize("leaf,full_leaf", [(1, 1), (2, 2), (3, 3), (1, 2), (1, 3)])
 def test_leaf_sizes_keep_hits_identical(krr_lib, cuda, leaf, full_leaf):
     """Leaf children of 1-3 triangles, everywhere or only in full nodes: the

@@ -25,6 +25,40 @@ def _views():
     return sc, out
 
 
+def test_graph_replay_after_instance_update(krr_lib, cuda):
+    """An instance update refits the BVH in place, so a frame captured before
+    it replays the moved scene: equal to an ordinary frame of a pass built
+    from the moved scene."""
+    import copy
+    sc, views = _views()
+    moved = copy.deepcopy(sc)
+    mesh, xf = moved.instances[6]
+    xf = np.array(xf, np.float32)
+    xf[:, 3] += np.array([0.08, 0.0, -0.05], np.float32)
+    moved.instances[6] = (mesh, xf)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        pt = WavefrontPathTracer({"max_depth": 5})
+        pt.set_scene(sc)
+        pt.resize_views(views)
+        out = torch.empty((pt.n_pixels, 4), device="cuda")
+        pt.begin_frame_views(1)
+        pt.render_flat(out)
+        pt.capture_frame(out)
+        pt.update_instances([6], xf[None])
+        pt.launch_frame(2)
+        s.synchronize()
+        got = out.cpu().numpy().copy()
+        ref = WavefrontPathTracer({"max_depth": 5})
+        ref.set_scene(moved)
+        ref.resize_views(views)
+        ref.begin_frame_views(2)
+        want = ref.render_flat().cpu().numpy()
+        s.synchronize()
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    assert pt.device_errors() == 0
+
+
 def test_batched_views_equal_single_views(krr_lib, cuda):
     sc, views = _views()
     pt = WavefrontPathTracer({"max_depth": 5})

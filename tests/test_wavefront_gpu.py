@@ -231,8 +231,9 @@ def test_megakernel_rejects_media(krr_lib, cuda):
 
 
 def test_update_instances_equals_fresh_scene(krr_lib, cuda):
-    """Animated instances: moving instances and rebuilding gives the frame a
-    pass built from the moved scene renders, bit for bit."""
+    """Animated instances: moving instances (boxes refitted over the existing
+    tree) gives the frame a pass built from the moved scene renders, bit for
+    bit; so do a full rebuild afterwards and moving them back."""
     import copy
     sc = scenes.large_scene(width=64, height=48, grid=128, n_spheres=12, sky_size=(64, 32))
     moved = copy.deepcopy(sc)
@@ -256,6 +257,17 @@ def test_update_instances_equals_fresh_scene(krr_lib, cuda):
     fresh.begin_frame(3, moved.camera)
     b = fresh.render().cpu().numpy()
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    pt.rebuild_bvh()
+    pt.begin_frame(3, sc.camera)
+    assert np.array_equal(pt.render().cpu().numpy().view(np.uint32), b.view(np.uint32))
+    pt.update_instances(idx, np.stack([np.array(sc.instances[k][1], np.float32) for k in idx]))
+    pt.begin_frame(3, sc.camera)
+    back = pt.render().cpu().numpy()
+    orig = WavefrontPathTracer({"max_depth": 6})
+    orig.set_scene(sc)
+    orig.resize(64, 48)
+    orig.begin_frame(3, sc.camera)
+    assert np.array_equal(back.view(np.uint32), orig.render().cpu().numpy().view(np.uint32))
     assert pt.device_errors() == 0
 
 
