@@ -228,7 +228,9 @@ __device__ __forceinline__ int quant_exponent(float ext) {
 // node quads 0 and 2-4, quad 1 left to the caller; format 1: the float planes,
 // quads 0-11) and returns the node's bounds.  Used by the collapse and by the
 // refit, so that both quantise alike: every quantised box contains its child
-// box (floor/ceil, then stepped outwards while rounding left it inside).
+// box (floor/ceil, then stepped outwards while rounding left it inside).  An
+// empty slot gets the inverted box lo = 255, hi = 0 on every axis, which no
+// ray enters (its entry distance exceeds its exit distance by 255 steps).
 __device__ void write_node_boxes(float4 *np, int format, const V3 *slo, const V3 *shi, uint32_t imask,
                                  V3 &out_lo, V3 &out_hi) {
     V3 lo = v3(INFINITY), hi = v3(-INFINITY);
@@ -260,7 +262,10 @@ __device__ void write_node_boxes(float4 *np, int format, const V3 *slo, const V3
     uint32_t qlo[3][2] = {{0, 0}, {0, 0}, {0, 0}};
     uint32_t qhi[3][2] = {{0, 0}, {0, 0}, {0, 0}};
     for (int s = 0; s < 8; ++s) {
-        if (slo[s].x == INFINITY) continue;
+        if (slo[s].x == INFINITY) {
+            for (int k = 0; k < 3; ++k) qlo[k][s >> 2] |= 0xffu << (8 * (s & 3));
+            continue;
+        }
         for (int k = 0; k < 3; ++k) {
             float p = get(lo, k), e = escale[k];
             float a = floorf((get(slo[s], k) - p) / e);
@@ -567,10 +572,12 @@ __device__ __forceinline__ void trace_body(const float4 *__restrict__ nodes,
     }
 }
 
+// FMT: 0 compressed nodes, 1 float nodes, 2 compressed nodes whose leaf
+// children all hold one triangle (the default build; a simpler child mask).
 // Compressed nodes: eight blocks per SM (64 registers, no spills); the float
 // node format keeps the compiler's register choice.
 template <int MODE, bool STATS, int FMT>
-__global__ void __launch_bounds__(kTraceThreads, FMT == 0 ? 8 : 1)
+__global__ void __launch_bounds__(kTraceThreads, FMT != 1 ? 8 : 1)
 k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, TraceLaunch L,
         unsigned long long *stats) {
     trace_body<MODE, STATS, FMT>(nodes, tris, L, stats);
@@ -579,7 +586,7 @@ k_trace(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, Trace
 // The mixed launch is held to the closest-hit kernel's 8 blocks per SM (the
 // grid is sized for that occupancy).
 template <int FMT>
-__global__ void __launch_bounds__(kTraceThreads, FMT == 0 ? 8 : 1)
+__global__ void __launch_bounds__(kTraceThreads, FMT != 1 ? 8 : 1)
 k_trace_mixed(const float4 *__restrict__ nodes, const float4 *__restrict__ tris, TraceLaunch L) {
     trace_body<2, false, FMT>(nodes, tris, L, nullptr);
 }
@@ -605,7 +612,7 @@ int traversal_grid_size() {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<0, false, 0>, kTraceThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<0, false, 2>, kTraceThreads, 0);
     if (per_sm < 1) per_sm = 1;
     g_grid_size = sms * per_sm;
     return g_grid_size;
@@ -625,14 +632,19 @@ static int launch_trace(const krr_accel *a, const TraceLaunch &l, cudaStream_t s
     lt.refill_below = a->refill_below;
     lt.postpone_pct = a->postpone_pct;
     const int grid = traversal_grid_size();
+    const bool single = a->max_leaf == 1 && a->full_leaf == 1;
     if constexpr (MODE == 2) {
         if (a->node_format == 1)
             k_trace_mixed<1><<<grid, kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, lt);
+        else if (single)
+            k_trace_mixed<2><<<grid, kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, lt);
         else
             k_trace_mixed<0><<<grid, kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, lt);
     } else {
         if (a->node_format == 1)
             k_trace<MODE, STATS, 1><<<grid, kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, lt, stats);
+        else if (single)
+            k_trace<MODE, STATS, 2><<<grid, kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, lt, stats);
         else
             k_trace<MODE, STATS, 0><<<grid, kTraceThreads, 0, s>>>(a->d_nodes, a->d_tris, lt, stats);
     }

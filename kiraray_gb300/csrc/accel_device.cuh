@@ -85,6 +85,10 @@ __device__ __forceinline__ float plane256(uint32_t w, int k) {
 // maximum of the entry distances is a non-negative float, and the ordering
 // of non-negative floats is the ordering of their bit patterns; a negative
 // exit distance is a negative integer and fails the test, as it should.
+// SINGLE: every leaf child holds one triangle, so a child's bit is one shift
+// of 1 by its meta byte's position field (empty slots never hit: their boxes
+// are inverted).
+template <bool SINGLE>
 __device__ __forceinline__ void visit_node(const float4 *__restrict__ nodes, uint32_t child,
                                            const RayPre &r, V3 inv, int oct, float tmax,
                                            uint2 &ng, uint2 &tg) {
@@ -138,7 +142,7 @@ __device__ __forceinline__ void visit_node(const float4 *__restrict__ nodes, uin
         int tfz = __float_as_int(fmaf(plane256(c < 4 ? fz0 : fz1, k), dz, foz));
         int t0 = __vimax3_s32(tnx, tny, max(tnz, tmin_i));
         int t1 = __vimin3_s32(tfx, tfy, min(tfz, tlim_i));
-        uint32_t bits = (m >> 5) << (m & 31u);
+        uint32_t bits = SINGLE ? __funnelshift_l(0u, 1u, m) : (m >> 5) << (m & 31u);
         hitmask |= (t0 <= t1) ? bits : 0u;
     }
     uint32_t cimask = ew >> 24;
@@ -196,7 +200,7 @@ __device__ __forceinline__ void visit(const float4 *__restrict__ nodes, uint32_t
                                       const RayPre &r, V3 inv, V3 oinv, int oct, float tmax,
                                       uint2 &ng, uint2 &tg) {
     if (FMT == 1) visit_node_f(nodes, child, r, inv, oinv, oct, tmax, ng, tg);
-    else visit_node(nodes, child, r, inv, oct, tmax, ng, tg);
+    else visit_node<FMT == 2>(nodes, child, r, inv, oct, tmax, ng, tg);
 }
 
 __device__ __forceinline__ V3 box_inverse(V3 d) {
