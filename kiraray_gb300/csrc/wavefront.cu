@@ -560,12 +560,52 @@ __global__ void k_clamp_count(int32_t *count, int cap) {
     if (threadIdx.x == 0 && *count > cap) *count = cap;
 }
 
+// Radiance of an emissive hit (handleHit, integrator.cpp:78-90): emitted
+// radiance times throughput, MIS-weighted against light sampling.
+__device__ __forceinline__ V3 hit_light_radiance(const DevScene &s, int32_t light, V3 p, V3 nrm,
+                                                  V3 wo, V3 ctx_p, uint32_t bsdf_type, uint32_t depth,
+                                                  V3 thp, V3 pu, V3 pl, int nee) {
+    const float lsel_pdf = 1.f / (float)s.n_lights;
+    const DevLight &l = s.lights[light];
+    const DevInstance &I = s.instances[l.index];
+    V3 Le = area_L(I, nrm, wo) * thp;
+    if (nee && depth && !(bsdf_type & BSDF_DELTA)) {
+        float light_pdf = area_pdf(s, l, p, nrm, ctx_p) * lsel_pdf;
+        Le = Le / mean(pl * light_pdf + pu);
+    } else {
+        Le = Le / mean(pu);
+    }
+    return Le;
+}
+
+// Radiance of a miss (handleMiss, integrator.cpp:92-108): every infinite
+// light, MIS-weighted against light sampling, times throughput.
+__device__ __forceinline__ V3 miss_radiance(const DevScene &s, V3 dir, uint32_t bsdf_type,
+                                             uint32_t depth, V3 thp, V3 pu, V3 pl, int nee) {
+    const float lsel_pdf = 1.f / (float)s.n_lights;
+    V3 L = v3(0.f);
+    for (int k = 0; k < s.n_infinite; ++k) {
+        const DevInfinite &e = s.infinite[k];
+        if (nee && depth && !(bsdf_type & BSDF_DELTA)) {
+            float light_pdf = kInv4Pi * lsel_pdf;
+            L += env_Li(e, dir) / mean(pu + pl * light_pdf);
+        } else {
+            L += env_Li(e, dir) / mean(pu);
+        }
+    }
+    return thp * L;
+}
+
 // Routing of a closest hit (__closesthit__/__miss__Closest, device.cu:43-74).
 // Four blocks per SM (64 registers): the mesh gathers are latency-bound.
+// With `inline_lights` (render(), no media) the radiance of a miss and of an
+// emissive hit is added here instead of through the miss and hit-light
+// queues: a path has one item per bounce, so each pixel's sum gets the same
+// terms in the same order as handleHit/handleMiss after this stage.
 __global__ void __launch_bounds__(kThreads, 4)
 k_hit_process(DevScene s, Queue rq, const float4 *__restrict__ hits, Queue next, Queue miss,
               Queue hitl, Queue scat, Queue msq, int enable_medium, uint32_t *err, NrcHook hook,
-              PixelState ps) {
+              PixelState ps, int inline_lights, int nee) {
     int n = *rq.count;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 h = hits[i];
@@ -579,6 +619,13 @@ k_hit_process(DevScene s, Queue rq, const float4 *__restrict__ hits, Queue next,
                 if (j >= 0) {
                     copy_ray_item(rq, i, msq, j);
                     msq.at(7, j) = make_float4(INFINITY, 0.f, 0.f, fbits(KRR_MISS));
+                }
+            } else if (inline_lights) {
+                if (s.n_infinite > 0) {
+                    float4 c1 = rq.at(1, i), c3 = rq.at(3, i), c4 = rq.at(4, i), c5 = rq.at(5, i),
+                           c6 = rq.at(6, i);
+                    add_radiance(ps, ubits(c5.w), miss_radiance(s, f3(c1), ubits(c3.w), ubits(c4.w),
+                                                                f3(c4), f3(c5), f3(c6), nee));
                 }
             } else {
                 int j = push_slot(miss.count, miss.cap, err);
@@ -619,7 +666,11 @@ k_hit_process(DevScene s, Queue rq, const float4 *__restrict__ hits, Queue next,
         if (hook.mode && nrc_vertex(hook, s, sf, ps, ubits(c5.w), ubits(c4.w), ubits(c3.w), thp, h.x,
                                     dir, f3(c5), f3(c6), err))
             continue;
-        if (sf.light >= 0) {
+        if (sf.light >= 0 && inline_lights) {
+            add_radiance(ps, ubits(c5.w), hit_light_radiance(s, sf.light, sf.p, sf.n, sf.wo, f3(c2),
+                                                             ubits(c3.w), ubits(c4.w), thp, f3(c5),
+                                                             f3(c6), nee));
+        } else if (sf.light >= 0) {
             int j = push_slot(hitl.count, hitl.cap, err);
             if (j >= 0) {
                 hitl.at(0, j) = f4(sf.p, ibits(sf.light));
@@ -651,46 +702,23 @@ k_hit_process(DevScene s, Queue rq, const float4 *__restrict__ hits, Queue next,
 // handleHit, integrator.cpp:78-90
 __global__ void k_handle_hit(DevScene s, Queue hitl, PixelState ps, int nee) {
     int n = *hitl.count;
-    float lsel_pdf = 1.f / (float)s.n_lights;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 c0 = hitl.at(0, i), c1 = hitl.at(1, i), c2 = hitl.at(2, i), c3 = hitl.at(3, i);
         float4 c4 = hitl.at(4, i), c5 = hitl.at(5, i), c6 = hitl.at(6, i), c7 = hitl.at(7, i);
-        const DevLight &l = s.lights[sbits(c0.w)];
-        const DevInstance &I = s.instances[l.index];
-        V3 p = f3(c0), nrm = f3(c1), wo = f3(c2);
-        V3 Le = area_L(I, nrm, wo) * f3(c5);
-        uint32_t bsdf_type = ubits(c3.w), depth = ubits(c4.w), pixel = ubits(c5.w);
-        V3 pu = f3(c6), pl = f3(c7);
-        if (nee && depth && !(bsdf_type & BSDF_DELTA)) {
-            float light_pdf = area_pdf(s, l, p, nrm, f3(c3)) * lsel_pdf;
-            Le = Le / mean(pl * light_pdf + pu);
-        } else {
-            Le = Le / mean(pu);
-        }
-        add_radiance(ps, pixel, Le);
+        add_radiance(ps, ubits(c5.w),
+                     hit_light_radiance(s, sbits(c0.w), f3(c0), f3(c1), f3(c2), f3(c3), ubits(c3.w),
+                                        ubits(c4.w), f3(c5), f3(c6), f3(c7), nee));
     }
 }
 
 // handleMiss, integrator.cpp:92-108
 __global__ void k_handle_miss(DevScene s, Queue miss, PixelState ps, int nee) {
     int n = *miss.count;
-    float lsel_pdf = 1.f / (float)s.n_lights;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 c1 = miss.at(1, i), c3 = miss.at(3, i), c4 = miss.at(4, i), c5 = miss.at(5, i),
                c6 = miss.at(6, i);
-        V3 dir = f3(c1), pu = f3(c5), pl = f3(c6);
-        uint32_t bsdf_type = ubits(c3.w), depth = ubits(c4.w), pixel = ubits(c5.w);
-        V3 L = v3(0.f);
-        for (int k = 0; k < s.n_infinite; ++k) {
-            const DevInfinite &e = s.infinite[k];
-            if (nee && depth && !(bsdf_type & BSDF_DELTA)) {
-                float light_pdf = kInv4Pi * lsel_pdf;
-                L += env_Li(e, dir) / mean(pu + pl * light_pdf);
-            } else {
-                L += env_Li(e, dir) / mean(pu);
-            }
-        }
-        add_radiance(ps, pixel, f3(c4) * L);
+        add_radiance(ps, ubits(c5.w),
+                     miss_radiance(s, f3(c1), ubits(c3.w), ubits(c4.w), f3(c4), f3(c5), f3(c6), nee));
     }
 }
 
@@ -1958,10 +1986,6 @@ static TraceLaunch closest_launch(krr_wf *wf, int depth) {
     return l;
 }
 
-// Routing of the closest hits of ray queue `depth` (already traced into
-// wf->hits when `traced`).  With a cache attached, the paths that stop at it
-// are evaluated and their radiance added here, or, with `defer_cache`, left in
-// the query buffer for one evaluation at the end of the sample (render()).
 // L[pixel] += throughput x cache(query) for the queued cache queries.
 static int nrc_evaluate_queries(krr_wf *wf, cudaStream_t st) {
     KRR_TRY(nrc_query_device(wf->nrc, wf->nrc_q_in, wf->nrc_q_count(), wf->n, wf->nrc_q_out, st));
@@ -1970,8 +1994,16 @@ static int nrc_evaluate_queries(krr_wf *wf, cudaStream_t st) {
     return KRR_OK;
 }
 
+// Routing of the closest hits of ray queue `depth` (already traced into
+// wf->hits when `traced`).  With a cache attached, the paths that stop at it
+// are evaluated and their radiance added here, or, with `in_render`, left in
+// the query buffer for one evaluation at the end of the sample; `in_render`
+// without media also adds miss and emission radiance in the routing kernel
+// (render() then skips handleHit/handleMiss).
 static int closest_stage(krr_wf *wf, int depth, cudaStream_t st, bool traced,
-                         bool defer_cache = false) {
+                         bool in_render = false) {
+    const bool defer_cache = in_render;
+    const int inline_lights = in_render && !wf->medium ? 1 : 0;
     int cur = depth & 1;
     Queue rq = wf->q(cur);
     if (!traced) KRR_TRY(launch_trace_closest(&wf->accel, closest_launch(wf, depth), st));
@@ -1994,7 +2026,7 @@ static int closest_stage(krr_wf *wf, int depth, cudaStream_t st, bool traced,
     k_hit_process<<<wf->grid, kThreads, 0, st>>>(wf->scene, rq, wf->hits, wf->q(cur ^ 1),
                                                   wf->q(Q_MISS), wf->q(Q_HIT_LIGHT), wf->q(Q_SCATTER),
                                                   wf->q(Q_MEDIUM_SAMPLE), wf->medium ? 1 : 0, wf->err(),
-                                                  hook, wf->ps);
+                                                  hook, wf->ps, inline_lights, wf->params.nee);
     KRR_CUDA(cudaGetLastError());
     if (wf->nrc && !defer_cache) KRR_TRY(nrc_evaluate_queries(wf, st));
     return KRR_OK;
@@ -2106,9 +2138,11 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
         for (int depth = 0;; ++depth) {
             KRR_TRY(krr_wf_reset_queues(wf, depth, stream));
             KRR_TRY(closest_stage(wf, depth, st, traced, true));
-            if (wf->medium) KRR_TRY(krr_wf_sample_medium_interaction(wf, depth, stream));
-            KRR_TRY(krr_wf_handle_hit(wf, stream));
-            KRR_TRY(krr_wf_handle_miss(wf, stream));
+            if (wf->medium) {
+                KRR_TRY(krr_wf_sample_medium_interaction(wf, depth, stream));
+                KRR_TRY(krr_wf_handle_hit(wf, stream));
+                KRR_TRY(krr_wf_handle_miss(wf, stream));
+            }
             if (depth == wf->params.max_depth) break;
             if (wf->medium) KRR_TRY(krr_wf_sample_medium_scattering(wf, depth, stream));
             KRR_TRY(krr_wf_generate_scatter_rays(wf, depth, stream));
