@@ -51,3 +51,11 @@ def test_invalid_arguments_fail_without_gpu_work(krr_lib):
     p = _lib.WfParams()
     krr_lib.krr_wf_params_default(C.byref(p))
     assert p.nee == 1 and p.max_depth == 10 and abs(p.rr - 0.8) < 1e-7 and p.clamp_max == 1e3
+    # refit, rebuild and the BVH settings check their arguments before any GPU work
+    assert krr_lib.krr_accel_refit_triangles(None, None, 0, None) == 1
+    assert krr_lib.krr_wf_rebuild_bvh(None, None) == 1
+    assert krr_lib.krr_wf_update_instances(None, 0, None, None, None) == 1
+    for bad in (0, 4, -1):
+        assert krr_lib.krr_set_bvh_max_leaf(bad) == 1
+        assert krr_lib.krr_set_bvh_full_node_leaf(bad) == 1
+    assert krr_lib.krr_set_bvh_node_format(2) == 1
