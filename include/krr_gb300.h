@@ -182,7 +182,8 @@ int krr_accel_stats_get(const krr_accel *accel, krr_accel_stats *out);
 int krr_accel_destroy(krr_accel *accel);
 /* New positions for the triangles of a built structure (same count and order,
  * h_vertices float3[3*n]): the boxes are refitted bottom-up over the existing
- * tree (about 1/10 of a build), the device buffers keep their addresses and
+ * tree (a quarter of a rebuild's time at 10.9M triangles), the device
+ * buffers keep their addresses and
  * hits stay exact; the tree's quality follows the motion, so a caller
  * rebuilds after large changes.  The update path of an OptiX AS (used by
  * OptixSceneSingleLevel::updateAccelStructure, optix.cpp:618-642). */
@@ -282,7 +283,7 @@ int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *scene, void *stream);
 int krr_wf_update_instances(krr_wf *wf, int32_t n, const int32_t *h_indices,
                             const float *h_transforms, void *stream);
 /* Full BVH build over the current instance transforms (restores the tree's
- * quality after large motion; about 9 ms for 10.9M triangles).  Drops a
+ * quality after large motion; about 13 ms for 10.9M triangles).  Drops a
  * captured frame graph (capture again). */
 int krr_wf_rebuild_bvh(krr_wf *wf, void *stream);
 /* RenderPass::resize (integrator.cpp:181-184): reallocates queues. */
