@@ -182,11 +182,11 @@ int krr_accel_stats_get(const krr_accel *accel, krr_accel_stats *out);
 int krr_accel_destroy(krr_accel *accel);
 /* New positions for the triangles of a built structure (same count and order,
  * h_vertices float3[3*n]): the boxes are refitted bottom-up over the existing
- * tree (a quarter of a rebuild's time at 10.9M triangles), the device
- * buffers keep their addresses and
- * hits stay exact; the tree's quality follows the motion, so a caller
- * rebuilds after large changes.  The update path of an OptiX AS (used by
- * OptixSceneSingleLevel::updateAccelStructure, optix.cpp:618-642). */
+ * tree (a quarter of a rebuild's time at 10.9M triangles), the device buffers
+ * keep their addresses and hits stay exact; the tree's quality follows the
+ * motion, so a caller rebuilds after large changes.  The update path of an
+ * OptiX AS (used by OptixSceneSingleLevel::updateAccelStructure,
+ * optix.cpp:618-642). */
 int krr_accel_refit_triangles(krr_accel *accel, const float *h_vertices, int64_t n_triangles,
                               void *stream);
 
