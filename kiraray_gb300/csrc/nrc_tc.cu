@@ -600,19 +600,18 @@ int nrc_forward_tc(const NrcGrid &g, const NrcMlp &mlp, const float *d_in, const
     if (!configured) {
         KRR_CUDA(cudaFuncSetAttribute(k_nrc_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
+        // the largest shared-memory carveout, so that several CTAs fit
+        KRR_CUDA(cudaFuncSetAttribute(k_nrc_forward_tc, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      cudaSharedmemCarveoutMaxShared));
         configured = true;
     }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    // as many CTAs as fit on an SM (registers and shared memory allow three;
-    // their 3 x 64 tensor-memory columns fit in 512): the hash gathers of one
-    // CTA's tile overlap the MMA chains of the others
-    static int per_sm = 0;
-    if (!per_sm) {
-        KRR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_nrc_forward_tc, kTcThreads, smem));
-        per_sm = std::max(1, std::min(per_sm, (int)(512 / kTcCols)));
-    }
+    // FWD_PER_SM CTAs per SM (registers, 60 KB of shared memory and 64
+    // tensor-memory columns each allow it): the hash gathers of one CTA's tile
+    // overlap the MMA chains of the others
+    const int per_sm = 3;
     int64_t tiles = (cap + kTcRows - 1) / kTcRows;
     int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sms * per_sm));
     k_nrc_forward_tc<<<grid, kTcThreads, smem, s>>>(g, mlp.layers, d_in, d_count, cap, table, packed,
