@@ -3,7 +3,6 @@
 Every stage computes each pixel independently, so a view rendered inside a
 batch must equal the same view rendered alone with the same seed, bit for
 bit, and a replayed graph must equal an ordinary frame."""
-import math
 
 import numpy as np
 import pytest

@@ -2,7 +2,6 @@
 (per pixel, same tolerance as tests/test_wavefront_gpu.py)."""
 import numpy as np
 import pytest
-import torch
 
 from kiraray_gb300 import scenes
 from kiraray_gb300.wavefront import WavefrontPathTracer

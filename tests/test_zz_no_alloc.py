@@ -10,7 +10,6 @@ This file is collected last so that a run stopping at the first failure has
 already run every other test."""
 import ctypes as C
 
-import numpy as np
 import pytest
 import torch
 
