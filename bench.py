@@ -75,35 +75,87 @@ def make_workload(seed_offset: int = 0):
 
 
 class ClockSampler:
-    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+    """Samples the SM clock, its maximum, the power draw and the clock event
+    (throttle) reasons during the timed region.  NVML (the library nvidia-smi
+    reads) is polled every 2 ms so that a timed region of a few tens of ms
+    still gets a median; without NVML, `nvidia-smi -lms 200` is read instead.
+    Read-only: no clock or power setting is touched."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason* bits
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown",
+               0x4: "sw_power_cap"}
 
-    def __init__(self, index: int):
+    def __init__(self, index: int, period_s: float = 0.002):
         self.index = index
-        self.rows = []
+        self.period = period_s
+        self.rows = []          # (sm_mhz, max_mhz, reasons set)
         self.proc = None
+        self.stop = threading.Event()
+        self.nvml = None
+
+    def _nvml_open(self):
+        import ctypes as C
+        for name in ("libnvidia-ml.so.1", "libnvidia-ml.so"):
+            try:
+                lib = C.CDLL(name)
+                break
+            except OSError:
+                lib = None
+        if lib is None or lib.nvmlInit_v2() != 0:
+            return None
+        h = C.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.index), C.byref(h)) != 0:
+            return None
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons", None)
+        return lib, h, reasons
+
+    def _poll_nvml(self):
+        import ctypes as C
+        lib, h, reasons = self.nvml
+        clk, mx, r = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        while not self.stop.is_set():
+            if lib.nvmlDeviceGetClockInfo(h, 1, C.byref(clk)) == 0 and \
+                    lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0:
+                bits = r.value if reasons is not None and reasons(h, C.byref(r)) == 0 else 0
+                self.rows.append((float(clk.value), float(mx.value),
+                                  {n for b, n in self.REASONS.items() if bits & b}))
+            time.sleep(self.period)
+
+    def _read_smi(self):
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                self.rows.append((float(parts[1]), float(parts[2]),
+                                  {n for n, v in zip(names, parts[5:9]) if v == "Active"}))
 
     def __enter__(self):
+        try:
+            self.nvml = self._nvml_open()
+        except Exception:
+            self.nvml = None
+        if self.nvml is not None:
+            self.thread = threading.Thread(target=self._poll_nvml, daemon=True)
+            self.thread.start()
+            return self
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
                  "--format=csv,noheader,nounits", "-lms", "200"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread = threading.Thread(target=self._read_smi, daemon=True)
             self.thread.start()
         except OSError:
             self.proc = None
         return self
 
-    def _read(self):
-        for line in self.proc.stdout:
-            parts = [p.strip() for p in line.split(",")]
-            if len(parts) >= 9:
-                self.rows.append(parts)
-
     def __exit__(self, *a):
+        self.stop.set()
+        if self.nvml is not None:
+            self.thread.join(timeout=2)
         if self.proc:
             self.proc.terminate()
             try:
@@ -114,28 +166,50 @@ class ClockSampler:
     def summary(self):
         if not self.rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({n for r in self.rows for n, v in zip(names, r[5:9]) if v == "Active"})
-        return {"sm_mhz": float(np.median(sm)) if sm else None,
-                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(self.rows)}
+        sm = [r[0] for r in self.rows]
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(r[1] for r in self.rows),
+                "reasons": sorted(set().union(*(r[2] for r in self.rows))),
+                "samples": len(self.rows), "source": "nvml" if self.nvml else "nvidia-smi"}
 
 
-def profile_traffic():
-    """DRAM bytes per launch of the traversal kernel from the committed ncu
-    summary (profiles/), or None."""
+def profile_figures():
+    """Per-launch figures of the traversal kernel from the committed ncu
+    summary (profiles/trace_closest_large_scene.md): DRAM bytes, L2 bytes
+    and executed warp instructions of the camera-ray launch, keyed lines
+    `name: value`."""
     p = ROOT / "profiles" / "trace_closest_large_scene.md"
+    out = {}
     if not p.exists():
-        return None
+        return out
     for line in p.read_text().splitlines():
-        if line.startswith("dram_bytes_per_launch_full_size:"):
-            try:
-                return float(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
+        for key in ("dram_bytes_per_launch_full_size", "l2_bytes_per_launch_full_size",
+                    "warp_inst_per_launch_full_size", "l2_peak_gbs"):
+            if line.startswith(key + ":"):
+                try:
+                    out[key] = float(line.split(":", 1)[1].strip().split()[0])
+                except ValueError:
+                    pass
+    return out
+
+
+def l2_copy_gbs(dev) -> float:
+    """Achievable L2 bandwidth, measured: a device-to-device copy between two
+    24 MiB buffers (both resident in the 129 MB L2), read + write bytes per
+    second, best of five batches of 50 copies."""
+    import torch
+    a = torch.empty(24 << 20, dtype=torch.uint8, device=dev)
+    b = torch.empty_like(a)
+    s = torch.cuda.current_stream()
+    best = 0.0
+    for _ in range(6):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(50):
+            b.copy_(a)
+        e1.record(s)
+        e1.synchronize()
+        best = max(best, 2 * a.numel() * 50 / (e0.elapsed_time(e1) / 1e3) / 1e9)
+    return best
 
 
 def peaks():
@@ -146,32 +220,47 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def cpu_baseline(tris, ray_sets, seconds: float, threads: int):
-    """Oracle BVH closest-hit on a bounded sample of the same ray sets."""
+CPU_SAMPLE = 64   # the CPU arms trace 1 in 64 of each ray set
+
+
+def cpu_sample(tris, rays, H, bvh):
+    """The CPU arms' ray sample: 1 in 64 of the camera rays and 1 in 64 of
+    their first-bounce rays (made from the oracle's hits of every camera
+    ray, which equal the GPU's bit for bit, with the GPU arm's seed)."""
+    hits = bvh.closest(rays)
+    bounce = H.bounce_rays(tris, rays, hits, 2)
+    return np.concatenate([rays[::CPU_SAMPLE], bounce[::CPU_SAMPLE]])
+
+
+def cpu_rate(bvh, sample, threads: int, steps: int | None = None, seconds: float | None = None):
+    """Oracle closest-hit throughput on `sample` (all rays per step), over
+    `steps` steps or as many as fit in `seconds`."""
+    bvh.closest(sample[:4096], threads)
+    t0 = time.perf_counter()
+    k = 0
+    while True:
+        bvh.closest(sample, threads)
+        k += 1
+        el = time.perf_counter() - t0
+        if (steps is not None and k >= steps) or (seconds is not None and el >= seconds):
+            break
+    return sample.shape[0] * k / el / 1e6, k, el
+
+
+def cpu_baseline(tris, rays, H, seconds: float, threads: int):
+    """The oracle BVH's closest hit on the CPU arms' sample (same sample and
+    code path as --impl reference)."""
     from oracle import pyoracle as O
 
     t0 = time.perf_counter()
     bvh = O.Bvh(tris)
     build_s = time.perf_counter() - t0
-    sample = np.concatenate([r[::16] for r in ray_sets])
-    n = 0
-    t0 = time.perf_counter()
-    chunk = 65536
-    i = 0
-    while True:
-        part = sample[i:i + chunk]
-        if part.shape[0] == 0:
-            i = 0
-            continue
-        bvh.closest(part, threads)
-        n += part.shape[0]
-        i += chunk
-        if time.perf_counter() - t0 >= seconds:
-            break
-    el = time.perf_counter() - t0
-    return {"value": n / el / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
-            "sample": f"{n} rays (1-in-16 sample of the camera + first-bounce sets, cycled) in "
-                      f"{el:.1f} s; oracle BVH build {build_s:.1f} s not included"}
+    sample = cpu_sample(tris, rays, H, bvh)
+    v, k, el = cpu_rate(bvh, sample, threads, seconds=seconds)
+    return {"value": v, "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"{sample.shape[0]} rays per pass (1-in-{CPU_SAMPLE} of the camera and "
+                      f"first-bounce sets), {k} passes in {el:.1f} s; oracle BVH build "
+                      f"{build_s:.1f} s not included"}
 
 
 # Algorithmic HBM bytes per input item of each wavefront stage (queue
@@ -510,17 +599,11 @@ def run_reference(args, rank):
 
     threads = os.cpu_count() or 1
     bvh = O.Bvh(tris)
-    prim = bvh.closest(rays[::8], threads)
-    bounce = H.bounce_rays(tris, rays[::8], prim, 2)
-    sample = np.concatenate([rays[::64], bounce[::8]])
-    per_step = max(1, int(sample.shape[0]))
+    sample = cpu_sample(tris, rays, H, bvh)
+    per_step = int(sample.shape[0])
     for _ in range(args.warmup):
         bvh.closest(sample[:4096], threads)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        bvh.closest(sample, threads)
-    el = time.perf_counter() - t0
-    v = per_step * args.steps / el / 1e6
+    v, _, el = cpu_rate(bvh, sample, threads, steps=args.steps)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
@@ -529,8 +612,8 @@ def run_reference(args, rank):
                        "note": "CPU restatement of the path (oracle/): the reference traces "
                                "with OptiX on RT cores, which cannot be built or run here"},
             "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": threads, "kind": "port",
-                             "sample": f"{per_step} rays per step (1-in-64 camera rays + "
-                                       f"1-in-64 first-bounce rays)"},
+                             "sample": f"{per_step} rays per step (1-in-{CPU_SAMPLE} of the "
+                                       f"camera and first-bounce sets)"},
             "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -639,10 +722,13 @@ def run_ours(args, rank, world, local):
     peak, peak_kind = peaks()
     launch_s = kern_ms / 1e3 / (args.steps * len(sets))
     achieved = alg_bytes / len(sets) / launch_s / 1e9
-    traffic = profile_traffic()
+    prof = profile_figures()
+    traffic = prof.get("dram_bytes_per_launch_full_size")
+    l2_peak = l2_copy_gbs(dev)
+    cam_launch_s = set_ms[0] / 1e3 / args.steps
     if rank != 0:
         return
-    cpu = (cpu_baseline(tris, [rays_np, bounce_np], args.cpu_seconds, os.cpu_count() or 1)
+    cpu = (cpu_baseline(tris, rays_np, H, args.cpu_seconds, os.cpu_count() or 1)
            if args.cpu_seconds > 0 else None)
     clocks = clk.summary()
     frame = wavefront_frame(sc, acc, peak) if args.frame else None
@@ -669,12 +755,26 @@ def run_ours(args, rank, world, local):
                    "parallelism": f"replicas{world}"},
         "e2e": e2e,
         "gpu_launches": args.steps * len(sets),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "roofline": {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_kind": peak_kind,
-                     "note": f"algorithmic bytes = 48 B ray+hit + {node_size:.0f} B per 8-wide node visit + "
-                             "48 B per triangle test, per launch; they are served mostly by L2, "
-                             "so the fraction is against the measured HBM copy bandwidth"},
+                     "note": f"issue-bound traversal (ncu: instruction issue, not DRAM or L2, is the "
+                             f"limit); achieved = algorithmic bytes (48 B ray+hit + {node_size:.0f} B "
+                             "per 8-wide node visit + 48 B per triangle test) per launch / launch time, "
+                             "against the measured HBM copy bandwidth (of measured); those bytes are "
+                             "served mostly by L1 and L2, so `l2` gives the L2 figure",
+                     "l2": {"achieved_gbs": (prof["l2_bytes_per_launch_full_size"] / cam_launch_s / 1e9
+                                             if "l2_bytes_per_launch_full_size" in prof else None),
+                            "peak_gbs": l2_peak,
+                            "peak_kind": "measured here: L2-resident device copy, read + write bytes",
+                            "bytes_per_launch": prof.get("l2_bytes_per_launch_full_size"),
+                            "launch": "camera rays, 2,073,600 (ncu lts__t_bytes.sum of one launch)"},
+                     "issue": {"warp_inst_per_ray": (prof["warp_inst_per_launch_full_size"] /
+                                                     rays0.shape[0]
+                                                     if "warp_inst_per_launch_full_size" in prof
+                                                     else None),
+                               "nodes_per_ray": node_visits / n_per_step,
+                               "tris_per_ray": tri_tests / n_per_step}},
         "cpu_baseline": cpu,
         "clocks": clocks,
         "ray_sets_mrays_s": dict(set_mrays, **({"shadow": frame["shadow_mrays_s"]} if frame else {})),
@@ -683,6 +783,8 @@ def run_ours(args, rank, world, local):
         "config_frames": frames,
         "time_to_relmse": nrc,
     }
+    l2 = line["roofline"]["l2"]
+    l2["frac"] = l2["achieved_gbs"] / l2["peak_gbs"] if l2["achieved_gbs"] else None
     print(json.dumps(line))
 
 

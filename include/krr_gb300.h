@@ -175,6 +175,15 @@ int krr_set_bvh_max_leaf(int32_t triangles);
  * its own with two or three children.  Hits are the same with any setting. */
 int krr_set_bvh_full_node_leaf(int32_t triangles);
 
+/* Binary tree behind the BVHs built from now on, process-wide: 0 = Karras
+ * radix tree over 63-bit Morton codes of the centroids, each axis scaled to
+ * its own extent (default); 1 = PLOC, parallel locally-ordered clustering
+ * (Meister and Bittner 2018) over Morton codes on cubic cells, a tree of
+ * smaller surface area for a slower build; 2 = the radix tree on cubic
+ * cells.  Either is collapsed into the same 8-wide nodes; hits are the same
+ * with any builder. */
+int krr_set_bvh_builder(int32_t builder);
+
 /* Build from host arrays of world-space triangles: h_vertices float3[3*n]. */
 int krr_accel_create_from_triangles(const float *h_vertices, int64_t n_triangles,
                                     krr_accel **out, void *stream);
@@ -203,9 +212,23 @@ int krr_accel_trace_any(const krr_accel *accel, const krr_ray *d_rays, int64_t n
 /* Per-triangle any-hit mask (global triangle order); NULL = all opaque. */
 int krr_accel_set_mask(krr_accel *accel, const uint8_t *h_mask);
 
+/* Device-side error flags of the traces on this structure since the last
+ * call (cleared on read; synchronises the stream): bit 0 = a ray needed more
+ * traversal stack than the limit allows and was cut off.  A cut-off
+ * closest-hit ray reports t = NaN with prim = KRR_MISS; a cut-off any-hit ray
+ * reports occluded = 0xFF (counted as blocked).  The entry points that wait
+ * for their results (krr_accel_trace_stats, _noalloc, _closest_host) return
+ * KRR_ERR_OVERFLOW instead.  The reference stops on errors
+ * (src/util/check.h:8-51). */
+int krr_accel_device_errors(const krr_accel *accel, uint32_t *out_flags, void *stream);
+/* Traversal stack entries a ray may use, 1..48 (default 48).  The build
+ * rejects trees deeper than 48 levels, so with the default no ray is cut off;
+ * a smaller limit exercises the overflow path above. */
+int krr_accel_set_stack_limit(krr_accel *accel, int32_t entries);
+
 /* Counter-instrumented replay of a trace: h_counts[0] = 8-wide nodes visited,
  * h_counts[1] = triangles tested, summed over the n rays.  Used to compute
- * the algorithmic bytes per ray of the roofline. */
+ * the algorithmic bytes per ray of the roofline.  Synchronous. */
 int krr_accel_trace_stats(const krr_accel *accel, const krr_ray *d_rays, int64_t n,
                           int32_t any_hit, unsigned long long *h_counts, void *stream);
 
@@ -218,10 +241,13 @@ int krr_accel_trace_stats(const krr_accel *accel, const krr_ray *d_rays, int64_t
  * KRR_NOALLOC_MAX_RAYS rays (about 1 MiB), resident on every GPU that loads
  * the library until exit; n must be 1..KRR_NOALLOC_MAX_RAYS or the call
  * returns KRR_ERR_INVALID_ARGUMENT.  The first call on each device looks up
- * the array's device address (make it before any stream capture).  All calls
- * share the array, so calls that overlap on the GPU race; counters are
- * cleared at the start of each call.  Calls no cudaMalloc, cudaFree or other
- * allocating routine. */
+ * the array's device address and keeps it for the life of the process (a
+ * device reset after that first call is not supported).  The call is
+ * synchronous (it waits for the stream and writes h_counts), so it cannot
+ * be recorded by stream capture.  All calls share the array, so calls that
+ * overlap on the GPU race; counters are cleared at the start of each call.
+ * Calls no cudaMalloc, cudaFree or other allocating routine.  Returns
+ * KRR_ERR_OVERFLOW when the stack limit cut a ray off. */
 #define KRR_NOALLOC_MAX_RAYS 65536
 int krr_accel_trace_stats_noalloc(const krr_accel *accel, const krr_ray *d_rays, int64_t n,
                                   int32_t any_hit, unsigned long long *h_counts, void *stream);
@@ -267,10 +293,24 @@ typedef struct krr_wf_params {
 } krr_wf_params;
 
 void krr_wf_params_default(krr_wf_params *p);
+/* The pass's JSON parameters, as WavefrontPathTracer::from_json reads them
+ * (src/render/wavefront/integrator.h:85-103): "nee", "enable_medium",
+ * "max_depth", "rr", "enable_clamp", "clamp_max" (plus "spp", "seed",
+ * "independent_samples"); absent keys keep the defaults, other keys are
+ * ignored; malformed JSON or a key of the wrong type returns
+ * KRR_ERR_INVALID_ARGUMENT. */
+int krr_wf_params_from_json(const char *params_json, krr_wf_params *out);
 
 int krr_wf_create(const krr_wf_params *params, krr_wf **out);
+/* krr_wf_create from the pass's JSON parameters (the `params` object of a
+ * passes[] entry, RenderPassFactory::deserizeInstance, src/main/renderer.cpp:
+ * 274-286); NULL = all defaults. */
+int krr_wf_create_json(const char *params_json, krr_wf **out);
 int krr_wf_destroy(krr_wf *wf);
 int krr_wf_set_params(krr_wf *wf, const krr_wf_params *params);
+int krr_wf_get_params(const krr_wf *wf, krr_wf_params *out);
+/* Changes the keys present in params_json, keeping the others. */
+int krr_wf_set_params_json(krr_wf *wf, const char *params_json);
 /* RenderPass::setScene (integrator.cpp:186-203): uploads the scene and
  * builds the BVH. */
 int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *scene, void *stream);
@@ -374,8 +414,20 @@ int krr_wf_ray_queue(krr_wf *wf, int32_t depth, const float **d_origin_tmin,
  * Ld|pixel, pu|medium, pl|time; ...).  Valid until the next resize. */
 int krr_wf_queue_view(krr_wf *wf, int32_t queue, const float **d_base, int32_t *channels,
                       int32_t *capacity);
-/* Error flags raised by device code since the last call (cleared on read). */
+/* Error flags raised by device code since the last call (cleared on read):
+ * bit 0 traversal stack limit, bit 1 queue overflow (consumers then read
+ * only the queue's capacity), bit 2 loop limit (medium tracking, interface
+ * crossings, tensor-core waits). */
 int krr_wf_device_errors(krr_wf *wf, uint32_t *out_flags, void *stream);
+/* Bounds of the medium tracking loops of the launches after this call:
+ * null collisions per majorant walk (default 2^20) and null-interface
+ * crossings per shadow ray (default 64).  A walk that runs out ends (the
+ * path or shadow ray carries no further radiance) and raises bit 2 of
+ * krr_wf_device_errors; the reference loops without bound
+ * (src/render/wavefront/wavefront.h:34-139).  A captured frame keeps the
+ * limits it was captured with. */
+int krr_wf_set_loop_limits(krr_wf *wf, int32_t max_null_collisions,
+                           int32_t max_interface_crossings);
 /* The BVH of the current scene (owned by the pass). */
 int krr_wf_accel(krr_wf *wf, const krr_accel **out);
 
@@ -435,6 +487,23 @@ int krr_nrc_gradients(krr_nrc *nrc, const float *d_inputs, const float *d_target
 /* which: 0 = MLP weights [layer][out rows][64], 1 = hash table [entry][2]. */
 int krr_nrc_get_params(const krr_nrc *nrc, int32_t which, float *h_dst, int64_t count);
 int krr_nrc_set_params(krr_nrc *nrc, int32_t which, const float *h_src, int64_t count);
+/* Device-side status of the cache (synchronises the stream): out_flags =
+ * error flags of its kernels since the last call (bit 2: a bounded
+ * tensor-core wait gave up; cleared on read); out_diverged = 1 once a
+ * training step's loss was not finite.  A diverged cache takes no more
+ * training steps and a pass with it attached renders as the plain tracer
+ * (no path stops at the cache) until krr_nrc_set_params or krr_nrc_load
+ * gives it new parameters. */
+int krr_nrc_status(krr_nrc *nrc, uint32_t *out_flags, int32_t *out_diverged, void *stream);
+/* Checkpoint of the cache's training state to a file: FP32 weights and hash
+ * table with their Adam moments, the step counter and bias corrections, the
+ * configuration (training settings and scene box) and the divergence flag
+ * (a flat binary file with a header).  krr_nrc_load restores it into a cache
+ * with the same encoding and network shape (else KRR_ERR_INVALID_ARGUMENT);
+ * training then continues from the saved step.  Both synchronise the
+ * device.  The reference has no checkpoints. */
+int krr_nrc_save(const krr_nrc *nrc, const char *path);
+int krr_nrc_load(krr_nrc *nrc, const char *path);
 /* Attaches a cache to the pass (NULL detaches: the plain tracer).  With a
  * cache, paths of 1 in train_pixel_stride pixels run unbiased and record
  * training targets; the others stop at the vertex after their first

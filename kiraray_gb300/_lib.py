@@ -128,6 +128,9 @@ SIGNATURES = {
     "krr_accel_set_mask": (_I, [_P, _P]),
     "krr_accel_trace_closest_host": (_I, [_P, _P, C.c_int64, _P, _P]),
     "krr_accel_set_tuning": (_I, [_P, C.c_int32, C.c_int32]),
+    "krr_set_bvh_builder": (_I, [C.c_int32]),
+    "krr_accel_set_stack_limit": (_I, [_P, C.c_int32]),
+    "krr_accel_device_errors": (_I, [_P, C.POINTER(C.c_uint32), _P]),
     "krr_accel_autotune": (_I, [_P, _P, C.c_int64, C.c_int32, C.POINTER(C.c_int32),
                                 C.POINTER(C.c_int32), C.POINTER(C.c_float), _P]),
     "krr_accel_trace_stats": (_I, [_P, _P, C.c_int64, C.c_int32, C.POINTER(C.c_ulonglong), _P]),
@@ -137,6 +140,10 @@ SIGNATURES = {
     "krr_wf_create": (_I, [C.POINTER(WfParams), C.POINTER(_P)]),
     "krr_wf_destroy": (_I, [_P]),
     "krr_wf_set_params": (_I, [_P, C.POINTER(WfParams)]),
+    "krr_wf_get_params": (_I, [_P, C.POINTER(WfParams)]),
+    "krr_wf_params_from_json": (_I, [C.c_char_p, C.POINTER(WfParams)]),
+    "krr_wf_create_json": (_I, [C.c_char_p, C.POINTER(_P)]),
+    "krr_wf_set_params_json": (_I, [_P, C.c_char_p]),
     "krr_wf_set_scene": (_I, [_P, C.POINTER(SceneDesc), _P]),
     "krr_wf_resize": (_I, [_P, C.c_int32, C.c_int32]),
     "krr_wf_begin_frame": (_I, [_P, C.c_int64, C.POINTER(CameraDesc), _P]),
@@ -161,6 +168,7 @@ SIGNATURES = {
                               C.POINTER(C.c_int32)]),
     "krr_wf_device_errors": (_I, [_P, C.POINTER(C.c_uint32), _P]),
     "krr_wf_accel": (_I, [_P, C.POINTER(_P)]),
+    "krr_wf_set_loop_limits": (_I, [_P, C.c_int32, C.c_int32]),
     "krr_accumulate_f64": (_I, [_P, _P, C.c_int64, _P]),
     "krr_nrc_config_default": (None, [C.POINTER(NrcConfig)]),
     "krr_nrc_create": (_I, [C.POINTER(NrcConfig), C.POINTER(_P)]),
@@ -170,6 +178,9 @@ SIGNATURES = {
     "krr_nrc_train_step": (_I, [_P, _P, _P, C.c_int64, C.POINTER(C.c_float), _P]),
     "krr_nrc_gradients": (_I, [_P, _P, _P, C.c_int64, _P, _P, C.POINTER(C.c_float)]),
     "krr_nrc_get_params": (_I, [_P, C.c_int32, _P, C.c_int64]),
+    "krr_nrc_status": (_I, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_int32), _P]),
+    "krr_nrc_save": (_I, [_P, C.c_char_p]),
+    "krr_nrc_load": (_I, [_P, C.c_char_p]),
     "krr_nrc_set_params": (_I, [_P, C.c_int32, _P, C.c_int64]),
     "krr_wf_set_nrc": (_I, [_P, _P, C.c_int32]),
     "krr_image_error": (_I, [_P, C.c_double, _P, C.c_int64, C.c_int32, C.POINTER(C.c_double),

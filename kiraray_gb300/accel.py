@@ -31,6 +31,12 @@ def set_max_leaf(triangles: int) -> None:
     check(_lib.load().krr_set_bvh_max_leaf(triangles), "krr_set_bvh_max_leaf")
 
 
+def set_builder(builder: int) -> None:
+    """Binary tree of the BVHs built from now on: 0 radix tree (default),
+    1 PLOC clustering, 2 radix tree on cubic Morton cells."""
+    check(_lib.load().krr_set_bvh_builder(builder), "krr_set_bvh_builder")
+
+
 def set_full_node_leaf(triangles: int) -> None:
     """Largest leaf (1..3 triangles) among the children of a full node."""
     check(_lib.load().krr_set_bvh_full_node_leaf(triangles), "krr_set_bvh_full_node_leaf")
@@ -110,6 +116,18 @@ class Accel:
                                                 int(any_hit), counts, _stream()),
               "krr_accel_trace_stats")
         return int(counts[0]), int(counts[1])
+
+    def device_errors(self) -> int:
+        """Error flags raised by traces since the last call (bit 0: a ray was
+        cut off by the stack limit); synchronises the stream."""
+        f = C.c_uint32()
+        check(_lib.load().krr_accel_device_errors(self._h, C.byref(f), _stream()),
+              "krr_accel_device_errors")
+        return int(f.value)
+
+    def set_stack_limit(self, entries: int) -> None:
+        """Traversal stack entries a ray may use (1..48, default 48)."""
+        check(_lib.load().krr_accel_set_stack_limit(self._h, entries), "krr_accel_set_stack_limit")
 
     def set_tuning(self, refill_below: int = 20, postpone_pct: int = 0) -> None:
         check(_lib.load().krr_accel_set_tuning(self._h, refill_below, postpone_pct), "set_tuning")

@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "accel.h"
@@ -33,6 +34,8 @@ namespace krr {
 namespace {
 
 constexpr uint32_t kLeafBit = 0x80000000u;
+// best-hit marker of a ray whose traversal the stack limit cut off
+constexpr uint32_t kCutRay = KRR_MISS - 1u;
 constexpr int kBuildThreads = 256;
 
 __device__ __forceinline__ void atomic_min_f(float *addr, float v) {
@@ -86,9 +89,12 @@ __device__ __forceinline__ uint64_t spread21(uint32_t x) {
 }
 
 // Morton codes of centroids and margin-widened leaf boxes.
+// cubic: one cell size on all three axes (the largest centroid extent), so
+// that the code's splits follow the scene's proportions; otherwise each axis
+// is normalised by its own extent.
 __global__ void k_leaf_setup(const float *__restrict__ v, int64_t n, const float *bounds,
-                             float margin, uint64_t *keys, uint32_t *vals, float4 *leaf_lo,
-                             float4 *leaf_hi) {
+                             float margin, int cubic, uint64_t *keys, uint32_t *vals,
+                             float4 *leaf_lo, float4 *leaf_hi) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     V3 a = ld3(v + 9 * i), b = ld3(v + 9 * i + 3), c = ld3(v + 9 * i + 6);
@@ -96,9 +102,10 @@ __global__ void k_leaf_setup(const float *__restrict__ v, int64_t n, const float
     V3 ce = (lo + hi) * 0.5f;
     V3 cmin = ld3(bounds), cmax = ld3(bounds + 3);
     V3 ext = cmax - cmin;
+    const float emax = fmaxf(ext.x, fmaxf(ext.y, ext.z));
     float q[3];
     for (int k = 0; k < 3; ++k) {
-        float e = get(ext, k);
+        float e = cubic ? emax : get(ext, k);
         float t = e > 0.f ? (get(ce, k) - get(cmin, k)) / e : 0.5f;
         q[k] = fminf(fmaxf(t * 2097152.f, 0.f), 2097151.f);
     }
@@ -116,10 +123,10 @@ __device__ __forceinline__ int delta_fn(const uint64_t *k, int n, int i, int j) 
     return __clzll(a ^ b);
 }
 
-// Karras 2012 radix tree: internal node i covers [first, last].
+// Karras 2012 radix tree: internal node i covers the sorted leaves [first, last]
+// (count = last - first + 1 of them).
 __global__ void k_karras(const uint64_t *__restrict__ keys, int n, uint32_t *left,
-                         uint32_t *right, int *first, int *last, int *parent_int,
-                         int *parent_leaf) {
+                         uint32_t *right, int *count, int *parent_int, int *parent_leaf) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     int d = (delta_fn(keys, n, i, i + 1) - delta_fn(keys, n, i, i - 1)) >= 0 ? 1 : -1;
@@ -138,8 +145,7 @@ __global__ void k_karras(const uint64_t *__restrict__ keys, int n, uint32_t *lef
     } while (t > 1);
     int gamma = i + s * d + min(d, 0);
     int lo = min(i, j), hi = max(i, j);
-    first[i] = lo;
-    last[i] = hi;
+    count[i] = hi - lo + 1;
     if (lo == gamma) { left[i] = kLeafBit | gamma; parent_leaf[gamma] = i; }
     else { left[i] = gamma; parent_int[gamma] = i; }
     if (hi == gamma + 1) { right[i] = kLeafBit | (gamma + 1); parent_leaf[gamma + 1] = i; }
@@ -190,28 +196,125 @@ struct CollapseItem {
     int depth;
 };
 
+// Binary tree handed to the collapse (LBVH or PLOC): internal node i has
+// children left[i], right[i] (kLeafBit | sorted leaf, or an internal index),
+// bounds int_lo/int_hi[i] and count[i] leaves below it.
 struct BinTree {
     const uint32_t *left, *right;
-    const int *first, *last;
+    const int *count;
     const float4 *int_lo, *int_hi, *leaf_lo, *leaf_hi;
     const uint32_t *sorted_idx;
 };
 
-__device__ __forceinline__ void ref_info(const BinTree &t, uint32_t ref, V3 &lo, V3 &hi,
-                                         int &first, int &count) {
+__device__ __forceinline__ void ref_info(const BinTree &t, uint32_t ref, V3 &lo, V3 &hi, int &count) {
     if (ref & kLeafBit) {
         uint32_t k = ref & ~kLeafBit;
         lo = f3(t.leaf_lo[k]); hi = f3(t.leaf_hi[k]);
-        first = (int)k; count = 1;
+        count = 1;
     } else {
         lo = f3(t.int_lo[ref]); hi = f3(t.int_hi[ref]);
-        first = t.first[ref]; count = t.last[ref] - t.first[ref] + 1;
+        count = t.count[ref];
     }
+}
+
+// Triangles (original ids) under a subtree of at most three leaves.
+__device__ __forceinline__ int subtree_leaves(const BinTree &t, uint32_t ref, uint32_t out[3]) {
+    uint32_t st[4];
+    int sp = 0, n = 0;
+    st[sp++] = ref;
+    while (sp > 0 && n < 3) {
+        uint32_t r = st[--sp];
+        if (r & kLeafBit) { out[n++] = t.sorted_idx[r & ~kLeafBit]; continue; }
+        if (sp + 2 > 4) break;
+        st[sp++] = t.right[r];
+        st[sp++] = t.left[r];
+    }
+    return n;
 }
 
 __device__ __forceinline__ float half_area(V3 lo, V3 hi) {
     V3 e = hi - lo;
     return e.x * e.y + e.y * e.z + e.z * e.x;
+}
+
+// ------------------------------------------------------------------ PLOC
+// Parallel locally-ordered clustering (Meister and Bittner, IEEE TVCG 2018):
+// the clusters stay in Morton order; each looks for the cluster within
+// `radius` positions whose merged box has the smallest surface area (ties to
+// the smaller position, so the globally closest pair is always mutual and
+// every round merges); mutual nearest neighbours merge into a new internal
+// node at the smaller position, the other position drops out, and the
+// survivors are compacted in order.  Higher-quality trees than the radix
+// tree for the same Morton order.
+struct Cluster {
+    float4 lo;   // box min | ref bits (kLeafBit | sorted leaf, or internal node)
+    float4 hi;   // box max | unused
+};
+constexpr int kPlocRadius = 16;
+constexpr int kPlocThreads = 256;
+
+__global__ void k_ploc_init(int n, const float4 *__restrict__ leaf_lo,
+                            const float4 *__restrict__ leaf_hi, Cluster *c) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 lo = leaf_lo[i];
+    lo.w = __uint_as_float(kLeafBit | (uint32_t)i);
+    c[i] = Cluster{lo, leaf_hi[i]};
+}
+
+__global__ void __launch_bounds__(kPlocThreads)
+k_ploc_nn(const Cluster *__restrict__ c, int n, int r, uint32_t *__restrict__ nn) {
+    __shared__ float4 slo[kPlocThreads + 2 * kPlocRadius], shi[kPlocThreads + 2 * kPlocRadius];
+    const int base = blockIdx.x * kPlocThreads;
+    for (int k = threadIdx.x; k < kPlocThreads + 2 * r; k += blockDim.x) {
+        const int g = base - r + k;
+        if (g >= 0 && g < n) { slo[k] = c[g].lo; shi[k] = c[g].hi; }
+    }
+    __syncthreads();
+    const int i = base + threadIdx.x;
+    if (i >= n) return;
+    const V3 lo = f3(slo[threadIdx.x + r]), hi = f3(shi[threadIdx.x + r]);
+    unsigned long long best = ~0ull;
+    const int jlo = max(i - r, 0), jhi = min(i + r, n - 1);
+    for (int j = jlo; j <= jhi; ++j) {
+        if (j == i) continue;
+        const int k = j - base + r;
+        const float a = half_area(vmin(lo, f3(slo[k])), vmax(hi, f3(shi[k])));
+        best = min(best, ((unsigned long long)__float_as_uint(a) << 32) | (uint32_t)j);
+    }
+    nn[i] = (uint32_t)best;
+}
+
+__global__ void k_ploc_merge(const Cluster *__restrict__ c, const uint32_t *__restrict__ nn, int n,
+                             Cluster *out, uint8_t *keep, uint32_t *left, uint32_t *right,
+                             int *count, float4 *int_lo, float4 *int_hi, int *node_counter) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t j = nn[i];
+    const Cluster ci = c[i];
+    if (nn[j] != (uint32_t)i) {
+        out[i] = ci;
+        keep[i] = 1;
+        return;
+    }
+    if ((uint32_t)i > j) {
+        keep[i] = 0;
+        return;
+    }
+    const Cluster cj = c[j];
+    const uint32_t ri = __float_as_uint(ci.lo.w), rj = __float_as_uint(cj.lo.w);
+    const int node = atomicAdd(node_counter, 1);
+    left[node] = ri;
+    right[node] = rj;
+    count[node] = ((ri & kLeafBit) ? 1 : count[ri]) + ((rj & kLeafBit) ? 1 : count[rj]);
+    const float4 lo = make_float4(fminf(ci.lo.x, cj.lo.x), fminf(ci.lo.y, cj.lo.y),
+                                  fminf(ci.lo.z, cj.lo.z), 0.f);
+    const float4 hi = make_float4(fmaxf(ci.hi.x, cj.hi.x), fmaxf(ci.hi.y, cj.hi.y),
+                                  fmaxf(ci.hi.z, cj.hi.z), 0.f);
+    int_lo[node] = lo;
+    int_hi[node] = hi;
+    out[i] = Cluster{make_float4(lo.x, lo.y, lo.z, __uint_as_float((uint32_t)node)), hi};
+    keep[i] = 1;
 }
 
 __device__ __forceinline__ int quant_exponent(float ext) {
@@ -299,10 +402,10 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
 
     uint32_t ref[8];
     V3 clo[8], chi[8];
-    int cfirst[8], ccount[8];
+    int ccount[8];
     int nc = 1;
     ref[0] = item.bref;
-    ref_info(t, ref[0], clo[0], chi[0], cfirst[0], ccount[0]);
+    ref_info(t, ref[0], clo[0], chi[0], ccount[0]);
     // Greedily open the largest child that cannot be a leaf (more than three
     // triangles) or, once all can be leaves, the largest internal one while
     // slots remain.
@@ -321,9 +424,9 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
         if (best < 0 || !best_must) break;
         uint32_t r = ref[best];
         ref[best] = t.left[r];
-        ref_info(t, ref[best], clo[best], chi[best], cfirst[best], ccount[best]);
+        ref_info(t, ref[best], clo[best], chi[best], ccount[best]);
         ref[nc] = t.right[r];
-        ref_info(t, ref[nc], clo[nc], chi[nc], cfirst[nc], ccount[nc]);
+        ref_info(t, ref[nc], clo[nc], chi[nc], ccount[nc]);
         ++nc;
     }
     // A child that stays internal becomes a node of its own; in a full node a
@@ -386,8 +489,9 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
             imask |= 1u << s;
         } else {
             m = (((1u << ccount[c]) - 1u) << 5) | (uint32_t)tri_off;
-            for (int k = 0; k < ccount[c]; ++k)
-                leaf_order[tri_base + tri_off + k] = t.sorted_idx[cfirst[c] + k];
+            uint32_t tri[3];
+            const int nl = subtree_leaves(t, ref[c], tri);
+            for (int k = 0; k < nl; ++k) leaf_order[tri_base + tri_off + k] = tri[k];
             tri_off += ccount[c];
         }
         meta[s >> 2] |= m << (8 * (s & 3));
@@ -442,8 +546,10 @@ __device__ __forceinline__ void trace_body(const float4 *__restrict__ nodes,
                                            const float4 *__restrict__ tris, const TraceLaunch &L,
                                            unsigned long long *stats) {
     const int lane = threadIdx.x & 31;
-    const int64_t n_any = MODE == 2 ? (int64_t)*L.d_any_count : 0;
-    const int64_t n = (L.d_count ? (int64_t)*L.d_count : L.n) + n_any;
+    // queue counts are clamped to the queue capacity (a queue that overflowed
+    // has its flag raised and a count above its storage)
+    const int64_t n_any = MODE == 2 ? min((int64_t)*L.d_any_count, L.n) : 0;
+    const int64_t n = (L.d_count ? min((int64_t)*L.d_count, L.n) : L.n) + n_any;
     bool any_ray = MODE == 1;
     uint2 stack[kTraversalStack];
     int sp = 0;
@@ -507,8 +613,8 @@ __device__ __forceinline__ void trace_body(const float4 *__restrict__ nodes,
             uint32_t imask = ng.y >> 8;
             uint32_t child = ng.x + __popc(imask & ((1u << slot) - 1u));
             if (ng.y & 0xffu) {
-                if (sp < kTraversalStack) stack[sp++] = ng;
-                else { atomicOr(L.err, (int)kErrStackOverflow); done = true; }
+                if (sp < L.stack_limit) stack[sp++] = ng;
+                else { atomicOr(L.err, (int)kErrStackOverflow); done = true; best_prim = kCutRay; }
             }
             if (STATS) ++n_nodes;
             visit<FMT>(nodes, child, r, inv, oinv, oct, tmax, ng, tg);
@@ -519,7 +625,7 @@ __device__ __forceinline__ void trace_body(const float4 *__restrict__ nodes,
         if (L.postpone_pct > 0) {
             unsigned tri_lanes = __ballot_sync(0xffffffffu, active && tg.y != 0u);
             if (active && fresh && tg.y && __popc(tri_lanes) * 100 < L.postpone_pct * __popc(act) &&
-                (ng.y & 0xffu) && sp < kTraversalStack) {
+                (ng.y & 0xffu) && sp < L.stack_limit) {
                 stack[sp++] = make_uint2(tg.x, tg.y | 0x80000000u);
                 tg.y = 0;
             }
@@ -555,12 +661,15 @@ __device__ __forceinline__ void trace_body(const float4 *__restrict__ nodes,
         }
         if (!active) continue;
         if (done) {
+            // a ray cut off by the stack limit: occluded = 0xFF (counted as
+            // blocked), or a miss record with t = NaN
             if (any_ray) {
-                L.occluded[ray_id] = best_prim != KRR_MISS ? 1 : 0;
+                L.occluded[ray_id] = best_prim == kCutRay ? 0xFF : (best_prim != KRR_MISS ? 1 : 0);
             } else {
-                float4 h = best_prim != KRR_MISS
+                float4 h = best_prim < kCutRay
                                ? make_float4(tmax, best_b1, best_b2, __uint_as_float(best_prim))
-                               : make_float4(INFINITY, 0.f, 0.f, __uint_as_float(KRR_MISS));
+                               : make_float4(best_prim == kCutRay ? __int_as_float(0x7fffffff) : INFINITY,
+                                             0.f, 0.f, __uint_as_float(KRR_MISS));
                 L.hits[ray_id] = h;
             }
             active = false;
@@ -595,8 +704,8 @@ int g_grid_size = 0;
 
 // An empty scene: every ray misses (MODE as k_trace).
 __global__ void k_all_miss(TraceLaunch L, int mode) {
-    const int64_t n_any = mode == 2 ? (int64_t)*L.d_any_count : 0;
-    const int64_t n = (L.d_count ? (int64_t)*L.d_count : L.n) + n_any;
+    const int64_t n_any = mode == 2 ? min((int64_t)*L.d_any_count, L.n) : 0;
+    const int64_t n = (L.d_count ? min((int64_t)*L.d_count, L.n) : L.n) + n_any;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const bool any = mode == 1 || (mode == 2 && i < n_any);
@@ -631,6 +740,7 @@ static int launch_trace(const krr_accel *a, const TraceLaunch &l, cudaStream_t s
     TraceLaunch lt = l;
     lt.refill_below = a->refill_below;
     lt.postpone_pct = a->postpone_pct;
+    lt.stack_limit = a->stack_limit;
     const int grid = traversal_grid_size();
     const bool single = a->max_leaf == 1 && a->full_leaf == 1;
     if constexpr (MODE == 2) {
@@ -821,6 +931,46 @@ int accel_refit(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     return KRR_OK;
 }
 
+// PLOC rounds over the Morton-ordered leaves until one cluster is left (its
+// ref is the root).  Internal nodes are numbered in creation order.
+static int build_ploc(int n, const float4 *leaf_lo, const float4 *leaf_hi, uint32_t *left,
+                      uint32_t *right, int *count, float4 *int_lo, float4 *int_hi,
+                      uint32_t *root_ref, cudaStream_t s) {
+    DevBuf<Cluster> ca, cb;
+    DevBuf<uint32_t> nn;
+    DevBuf<uint8_t> keep;
+    DevBuf<int> counters;   // [0] node counter, [1] clusters kept
+    KRR_CUDA(ca.alloc(n)); KRR_CUDA(cb.alloc(n)); KRR_CUDA(nn.alloc(n)); KRR_CUDA(keep.alloc(n));
+    KRR_CUDA(counters.alloc(2));
+    KRR_CUDA(cudaMemsetAsync(counters.p, 0, 2 * sizeof(int), s));
+    size_t tmp_bytes = 0;
+    KRR_CUDA(cub::DeviceSelect::Flagged(nullptr, tmp_bytes, cb.p, keep.p, ca.p, counters.p + 1, n, s));
+    DevBuf<uint8_t> tmp;
+    KRR_CUDA(tmp.alloc(tmp_bytes));
+    k_ploc_init<<<blocks_for(n), kBuildThreads, 0, s>>>(n, leaf_lo, leaf_hi, ca.p);
+    KRR_CUDA(cudaGetLastError());
+    int m = n, rounds = 0;
+    while (m > 1) {
+        const int r = std::min(kPlocRadius, m - 1);
+        k_ploc_nn<<<blocks_for(m, kPlocThreads), kPlocThreads, 0, s>>>(ca.p, m, r, nn.p);
+        k_ploc_merge<<<blocks_for(m), kBuildThreads, 0, s>>>(ca.p, nn.p, m, cb.p, keep.p, left, right,
+                                                            count, int_lo, int_hi, counters.p);
+        KRR_CUDA(cudaGetLastError());
+        KRR_CUDA(cub::DeviceSelect::Flagged(tmp.p, tmp_bytes, cb.p, keep.p, ca.p, counters.p + 1, m, s));
+        int kept = m;
+        KRR_CUDA(cudaMemcpyAsync(&kept, counters.p + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+        KRR_CUDA(cudaStreamSynchronize(s));
+        if (kept >= m || kept < 1 || ++rounds > 100000)
+            return fail(KRR_ERR_OVERFLOW, "PLOC clustering made no progress (%d clusters)", m);
+        m = kept;
+    }
+    Cluster root{};
+    KRR_CUDA(cudaMemcpyAsync(&root, ca.p, sizeof(Cluster), cudaMemcpyDeviceToHost, s));
+    KRR_CUDA(cudaStreamSynchronize(s));
+    std::memcpy(root_ref, &root.lo.w, sizeof(uint32_t));
+    return KRR_OK;
+}
+
 int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     KRR_CHECK_ARG(n >= 0 && n < (int64_t)0x7fffffff, "triangle count out of range");
     accel_free(a);
@@ -851,8 +1001,9 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     KRR_CUDA(keys.alloc(n)); KRR_CUDA(keys2.alloc(n));
     KRR_CUDA(vals.alloc(n)); KRR_CUDA(vals2.alloc(n));
     KRR_CUDA(tlo.alloc(n)); KRR_CUDA(thi.alloc(n));
-    k_leaf_setup<<<blocks_for(n), kBuildThreads, 0, s>>>(d_v, n, bounds.p, margin, keys.p, vals.p,
-                                                          tlo.p, thi.p);
+    a->builder = default_builder();
+    k_leaf_setup<<<blocks_for(n), kBuildThreads, 0, s>>>(d_v, n, bounds.p, margin, a->builder != 0,
+                                                          keys.p, vals.p, tlo.p, thi.p);
     KRR_CUDA(cudaGetLastError());
 
     // sort by Morton code
@@ -874,20 +1025,25 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
 
     int64_t ni = std::max<int64_t>(n - 1, 1);
     DevBuf<uint32_t> left, right;
-    DevBuf<int> first, last, par_int, par_leaf, flags;
-    KRR_CUDA(left.alloc(ni)); KRR_CUDA(right.alloc(ni));
-    KRR_CUDA(first.alloc(ni)); KRR_CUDA(last.alloc(ni));
-    KRR_CUDA(par_int.alloc(ni)); KRR_CUDA(par_leaf.alloc(n)); KRR_CUDA(flags.alloc(ni));
+    DevBuf<int> count;
+    KRR_CUDA(left.alloc(ni)); KRR_CUDA(right.alloc(ni)); KRR_CUDA(count.alloc(ni));
     KRR_CUDA(ilo.alloc(ni)); KRR_CUDA(ihi.alloc(ni));
-    KRR_CUDA(cudaMemsetAsync(flags.p, 0, ni * sizeof(int), s));
-    if (n > 1) {
-        k_karras<<<blocks_for(n - 1), kBuildThreads, 0, s>>>(skeys, (int)n, left.p, right.p, first.p,
-                                                              last.p, par_int.p, par_leaf.p);
+    uint32_t root_ref = kLeafBit | 0u;
+    if (n > 1 && a->builder == 1) {
+        KRR_TRY(build_ploc((int)n, llo.p, lhi.p, left.p, right.p, count.p, ilo.p, ihi.p, &root_ref, s));
+    } else if (n > 1) {
+        DevBuf<int> par_int, par_leaf, flags;
+        KRR_CUDA(par_int.alloc(ni)); KRR_CUDA(par_leaf.alloc(n)); KRR_CUDA(flags.alloc(ni));
+        KRR_CUDA(cudaMemsetAsync(flags.p, 0, ni * sizeof(int), s));
+        k_karras<<<blocks_for(n - 1), kBuildThreads, 0, s>>>(skeys, (int)n, left.p, right.p, count.p,
+                                                              par_int.p, par_leaf.p);
         KRR_CUDA(cudaGetLastError());
         k_bottom_up<<<blocks_for(n), kBuildThreads, 0, s>>>((int)n, left.p, right.p, par_int.p,
                                                              par_leaf.p, llo.p, lhi.p, ilo.p, ihi.p,
                                                              flags.p);
         KRR_CUDA(cudaGetLastError());
+        root_ref = 0;
+        KRR_CUDA(cudaStreamSynchronize(s));   // the scratch above is freed on return
     }
 
     // collapse, level by level
@@ -904,9 +1060,9 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     KRR_CUDA(counters.alloc(8));
     int hc[8] = {1, 0, 0, 1, 0, 0, 0, 0};
     KRR_CUDA(cudaMemcpyAsync(counters.p, hc, sizeof(hc), cudaMemcpyHostToDevice, s));
-    CollapseItem root{n > 1 ? 0u : (kLeafBit | 0u), 0u, 1};
+    CollapseItem root{root_ref, 0u, 1};
     KRR_CUDA(cudaMemcpyAsync(qa.p, &root, sizeof(root), cudaMemcpyHostToDevice, s));
-    BinTree bt{left.p, right.p, first.p, last.p, ilo.p, ihi.p, llo.p, lhi.p, sidx};
+    BinTree bt{left.p, right.p, count.p, ilo.p, ihi.p, llo.p, lhi.p, sidx};
     int n_in = 1;
     a->level_first.assign({0, 1});
     CollapseItem *qin = qa.p, *qout = qb.p;
@@ -1003,6 +1159,16 @@ extern "C" int krr_accel_refit_triangles(krr_accel *a, const float *h_vertices, 
     return cuda_status(e, "cudaStreamSynchronize", __FILE__, __LINE__);
 }
 
+static int g_builder = 0;
+int krr::default_builder() { return g_builder; }
+
+extern "C" int krr_set_bvh_builder(int32_t builder) {
+    KRR_CHECK_ARG(builder >= 0 && builder <= 2,
+                  "builder must be 0 (radix tree), 1 (PLOC) or 2 (radix tree, cubic Morton cells)");
+    g_builder = builder;
+    return KRR_OK;
+}
+
 static int g_node_format = 0;
 static int g_max_leaf = 1;
 int krr::default_node_format() { return g_node_format; }
@@ -1074,6 +1240,34 @@ static TraceLaunch aos_launch(const krr_accel *a, const krr_ray *d_rays, int64_t
     return l;
 }
 
+// Reads and clears the traversal error flags at d_err (device) after the
+// stream's work; a raised stack-overflow flag becomes KRR_ERR_OVERFLOW.
+int krr::take_trace_errors(int *d_err, cudaStream_t s, uint32_t *out_flags) {
+    uint32_t flags = 0;
+    KRR_CUDA(cudaMemcpyAsync(&flags, d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    KRR_CUDA(cudaMemsetAsync(d_err, 0, sizeof(uint32_t), s));
+    KRR_CUDA(cudaStreamSynchronize(s));
+    if (out_flags) *out_flags = flags;
+    if (flags & kErrStackOverflow)
+        return fail(KRR_ERR_OVERFLOW, "traversal stack limit reached: rays were cut off (t = NaN / occluded = 0xFF)");
+    return KRR_OK;
+}
+
+extern "C" int krr_accel_device_errors(const krr_accel *a, uint32_t *out_flags, void *stream) {
+    KRR_CHECK_ARG(a && out_flags, "NULL argument");
+    *out_flags = 0;
+    if (!a->d_scratch) return KRR_OK;
+    int st = take_trace_errors(a->d_scratch + 4, as_stream(stream), out_flags);
+    return st == KRR_ERR_OVERFLOW ? KRR_OK : st;
+}
+
+extern "C" int krr_accel_set_stack_limit(krr_accel *a, int32_t entries) {
+    KRR_CHECK_ARG(a != nullptr, "accel is NULL");
+    KRR_CHECK_ARG(entries >= 1 && entries <= kTraversalStack, "stack limit must be 1..48 entries");
+    a->stack_limit = entries;
+    return KRR_OK;
+}
+
 extern "C" int krr_accel_trace_closest(const krr_accel *a, const krr_ray *d_rays, int64_t n,
                                        krr_hit *d_hits, void *stream) {
     KRR_CHECK_ARG(a && (n == 0 || (d_rays && d_hits)), "NULL argument");
@@ -1111,7 +1305,7 @@ extern "C" int krr_accel_trace_stats(const krr_accel *a, const krr_ray *d_rays, 
     if (st == KRR_OK) {
         KRR_CUDA(cudaMemcpyAsync(h_counts, d_counts, 2 * sizeof(unsigned long long),
                                  cudaMemcpyDeviceToHost, s));
-        KRR_CUDA(cudaStreamSynchronize(s));
+        st = take_trace_errors(l.err, s, nullptr);
     }
     cudaFree(d_counts);
     cudaFree(hits);
@@ -1157,8 +1351,7 @@ extern "C" int krr_accel_trace_closest_host(const krr_accel *a, const krr_ray *h
             TraceLaunch l = aos_launch(a, reinterpret_cast<const krr_ray *>(pr.devicePointer), n);
             l.hits = reinterpret_cast<float4 *>(ph.devicePointer);
             KRR_TRY(launch_trace_closest(a, l, s));
-            KRR_CUDA(cudaStreamSynchronize(s));
-            return KRR_OK;
+            return take_trace_errors(l.err, s, nullptr);
         }
     }
     // Otherwise (pageable memory, or no coherent link): chunks of rays are
@@ -1208,6 +1401,7 @@ extern "C" int krr_accel_trace_closest_host(const krr_accel *a, const krr_ray *h
     cudaEventRecord(m->stage_ev[1], aux);
     cudaStreamWaitEvent(s, m->stage_ev[1], 0);
     check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    if (st == KRR_OK) st = take_trace_errors(a->d_scratch + 4, s, nullptr);
     return st;
 }
 

@@ -46,9 +46,11 @@ struct krr_accel {
     float scene_lo[3] = {0, 0, 0}, scene_hi[3] = {0, 0, 0};
     int refill_below = 20;       // traversal tuning (krr_accel_set_tuning)
     int postpone_pct = 0;
+    int stack_limit = 48;        // krr_accel_set_stack_limit (kTraversalStack by default)
     int node_format = 0;         // 0 compressed (80 B), 1 float (224 B)
     int max_leaf = 1;            // triangles per leaf child (1..3)
     int full_leaf = 1;           // triangles per leaf child of a full node (max_leaf..3)
+    int builder = 0;             // binary tree: 0 radix tree, 1 PLOC, 2 radix tree on cubic cells
     // host-buffer entry point (krr_accel_trace_closest_host): device staging
     // for rays (2 float4 each) and hits, grown on demand, and a second stream
     // with two events, kept across calls so that a call allocates nothing
@@ -71,6 +73,7 @@ constexpr int kNodeQuads[2] = {5, 14};   // float4 per node, by node format
 int default_node_format();
 int default_max_leaf();   // krr_set_bvh_max_leaf
 int default_full_leaf();  // krr_set_bvh_full_node_leaf
+int default_builder();    // krr_set_bvh_builder
 constexpr int kTraceThreads = 128;
 
 // Build from device world-space vertices (float3 x 3 per triangle).
@@ -84,14 +87,15 @@ struct TraceLaunch {
     const float4 *ray_o;      // origin.xyz, tmin
     const float4 *ray_d;      // direction.xyz, tmax
     int ray_stride;           // float4 stride between consecutive rays
-    int64_t n;                // ray count if d_count == nullptr
-    const int *d_count;       // device ray count (queue counter) or nullptr
+    int64_t n;                // ray count if d_count == nullptr, else the queue capacity
+    const int *d_count;       // device ray count (queue counter, read as min(*d_count, n)) or nullptr
     float4 *hits;             // closest: t, b1, b2, prim bits
     uint8_t *occluded;        // any-hit output
     int *counter;             // scratch work counter (zeroed by the launcher)
     int *err;                 // device error flags
     int refill_below;         // refill a warp's idle lanes when fewer lanes are busy
     int postpone_pct;         // postpone triangles when fewer % of busy lanes have some
+    int stack_limit;          // traversal stack entries a ray may use (1..kTraversalStack)
     // Mixed launches only: an any-hit ray set traced in the same launch as
     // the closest-hit set above (same stride); its rays take indices
     // [0, *d_any_count) of the shared work counter.
@@ -107,5 +111,8 @@ int launch_trace_any(const krr_accel *a, const TraceLaunch &l, cudaStream_t s);
 // latency tail of the longest ray is paid once.
 int launch_trace_mixed(const krr_accel *a, const TraceLaunch &l, cudaStream_t s);
 int traversal_grid_size();
+// Reads and clears the traversal error flags (device int at d_err) after the
+// stream's work; KRR_ERR_OVERFLOW if a ray was cut off by the stack limit.
+int take_trace_errors(int *d_err, cudaStream_t s, uint32_t *out_flags);
 
 }  // namespace krr

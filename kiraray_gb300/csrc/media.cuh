@@ -11,8 +11,6 @@
 
 namespace krr {
 
-constexpr int kMaxNullCollisions = 1 << 20;   // bounded tracking loops
-constexpr int kMaxInterfaceCrossings = 64;    // bounded shadow segments
 
 struct MediumProps {
     V3 sigma_a, sigma_s;
@@ -233,7 +231,7 @@ __device__ __forceinline__ V3 hg_sample(float g0, V3 wo, float u0, float u1, flo
 // over null collisions is bounded; running out sets an error flag and stops.
 template <typename F>
 __device__ V3 sample_t_maj(const DevMedium &m, V3 o, V3 d, float tmax, Pcg &rng, int ch,
-                           uint32_t *err, bool &aborted, F &&cb) {
+                           int max_null, uint32_t *err, bool &aborted, F &&cb) {
     aborted = false;
     tmax *= length(d);
     d = normalize(d);
@@ -252,7 +250,7 @@ __device__ V3 sample_t_maj(const DevMedium &m, V3 o, V3 d, float tmax, Pcg &rng,
         }
         float tmin = seg.tmin;
         while (true) {
-            if (++guard > kMaxNullCollisions) {
+            if (++guard > max_null) {
                 atomicOr(err, (uint32_t)kErrLoopLimit);
                 aborted = true;
                 return v3(1.f);

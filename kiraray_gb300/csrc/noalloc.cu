@@ -20,8 +20,14 @@
 // Set-up: host code cannot use the array's name as a device address (on the
 // host it names a stand-in object, not device memory), so the first call on
 // each device looks the address up with cudaGetSymbolAddress, with that
-// device current, and caches it.  Make that first call on a device before
-// any stream capture begins on it.
+// device current, and caches it for the life of the process: a device reset
+// (cudaDeviceReset) after that first call is not supported.
+//
+// The call is synchronous: it waits for the stream and copies the counts to
+// the caller's host array before it returns, so it cannot be recorded into
+// a CUDA graph by stream capture.  A traversal cut off by the stack limit
+// (krr_accel_set_stack_limit) makes it return KRR_ERR_OVERFLOW, as the
+// allocating entry point does.
 #include <mutex>
 
 #include "accel.h"
@@ -94,6 +100,5 @@ extern "C" int krr_accel_trace_stats_noalloc(const krr_accel *a, const krr_ray *
     KRR_TRY(launch_trace_stats(a, l, any_hit != 0, counts, s));
     KRR_CUDA(cudaMemcpyAsync(h_counts, counts, 2 * sizeof(unsigned long long),
                              cudaMemcpyDeviceToHost, s));
-    KRR_CUDA(cudaStreamSynchronize(s));
-    return KRR_OK;
+    return take_trace_errors(err, s, nullptr);
 }

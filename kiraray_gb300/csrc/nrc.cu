@@ -292,7 +292,11 @@ __global__ void k_encode_bwd(NrcGrid g, const float *__restrict__ in, const floa
 
 // Adam on an FP32 master array; writes the BF16 copy and clears the gradient.
 // Advances the device step counter and stores the bias corrections.
-__global__ void k_adam_step(int64_t *step, double b1, double b2) {
+// A loss that is not finite marks the cache as diverged (err[1]); a diverged
+// cache takes no further steps.
+__global__ void k_adam_step(int64_t *step, double b1, double b2, const float *loss, uint32_t *err) {
+    if (!isfinite(*loss)) err[1] = 1u;
+    if (err[1]) return;
     int64_t t = *step + 1;
     *step = t;
     float *bc = reinterpret_cast<float *>(step + 1);
@@ -339,7 +343,14 @@ __device__ __forceinline__ void adam_store4(float *m, float *v, float *w, float 
 
 __global__ void k_adam(float *__restrict__ w, float *__restrict__ m, float *__restrict__ v,
                        float *__restrict__ grad, __nv_bfloat16 *__restrict__ wb, int64_t n, float lr,
-                       float b1, float b2, float eps, float grad_scale, const int64_t *__restrict__ step) {
+                       float b1, float b2, float eps, float grad_scale, const int64_t *__restrict__ step,
+                       const uint32_t *__restrict__ diverged) {
+    if (*diverged) {   // keep the parameters; drop the gradient
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+             i += (int64_t)gridDim.x * blockDim.x)
+            grad[i] = 0.f;
+        return;
+    }
     AdamArgs a{lr, b1, b2, eps, grad_scale, reinterpret_cast<const float *>(step + 1)[0],
                reinterpret_cast<const float *>(step + 1)[1]};
     const int64_t n4 = n >> 2;
@@ -457,6 +468,8 @@ NrcView nrc_view(const krr_nrc *n) { return NrcView{n->grid, n->mlp, n->table, n
 int64_t nrc_batch_size(const krr_nrc *n) { return n->cfg.batch_size; }
 int32_t nrc_train_stride(const krr_nrc *n) { return n->cfg.train_pixel_stride; }
 float nrc_termination_spread(const krr_nrc *n) { return n->cfg.termination_spread; }
+const uint32_t *nrc_diverged_flag(const krr_nrc *n) { return n->err + 1; }
+uint32_t *nrc_error_flags(krr_nrc *n) { return n->err; }
 
 int nrc_query_device(krr_nrc *n, const float *d_inputs, const int32_t *d_count, int64_t cap,
                      float *d_out, cudaStream_t s) {
@@ -525,15 +538,15 @@ int nrc_train_device(krr_nrc *n, const float *d_inputs, const float *d_targets,
     const float scale = n->cfg.loss_scale;
     // Adam
     const krr_nrc_config &c = n->cfg;
-    k_adam_step<<<1, 1, 0, s>>>(n->step, (double)c.beta1, (double)c.beta2);
+    k_adam_step<<<1, 1, 0, s>>>(n->step, (double)c.beta1, (double)c.beta2, n->loss, n->err);
     k_adam<<<grid_for(n->mlp.n_params), kThreads, 0, s>>>(n->w_master, n->w_m, n->w_v, n->w_grad,
                                                            n->weights, n->mlp.n_params, c.learning_rate,
                                                            c.beta1, c.beta2, c.epsilon, 1.f / scale,
-                                                           n->step);
+                                                           n->step, n->err + 1);
     int64_t tn = (int64_t)n->n_entries * n->grid.features;
     k_adam<<<grid_for(tn), kThreads, 0, s>>>(n->table_master, n->table_m, n->table_v, n->table_grad,
                                              n->table, tn, c.learning_rate, c.beta1, c.beta2,
-                                             c.epsilon, 1.f / scale, n->step);
+                                             c.epsilon, 1.f / scale, n->step, n->err + 1);
     KRR_CUDA(cudaGetLastError());
     return pack_weights(n, s);
 }
@@ -729,6 +742,133 @@ extern "C" int krr_nrc_set_params(krr_nrc *n, int32_t which, const float *h_src,
     KRR_CUDA(cudaMemcpy(dst, h_src, total * 4, cudaMemcpyHostToDevice));
     k_to_bf16<<<grid_for(total), kThreads>>>(dst, bdst, total);
     if (which == 0) KRR_TRY(pack_weights(n, 0));
+    KRR_CUDA(cudaMemset(n->err + 1, 0, sizeof(uint32_t)));   // new parameters: not diverged
+    KRR_CUDA(cudaDeviceSynchronize());
+    return KRR_OK;
+}
+
+extern "C" int krr_nrc_status(krr_nrc *n, uint32_t *out_flags, int32_t *out_diverged, void *stream) {
+    KRR_CHECK_ARG(n != nullptr, "NULL argument");
+    cudaStream_t s = as_stream(stream);
+    uint32_t w[2] = {0, 0};
+    KRR_CUDA(cudaMemcpyAsync(w, n->err, sizeof(w), cudaMemcpyDeviceToHost, s));
+    KRR_CUDA(cudaMemsetAsync(n->err, 0, sizeof(uint32_t), s));
+    KRR_CUDA(cudaStreamSynchronize(s));
+    if (out_flags) *out_flags = w[0];
+    if (out_diverged) *out_diverged = w[1] ? 1 : 0;
+    return KRR_OK;
+}
+
+// Checkpoint file: a fixed header, then the FP32 arrays in this order: MLP
+// weights, their Adam moments m and v, hash table, its moments m and v.
+namespace {
+struct NrcFileHeader {
+    char magic[8];              // "KRRNRC01"
+    uint32_t header_bytes;      // sizeof(NrcFileHeader)
+    uint32_t config_bytes;      // sizeof(krr_nrc_config)
+    krr_nrc_config cfg;
+    int64_t n_params;
+    int64_t n_table_values;     // entries x 2
+    int64_t step;
+    float bias_correction[2];
+    uint32_t diverged;
+    uint32_t reserved;
+};
+constexpr char kNrcMagic[8] = {'K', 'R', 'R', 'N', 'R', 'C', '0', '1'};
+
+bool same_structure(const krr_nrc_config &a, const krr_nrc_config &b) {
+    return a.n_levels == b.n_levels && a.features_per_level == b.features_per_level &&
+           a.log2_table_size == b.log2_table_size && a.base_resolution == b.base_resolution &&
+           a.max_resolution == b.max_resolution && a.hidden_layers == b.hidden_layers;
+}
+}  // namespace
+
+extern "C" int krr_nrc_save(const krr_nrc *n, const char *path) {
+    KRR_CHECK_ARG(n && path, "NULL argument");
+    KRR_CUDA(cudaDeviceSynchronize());
+    NrcFileHeader h{};
+    std::memcpy(h.magic, kNrcMagic, 8);
+    h.header_bytes = sizeof(NrcFileHeader);
+    h.config_bytes = sizeof(krr_nrc_config);
+    h.cfg = n->cfg;
+    h.n_params = n->mlp.n_params;
+    h.n_table_values = (int64_t)n->n_entries * 2;
+    unsigned char st[16];
+    KRR_CUDA(cudaMemcpy(st, n->step, 16, cudaMemcpyDeviceToHost));
+    std::memcpy(&h.step, st, 8);
+    std::memcpy(h.bias_correction, st + 8, 8);
+    uint32_t w[2];
+    KRR_CUDA(cudaMemcpy(w, n->err, sizeof(w), cudaMemcpyDeviceToHost));
+    h.diverged = w[1];
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return fail(KRR_ERR_INVALID_ARGUMENT, "krr_nrc_save: cannot open %s", path);
+    bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1;
+    std::vector<float> buf;
+    const float *arrays[6] = {n->w_master, n->w_m, n->w_v, n->table_master, n->table_m, n->table_v};
+    for (int k = 0; k < 6 && ok; ++k) {
+        const size_t cnt = (size_t)(k < 3 ? h.n_params : h.n_table_values);
+        buf.resize(cnt);
+        if (cudaMemcpy(buf.data(), arrays[k], cnt * 4, cudaMemcpyDeviceToHost) != cudaSuccess) {
+            std::fclose(f);
+            return fail(KRR_ERR_CUDA, "krr_nrc_save: device copy failed");
+        }
+        ok = std::fwrite(buf.data(), 4, cnt, f) == cnt;
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) return fail(KRR_ERR_INVALID_ARGUMENT, "krr_nrc_save: write to %s failed", path);
+    return KRR_OK;
+}
+
+extern "C" int krr_nrc_load(krr_nrc *n, const char *path) {
+    KRR_CHECK_ARG(n && path, "NULL argument");
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return fail(KRR_ERR_INVALID_ARGUMENT, "krr_nrc_load: cannot open %s", path);
+    NrcFileHeader h{};
+    const bool hdr = std::fread(&h, sizeof(h), 1, f) == 1;
+    if (!hdr || std::memcmp(h.magic, kNrcMagic, 8) != 0 || h.header_bytes != sizeof(NrcFileHeader) ||
+        h.config_bytes != sizeof(krr_nrc_config)) {
+        std::fclose(f);
+        return fail(KRR_ERR_INVALID_ARGUMENT, "krr_nrc_load: %s is not a cache checkpoint", path);
+    }
+    if (!same_structure(h.cfg, n->cfg) || h.n_params != n->mlp.n_params ||
+        h.n_table_values != (int64_t)n->n_entries * 2) {
+        std::fclose(f);
+        return fail(KRR_ERR_INVALID_ARGUMENT,
+                    "krr_nrc_load: the checkpoint's encoding or network shape differs from the cache's");
+    }
+    KRR_CUDA(cudaDeviceSynchronize());
+    std::vector<float> buf;
+    float *arrays[6] = {n->w_master, n->w_m, n->w_v, n->table_master, n->table_m, n->table_v};
+    for (int k = 0; k < 6; ++k) {
+        const size_t cnt = (size_t)(k < 3 ? h.n_params : h.n_table_values);
+        buf.resize(cnt);
+        if (std::fread(buf.data(), 4, cnt, f) != cnt) {
+            std::fclose(f);
+            return fail(KRR_ERR_INVALID_ARGUMENT, "krr_nrc_load: %s is truncated", path);
+        }
+        KRR_CUDA(cudaMemcpy(arrays[k], buf.data(), cnt * 4, cudaMemcpyHostToDevice));
+    }
+    std::fclose(f);
+    // training settings (learning rate, batch, stride, ...) and the scene box
+    // the table was trained over come with the checkpoint
+    n->cfg = h.cfg;
+    if (n->cfg.train_pixel_stride < 1) n->cfg.train_pixel_stride = 1;
+    for (int a = 0; a < 3; ++a) {
+        n->grid.lo[a] = h.cfg.scene_lo[a];
+        const float e = h.cfg.scene_hi[a] - h.cfg.scene_lo[a];
+        n->grid.inv_extent[a] = e > 0.f ? 1.f / e : 1.f;
+    }
+    unsigned char st[16];
+    std::memcpy(st, &h.step, 8);
+    std::memcpy(st + 8, h.bias_correction, 8);
+    KRR_CUDA(cudaMemcpy(n->step, st, 16, cudaMemcpyHostToDevice));
+    uint32_t w[2] = {0, h.diverged};
+    KRR_CUDA(cudaMemcpy(n->err, w, sizeof(w), cudaMemcpyHostToDevice));
+    KRR_CUDA(cudaMemset(n->w_grad, 0, (size_t)h.n_params * 4));
+    KRR_CUDA(cudaMemset(n->table_grad, 0, (size_t)h.n_table_values * 4));
+    k_to_bf16<<<grid_for(h.n_params), kThreads>>>(n->w_master, n->weights, h.n_params);
+    k_to_bf16<<<grid_for(h.n_table_values), kThreads>>>(n->table_master, n->table, h.n_table_values);
+    KRR_TRY(pack_weights(n, 0));
     KRR_CUDA(cudaDeviceSynchronize());
     return KRR_OK;
 }

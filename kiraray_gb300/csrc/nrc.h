@@ -101,6 +101,12 @@ int nrc_forward_tc(const NrcGrid &g, const NrcMlp &mlp, const float *d_in, const
                    int64_t cap, const __nv_bfloat16 *table, const uint8_t *packed, float *d_out,
                    __nv_bfloat16 *acts, uint32_t *err, cudaStream_t s);
 int32_t nrc_train_stride(const krr_nrc *n);
+// Device word that is non-zero once a training step's loss was not finite:
+// the cache has diverged, takes no further Adam steps, and the pass runs the
+// plain tracer (no path stops at it) until new parameters are loaded.
+const uint32_t *nrc_diverged_flag(const krr_nrc *n);
+// Device error flags of the cache's kernels (bounded tensor-core waits).
+uint32_t *nrc_error_flags(krr_nrc *n);
 float nrc_termination_spread(const krr_nrc *n);
 constexpr int kNrcRecFloats = 20;   // training vertex: record 13 | throughput 3 | L 3 | pad
 }  // namespace krr

@@ -546,6 +546,28 @@ k_nrc_backward_tc(int layers, const float *__restrict__ dy_out, const __nv_bfloa
 
 }  // namespace
 
+// Resident CTAs per SM of a tensor-memory kernel, from its registers, its
+// shared memory (carveout at the maximum) and its tensor-memory columns.
+// (The occupancy query does not count tensor memory and reported one CTA
+// for this kernel, the carveout preference not yet applied.)
+static int tc_ctas_per_sm(const void *fn, int threads, size_t smem, int dev) {
+    cudaFuncAttributes fa{};
+    int regs_sm = 0, smem_sm = 0, smem_reserved = 0, threads_sm = 0;
+    if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess ||
+        cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&smem_reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&threads_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    const int by_regs = regs_sm / std::max(1, threads * std::max(1, fa.numRegs));
+    const int by_smem = smem_sm / (int)std::max<size_t>(1, smem + fa.sharedSizeBytes + smem_reserved);
+    const int by_threads = threads_sm / threads;
+    const int by_tmem = 512 / (int)kTcCols;
+    return std::max(1, std::min(std::min(by_regs, by_smem), std::min(by_threads, by_tmem)));
+}
+
 size_t nrc_tc_smem_bytes(int layers) {
     size_t w = (size_t)(layers - 1) * kLayerBytes + kOutBytes;
     size_t a = ((w + 1023) & ~(size_t)1023) + kTcRows * kNrcIn * 2;
@@ -608,10 +630,11 @@ int nrc_forward_tc(const NrcGrid &g, const NrcMlp &mlp, const float *d_in, const
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    // FWD_PER_SM CTAs per SM (registers, 60 KB of shared memory and 64
-    // tensor-memory columns each allow it): the hash gathers of one CTA's tile
-    // overlap the MMA chains of the others
-    const int per_sm = 3;
+    // several CTAs per SM, so that the hash gathers of one CTA's tile overlap
+    // the MMA chains of the others: as many as registers, shared memory and
+    // the 512 tensor-memory columns allow (3 for five hidden layers)
+    static int per_sm = 0;
+    if (!per_sm) per_sm = tc_ctas_per_sm((const void *)k_nrc_forward_tc, kTcThreads, smem, dev);
     int64_t tiles = (cap + kTcRows - 1) / kTcRows;
     int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sms * per_sm));
     k_nrc_forward_tc<<<grid, kTcThreads, smem, s>>>(g, mlp.layers, d_in, d_count, cap, table, packed,

@@ -113,6 +113,8 @@ struct krr_wf {
     int64_t nrc_slots = 0;
     float *nrc_b_in = nullptr, *nrc_b_t = nullptr;   // training batch
     float2 *nrc_spread = nullptr;    // [n] path spread (a0, sum of sqrt spreads)
+    int32_t max_null_collisions = kMaxNullCollisions;       // krr_wf_set_loop_limits
+    int32_t max_interface_crossings = kMaxInterfaceCrossings;
 
     Queue q(int k) const { return Queue{qbuf[k], (int32_t)n, d_counts + k}; }
     int32_t *nrc_q_count() const { return d_counts + 9; }
@@ -443,6 +445,7 @@ __device__ __forceinline__ void copy_ray_item(const Queue &src, int i, const Que
 // pixel / stride.
 struct NrcHook {
     int32_t mode;
+    const uint32_t *diverged;  // non-zero: the cache diverged, trace as without it
     int32_t stride;
     const FrameConst *frame;   // offset = frame->nrc_offset
     float *q_in;
@@ -475,7 +478,7 @@ __device__ __forceinline__ bool nrc_vertex(const NrcHook &h, const DevScene &s, 
                                            const PixelState &ps, uint32_t pixel, uint32_t depth,
                                            uint32_t prev_flags, V3 thp, float t, V3 dir, V3 pu,
                                            V3 pl, uint32_t *err) {
-    if (!h.mode) return false;
+    if (!h.mode || *h.diverged) return false;
     const float cosv = fmaxf(fabsf(dot(sf.n, dir)), 1e-4f);
     if (depth == 0) {
         h.spread[pixel] = make_float2(t * t / (4.f * kPi * cosv), 0.f);
@@ -514,8 +517,8 @@ __device__ __forceinline__ bool nrc_vertex(const NrcHook &h, const DevScene &s, 
 
 // L[pixel] += throughput x max(cache, 0)
 __global__ void k_nrc_apply(const float *__restrict__ out, const float4 *__restrict__ meta,
-                            const int32_t *count, PixelState ps) {
-    int n = *count;
+                            const int32_t *count, int cap, PixelState ps) {
+    int n = min(*count, cap);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 m = meta[i];
         V3 c{fmaxf(out[3 * i], 0.f), fmaxf(out[3 * i + 1], 0.f), fmaxf(out[3 * i + 2], 0.f)};
@@ -606,7 +609,7 @@ __global__ void __launch_bounds__(kThreads, 4)
 k_hit_process(DevScene s, Queue rq, const float4 *__restrict__ hits, Queue next, Queue miss,
               Queue hitl, Queue scat, Queue msq, int enable_medium, uint32_t *err, NrcHook hook,
               PixelState ps, int inline_lights, int nee) {
-    int n = *rq.count;
+    int n = min(*rq.count, rq.cap);   // an overflowed queue holds cap items
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 h = hits[i];
         uint32_t gid = ubits(h.w);
@@ -701,7 +704,7 @@ k_hit_process(DevScene s, Queue rq, const float4 *__restrict__ hits, Queue next,
 
 // handleHit, integrator.cpp:78-90
 __global__ void k_handle_hit(DevScene s, Queue hitl, PixelState ps, int nee) {
-    int n = *hitl.count;
+    int n = min(*hitl.count, hitl.cap);   // an overflowed queue holds cap items
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 c0 = hitl.at(0, i), c1 = hitl.at(1, i), c2 = hitl.at(2, i), c3 = hitl.at(3, i);
         float4 c4 = hitl.at(4, i), c5 = hitl.at(5, i), c6 = hitl.at(6, i), c7 = hitl.at(7, i);
@@ -713,7 +716,7 @@ __global__ void k_handle_hit(DevScene s, Queue hitl, PixelState ps, int nee) {
 
 // handleMiss, integrator.cpp:92-108
 __global__ void k_handle_miss(DevScene s, Queue miss, PixelState ps, int nee) {
-    int n = *miss.count;
+    int n = min(*miss.count, miss.cap);   // an overflowed queue holds cap items
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 c1 = miss.at(1, i), c3 = miss.at(3, i), c4 = miss.at(4, i), c5 = miss.at(5, i),
                c6 = miss.at(6, i);
@@ -846,7 +849,7 @@ k_scatter_process(DevScene s, Queue scat, const int32_t *__restrict__ lists,
 
 // Radiance of unoccluded shadow rays (__raygen__Shadow, device.cu:92-100).
 __global__ void k_shadow_resolve(Queue shadow, const uint8_t *__restrict__ occluded, PixelState ps) {
-    int n = *shadow.count;
+    int n = min(*shadow.count, shadow.cap);   // an overflowed queue holds cap items
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (occluded[i]) continue;
         float4 c2 = shadow.at(2, i), c3 = shadow.at(3, i), c4 = shadow.at(4, i);
@@ -860,7 +863,7 @@ __global__ void k_shadow_resolve(Queue shadow, const uint8_t *__restrict__ occlu
 __global__ void __launch_bounds__(kThreads, 3)
 k_medium_sample(DevScene s, Queue msq, Queue next, Queue miss, Queue hitl, Queue scat,
                 Queue mscat, PixelState ps, int max_depth, uint32_t *err) {
-    int n = *msq.count;
+    int n = min(*msq.count, msq.cap);   // an overflowed queue holds cap items
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 c0 = msq.at(0, i), c1 = msq.at(1, i), c2 = msq.at(2, i), c3 = msq.at(3, i);
         float4 c4 = msq.at(4, i), c5 = msq.at(5, i), c6 = msq.at(6, i), h = msq.at(7, i);
@@ -875,7 +878,7 @@ k_medium_sample(DevScene s, Queue msq, Queue next, Queue miss, Queue hitl, Queue
         const DevMedium &m = s.media[medium];
         bool scattered = false;
         bool aborted;
-        V3 T_maj = sample_t_maj(m, o, dir, tmax_hit, rng, ch, err, aborted,
+        V3 T_maj = sample_t_maj(m, o, dir, tmax_hit, rng, ch, s.max_null_collisions, err, aborted,
             [&](V3 p, const MediumProps &mp, V3 sigma_maj, V3 Tm) -> bool {
                 float p_absorb = get(mp.sigma_a, ch) / get(sigma_maj, ch);
                 float p_scatter = get(mp.sigma_s, ch) / get(sigma_maj, ch);
@@ -975,7 +978,7 @@ k_medium_sample(DevScene s, Queue msq, Queue next, Queue miss, Queue hitl, Queue
 // sampleMediumScattering, medium.cpp:105-153
 __global__ void k_medium_scatter(DevScene s, Queue mscat, Queue next, Queue shadow, PixelState ps,
                                  int nee, uint32_t *err) {
-    int n = *mscat.count;
+    int n = min(*mscat.count, mscat.cap);   // an overflowed queue holds cap items
     float sel_pdf = 1.f / (float)s.n_lights;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 c0 = mscat.at(0, i), c1 = mscat.at(1, i), c2 = mscat.at(2, i), c3 = mscat.at(3, i);
@@ -1045,7 +1048,7 @@ template <int FMT>
 __global__ void __launch_bounds__(kThreads, 3)
 k_shadow_tr(DevScene s, const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
             Queue shadow, PixelState ps, uint32_t *err, int *trace_err) {
-    int n = *shadow.count;
+    int n = min(*shadow.count, shadow.cap);   // an overflowed queue holds cap items
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 c0 = shadow.at(0, i), c1 = shadow.at(1, i), c2 = shadow.at(2, i), c3 = shadow.at(3, i),
                c4 = shadow.at(4, i);
@@ -1072,7 +1075,8 @@ k_shadow_tr(DevScene s, const float4 *__restrict__ nodes, const float4 *__restri
             if (medium >= 0) {
                 float t_end = visible ? tmax : length(sf.p - o) / length(d);
                 bool aborted;
-                V3 T_maj = sample_t_maj(s.media[medium], o, d, t_end, rng, ch, err, aborted,
+                V3 T_maj = sample_t_maj(s.media[medium], o, d, t_end, rng, ch, s.max_null_collisions,
+                                        err, aborted,
                     [&](V3, const MediumProps &mp, V3 sigma_maj, V3 Tm) -> bool {
                         V3 sigma_n = vmax(sigma_maj - mp.sigma_a - mp.sigma_s, v3(0.f));
                         float pr = get(Tm, ch) * get(sigma_maj, ch);
@@ -1100,7 +1104,7 @@ k_shadow_tr(DevScene s, const float4 *__restrict__ nodes, const float4 *__restri
             medium = medium_towards(sf.interface_in, sf.interface_out, medium, sf.n, nd);
             o = po;
             d = nd;
-            if (++crossings > kMaxInterfaceCrossings) {
+            if (++crossings > s.max_interface_crossings) {
                 atomicOr(err, (uint32_t)kErrLoopLimit);
                 T_ray = v3(0.f);
                 break;
@@ -1124,7 +1128,7 @@ template <int FMT>
 __global__ void k_shadow_split(const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
                                Queue shadow, Queue tracked, PixelState ps, uint32_t *err,
                                int *trace_err) {
-    int n = *shadow.count;
+    int n = min(*shadow.count, shadow.cap);   // an overflowed queue holds cap items
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 c0 = shadow.at(0, i), c1 = shadow.at(1, i), c3 = shadow.at(3, i);
         V3 d = f3(c1);
@@ -1533,6 +1537,12 @@ extern "C" int krr_wf_destroy(krr_wf *wf) {
     return KRR_OK;
 }
 
+extern "C" int krr_wf_get_params(const krr_wf *wf, krr_wf_params *out) {
+    KRR_CHECK_ARG(wf && out, "NULL argument");
+    *out = wf->params;
+    return KRR_OK;
+}
+
 extern "C" int krr_wf_set_params(krr_wf *wf, const krr_wf_params *params) {
     KRR_CHECK_ARG(wf && params, "NULL argument");
     KRR_CHECK_ARG(params->max_depth >= 0 && params->spp >= 1, "bad parameters");
@@ -1748,6 +1758,8 @@ extern "C" int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *sd, void *stre
     }
     KRR_TRY(dev_upload(wf, const_cast<DevMedium **>(&s.media), media.data(), media.size()));
     s.n_media = sd->n_media;
+    s.max_null_collisions = wf->max_null_collisions;
+    s.max_interface_crossings = wf->max_interface_crossings;
     wf->scene = s;
     wf->has_scene = true;
     wf->medium = wf->params.enable_medium && s.n_media > 0;
@@ -1979,6 +1991,7 @@ static TraceLaunch closest_launch(krr_wf *wf, int depth) {
     l.ray_o = rq.base;
     l.ray_d = rq.base + wf->n;
     l.ray_stride = 1;
+    l.n = rq.cap;
     l.d_count = rq.count;
     l.hits = wf->hits;
     l.counter = wf->accel.d_scratch;
@@ -1989,7 +2002,8 @@ static TraceLaunch closest_launch(krr_wf *wf, int depth) {
 // L[pixel] += throughput x cache(query) for the queued cache queries.
 static int nrc_evaluate_queries(krr_wf *wf, cudaStream_t st) {
     KRR_TRY(nrc_query_device(wf->nrc, wf->nrc_q_in, wf->nrc_q_count(), wf->n, wf->nrc_q_out, st));
-    k_nrc_apply<<<wf->grid, kThreads, 0, st>>>(wf->nrc_q_out, wf->nrc_q_meta, wf->nrc_q_count(), wf->ps);
+    k_nrc_apply<<<wf->grid, kThreads, 0, st>>>(wf->nrc_q_out, wf->nrc_q_meta, wf->nrc_q_count(),
+                                                (int)wf->n, wf->ps);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }
@@ -2010,6 +2024,7 @@ static int closest_stage(krr_wf *wf, int depth, cudaStream_t st, bool traced,
     NrcHook hook{};
     if (wf->nrc) {
         hook.mode = 1;
+        hook.diverged = nrc_diverged_flag(wf->nrc);
         hook.stride = nrc_train_stride(wf->nrc);
         hook.frame = wf->d_frame;
         hook.q_in = wf->nrc_q_in;
@@ -2096,6 +2111,7 @@ extern "C" int krr_wf_trace_shadow(krr_wf *wf, void *stream) {
     l.ray_o = sq.base;
     l.ray_d = sq.base + wf->n;
     l.ray_stride = 1;
+    l.n = sq.cap;
     l.d_count = sq.count;
     l.occluded = wf->occluded;
     l.counter = wf->accel.d_scratch;
@@ -2254,8 +2270,26 @@ extern "C" int krr_wf_device_errors(krr_wf *wf, uint32_t *out, void *stream) {
         KRR_CUDA(cudaMemcpyAsync(&flags[1], wf->accel.d_scratch + 4, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         KRR_CUDA(cudaMemsetAsync(wf->accel.d_scratch + 4, 0, sizeof(uint32_t), st));
     }
+    uint32_t cache_flags = 0;
+    if (wf->nrc) {   // the attached cache's bounded tensor-core waits
+        KRR_CUDA(cudaMemcpyAsync(&cache_flags, nrc_error_flags(wf->nrc), sizeof(uint32_t),
+                                 cudaMemcpyDeviceToHost, st));
+        KRR_CUDA(cudaMemsetAsync(nrc_error_flags(wf->nrc), 0, sizeof(uint32_t), st));
+    }
     KRR_CUDA(cudaStreamSynchronize(st));
-    *out = flags[0] | flags[1];
+    *out = flags[0] | flags[1] | cache_flags;
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_set_loop_limits(krr_wf *wf, int32_t max_null_collisions,
+                                      int32_t max_interface_crossings) {
+    KRR_CHECK_ARG(wf != nullptr, "NULL argument");
+    KRR_CHECK_ARG(max_null_collisions >= 1 && max_interface_crossings >= 1,
+                  "loop limits must be at least 1");
+    wf->max_null_collisions = max_null_collisions;
+    wf->max_interface_crossings = max_interface_crossings;
+    wf->scene.max_null_collisions = max_null_collisions;
+    wf->scene.max_interface_crossings = max_interface_crossings;
     return KRR_OK;
 }
 

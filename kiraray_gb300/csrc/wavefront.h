@@ -66,6 +66,9 @@ struct DevMedium {
     float idx_scale[3];        // n / (hi - lo) per axis: world to voxel index
 };
 
+constexpr int kMaxNullCollisions = 1 << 20;   // default bound of the tracking loops
+constexpr int kMaxInterfaceCrossings = 64;    // default bound of the shadow segments
+
 struct DevScene {
     const DevMesh *meshes;
     const DevInstance *instances;
@@ -77,6 +80,11 @@ struct DevScene {
     int32_t n_infinite;
     const DevMedium *media;
     int32_t n_media;
+    // bounds of the tracking loops (krr_wf_set_loop_limits): null collisions
+    // per majorant walk and interface crossings per shadow ray; running out
+    // raises kErrLoopLimit and ends the walk
+    int32_t max_null_collisions;
+    int32_t max_interface_crossings;
 };
 
 // A queue: `channels` float4 planes of `cap` items and an item counter.

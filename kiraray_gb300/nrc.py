@@ -48,6 +48,22 @@ class NeuralRadianceCache:
         self._h = C.c_void_p()
         check(self.lib.krr_nrc_create(C.byref(self.cfg), C.byref(self._h)), "krr_nrc_create")
 
+    def status(self) -> tuple[int, bool]:
+        """(error flags of the cache's kernels since the last call, diverged):
+        a diverged cache (a non-finite training loss) stops training and the
+        pass renders as the plain tracer until new parameters are loaded."""
+        flags, div = C.c_uint32(), C.c_int32()
+        check(self.lib.krr_nrc_status(self._h, C.byref(flags), C.byref(div), _stream()),
+              "krr_nrc_status")
+        return int(flags.value), bool(div.value)
+
+    def save(self, path: str) -> None:
+        """Checkpoint: weights, hash table, Adam moments and step to a file."""
+        check(self.lib.krr_nrc_save(self._h, str(path).encode()), "krr_nrc_save")
+
+    def load(self, path: str) -> None:
+        check(self.lib.krr_nrc_load(self._h, str(path).encode()), "krr_nrc_load")
+
     def info(self) -> _lib.NrcInfo:
         i = _lib.NrcInfo()
         check(self.lib.krr_nrc_info(self._h, C.byref(i)), "krr_nrc_info")

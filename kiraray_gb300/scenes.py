@@ -242,6 +242,34 @@ class Scene:
 
 
 # ----------------------------------------------------------------- helpers
+def bounce_rays(tris: np.ndarray, rays: np.ndarray, hits: np.ndarray, seed: int) -> np.ndarray:
+    """Cosine-weighted rays from the primary hit points around the geometric
+    normal facing the incoming ray (first-bounce diffuse set)."""
+    prim = hits[:, 3].view(np.uint32)
+    ok = prim != 0xFFFFFFFF
+    t = hits[ok, 0:1].astype(np.float64)
+    o = rays[ok, 0:3].astype(np.float64) + t * rays[ok, 4:7]
+    v = tris[prim[ok]].reshape(-1, 3, 3).astype(np.float64)
+    n = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
+    n /= np.linalg.norm(n, axis=-1, keepdims=True) + 1e-30
+    flip = np.sum(n * rays[ok, 4:7], -1) > 0
+    n[flip] *= -1
+    rng = np.random.default_rng(seed)
+    u1, u2 = rng.random(n.shape[0]), rng.random(n.shape[0])
+    r, phi = np.sqrt(u1), 2 * np.pi * u2
+    local = np.stack([r * np.cos(phi), r * np.sin(phi), np.sqrt(np.maximum(0, 1 - u1))], -1)
+    a = np.where(np.abs(n[:, :1]) > 0.9, np.array([[0, 1, 0]]), np.array([[1, 0, 0]]))
+    tt = np.cross(a, n)
+    tt /= np.linalg.norm(tt, axis=-1, keepdims=True)
+    bb = np.cross(n, tt)
+    d = local[:, :1] * tt + local[:, 1:2] * bb + local[:, 2:3] * n
+    out = np.zeros((n.shape[0], 8), np.float32)
+    out[:, :3] = o + n * 1e-4
+    out[:, 4:7] = d
+    out[:, 7] = np.inf
+    return out
+
+
 def _xform(scale=(1, 1, 1), rot_y_deg=0.0, translate=(0, 0, 0)) -> np.ndarray:
     c, s = math.cos(math.radians(rot_y_deg)), math.sin(math.radians(rot_y_deg))
     r = np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]], np.float64)

@@ -50,6 +50,25 @@ class WavefrontPathTracer:
         self._keep = None
         self.scene = None
 
+    @classmethod
+    def from_json(cls, params_json: str) -> "WavefrontPathTracer":
+        """The pass created from its JSON parameters through the C ABI
+        (krr_wf_create_json: the reference's from_json keys and defaults)."""
+        obj = cls.__new__(cls)
+        obj.lib = _lib.load()
+        obj._h = C.c_void_p()
+        check(obj.lib.krr_wf_create_json(params_json.encode(), C.byref(obj._h)), "krr_wf_create_json")
+        obj.params = _lib.WfParams()
+        check(obj.lib.krr_wf_get_params(obj._h, C.byref(obj.params)), "krr_wf_get_params")
+        obj.width = obj.height = 0
+        obj._keep = None
+        obj.scene = None
+        return obj
+
+    def set_params_json(self, params_json: str):
+        check(self.lib.krr_wf_set_params_json(self._h, params_json.encode()), "krr_wf_set_params_json")
+        check(self.lib.krr_wf_get_params(self._h, C.byref(self.params)), "krr_wf_get_params")
+
     # from_json, integrator.h:94-103
     def _apply(self, params: dict):
         for k, v in params.items():
@@ -203,6 +222,13 @@ class WavefrontPathTracer:
         out = torch.empty((self.n_pixels, 4), dtype=torch.float32, device="cuda")
         check(self.lib.krr_wf_read_radiance(self._h, out.data_ptr(), _stream()), "read_radiance")
         return out
+
+    def set_loop_limits(self, max_null_collisions: int = 1 << 20,
+                        max_interface_crossings: int = 64) -> None:
+        """Bounds of the medium tracking loops; a walk that runs out raises
+        the loop-limit flag (bit 2 of device_errors) and ends."""
+        check(self.lib.krr_wf_set_loop_limits(self._h, max_null_collisions,
+                                              max_interface_crossings), "set_loop_limits")
 
     def device_errors(self) -> int:
         v = C.c_uint32()

@@ -328,3 +328,62 @@ def test_leaf_sizes_keep_hits_identical(krr_lib, cuda, leaf, full_leaf):
     r = H.vertex_edge_rays(12, 3)
     ga = build(g)
     _assert_bits_equal(_gpu_closest(ga, r), O.closest_brute(g, r), f"{tag} edges")
+
+
+def test_stack_limit_cuts_rays_off_and_reports_overflow(krr_lib, cuda):
+    """A traversal stack limit below the tree's needs cuts rays off: the
+    overflow flag is raised, cut-off rays report t = NaN and a miss, every
+    other ray keeps its exact hit, and the synchronous entry points return
+    KRR_ERR_OVERFLOW.  With the default limit nothing is cut off."""
+    from kiraray_gb300._lib import KrrError
+    sc = scenes.large_scene(width=96, height=64, grid=128, n_spheres=40, sky_size=(64, 32))
+    tris = sc.world_triangles()
+    rays = H.pinhole_rays(sc, jitter_seed=2)
+    want = O.Bvh(tris).closest(rays)
+    acc = Accel(tris)
+    assert acc.device_errors() == 0
+    acc.set_stack_limit(1)
+    got = _gpu_closest(acc, rays)
+    assert acc.device_errors() & 1
+    cut = np.isnan(got[:, 0])
+    assert 0 < cut.sum() < rays.shape[0]
+    assert np.all(got[cut, 3].view(np.uint32) == 0xFFFFFFFF)
+    _assert_bits_equal(got[~cut], want[~cut], "rays within the stack limit")
+    occ = acc.trace_any(torch.from_numpy(rays).cuda()).cpu().numpy()
+    assert acc.device_errors() & 1
+    assert set(np.unique(occ)) <= {0, 1, 0xFF} and (occ == 0xFF).any()
+    with pytest.raises(KrrError, match="stack limit"):
+        acc.trace_stats(torch.from_numpy(rays).cuda())
+    acc.set_stack_limit(48)
+    _assert_bits_equal(_gpu_closest(acc, rays), want, "default stack limit")
+    assert acc.device_errors() == 0
+    with pytest.raises(KrrError):
+        acc.set_stack_limit(49)
+
+
+@pytest.mark.parametrize("builder", [1, 2])
+def test_builders_give_identical_hits(krr_lib, cuda, builder):
+    """PLOC clustering and the radix tree on cubic cells build other trees
+    over the same triangles; the hits stay bit-identical to the oracle's."""
+    from kiraray_gb300.accel import set_builder
+    sc = scenes.large_scene(width=160, height=90, grid=256, n_spheres=60, sky_size=(64, 32))
+    tris = sc.world_triangles()
+    rays = H.pinhole_rays(sc, jitter_seed=9)
+    ob = O.Bvh(tris)
+    want = ob.closest(rays)
+    b = H.bounce_rays(tris, rays, want, 4)
+    set_builder(builder)
+    try:
+        acc = Accel(tris)
+        soup = H.random_soup(3000, 17)
+        acc_soup = Accel(soup)
+        single = Accel(soup[:1])
+    finally:
+        set_builder(0)
+    _assert_bits_equal(_gpu_closest(acc, rays), want, f"builder {builder} camera rays")
+    _assert_bits_equal(_gpu_closest(acc, b), ob.closest(b), f"builder {builder} bounce rays")
+    r = H.random_rays(2000, 18)
+    _assert_bits_equal(_gpu_closest(acc_soup, r), O.closest_brute(soup, r), f"builder {builder} soup")
+    _assert_bits_equal(_gpu_closest(single, r), O.closest_brute(soup[:1], r), "one triangle")
+    assert acc.stats()["max_depth"] <= 48
+    assert acc.device_errors() == 0

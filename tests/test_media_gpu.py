@@ -44,3 +44,25 @@ def test_medium_disabled_ignores_media(krr_lib, cuda):
     # with media off the null box only relays rays (each crossing still uses
     # one bounce of the loop, as in the reference): no pixel goes black
     assert (L.sum(1) > 0).mean() > 0.4
+
+
+def test_loop_limits_raise_the_flag_and_end_the_walk(krr_lib, cuda):
+    """A null-collision bound of 1 ends the tracking walks early and raises
+    the loop-limit flag (bit 2); the defaults raise nothing and match the
+    oracle again."""
+    sc = scenes.volume_box(64, 64, max_depth=8, grid=32)
+    pt = WavefrontPathTracer({"max_depth": 8})
+    pt.set_scene(sc)
+    pt.resize(sc.width, sc.height)
+    pt.set_loop_limits(1, 64)
+    L, img = gpu_frame(pt, sc, 1)
+    assert pt.device_errors() & 4
+    assert np.isfinite(img).all()
+    pt.set_loop_limits(1 << 20, 1)
+    gpu_frame(pt, sc, 1)
+    assert pt.device_errors() & 4   # shadow rays cross the box's two null interfaces
+    pt.set_loop_limits()
+    L, _ = gpu_frame(pt, sc, 1)
+    assert pt.device_errors() == 0
+    oL, _ = O.PathTracer(sc).render({"max_depth": 8}, 1)
+    compare(L[:, :3], oL, "volume frame after the limits are restored")

@@ -66,3 +66,38 @@ def test_noalloc_rejects_sizes_beyond_the_static_scratch(krr_lib, cuda):
     st = lib.krr_accel_trace_stats_noalloc(acc._h, rays.data_ptr(), 0, 0, out,
                                            torch.cuda.current_stream().cuda_stream)
     assert st == 1
+
+
+def test_noalloc_leaves_device_memory_unchanged(krr_lib, cuda):
+    """Free device memory (cudaMemGetInfo) is the same before and after calls
+    of the no-allocation entry point; nothing between the two readings goes
+    through torch's caching allocator."""
+    tris = H.random_soup(3000, 21)
+    acc = Accel(tris)
+    lib = _lib.load()
+    rays = torch.from_numpy(H.random_rays(20000, 22)).cuda()
+    _counts(lib.krr_accel_trace_stats_noalloc, acc, rays, False)   # set-up on this device
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    for any_hit in (False, True, False):
+        _counts(lib.krr_accel_trace_stats_noalloc, acc, rays, any_hit)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
+
+
+def test_noalloc_reports_a_stack_overflow(krr_lib, cuda):
+    """A traversal stack limit that cuts rays off makes the call return
+    KRR_ERR_OVERFLOW, as the allocating entry point does."""
+    sc = scenes.large_scene(width=64, height=48, grid=96, n_spheres=30, sky_size=(32, 16))
+    acc = Accel(sc.world_triangles())
+    lib = _lib.load()
+    rays = torch.from_numpy(H.pinhole_rays(sc, jitter_seed=1)).cuda()
+    acc.set_stack_limit(1)
+    out = (C.c_ulonglong * 2)()
+    for fn in (lib.krr_accel_trace_stats_noalloc, lib.krr_accel_trace_stats):
+        st = fn(acc._h, rays.data_ptr(), rays.shape[0], 0, out,
+                torch.cuda.current_stream().cuda_stream)
+        assert st == 3, fn.__name__   # KRR_ERR_OVERFLOW
+    acc.set_stack_limit(48)
+    assert _counts(lib.krr_accel_trace_stats_noalloc, acc, rays, False) == \
+        _counts(lib.krr_accel_trace_stats, acc, rays, False)
