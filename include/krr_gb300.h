@@ -177,11 +177,11 @@ int krr_set_bvh_full_node_leaf(int32_t triangles);
 
 /* Binary tree behind the BVHs built from now on, process-wide: 0 = Karras
  * radix tree over 63-bit Morton codes of the centroids, each axis scaled to
- * its own extent (default); 1 = PLOC, parallel locally-ordered clustering
- * (Meister and Bittner 2018) over Morton codes on cubic cells, a tree of
- * smaller surface area for a slower build; 2 = the radix tree on cubic
- * cells.  Either is collapsed into the same 8-wide nodes; hits are the same
- * with any builder. */
+ * its own extent; 1 = PLOC, parallel locally-ordered clustering (Meister and
+ * Bittner 2018) over Morton codes on cubic cells; 2 = the radix tree on
+ * cubic cells (default: the fewest node visits on the bench scene).  Either
+ * is collapsed into the same 8-wide nodes; hits are the same with any
+ * builder. */
 int krr_set_bvh_builder(int32_t builder);
 
 /* Build from host arrays of world-space triangles: h_vertices float3[3*n]. */

@@ -32,8 +32,8 @@ def set_max_leaf(triangles: int) -> None:
 
 
 def set_builder(builder: int) -> None:
-    """Binary tree of the BVHs built from now on: 0 radix tree (default),
-    1 PLOC clustering, 2 radix tree on cubic Morton cells."""
+    """Binary tree of the BVHs built from now on: 0 radix tree on per-axis
+    Morton cells, 1 PLOC clustering, 2 radix tree on cubic cells (default)."""
     check(_lib.load().krr_set_bvh_builder(builder), "krr_set_bvh_builder")
 
 

@@ -35,6 +35,33 @@ class Accumulator:
                                              _stream()), "krr_accumulate_f64")
         self.frames += 1
 
+    MAGIC = b"KRRACC01"
+
+    def save(self, path) -> None:
+        """Checkpoint of the FP64 running sum and its frame count (a header
+        of magic, pixel count and frames, then n x 3 float64), so that a
+        convergence run can resume."""
+        import numpy as np
+        torch.cuda.synchronize()
+        with open(path, "wb") as f:
+            f.write(self.MAGIC)
+            f.write(np.array([self.n, self.frames], np.int64).tobytes())
+            f.write(self.sum.cpu().numpy().astype(np.float64).tobytes())
+
+    def load(self, path) -> None:
+        import numpy as np
+        with open(path, "rb") as f:
+            if f.read(8) != self.MAGIC:
+                raise ValueError(f"{path} is not an accumulation checkpoint")
+            n, frames = np.frombuffer(f.read(16), np.int64)
+            if n != self.n:
+                raise ValueError(f"{path} holds {n} pixels, this accumulator {self.n}")
+            data = np.frombuffer(f.read(int(n) * 24), np.float64)
+            if data.size != 3 * n:
+                raise ValueError(f"{path} is truncated")
+        self.sum.copy_(torch.from_numpy(data.reshape(-1, 3).copy()))
+        self.frames = int(frames)
+
     def image(self) -> torch.Tensor:
         """float32 [n, 4] mean image."""
         out = torch.ones((self.n, 4), dtype=torch.float32, device="cuda")

@@ -1,8 +1,9 @@
 """Fixed workloads for profiling the pass under a profiler (ncu launch lists
 and single-kernel captures); prints the device time of each repetition.
 
-    python -m kiraray_gb300.profile trace [--reps 4]
+    python -m kiraray_gb300.profile trace [--reps 4] [--builder 0]
         closest hits of the 1920x1080 camera rays of the 10.9M-triangle scene
+        (BVH builder as krr_set_bvh_builder)
     python -m kiraray_gb300.profile update [--reps 5]
         an instance update of the large scene (re-flatten + BVH refit) against
         a full BVH rebuild, host wall time per call
@@ -31,12 +32,14 @@ def _timed(fn) -> float:
     return e0.elapsed_time(e1)
 
 
-def trace(reps: int) -> dict:
+def trace(reps: int, builder: int = 2) -> dict:
     from . import scenes
-    from .accel import Accel
+    from .accel import Accel, set_builder
 
     sc = scenes.large_scene()
+    set_builder(builder)
     acc = Accel(sc.world_triangles())
+    set_builder(2)
     rays = torch.from_numpy(scenes.pinhole_rays(sc)).cuda()
     ms = [_timed(lambda: acc.trace_closest(rays)) for _ in range(reps)]
     return {"workload": "trace", "rays": int(rays.shape[0]), "ms": ms}
@@ -107,6 +110,7 @@ def main() -> None:
     sub = ap.add_subparsers(dest="cmd", required=True)
     t = sub.add_parser("trace")
     t.add_argument("--reps", type=int, default=4)
+    t.add_argument("--builder", type=int, default=2, choices=[0, 1, 2])
     u = sub.add_parser("update")
     u.add_argument("--reps", type=int, default=5)
     f = sub.add_parser("frame")
@@ -120,7 +124,7 @@ def main() -> None:
     from .build import build
     build()
     if a.cmd == "trace":
-        r = trace(a.reps)
+        r = trace(a.reps, a.builder)
     elif a.cmd == "update":
         r = update(a.reps)
     else:

@@ -361,10 +361,11 @@ def test_stack_limit_cuts_rays_off_and_reports_overflow(krr_lib, cuda):
         acc.set_stack_limit(49)
 
 
-@pytest.mark.parametrize("builder", [1, 2])
+@pytest.mark.parametrize("builder", [0, 1])
 def test_builders_give_identical_hits(krr_lib, cuda, builder):
-    """PLOC clustering and the radix tree on cubic cells build other trees
-    over the same triangles; the hits stay bit-identical to the oracle's."""
+    """The radix tree on per-axis cells and PLOC clustering build other trees
+    than the default (radix tree on cubic cells) over the same triangles; the
+    hits stay bit-identical to the oracle's."""
     from kiraray_gb300.accel import set_builder
     sc = scenes.large_scene(width=160, height=90, grid=256, n_spheres=60, sky_size=(64, 32))
     tris = sc.world_triangles()
@@ -379,7 +380,7 @@ def test_builders_give_identical_hits(krr_lib, cuda, builder):
         acc_soup = Accel(soup)
         single = Accel(soup[:1])
     finally:
-        set_builder(0)
+        set_builder(2)
     _assert_bits_equal(_gpu_closest(acc, rays), want, f"builder {builder} camera rays")
     _assert_bits_equal(_gpu_closest(acc, b), ob.closest(b), f"builder {builder} bounce rays")
     r = H.random_rays(2000, 18)

@@ -50,3 +50,22 @@ def test_tonemap_matches_oracle(krr_lib, cuda, op, gamma):
     want = tonemap_ref(img, op, 1.7, gamma)
     assert np.all(got[..., 3] == 1.0)
     np.testing.assert_allclose(got, want, rtol=2e-6, atol=2e-7)
+
+
+def test_accumulation_checkpoint_resumes(krr_lib, cuda, tmp_path):
+    """An FP64 accumulation saved after some frames and loaded into a new
+    accumulator continues to the same sum bit for bit."""
+    frames = [torch.rand((32 * 16, 4), device="cuda") for _ in range(6)]
+    a = Accumulator(32, 16)
+    for f in frames[:4]:
+        a.add(f)
+    a.save(tmp_path / "acc.bin")
+    b = Accumulator(32, 16)
+    b.load(tmp_path / "acc.bin")
+    for f in frames[4:]:
+        a.add(f)
+        b.add(f)
+    assert b.frames == a.frames == 6
+    assert torch.equal(a.sum, b.sum)
+    with pytest.raises(ValueError):
+        Accumulator(8, 8).load(tmp_path / "acc.bin")
