@@ -427,10 +427,13 @@ def config_frames(args):
 
 def batched_views(args):
     """64 views, sides log-uniform in [256, 1024] (view i seeded 100 + i),
-    even views on the large scene and odd views on the volume box, the
-    neural radiance cache attached to both passes; the two passes run as one
-    CUDA graph with a branch per pass.  Reports device time per frame (all
-    views) and the same frames run pass after pass."""
+    even views on the large scene (max depth 8) and odd views on the volume
+    box (max depth 16), one neural radiance cache for both, all in ONE
+    wavefront: every stage of a bounce is one launch over the items of all
+    views of both scenes, under a captured CUDA graph, with the launch shapes
+    and queue capacity chosen by the autotuner (krr_wf_autotune).  Reports
+    device time per frame, and for comparison the two scenes as two passes
+    in one graph (a branch per pass, each with its own cache)."""
     if args.views <= 0:
         return None
     import math
@@ -442,7 +445,7 @@ def batched_views(args):
 
     big = scenes.large_scene(width=64, height=64, seed=1)
     vol = scenes.volume_box(64, 64)
-    views = ([], [])
+    views = []
     total = 0
     for i in range(args.views):
         rng = np.random.default_rng(100 + i)
@@ -455,53 +458,77 @@ def batched_views(args):
         else:
             pos = (0.5 + 1.9 * math.sin(a), 0.5, 0.5 - 1.9 * math.cos(a))
             cam = scenes._camera(pos, (0.5, 0.5, 0.0), 40.0, w, h)
-        views[i % 2].append((cam, w, h, 100 + i))
+        views.append((cam, w, h, 100 + i, i % 2))
         total += w * h
     stream = torch.cuda.Stream()
+
+    def timed(fn, frames):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ms = []
+        for f in frames:
+            e0.record(stream)
+            fn(f)
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return sorted(ms)[len(ms) // 2]
+
     with torch.cuda.stream(stream):
+        # one wavefront over both scenes
+        pt = WavefrontPathTracer({"max_depth": 8}, seed=0)
+        pt.set_scenes([big, vol])
+        pt.set_scene_max_depth(1, vol.max_depth)
+        pt.resize_views(views)
+        lo, hi = pt.cache_box()
+        pt.set_nrc(NeuralRadianceCache(lo, hi, seed=3), train=True)
+        out = torch.empty((pt.n_pixels, 4), device="cuda")
+        pt.begin_frame_views(1)
+        pt.render_flat(out)
+        tuning = pt.autotune(out, frames=2)
+        pt.begin_frame_views(2)
+        pt.render_flat(out)
+        pt.capture_frame(out)
+        for f in range(3, 6):
+            pt.launch_frame(f)
+        stream.synchronize()
+        one = timed(pt.launch_frame, range(6, 6 + args.view_frames))
+        errors = pt.device_errors()
+        launch = pt.launch()
+        del pt
+
+        # the same views as two passes, one graph with a branch per pass
         passes, outs = [], []
-        for sc, vs in ((big, views[0]), (vol, views[1])):
-            pt = WavefrontPathTracer({"max_depth": sc.max_depth}, seed=0)
-            pt.set_scene(sc)
+        for sc, k in ((big, 0), (vol, 1)):
+            p = WavefrontPathTracer({"max_depth": sc.max_depth}, seed=0)
+            p.set_scene(sc)
             tris = sc.world_triangles().reshape(-1, 3)
-            pt.set_nrc(NeuralRadianceCache(tris.min(0), tris.max(0), seed=3), train=True)
-            pt.resize_views(vs)
-            out = torch.empty((pt.n_pixels, 4), device="cuda")
-            pt.begin_frame_views(1)
-            pt.render_flat(out)
-            passes.append(pt)
-            outs.append(out)
+            p.set_nrc(NeuralRadianceCache(tris.min(0), tris.max(0), seed=3), train=True)
+            p.resize_views([v[:4] for v in views if v[4] == k])
+            o = torch.empty((p.n_pixels, 4), device="cuda")
+            p.begin_frame_views(1)
+            p.render_flat(o)
+            passes.append(p)
+            outs.append(o)
         group = FrameGroup(passes, outs)
         group.capture()
-        for p, o in zip(passes, outs):
-            p.capture_frame(o)
-
-        def timed(fn, frames):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            ms = []
-            for f in frames:
-                e0.record(stream)
-                fn(f)
-                e1.record(stream)
-                e1.synchronize()
-                ms.append(e0.elapsed_time(e1))
-            return sorted(ms)[len(ms) // 2]
-
         for f in range(2, 5):
             group.launch(f)
         stream.synchronize()
         grouped = timed(group.launch, range(5, 5 + args.view_frames))
-
-        def one_after_other(f):
-            for p in passes:
-                p.launch_frame(f)
-        sequential = timed(one_after_other, range(5 + args.view_frames, 5 + 2 * args.view_frames))
-        errors = sum(p.device_errors() for p in passes)
+        errors += sum(p.device_errors() for p in passes)
         group.close()
     return {"views": args.views, "pixels_per_frame": total, "scenes": ["large_scene", "volume_box"],
-            "nrc": True, "frame_ms_group_graph": round(grouped, 3),
-            "frame_ms_pass_after_pass": round(sequential, 3),
-            "mpaths_per_s": round(total / grouped / 1e3, 1), "device_errors": errors}
+            "max_depth": {"large_scene": 8, "volume_box": vol.max_depth}, "nrc": True,
+            "one_wavefront": True, "launches_per_stage_per_bounce": 1,
+            "frame_ms": round(one, 3), "mpaths_per_s": round(total / one / 1e3, 1),
+            "autotuner": {"block": tuning["block"], "blocks_per_sm": tuning["blocks_per_sm"],
+                          "queue_capacity": tuning["queue_capacity"],
+                          "wave": tuning["wave"] or total, "candidates": tuning["candidates"],
+                          "frame_ms_chosen": round(tuning["frame_ms"], 3),
+                          "frame_ms_defaults": round(tuning["default_frame_ms"], 3),
+                          "note": "eager frames, cache not training during the trials"},
+            "launch": launch,
+            "frame_ms_two_passes_graph": round(grouped, 3), "device_errors": errors}
 
 
 NRC_TUNED = {"learning_rate": 3e-3, "batch_size": 16384, "termination_spread": 0.05}

@@ -314,6 +314,24 @@ int krr_wf_set_params_json(krr_wf *wf, const char *params_json);
 /* RenderPass::setScene (integrator.cpp:186-203): uploads the scene and
  * builds the BVH. */
 int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *scene, void *stream);
+/* Several scenes (1..255) in one pass, so that views of different scenes
+ * share one wavefront: every stage of a bounce is one launch over the items
+ * of all views.  Each view names its scene (krr_view.scene); each scene keeps
+ * its own lights, environment, media and BVH (one tree per scene in one node
+ * array, each ray starting at its scene's root), and a view's frame equals
+ * the same view of a pass holding its scene alone, bit for bit.  With a
+ * radiance cache attached, each scene's positions are offset so that the
+ * scenes occupy disjoint regions of the cache's box (krr_wf_cache_box).
+ * Instance updates (krr_wf_update_instances) and the megakernel variant
+ * take one scene only; krr_wf_rebuild_bvh rebuilds every scene's tree. */
+int krr_wf_set_scenes(krr_wf *wf, const krr_scene_desc *scenes, int32_t n_scenes, void *stream);
+/* Path depth of one scene of the pass (max_depth >= 0), or -1 for the
+ * pass's max_depth (the default): a view of that scene then equals its
+ * scene's pass with that max_depth. */
+int krr_wf_set_scene_max_depth(krr_wf *wf, int32_t scene, int32_t max_depth);
+/* Box the radiance cache should cover for this pass (scene_lo/hi of its
+ * krr_nrc_config): the union of the scenes' boxes after their offsets. */
+int krr_wf_cache_box(krr_wf *wf, float *out_lo3, float *out_hi3);
 /* Scene::update for animated instances (src/core/scene.cpp:17-31,
  * src/core/device/optix.cpp:618-642): instance h_indices[k] gets the
  * row-major 3x4 transform h_transforms[12k..12k+11]; the world-space
@@ -353,6 +371,8 @@ typedef struct krr_view {
     krr_camera_desc camera;
     int32_t width, height;
     uint32_t seed;
+    int32_t scene;    /* scene of the view (krr_wf_set_scenes), 0 with one scene;
+                         camera.medium indexes that scene's media */
 } krr_view;
 int krr_wf_resize_views(krr_wf *wf, const krr_view *views, int32_t n_views);
 int krr_wf_begin_frame_views(krr_wf *wf, int64_t frame_index, const krr_view *views,
@@ -364,6 +384,32 @@ int krr_wf_begin_frame_views(krr_wf *wf, int64_t frame_index, const krr_view *vi
 int krr_wf_capture_frame(krr_wf *wf, float *d_out, void *stream);
 int krr_wf_launch_frame(krr_wf *wf, int64_t frame_index, const krr_view *views, int32_t n_views,
                         void *stream);
+
+/* Launch shapes of the stage kernels and the queue capacity: threads per
+ * block (64, 128 or 256; default 256), resident blocks per SM of the
+ * grid-stride stage kernels (1..32; default 8), and `wave`, the pixels that
+ * go through the bounces together in render() (0 = all of them, the
+ * reference's W*H queues, integrator.cpp:25; default).  Queues hold
+ * min(wave, pixels) items, so a smaller wave needs less memory; frames are
+ * the same with any setting.  The stage entry points need wave 0.
+ * Reallocates the queues when the wave changes (drops a captured frame). */
+int krr_wf_set_launch(krr_wf *wf, int32_t block, int32_t blocks_per_sm, int64_t wave);
+int krr_wf_get_launch(const krr_wf *wf, int32_t *block, int32_t *blocks_per_sm, int64_t *wave,
+                      int64_t *queue_capacity);
+typedef struct krr_wf_tuning {
+    int32_t block, blocks_per_sm;
+    int64_t wave, queue_capacity;
+    float frame_ms;             /* median frame time with the chosen settings */
+    float default_frame_ms;     /* with the defaults (256 threads, 8 per SM, all pixels) */
+    int32_t candidates;
+    int32_t reserved;
+} krr_wf_tuning;
+/* Autotuner: renders `frames` frames per candidate setting of
+ * krr_wf_set_launch (128/256 threads x 4/8/16 blocks per SM x waves of all,
+ * half or a quarter of the pixels) with the current cameras into d_out,
+ * keeps the fastest and reports it.  An attached cache does not train
+ * during the trials.  Synchronises the stream. */
+int krr_wf_autotune(krr_wf *wf, float *d_out_rgba, int32_t frames, krr_wf_tuning *out, void *stream);
 
 /* Frame groups: several passes (for instance two scenes, each with its own
  * batched views) captured as one CUDA graph whose branches run the passes'

@@ -57,9 +57,16 @@ class CameraDesc(C.Structure):
                 ("shutter_time", C.c_float), ("medium", C.c_int32)]
 
 
+class WfTuning(C.Structure):
+    _fields_ = [("block", C.c_int32), ("blocks_per_sm", C.c_int32), ("wave", C.c_int64),
+                ("queue_capacity", C.c_int64), ("frame_ms", C.c_float),
+                ("default_frame_ms", C.c_float), ("candidates", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
 class ViewDesc(C.Structure):
     _fields_ = [("camera", CameraDesc), ("width", C.c_int32), ("height", C.c_int32),
-                ("seed", C.c_uint32)]
+                ("seed", C.c_uint32), ("scene", C.c_int32)]
 
 
 class SceneDesc(C.Structure):
@@ -169,6 +176,13 @@ SIGNATURES = {
     "krr_wf_device_errors": (_I, [_P, C.POINTER(C.c_uint32), _P]),
     "krr_wf_accel": (_I, [_P, C.POINTER(_P)]),
     "krr_wf_set_loop_limits": (_I, [_P, C.c_int32, C.c_int32]),
+    "krr_wf_set_scenes": (_I, [_P, _P, C.c_int32, _P]),
+    "krr_wf_set_launch": (_I, [_P, C.c_int32, C.c_int32, C.c_int64]),
+    "krr_wf_set_scene_max_depth": (_I, [_P, C.c_int32, C.c_int32]),
+    "krr_wf_get_launch": (_I, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                               C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "krr_wf_autotune": (_I, [_P, _P, C.c_int32, C.POINTER(WfTuning), _P]),
+    "krr_wf_cache_box": (_I, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "krr_accumulate_f64": (_I, [_P, _P, C.c_int64, _P]),
     "krr_nrc_config_default": (None, [C.POINTER(NrcConfig)]),
     "krr_nrc_create": (_I, [C.POINTER(NrcConfig), C.POINTER(_P)]),

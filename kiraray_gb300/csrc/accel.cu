@@ -584,6 +584,11 @@ __device__ __forceinline__ void trace_body(const float4 *__restrict__ nodes,
                         else idx -= n_any;
                     }
                     ray_id = idx;
+                    uint32_t root = 0;
+                    if (L.roots) {
+                        const float4 *pp = (MODE == 2 && any_ray) ? L.any_pix : L.ray_pix;
+                        root = L.roots[L.pixel_part[__float_as_uint(pp[idx * L.ray_stride].w)]];
+                    }
                     float4 ro = po[idx * L.ray_stride];
                     float4 rd = pd[idx * L.ray_stride];
                     V3 o = f3(ro), d = f3(rd);
@@ -592,7 +597,7 @@ __device__ __forceinline__ void trace_body(const float4 *__restrict__ nodes,
                     inv = box_inverse(d);
                     oinv = V3{-o.x * inv.x, -o.y * inv.y, -o.z * inv.z};
                     oct = (inv.x < 0.f ? 1 : 0) | (inv.y < 0.f ? 2 : 0) | (inv.z < 0.f ? 4 : 0);
-                    ng = make_uint2(0u, (1u << oct) | (1u << 8));
+                    ng = make_uint2(root, (1u << oct) | (1u << 8));
                     tg = make_uint2(0u, 0u);
                     sp = 0;
                     best_prim = KRR_MISS;
@@ -785,7 +790,11 @@ void accel_free(krr_accel *a) {
     cudaFree(a->stage_rays);
     cudaFree(a->stage_hits);
     cudaFree(a->d_node_bounds);
+    cudaFree(a->d_roots);
     a->d_node_bounds = nullptr;
+    a->d_roots = nullptr;
+    a->roots.clear();
+    a->part_bounds.clear();
     a->level_first.clear();
     if (a->stage_aux) cudaStreamDestroy(a->stage_aux);
     for (cudaEvent_t &e : a->stage_ev)
@@ -908,6 +917,7 @@ static int scene_bounds_margin(krr_accel *a, const float *d_v, int64_t n, cudaSt
 int accel_refit(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     KRR_CHECK_ARG(a && a->d_scratch, "acceleration structure not built");
     KRR_CHECK_ARG(n == a->n_tris, "a refit keeps the triangle count of the build");
+    KRR_CHECK_ARG(a->roots.empty(), "a structure of several scenes is rebuilt, not refitted");
     if (n == 0) return KRR_OK;
     KRR_CHECK_ARG(d_v != nullptr, "vertices are NULL");
     float margin = 0.f;
@@ -1110,12 +1120,136 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     return KRR_OK;
 }
 
+// Relocation of one part's tree into the combined arrays: child and
+// triangle base indices move by the part's node and triangle offsets, the
+// triangle ids by the part's first global id.
+__global__ void k_relocate_nodes(float4 *nodes, int64_t n, int quads, int ref_quad, uint32_t node_off,
+                                 uint32_t tri_off) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 *q = nodes + quads * (size_t)i + ref_quad;
+    float4 v = *q;
+    v.x = __uint_as_float(__float_as_uint(v.x) + node_off);
+    v.y = __uint_as_float(__float_as_uint(v.y) + tri_off);
+    *q = v;
+}
+
+__global__ void k_relocate_tris(float4 *tris, uint32_t *leaf_of_prim, int64_t n, uint32_t id_off) {
+    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    float4 v0 = tris[3 * (size_t)k];
+    v0.w = __uint_as_float(__float_as_uint(v0.w) + id_off);
+    tris[3 * (size_t)k] = v0;
+    leaf_of_prim[k] += id_off;   // the part's local slot -> combined slot (same offset)
+}
+
+// A node with every slot empty (inverted boxes): the root of a part without
+// triangles, which every ray misses.
+__global__ void k_empty_node(float4 *np, int format) {
+    V3 slo[8], shi[8];
+    for (int k = 0; k < 8; ++k) { slo[k] = v3(INFINITY); shi[k] = v3(-INFINITY); }
+    V3 lo, hi;
+    write_node_boxes(np, format, slo, shi, 0u, lo, hi);
+    const float4 refs = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (format == 1) { np[12] = refs; np[13] = refs; }
+    else {
+        np[0] = make_float4(0.f, 0.f, 0.f, __uint_as_float(127u | (127u << 8) | (127u << 16)));
+        np[1] = refs;
+    }
+}
+
 int accel_set_mask(krr_accel *a, const uint8_t *d_mask, cudaStream_t s) {
     if (a->n_tris == 0) return KRR_OK;
     k_set_mask<<<blocks_for(a->n_tris), kBuildThreads, 0, s>>>(a->d_tris, a->d_leaf_of_prim, d_mask,
                                                                a->n_tris);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
+}
+
+int accel_build_parts(krr_accel *a, const float *d_v, const int64_t *part_begin, int n_parts,
+                      cudaStream_t s) {
+    KRR_CHECK_ARG(n_parts >= 1 && n_parts <= 255, "1..255 scene parts");
+    const int64_t n = part_begin[n_parts] - part_begin[0];
+    if (n_parts == 1) {
+        KRR_TRY(accel_build(a, d_v, n, s));
+        a->part_bounds.assign({a->scene_lo[0], a->scene_lo[1], a->scene_lo[2], a->scene_hi[0],
+                               a->scene_hi[1], a->scene_hi[2]});
+        return KRR_OK;
+    }
+    std::vector<krr_accel> parts(n_parts);
+    int st = KRR_OK;
+    for (int p = 0; p < n_parts && st == KRR_OK; ++p)
+        st = accel_build(&parts[p], d_v + 9 * (size_t)part_begin[p], part_begin[p + 1] - part_begin[p], s);
+    auto release = [&]() { for (auto &q : parts) accel_free(&q); };
+    if (st != KRR_OK) { release(); return st; }
+    accel_free(a);
+    a->node_format = parts[0].node_format;
+    a->max_leaf = parts[0].max_leaf;
+    a->full_leaf = parts[0].full_leaf;
+    a->builder = parts[0].builder;
+    const int quads = kNodeQuads[a->node_format];
+    int64_t n_nodes = 0;
+    a->roots.assign(n_parts, 0);
+    for (int p = 0; p < n_parts; ++p) {
+        a->roots[p] = (uint32_t)n_nodes;
+        n_nodes += parts[p].n_tris ? parts[p].n_nodes : 1;   // an empty part gets an empty node
+    }
+    a->n_tris = n;
+    a->n_nodes = n_nodes;
+    a->max_depth = 0;
+    a->build_ms = 0.0;
+    for (int k = 0; k < 3; ++k) { a->scene_lo[k] = INFINITY; a->scene_hi[k] = -INFINITY; }
+    a->part_bounds.assign(6 * (size_t)n_parts, 0.f);
+    for (int p = 0; p < n_parts; ++p)
+        if (parts[p].n_tris)
+            for (int k = 0; k < 3; ++k) {
+                a->part_bounds[6 * p + k] = parts[p].scene_lo[k];
+                a->part_bounds[6 * p + 3 + k] = parts[p].scene_hi[k];
+            }
+    auto check = [&](cudaError_t e, const char *what) {
+        if (st == KRR_OK && e != cudaSuccess) st = cuda_status(e, what, __FILE__, __LINE__);
+    };
+    check(cudaMalloc(&a->d_scratch, 64), "cudaMalloc");
+    if (st == KRR_OK) check(cudaMemsetAsync(a->d_scratch, 0, 64, s), "cudaMemsetAsync");
+    check(cudaMalloc(&a->d_nodes, quads * sizeof(float4) * (size_t)n_nodes), "cudaMalloc");
+    check(cudaMalloc(&a->d_tris, 3 * sizeof(float4) * (size_t)std::max<int64_t>(n, 1)), "cudaMalloc");
+    check(cudaMalloc(&a->d_leaf_of_prim, sizeof(uint32_t) * (size_t)std::max<int64_t>(n, 1)), "cudaMalloc");
+    check(cudaMalloc(&a->d_roots, sizeof(uint32_t) * n_parts), "cudaMalloc");
+    for (int p = 0; p < n_parts && st == KRR_OK; ++p) {
+        const krr_accel &q = parts[p];
+        const int64_t tri0 = part_begin[p] - part_begin[0];
+        float4 *nodes = a->d_nodes + quads * (size_t)a->roots[p];
+        a->max_depth = std::max(a->max_depth, q.max_depth);
+        a->build_ms += q.build_ms;
+        if (q.n_tris == 0) {
+            k_empty_node<<<1, 1, 0, s>>>(nodes, a->node_format);
+            check(cudaGetLastError(), "k_empty_node");
+            continue;
+        }
+        for (int k = 0; k < 3; ++k) {
+            a->scene_lo[k] = std::min(a->scene_lo[k], q.scene_lo[k]);
+            a->scene_hi[k] = std::max(a->scene_hi[k], q.scene_hi[k]);
+        }
+        check(cudaMemcpyAsync(nodes, q.d_nodes, quads * sizeof(float4) * (size_t)q.n_nodes,
+                              cudaMemcpyDeviceToDevice, s), "cudaMemcpyAsync");
+        check(cudaMemcpyAsync(a->d_tris + 3 * (size_t)tri0, q.d_tris, 3 * sizeof(float4) * (size_t)q.n_tris,
+                              cudaMemcpyDeviceToDevice, s), "cudaMemcpyAsync");
+        check(cudaMemcpyAsync(a->d_leaf_of_prim + tri0, q.d_leaf_of_prim, sizeof(uint32_t) * (size_t)q.n_tris,
+                              cudaMemcpyDeviceToDevice, s), "cudaMemcpyAsync");
+        k_relocate_nodes<<<blocks_for(q.n_nodes), kBuildThreads, 0, s>>>(
+            nodes, q.n_nodes, quads, a->node_format == 1 ? 12 : 1, a->roots[p], (uint32_t)tri0);
+        k_relocate_tris<<<blocks_for(q.n_tris), kBuildThreads, 0, s>>>(a->d_tris + 3 * (size_t)tri0,
+                                                                        a->d_leaf_of_prim + tri0, q.n_tris,
+                                                                        (uint32_t)tri0);
+        check(cudaGetLastError(), "relocate");
+    }
+    if (st == KRR_OK)
+        check(cudaMemcpyAsync(a->d_roots, a->roots.data(), sizeof(uint32_t) * n_parts, cudaMemcpyHostToDevice, s),
+              "cudaMemcpyAsync");
+    if (st == KRR_OK) check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    release();
+    a->level_first.clear();   // no refit of a multi-part structure
+    return st;
 }
 
 }  // namespace krr

@@ -57,6 +57,11 @@ struct krr_accel {
     // refit (krr_accel_refit): first node of each tree level (level L holds
     // nodes [level_first[L-1], level_first[L])) and the refitted node bounds
     std::vector<int32_t> level_first;
+    // several BVHs in one node array (accel_build_parts): the root node of
+    // each part; rays pick their part's root.  Empty with one part (root 0).
+    std::vector<uint32_t> roots;
+    uint32_t *d_roots = nullptr;
+    std::vector<float> part_bounds;    // per part: lo.xyz, hi.xyz (accel_build_parts)
     float4 *d_node_bounds = nullptr;   // 2 per node: lo, hi
     float4 *stage_rays = nullptr;
     float4 *stage_hits = nullptr;
@@ -82,6 +87,12 @@ int accel_build(krr_accel *a, const float *d_vertices, int64_t n_tris, cudaStrea
 // bottom-up over the existing tree; the buffers keep their addresses.
 int accel_refit(krr_accel *a, const float *d_vertices, int64_t n_tris, cudaStream_t stream);
 void accel_free(krr_accel *a);
+// Several BVHs, one per part of the triangles (part p holds the global ids
+// [part_begin[p], part_begin[p + 1])), in one node and triangle array: part
+// p's tree starts at a->roots[p].  Hits are those of a build per part.  One
+// part builds as accel_build.
+int accel_build_parts(krr_accel *a, const float *d_vertices, const int64_t *part_begin, int n_parts,
+                      cudaStream_t stream);
 
 struct TraceLaunch {
     const float4 *ray_o;      // origin.xyz, tmin
@@ -102,6 +113,13 @@ struct TraceLaunch {
     const float4 *any_o;
     const float4 *any_d;
     const int *d_any_count;
+    // Several BVHs (accel_build_parts): ray i starts at roots[pixel_part[p]]
+    // with p the pixel id in ray_pix[i * ray_stride].w (any_pix for the
+    // any-hit set); roots == nullptr: every ray starts at node 0.
+    const uint32_t *roots;
+    const uint8_t *pixel_part;
+    const float4 *ray_pix;
+    const float4 *any_pix;
 };
 
 int launch_trace_closest(const krr_accel *a, const TraceLaunch &l, cudaStream_t s);

@@ -210,21 +210,22 @@ __device__ __forceinline__ V3 box_inverse(V3 d) {
     return V3{1.f / dx, 1.f / dy, 1.f / dz};
 }
 
-// Single-ray traversal for kernels that trace inside their own loops.
+// Single-ray traversal for kernels that trace inside their own loops, from
+// node `root` (a part's tree in a multi-part node array).
 // Closest hit: returns (t, b1, b2, id bits) or id KRR_MISS; any hit: the id
 // of some blocking triangle (mask != 0, or any triangle when !MASKED) or
 // KRR_MISS.  Same hit as the persistent kernel (the result does not depend
 // on traversal order).
 template <bool ANY, int FMT, bool MASKED = true>
 __device__ float4 traverse_ray(const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
-                               V3 o, V3 d, float tmin, float tmax, int *err) {
+                               V3 o, V3 d, float tmin, float tmax, int *err, uint32_t root = 0) {
     RayPre r = ray_pre(o, d, tmin);
     V3 inv = box_inverse(d);
     V3 oinv = V3{-o.x * inv.x, -o.y * inv.y, -o.z * inv.z};
     int oct = (inv.x < 0.f ? 1 : 0) | (inv.y < 0.f ? 2 : 0) | (inv.z < 0.f ? 4 : 0);
     uint2 stack[kTraversalStack];
     int sp = 0;
-    uint2 ng = make_uint2(0u, (1u << oct) | (1u << 8)), tg = make_uint2(0u, 0u);
+    uint2 ng = make_uint2(root, (1u << oct) | (1u << 8)), tg = make_uint2(0u, 0u);
     float b1b = 0.f, b2b = 0.f;
     uint32_t best = KRR_MISS;
     while (true) {

@@ -51,6 +51,8 @@ struct DevView {
     int64_t offset;
     uint32_t sample_index;   // frame_index * spp + seed of the view
     uint32_t seed;           // seed of the view (kept for replays without new views)
+    int32_t part;            // scene of the view (krr_wf_set_scenes)
+    int32_t pad;
 };
 
 // Per-frame constants read by kernels from device memory (so that a frame
@@ -77,8 +79,26 @@ struct krr_wf {
     bool has_scene = false;
     bool medium = false;        // enable_medium && scene has media
     DevScene scene{};
-    float scene_radius = 1.f;
     krr_accel accel{};
+    // scenes of the pass (krr_wf_set_scenes): first global triangle id of each
+    // (and the total at the end), light ranges, first medium, bounding-sphere
+    // radius, the scene of each infinite light, the cache's box
+    std::vector<int64_t> part_tri_begin{0, 0};
+    std::vector<DevScenePart> parts{DevScenePart{}};
+    std::vector<int32_t> part_media_begin{0};
+    std::vector<float> part_radius{1.f};
+    std::vector<int32_t> inf_part;
+    std::vector<int32_t> part_own_depth;   // -1: the pass's max_depth
+    int32_t n_parts = 1;
+    uint8_t *d_pixel_part = nullptr;   // [n] scene of each pixel's view
+    // launch shapes and queue capacity (krr_wf_set_launch, krr_wf_autotune):
+    // threads per block and resident blocks per SM of the stage kernels, and
+    // the pixels traced together in render() (queue capacity; 0 = all)
+    int32_t block = 256;
+    int32_t blocks_per_sm = 8;
+    int64_t wave = 0;
+    int64_t qcap = 0;                  // allocated queue capacity
+    float cache_lo[3] = {0, 0, 0}, cache_hi[3] = {1, 1, 1};
     std::vector<void *> scene_allocs;
     std::vector<DevInstance> h_instances;     // host copies for instance updates
     float *d_world = nullptr;                 // flattened triangles, kept for refits
@@ -116,7 +136,7 @@ struct krr_wf {
     int32_t max_null_collisions = kMaxNullCollisions;       // krr_wf_set_loop_limits
     int32_t max_interface_crossings = kMaxInterfaceCrossings;
 
-    Queue q(int k) const { return Queue{qbuf[k], (int32_t)n, d_counts + k}; }
+    Queue q(int k) const { return Queue{qbuf[k], (int32_t)qcap, d_counts + k}; }
     int32_t *nrc_q_count() const { return d_counts + 9; }
     int32_t *nrc_b_count() const { return d_counts + 10; }
     int32_t *shadow_tracked_count() const { return d_counts + 11; }
@@ -131,6 +151,15 @@ struct krr_wf {
         return c;
     }
 };
+
+static int sync_part_depths(krr_wf *wf);
+
+// Bounces of the render loop: the largest path depth of the pass's scenes.
+static int loop_depth(const krr_wf *wf) {
+    int d = wf->params.max_depth;
+    for (const DevScenePart &p : wf->parts) d = std::max(d, p.max_depth);
+    return d;
+}
 
 namespace {
 
@@ -395,12 +424,14 @@ __global__ void k_begin_frame(PixelState ps, const DevView *__restrict__ views,
 }
 
 // generateCameraRays + CameraData::getRay, integrator.cpp:166-179, camera.h:32-58
+// Pixels [p0, p0 + n) of the frame into ray queue items 0..n-1.
 __global__ void k_camera_rays(PixelState ps, Queue rq, const DevView *__restrict__ views,
-                              const FrameConst *__restrict__ fc, int64_t n) {
+                              const FrameConst *__restrict__ fc, int64_t p0, int64_t n) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *rq.count = (int32_t)n;
     const int nv = fc->n_views;
-    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n;
-         g += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t g = p0 + q;
         const DevView &v = views[view_of(views, nv, g)];
         const DevCamera &cam = v.cam;
         int64_t i = g - v.offset;
@@ -418,13 +449,13 @@ __global__ void k_camera_rays(PixelState ps, Queue rq, const DevView *__restrict
         V3 o = V3{cam.pos[0], cam.pos[1], cam.pos[2]};
         V3 d = mat3_mul(cam.rot, fd);
         float time = cam.shutter_open + cam.shutter_time * tm;
-        rq.at(0, g) = f4(o, 0.f);
-        rq.at(1, g) = f4(d, INFINITY);
-        rq.at(2, g) = make_float4(0.f, 0.f, 0.f, ibits(cam.medium));
-        rq.at(3, g) = make_float4(0.f, 0.f, 0.f, fbits(0u));
-        rq.at(4, g) = make_float4(1.f, 1.f, 1.f, fbits(0u));
-        rq.at(5, g) = make_float4(1.f, 1.f, 1.f, fbits((uint32_t)g));
-        rq.at(6, g) = make_float4(1.f, 1.f, 1.f, time);
+        rq.at(0, q) = f4(o, 0.f);
+        rq.at(1, q) = f4(d, INFINITY);
+        rq.at(2, q) = make_float4(0.f, 0.f, 0.f, ibits(cam.medium));
+        rq.at(3, q) = make_float4(0.f, 0.f, 0.f, fbits(0u));
+        rq.at(4, q) = make_float4(1.f, 1.f, 1.f, fbits(0u));
+        rq.at(5, q) = make_float4(1.f, 1.f, 1.f, fbits((uint32_t)g));
+        rq.at(6, q) = make_float4(1.f, 1.f, 1.f, time);
     }
 }
 
@@ -459,9 +490,16 @@ struct NrcHook {
     float spread_c;            // termination threshold c of a(x1..xn) > c a0
 };
 
-__device__ __forceinline__ void nrc_features(const DevScene &s, const Surf &sf, float *dst) {
+// Cache record of a surface vertex; in a pass of several scenes the position
+// is offset so that each scene has its own region of the cache's box.
+__device__ __forceinline__ void nrc_features(const DevScene &s, const Surf &sf, uint32_t pixel,
+                                             float *dst) {
     const DevMaterial &m = s.materials[sf.material];
     dst[0] = sf.p.x; dst[1] = sf.p.y; dst[2] = sf.p.z;
+    if (s.pixel_part) {
+        const DevScenePart &P = part_of(s, pixel);
+        dst[0] += P.cache_offset[0]; dst[1] += P.cache_offset[1]; dst[2] += P.cache_offset[2];
+    }
     dst[3] = sf.n.x; dst[4] = sf.n.y; dst[5] = sf.n.z;
     dst[6] = 1.f - m.spec_alpha;
     dst[7] = m.diffuse[0]; dst[8] = m.diffuse[1]; dst[9] = m.diffuse[2];
@@ -499,7 +537,7 @@ __device__ __forceinline__ bool nrc_vertex(const NrcHook &h, const DevScene &s, 
         int k = h.rec_count[slot];
         if (k < h.rec_max) {
             float *r = h.rec + ((size_t)slot * h.rec_max + k) * kNrcRecFloats;
-            nrc_features(s, sf, r);
+            nrc_features(s, sf, pixel, r);
             float4 l = ps.L[pixel];
             r[kNrcInputs + 0] = thp.x; r[kNrcInputs + 1] = thp.y; r[kNrcInputs + 2] = thp.z;
             r[kNrcInputs + 3] = l.x; r[kNrcInputs + 4] = l.y; r[kNrcInputs + 5] = l.z;
@@ -509,7 +547,7 @@ __device__ __forceinline__ bool nrc_vertex(const NrcHook &h, const DevScene &s, 
     }
     int j = push_slot(h.q_count, h.q_cap, err);
     if (j >= 0) {
-        nrc_features(s, sf, h.q_in + (size_t)kNrcInputs * j);
+        nrc_features(s, sf, pixel, h.q_in + (size_t)kNrcInputs * j);
         h.q_meta[j] = make_float4(thp.x, thp.y, thp.z, __uint_as_float(pixel));
     }
     return true;
@@ -565,10 +603,11 @@ __global__ void k_clamp_count(int32_t *count, int cap) {
 
 // Radiance of an emissive hit (handleHit, integrator.cpp:78-90): emitted
 // radiance times throughput, MIS-weighted against light sampling.
-__device__ __forceinline__ V3 hit_light_radiance(const DevScene &s, int32_t light, V3 p, V3 nrm,
-                                                  V3 wo, V3 ctx_p, uint32_t bsdf_type, uint32_t depth,
-                                                  V3 thp, V3 pu, V3 pl, int nee) {
-    const float lsel_pdf = 1.f / (float)s.n_lights;
+__device__ __forceinline__ V3 hit_light_radiance(const DevScene &s, const DevScenePart &P,
+                                                  int32_t light, V3 p, V3 nrm, V3 wo, V3 ctx_p,
+                                                  uint32_t bsdf_type, uint32_t depth, V3 thp, V3 pu,
+                                                  V3 pl, int nee) {
+    const float lsel_pdf = 1.f / (float)P.n_lights;
     const DevLight &l = s.lights[light];
     const DevInstance &I = s.instances[l.index];
     V3 Le = area_L(I, nrm, wo) * thp;
@@ -583,12 +622,13 @@ __device__ __forceinline__ V3 hit_light_radiance(const DevScene &s, int32_t ligh
 
 // Radiance of a miss (handleMiss, integrator.cpp:92-108): every infinite
 // light, MIS-weighted against light sampling, times throughput.
-__device__ __forceinline__ V3 miss_radiance(const DevScene &s, V3 dir, uint32_t bsdf_type,
-                                             uint32_t depth, V3 thp, V3 pu, V3 pl, int nee) {
-    const float lsel_pdf = 1.f / (float)s.n_lights;
+__device__ __forceinline__ V3 miss_radiance(const DevScene &s, const DevScenePart &P, V3 dir,
+                                             uint32_t bsdf_type, uint32_t depth, V3 thp, V3 pu, V3 pl,
+                                             int nee) {
+    const float lsel_pdf = 1.f / (float)P.n_lights;
     V3 L = v3(0.f);
-    for (int k = 0; k < s.n_infinite; ++k) {
-        const DevInfinite &e = s.infinite[k];
+    for (int k = 0; k < P.n_infinite; ++k) {
+        const DevInfinite &e = s.infinite[P.inf_begin + k];
         if (nee && depth && !(bsdf_type & BSDF_DELTA)) {
             float light_pdf = kInv4Pi * lsel_pdf;
             L += env_Li(e, dir) / mean(pu + pl * light_pdf);
@@ -627,8 +667,11 @@ k_hit_process(DevScene s, Queue rq, const float4 *__restrict__ hits, Queue next,
                 if (s.n_infinite > 0) {
                     float4 c1 = rq.at(1, i), c3 = rq.at(3, i), c4 = rq.at(4, i), c5 = rq.at(5, i),
                            c6 = rq.at(6, i);
-                    add_radiance(ps, ubits(c5.w), miss_radiance(s, f3(c1), ubits(c3.w), ubits(c4.w),
-                                                                f3(c4), f3(c5), f3(c6), nee));
+                    const DevScenePart &P = part_of(s, ubits(c5.w));
+                    if (P.n_infinite > 0)
+                        add_radiance(ps, ubits(c5.w),
+                                     miss_radiance(s, P, f3(c1), ubits(c3.w), ubits(c4.w), f3(c4),
+                                                   f3(c5), f3(c6), nee));
                 }
             } else {
                 int j = push_slot(miss.count, miss.cap, err);
@@ -670,9 +713,9 @@ k_hit_process(DevScene s, Queue rq, const float4 *__restrict__ hits, Queue next,
                                     dir, f3(c5), f3(c6), err))
             continue;
         if (sf.light >= 0 && inline_lights) {
-            add_radiance(ps, ubits(c5.w), hit_light_radiance(s, sf.light, sf.p, sf.n, sf.wo, f3(c2),
-                                                             ubits(c3.w), ubits(c4.w), thp, f3(c5),
-                                                             f3(c6), nee));
+            add_radiance(ps, ubits(c5.w),
+                         hit_light_radiance(s, part_of(s, ubits(c5.w)), sf.light, sf.p, sf.n, sf.wo,
+                                            f3(c2), ubits(c3.w), ubits(c4.w), thp, f3(c5), f3(c6), nee));
         } else if (sf.light >= 0) {
             int j = push_slot(hitl.count, hitl.cap, err);
             if (j >= 0) {
@@ -709,8 +752,8 @@ __global__ void k_handle_hit(DevScene s, Queue hitl, PixelState ps, int nee) {
         float4 c0 = hitl.at(0, i), c1 = hitl.at(1, i), c2 = hitl.at(2, i), c3 = hitl.at(3, i);
         float4 c4 = hitl.at(4, i), c5 = hitl.at(5, i), c6 = hitl.at(6, i), c7 = hitl.at(7, i);
         add_radiance(ps, ubits(c5.w),
-                     hit_light_radiance(s, sbits(c0.w), f3(c0), f3(c1), f3(c2), f3(c3), ubits(c3.w),
-                                        ubits(c4.w), f3(c5), f3(c6), f3(c7), nee));
+                     hit_light_radiance(s, part_of(s, ubits(c5.w)), sbits(c0.w), f3(c0), f3(c1), f3(c2),
+                                        f3(c3), ubits(c3.w), ubits(c4.w), f3(c5), f3(c6), f3(c7), nee));
     }
 }
 
@@ -721,7 +764,8 @@ __global__ void k_handle_miss(DevScene s, Queue miss, PixelState ps, int nee) {
         float4 c1 = miss.at(1, i), c3 = miss.at(3, i), c4 = miss.at(4, i), c5 = miss.at(5, i),
                c6 = miss.at(6, i);
         add_radiance(ps, ubits(c5.w),
-                     miss_radiance(s, f3(c1), ubits(c3.w), ubits(c4.w), f3(c4), f3(c5), f3(c6), nee));
+                     miss_radiance(s, part_of(s, ubits(c5.w)), f3(c1), ubits(c3.w), ubits(c4.w), f3(c4),
+                                   f3(c5), f3(c6), nee));
     }
 }
 
@@ -747,12 +791,13 @@ __device__ __forceinline__ void scatter_item(const DevScene &s, const Queue &sca
     Bsdf bsdf = Bsdf::setup(sd);
     // a scene without emitters has nothing to sample (the reference indexes an
     // empty light list there); NEE and its draws are skipped
-    if (nee && (bsdf_type & BSDF_SMOOTH) && s.n_lights > 0) {
+    const DevScenePart &P = part_of(s, pixel);
+    if (nee && (bsdf_type & BSDF_SMOOTH) && P.n_lights > 0) {
         float ul = rng.get1d();
-        uint32_t lid = (uint32_t)(ul * (float)s.n_lights);
-        float sel_pdf = 1.f / (float)s.n_lights;
+        uint32_t lid = (uint32_t)(ul * (float)P.n_lights);
+        float sel_pdf = 1.f / (float)P.n_lights;
         float u0 = rng.get1d(), u1 = rng.get1d();
-        LightSample ls = sample_li(s, s.lights[lid], u0, u1, p);
+        LightSample ls = sample_li(s, s.lights[P.light_begin + lid], u0, u1, p);
         // spawnRayTo(Interaction), raytracing.h:151-160
         V3 to = offset_ray_origin(ls.p, ls.n, p - ls.p);
         V3 po = offset_ray_origin(p, nrm, to - p);
@@ -814,6 +859,9 @@ __global__ void k_scatter_classify(DevScene s, Queue scat, PixelState ps, float 
     const int lane = threadIdx.x & 31;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t pixel = ubits(scat.at(2, i).w);
+        // a path of a scene with a smaller depth than the pass's ends here,
+        // as its scene's pass ends the bounce loop (no draws)
+        if (s.pixel_part && (int)ubits(scat.at(1, i).w) >= part_of(s, pixel).max_depth) continue;
         Pcg rng = load_rng(ps, pixel);
         if (rng.get1d() >= rr) {
             store_rng(ps, pixel, rng);   // the path ends here
@@ -922,7 +970,7 @@ k_medium_sample(DevScene s, Queue msq, Queue next, Queue miss, Queue hitl, Queue
             pu *= r;
             pl *= r;
         }
-        if (scattered || !any(thp) || !any(pu) || (int)depth == max_depth) continue;
+        if (scattered || !any(thp) || !any(pu) || (int)depth == part_of(s, pixel).max_depth) continue;
         if (isinf(tmax_hit)) {
             int j = push_slot(miss.count, miss.cap, err);
             if (j >= 0) {
@@ -979,20 +1027,22 @@ k_medium_sample(DevScene s, Queue msq, Queue next, Queue miss, Queue hitl, Queue
 __global__ void k_medium_scatter(DevScene s, Queue mscat, Queue next, Queue shadow, PixelState ps,
                                  int nee, uint32_t *err) {
     int n = min(*mscat.count, mscat.cap);   // an overflowed queue holds cap items
-    float sel_pdf = 1.f / (float)s.n_lights;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 c0 = mscat.at(0, i), c1 = mscat.at(1, i), c2 = mscat.at(2, i), c3 = mscat.at(3, i);
         V3 p = f3(c0), wo = f3(c1), wthp = f3(c2), wpu = f3(c3);
         int32_t medium = sbits(c0.w);
         uint32_t depth = ubits(c1.w), pixel = ubits(c2.w);
+        if (s.pixel_part && (int)depth >= part_of(s, pixel).max_depth) continue;   // as k_scatter_classify
         float time = c3.w;
         float g = s.media[medium].g;
         Pcg rng = load_rng(ps, pixel);
-        if (nee && s.n_lights > 0) {
+        const DevScenePart &P = part_of(s, pixel);
+        const float sel_pdf = 1.f / (float)P.n_lights;
+        if (nee && P.n_lights > 0) {
             float ul = rng.get1d();
-            uint32_t lid = (uint32_t)(ul * (float)s.n_lights);
+            uint32_t lid = (uint32_t)(ul * (float)P.n_lights);
             float u0 = rng.get1d(), u1 = rng.get1d();
-            LightSample ls = sample_li(s, s.lights[lid], u0, u1, p);
+            LightSample ls = sample_li(s, s.lights[P.light_begin + lid], u0, u1, p);
             V3 to = offset_ray_origin(ls.p, ls.n, p - ls.p);
             V3 d = to - p;
             V3 wi = normalize(d);
@@ -1061,8 +1111,9 @@ k_shadow_tr(DevScene s, const float4 *__restrict__ nodes, const float4 *__restri
         int ch = main_index(ps.L[pixel].w);
         V3 T_ray = v3(1.f), pu = v3(1.f), pl = v3(1.f);
         int crossings = 0;
+        const uint32_t root = root_of(s, pixel);
         while (fabsf(d.x) > kRayEps * 2 || fabsf(d.y) > kRayEps * 2 || fabsf(d.z) > kRayEps * 2) {
-            float4 h = traverse_ray<false, FMT>(nodes, tris, o, d, 0.f, tmax, trace_err);
+            float4 h = traverse_ray<false, FMT>(nodes, tris, o, d, 0.f, tmax, trace_err, root);
             bool visible = ubits(h.w) == KRR_MISS;
             Surf sf;
             if (!visible) {
@@ -1123,21 +1174,35 @@ k_shadow_tr(DevScene s, const float4 *__restrict__ nodes, const float4 *__restri
 // here with the same expression.  Every other ray (one that starts in a
 // medium, meets a surface or has a zero-length direction) is copied to
 // `tracked` for k_shadow_tr, so that the tracker's warps hold only the long
-// ratio-tracking loops.
+// ratio-tracking loops.  In a pass of several scenes, the shadow rays of a
+// scene without media need no tracking at all: the transmittance loop there
+// draws no samples and ends at the first opaque surface, so an any-hit test
+// that ignores null-material surfaces decides them, as traceShadow does
+// without media.
 template <int FMT>
-__global__ void k_shadow_split(const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
-                               Queue shadow, Queue tracked, PixelState ps, uint32_t *err,
-                               int *trace_err) {
+__global__ void k_shadow_split(DevScene s, const float4 *__restrict__ nodes,
+                               const float4 *__restrict__ tris, Queue shadow, Queue tracked,
+                               PixelState ps, uint32_t *err, int *trace_err) {
     int n = min(*shadow.count, shadow.cap);   // an overflowed queue holds cap items
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 c0 = shadow.at(0, i), c1 = shadow.at(1, i), c3 = shadow.at(3, i);
+        float4 c0 = shadow.at(0, i), c1 = shadow.at(1, i), c2 = shadow.at(2, i), c3 = shadow.at(3, i);
         V3 d = f3(c1);
+        const uint32_t pixel = ubits(c2.w);
+        const uint32_t root = root_of(s, pixel);
         bool moving = fabsf(d.x) > kRayEps * 2 || fabsf(d.y) > kRayEps * 2 || fabsf(d.z) > kRayEps * 2;
-        if (sbits(c3.w) < 0 && moving) {
-            float4 h = traverse_ray<true, FMT, false>(nodes, tris, f3(c0), d, 0.f, c1.w, trace_err);
+        if (s.pixel_part && !part_of(s, pixel).has_media) {
+            float4 h = traverse_ray<true, FMT, true>(nodes, tris, f3(c0), d, 0.f, c1.w, trace_err, root);
             if (ubits(h.w) == KRR_MISS) {
-                float4 c2 = shadow.at(2, i), c4 = shadow.at(4, i);
-                add_radiance(ps, ubits(c2.w), f3(c2) * v3(1.f) / mean(f3(c3) * v3(1.f) + f3(c4) * v3(1.f)));
+                float4 c4 = shadow.at(4, i);
+                add_radiance(ps, pixel, f3(c2) * v3(1.f) / mean(f3(c3) * v3(1.f) + f3(c4) * v3(1.f)));
+            }
+            continue;
+        }
+        if (sbits(c3.w) < 0 && moving) {
+            float4 h = traverse_ray<true, FMT, false>(nodes, tris, f3(c0), d, 0.f, c1.w, trace_err, root);
+            if (ubits(h.w) == KRR_MISS) {
+                float4 c4 = shadow.at(4, i);
+                add_radiance(ps, pixel, f3(c2) * v3(1.f) / mean(f3(c3) * v3(1.f) + f3(c4) * v3(1.f)));
                 continue;
             }
         }
@@ -1402,6 +1467,20 @@ int grid_for(int64_t n) {
     return (int)std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)sms * 8));
 }
 
+// Blocks of the grid-stride stage kernels: enough for n items, at most the
+// pass's blocks per SM on every SM.
+int stage_grid(const krr_wf *wf, int64_t n) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    int64_t g = (n + wf->block - 1) / wf->block;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)sms * wf->blocks_per_sm));
+}
+
 template <typename T>
 int dev_upload(krr_wf *wf, T **dst, const T *src, size_t count) {
     *dst = nullptr;
@@ -1430,6 +1509,8 @@ void free_queues(krr_wf *wf) {
     cudaFree(wf->scatter_lists); wf->scatter_lists = nullptr;
     cudaFree(wf->ps.L); cudaFree(wf->ps.pixel); cudaFree(wf->ps.rng);
     wf->ps = PixelState{};
+    cudaFree(wf->d_pixel_part); wf->d_pixel_part = nullptr;
+    wf->scene.pixel_part = nullptr;
 }
 
 // 3x3 inverse-transpose of a row-major 3x4 transform's linear part, in double.
@@ -1463,7 +1544,7 @@ static int alloc_nrc_buffers(krr_wf *wf) {
     if (!wf->nrc || !wf->n) return KRR_OK;
     int stride = nrc_train_stride(wf->nrc);
     wf->nrc_slots = (wf->n + stride - 1) / stride;
-    wf->nrc_rec_max = std::min(16, std::max(1, wf->params.max_depth + 1));
+    wf->nrc_rec_max = std::min(16, std::max(1, loop_depth(wf) + 1));
     int64_t batch = nrc_batch_size(wf->nrc);
     KRR_CUDA(cudaMalloc(&wf->nrc_q_in, (size_t)wf->n * kNrcInputs * sizeof(float)));
     KRR_CUDA(cudaMalloc(&wf->nrc_q_meta, (size_t)wf->n * sizeof(float4)));
@@ -1548,6 +1629,17 @@ extern "C" int krr_wf_set_params(krr_wf *wf, const krr_wf_params *params) {
     KRR_CHECK_ARG(params->max_depth >= 0 && params->spp >= 1, "bad parameters");
     wf->params = *params;
     wf->medium = wf->params.enable_medium && wf->scene.n_media > 0;
+    return sync_part_depths(wf);
+}
+
+extern "C" int krr_wf_set_scene_max_depth(krr_wf *wf, int32_t scene, int32_t max_depth) {
+    KRR_CHECK_ARG(wf && wf->has_scene, "no scene");
+    KRR_CHECK_ARG(scene >= 0 && scene < wf->n_parts, "scene index out of range");
+    KRR_CHECK_ARG(max_depth >= -1, "max_depth >= 0, or -1 for the pass's");
+    wf->part_own_depth.resize(wf->parts.size(), -1);
+    wf->part_own_depth[scene] = max_depth;
+    KRR_TRY(sync_part_depths(wf));
+    if (wf->n) KRR_TRY(alloc_nrc_buffers(wf));   // training records per path vertex
     return KRR_OK;
 }
 
@@ -1556,6 +1648,35 @@ extern "C" int krr_wf_set_params(krr_wf *wf, const krr_wf_params *params) {
 // bounding-box diagonal, src/core/device/scene.cpp:108).
 // World-space triangles of the instances into the BVH: a full build, or with
 // `refit` new boxes over the existing tree (same triangles, moved).
+// The scene of each pixel (its view's) for a pass with several scenes; the
+// views must name scenes the pass holds.
+static int fill_pixel_parts(krr_wf *wf, cudaStream_t st) {
+    for (const DevView &v : wf->layout)
+        KRR_CHECK_ARG(v.part >= 0 && (!wf->has_scene || v.part < wf->n_parts),
+                      "a view names a scene the pass does not hold");
+    if (wf->n_parts <= 1 || !wf->n) {
+        wf->scene.pixel_part = nullptr;
+        return KRR_OK;
+    }
+    if (!wf->d_pixel_part) KRR_CUDA(cudaMalloc(&wf->d_pixel_part, (size_t)wf->n));
+    for (const DevView &v : wf->layout)
+        KRR_CUDA(cudaMemsetAsync(wf->d_pixel_part + v.offset, v.part, (size_t)v.w * v.h, st));
+    wf->scene.pixel_part = wf->d_pixel_part;
+    return KRR_OK;
+}
+
+// Each scene's path depth: its own (krr_wf_set_scene_max_depth) or the
+// pass's; uploaded with the scene parts.
+static int sync_part_depths(krr_wf *wf) {
+    wf->part_own_depth.resize(wf->parts.size(), -1);
+    for (size_t p = 0; p < wf->parts.size(); ++p)
+        wf->parts[p].max_depth = wf->part_own_depth[p] >= 0 ? wf->part_own_depth[p] : wf->params.max_depth;
+    if (wf->scene.parts)
+        KRR_CUDA(cudaMemcpy(const_cast<DevScenePart *>(wf->scene.parts), wf->parts.data(),
+                            wf->parts.size() * sizeof(DevScenePart), cudaMemcpyHostToDevice));
+    return KRR_OK;
+}
+
 static int rebuild_bvh(krr_wf *wf, cudaStream_t st, bool refit = false) {
     const uint64_t n_tris = wf->n_tris;
     DevScene &s = wf->scene;
@@ -1567,7 +1688,7 @@ static int rebuild_bvh(krr_wf *wf, cudaStream_t st, bool refit = false) {
     if (n_tris) k_flatten<<<grid_for(n_tris), kThreads, 0, st>>>(s, wf->n_instances, d_world, n_tris);
     KRR_CUDA(cudaGetLastError());
     int stat = refit ? accel_refit(&wf->accel, d_world, (int64_t)n_tris, st)
-                     : accel_build(&wf->accel, d_world, (int64_t)n_tris, st);
+                     : accel_build_parts(&wf->accel, d_world, wf->part_tri_begin.data(), wf->n_parts, st);
     if (stat == KRR_OK) stat = cuda_status(cudaStreamSynchronize(st), "BVH", __FILE__, __LINE__);
     if (!refit || stat != KRR_OK) {
         cudaFree(wf->d_world);
@@ -1586,118 +1707,194 @@ static int rebuild_bvh(krr_wf *wf, cudaStream_t st, bool refit = false) {
         cudaFree(mask);
         if (stat != KRR_OK) return stat;
     }
-    float dx = wf->accel.scene_hi[0] - wf->accel.scene_lo[0];
-    float dy = wf->accel.scene_hi[1] - wf->accel.scene_lo[1];
-    float dz = wf->accel.scene_hi[2] - wf->accel.scene_lo[2];
-    wf->scene_radius = std::sqrt(dx * dx + dy * dy + dz * dz);
+    // per scene: the bounding-box diagonal (scene radius of the infinite
+    // lights, src/core/device/scene.cpp:108) and the cache offset that puts
+    // the scenes side by side along x, one scene width apart
+    const krr_accel &a = wf->accel;
+    const int np = wf->n_parts;
+    std::vector<float> b(6 * (size_t)np);
+    for (int p = 0; p < np; ++p)
+        for (int k = 0; k < 6; ++k)
+            b[6 * p + k] = np == 1 ? (k < 3 ? a.scene_lo[k] : a.scene_hi[k - 3])
+                                   : a.part_bounds[6 * (size_t)p + k];
+    wf->part_radius.assign(np, 0.f);
+    float x_end = 0.f;
+    for (int k = 0; k < 3; ++k) { wf->cache_lo[k] = INFINITY; wf->cache_hi[k] = -INFINITY; }
+    for (int p = 0; p < np; ++p) {
+        const float dx = b[6 * p + 3] - b[6 * p], dy = b[6 * p + 4] - b[6 * p + 1], dz = b[6 * p + 5] - b[6 * p + 2];
+        wf->part_radius[p] = std::sqrt(dx * dx + dy * dy + dz * dz);
+        DevScenePart &P = wf->parts[p];
+        P.cache_offset[0] = p == 0 ? 0.f : x_end + std::max(dx, 1e-3f) - b[6 * p];
+        P.cache_offset[1] = P.cache_offset[2] = 0.f;
+        x_end = b[6 * p + 3] + P.cache_offset[0];
+        for (int k = 0; k < 3; ++k) {
+            wf->cache_lo[k] = std::min(wf->cache_lo[k], b[6 * p + k] + P.cache_offset[k]);
+            wf->cache_hi[k] = std::max(wf->cache_hi[k], b[6 * p + 3 + k] + P.cache_offset[k]);
+        }
+    }
+    if (s.parts)
+        KRR_CUDA(cudaMemcpy(const_cast<DevScenePart *>(s.parts), wf->parts.data(),
+                            wf->parts.size() * sizeof(DevScenePart), cudaMemcpyHostToDevice));
+    s.part_roots = np > 1 ? wf->accel.d_roots : nullptr;
+    if (!wf->h_infinite.empty() && s.infinite) {
+        for (size_t i = 0; i < wf->h_infinite.size(); ++i)
+            wf->h_infinite[i].scene_radius = wf->part_radius[wf->inf_part[i]];
+        KRR_CUDA(cudaMemcpy(const_cast<DevInfinite *>(s.infinite), wf->h_infinite.data(),
+                            wf->h_infinite.size() * sizeof(DevInfinite), cudaMemcpyHostToDevice));
+    }
     return KRR_OK;
 }
 
 extern "C" int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *sd, void *stream) {
     KRR_CHECK_ARG(wf && sd, "NULL argument");
-    KRR_CHECK_ARG(sd->n_meshes >= 0 && sd->n_instances >= 0 && sd->n_materials >= 0,
-                  "negative counts");
+    return krr_wf_set_scenes(wf, sd, 1, stream);
+}
+
+extern "C" int krr_wf_set_scenes(krr_wf *wf, const krr_scene_desc *scenes, int32_t n_scenes,
+                                 void *stream) {
+    KRR_CHECK_ARG(wf && scenes, "NULL argument");
+    KRR_CHECK_ARG(n_scenes >= 1 && n_scenes <= 255, "1..255 scenes");
+    for (int p = 0; p < n_scenes; ++p)
+        KRR_CHECK_ARG(scenes[p].n_meshes >= 0 && scenes[p].n_instances >= 0 &&
+                          scenes[p].n_materials >= 0 && scenes[p].n_infinite_lights >= 0 &&
+                          scenes[p].n_media >= 0,
+                      "negative counts");
     cudaStream_t st = as_stream(stream);
     cudaDeviceSynchronize();
     free_scene(wf);
 
+    // where each scene's meshes, materials, instances, infinite lights and
+    // media start in the pass's arrays
+    std::vector<int32_t> mesh0(n_scenes + 1, 0), mat0(n_scenes + 1, 0), inst0(n_scenes + 1, 0),
+        inf0(n_scenes + 1, 0), med0(n_scenes + 1, 0);
+    for (int p = 0; p < n_scenes; ++p) {
+        mesh0[p + 1] = mesh0[p] + scenes[p].n_meshes;
+        mat0[p + 1] = mat0[p] + scenes[p].n_materials;
+        inst0[p + 1] = inst0[p] + scenes[p].n_instances;
+        inf0[p + 1] = inf0[p] + scenes[p].n_infinite_lights;
+        med0[p + 1] = med0[p] + scenes[p].n_media;
+    }
+
     // meshes
-    std::vector<DevMesh> meshes(sd->n_meshes);
-    for (int i = 0; i < sd->n_meshes; ++i) {
-        const krr_mesh_desc &m = sd->meshes[i];
-        KRR_CHECK_ARG(m.h_positions && m.h_normals && m.h_indices, "mesh arrays missing (normals are required)");
-        KRR_CHECK_ARG(m.material < sd->n_materials, "mesh material out of range");
-        KRR_CHECK_ARG(m.medium_inside < sd->n_media && m.medium_outside < sd->n_media,
-                      "mesh medium out of range");
-        // meshes that share arrays (same host pointers) share device copies
-        int shared = -1;
-        for (int j = 0; j < i; ++j)
-            if (sd->meshes[j].h_positions == m.h_positions && sd->meshes[j].h_indices == m.h_indices &&
-                sd->meshes[j].n_vertices == m.n_vertices && sd->meshes[j].n_triangles == m.n_triangles &&
-                sd->meshes[j].h_normals == m.h_normals && sd->meshes[j].h_texcoords == m.h_texcoords) {
-                shared = j;
-                break;
+    std::vector<DevMesh> meshes(mesh0[n_scenes]);
+    for (int p = 0; p < n_scenes; ++p) {
+        const krr_scene_desc *sd = scenes + p;
+        for (int i = 0; i < sd->n_meshes; ++i) {
+            const krr_mesh_desc &m = sd->meshes[i];
+            KRR_CHECK_ARG(m.h_positions && m.h_normals && m.h_indices, "mesh arrays missing (normals are required)");
+            KRR_CHECK_ARG(m.material < sd->n_materials, "mesh material out of range");
+            KRR_CHECK_ARG(m.medium_inside < sd->n_media && m.medium_outside < sd->n_media,
+                          "mesh medium out of range");
+            // meshes that share arrays (same host pointers) share device copies
+            int shared = -1;
+            for (int j = 0; j < i; ++j)
+                if (sd->meshes[j].h_positions == m.h_positions && sd->meshes[j].h_indices == m.h_indices &&
+                    sd->meshes[j].n_vertices == m.n_vertices && sd->meshes[j].n_triangles == m.n_triangles &&
+                    sd->meshes[j].h_normals == m.h_normals && sd->meshes[j].h_texcoords == m.h_texcoords) {
+                    shared = mesh0[p] + j;
+                    break;
+                }
+            DevMesh d{};
+            if (shared >= 0) {
+                d = meshes[shared];
+            } else {
+                for (int64_t k = 0; k < 3 * m.n_triangles; ++k)
+                    KRR_CHECK_ARG(m.h_indices[k] < (uint64_t)m.n_vertices, "mesh index out of range");
+                KRR_TRY(dev_upload(wf, const_cast<float **>(&d.pos), m.h_positions, 3 * m.n_vertices));
+                KRR_TRY(dev_upload(wf, const_cast<float **>(&d.nrm), m.h_normals, 3 * m.n_vertices));
+                if (m.h_texcoords) KRR_TRY(dev_upload(wf, const_cast<float **>(&d.uv), m.h_texcoords, 2 * m.n_vertices));
+                KRR_TRY(dev_upload(wf, const_cast<uint32_t **>(&d.idx), m.h_indices, 3 * m.n_triangles));
             }
-        DevMesh d{};
-        if (shared >= 0) {
-            d = meshes[shared];
-        } else {
-            for (int64_t k = 0; k < 3 * m.n_triangles; ++k)
-                KRR_CHECK_ARG(m.h_indices[k] < (uint64_t)m.n_vertices, "mesh index out of range");
-            KRR_TRY(dev_upload(wf, const_cast<float **>(&d.pos), m.h_positions, 3 * m.n_vertices));
-            KRR_TRY(dev_upload(wf, const_cast<float **>(&d.nrm), m.h_normals, 3 * m.n_vertices));
-            if (m.h_texcoords) KRR_TRY(dev_upload(wf, const_cast<float **>(&d.uv), m.h_texcoords, 2 * m.n_vertices));
-            KRR_TRY(dev_upload(wf, const_cast<uint32_t **>(&d.idx), m.h_indices, 3 * m.n_triangles));
+            d.material = m.material >= 0 ? m.material + mat0[p] : m.material;
+            d.medium_inside = m.medium_inside >= 0 ? m.medium_inside + med0[p] : m.medium_inside;
+            d.medium_outside = m.medium_outside >= 0 ? m.medium_outside + med0[p] : m.medium_outside;
+            meshes[mesh0[p] + i] = d;
         }
-        d.material = m.material;
-        d.medium_inside = m.medium_inside;
-        d.medium_outside = m.medium_outside;
-        meshes[i] = d;
     }
     // materials (src/scene/krrscene.cpp:208-227: specular alpha = 1 - roughness)
-    std::vector<DevMaterial> mats(std::max(1, sd->n_materials));
-    for (int i = 0; i < sd->n_materials; ++i) {
-        const krr_material_desc &m = sd->materials[i];
-        KRR_CHECK_ARG(m.type >= 0 && m.type <= 3, "unknown material type");
-        DevMaterial d{};
-        d.type = m.type;
-        for (int k = 0; k < 3; ++k) d.diffuse[k] = m.diffuse[k];
-        d.spec_alpha = 1.f - m.roughness;
-        d.spec_trans = m.specular_transmission;
-        d.eta = m.eta;
-        d.anisotropic = m.anisotropic;
-        mats[i] = d;
-    }
-    // instances, triangle offsets and the light list (src/core/device/scene.cpp:93-132)
-    std::vector<DevInstance> insts(sd->n_instances);
+    std::vector<DevMaterial> mats(std::max(1, mat0[n_scenes]));
+    for (int p = 0; p < n_scenes; ++p)
+        for (int i = 0; i < scenes[p].n_materials; ++i) {
+            const krr_material_desc &m = scenes[p].materials[i];
+            KRR_CHECK_ARG(m.type >= 0 && m.type <= 3, "unknown material type");
+            DevMaterial d{};
+            d.type = m.type;
+            for (int k = 0; k < 3; ++k) d.diffuse[k] = m.diffuse[k];
+            d.spec_alpha = 1.f - m.roughness;
+            d.spec_trans = m.specular_transmission;
+            d.eta = m.eta;
+            d.anisotropic = m.anisotropic;
+            mats[mat0[p] + i] = d;
+        }
+    // instances, triangle offsets and each scene's light list
+    // (src/core/device/scene.cpp:93-132): its mesh lights, then its infinite
+    // lights
+    std::vector<DevInstance> insts(inst0[n_scenes]);
     std::vector<DevLight> lights;
-    std::vector<uint32_t> offsets(std::max(1, sd->n_instances));
+    std::vector<uint32_t> offsets(std::max(1, inst0[n_scenes]));
+    std::vector<DevScenePart> parts(n_scenes);
+    std::vector<int64_t> tri_begin(n_scenes + 1, 0);
     uint64_t n_tris = 0;
-    for (int i = 0; i < sd->n_instances; ++i) {
-        const krr_instance_desc &in = sd->instances[i];
-        KRR_CHECK_ARG(in.mesh >= 0 && in.mesh < sd->n_meshes, "instance mesh out of range");
-        const krr_mesh_desc &m = sd->meshes[in.mesh];
-        DevInstance d{};
-        std::memcpy(d.xf, in.transform, sizeof(d.xf));
-        inverse_transpose(in.transform, d.nxf);
-        d.mesh = in.mesh;
-        d.prim_offset = (uint32_t)n_tris;
-        offsets[i] = (uint32_t)n_tris;
-        d.light_offset = -1;
-        float le[3] = {m.emission[0], m.emission[1], m.emission[2]};
-        if (le[0] > 0.f || le[1] > 0.f || le[2] > 0.f) {
-            float scale = std::max(le[0], std::max(le[1], le[2]));   // mesh.cpp:47-48
-            for (int k = 0; k < 3; ++k) d.le[k] = le[k] / scale;
-            d.le_scale = scale;
-            d.light_offset = (int32_t)lights.size();
-            for (int64_t t = 0; t < m.n_triangles; ++t) lights.push_back(DevLight{0, i, (uint32_t)t, 0});
+    for (int p = 0; p < n_scenes; ++p) {
+        const krr_scene_desc *sd = scenes + p;
+        DevScenePart &P = parts[p];
+        P.light_begin = (int32_t)lights.size();
+        tri_begin[p] = (int64_t)n_tris;
+        for (int i = 0; i < sd->n_instances; ++i) {
+            const krr_instance_desc &in = sd->instances[i];
+            KRR_CHECK_ARG(in.mesh >= 0 && in.mesh < sd->n_meshes, "instance mesh out of range");
+            const krr_mesh_desc &m = sd->meshes[in.mesh];
+            const int gi = inst0[p] + i;
+            DevInstance d{};
+            std::memcpy(d.xf, in.transform, sizeof(d.xf));
+            inverse_transpose(in.transform, d.nxf);
+            d.mesh = in.mesh + mesh0[p];
+            d.prim_offset = (uint32_t)n_tris;
+            offsets[gi] = (uint32_t)n_tris;
+            d.light_offset = -1;
+            float le[3] = {m.emission[0], m.emission[1], m.emission[2]};
+            if (le[0] > 0.f || le[1] > 0.f || le[2] > 0.f) {
+                float scale = std::max(le[0], std::max(le[1], le[2]));   // mesh.cpp:47-48
+                for (int k = 0; k < 3; ++k) d.le[k] = le[k] / scale;
+                d.le_scale = scale;
+                d.light_offset = (int32_t)lights.size();
+                for (int64_t t = 0; t < m.n_triangles; ++t) lights.push_back(DevLight{0, gi, (uint32_t)t, 0});
+            }
+            insts[gi] = d;
+            n_tris += (uint64_t)m.n_triangles;
+            KRR_CHECK_ARG(n_tris < 0x7fffffffull, "too many triangles");
         }
-        insts[i] = d;
-        n_tris += (uint64_t)m.n_triangles;
-        KRR_CHECK_ARG(n_tris < 0x7fffffffull, "too many triangles");
+        // infinite lights follow the scene's mesh lights
+        P.inf_begin = inf0[p];
+        P.n_infinite = sd->n_infinite_lights;
+        for (int i = 0; i < sd->n_infinite_lights; ++i) lights.push_back(DevLight{1, inf0[p] + i, 0, 0});
+        P.n_lights = (int32_t)lights.size() - P.light_begin;
+        P.has_media = sd->n_media > 0 ? 1 : 0;
     }
-    // infinite lights follow the mesh lights
-    std::vector<DevInfinite> infs(std::max(0, sd->n_infinite_lights));
-    for (int i = 0; i < sd->n_infinite_lights; ++i) {
-        const krr_infinite_light_desc &l = sd->infinite_lights[i];
-        DevInfinite d{};
-        for (int k = 0; k < 3; ++k) d.tint[k] = l.tint[k];
-        d.scale = l.scale;
-        std::memcpy(d.rot, l.rotation, sizeof(d.rot));
-        if (l.h_image) {
-            KRR_CHECK_ARG(l.width > 0 && l.height > 0, "environment image size");
-            float4 *img = nullptr;
-            KRR_TRY(dev_upload(wf, &img, reinterpret_cast<const float4 *>(l.h_image),
-                               (size_t)l.width * l.height));
-            d.image = img;
-            d.w = l.width;
-            d.h = l.height;
+    tri_begin[n_scenes] = (int64_t)n_tris;
+    std::vector<DevInfinite> infs(std::max(0, inf0[n_scenes]));
+    std::vector<int32_t> inf_part(inf0[n_scenes]);
+    for (int p = 0; p < n_scenes; ++p)
+        for (int i = 0; i < scenes[p].n_infinite_lights; ++i) {
+            const krr_infinite_light_desc &l = scenes[p].infinite_lights[i];
+            DevInfinite d{};
+            for (int k = 0; k < 3; ++k) d.tint[k] = l.tint[k];
+            d.scale = l.scale;
+            std::memcpy(d.rot, l.rotation, sizeof(d.rot));
+            if (l.h_image) {
+                KRR_CHECK_ARG(l.width > 0 && l.height > 0, "environment image size");
+                float4 *img = nullptr;
+                KRR_TRY(dev_upload(wf, &img, reinterpret_cast<const float4 *>(l.h_image),
+                                   (size_t)l.width * l.height));
+                d.image = img;
+                d.w = l.width;
+                d.h = l.height;
+            }
+            infs[inf0[p] + i] = d;
+            inf_part[inf0[p] + i] = p;
         }
-        infs[i] = d;
-        lights.push_back(DevLight{1, i, 0, 0});
-    }
     // A scene without lights is accepted: light sampling is skipped (every
-    // NEE site tests n_lights) and the frame is black.
+    // NEE site tests the scene's light count) and its frames are black.
 
     DevScene s{};
     KRR_TRY(dev_upload(wf, const_cast<DevMesh **>(&s.meshes), meshes.data(), meshes.size()));
@@ -1705,6 +1902,8 @@ extern "C" int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *sd, void *stre
     KRR_TRY(dev_upload(wf, const_cast<DevInstance **>(&s.instances), insts.data(), insts.size()));
     KRR_TRY(dev_upload(wf, const_cast<DevLight **>(&s.lights), lights.data(), lights.size()));
     s.n_lights = (int32_t)lights.size();
+    KRR_TRY(dev_upload(wf, const_cast<DevScenePart **>(&s.parts), parts.data(), parts.size()));
+    s.n_parts = n_scenes;
     uint32_t *d_offsets = nullptr;
     KRR_TRY(dev_upload(wf, &d_offsets, offsets.data(), offsets.size()));
     uint32_t *tri_inst = nullptr;
@@ -1712,58 +1911,73 @@ extern "C" int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *sd, void *stre
     wf->scene_allocs.push_back(tri_inst);
     if (n_tris)
         k_fill_instance_ids<<<grid_for(n_tris), kThreads, 0, st>>>(tri_inst, d_offsets,
-                                                                   sd->n_instances, n_tris);
+                                                                   inst0[n_scenes], n_tris);
     KRR_CUDA(cudaGetLastError());
     s.tri_instance = tri_inst;
-
-    // world-space triangles and the BVH
-    wf->n_instances = sd->n_instances;
-    wf->n_tris = n_tris;
-    wf->h_instances = insts;
-    wf->scene = s;   // rebuild_bvh reads the uploaded instances
-    KRR_TRY(rebuild_bvh(wf, st));
-    for (auto &d : infs) d.scene_radius = wf->scene_radius;
     KRR_TRY(dev_upload(wf, const_cast<DevInfinite **>(&s.infinite), infs.data(), infs.size()));
     s.n_infinite = (int32_t)infs.size();
-    wf->h_infinite = infs;
 
     // media
-    std::vector<DevMedium> media(sd->n_media);
-    for (int i = 0; i < sd->n_media; ++i) {
-        const krr_medium_desc &m = sd->media[i];
-        DevMedium d{};
-        d.nx = m.nx; d.ny = m.ny; d.nz = m.nz;
-        for (int k = 0; k < 3; ++k) {
-            d.lo[k] = m.bounds_min[k]; d.hi[k] = m.bounds_max[k];
-            d.sigma_t[k] = m.sigma_t[k]; d.albedo[k] = m.albedo[k];
-            d.mres[k] = std::max(1, m.majorant_res[k]);
-            d.idx_scale[k] = (float)(k == 0 ? m.nx : k == 1 ? m.ny : m.nz) / (d.hi[k] - d.lo[k]);
+    std::vector<DevMedium> media(med0[n_scenes]);
+    for (int p = 0; p < n_scenes; ++p)
+        for (int i = 0; i < scenes[p].n_media; ++i) {
+            const krr_medium_desc &m = scenes[p].media[i];
+            DevMedium d{};
+            d.nx = m.nx; d.ny = m.ny; d.nz = m.nz;
+            for (int k = 0; k < 3; ++k) {
+                d.lo[k] = m.bounds_min[k]; d.hi[k] = m.bounds_max[k];
+                d.sigma_t[k] = m.sigma_t[k]; d.albedo[k] = m.albedo[k];
+                d.mres[k] = std::max(1, m.majorant_res[k]);
+                d.idx_scale[k] = (float)(k == 0 ? m.nx : k == 1 ? m.ny : m.nz) / (d.hi[k] - d.lo[k]);
+            }
+            d.g = m.g;
+            d.scale = m.scale;
+            if (m.h_density) {
+                KRR_CHECK_ARG(m.nx > 0 && m.ny > 0 && m.nz > 0, "density grid size");
+                uint16_t *g = nullptr;
+                KRR_TRY(dev_upload(wf, &g, m.h_density, (size_t)m.nx * m.ny * m.nz));
+                d.density = g;
+                float *maj = nullptr;
+                size_t nm = (size_t)d.mres[0] * d.mres[1] * d.mres[2];
+                KRR_CUDA(cudaMalloc(&maj, nm * sizeof(float)));
+                wf->scene_allocs.push_back(maj);
+                k_build_majorant<<<grid_for((int64_t)nm), kThreads, 0, st>>>(d, maj);
+                KRR_CUDA(cudaGetLastError());
+                d.majorant = maj;
+            }
+            media[med0[p] + i] = d;
         }
-        d.g = m.g;
-        d.scale = m.scale;
-        if (m.h_density) {
-            KRR_CHECK_ARG(m.nx > 0 && m.ny > 0 && m.nz > 0, "density grid size");
-            uint16_t *g = nullptr;
-            KRR_TRY(dev_upload(wf, &g, m.h_density, (size_t)m.nx * m.ny * m.nz));
-            d.density = g;
-            float *maj = nullptr;
-            size_t nm = (size_t)d.mres[0] * d.mres[1] * d.mres[2];
-            KRR_CUDA(cudaMalloc(&maj, nm * sizeof(float)));
-            wf->scene_allocs.push_back(maj);
-            k_build_majorant<<<grid_for((int64_t)nm), kThreads, 0, st>>>(d, maj);
-            KRR_CUDA(cudaGetLastError());
-            d.majorant = maj;
-        }
-        media[i] = d;
-    }
     KRR_TRY(dev_upload(wf, const_cast<DevMedium **>(&s.media), media.data(), media.size()));
-    s.n_media = sd->n_media;
+    s.n_media = med0[n_scenes];
     s.max_null_collisions = wf->max_null_collisions;
     s.max_interface_crossings = wf->max_interface_crossings;
-    wf->scene = s;
+    s.pixel_part = n_scenes > 1 ? wf->d_pixel_part : nullptr;
+
+    // world-space triangles and the BVHs (one tree per scene)
+    wf->n_instances = inst0[n_scenes];
+    wf->n_tris = n_tris;
+    wf->h_instances = insts;
+    wf->h_infinite = infs;
+    wf->inf_part = inf_part;
+    wf->parts = parts;
+    wf->n_parts = n_scenes;
+    wf->part_own_depth.assign(n_scenes, -1);
+    for (auto &P : wf->parts) P.max_depth = wf->params.max_depth;
+    wf->part_tri_begin = tri_begin;
+    wf->part_media_begin.assign(med0.begin(), med0.end() - 1);
+    wf->scene = s;   // rebuild_bvh reads the uploaded instances and updates parts and radii
+    KRR_TRY(rebuild_bvh(wf, st));
     wf->has_scene = true;
-    wf->medium = wf->params.enable_medium && s.n_media > 0;
+    wf->medium = wf->params.enable_medium && wf->scene.n_media > 0;
+    KRR_TRY(fill_pixel_parts(wf, st));
     KRR_CUDA(cudaStreamSynchronize(st));
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_cache_box(krr_wf *wf, float *lo, float *hi) {
+    KRR_CHECK_ARG(wf && lo && hi, "NULL argument");
+    KRR_CHECK_ARG(wf->has_scene, "no scene");
+    for (int k = 0; k < 3; ++k) { lo[k] = wf->cache_lo[k]; hi[k] = wf->cache_hi[k]; }
     return KRR_OK;
 }
 
@@ -1791,17 +2005,20 @@ static int set_layout(krr_wf *wf, std::vector<DevView> layout) {
     wf->width = layout.size() == 1 ? layout[0].w : 0;
     wf->height = layout.size() == 1 ? layout[0].h : 0;
     wf->n = n;
+    wf->qcap = wf->wave > 0 ? std::min(wf->wave, n) : n;
     for (int k = 0; k < Q_COUNT; ++k)
-        KRR_CUDA(cudaMalloc(&wf->qbuf[k], (size_t)kChannels[k] * wf->n * sizeof(float4)));
+        KRR_CUDA(cudaMalloc(&wf->qbuf[k], (size_t)kChannels[k] * wf->qcap * sizeof(float4)));
     KRR_CUDA(cudaMalloc(&wf->d_counts, 16 * sizeof(int32_t)));
     KRR_CUDA(cudaMemset(wf->d_counts, 0, 16 * sizeof(int32_t)));
-    KRR_CUDA(cudaMalloc(&wf->hits, wf->n * sizeof(float4)));
-    KRR_CUDA(cudaMalloc(&wf->occluded, wf->n));
-    KRR_CUDA(cudaMalloc(&wf->scatter_lists, 2 * wf->n * sizeof(int32_t)));
+    KRR_CUDA(cudaMalloc(&wf->hits, wf->qcap * sizeof(float4)));
+    KRR_CUDA(cudaMalloc(&wf->occluded, wf->qcap));
+    KRR_CUDA(cudaMalloc(&wf->scatter_lists, 2 * wf->qcap * sizeof(int32_t)));
     KRR_CUDA(cudaMalloc(&wf->ps.L, wf->n * sizeof(float4)));
     KRR_CUDA(cudaMalloc(&wf->ps.pixel, wf->n * sizeof(float4)));
     KRR_CUDA(cudaMalloc(&wf->ps.rng, wf->n * sizeof(ulonglong2)));
-    wf->grid = grid_for(wf->n);
+    wf->grid = stage_grid(wf, wf->n);
+    KRR_TRY(fill_pixel_parts(wf, 0));
+    KRR_CUDA(cudaDeviceSynchronize());
     return alloc_nrc_buffers(wf);
 }
 
@@ -1821,18 +2038,13 @@ extern "C" int krr_wf_rebuild_bvh(krr_wf *wf, void *stream) {
         cudaGraphExecDestroy(wf->graph);
         wf->graph = nullptr;
     }
-    KRR_TRY(rebuild_bvh(wf, st));
-    if (!wf->h_infinite.empty()) {
-        for (auto &d : wf->h_infinite) d.scene_radius = wf->scene_radius;
-        KRR_CUDA(cudaMemcpy(const_cast<DevInfinite *>(wf->scene.infinite), wf->h_infinite.data(),
-                            wf->h_infinite.size() * sizeof(DevInfinite), cudaMemcpyHostToDevice));
-    }
-    return KRR_OK;
+    return rebuild_bvh(wf, st);
 }
 
 extern "C" int krr_wf_update_instances(krr_wf *wf, int32_t n, const int32_t *h_indices,
                                        const float *h_transforms, void *stream) {
     KRR_CHECK_ARG(wf && wf->has_scene, "no scene");
+    KRR_CHECK_ARG(wf->n_parts == 1, "instance updates take a pass with one scene");
     KRR_CHECK_ARG(n >= 0 && (n == 0 || (h_indices && h_transforms)), "bad argument");
     for (int k = 0; k < n; ++k)
         KRR_CHECK_ARG(h_indices[k] >= 0 && h_indices[k] < wf->n_instances, "instance index out of range");
@@ -1847,13 +2059,7 @@ extern "C" int krr_wf_update_instances(krr_wf *wf, int32_t n, const int32_t *h_i
     KRR_CUDA(cudaMemcpy(const_cast<DevInstance *>(wf->scene.instances), wf->h_instances.data(),
                         wf->h_instances.size() * sizeof(DevInstance), cudaMemcpyHostToDevice));
     // a refit keeps every device buffer in place, so a captured frame stays valid
-    KRR_TRY(rebuild_bvh(wf, st, true));
-    if (!wf->h_infinite.empty()) {
-        for (auto &d : wf->h_infinite) d.scene_radius = wf->scene_radius;
-        KRR_CUDA(cudaMemcpy(const_cast<DevInfinite *>(wf->scene.infinite), wf->h_infinite.data(),
-                            wf->h_infinite.size() * sizeof(DevInfinite), cudaMemcpyHostToDevice));
-    }
-    return KRR_OK;
+    return rebuild_bvh(wf, st, true);
 }
 
 extern "C" int krr_wf_resize(krr_wf *wf, int32_t width, int32_t height) {
@@ -1872,6 +2078,7 @@ extern "C" int krr_wf_resize_views(krr_wf *wf, const krr_view *views, int32_t n_
         layout[i].w = views[i].width;
         layout[i].h = views[i].height;
         layout[i].seed = (uint32_t)views[i].seed;
+        layout[i].part = views[i].scene;
     }
     return set_layout(wf, layout);
 }
@@ -1904,10 +2111,16 @@ static int make_camera(const krr_camera_desc *c, DevCamera &d) {
 // given host arrays (cameras == nullptr keeps the current cameras).
 static int fill_frame(krr_wf *wf, int64_t frame_index, const krr_camera_desc *single,
                       const krr_view *views, int32_t n_views, DevView *dv, FrameConst *fc) {
+    // a camera's medium indexes its scene's media
+    auto camera_medium = [&](DevView &v) {
+        if (v.cam.medium >= 0 && v.part < (int)wf->part_media_begin.size())
+            v.cam.medium += wf->part_media_begin[v.part];
+    };
     if (single) {
         KRR_CHECK_ARG(wf->n_views == 1, "the pass has a multi-view layout: use begin_frame_views");
         DevView v = wf->layout[0];
         KRR_TRY(make_camera(single, v.cam));
+        camera_medium(v);
         v.seed = (uint32_t)wf->params.seed;
         v.sample_index = (uint32_t)(frame_index * wf->params.spp + v.seed);
         wf->layout[0] = v;
@@ -1916,7 +2129,9 @@ static int fill_frame(krr_wf *wf, int64_t frame_index, const krr_camera_desc *si
         for (int i = 0; i < n_views; ++i) {
             KRR_CHECK_ARG(views[i].width == wf->layout[i].w && views[i].height == wf->layout[i].h,
                           "view size differs from the layout");
+            KRR_CHECK_ARG(views[i].scene == wf->layout[i].part, "view scene differs from the layout");
             KRR_TRY(make_camera(&views[i].camera, wf->layout[i].cam));
+            camera_medium(wf->layout[i]);
             wf->layout[i].seed = (uint32_t)views[i].seed;
             wf->layout[i].sample_index = (uint32_t)(frame_index * wf->params.spp + views[i].seed);
         }
@@ -1935,7 +2150,7 @@ static int fill_frame(krr_wf *wf, int64_t frame_index, const krr_camera_desc *si
 }
 
 static int launch_begin_frame(krr_wf *wf, cudaStream_t st) {
-    k_begin_frame<<<wf->grid, kThreads, 0, st>>>(wf->ps, wf->d_views, wf->d_frame, wf->n);
+    k_begin_frame<<<wf->grid, wf->block, 0, st>>>(wf->ps, wf->d_views, wf->d_frame, wf->n);
     KRR_CUDA(cudaGetLastError());
     if (wf->nrc && wf->nrc_rec_count)
         KRR_CUDA(cudaMemsetAsync(wf->nrc_rec_count, 0, wf->nrc_slots * sizeof(int32_t), st));
@@ -1969,13 +2184,19 @@ extern "C" int krr_wf_begin_frame_views(krr_wf *wf, int64_t frame_index, const k
     return begin_frame_common(wf, frame_index, nullptr, views, n_views, as_stream(stream));
 }
 
-extern "C" int krr_wf_generate_camera_rays(krr_wf *wf, void *stream) {
-    KRR_TRY(ready(wf));
-    cudaStream_t st = as_stream(stream);
-    k_camera_rays<<<wf->grid, kThreads, 0, st>>>(wf->ps, wf->q(Q_RAY0), wf->d_views, wf->d_frame,
-                                                  wf->n);
+static int camera_rays(krr_wf *wf, int64_t p0, int64_t count, cudaStream_t st) {
+    k_camera_rays<<<stage_grid(wf, count), wf->block, 0, st>>>(wf->ps, wf->q(Q_RAY0), wf->d_views,
+                                                               wf->d_frame, p0, count);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
+}
+
+extern "C" int krr_wf_generate_camera_rays(krr_wf *wf, void *stream) {
+    KRR_TRY(ready(wf));
+    KRR_CHECK_ARG(wf->qcap == wf->n,
+                  "the stage entry points trace every pixel at once: the queue capacity must be the "
+                  "pixel count (krr_wf_set_launch with wave 0)");
+    return camera_rays(wf, 0, wf->n, as_stream(stream));
 }
 
 extern "C" int krr_wf_reset_queues(krr_wf *wf, int32_t depth, void *stream) {
@@ -1985,24 +2206,34 @@ extern "C" int krr_wf_reset_queues(krr_wf *wf, int32_t depth, void *stream) {
     return KRR_OK;
 }
 
+// Several scenes: each ray starts at its pixel's scene's root; the pixel id
+// is in plane `pix_plane` of the queue.
+static void set_roots(const krr_wf *wf, TraceLaunch &l, const Queue &q, int pix_plane, bool any_set) {
+    if (wf->n_parts <= 1) return;
+    l.roots = wf->accel.d_roots;
+    l.pixel_part = wf->d_pixel_part;
+    (any_set ? l.any_pix : l.ray_pix) = q.base + (size_t)pix_plane * q.cap;
+}
+
 static TraceLaunch closest_launch(krr_wf *wf, int depth) {
     Queue rq = wf->q(depth & 1);
     TraceLaunch l{};
     l.ray_o = rq.base;
-    l.ray_d = rq.base + wf->n;
+    l.ray_d = rq.base + rq.cap;
     l.ray_stride = 1;
     l.n = rq.cap;
     l.d_count = rq.count;
     l.hits = wf->hits;
     l.counter = wf->accel.d_scratch;
     l.err = wf->accel.d_scratch + 4;
+    set_roots(wf, l, rq, 5, false);   // Ray: plane 5 = pu | pixel
     return l;
 }
 
 // L[pixel] += throughput x cache(query) for the queued cache queries.
 static int nrc_evaluate_queries(krr_wf *wf, cudaStream_t st) {
     KRR_TRY(nrc_query_device(wf->nrc, wf->nrc_q_in, wf->nrc_q_count(), wf->n, wf->nrc_q_out, st));
-    k_nrc_apply<<<wf->grid, kThreads, 0, st>>>(wf->nrc_q_out, wf->nrc_q_meta, wf->nrc_q_count(),
+    k_nrc_apply<<<wf->grid, wf->block, 0, st>>>(wf->nrc_q_out, wf->nrc_q_meta, wf->nrc_q_count(),
                                                 (int)wf->n, wf->ps);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
@@ -2038,7 +2269,7 @@ static int closest_stage(krr_wf *wf, int depth, cudaStream_t st, bool traced,
         hook.spread_c = nrc_termination_spread(wf->nrc);
         if (!defer_cache) KRR_CUDA(cudaMemsetAsync(wf->nrc_q_count(), 0, sizeof(int32_t), st));
     }
-    k_hit_process<<<wf->grid, kThreads, 0, st>>>(wf->scene, rq, wf->hits, wf->q(cur ^ 1),
+    k_hit_process<<<wf->grid, wf->block, 0, st>>>(wf->scene, rq, wf->hits, wf->q(cur ^ 1),
                                                   wf->q(Q_MISS), wf->q(Q_HIT_LIGHT), wf->q(Q_SCATTER),
                                                   wf->q(Q_MEDIUM_SAMPLE), wf->medium ? 1 : 0, wf->err(),
                                                   hook, wf->ps, inline_lights, wf->params.nee);
@@ -2060,18 +2291,19 @@ static int trace_shadow_and_next(krr_wf *wf, int depth, cudaStream_t st) {
     Queue sq = wf->q(Q_SHADOW);
     TraceLaunch l = closest_launch(wf, depth + 1);
     l.any_o = sq.base;
-    l.any_d = sq.base + wf->n;
+    l.any_d = sq.base + sq.cap;
     l.d_any_count = sq.count;
     l.occluded = wf->occluded;
+    set_roots(wf, l, sq, 2, true);   // Shadow: plane 2 = Ld | pixel
     KRR_TRY(launch_trace_mixed(&wf->accel, l, st));
-    k_shadow_resolve<<<wf->grid, kThreads, 0, st>>>(sq, wf->occluded, wf->ps);
+    k_shadow_resolve<<<wf->grid, wf->block, 0, st>>>(sq, wf->occluded, wf->ps);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }
 
 extern "C" int krr_wf_handle_hit(krr_wf *wf, void *stream) {
     KRR_TRY(ready(wf));
-    k_handle_hit<<<wf->grid, kThreads, 0, as_stream(stream)>>>(wf->scene, wf->q(Q_HIT_LIGHT), wf->ps,
+    k_handle_hit<<<wf->grid, wf->block, 0, as_stream(stream)>>>(wf->scene, wf->q(Q_HIT_LIGHT), wf->ps,
                                                                wf->params.nee);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
@@ -2080,7 +2312,7 @@ extern "C" int krr_wf_handle_hit(krr_wf *wf, void *stream) {
 extern "C" int krr_wf_handle_miss(krr_wf *wf, void *stream) {
     KRR_TRY(ready(wf));
     if (wf->scene.n_infinite == 0) return KRR_OK;
-    k_handle_miss<<<wf->grid, kThreads, 0, as_stream(stream)>>>(wf->scene, wf->q(Q_MISS), wf->ps,
+    k_handle_miss<<<wf->grid, wf->block, 0, as_stream(stream)>>>(wf->scene, wf->q(Q_MISS), wf->ps,
                                                                 wf->params.nee);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
@@ -2091,10 +2323,10 @@ extern "C" int krr_wf_generate_scatter_rays(krr_wf *wf, int32_t depth, void *str
     int cur = depth & 1;
     cudaStream_t st = as_stream(stream);
     KRR_CUDA(cudaMemsetAsync(wf->scatter_class_counts(), 0, 4 * sizeof(int32_t), st));
-    k_scatter_classify<<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->q(Q_SCATTER), wf->ps,
+    k_scatter_classify<<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->q(Q_SCATTER), wf->ps,
                                                       wf->params.rr, wf->scatter_lists,
                                                       wf->scatter_class_counts());
-    k_scatter_process<<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->q(Q_SCATTER), wf->scatter_lists,
+    k_scatter_process<<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->q(Q_SCATTER), wf->scatter_lists,
                                                      wf->scatter_class_counts(), wf->q(cur ^ 1),
                                                      wf->q(Q_SHADOW), wf->ps, wf->params.nee,
                                                      wf->params.rr, wf->err());
@@ -2109,15 +2341,16 @@ extern "C" int krr_wf_trace_shadow(krr_wf *wf, void *stream) {
     Queue sq = wf->q(Q_SHADOW);
     TraceLaunch l{};
     l.ray_o = sq.base;
-    l.ray_d = sq.base + wf->n;
+    l.ray_d = sq.base + sq.cap;
     l.ray_stride = 1;
     l.n = sq.cap;
     l.d_count = sq.count;
     l.occluded = wf->occluded;
     l.counter = wf->accel.d_scratch;
     l.err = wf->accel.d_scratch + 4;
+    set_roots(wf, l, sq, 2, false);
     KRR_TRY(launch_trace_any(&wf->accel, l, st));
-    k_shadow_resolve<<<wf->grid, kThreads, 0, st>>>(sq, wf->occluded, wf->ps);
+    k_shadow_resolve<<<wf->grid, wf->block, 0, st>>>(sq, wf->occluded, wf->ps);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }
@@ -2134,6 +2367,101 @@ extern "C" int krr_wf_sample_medium_scattering(krr_wf *wf, int32_t depth, void *
     return launch_medium_scatter(wf, depth, as_stream(stream));
 }
 
+extern "C" int krr_wf_set_launch(krr_wf *wf, int32_t block, int32_t blocks_per_sm, int64_t wave) {
+    KRR_CHECK_ARG(wf != nullptr, "NULL argument");
+    KRR_CHECK_ARG(block == 64 || block == 128 || block == 256, "block must be 64, 128 or 256 threads");
+    KRR_CHECK_ARG(blocks_per_sm >= 1 && blocks_per_sm <= 32, "blocks per SM must be 1..32");
+    KRR_CHECK_ARG(wave >= 0, "wave must be >= 0 (0 = every pixel at once)");
+    const bool realloc = wave != wf->wave;
+    wf->block = block;
+    wf->blocks_per_sm = blocks_per_sm;
+    wf->wave = wave;
+    if (realloc && wf->n) return set_layout(wf, wf->layout);   // queues of the new capacity
+    if (wf->n) wf->grid = stage_grid(wf, wf->n);
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_get_launch(const krr_wf *wf, int32_t *block, int32_t *blocks_per_sm,
+                                 int64_t *wave, int64_t *queue_capacity) {
+    KRR_CHECK_ARG(wf != nullptr, "NULL argument");
+    if (block) *block = wf->block;
+    if (blocks_per_sm) *blocks_per_sm = wf->blocks_per_sm;
+    if (wave) *wave = wf->wave;
+    if (queue_capacity) *queue_capacity = wf->qcap;
+    return KRR_OK;
+}
+
+// Autotuner of the pass's launch shapes and queue capacity: renders
+// `frames` frames (the current cameras, frame indices from 1) with each
+// candidate (threads per block 128 / 256 x blocks per SM 4 / 8 / 16 x waves
+// of all, half or a quarter of the pixels, the last two only from 2^20
+// pixels up), times them with CUDA events on the stream, keeps the fastest
+// by median frame time and applies it.  An attached cache does not train
+// during the trials.  The frames are the same with every candidate.
+extern "C" int krr_wf_autotune(krr_wf *wf, float *d_out, int32_t frames, krr_wf_tuning *out,
+                               void *stream) {
+    KRR_TRY(ready(wf));
+    KRR_CHECK_ARG(d_out && out && frames >= 1, "bad argument");
+    cudaStream_t st = as_stream(stream);
+    const bool train = wf->nrc_train;
+    wf->nrc_train = false;
+    const int32_t block0 = wf->block, bps0 = wf->blocks_per_sm;
+    const int64_t wave0 = wf->wave;
+    std::vector<int64_t> waves{0};
+    if (wf->n >= (1 << 20))
+        for (int d : {2, 4}) waves.push_back(((wf->n + d - 1) / d + 4095) / 4096 * 4096);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = INFINITY, first = INFINITY;
+    int32_t bb = block0, bbps = bps0;
+    int64_t bw = wave0;
+    int st_code = KRR_OK, n_cand = 0;
+    for (int64_t w : waves) {
+        for (int32_t b : {256, 128}) {
+            for (int32_t bps : {8, 4, 16}) {
+                st_code = krr_wf_set_launch(wf, b, bps, w);
+                if (st_code != KRR_OK) break;
+                std::vector<float> ms;
+                for (int f = 0; f <= frames && st_code == KRR_OK; ++f) {   // frame 0 warms up
+                    st_code = begin_frame_common(wf, 1 + f, nullptr, nullptr, 0, st);
+                    if (st_code != KRR_OK) break;
+                    cudaEventRecord(e0, st);
+                    st_code = krr_wf_render(wf, d_out, stream);
+                    cudaEventRecord(e1, st);
+                    cudaEventSynchronize(e1);
+                    float t = 0.f;
+                    cudaEventElapsedTime(&t, e0, e1);
+                    if (f > 0) ms.push_back(t);
+                }
+                if (st_code != KRR_OK) break;
+                std::sort(ms.begin(), ms.end());
+                const float med = ms[ms.size() / 2];
+                if (n_cand++ == 0) first = med;
+                if (med < best) { best = med; bb = b; bbps = bps; bw = w; }
+            }
+            if (st_code != KRR_OK) break;
+        }
+        if (st_code != KRR_OK) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    wf->nrc_train = train;
+    if (st_code != KRR_OK) {
+        krr_wf_set_launch(wf, block0, bps0, wave0);
+        return st_code;
+    }
+    KRR_TRY(krr_wf_set_launch(wf, bb, bbps, bw));
+    out->block = bb;
+    out->blocks_per_sm = bbps;
+    out->wave = bw;
+    out->queue_capacity = wf->qcap;
+    out->frame_ms = best;
+    out->default_frame_ms = first;
+    out->candidates = n_cand;
+    return KRR_OK;
+}
+
 extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
     KRR_TRY(ready(wf));
     KRR_CHECK_ARG(d_out != nullptr, "output is NULL");
@@ -2145,34 +2473,39 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
     // evaluated in one launch at the end of the sample: a stopped path gets no
     // other radiance afterwards, so each pixel's sum is the same, in the same
     // order, as with one evaluation per depth.
+    // The pixels go through the bounces in waves of the queue capacity (all
+    // at once by default); a pixel's path touches only its own state, so the
+    // waves give the same frame as one pass over all pixels.
     const bool fuse = wf->params.nee && !wf->medium;
     for (int s = 0; s < wf->params.spp; ++s) {
-        KRR_TRY(krr_wf_reset_queues(wf, -1, stream));
-        KRR_TRY(krr_wf_generate_camera_rays(wf, stream));
-        if (wf->nrc) KRR_CUDA(cudaMemsetAsync(wf->nrc_q_count(), 0, sizeof(int32_t), st));
-        bool traced = false;
-        for (int depth = 0;; ++depth) {
-            KRR_TRY(krr_wf_reset_queues(wf, depth, stream));
-            KRR_TRY(closest_stage(wf, depth, st, traced, true));
-            if (wf->medium) {
-                KRR_TRY(krr_wf_sample_medium_interaction(wf, depth, stream));
-                KRR_TRY(krr_wf_handle_hit(wf, stream));
-                KRR_TRY(krr_wf_handle_miss(wf, stream));
+        for (int64_t p0 = 0; p0 < wf->n; p0 += wf->qcap) {
+            KRR_TRY(krr_wf_reset_queues(wf, -1, stream));
+            KRR_TRY(camera_rays(wf, p0, std::min(wf->qcap, wf->n - p0), st));
+            if (wf->nrc) KRR_CUDA(cudaMemsetAsync(wf->nrc_q_count(), 0, sizeof(int32_t), st));
+            bool traced = false;
+            for (int depth = 0;; ++depth) {
+                KRR_TRY(krr_wf_reset_queues(wf, depth, stream));
+                KRR_TRY(closest_stage(wf, depth, st, traced, true));
+                if (wf->medium) {
+                    KRR_TRY(krr_wf_sample_medium_interaction(wf, depth, stream));
+                    KRR_TRY(krr_wf_handle_hit(wf, stream));
+                    KRR_TRY(krr_wf_handle_miss(wf, stream));
+                }
+                if (depth == loop_depth(wf)) break;
+                if (wf->medium) KRR_TRY(krr_wf_sample_medium_scattering(wf, depth, stream));
+                KRR_TRY(krr_wf_generate_scatter_rays(wf, depth, stream));
+                traced = fuse;
+                if (fuse) KRR_TRY(trace_shadow_and_next(wf, depth, st));
+                else if (wf->params.nee) KRR_TRY(krr_wf_trace_shadow(wf, stream));
             }
-            if (depth == wf->params.max_depth) break;
-            if (wf->medium) KRR_TRY(krr_wf_sample_medium_scattering(wf, depth, stream));
-            KRR_TRY(krr_wf_generate_scatter_rays(wf, depth, stream));
-            traced = fuse;
-            if (fuse) KRR_TRY(trace_shadow_and_next(wf, depth, st));
-            else if (wf->params.nee) KRR_TRY(krr_wf_trace_shadow(wf, stream));
+            if (wf->nrc) KRR_TRY(nrc_evaluate_queries(wf, st));
         }
-        if (wf->nrc) KRR_TRY(nrc_evaluate_queries(wf, st));
         if (wf->nrc && wf->nrc_train) KRR_TRY(nrc_train_frame(wf, st));
-        k_accumulate<<<wf->grid, kThreads, 0, st>>>(wf->ps, wf->n,
+        k_accumulate<<<wf->grid, wf->block, 0, st>>>(wf->ps, wf->n,
                                                      wf->params.independent_samples && s + 1 < wf->params.spp);
         KRR_CUDA(cudaGetLastError());
     }
-    k_resolve<<<wf->grid, kThreads, 0, st>>>(wf->ps, reinterpret_cast<float4 *>(d_out), wf->d_views,
+    k_resolve<<<wf->grid, wf->block, 0, st>>>(wf->ps, reinterpret_cast<float4 *>(d_out), wf->d_views,
                                               wf->d_frame, wf->n, (float)wf->params.spp,
                                               wf->params.enable_clamp, wf->params.clamp_max);
     KRR_CUDA(cudaGetLastError());
@@ -2183,6 +2516,7 @@ extern "C" int krr_wf_render_megakernel(krr_wf *wf, float *d_out, void *stream) 
     KRR_TRY(ready(wf));
     KRR_CHECK_ARG(d_out != nullptr, "output is NULL");
     KRR_CHECK_ARG(!wf->medium, "the megakernel pass traces surfaces only; the scene has media");
+    KRR_CHECK_ARG(wf->n_parts == 1, "the megakernel pass takes one scene");
     KRR_CHECK_ARG(!wf->nrc, "the megakernel pass has no cache hooks; detach the cache first");
     cudaStream_t st = as_stream(stream);
     static int grid[2] = {0, 0};
@@ -2242,9 +2576,9 @@ extern "C" int krr_wf_ray_queue(krr_wf *wf, int32_t depth, const float **d_origi
     KRR_CHECK_ARG(d_origin_tmin && d_dir_tmax, "NULL argument");
     const float4 *b = wf->qbuf[depth & 1];
     *d_origin_tmin = reinterpret_cast<const float *>(b);
-    *d_dir_tmax = reinterpret_cast<const float *>(b + wf->n);
-    if (d_pu_pixel) *d_pu_pixel = reinterpret_cast<const float *>(b + 5 * wf->n);
-    if (capacity) *capacity = (int32_t)wf->n;
+    *d_dir_tmax = reinterpret_cast<const float *>(b + wf->qcap);
+    if (d_pu_pixel) *d_pu_pixel = reinterpret_cast<const float *>(b + 5 * wf->qcap);
+    if (capacity) *capacity = (int32_t)wf->qcap;
     return KRR_OK;
 }
 
@@ -2254,7 +2588,7 @@ extern "C" int krr_wf_queue_view(krr_wf *wf, int32_t queue, const float **d_base
     KRR_CHECK_ARG(queue >= 0 && queue < Q_COUNT && d_base, "bad queue");
     *d_base = reinterpret_cast<const float *>(wf->qbuf[queue]);
     if (channels) *channels = kChannels[queue];
-    if (capacity) *capacity = (int32_t)wf->n;
+    if (capacity) *capacity = (int32_t)wf->qcap;
     return KRR_OK;
 }
 
@@ -2452,7 +2786,7 @@ extern "C" int krr_wf_group_launch(krr_wf_group *g, int64_t frame_index, void *s
 
 namespace krr {
 int launch_medium_sample(krr_wf *wf, int depth, cudaStream_t st) {
-    k_medium_sample<<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->q(Q_MEDIUM_SAMPLE),
+    k_medium_sample<<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->q(Q_MEDIUM_SAMPLE),
                                                     wf->q((depth & 1) ^ 1), wf->q(Q_MISS),
                                                     wf->q(Q_HIT_LIGHT), wf->q(Q_SCATTER),
                                                     wf->q(Q_MEDIUM_SCATTER), wf->ps,
@@ -2461,7 +2795,7 @@ int launch_medium_sample(krr_wf *wf, int depth, cudaStream_t st) {
     return KRR_OK;
 }
 int launch_medium_scatter(krr_wf *wf, int depth, cudaStream_t st) {
-    k_medium_scatter<<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->q(Q_MEDIUM_SCATTER),
+    k_medium_scatter<<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->q(Q_MEDIUM_SCATTER),
                                                      wf->q((depth & 1) ^ 1), wf->q(Q_SHADOW), wf->ps,
                                                      wf->params.nee, wf->err());
     KRR_CUDA(cudaGetLastError());
@@ -2473,18 +2807,18 @@ int launch_medium_scatter(krr_wf *wf, int depth, cudaStream_t st) {
 // own counter and ratio-tracked by k_shadow_tr.
 int launch_trace_shadow_tr(krr_wf *wf, cudaStream_t st) {
     static_assert(kMediumSampleCh >= kShadowCh, "tracked shadow rays need five planes");
-    Queue tracked{wf->qbuf[Q_MEDIUM_SAMPLE], (int32_t)wf->n, wf->shadow_tracked_count()};
+    Queue tracked{wf->qbuf[Q_MEDIUM_SAMPLE], (int32_t)wf->qcap, wf->shadow_tracked_count()};
     KRR_CUDA(cudaMemsetAsync(tracked.count, 0, sizeof(int32_t), st));
     int *terr = wf->accel.d_scratch + 4;
     if (wf->accel.node_format == 1) {
-        k_shadow_split<1><<<wf->grid, kThreads, 0, st>>>(wf->accel.d_nodes, wf->accel.d_tris,
+        k_shadow_split<1><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris,
                                                           wf->q(Q_SHADOW), tracked, wf->ps, wf->err(), terr);
-        k_shadow_tr<1><<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris,
+        k_shadow_tr<1><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris,
                                                        tracked, wf->ps, wf->err(), terr);
     } else {
-        k_shadow_split<0><<<wf->grid, kThreads, 0, st>>>(wf->accel.d_nodes, wf->accel.d_tris,
+        k_shadow_split<0><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris,
                                                           wf->q(Q_SHADOW), tracked, wf->ps, wf->err(), terr);
-        k_shadow_tr<0><<<wf->grid, kThreads, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris,
+        k_shadow_tr<0><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris,
                                                        tracked, wf->ps, wf->err(), terr);
     }
     KRR_CUDA(cudaGetLastError());

@@ -66,6 +66,20 @@ struct DevMedium {
     float idx_scale[3];        // n / (hi - lo) per axis: world to voxel index
 };
 
+// One scene of a pass that traces several scenes in one wavefront
+// (krr_wf_set_scenes): its lights and infinite lights are ranges of the
+// pass's lists; its meshes, instances, materials and media are ranges of
+// the pass's arrays with the indices relocated; its triangles are a range
+// of the global ids and its BVH a root of the pass's node array.
+struct DevScenePart {
+    int32_t light_begin, n_lights;     // light list [begin, begin + n): mesh lights, then infinite
+    int32_t inf_begin, n_infinite;     // infinite lights
+    float cache_offset[3];             // added to positions fed to the radiance cache
+    int32_t has_media;                 // the scene's meshes bound a medium
+    int32_t max_depth;                 // the scene's path depth (the pass's, or its own)
+    int32_t pad;
+};
+
 constexpr int kMaxNullCollisions = 1 << 20;   // default bound of the tracking loops
 constexpr int kMaxInterfaceCrossings = 64;    // default bound of the shadow segments
 
@@ -85,7 +99,22 @@ struct DevScene {
     // raises kErrLoopLimit and ends the walk
     int32_t max_null_collisions;
     int32_t max_interface_crossings;
+    // scene parts (one for a single scene); pixel_part[pixel] picks the part
+    // of a pixel's view, nullptr with a single part
+    const DevScenePart *parts;
+    const uint8_t *pixel_part;
+    const uint32_t *part_roots;   // BVH root of each part (nullptr: one part, root 0)
+    int32_t n_parts;
 };
+
+// BVH root node of a pixel's scene.
+__device__ __forceinline__ uint32_t root_of(const DevScene &s, uint32_t pixel) {
+    return s.part_roots ? s.part_roots[s.pixel_part[pixel]] : 0u;
+}
+
+__device__ __forceinline__ const DevScenePart &part_of(const DevScene &s, uint32_t pixel) {
+    return s.parts[s.pixel_part ? s.pixel_part[pixel] : 0];
+}
 
 // A queue: `channels` float4 planes of `cap` items and an item counter.
 struct Queue {

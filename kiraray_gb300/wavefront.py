@@ -116,24 +116,67 @@ class WavefrontPathTracer:
         self.n_pixels = width * height
         self._views = None
 
-    def resize_views(self, views):
-        """Batched views: list of (camera, width, height, seed)."""
+    @staticmethod
+    def _view_array(views):
+        """(camera, width, height, seed[, scene]) tuples -> krr_view array."""
         arr = (_lib.ViewDesc * len(views))()
-        for i, (cam, w, h, seed) in enumerate(views):
+        for i, v in enumerate(views):
+            cam, w, h, seed = v[:4]
             arr[i].camera = cam.desc()
             arr[i].width, arr[i].height, arr[i].seed = w, h, seed
+            arr[i].scene = v[4] if len(v) > 4 else 0
+        return arr
+
+    def resize_views(self, views):
+        """Batched views: list of (camera, width, height, seed[, scene])."""
+        arr = self._view_array(views)
         check(self.lib.krr_wf_resize_views(self._h, arr, len(views)), "krr_wf_resize_views")
         self._views = arr
         self.width = self.height = 0
-        self.n_pixels = sum(w * h for _, w, h, _ in views)
+        self.n_pixels = sum(v[1] * v[2] for v in views)
+
+    def set_scenes(self, scenes):
+        """Several scenes in one wavefront; views name theirs by index."""
+        descs = [sc.desc() for sc in scenes]
+        arr = (_lib.SceneDesc * len(scenes))(*[d for d, _ in descs])
+        check(self.lib.krr_wf_set_scenes(self._h, arr, len(scenes), _stream()), "krr_wf_set_scenes")
+        self._keep = (descs, arr)
+        self.scene = scenes[0]
+        self.scenes = list(scenes)
+
+    def set_launch(self, block: int = 256, blocks_per_sm: int = 8, wave: int = 0) -> None:
+        """Stage-kernel launch shapes and the queue capacity (wave 0: every
+        pixel at once)."""
+        check(self.lib.krr_wf_set_launch(self._h, block, blocks_per_sm, wave), "krr_wf_set_launch")
+
+    def launch(self) -> dict:
+        b, bps, w, cap = C.c_int32(), C.c_int32(), C.c_int64(), C.c_int64()
+        check(self.lib.krr_wf_get_launch(self._h, C.byref(b), C.byref(bps), C.byref(w), C.byref(cap)),
+              "krr_wf_get_launch")
+        return {"block": b.value, "blocks_per_sm": bps.value, "wave": w.value,
+                "queue_capacity": cap.value}
+
+    def autotune(self, out: torch.Tensor, frames: int = 3) -> dict:
+        """Times frames for each candidate launch shape / queue capacity and
+        keeps the fastest (krr_wf_autotune)."""
+        t = _lib.WfTuning()
+        check(self.lib.krr_wf_autotune(self._h, out.data_ptr(), frames, C.byref(t), _stream()),
+              "krr_wf_autotune")
+        return {k: getattr(t, k) for k, _ in t._fields_ if k != "reserved"}
+
+    def set_scene_max_depth(self, scene: int, max_depth: int) -> None:
+        """Path depth of one scene of the pass (-1: the pass's)."""
+        check(self.lib.krr_wf_set_scene_max_depth(self._h, scene, max_depth),
+              "krr_wf_set_scene_max_depth")
+
+    def cache_box(self):
+        lo, hi = (C.c_float * 3)(), (C.c_float * 3)()
+        check(self.lib.krr_wf_cache_box(self._h, lo, hi), "krr_wf_cache_box")
+        return tuple(lo), tuple(hi)
 
     def begin_frame_views(self, frame_index: int, views=None):
         if views is not None:
-            arr = (_lib.ViewDesc * len(views))()
-            for i, (cam, w, h, seed) in enumerate(views):
-                arr[i].camera = cam.desc()
-                arr[i].width, arr[i].height, arr[i].seed = w, h, seed
-            self._views = arr
+            self._views = self._view_array(views)
         check(self.lib.krr_wf_begin_frame_views(self._h, frame_index, self._views,
                                                 len(self._views), _stream()),
               "krr_wf_begin_frame_views")

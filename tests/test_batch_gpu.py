@@ -189,3 +189,108 @@ def test_frame_group_equals_passes_alone(krr_lib, cuda):
                 assert np.array_equal(got[f][k].view(np.uint32), want.view(np.uint32)), (f, k)
         grp.close()
     assert pa.device_errors() == 0 and pb.device_errors() == 0
+
+
+def _two_scene_views():
+    big = scenes.large_scene(width=8, height=8, grid=128, n_spheres=30, sky_size=(64, 32))
+    vol = scenes.volume_box(8, 8, max_depth=8, grid=32)
+    views = []
+    for i, (w, h) in enumerate(((40, 24), (33, 21), (24, 40), (16, 16))):
+        if i % 2 == 0:
+            cam = scenes._camera((3.0 * i, 22.0, -62.0), (0.0, 2.0, 0.0), 45.0, w, h)
+        else:
+            cam = scenes._camera((0.5 + 0.1 * i, 0.5, -1.4), (0.5, 0.5, 0.0), 40.0, w, h)
+        views.append((cam, w, h, 200 + i, i % 2))
+    return [big, vol], views
+
+
+def _alone(sc, view, frame, max_depth):
+    cam, w, h, seed = view[:4]
+    pt = WavefrontPathTracer({"max_depth": max_depth})
+    pt.set_scene(sc)
+    pt.resize_views([(cam, w, h, seed)])
+    pt.begin_frame_views(frame)
+    out = pt.render_flat().cpu().numpy()
+    assert pt.device_errors() == 0
+    return out
+
+
+def test_scenes_in_one_wavefront_equal_each_scene_alone(krr_lib, cuda):
+    """Views of two scenes (the large scene without media at max depth 8, the
+    volume box with a medium at max depth 12) in one pass: one launch per
+    stage per bounce serves both, and every view equals its scene's pass
+    rendering that view alone."""
+    (big, vol), views = _two_scene_views()
+    pt = WavefrontPathTracer({"max_depth": 8})
+    pt.set_scenes([big, vol])
+    pt.set_scene_max_depth(1, 12)
+    pt.resize_views(views)
+    pt.begin_frame_views(2)
+    batch = pt.render_flat().cpu().numpy()
+    assert pt.device_errors() == 0
+    off = 0
+    for v in views:
+        w, h = v[1], v[2]
+        want = _alone((big, vol)[v[4]], v, 2, (8, 12)[v[4]])
+        assert np.array_equal(batch[off:off + w * h].view(np.uint32), want.view(np.uint32)), v[4]
+        off += w * h
+    # a view naming a scene the pass does not hold is rejected
+    with pytest.raises(Exception):
+        pt.resize_views([(views[0][0], 8, 8, 1, 2)])
+
+
+def test_launch_shapes_and_waves_keep_the_frame(krr_lib, cuda):
+    """Threads per block, blocks per SM and waves of pixels (queue capacity
+    below the pixel count) change nothing in the frame."""
+    (big, vol), views = _two_scene_views()
+    pt = WavefrontPathTracer({"max_depth": 8})
+    pt.set_scenes([big, vol])
+    pt.resize_views(views)
+    pt.begin_frame_views(3)
+    want = pt.render_flat().cpu().numpy()
+    n = pt.n_pixels
+    for block, bps, wave in ((128, 4, 0), (64, 16, n // 3 + 5), (256, 2, 1000)):
+        pt.set_launch(block, bps, wave)
+        assert pt.launch()["queue_capacity"] == (min(wave, n) if wave else n)
+        pt.begin_frame_views(3)
+        got = pt.render_flat().cpu().numpy()
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (block, bps, wave)
+    assert pt.device_errors() == 0
+    with pytest.raises(Exception):   # the stage entry points need every pixel in the queues
+        pt.generate_camera_rays()
+
+
+def test_autotuner_keeps_the_frame(krr_lib, cuda):
+    (big, vol), views = _two_scene_views()
+    pt = WavefrontPathTracer({"max_depth": 8})
+    pt.set_scenes([big, vol])
+    pt.resize_views(views)
+    pt.begin_frame_views(4)
+    want = pt.render_flat().cpu().numpy()
+    out = torch.empty((pt.n_pixels, 4), device="cuda")
+    t = pt.autotune(out, frames=2)
+    assert t["candidates"] == 6 and t["frame_ms"] > 0
+    assert t["frame_ms"] <= t["default_frame_ms"]
+    assert pt.launch()["block"] == t["block"]
+    pt.begin_frame_views(4)
+    got = pt.render_flat().cpu().numpy()
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_cache_across_scenes_in_one_wavefront(krr_lib, cuda):
+    """One cache for both scenes: their positions are offset into disjoint
+    regions of the cache's box; frames stay finite and the cache trains."""
+    (big, vol), views = _two_scene_views()
+    pt = WavefrontPathTracer({"max_depth": 8})
+    pt.set_scenes([big, vol])
+    pt.resize_views(views)
+    lo, hi = pt.cache_box()
+    assert hi[0] - lo[0] > 100.0   # the volume box sits beside the large scene
+    cache = NeuralRadianceCache(lo, hi, batch_size=2048)
+    pt.set_nrc(cache, train=True)
+    for f in range(1, 6):
+        pt.begin_frame_views(f)
+        img = pt.render_flat()
+    assert torch.isfinite(img).all()
+    assert cache.info().step == 5
+    assert pt.device_errors() == 0
