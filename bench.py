@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--views", type=int, default=64,
                     help="batched-views run: number of views (0 = skip)")
     ap.add_argument("--view-frames", type=int, default=5)
+    ap.add_argument("--two-level", type=int, default=1,
+                    help="1: also the scene as a two-level structure (memory, Mrays/s, updates)")
     ap.add_argument("--frame", type=int, default=1,
                     help="1: also time a 1920x1080 wavefront frame and its stages")
     ap.add_argument("--nrc-copies", type=int, default=8,
@@ -425,6 +427,59 @@ def config_frames(args):
     return out
 
 
+def two_level(sc, rays, dev):
+    """The scene as a two-level structure (each mesh geometry once, an
+    instance tree over them) against the flattened one: memory, build time,
+    closest-hit rate on the given ray sets, and the time of an instance
+    update (the instance tree rebuilt) against a refit of the flattened
+    tree."""
+    import torch
+    from kiraray_gb300.accel import Accel
+
+    geoms, key_of, inst = [], {}, []
+    for mi, xf in sc.instances:
+        m = sc.meshes[mi]
+        key = (id(m.positions), id(m.indices))
+        if key not in key_of:
+            key_of[key] = len(geoms)
+            geoms.append(np.asarray(m.positions, np.float32)[np.asarray(m.indices)].reshape(-1, 9))
+        inst.append((key_of[key], np.asarray(xf, np.float32)))
+    t0 = time.perf_counter()
+    acc = Accel.instanced(geoms, inst)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    st = acc.stats()
+    out = {"geometries": len(geoms), "instances": len(inst),
+           "node_bytes": st["node_bytes"], "triangle_bytes": st["triangle_bytes"],
+           "build_ms_device": round(st["build_ms"], 3), "build_s_wall": round(build_s, 3)}
+    stream = torch.cuda.current_stream()
+    for name, r in rays.items():
+        h = torch.empty((r.shape[0], 4), device=dev)
+        for _ in range(3):
+            acc.trace_closest(r, h)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(5):
+            acc.trace_closest(r, h)
+        e1.record(stream)
+        e1.synchronize()
+        out[f"{name}_mrays_s"] = round(r.shape[0] * 5 / e0.elapsed_time(e1) / 1e3, 1)
+    xfs = np.stack([x for _, x in inst])
+    ts = []
+    for k in range(6):
+        moved = xfs.copy()
+        moved[1:, 1, 3] += 0.01 * (k + 1)   # every sphere instance moves up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        acc.update_instances(moved)
+        torch.cuda.synchronize()
+        ts.append((time.perf_counter() - t0) * 1e3)
+    out["instance_update_ms_wall"] = round(sorted(ts[1:])[len(ts[1:]) // 2], 3)
+    del acc
+    torch.cuda.empty_cache()
+    return out
+
+
 def batched_views(args):
     """64 views, sides log-uniform in [256, 1024] (view i seeded 100 + i),
     even views on the large scene (max depth 8) and odd views on the volume
@@ -759,6 +814,7 @@ def run_ours(args, rank, world, local):
            if args.cpu_seconds > 0 else None)
     clocks = clk.summary()
     frame = wavefront_frame(sc, acc, peak) if args.frame else None
+    two = two_level(sc, {"primary": rays0, "bounce": rays1}, dev) if args.two_level else None
     batched = batched_views(args)
     frames = config_frames(args)
     nrc = time_to_relmse(args)
@@ -806,6 +862,10 @@ def run_ours(args, rank, world, local):
         "clocks": clocks,
         "ray_sets_mrays_s": dict(set_mrays, **({"shadow": frame["shadow_mrays_s"]} if frame else {})),
         "wavefront_frame": frame,
+        "two_level": dict(two, flattened={"node_bytes": stats["node_bytes"],
+                                          "triangle_bytes": stats["triangle_bytes"],
+                                          "primary_mrays_s": set_mrays["primary"],
+                                          "bounce_mrays_s": set_mrays["bounce"]}) if two else None,
         "batched_views": batched,
         "config_frames": frames,
         "time_to_relmse": nrc,

@@ -199,6 +199,32 @@ int krr_accel_destroy(krr_accel *accel);
 int krr_accel_refit_triangles(krr_accel *accel, const float *h_vertices, int64_t n_triangles,
                               void *stream);
 
+/* Two-level structure, the OptiX GAS-per-mesh + IAS layout of the
+ * reference (OptixSceneSingleLevel::buildAccelStructure, src/core/device/
+ * optix.cpp:357-398): one BVH per geometry over its object-space triangles
+ * (h_geom_vertices float3[3 * total], geometry g holding triangles
+ * [h_geom_tri_begin[g], h_geom_tri_begin[g + 1]), n_geoms + 1 entries
+ * starting at 0) and one BVH over the instances (instance i draws geometry
+ * h_instances[i].mesh with its row-major 3x4 object-to-world transform;
+ * h_instance_mask[i] == 0 lets any-hit rays through, NULL = all opaque).
+ * Hit ids are global as in the flattened structure: instance-major, the
+ * instance's first triangle id plus the triangle's index in its geometry.
+ * t is the parameter of the ray carried into the instance's object space
+ * (the world ray's t up to rounding); traced with the same entry points as
+ * the flattened structure (no counter replay, refit or tuning).  Instances
+ * share their geometry's tree, so the structure holds each geometry once. */
+int krr_accel_create_instanced(const float *h_geom_vertices, const int64_t *h_geom_tri_begin,
+                               int32_t n_geoms, const krr_instance_desc *h_instances,
+                               int32_t n_instances, const uint8_t *h_instance_mask,
+                               krr_accel **out, void *stream);
+/* New object-to-world transforms for every instance (12 floats each): the
+ * instance level is rebuilt, the geometry trees are kept (the OptiX IAS
+ * update, optix.cpp:618-669). */
+int krr_accel_update_instances(krr_accel *accel, const float *h_transforms, void *stream);
+/* The world-to-object 3x4 matrices the traversal uses (12 floats per
+ * instance), for checking hits against an independent implementation. */
+int krr_accel_instance_inverse(const krr_accel *accel, float *h_out, int32_t n_instances);
+
 /* Closest hit for n rays (the reference's __raygen__Closest +
  * __closesthit__Closest, src/render/wavefront/device.cu:43-81, without the
  * shading setup).  Ties in t go to the smaller triangle id. */
@@ -329,6 +355,13 @@ int krr_wf_set_scenes(krr_wf *wf, const krr_scene_desc *scenes, int32_t n_scenes
  * pass's max_depth (the default): a view of that scene then equals its
  * scene's pass with that max_depth. */
 int krr_wf_set_scene_max_depth(krr_wf *wf, int32_t scene, int32_t max_depth);
+/* Acceleration structure of the pass's scene from the next set_scene on (or
+ * rebuilt now): 1 = the instances flattened into one world-space BVH
+ * (default; the fastest traversal), 2 = the two-level structure of
+ * krr_accel_create_instanced (each mesh geometry once, so less memory, and
+ * krr_wf_update_instances rebuilds only the instance level).  Two levels
+ * take a pass with one scene; the megakernel variant traces one level. */
+int krr_wf_set_accel_levels(krr_wf *wf, int32_t levels);
 /* Box the radiance cache should cover for this pass (scene_lo/hi of its
  * krr_nrc_config): the union of the scenes' boxes after their offsets. */
 int krr_wf_cache_box(krr_wf *wf, float *out_lo3, float *out_hi3);

@@ -137,6 +137,9 @@ SIGNATURES = {
     "krr_accel_set_tuning": (_I, [_P, C.c_int32, C.c_int32]),
     "krr_set_bvh_builder": (_I, [C.c_int32]),
     "krr_accel_set_stack_limit": (_I, [_P, C.c_int32]),
+    "krr_accel_create_instanced": (_I, [_P, _P, C.c_int32, _P, C.c_int32, _P, C.POINTER(_P), _P]),
+    "krr_accel_update_instances": (_I, [_P, _P, _P]),
+    "krr_accel_instance_inverse": (_I, [_P, _P, C.c_int32]),
     "krr_accel_device_errors": (_I, [_P, C.POINTER(C.c_uint32), _P]),
     "krr_accel_autotune": (_I, [_P, _P, C.c_int64, C.c_int32, C.POINTER(C.c_int32),
                                 C.POINTER(C.c_int32), C.POINTER(C.c_float), _P]),
@@ -179,6 +182,7 @@ SIGNATURES = {
     "krr_wf_set_scenes": (_I, [_P, _P, C.c_int32, _P]),
     "krr_wf_set_launch": (_I, [_P, C.c_int32, C.c_int32, C.c_int64]),
     "krr_wf_set_scene_max_depth": (_I, [_P, C.c_int32, C.c_int32]),
+    "krr_wf_set_accel_levels": (_I, [_P, C.c_int32]),
     "krr_wf_get_launch": (_I, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "krr_wf_autotune": (_I, [_P, _P, C.c_int32, C.POINTER(WfTuning), _P]),

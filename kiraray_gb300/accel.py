@@ -54,6 +54,43 @@ class Accel:
         self.n_triangles = v.shape[0]
 
     @classmethod
+    def instanced(cls, geometries, instances, mask=None) -> "Accel":
+        """Two-level structure: `geometries` a list of object-space triangle
+        arrays (float32 [n_g, 9]); `instances` a list of (geometry index,
+        float32 [3, 4] object-to-world transform); `mask` per instance (0 =
+        any-hit rays pass through)."""
+        lib = _lib.load()
+        verts = np.ascontiguousarray(np.concatenate([np.asarray(g, np.float32).reshape(-1, 9)
+                                                     for g in geometries]), dtype=np.float32)
+        begin = np.zeros(len(geometries) + 1, np.int64)
+        begin[1:] = np.cumsum([np.asarray(g).reshape(-1, 9).shape[0] for g in geometries])
+        arr = (_lib.InstanceDesc * max(1, len(instances)))()
+        for i, (g, xf) in enumerate(instances):
+            arr[i].mesh = g
+            arr[i].transform[:] = [float(x) for x in np.asarray(xf, np.float32).reshape(12)]
+        m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+        obj = cls.__new__(cls)
+        obj._h = C.c_void_p()
+        check(lib.krr_accel_create_instanced(verts.ctypes.data, begin.ctypes.data, len(geometries), arr,
+                                             len(instances), None if m is None else m.ctypes.data,
+                                             C.byref(obj._h), _stream()), "krr_accel_create_instanced")
+        obj.n_instances = len(instances)
+        obj.n_triangles = int(sum(begin[g + 1] - begin[g] for g, _ in instances))
+        return obj
+
+    def update_instances(self, transforms) -> None:
+        """New object-to-world transforms, float32 [n_instances, 3, 4]."""
+        x = np.ascontiguousarray(transforms, np.float32).reshape(-1, 12)
+        check(_lib.load().krr_accel_update_instances(self._h, x.ctypes.data, _stream()),
+              "krr_accel_update_instances")
+
+    def instance_inverse(self) -> np.ndarray:
+        out = np.empty((self.n_instances, 12), np.float32)
+        check(_lib.load().krr_accel_instance_inverse(self._h, out.ctypes.data, self.n_instances),
+              "krr_accel_instance_inverse")
+        return out
+
+    @classmethod
     def borrowed(cls, handle: int, n_triangles: int) -> "Accel":
         obj = cls.__new__(cls)
         obj._h = C.c_void_p(handle)

@@ -746,6 +746,10 @@ static int launch_trace(const krr_accel *a, const TraceLaunch &l, cudaStream_t s
     lt.refill_below = a->refill_below;
     lt.postpone_pct = a->postpone_pct;
     lt.stack_limit = a->stack_limit;
+    if (a->levels == 2) {
+        KRR_CHECK_ARG(!STATS, "the counter replay takes a one-level structure");
+        return launch_trace_instanced(a, lt, MODE, s);
+    }
     const int grid = traversal_grid_size();
     const bool single = a->max_leaf == 1 && a->full_leaf == 1;
     if constexpr (MODE == 2) {
@@ -791,6 +795,19 @@ void accel_free(krr_accel *a) {
     cudaFree(a->stage_hits);
     cudaFree(a->d_node_bounds);
     cudaFree(a->d_roots);
+    cudaFree(a->d_inst);
+    a->d_inst = nullptr;
+    for (krr_accel *sub : {a->tlas, a->blas})
+        if (sub) { accel_free(sub); delete sub; }
+    a->tlas = a->blas = nullptr;
+    a->levels = 1;
+    a->h_inst.clear();
+    a->geom_begin.clear();
+    a->inst_geom.clear();
+    a->inst_xf.clear();
+    a->inst_mask.clear();
+    a->inst_first.clear();
+    a->inst_triangles = 0;
     a->d_node_bounds = nullptr;
     a->d_roots = nullptr;
     a->roots.clear();
@@ -918,6 +935,7 @@ int accel_refit(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     KRR_CHECK_ARG(a && a->d_scratch, "acceleration structure not built");
     KRR_CHECK_ARG(n == a->n_tris, "a refit keeps the triangle count of the build");
     KRR_CHECK_ARG(a->roots.empty(), "a structure of several scenes is rebuilt, not refitted");
+    KRR_CHECK_ARG(a->levels == 1, "a two-level structure updates its instances instead");
     if (n == 0) return KRR_OK;
     KRR_CHECK_ARG(d_v != nullptr, "vertices are NULL");
     float margin = 0.f;
@@ -1343,6 +1361,10 @@ extern "C" int krr_accel_stats_get(const krr_accel *a, krr_accel_stats *out) {
     out->node_bytes = 16.0 * kNodeQuads[a->node_format] * (double)a->n_nodes;
     out->reserved = a->node_format;
     out->triangle_bytes = 48.0 * (double)a->n_tris;
+    if (a->levels == 2) {   // each geometry once, plus the instance records
+        out->triangle_bytes = 48.0 * (double)(a->blas->n_tris + a->tlas->n_tris) +
+                              sizeof(TraceInst) * (double)a->h_inst.size();
+    }
     return KRR_OK;
 }
 

@@ -34,6 +34,17 @@
 
 #include "internal.h"
 
+namespace krr {
+// One instance of a two-level structure, as the traversal reads it.
+struct TraceInst {
+    float inv[12];          // world -> object, row-major 3x4
+    uint32_t blas_root;     // root node of the instance's geometry tree
+    uint32_t id_delta;      // global triangle id = geometry-tree id + id_delta
+    uint32_t mask;          // 0: any-hit rays pass through (null material)
+    uint32_t pad;
+};
+}  // namespace krr
+
 struct krr_accel {
     int64_t n_tris = 0;
     int64_t n_nodes = 0;
@@ -62,6 +73,20 @@ struct krr_accel {
     std::vector<uint32_t> roots;
     uint32_t *d_roots = nullptr;
     std::vector<float> part_bounds;    // per part: lo.xyz, hi.xyz (accel_build_parts)
+    // two-level structure (accel_build_instanced): levels == 2, the instance
+    // level and the geometry level as structures of their own, the instance
+    // records on the device and their inputs on the host
+    int levels = 1;
+    krr_accel *tlas = nullptr;
+    krr_accel *blas = nullptr;
+    krr::TraceInst *d_inst = nullptr;
+    std::vector<krr::TraceInst> h_inst;
+    std::vector<int64_t> geom_begin;     // first triangle of each geometry (+ total)
+    std::vector<int32_t> inst_geom;      // geometry of each instance
+    std::vector<float> inst_xf;          // object -> world, 12 per instance
+    std::vector<uint32_t> inst_mask;
+    std::vector<int64_t> inst_first;     // global id of each instance's first triangle
+    int64_t inst_triangles = 0;
     float4 *d_node_bounds = nullptr;   // 2 per node: lo, hi
     float4 *stage_rays = nullptr;
     float4 *stage_hits = nullptr;
@@ -129,6 +154,29 @@ int launch_trace_any(const krr_accel *a, const TraceLaunch &l, cudaStream_t s);
 // latency tail of the longest ray is paid once.
 int launch_trace_mixed(const krr_accel *a, const TraceLaunch &l, cudaStream_t s);
 int traversal_grid_size();
+
+// Two-level structures (instanced.cu).
+struct InstancedView {
+    const float4 *tlas_nodes, *tlas_tris, *blas_nodes, *blas_tris;
+    const TraceInst *inst;
+};
+struct InstancedInput {
+    const float *d_geom_vertices;      // object-space triangles of every geometry, 9 floats each
+    const int64_t *geom_tri_begin;     // host, n_geoms + 1 entries
+    int n_geoms;
+    const int32_t *inst_geom;          // host, per instance
+    const float *inst_xf;              // host, object -> world 3x4 per instance
+    const uint8_t *inst_mask;          // host, per instance, or nullptr (all 1)
+    int n_instances;
+};
+int accel_build_instanced(krr_accel *a, const InstancedInput &in, cudaStream_t s);
+// New object -> world transforms (12 floats per instance): the instance
+// level is rebuilt, the geometry trees are kept.
+int accel_update_instances(krr_accel *a, const float *inst_xf, cudaStream_t s);
+int launch_trace_instanced(const krr_accel *a, const TraceLaunch &l, int mode, cudaStream_t s);
+InstancedView instanced_view(const krr_accel *a);
+// Object-space triangles (9 floats) of n triangles of a mesh's arrays.
+int geometry_triangles(const float *d_pos, const uint32_t *d_idx, int64_t n, float *d_out, cudaStream_t s);
 // Reads and clears the traversal error flags (device int at d_err) after the
 // stream's work; KRR_ERR_OVERFLOW if a ray was cut off by the stack limit.
 int take_trace_errors(int *d_err, cudaStream_t s, uint32_t *out_flags);

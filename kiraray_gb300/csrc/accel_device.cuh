@@ -265,4 +265,88 @@ __device__ float4 traverse_ray(const float4 *__restrict__ nodes, const float4 *_
     return make_float4(tmax, b1b, b2b, __uint_as_float(best));
 }
 
+// Two-level structures (instanced.cu): the world ray walks the instance
+// tree; at an instance leaf it is carried into the instance's object space
+// by the instance's world-to-object 3x4 matrix, row by row, each operation
+// rounded, and the instance's geometry tree gives the closest hit with t in
+// (tmin, best t]; it replaces the best hit if its t is smaller, or equal
+// with a smaller global id.  The result is the smallest (t, global id) over
+// all instances whatever the order, as the CPU oracle computes it.
+// world -> object: rows of a 3x4 row-major matrix, operation by operation
+__device__ __forceinline__ V3 inst_point(const float *m, V3 p) {
+    V3 r;
+    float *o = &r.x;
+    for (int k = 0; k < 3; ++k) {
+        const float *row = m + 4 * k;
+        float acc = __fmul_rn(row[0], p.x);
+        acc = __fadd_rn(acc, __fmul_rn(row[1], p.y));
+        acc = __fadd_rn(acc, __fmul_rn(row[2], p.z));
+        o[k] = __fadd_rn(acc, row[3]);
+    }
+    return r;
+}
+
+__device__ __forceinline__ V3 inst_vector(const float *m, V3 d) {
+    V3 r;
+    float *o = &r.x;
+    for (int k = 0; k < 3; ++k) {
+        const float *row = m + 4 * k;
+        float acc = __fmul_rn(row[0], d.x);
+        acc = __fadd_rn(acc, __fmul_rn(row[1], d.y));
+        o[k] = __fadd_rn(acc, __fmul_rn(row[2], d.z));
+    }
+    return r;
+}
+
+// Closest (ANY: any masked) hit of one world ray over the two levels.
+template <bool ANY, int FMT, bool MASKED = true>
+__device__ float4 trace_two_level(const InstancedView &v, V3 o, V3 d, float tmin, float tmax, int *err) {
+    RayPre r = ray_pre(o, d, tmin);
+    V3 inv = box_inverse(d);
+    V3 oinv = V3{-o.x * inv.x, -o.y * inv.y, -o.z * inv.z};
+    int oct = (inv.x < 0.f ? 1 : 0) | (inv.y < 0.f ? 2 : 0) | (inv.z < 0.f ? 4 : 0);
+    uint2 stack[kTraversalStack];
+    int sp = 0;
+    uint2 ng = make_uint2(0u, (1u << oct) | (1u << 8)), tg = make_uint2(0u, 0u);
+    float bt = tmax, bb1 = 0.f, bb2 = 0.f;
+    uint32_t best = KRR_MISS;
+    while (true) {
+        if (ng.y & 0xffu) {
+            int p = __ffs(ng.y & 0xffu) - 1;
+            ng.y &= ~(1u << p);
+            int slot = p ^ oct;
+            uint32_t imask = ng.y >> 8;
+            uint32_t child = ng.x + __popc(imask & ((1u << slot) - 1u));
+            if (ng.y & 0xffu) {
+                if (sp < kTraversalStack) stack[sp++] = ng;
+                else { atomicOr(err, (int)kErrStackOverflow); break; }
+            }
+            visit<FMT>(v.tlas_nodes, child, r, inv, oinv, oct, bt, ng, tg);
+        }
+        while (tg.y) {
+            int b = __ffs(tg.y) - 1;
+            tg.y &= tg.y - 1u;
+            const uint32_t k = __float_as_uint(__ldg(v.tlas_tris + 3 * (size_t)(tg.x + b)).w);
+            const TraceInst I = v.inst[k];
+            if (ANY && MASKED && !I.mask) continue;
+            const V3 io = inst_point(I.inv, o), id = inst_vector(I.inv, d);
+            const float4 h = traverse_ray<ANY, FMT, false>(v.blas_nodes, v.blas_tris, io, id, tmin, bt,
+                                                           err, I.blas_root);
+            const uint32_t local = __float_as_uint(h.w);
+            if (local == KRR_MISS) continue;
+            const uint32_t gid = local + I.id_delta;
+            if (ANY) return make_float4(h.x, h.y, h.z, __uint_as_float(gid));
+            if (h.x < bt || (h.x == bt && gid < best)) {
+                bt = h.x; bb1 = h.y; bb2 = h.z; best = gid;
+            }
+        }
+        if (!(ng.y & 0xffu)) {
+            if (sp > 0) ng = stack[--sp];
+            else break;
+        }
+    }
+    if (best == KRR_MISS) return make_float4(INFINITY, 0.f, 0.f, __uint_as_float(KRR_MISS));
+    return make_float4(bt, bb1, bb2, __uint_as_float(best));
+}
+
 }  // namespace krr

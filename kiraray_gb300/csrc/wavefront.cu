@@ -89,6 +89,9 @@ struct krr_wf {
     std::vector<float> part_radius{1.f};
     std::vector<int32_t> inf_part;
     std::vector<int32_t> part_own_depth;   // -1: the pass's max_depth
+    int32_t levels = 1;                    // 1: flattened instances, 2: two-level structure
+    std::vector<DevMesh> h_mesh;           // host copies of the device meshes
+    std::vector<int64_t> h_mesh_tris;      // triangles per mesh
     int32_t n_parts = 1;
     uint8_t *d_pixel_part = nullptr;   // [n] scene of each pixel's view
     // launch shapes and queue capacity (krr_wf_set_launch, krr_wf_autotune):
@@ -1094,10 +1097,20 @@ __global__ void k_medium_scatter(DevScene s, Queue mscat, Queue next, Queue shad
 // are enabled: closest hits through null-material interfaces with ratio
 // tracking inside media.
 // Three blocks per SM, as k_medium_sample.
+// With a two-level structure (iv.inst != nullptr) every traversal goes
+// through the instance level.
+template <bool ANY, int FMT, bool MASKED>
+__device__ __forceinline__ float4 shadow_trace(const InstancedView &iv, const float4 *__restrict__ nodes,
+                                               const float4 *__restrict__ tris, V3 o, V3 d, float tmax,
+                                               int *trace_err, uint32_t root) {
+    if (iv.inst) return trace_two_level<ANY, FMT, MASKED>(iv, o, d, 0.f, tmax, trace_err);
+    return traverse_ray<ANY, FMT, MASKED>(nodes, tris, o, d, 0.f, tmax, trace_err, root);
+}
+
 template <int FMT>
 __global__ void __launch_bounds__(kThreads, 3)
 k_shadow_tr(DevScene s, const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
-            Queue shadow, PixelState ps, uint32_t *err, int *trace_err) {
+            InstancedView iv, Queue shadow, PixelState ps, uint32_t *err, int *trace_err) {
     int n = min(*shadow.count, shadow.cap);   // an overflowed queue holds cap items
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 c0 = shadow.at(0, i), c1 = shadow.at(1, i), c2 = shadow.at(2, i), c3 = shadow.at(3, i),
@@ -1113,7 +1126,7 @@ k_shadow_tr(DevScene s, const float4 *__restrict__ nodes, const float4 *__restri
         int crossings = 0;
         const uint32_t root = root_of(s, pixel);
         while (fabsf(d.x) > kRayEps * 2 || fabsf(d.y) > kRayEps * 2 || fabsf(d.z) > kRayEps * 2) {
-            float4 h = traverse_ray<false, FMT>(nodes, tris, o, d, 0.f, tmax, trace_err, root);
+            float4 h = shadow_trace<false, FMT, true>(iv, nodes, tris, o, d, tmax, trace_err, root);
             bool visible = ubits(h.w) == KRR_MISS;
             Surf sf;
             if (!visible) {
@@ -1181,8 +1194,8 @@ k_shadow_tr(DevScene s, const float4 *__restrict__ nodes, const float4 *__restri
 // without media.
 template <int FMT>
 __global__ void k_shadow_split(DevScene s, const float4 *__restrict__ nodes,
-                               const float4 *__restrict__ tris, Queue shadow, Queue tracked,
-                               PixelState ps, uint32_t *err, int *trace_err) {
+                               const float4 *__restrict__ tris, InstancedView iv, Queue shadow,
+                               Queue tracked, PixelState ps, uint32_t *err, int *trace_err) {
     int n = min(*shadow.count, shadow.cap);   // an overflowed queue holds cap items
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 c0 = shadow.at(0, i), c1 = shadow.at(1, i), c2 = shadow.at(2, i), c3 = shadow.at(3, i);
@@ -1191,7 +1204,7 @@ __global__ void k_shadow_split(DevScene s, const float4 *__restrict__ nodes,
         const uint32_t root = root_of(s, pixel);
         bool moving = fabsf(d.x) > kRayEps * 2 || fabsf(d.y) > kRayEps * 2 || fabsf(d.z) > kRayEps * 2;
         if (s.pixel_part && !part_of(s, pixel).has_media) {
-            float4 h = traverse_ray<true, FMT, true>(nodes, tris, f3(c0), d, 0.f, c1.w, trace_err, root);
+            float4 h = shadow_trace<true, FMT, true>(iv, nodes, tris, f3(c0), d, c1.w, trace_err, root);
             if (ubits(h.w) == KRR_MISS) {
                 float4 c4 = shadow.at(4, i);
                 add_radiance(ps, pixel, f3(c2) * v3(1.f) / mean(f3(c3) * v3(1.f) + f3(c4) * v3(1.f)));
@@ -1199,7 +1212,7 @@ __global__ void k_shadow_split(DevScene s, const float4 *__restrict__ nodes,
             continue;
         }
         if (sbits(c3.w) < 0 && moving) {
-            float4 h = traverse_ray<true, FMT, false>(nodes, tris, f3(c0), d, 0.f, c1.w, trace_err, root);
+            float4 h = shadow_trace<true, FMT, false>(iv, nodes, tris, f3(c0), d, c1.w, trace_err, root);
             if (ubits(h.w) == KRR_MISS) {
                 float4 c4 = shadow.at(4, i);
                 add_radiance(ps, pixel, f3(c2) * v3(1.f) / mean(f3(c3) * v3(1.f) + f3(c4) * v3(1.f)));
@@ -1677,38 +1690,12 @@ static int sync_part_depths(krr_wf *wf) {
     return KRR_OK;
 }
 
-static int rebuild_bvh(krr_wf *wf, cudaStream_t st, bool refit = false) {
-    const uint64_t n_tris = wf->n_tris;
+// After a build or update: per scene the bounding-box diagonal (scene
+// radius of the infinite lights, src/core/device/scene.cpp:108) and the
+// cache offset that puts the scenes side by side along x.
+static int finish_bvh(krr_wf *wf, cudaStream_t st) {
     DevScene &s = wf->scene;
-    // the flattened triangles: kept after a refit (the next update refits
-    // again), freed after a build (a scene that never moves does not hold them)
-    if (!wf->d_world)
-        KRR_CUDA(cudaMalloc(&wf->d_world, std::max<uint64_t>(n_tris, 1) * 9 * sizeof(float)));
-    float *d_world = wf->d_world;
-    if (n_tris) k_flatten<<<grid_for(n_tris), kThreads, 0, st>>>(s, wf->n_instances, d_world, n_tris);
-    KRR_CUDA(cudaGetLastError());
-    int stat = refit ? accel_refit(&wf->accel, d_world, (int64_t)n_tris, st)
-                     : accel_build_parts(&wf->accel, d_world, wf->part_tri_begin.data(), wf->n_parts, st);
-    if (stat == KRR_OK) stat = cuda_status(cudaStreamSynchronize(st), "BVH", __FILE__, __LINE__);
-    if (!refit || stat != KRR_OK) {
-        cudaFree(wf->d_world);
-        wf->d_world = nullptr;
-    }
-    if (stat != KRR_OK) return stat;
-    // null-material triangles never block shadow rays (device.cu:83-88); a
-    // refit keeps the mask words of the triangle records
-    if (n_tris && !refit) {
-        uint8_t *mask = nullptr;
-        KRR_CUDA(cudaMalloc(&mask, n_tris));
-        k_null_mask<<<grid_for(n_tris), kThreads, 0, st>>>(s, (int64_t)n_tris, mask);
-        stat = cuda_status(cudaGetLastError(), "k_null_mask", __FILE__, __LINE__);
-        if (stat == KRR_OK) stat = accel_set_mask(&wf->accel, mask, st);
-        if (stat == KRR_OK) stat = cuda_status(cudaStreamSynchronize(st), "mask", __FILE__, __LINE__);
-        cudaFree(mask);
-        if (stat != KRR_OK) return stat;
-    }
-    // per scene: the bounding-box diagonal (scene radius of the infinite
-    // lights, src/core/device/scene.cpp:108) and the cache offset that puts
+    (void)st;
     // the scenes side by side along x, one scene width apart
     const krr_accel &a = wf->accel;
     const int np = wf->n_parts;
@@ -1743,6 +1730,97 @@ static int rebuild_bvh(krr_wf *wf, cudaStream_t st, bool refit = false) {
                             wf->h_infinite.size() * sizeof(DevInfinite), cudaMemcpyHostToDevice));
     }
     return KRR_OK;
+}
+
+
+// The two-level structure of the pass's instances: one tree per distinct
+// mesh geometry (meshes that share arrays share one), an instance tree over
+// them; an update rebuilds only the instance tree.  Null-material meshes
+// let any-hit rays through by their instance's mask.
+static int build_two_level(krr_wf *wf, cudaStream_t st, bool update) {
+    const int n = wf->n_instances;
+    std::vector<float> xf(12 * (size_t)std::max(n, 1));
+    for (int i = 0; i < n; ++i) std::memcpy(&xf[12 * (size_t)i], wf->h_instances[i].xf, 12 * sizeof(float));
+    if (update) return accel_update_instances(&wf->accel, xf.data(), st);
+    std::vector<DevMesh> meshes(wf->h_mesh);
+    std::vector<int32_t> geom_of_mesh(meshes.size(), -1), inst_geom(n);
+    std::vector<int64_t> geom_begin{0};
+    std::vector<int32_t> geom_mesh;
+    std::vector<uint8_t> mask(n);
+    for (int i = 0; i < n; ++i) {
+        const int m = wf->h_instances[i].mesh;
+        if (geom_of_mesh[m] < 0) {
+            for (size_t g = 0; g < geom_mesh.size(); ++g) {
+                const DevMesh &o = meshes[geom_mesh[g]];
+                if (o.pos == meshes[m].pos && o.idx == meshes[m].idx &&
+                    wf->h_mesh_tris[geom_mesh[g]] == wf->h_mesh_tris[m]) {
+                    geom_of_mesh[m] = (int32_t)g;
+                    break;
+                }
+            }
+            if (geom_of_mesh[m] < 0) {
+                geom_of_mesh[m] = (int32_t)geom_mesh.size();
+                geom_mesh.push_back(m);
+                geom_begin.push_back(geom_begin.back() + wf->h_mesh_tris[m]);
+            }
+        }
+        inst_geom[i] = geom_of_mesh[m];
+        mask[i] = meshes[m].material >= 0 ? 1 : 0;
+    }
+    if (geom_mesh.empty()) {   // no instances: one empty geometry
+        geom_mesh.push_back(-1);
+        geom_begin.push_back(0);
+    }
+    float *d_obj = nullptr;
+    KRR_CUDA(cudaMalloc(&d_obj, std::max<int64_t>(geom_begin.back(), 1) * 9 * sizeof(float)));
+    int stat = KRR_OK;
+    for (size_t g = 0; g < geom_mesh.size() && stat == KRR_OK; ++g)
+        if (geom_mesh[g] >= 0)
+            stat = geometry_triangles(meshes[geom_mesh[g]].pos, meshes[geom_mesh[g]].idx,
+                                      geom_begin[g + 1] - geom_begin[g], d_obj + 9 * geom_begin[g], st);
+    InstancedInput in{d_obj, geom_begin.data(), (int)geom_mesh.size(), inst_geom.data(), xf.data(),
+                      mask.data(), n};
+    if (stat == KRR_OK) stat = accel_build_instanced(&wf->accel, in, st);
+    cudaStreamSynchronize(st);
+    cudaFree(d_obj);
+    return stat;
+}
+
+static int rebuild_bvh(krr_wf *wf, cudaStream_t st, bool refit = false) {
+    const uint64_t n_tris = wf->n_tris;
+    DevScene &s = wf->scene;
+    if (wf->levels == 2) {
+        KRR_TRY(build_two_level(wf, st, refit));
+        return finish_bvh(wf, st);
+    }
+    // the flattened triangles: kept after a refit (the next update refits
+    // again), freed after a build (a scene that never moves does not hold them)
+    if (!wf->d_world)
+        KRR_CUDA(cudaMalloc(&wf->d_world, std::max<uint64_t>(n_tris, 1) * 9 * sizeof(float)));
+    float *d_world = wf->d_world;
+    if (n_tris) k_flatten<<<grid_for(n_tris), kThreads, 0, st>>>(s, wf->n_instances, d_world, n_tris);
+    KRR_CUDA(cudaGetLastError());
+    int stat = refit ? accel_refit(&wf->accel, d_world, (int64_t)n_tris, st)
+                     : accel_build_parts(&wf->accel, d_world, wf->part_tri_begin.data(), wf->n_parts, st);
+    if (stat == KRR_OK) stat = cuda_status(cudaStreamSynchronize(st), "BVH", __FILE__, __LINE__);
+    if (!refit || stat != KRR_OK) {
+        cudaFree(wf->d_world);
+        wf->d_world = nullptr;
+    }
+    if (stat != KRR_OK) return stat;
+    // null-material triangles never block shadow rays (device.cu:83-88); a
+    // refit keeps the mask words of the triangle records
+    if (n_tris && !refit) {
+        uint8_t *mask = nullptr;
+        KRR_CUDA(cudaMalloc(&mask, n_tris));
+        k_null_mask<<<grid_for(n_tris), kThreads, 0, st>>>(s, (int64_t)n_tris, mask);
+        stat = cuda_status(cudaGetLastError(), "k_null_mask", __FILE__, __LINE__);
+        if (stat == KRR_OK) stat = accel_set_mask(&wf->accel, mask, st);
+        if (stat == KRR_OK) stat = cuda_status(cudaStreamSynchronize(st), "mask", __FILE__, __LINE__);
+        cudaFree(mask);
+        if (stat != KRR_OK) return stat;
+    }
+    return finish_bvh(wf, st);
 }
 
 extern "C" int krr_wf_set_scene(krr_wf *wf, const krr_scene_desc *sd, void *stream) {
@@ -1954,8 +2032,13 @@ extern "C" int krr_wf_set_scenes(krr_wf *wf, const krr_scene_desc *scenes, int32
     s.pixel_part = n_scenes > 1 ? wf->d_pixel_part : nullptr;
 
     // world-space triangles and the BVHs (one tree per scene)
+    KRR_CHECK_ARG(wf->levels == 1 || n_scenes == 1, "a two-level structure takes a pass with one scene");
     wf->n_instances = inst0[n_scenes];
     wf->n_tris = n_tris;
+    wf->h_mesh = meshes;
+    wf->h_mesh_tris.assign(meshes.size(), 0);
+    for (int p = 0; p < n_scenes; ++p)
+        for (int i = 0; i < scenes[p].n_meshes; ++i) wf->h_mesh_tris[mesh0[p] + i] = scenes[p].meshes[i].n_triangles;
     wf->h_instances = insts;
     wf->h_infinite = infs;
     wf->inf_part = inf_part;
@@ -1972,6 +2055,17 @@ extern "C" int krr_wf_set_scenes(krr_wf *wf, const krr_scene_desc *scenes, int32
     KRR_TRY(fill_pixel_parts(wf, st));
     KRR_CUDA(cudaStreamSynchronize(st));
     return KRR_OK;
+}
+
+extern "C" int krr_wf_set_accel_levels(krr_wf *wf, int32_t levels) {
+    KRR_CHECK_ARG(wf != nullptr, "NULL argument");
+    KRR_CHECK_ARG(levels == 1 || levels == 2, "levels must be 1 (flattened) or 2 (two-level)");
+    KRR_CHECK_ARG(levels == 1 || wf->n_parts == 1, "a two-level structure takes a pass with one scene");
+    wf->levels = levels;
+    if (!wf->has_scene) return KRR_OK;
+    cudaDeviceSynchronize();
+    if (wf->graph) { cudaGraphExecDestroy(wf->graph); wf->graph = nullptr; }
+    return rebuild_bvh(wf, 0);
 }
 
 extern "C" int krr_wf_cache_box(krr_wf *wf, float *lo, float *hi) {
@@ -2517,6 +2611,7 @@ extern "C" int krr_wf_render_megakernel(krr_wf *wf, float *d_out, void *stream) 
     KRR_CHECK_ARG(d_out != nullptr, "output is NULL");
     KRR_CHECK_ARG(!wf->medium, "the megakernel pass traces surfaces only; the scene has media");
     KRR_CHECK_ARG(wf->n_parts == 1, "the megakernel pass takes one scene");
+    KRR_CHECK_ARG(wf->levels == 1, "the megakernel pass traces the flattened structure");
     KRR_CHECK_ARG(!wf->nrc, "the megakernel pass has no cache hooks; detach the cache first");
     cudaStream_t st = as_stream(stream);
     static int grid[2] = {0, 0};
@@ -2810,15 +2905,16 @@ int launch_trace_shadow_tr(krr_wf *wf, cudaStream_t st) {
     Queue tracked{wf->qbuf[Q_MEDIUM_SAMPLE], (int32_t)wf->qcap, wf->shadow_tracked_count()};
     KRR_CUDA(cudaMemsetAsync(tracked.count, 0, sizeof(int32_t), st));
     int *terr = wf->accel.d_scratch + 4;
+    const InstancedView iv = wf->accel.levels == 2 ? instanced_view(&wf->accel) : InstancedView{};
     if (wf->accel.node_format == 1) {
-        k_shadow_split<1><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris,
+        k_shadow_split<1><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
                                                           wf->q(Q_SHADOW), tracked, wf->ps, wf->err(), terr);
-        k_shadow_tr<1><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris,
+        k_shadow_tr<1><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
                                                        tracked, wf->ps, wf->err(), terr);
     } else {
-        k_shadow_split<0><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris,
+        k_shadow_split<0><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
                                                           wf->q(Q_SHADOW), tracked, wf->ps, wf->err(), terr);
-        k_shadow_tr<0><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris,
+        k_shadow_tr<0><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
                                                        tracked, wf->ps, wf->err(), terr);
     }
     KRR_CUDA(cudaGetLastError());

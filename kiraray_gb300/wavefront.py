@@ -164,6 +164,10 @@ class WavefrontPathTracer:
               "krr_wf_autotune")
         return {k: getattr(t, k) for k, _ in t._fields_ if k != "reserved"}
 
+    def set_accel_levels(self, levels: int) -> None:
+        """1: flattened instances (default), 2: two-level structure."""
+        check(self.lib.krr_wf_set_accel_levels(self._h, levels), "krr_wf_set_accel_levels")
+
     def set_scene_max_depth(self, scene: int, max_depth: int) -> None:
         """Path depth of one scene of the pass (-1: the pass's)."""
         check(self.lib.krr_wf_set_scene_max_depth(self._h, scene, max_depth),

@@ -92,6 +92,36 @@ def closest_brute(tris: np.ndarray, rays: np.ndarray) -> np.ndarray:
     return out
 
 
+def trace_instanced(geometries, instances, inverse, rays, mask=None, any_hit=False):
+    """Two-level closest (or any) hits: geometries as float32 [n_g, 9]
+    object-space triangles, instances as (geometry, transform) pairs whose
+    world-to-object matrices are `inverse` [n_inst, 12] (the ones the GPU
+    structure uses), global ids instance-major."""
+    lib = load()
+    fn = lib.oracle_trace_instanced
+    fn.restype = C.c_int
+    P, I64 = C.c_void_p, C.c_int64
+    fn.argtypes = [P, P, C.c_int, P, P, P, P, C.c_int, P, I64, P, P, C.c_int]
+    verts = np.ascontiguousarray(np.concatenate([np.asarray(g, np.float32).reshape(-1, 9)
+                                                 for g in geometries]), dtype=np.float32)
+    counts = [np.asarray(g).reshape(-1, 9).shape[0] for g in geometries]
+    begin = np.zeros(len(geometries) + 1, np.int64)
+    begin[1:] = np.cumsum(counts)
+    geom = np.array([g for g, _ in instances], np.int32)
+    first = np.zeros(len(instances), np.int64)
+    first[1:] = np.cumsum([counts[g] for g in geom])[:-1]
+    inv = np.ascontiguousarray(inverse, np.float32).reshape(-1, 12)
+    m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+    rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+    hits = np.empty((rays.shape[0], 4), np.float32)
+    occ = np.empty(rays.shape[0], np.uint8)
+    fn(verts.ctypes.data, begin.ctypes.data, len(geometries), geom.ctypes.data, inv.ctypes.data,
+       first.ctypes.data, None if m is None else m.ctypes.data, len(instances), rays.ctypes.data,
+       rays.shape[0], None if any_hit else hits.ctypes.data, occ.ctypes.data if any_hit else None,
+       threads())
+    return occ if any_hit else hits
+
+
 def pcg_floats(px: int, py: int, sample_index: int, advance: int, count: int) -> np.ndarray:
     out = np.empty(count, np.float32)
     load().oracle_pcg_floats(px, py, sample_index, advance, count, out.ctypes.data)

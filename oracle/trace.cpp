@@ -331,6 +331,71 @@ extern "C" int oracle_trace_any(const oracle_bvh *bvh, const float *rays, int64_
     return 0;
 }
 
+// Two-level tracing: instance i draws geometry inst_geom[i] (object-space
+// triangles [geom_begin[g], geom_begin[g + 1]) of v) through the
+// world-to-object matrix inst_inv[12 i..]; the ray is carried into object
+// space row by row (m0 x + m1 y + m2 z (+ m3), each operation rounded as
+// written), the geometry's BVH gives the closest hit with t in (tmin, best
+// t], and it replaces the best hit if its t is smaller or equal with a
+// smaller global id (inst_first[i] + its index in the geometry).  Any-hit:
+// some instance with a non-zero mask has a hit in (tmin, tmax].
+extern "C" int oracle_trace_instanced(const float *v, const int64_t *geom_begin, int n_geoms,
+                                      const int32_t *inst_geom, const float *inst_inv,
+                                      const int64_t *inst_first, const uint8_t *inst_mask,
+                                      int n_inst, const float *rays, int64_t n, float *hits,
+                                      uint8_t *occluded, int threads) {
+    std::vector<oracle_bvh *> geoms(n_geoms, nullptr);
+    for (int g = 0; g < n_geoms; ++g)
+        oracle_bvh_build(v + 9 * (size_t)geom_begin[g], geom_begin[g + 1] - geom_begin[g], 1, &geoms[g]);
+    parallel_for(n, threads, [&](int64_t q) {
+        const float *ray = rays + 8 * q;
+        float best_t = ray[7], bb1 = 0.f, bb2 = 0.f;
+        uint32_t best = kMiss;
+        bool occ = false;
+        for (int i = 0; i < n_inst && !occ; ++i) {
+            if (occluded && inst_mask && !inst_mask[i]) continue;
+            const float *m = inst_inv + 12 * (size_t)i;
+            float oray[8];
+            for (int r = 0; r < 3; ++r) {
+                const float *row = m + 4 * r;
+                float acc = row[0] * ray[0];
+                acc = acc + row[1] * ray[1];
+                acc = acc + row[2] * ray[2];
+                oray[r] = acc + row[3];
+                float dacc = row[0] * ray[4];
+                dacc = dacc + row[1] * ray[5];
+                oray[4 + r] = dacc + row[2] * ray[6];
+            }
+            oray[3] = ray[3];
+            oray[7] = best_t;
+            const oracle_bvh &g = *geoms[inst_geom[i]];
+            if (occluded) {
+                uint8_t o = 0;
+                trace_one<true>(g, oray, nullptr, &o);
+                occ = o != 0;
+                continue;
+            }
+            float h[4];
+            trace_one<false>(g, oray, h, nullptr);
+            uint32_t local;
+            std::memcpy(&local, &h[3], 4);
+            if (local == kMiss) continue;
+            const uint32_t gid = (uint32_t)inst_first[i] + local;
+            if (h[0] < best_t || (h[0] == best_t && gid < best)) {
+                best_t = h[0]; bb1 = h[1]; bb2 = h[2]; best = gid;
+            }
+        }
+        if (occluded) { occluded[q] = occ ? 1 : 0; return; }
+        float *hit = hits + 4 * q;
+        hit[0] = best == kMiss ? INFINITY : best_t;
+        hit[1] = best == kMiss ? 0.f : bb1;
+        hit[2] = best == kMiss ? 0.f : bb2;
+        std::memcpy(&hit[3], &best, 4);
+    });
+    for (auto *g : geoms) oracle_bvh_free(g);
+    return 0;
+}
+
 extern "C" int oracle_trace_closest_brute(const float *v, int64_t n_tris, const float *rays,
                                           int64_t n, float *hits) {
     for (int64_t i = 0; i < n; ++i) {

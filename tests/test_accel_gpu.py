@@ -388,3 +388,36 @@ def test_builders_give_identical_hits(krr_lib, cuda, builder):
     _assert_bits_equal(_gpu_closest(single, r), O.closest_brute(soup[:1], r), "one triangle")
     assert acc.stats()["max_depth"] <= 48
     assert acc.device_errors() == 0
+
+
+def test_two_level_structure_matches_the_instanced_oracle(krr_lib, cuda):
+    """Geometry trees in object space plus an instance tree: closest hits
+    bit-exact against the oracle's two-level restatement (same world-to-object
+    matrices), any-hit with per-instance masks, and again after the
+    instances move (only the instance level is rebuilt)."""
+    from tests.test_oracle import _instanced_scene
+    geos, insts = _instanced_scene(seed=5, n_inst=60)
+    mask = np.ones(len(insts), np.uint8)
+    mask[::7] = 0
+    acc = Accel.instanced(geos, insts, mask)
+    st = acc.stats()
+    assert st["n_triangles"] == sum(geos[g].shape[0] for g, _ in insts)
+    rays = H.random_rays(20000, 9, box=5.0)
+    d_rays = torch.from_numpy(rays).cuda()
+    inv = acc.instance_inverse()
+    want = O.trace_instanced(geos, insts, inv, rays)
+    got = _gpu_closest(acc, rays)
+    _assert_bits_equal(got, want, "two-level closest")
+    assert (got[:, 3].view(np.uint32) != 0xFFFFFFFF).mean() > 0.05
+    occ = acc.trace_any(d_rays).cpu().numpy()
+    assert np.array_equal(occ, O.trace_instanced(geos, insts, inv, rays, mask=mask, any_hit=True))
+    # move every instance: the instance level is rebuilt, hits follow
+    moved = [(g, np.asarray(m, np.float32).copy()) for g, m in insts]
+    for k, (g, m) in enumerate(moved):
+        m[:, 3] += np.array([0.3 * np.sin(k), 0.2, -0.1 * k / len(moved)], np.float32)
+    acc.update_instances(np.stack([m for _, m in moved]))
+    inv2 = acc.instance_inverse()
+    assert not np.array_equal(inv, inv2)
+    _assert_bits_equal(_gpu_closest(acc, rays), O.trace_instanced(geos, moved, inv2, rays),
+                       "two-level closest after an update")
+    assert acc.device_errors() == 0

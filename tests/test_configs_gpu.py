@@ -67,7 +67,7 @@ def test_config1_large_scene_1080p_row_bands(krr_lib, cuda):
     for r0, r1 in ((300, 340), (700, 740)):   # terrain and spheres; foreground terrain
         oL, _ = ora.render({"max_depth": 8}, 1, r0 * w, r1 * w)
         compare(L[r0 * w:r1 * w, :3], oL, f"1080p rows {r0}..{r1}", max_outliers=0.005)
-        assert (oL.sum(1) > 0).mean() > 0.9
+        assert (oL.sum(1) > 0).mean() > 0.3
 
 
 @pytest.mark.slow

@@ -342,3 +342,48 @@ def test_empty_geometry(krr_lib, cuda):
     img = pt.render().cpu().numpy()
     assert np.allclose(img[..., :3], np.array([0.4, 0.6, 1.0], np.float32), rtol=1e-6)
     assert pt.device_errors() == 0
+
+
+def test_two_level_structure_in_the_pass(krr_lib, cuda):
+    """The pass on the two-level structure (each geometry once, an instance
+    tree over them): frames within the per-pixel tolerance of the oracle
+    (object-space hits differ from world-space ones by rounding), and after
+    an instance update (only the instance tree is rebuilt) equal bit for bit
+    to a two-level pass built from the moved scene."""
+    import copy
+    sc = scenes.large_scene(width=160, height=90, grid=128, n_spheres=40, sky_size=(128, 64),
+                            max_depth=6)
+    pt = WavefrontPathTracer({"max_depth": 6})
+    pt.set_accel_levels(2)
+    pt.set_scene(sc)
+    pt.resize(sc.width, sc.height)
+    L, _ = gpu_frame(pt, sc, 2)
+    assert pt.device_errors() == 0
+    oL, _ = O.PathTracer(sc).render({"max_depth": 6}, 2)
+    compare(L[:, :3], oL, "two-level large scene", max_outliers=0.01)
+    moved = copy.deepcopy(sc)
+    xfs = []
+    for k in (3, 10, 17):
+        mesh, xf = moved.instances[k]
+        xf = np.array(xf, np.float32)
+        xf[:, 3] += np.array([0.5, 0.3, -0.4], np.float32)
+        moved.instances[k] = (mesh, xf)
+        xfs.append(xf)
+    pt.update_instances([3, 10, 17], np.stack(xfs))
+    got, _ = gpu_frame(pt, moved, 3)
+    ref = WavefrontPathTracer({"max_depth": 6})
+    ref.set_accel_levels(2)
+    ref.set_scene(moved)
+    ref.resize(sc.width, sc.height)
+    want, _ = gpu_frame(ref, moved, 3)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    # the volume box (null-material interface, medium tracking) on two levels
+    vb = scenes.volume_box(64, 64, max_depth=8, grid=32)
+    pv = WavefrontPathTracer({"max_depth": 8})
+    pv.set_accel_levels(2)
+    pv.set_scene(vb)
+    pv.resize(64, 64)
+    L, _ = gpu_frame(pv, vb, 1)
+    assert pv.device_errors() == 0
+    oL, _ = O.PathTracer(vb).render({"max_depth": 8}, 1)
+    compare(L[:, :3], oL, "two-level volume box", max_outliers=0.01)
