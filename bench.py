@@ -305,17 +305,22 @@ def wavefront_frame(sc, acc, peak, frames: int = 5):
         e1.synchronize()
         ms.append(e0.elapsed_time(e1))
     frame_ms = sorted(ms)[len(ms) // 2]
-    # the same frames from the megakernel (one thread per path, no queues)
-    mk = []
-    for f in range(10, 10 + frames):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        pt.begin_frame(f, sc.camera)
-        e0.record(s)
-        pt.render_megakernel(out)
-        e1.record(s)
-        e1.synchronize()
-        mk.append(e0.elapsed_time(e1))
-    mk_ms = sorted(mk)[len(mk) // 2]
+    # the same frames from the megakernel (one thread per path, no queues),
+    # with the per-bounce regrouping of paths by hit class and without
+    mk_ms = {}
+    for reorder in (1, 0):
+        pt.set_megakernel_reorder(reorder)
+        mk = []
+        for f in range(10, 10 + frames):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            pt.begin_frame(f, sc.camera)
+            e0.record(s)
+            pt.render_megakernel(out)
+            e1.record(s)
+            e1.synchronize()
+            mk.append(e0.elapsed_time(e1))
+        mk_ms[reorder] = sorted(mk)[len(mk) // 2]
+    pt.set_megakernel_reorder(1)
 
     def stage_loop(count: bool, shadow_rays=None):
         items = {k: 0 for k in STAGE_BYTES}
@@ -375,7 +380,8 @@ def wavefront_frame(sc, acc, peak, frames: int = 5):
     shadow_mrays = rs.shape[0] * 10 / (e0.elapsed_time(e1) / 1e3) / 1e6
     return {"resolution": f"{sc.width}x{sc.height}", "max_depth": sc.max_depth,
             "frame_ms": round(frame_ms, 3), "paths_per_s": round(sc.width * sc.height / frame_ms * 1e3),
-            "megakernel_frame_ms": round(mk_ms, 3),
+            "megakernel_frame_ms": round(mk_ms[1], 3),
+            "megakernel_frame_ms_without_reorder": round(mk_ms[0], 3),
             "stages": stages, "shadow_rays": int(rs.shape[0]), "shadow_mrays_s": round(shadow_mrays, 1),
             "note": "stage loop timed stage by stage (each with its own events); render() traces "
                     "each bounce's shadow rays with the next bounce's rays in one launch"}

@@ -394,6 +394,13 @@ int krr_wf_render(krr_wf *wf, float *d_out_rgba, void *stream);
  * returns KRR_ERR_INVALID_ARGUMENT for scenes with media or with a cache
  * attached. */
 int krr_wf_render_megakernel(krr_wf *wf, float *d_out_rgba, void *stream);
+/* Coherence step of the megakernel variant (default 1): the 128 paths of a
+ * block advance one bounce at a time and, after each closest hit, are
+ * regrouped through shared memory by hit class (miss / null, diffuse,
+ * dielectric, conductor, finished), as the reference's megakernel calls
+ * optixReorder(hit, 1) (src/render/megakernel/device.cu:173-176).  0: one
+ * path per thread from start to end.  Frames are the same either way. */
+int krr_wf_set_megakernel_reorder(krr_wf *wf, int32_t reorder);
 
 /* Batched views: many cameras of different sizes in one wavefront (one
  * launch per stage per bounce).  krr_wf_resize_views replaces resize; each

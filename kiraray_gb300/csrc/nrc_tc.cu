@@ -1,16 +1,17 @@
 // Fused neural-radiance-cache forward pass on the 5th-generation tensor
-// cores (tcgen05), one 128-row tile of queries at a time per CTA.
+// cores (tcgen05), two 128-row tiles of queries in flight per CTA.
 //
-// Per tile: the 128 threads encode their query (hash grid, trilinear) into
-// a 128x64 BF16 activation tile in shared memory; then for each of the six
-// layers one elected thread issues four tcgen05.mma.kind::f16 (M=128,
-// N=64 or 16, K=16, BF16 x BF16 -> FP32 in tensor memory), commits them to
-// an mbarrier, and all threads read the accumulator rows back with
-// tcgen05.ld, apply ReLU, round to BF16 and write the next activation tile
-// (or the RGB output).  All weights (43 KB, BF16) stay resident in shared
-// memory for the CTA's lifetime.  Waits on the mbarrier are bounded: a wait
-// that gives up sets an error flag and the CTA frees its tensor memory and
-// returns.
+// Per tile: four encoder warps encode the queries (hash grid, trilinear)
+// into a 128x64 BF16 activation tile in shared memory while four MLP warps
+// run the previous tile: for each of the six layers one elected thread
+// issues four tcgen05.mma.kind::f16 (M=128, N=64 or 16, K=16, BF16 x BF16 ->
+// FP32 in tensor memory), commits them to an mbarrier, and the 128 MLP
+// threads read the accumulator rows back with tcgen05.ld, apply ReLU, round
+// to BF16 and write the next activation tile (or the RGB output).  All
+// weights (43 KB, BF16) stay resident in shared memory for the CTA's
+// lifetime.  Waits on the mbarrier are bounded: a wait that gives up sets an
+// error flag, and the CTA finishes without further tensor-core work and
+// frees its tensor memory.
 //
 // Shared-memory operands use the canonical K-major layout without swizzle:
 // 8x8-element core matrices of 128 contiguous bytes, core (i, j) of a tile
@@ -128,19 +129,6 @@ __device__ __forceinline__ void store_row(uint8_t *tile, uint32_t r, const float
     }
 }
 
-// Copies the rows < n of a canonical 128x64 BF16 tile to a row-major global
-// array (16-byte chunks; eight consecutive threads write one 128-byte row, so
-// a warp writes four whole rows per instruction).
-__device__ __forceinline__ void dump_tile(const uint8_t *tile, __nv_bfloat16 *dst, int64_t row0,
-                                          int64_t n) {
-    for (int c = threadIdx.x; c < kTcRows * 8; c += blockDim.x) {
-        const int r = c >> 3, j = c & 7;
-        if (row0 + r < n)
-            reinterpret_cast<uint4 *>(dst + (row0 + r) * kNrcIn)[j] =
-                *reinterpret_cast<const uint4 *>(tile + canon((uint32_t)r, (uint32_t)(8 * j)));
-    }
-}
-
 // Packs the BF16 weights [layer][out][64] into canonical tiles.
 __global__ void k_pack_weights(const __nv_bfloat16 *__restrict__ w, NrcMlp mlp, uint8_t *packed) {
     int total = mlp.n_params;
@@ -213,18 +201,42 @@ __device__ __forceinline__ void encode_row(const NrcGrid &g, const float *q,
     for (int k = o + kNrcExtra; k < kNrcIn; ++k) x[k] = 0.f;
 }
 
+__device__ __forceinline__ void bar_sync(int id, int n) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+__device__ __forceinline__ void bar_arrive(int id, int n) {
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+// Named barriers of the forward kernel (0 is __syncthreads): a tile buffer
+// is full (encoders -> MLP warps), a tile buffer is free again (MLP warps
+// -> encoders), and the MLP warps' own per-layer barrier.
+constexpr int kBarFull = 1, kBarEmpty = 3, kBarMlp = 5;
+constexpr int kFwThreads = 256;   // warps 0-3: MLP (tensor-memory lanes 0-127); 4-7: encoders
+
 // out[i][0..3) for i < *count (or cap); optional per-layer activation dump
 // (bf16 [layers][cap][64], row-major) for the training backward pass.
-__global__ void __launch_bounds__(kTcThreads, 1)
+//
+// Warp-specialised: warps 4-7 encode the rows of the CTA's next tile (the
+// hash-grid gathers) into one of two activation buffers while warps 0-3 run
+// the six layers of the current tile out of the other (one thread issues
+// the MMAs, all 128 read the accumulator rows back, apply ReLU and write the
+// next layer's input in place), so the gathers of tile k+1 overlap the MMA
+// chain of tile k.  The groups hand the buffers over with named barriers;
+// after a failed (bounded) accumulator wait the MLP warps skip the compute
+// of the remaining tiles but keep handing buffers back, so no warp waits
+// forever.
+__global__ void __launch_bounds__(kFwThreads, 1)
 k_nrc_forward_tc(NrcGrid g, int layers, const float *__restrict__ in, const int32_t *d_count,
                  int64_t cap, const __nv_bfloat16 *__restrict__ table,
                  const uint8_t *__restrict__ packed_w, float *__restrict__ out,
                  __nv_bfloat16 *__restrict__ acts, uint32_t *err) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t *sw = smem;                                              // weights
-    uint8_t *sa = smem + (layers - 1) * kLayerBytes + kOutBytes;     // activation tile
-    sa = reinterpret_cast<uint8_t *>(((uintptr_t)sa + 1023) & ~(uintptr_t)1023);
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(sa + kTcRows * kNrcIn * 2);
+    uint8_t *sa0 = smem + (layers - 1) * kLayerBytes + kOutBytes;    // activation tiles
+    sa0 = reinterpret_cast<uint8_t *>(((uintptr_t)sa0 + 1023) & ~(uintptr_t)1023);
+    uint8_t *sa1 = sa0 + kTcRows * kNrcIn * 2;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(sa1 + kTcRows * kNrcIn * 2);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
     uint32_t *fail_flag = tmem_slot + 1;
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -247,83 +259,104 @@ k_nrc_forward_tc(NrcGrid g, int layers, const float *__restrict__ in, const int3
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t my_lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
 
-    int64_t n = d_count ? min((int64_t)*d_count, cap) : cap;
-    int64_t tiles = (n + kTcRows - 1) / kTcRows;
-    uint32_t phase = 0;
-    bool failed = false;
-    float x[kNrcIn];
-    for (int64_t t = blockIdx.x; t < tiles && !failed; t += gridDim.x) {
-        int64_t row = t * kTcRows + tid;
-        if (row < n) encode_row(g, in + kNrcInputs * row, table, x);
-        else
-            for (int k = 0; k < kNrcIn; ++k) x[k] = 0.f;
-        store_row(sa, (uint32_t)tid, x);
-        fence_proxy_async();
-        fence_before_sync();
-        __syncthreads();
-        for (int l = 0; l < layers; ++l) {
-            const bool last = l + 1 == layers;
-            const int nrows = last ? kNrcOutPad : kNrcWidth;
-            // the tile holds this layer's input X_l, complete since the last
-            // barrier: dump it for the backward pass while the MMAs read it
-            // (it is overwritten only after the accumulator wait's barrier)
-            if (acts) dump_tile(sa, acts + (size_t)l * cap * kNrcIn, t * kTcRows, n);
-            if (tid == 0) {
-                fence_after_sync();
-                const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sw + l * kLayerBytes);
-                const uint32_t idesc = idesc_bf16(kTcRows, nrows);
+    const int64_t n = d_count ? min((int64_t)*d_count, cap) : cap;
+    const int64_t tiles = (n + kTcRows - 1) / kTcRows;
+    if (warp >= 4) {
+        // encoders: row r of each tile into the free buffer
+        const int r = tid - 128;
+        float x[kNrcIn];
+        int k = 0;
+        for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x, ++k) {
+            uint8_t *sa = (k & 1) ? sa1 : sa0;
+            if (k >= 2) bar_sync(kBarEmpty + (k & 1), kFwThreads);
+            const int64_t row = t * kTcRows + r;
+            if (row < n) encode_row(g, in + kNrcInputs * row, table, x);
+            else
+                for (int q = 0; q < kNrcIn; ++q) x[q] = 0.f;
+            store_row(sa, (uint32_t)r, x);
+            fence_proxy_async();   // the tensor cores read the tile through the async proxy
+            bar_arrive(kBarFull + (k & 1), kFwThreads);
+        }
+    } else {
+        const uint32_t my_lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+        uint32_t phase = 0;
+        bool failed = false;
+        int k = 0;
+        for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x, ++k) {
+            uint8_t *sa = (k & 1) ? sa1 : sa0;
+            bar_sync(kBarFull + (k & 1), kFwThreads);
+            const int64_t row = t * kTcRows + tid;
+            for (int l = 0; l < layers && !failed; ++l) {
+                const bool last = l + 1 == layers;
+                const int nrows = last ? kNrcOutPad : kNrcWidth;
+                // the tile holds this layer's input X_l: dump it for the
+                // backward pass while the MMAs read it (it is overwritten
+                // only after the accumulator wait's barrier)
+                if (acts) {
+                    __nv_bfloat16 *dst = acts + (size_t)l * cap * kNrcIn;
+                    for (int c = tid; c < kTcRows * 8; c += kTcRows) {
+                        const int rr = c >> 3, j = c & 7;
+                        if (t * kTcRows + rr < n)
+                            reinterpret_cast<uint4 *>(dst + (t * kTcRows + rr) * kNrcIn)[j] =
+                                *reinterpret_cast<const uint4 *>(sa + canon((uint32_t)rr, (uint32_t)(8 * j)));
+                    }
+                }
+                if (tid == 0) {
+                    fence_after_sync();
+                    const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sw + l * kLayerBytes);
+                    const uint32_t idesc = idesc_bf16(kTcRows, nrows);
 #pragma unroll
-                for (int kk = 0; kk < kNrcIn / 16; ++kk)
-                    tc_mma(tmem, smem_desc(a0 + 256u * kk, 128u, 1024u),
-                           smem_desc(b0 + 256u * kk, 128u, 1024u), idesc, kk > 0 ? 1u : 0u);
-                tc_commit(smem_u32(mbar));
-            }
-            // thread 0 waits for the accumulator (bounded) and tells the
-            // others; the decision to stop is uniform across the CTA
-            if (tid == 0) {
-                uint32_t spins = 0, ok = 0;
-                while (!(ok = mbar_try_wait(smem_u32(mbar), phase)) && ++spins < kWaitLimit) {
+                    for (int kk = 0; kk < kNrcIn / 16; ++kk)
+                        tc_mma(tmem, smem_desc(a0 + 256u * kk, 128u, 1024u),
+                               smem_desc(b0 + 256u * kk, 128u, 1024u), idesc, kk > 0 ? 1u : 0u);
+                    tc_commit(smem_u32(mbar));
+                    // bounded wait for the accumulator; the decision to stop
+                    // is uniform across the MLP warps
+                    uint32_t spins = 0, ok = 0;
+                    while (!(ok = mbar_try_wait(smem_u32(mbar), phase)) && ++spins < kWaitLimit) {
+                    }
+                    *fail_flag = ok ? 0u : 1u;
+                    if (!ok) atomicOr(err, (uint32_t)kErrLoopLimit);
                 }
-                *fail_flag = ok ? 0u : 1u;
-                if (!ok) atomicOr(err, (uint32_t)kErrLoopLimit);
-            }
-            __syncthreads();
-            if (*fail_flag) {
-                failed = true;
-                break;
-            }
-            {
-                uint32_t spins = 0;   // already complete: returns at once
-                while (!mbar_try_wait(smem_u32(mbar), phase) && ++spins < kWaitLimit) {
+                bar_sync(kBarMlp, kTcRows);
+                if (*fail_flag) {
+                    failed = true;
+                    break;
                 }
+                {
+                    uint32_t spins = 0;   // already complete: returns at once
+                    while (!mbar_try_wait(smem_u32(mbar), phase) && ++spins < kWaitLimit) {
+                    }
+                }
+                phase ^= 1u;
+                fence_after_sync();
+                float v[kNrcIn];
+                tmem_ld16(my_lane_addr + 0, v);
+                if (!last) {
+                    tmem_ld16(my_lane_addr + 16, v + 16);
+                    tmem_ld16(my_lane_addr + 32, v + 32);
+                    tmem_ld16(my_lane_addr + 48, v + 48);
+                }
+                tmem_wait_ld();
+                if (!last) {
+                    for (int q = 0; q < kNrcIn; ++q) v[q] = fmaxf(v[q], 0.f);
+                    store_row(sa, (uint32_t)tid, v);
+                    fence_proxy_async();
+                } else if (row < n) {
+                    out[row * kNrcOutPad + 0] = v[0];
+                    out[row * kNrcOutPad + 1] = v[1];
+                    out[row * kNrcOutPad + 2] = v[2];
+                }
+                fence_before_sync();
+                bar_sync(kBarMlp, kTcRows);
             }
-            phase ^= 1u;
-            fence_after_sync();
-            float v[kNrcIn];
-            tmem_ld16(my_lane_addr + 0, v);
-            if (!last) {
-                tmem_ld16(my_lane_addr + 16, v + 16);
-                tmem_ld16(my_lane_addr + 32, v + 32);
-                tmem_ld16(my_lane_addr + 48, v + 48);
-            }
-            tmem_wait_ld();
-            if (!last) {
-                for (int k = 0; k < kNrcIn; ++k) v[k] = fmaxf(v[k], 0.f);
-                store_row(sa, (uint32_t)tid, v);
-                fence_proxy_async();
-            } else if (row < n) {
-                out[row * kNrcOutPad + 0] = v[0];
-                out[row * kNrcOutPad + 1] = v[1];
-                out[row * kNrcOutPad + 2] = v[2];
-            }
-            fence_before_sync();
-            __syncthreads();
+            bar_arrive(kBarEmpty + (k & 1), kFwThreads);   // the buffer is free
         }
     }
-    fence_after_sync();
+    fence_before_sync();
     __syncthreads();
+    fence_after_sync();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols));
 }
@@ -570,7 +603,7 @@ static int tc_ctas_per_sm(const void *fn, int threads, size_t smem, int dev) {
 
 size_t nrc_tc_smem_bytes(int layers) {
     size_t w = (size_t)(layers - 1) * kLayerBytes + kOutBytes;
-    size_t a = ((w + 1023) & ~(size_t)1023) + kTcRows * kNrcIn * 2;
+    size_t a = ((w + 1023) & ~(size_t)1023) + 2 * kTcRows * kNrcIn * 2;   // two tile buffers
     return a + 64 + 1024;   // mbarrier, tensor-memory slot, alignment slack
 }
 
@@ -634,10 +667,10 @@ int nrc_forward_tc(const NrcGrid &g, const NrcMlp &mlp, const float *d_in, const
     // the MMA chains of the others: as many as registers, shared memory and
     // the 512 tensor-memory columns allow (3 for five hidden layers)
     static int per_sm = 0;
-    if (!per_sm) per_sm = tc_ctas_per_sm((const void *)k_nrc_forward_tc, kTcThreads, smem, dev);
+    if (!per_sm) per_sm = tc_ctas_per_sm((const void *)k_nrc_forward_tc, kFwThreads, smem, dev);
     int64_t tiles = (cap + kTcRows - 1) / kTcRows;
     int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)sms * per_sm));
-    k_nrc_forward_tc<<<grid, kTcThreads, smem, s>>>(g, mlp.layers, d_in, d_count, cap, table, packed,
+    k_nrc_forward_tc<<<grid, kFwThreads, smem, s>>>(g, mlp.layers, d_in, d_count, cap, table, packed,
                                                     d_out, acts, err);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;

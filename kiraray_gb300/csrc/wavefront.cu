@@ -90,6 +90,7 @@ struct krr_wf {
     std::vector<int32_t> inf_part;
     std::vector<int32_t> part_own_depth;   // -1: the pass's max_depth
     int32_t levels = 1;                    // 1: flattened instances, 2: two-level structure
+    int32_t mk_reorder = 1;                // megakernel: reorder paths by hit class per bounce
     std::vector<DevMesh> h_mesh;           // host copies of the device meshes
     std::vector<int64_t> h_mesh_tris;      // triangles per mesh
     int32_t n_parts = 1;
@@ -644,10 +645,11 @@ __device__ __forceinline__ V3 miss_radiance(const DevScene &s, const DevScenePar
 
 // Routing of a closest hit (__closesthit__/__miss__Closest, device.cu:43-74).
 // Four blocks per SM (64 registers): the mesh gathers are latency-bound.
-// With `inline_lights` (render(), no media) the radiance of a miss and of an
-// emissive hit is added here instead of through the miss and hit-light
-// queues: a path has one item per bounce, so each pixel's sum gets the same
-// terms in the same order as handleHit/handleMiss after this stage.
+// With `inline_lights` (render()) the radiance of a miss and of an emissive
+// hit of a ray outside every medium is added here instead of through the
+// miss and hit-light queues: a path has one item per bounce, so each pixel's
+// sum gets the same terms in the same order as handleHit/handleMiss after
+// this stage.
 __global__ void __launch_bounds__(kThreads, 4)
 k_hit_process(DevScene s, Queue rq, const float4 *__restrict__ hits, Queue next, Queue miss,
               Queue hitl, Queue scat, Queue msq, int enable_medium, uint32_t *err, NrcHook hook,
@@ -1256,13 +1258,162 @@ __global__ void k_resolve(PixelState ps, float4 *out, const DevView *__restrict_
 
 // ---------------------------------------------------------------- megakernel
 // The stage loop of integrator.cpp:223-266 run as one kernel, one thread per
-// pixel: each bounce's closest hit, emission or environment, NEE shadow ray
-// and BSDF sample are taken in registers in the stages' order, with the same
-// device functions, so a pixel's radiance equals the wavefront pass's bit for
-// bit.  It is the queue-free side of an A/B against the wavefront (the
-// reference's MegakernelPathTracer, src/render/megakernel/device.cu:148-195,
-// has the same structure but its own sampling and MIS).  Surfaces only: no
-// media and no cache hooks.
+// pixel path: each bounce's closest hit, emission or environment, NEE shadow
+// ray and BSDF sample are taken in registers in the stages' order, with the
+// same device functions, so a pixel's radiance equals the wavefront pass's
+// bit for bit.  It is the queue-free side of an A/B against the wavefront
+// (the reference's MegakernelPathTracer, src/render/megakernel/device.cu:
+// 148-195, has the same structure but its own sampling and MIS).  Surfaces
+// only: no media and no cache hooks.
+
+// One path of the megakernel between bounces.
+struct MkPath {
+    V3 ro, rd, thp, pu, pl, ctx_p, L, acc;
+    ulonglong2 rng;        // Pcg state, inc
+    float4 hit;            // closest hit of ro, rd: t, b1, b2, id
+    uint32_t pixel, flags, depth;
+    int32_t medium;
+    uint32_t alive;
+};
+
+// generateCameraRays for the path's pixel (integrator.cpp:166-179).
+__device__ __forceinline__ void mk_camera(MkPath &p, Pcg &rng, const DevView &v, int64_t i) {
+    const DevCamera &cam = v.cam;
+    float fx = rng.get1d(), fy = rng.get1d();
+    float lx = rng.get1d(), ly = rng.get1d();
+    float tm = rng.get1d();
+    (void)lx; (void)ly; (void)tm;
+    float px = (float)(i % v.w) + 0.5f + fx;
+    float py = (float)(i / v.w) + 0.5f + fy;
+    float ndcx = (2 * px) / (float)v.w + (-1.f);
+    float ndcy = (2 * py) / (float)v.h + (-1.f);
+    V3 fd = normalize(V3{cam.tan_fov * cam.aspect * ndcx, cam.tan_fov * ndcy, -1.f});
+    p.ro = V3{cam.pos[0], cam.pos[1], cam.pos[2]};
+    p.rd = mat3_mul(cam.rot, fd);
+    p.ctx_p = v3(0.f);
+    p.thp = p.pu = p.pl = v3(1.f);
+    p.flags = 0u;
+    p.depth = 0u;
+    p.medium = cam.medium;
+    p.alive = 1u;
+}
+
+// One bounce after the closest hit p.hit: handleMiss / handleHit, then
+// generateScatterRays with its NEE shadow ray traced in place; returns
+// whether the path continues (its next ray in p.ro, p.rd).
+template <int FMT>
+__device__ __forceinline__ bool mk_bounce(const DevScene &s, const WfConst &c, const float4 *__restrict__ nodes,
+                                          const float4 *__restrict__ tris, MkPath &p, Pcg &rng, int iter,
+                                          float lsel_pdf, int *trace_err) {
+    const float4 h = p.hit;
+    const uint32_t gid = ubits(h.w);
+    bool next = false, scatter = false;
+    Surf sf;
+    if (gid == KRR_MISS) {
+        if (s.n_infinite > 0) {
+            V3 Lm = v3(0.f);
+            for (int k = 0; k < s.n_infinite; ++k) {
+                const DevInfinite &e = s.infinite[k];
+                if (c.nee && p.depth && !(p.flags & BSDF_DELTA)) {
+                    float light_pdf = kInv4Pi * lsel_pdf;
+                    Lm += env_Li(e, p.rd) / mean(p.pu + p.pl * light_pdf);
+                } else {
+                    Lm += env_Li(e, p.rd) / mean(p.pu);
+                }
+            }
+            V3 add = p.thp * Lm;
+            p.L = add + p.L;
+        }
+    } else {
+        sf = prepare_surface(s, h.y, h.z, gid, p.rd);
+        if (sf.material < 0) {
+            // null material: the same ray continues from the interface
+            p.ro = offset_ray_origin(sf.p, sf.n, p.rd);
+            p.medium = medium_towards(sf.interface_in, sf.interface_out, p.medium, sf.n, p.rd);
+            next = true;
+        } else {
+            if (sf.light >= 0) {
+                const DevLight &l = s.lights[sf.light];
+                const DevInstance &I = s.instances[l.index];
+                V3 Le = area_L(I, sf.n, sf.wo) * p.thp;
+                if (c.nee && p.depth && !(p.flags & BSDF_DELTA)) {
+                    float light_pdf = area_pdf(s, l, sf.p, sf.n, p.ctx_p) * lsel_pdf;
+                    Le = Le / mean(p.pl * light_pdf + p.pu);
+                } else {
+                    Le = Le / mean(p.pu);
+                }
+                p.L = Le + p.L;
+            }
+            scatter = any(p.thp);
+        }
+    }
+    if (iter == c.max_depth) return false;
+    if (scatter) {
+        if (rng.get1d() >= c.rr) return false;
+        V3 sthp = p.thp / c.rr;
+        const DevMesh &M = s.meshes[sf.mesh];
+        bool transition = M.medium_inside != M.medium_outside;
+        int32_t mi = transition ? M.medium_inside : -2, mo = transition ? M.medium_outside : -2;
+        const V3 tg = sf.t, bt = sf.b, nrm = sf.n, pp = sf.p;
+        auto to_local = [&](V3 w) { return V3{dot(tg, w), dot(bt, w), dot(nrm, w)}; };
+        V3 wo_local = to_local(sf.wo);
+        ShadingData sd = shading_data(s, sf.material);
+        uint32_t bsdf_type = bsdf_type_of(sd);
+        Bsdf bsdf = Bsdf::setup(sd);
+        if (c.nee && (bsdf_type & BSDF_SMOOTH) && s.n_lights > 0) {
+            float ul = rng.get1d();
+            uint32_t lid = (uint32_t)(ul * (float)s.n_lights);
+            float sel_pdf = 1.f / (float)s.n_lights;
+            float u0 = rng.get1d(), u1 = rng.get1d();
+            LightSample ls = sample_li(s, s.lights[lid], u0, u1, pp);
+            V3 to = offset_ray_origin(ls.p, ls.n, pp - ls.p);
+            V3 po = offset_ray_origin(pp, nrm, to - pp);
+            V3 d = to - po;
+            V3 wi_world = normalize(d);
+            V3 wi_local = to_local(wi_world);
+            float light_pdf = sel_pdf * ls.pdf;
+            V3 fv = bsdf.f(wo_local, wi_local);
+            float bsdf_pdf = bsdf.pdf(wo_local, wi_local);
+            if (light_pdf > 0 && any(fv)) {
+                V3 Ld = ls.L * sthp * fv * fabsf(wi_local.z);
+                if (any(Ld)) {
+                    // traceShadow + resolve
+                    float4 sh = traverse_ray<true, FMT>(nodes, tris, po, d, 0.f, 1.f, trace_err);
+                    if (ubits(sh.w) == KRR_MISS) {
+                        V3 add = Ld / mean(p.pu * light_pdf + p.pu * bsdf_pdf);
+                        p.L = add + p.L;
+                    }
+                }
+            }
+        }
+        BsdfSample bs = bsdf.sample(wo_local, [&]() { return rng.get1d(); });
+        if (bs.pdf != 0 && any(bs.f)) {
+            V3 wi_world = tg * bs.wi.x + bt * bs.wi.y + nrm * bs.wi.z;
+            V3 nthp = sthp * bs.f * fabsf(bs.wi.z) / bs.pdf;
+            if (any(nthp)) {
+                p.ro = offset_ray_origin(pp, nrm, wi_world);
+                p.medium = medium_towards(mi, mo, p.medium, nrm, wi_world);
+                p.rd = wi_world;
+                p.ctx_p = pp;
+                p.flags = bs.flags;
+                p.thp = nthp;
+                p.depth = p.depth + 1;
+                p.pl = p.pu / bs.pdf;
+                next = true;
+            }
+        }
+    }
+    return next;
+}
+
+__device__ __forceinline__ void mk_finish_pixel(const MkPath &p, const DevView &v, int64_t i, const WfConst &c,
+                                                float4 *__restrict__ out) {
+    V3 col = p.acc / (float)c.spp;
+    if (c.enable_clamp) col = vmin(vmax(col, v3(0.f)), v3(c.clamp_max));
+    const int64_t x = i % v.w, y = i / v.w;
+    out[v.offset + (v.h - 1 - y) * (int64_t)v.w + x] = f4(col, 1.f);
+}
+
 template <int FMT>
 __global__ void __launch_bounds__(128)
 k_megakernel(DevScene s, const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
@@ -1274,146 +1425,115 @@ k_megakernel(DevScene s, const float4 *__restrict__ nodes, const float4 *__restr
     for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n;
          g += (int64_t)gridDim.x * blockDim.x) {
         const DevView &v = views[view_of(views, nv, g)];
-        const DevCamera &cam = v.cam;
         const int64_t i = g - v.offset;
-        const uint32_t pixel = (uint32_t)g;
-        Pcg rng = load_rng(ps, pixel);
+        Pcg rng = load_rng(ps, (uint32_t)g);
         const float4 l0 = ps.L[g], p0 = ps.pixel[g];
-        V3 L = f3(l0), acc = f3(p0);
+        MkPath p;
+        p.L = f3(l0);
+        p.acc = f3(p0);
         for (int sample = 0; sample < c.spp; ++sample) {
-            // generateCameraRays
-            float fx = rng.get1d(), fy = rng.get1d();
-            float lx = rng.get1d(), ly = rng.get1d();
-            float tm = rng.get1d();
-            (void)lx; (void)ly;
-            float px = (float)(i % v.w) + 0.5f + fx;
-            float py = (float)(i / v.w) + 0.5f + fy;
-            float ndcx = (2 * px) / (float)v.w + (-1.f);
-            float ndcy = (2 * py) / (float)v.h + (-1.f);
-            V3 fd = normalize(V3{cam.tan_fov * cam.aspect * ndcx, cam.tan_fov * ndcy, -1.f});
-            V3 ro = V3{cam.pos[0], cam.pos[1], cam.pos[2]};
-            V3 rd = mat3_mul(cam.rot, fd);
-            const float time = cam.shutter_open + cam.shutter_time * tm;
-            V3 ctx_p = v3(0.f), ctx_n = v3(0.f), thp = v3(1.f), pu = v3(1.f), pl = v3(1.f);
-            uint32_t flags = 0u, depth = 0u;
-            int32_t medium = cam.medium;
+            mk_camera(p, rng, v, i);
             for (int iter = 0;; ++iter) {
-                const float4 h = traverse_ray<false, FMT>(nodes, tris, ro, rd, 0.f, INFINITY, trace_err);
-                const uint32_t gid = ubits(h.w);
-                bool next = false, scatter = false;
-                Surf sf;
-                if (gid == KRR_MISS) {
-                    // handleMiss
-                    if (s.n_infinite > 0) {
-                        V3 Lm = v3(0.f);
-                        for (int k = 0; k < s.n_infinite; ++k) {
-                            const DevInfinite &e = s.infinite[k];
-                            if (c.nee && depth && !(flags & BSDF_DELTA)) {
-                                float light_pdf = kInv4Pi * lsel_pdf;
-                                Lm += env_Li(e, rd) / mean(pu + pl * light_pdf);
-                            } else {
-                                Lm += env_Li(e, rd) / mean(pu);
-                            }
-                        }
-                        V3 add = thp * Lm;
-                        L = add + L;
-                    }
-                } else {
-                    sf = prepare_surface(s, h.y, h.z, gid, rd);
-                    if (sf.material < 0) {
-                        // null material: the same ray continues from the interface
-                        ro = offset_ray_origin(sf.p, sf.n, rd);
-                        medium = medium_towards(sf.interface_in, sf.interface_out, medium, sf.n, rd);
-                        next = true;
-                    } else {
-                        if (sf.light >= 0) {
-                            // handleHit
-                            const DevLight &l = s.lights[sf.light];
-                            const DevInstance &I = s.instances[l.index];
-                            V3 Le = area_L(I, sf.n, sf.wo) * thp;
-                            if (c.nee && depth && !(flags & BSDF_DELTA)) {
-                                float light_pdf = area_pdf(s, l, sf.p, sf.n, ctx_p) * lsel_pdf;
-                                Le = Le / mean(pl * light_pdf + pu);
-                            } else {
-                                Le = Le / mean(pu);
-                            }
-                            L = Le + L;
-                        }
-                        scatter = any(thp);
-                    }
-                }
-                if (iter == c.max_depth) break;
-                if (scatter) {
-                    // generateScatterRays
-                    if (rng.get1d() >= c.rr) break;
-                    V3 sthp = thp / c.rr;
-                    const DevMesh &M = s.meshes[sf.mesh];
-                    bool transition = M.medium_inside != M.medium_outside;
-                    int32_t mi = transition ? M.medium_inside : -2, mo = transition ? M.medium_outside : -2;
-                    const V3 tg = sf.t, bt = sf.b, nrm = sf.n, p = sf.p;
-                    auto to_local = [&](V3 w) { return V3{dot(tg, w), dot(bt, w), dot(nrm, w)}; };
-                    V3 wo_local = to_local(sf.wo);
-                    ShadingData sd = shading_data(s, sf.material);
-                    uint32_t bsdf_type = bsdf_type_of(sd);
-                    Bsdf bsdf = Bsdf::setup(sd);
-                    if (c.nee && (bsdf_type & BSDF_SMOOTH) && s.n_lights > 0) {
-                        float ul = rng.get1d();
-                        uint32_t lid = (uint32_t)(ul * (float)s.n_lights);
-                        float sel_pdf = 1.f / (float)s.n_lights;
-                        float u0 = rng.get1d(), u1 = rng.get1d();
-                        LightSample ls = sample_li(s, s.lights[lid], u0, u1, p);
-                        V3 to = offset_ray_origin(ls.p, ls.n, p - ls.p);
-                        V3 po = offset_ray_origin(p, nrm, to - p);
-                        V3 d = to - po;
-                        V3 wi_world = normalize(d);
-                        V3 wi_local = to_local(wi_world);
-                        float light_pdf = sel_pdf * ls.pdf;
-                        V3 fv = bsdf.f(wo_local, wi_local);
-                        float bsdf_pdf = bsdf.pdf(wo_local, wi_local);
-                        if (light_pdf > 0 && any(fv)) {
-                            V3 Ld = ls.L * sthp * fv * fabsf(wi_local.z);
-                            if (any(Ld)) {
-                                // traceShadow + resolve
-                                float4 sh = traverse_ray<true, FMT>(nodes, tris, po, d, 0.f, 1.f, trace_err);
-                                if (ubits(sh.w) == KRR_MISS) {
-                                    V3 add = Ld / mean(pu * light_pdf + pu * bsdf_pdf);
-                                    L = add + L;
-                                }
-                            }
-                        }
-                    }
-                    BsdfSample bs = bsdf.sample(wo_local, [&]() { return rng.get1d(); });
-                    if (bs.pdf != 0 && any(bs.f)) {
-                        V3 wi_world = tg * bs.wi.x + bt * bs.wi.y + nrm * bs.wi.z;
-                        V3 nthp = sthp * bs.f * fabsf(bs.wi.z) / bs.pdf;
-                        if (any(nthp)) {
-                            ro = offset_ray_origin(p, nrm, wi_world);
-                            medium = medium_towards(mi, mo, medium, nrm, wi_world);
-                            rd = wi_world;
-                            ctx_p = p;
-                            ctx_n = nrm;
-                            flags = bs.flags;
-                            thp = nthp;
-                            depth = depth + 1;
-                            pl = pu / bs.pdf;
-                            next = true;
-                        }
-                    }
-                }
-                if (!next) break;
+                p.hit = traverse_ray<false, FMT>(nodes, tris, p.ro, p.rd, 0.f, INFINITY, trace_err);
+                if (!mk_bounce<FMT>(s, c, nodes, tris, p, rng, iter, lsel_pdf, trace_err)) break;
             }
-            (void)ctx_n;
-            (void)time;
-            acc = V3{acc.x + L.x, acc.y + L.y, acc.z + L.z};
-            if (independent && sample + 1 < c.spp) L = v3(0.f);
+            p.acc = V3{p.acc.x + p.L.x, p.acc.y + p.L.y, p.acc.z + p.L.z};
+            if (independent && sample + 1 < c.spp) p.L = v3(0.f);
         }
-        store_rng(ps, pixel, rng);
-        ps.L[g] = make_float4(L.x, L.y, L.z, l0.w);
-        ps.pixel[g] = make_float4(acc.x, acc.y, acc.z, 0.f);
-        V3 col = acc / (float)c.spp;
-        if (c.enable_clamp) col = vmin(vmax(col, v3(0.f)), v3(c.clamp_max));
-        const int64_t x = i % v.w, y = i / v.w;
-        out[v.offset + (v.h - 1 - y) * (int64_t)v.w + x] = f4(col, 1.f);
+        store_rng(ps, (uint32_t)g, rng);
+        ps.L[g] = make_float4(p.L.x, p.L.y, p.L.z, l0.w);
+        ps.pixel[g] = make_float4(p.acc.x, p.acc.y, p.acc.z, 0.f);
+        mk_finish_pixel(p, v, i, c, out);
+    }
+}
+
+// The megakernel with a coherence step in the manner of the reference's
+// optixReorder(hit, 1) (src/render/megakernel/device.cu:173-176): the 128
+// paths of a block advance one bounce at a time; after each closest hit the
+// paths move between the block's threads (through shared memory) so that
+// paths that missed, paths on each material class and finished paths are
+// contiguous, and each warp shades paths of one class.  A path's arithmetic
+// is unchanged, so the frame equals the unsorted megakernel's and the
+// wavefront's bit for bit.
+constexpr int kMkThreads = 128;
+
+__device__ __forceinline__ int mk_class(const DevScene &s, const MkPath &p) {
+    if (!p.alive) return 4;
+    const uint32_t gid = ubits(p.hit.w);
+    if (gid == KRR_MISS) return 0;
+    const DevInstance &I = s.instances[s.tri_instance[gid]];
+    const int32_t m = s.meshes[I.mesh].material;
+    return m < 0 ? 0 : min(max(s.materials[m].type, 0), 3);
+}
+
+template <int FMT>
+__global__ void __launch_bounds__(kMkThreads)
+k_megakernel_sorted(DevScene s, const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
+                    const DevView *__restrict__ views, const FrameConst *__restrict__ fc, PixelState ps,
+                    WfConst c, int independent, int64_t n, float4 *__restrict__ out, uint32_t *err,
+                    int *trace_err) {
+    __shared__ MkPath sh[kMkThreads];
+    __shared__ int counts[5];
+    const int nv = fc->n_views;
+    const float lsel_pdf = 1.f / (float)s.n_lights;
+    const int tid = threadIdx.x;
+    for (int64_t base = blockIdx.x * (int64_t)kMkThreads; base < n; base += (int64_t)gridDim.x * kMkThreads) {
+        const int64_t g0 = base + tid;
+        for (int sample = 0; sample < c.spp; ++sample) {
+            MkPath p;
+            if (g0 < n) {
+                const DevView &v = views[view_of(views, nv, g0)];
+                Pcg rng = load_rng(ps, (uint32_t)g0);
+                const float4 l0 = ps.L[g0], p0 = ps.pixel[g0];
+                p.L = f3(l0);
+                p.acc = f3(p0);
+                p.pixel = (uint32_t)g0;
+                mk_camera(p, rng, v, g0 - v.offset);
+                p.rng = make_ulonglong2(rng.state, rng.inc);
+            } else {
+                p.alive = 0u;
+                p.pixel = 0xFFFFFFFFu;
+            }
+            for (int iter = 0;; ++iter) {
+                if (!__syncthreads_or(p.alive)) break;
+                if (p.alive) p.hit = traverse_ray<false, FMT>(nodes, tris, p.ro, p.rd, 0.f, INFINITY, trace_err);
+                // reorder: counting sort of the block's paths by class
+                const int cls = mk_class(s, p);
+                if (tid < 5) counts[tid] = 0;
+                __syncthreads();
+                const int rank = atomicAdd(&counts[cls], 1);
+                __syncthreads();
+                int off = 0;
+                for (int k = 0; k < cls; ++k) off += counts[k];
+                sh[off + rank] = p;
+                __syncthreads();
+                p = sh[tid];
+                __syncthreads();
+                if (p.alive) {
+                    Pcg rng{p.rng.x, p.rng.y};
+                    const bool next = mk_bounce<FMT>(s, c, nodes, tris, p, rng, iter, lsel_pdf, trace_err);
+                    p.rng = make_ulonglong2(rng.state, rng.inc);
+                    if (!next) {
+                        // the path's sample ends: its pixel's sums and sampler
+                        p.acc = V3{p.acc.x + p.L.x, p.acc.y + p.L.y, p.acc.z + p.L.z};
+                        if (independent && sample + 1 < c.spp) p.L = v3(0.f);
+                        ps.rng[p.pixel] = p.rng;
+                        ps.L[p.pixel] = make_float4(p.L.x, p.L.y, p.L.z, ps.L[p.pixel].w);
+                        ps.pixel[p.pixel] = make_float4(p.acc.x, p.acc.y, p.acc.z, 0.f);
+                        p.alive = 0u;
+                    }
+                }
+            }
+            __syncthreads();   // every path of the block has stored its pixel
+        }
+        if (g0 < n) {
+            const DevView &v = views[view_of(views, nv, g0)];
+            const float4 a = ps.pixel[g0];
+            MkPath q;
+            q.acc = f3(a);
+            mk_finish_pixel(q, v, g0 - v.offset, c, out);
+        }
+        __syncthreads();
     }
 }
 
@@ -2341,8 +2461,13 @@ static int nrc_evaluate_queries(krr_wf *wf, cudaStream_t st) {
 // (render() then skips handleHit/handleMiss).
 static int closest_stage(krr_wf *wf, int depth, cudaStream_t st, bool traced,
                          bool in_render = false) {
+    // In render() the radiance of misses and emissive hits of rays outside
+    // every medium is added here; rays inside a medium go to the medium
+    // stage, which queues theirs for handleHit/handleMiss.  A path has one
+    // item per bounce, so each pixel's sum gets the same terms in the same
+    // order either way.
     const bool defer_cache = in_render;
-    const int inline_lights = in_render && !wf->medium ? 1 : 0;
+    const int inline_lights = in_render ? 1 : 0;
     int cur = depth & 1;
     Queue rq = wf->q(cur);
     if (!traced) KRR_TRY(launch_trace_closest(&wf->accel, closest_launch(wf, depth), st));
@@ -2606,6 +2731,12 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
     return KRR_OK;
 }
 
+extern "C" int krr_wf_set_megakernel_reorder(krr_wf *wf, int32_t reorder) {
+    KRR_CHECK_ARG(wf && (reorder == 0 || reorder == 1), "reorder must be 0 or 1");
+    wf->mk_reorder = reorder;
+    return KRR_OK;
+}
+
 extern "C" int krr_wf_render_megakernel(krr_wf *wf, float *d_out, void *stream) {
     KRR_TRY(ready(wf));
     KRR_CHECK_ARG(d_out != nullptr, "output is NULL");
@@ -2614,28 +2745,32 @@ extern "C" int krr_wf_render_megakernel(krr_wf *wf, float *d_out, void *stream) 
     KRR_CHECK_ARG(wf->levels == 1, "the megakernel pass traces the flattened structure");
     KRR_CHECK_ARG(!wf->nrc, "the megakernel pass has no cache hooks; detach the cache first");
     cudaStream_t st = as_stream(stream);
-    static int grid[2] = {0, 0};
-    const int fmt = wf->accel.node_format;
-    if (!grid[fmt]) {
+    static int grid[2][2] = {{0, 0}, {0, 0}};
+    const int fmt = wf->accel.node_format, sorted = wf->mk_reorder;
+    if (!grid[sorted][fmt]) {
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (fmt == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_megakernel<1>, 128, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_megakernel<0>, 128, 0);
-        grid[fmt] = std::max(1, sms) * std::max(1, per_sm);
+        const void *fn = sorted ? (fmt == 1 ? (const void *)k_megakernel_sorted<1> : (const void *)k_megakernel_sorted<0>)
+                                : (fmt == 1 ? (const void *)k_megakernel<1> : (const void *)k_megakernel<0>);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 128, 0);
+        grid[sorted][fmt] = std::max(1, sms) * std::max(1, per_sm);
     }
-    const int blocks = (int)std::min<int64_t>(grid[fmt], (wf->n + 127) / 128);
+    const int blocks = (int)std::min<int64_t>(grid[sorted][fmt], (wf->n + 127) / 128);
     WfConst c = wf->consts();
-    if (fmt == 1)
-        k_megakernel<1><<<blocks, 128, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, wf->d_views,
-                                                 wf->d_frame, wf->ps, c, wf->params.independent_samples,
-                                                 wf->n, reinterpret_cast<float4 *>(d_out), wf->err(),
-                                                 wf->accel.d_scratch + 4);
-    else
-        k_megakernel<0><<<blocks, 128, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, wf->d_views,
-                                                 wf->d_frame, wf->ps, c, wf->params.independent_samples,
-                                                 wf->n, reinterpret_cast<float4 *>(d_out), wf->err(),
-                                                 wf->accel.d_scratch + 4);
+    float4 *out = reinterpret_cast<float4 *>(d_out);
+    int *terr = wf->accel.d_scratch + 4;
+    const int ind = wf->params.independent_samples;
+#define KRR_MK_LAUNCH(K) K<<<blocks, 128, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, wf->d_views, \
+                                                   wf->d_frame, wf->ps, c, ind, wf->n, out, wf->err(), terr)
+    if (sorted) {
+        if (fmt == 1) KRR_MK_LAUNCH(k_megakernel_sorted<1>);
+        else KRR_MK_LAUNCH(k_megakernel_sorted<0>);
+    } else {
+        if (fmt == 1) KRR_MK_LAUNCH(k_megakernel<1>);
+        else KRR_MK_LAUNCH(k_megakernel<0>);
+    }
+#undef KRR_MK_LAUNCH
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }

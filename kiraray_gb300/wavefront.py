@@ -164,6 +164,12 @@ class WavefrontPathTracer:
               "krr_wf_autotune")
         return {k: getattr(t, k) for k, _ in t._fields_ if k != "reserved"}
 
+    def set_megakernel_reorder(self, reorder: bool) -> None:
+        """Megakernel variant: regroup a block's paths by hit class after
+        each closest hit (default) or keep one path per thread."""
+        check(self.lib.krr_wf_set_megakernel_reorder(self._h, int(bool(reorder))),
+              "krr_wf_set_megakernel_reorder")
+
     def set_accel_levels(self, levels: int) -> None:
         """1: flattened instances (default), 2: two-level structure."""
         check(self.lib.krr_wf_set_accel_levels(self._h, levels), "krr_wf_set_accel_levels")

@@ -209,12 +209,16 @@ def test_resize_and_rescene(krr_lib, cuda):
     assert torch.isfinite(pt.render()).all()
 
 
+@pytest.mark.parametrize("reorder", [1, 0])
 @pytest.mark.parametrize("params,spp", [({"max_depth": 5}, 1), ({"max_depth": 3, "nee": False}, 1),
                                         ({"max_depth": 4, "enable_clamp": True, "clamp_max": 1.5}, 2),
                                         ({"max_depth": 4, "independent_samples": 1}, 3)])
-def test_megakernel_equals_wavefront_cornell(krr_lib, cuda, params, spp):
+def test_megakernel_equals_wavefront_cornell(krr_lib, cuda, params, spp, reorder):
+    """The megakernel, with and without regrouping paths by hit class after
+    each closest hit, equals the wavefront bit for bit."""
     sc = scenes.cornell_box(64, 48, max_depth=params["max_depth"])
     pt = WavefrontPathTracer(params, spp=spp, seed=9)
+    pt.set_megakernel_reorder(reorder)
     pt.set_scene(sc)
     pt.resize(64, 48)
     pt.begin_frame(4, sc.camera)
@@ -228,11 +232,14 @@ def test_megakernel_equals_wavefront_cornell(krr_lib, cuda, params, spp):
     assert pt.device_errors() == 0
 
 
-def test_megakernel_equals_wavefront_large_scene_views(krr_lib, cuda):
-    """Conductors, dielectrics, the environment and two batched views."""
+@pytest.mark.parametrize("reorder", [1, 0])
+def test_megakernel_equals_wavefront_large_scene_views(krr_lib, cuda, reorder):
+    """Conductors, dielectrics, the environment and two batched views (view
+    sizes not multiples of the 128-path blocks)."""
     sc = scenes.large_scene(width=96, height=64, grid=256, n_spheres=40, sky_size=(64, 32))
     views = [(sc.camera, 96, 64, 3), (sc.camera, 40, 30, 1 << 24)]
     pt = WavefrontPathTracer({"max_depth": 8})
+    pt.set_megakernel_reorder(reorder)
     pt.set_scene(sc)
     pt.resize_views(views)
     pt.begin_frame_views(2)
