@@ -419,6 +419,20 @@ def config_frames(args):
             if f > 3:
                 ms.append(e0.elapsed_time(e1))
         gpu_ms = sorted(ms)[len(ms) // 2]
+        queue_order_ms = None
+        if sc.media:   # the tracking kernels in queue order, for comparison
+            pt.set_media_order(0)
+            qo = []
+            for f in range(9, 14):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                pt.begin_frame(f, sc.camera)
+                e0.record(s)
+                pt.render(img)
+                e1.record(s)
+                e1.synchronize()
+                qo.append(e0.elapsed_time(e1))
+            queue_order_ms = round(sorted(qo)[len(qo) // 2], 3)
+            pt.set_media_order(1)
         n = sc.width * sc.height
         band = n // frac
         lo = (n - band) // 2 // sc.width * sc.width
@@ -430,6 +444,8 @@ def config_frames(args):
                      "cpu_frame_ms_est": round(cpu_ms, 1), "cpu_cores": os.cpu_count() or 1,
                      "cpu_sample": f"rows {lo // sc.width}..{(lo + band) // sc.width} (1/{frac} of the pixels)",
                      "device_errors": pt.device_errors()}
+        if queue_order_ms is not None:
+            out[name]["gpu_frame_ms_tracking_in_queue_order"] = queue_order_ms
     return out
 
 
@@ -632,9 +648,12 @@ def time_to_relmse(args):
         return time_to_error_views(pt, sc, ref, copies, target=0.01, max_frames=max_frames,
                                    check_every=8, max_seconds=args.nrc_max_seconds)
 
-    # the cache as specified (Adam lr 1e-2, 65,536 training records per frame,
-    # spread threshold 0.01), then with the settings a sweep on this scene chose
+    # the cache as specified (Adam lr 1e-2, 65,536 training records per frame)
+    # with its two query rules: the path-spread rule (spread threshold 0.01,
+    # the default) and the vertex after the first diffuse bounce (threshold
+    # 0); then with the settings a sweep on this scene chose
     res_nrc = nrc_run()
+    res_first = nrc_run(termination_spread=0.0)
     res_tuned = nrc_run(**NRC_TUNED)
 
     def extrapolated(res):
@@ -658,6 +677,12 @@ def time_to_relmse(args):
     if res_nrc["seconds"]:
         out["nrc_time_fraction"] = res_nrc["seconds"] / (res_plain["seconds"] or
                                                          extrapolated(res_plain))
+    out["query_rule"] = "path spread a > 0.01 a0 (Mueller et al. 2021)"
+    out["nrc_first_diffuse_vertex"] = {
+        "config": {"termination_spread": 0.0}, "seconds": res_first["seconds"], "spp": res_first["spp"],
+        "ms_per_frame": round(res_first["ms_per_frame"], 3), "final_relmse": res_first["final_error"],
+        "time_fraction": (res_first["seconds"] / (res_plain["seconds"] or extrapolated(res_plain))
+                          if res_first["seconds"] else None)}
     out["nrc_tuned"] = {"config": NRC_TUNED, "seconds": res_tuned["seconds"], "spp": res_tuned["spp"],
                         "ms_per_frame": round(res_tuned["ms_per_frame"], 3),
                         "final_relmse": res_tuned["final_error"]}

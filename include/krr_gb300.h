@@ -401,6 +401,12 @@ int krr_wf_render_megakernel(krr_wf *wf, float *d_out_rgba, void *stream);
  * optixReorder(hit, 1) (src/render/megakernel/device.cu:173-176).  0: one
  * path per thread from start to end.  Frames are the same either way. */
 int krr_wf_set_megakernel_reorder(krr_wf *wf, int32_t reorder);
+/* Order of the medium tracking launches (default 1): their items are taken
+ * class by class of estimated optical depth (the ray's length inside the
+ * media's boxes times the largest sigma_t), so that a warp's rays take
+ * similar numbers of null collisions; 0 = queue order.  Frames are the same
+ * either way. */
+int krr_wf_set_media_order(krr_wf *wf, int32_t order);
 
 /* Batched views: many cameras of different sizes in one wavefront (one
  * launch per stage per bounce).  krr_wf_resize_views replaces resize; each

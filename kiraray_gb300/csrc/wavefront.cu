@@ -91,6 +91,8 @@ struct krr_wf {
     std::vector<int32_t> part_own_depth;   // -1: the pass's max_depth
     int32_t levels = 1;                    // 1: flattened instances, 2: two-level structure
     int32_t mk_reorder = 1;                // megakernel: reorder paths by hit class per bounce
+    int32_t media_order = 1;               // tracking kernels take their items by work class
+    int32_t *work_counts = nullptr;        // [32] work-class counts and cursors
     std::vector<DevMesh> h_mesh;           // host copies of the device meshes
     std::vector<int64_t> h_mesh_tris;      // triangles per mesh
     int32_t n_parts = 1;
@@ -910,14 +912,89 @@ __global__ void k_shadow_resolve(Queue shadow, const uint8_t *__restrict__ occlu
     }
 }
 
+// ------------------------------------------------------ media work order
+// The tracking kernels loop over null collisions, whose number grows with
+// the optical depth a ray crosses; in queue order the lanes of a warp hold
+// rays of very different depths and wait for the longest.  Before each
+// tracking launch the items are counted into kWorkClasses classes of
+// estimated optical depth (log2 of 1 + the length of the ray inside the
+// media's boxes times the largest density-scaled sigma_t) and an index
+// permutation lists them class by class, so that warps hold rays of similar
+// work.  Each item is computed as before; only the order changes.
+constexpr int kWorkClasses = 16;
+
+__device__ __forceinline__ float box_overlap(const DevMedium &m, V3 o, V3 d, float tmax) {
+    float t0 = 0.f, t1 = tmax;
+    for (int a = 0; a < 3; ++a) {
+        const float oa = get(o, a), da = get(d, a);
+        if (fabsf(da) < 1e-20f) {
+            if (oa < m.lo[a] || oa > m.hi[a]) return 0.f;
+            continue;
+        }
+        float ta = (m.lo[a] - oa) / da, tb = (m.hi[a] - oa) / da;
+        if (ta > tb) { float q = ta; ta = tb; tb = q; }
+        t0 = fmaxf(t0, ta);
+        t1 = fminf(t1, tb);
+    }
+    return t1 > t0 ? (t1 - t0) * length(d) : 0.f;
+}
+
+__device__ __forceinline__ int work_class(const DevScene &s, V3 o, V3 d, float tmax) {
+    float tau = 0.f;
+    for (int k = 0; k < s.n_media; ++k) {
+        const DevMedium &m = s.media[k];
+        const float sig = fmaxf(m.sigma_t[0], fmaxf(m.sigma_t[1], m.sigma_t[2])) * (m.density ? m.scale : 1.f);
+        tau += box_overlap(m, o, d, isinf(tmax) ? 3.402823466e38f : tmax) * sig;
+    }
+    return min(kWorkClasses - 1, (int)log2f(1.f + fminf(tau, 1e30f)));
+}
+
+// counts[0..16): items per class; classes[i]: item i's class.  ITEMS 0: a
+// medium-sample queue (plane 0 origin, 1 direction, 7 hit with t), 1: a
+// tracked shadow queue (plane 0 origin, 1 direction | tmax).
+template <int ITEMS>
+__global__ void k_work_classes(DevScene s, Queue q, uint8_t *__restrict__ classes, int32_t *counts) {
+    const int n = min(*q.count, q.cap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 c0 = q.at(0, i), c1 = q.at(1, i);
+        const float tmax = ITEMS == 0 ? q.at(7, i).x : c1.w;
+        const int k = work_class(s, f3(c0), f3(c1), tmax);
+        classes[i] = (uint8_t)k;
+        const unsigned peers = __match_any_sync(__activemask(), k);
+        if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(counts + k, __popc(peers));
+    }
+}
+
+// order: the item indices class by class (counts[16..32) are the cursors).
+__global__ void k_work_order(Queue q, const uint8_t *__restrict__ classes, int32_t *counts,
+                             int32_t *__restrict__ order) {
+    __shared__ int32_t start[kWorkClasses];
+    if (threadIdx.x == 0) {
+        int32_t acc = 0;
+        for (int k = 0; k < kWorkClasses; ++k) { start[k] = acc; acc += counts[k]; }
+    }
+    __syncthreads();
+    const int n = min(*q.count, q.cap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int k = classes[i];
+        const unsigned peers = __match_any_sync(__activemask(), k);
+        const int leader = __ffs(peers) - 1;
+        int base = 0;
+        if ((threadIdx.x & 31) == leader) base = atomicAdd(counts + kWorkClasses + k, __popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        order[start[k] + base + __popc(peers & ((1u << (threadIdx.x & 31)) - 1u))] = i;
+    }
+}
+
 // sampleMediumInteraction, medium.cpp:13-103 (the medium has no emission).
 // Three blocks of 256 per SM (at most 80 registers): the tracking loops are
 // latency-bound, and the extra warps outweigh a few spilled registers.
 __global__ void __launch_bounds__(kThreads, 3)
 k_medium_sample(DevScene s, Queue msq, Queue next, Queue miss, Queue hitl, Queue scat,
-                Queue mscat, PixelState ps, int max_depth, uint32_t *err) {
+                Queue mscat, PixelState ps, const int32_t *__restrict__ order, uint32_t *err) {
     int n = min(*msq.count, msq.cap);   // an overflowed queue holds cap items
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int ii = blockIdx.x * blockDim.x + threadIdx.x; ii < n; ii += gridDim.x * blockDim.x) {
+        const int i = order ? order[ii] : ii;
         float4 c0 = msq.at(0, i), c1 = msq.at(1, i), c2 = msq.at(2, i), c3 = msq.at(3, i);
         float4 c4 = msq.at(4, i), c5 = msq.at(5, i), c6 = msq.at(6, i), h = msq.at(7, i);
         V3 o = f3(c0), dir = f3(c1);
@@ -1112,9 +1189,11 @@ __device__ __forceinline__ float4 shadow_trace(const InstancedView &iv, const fl
 template <int FMT>
 __global__ void __launch_bounds__(kThreads, 3)
 k_shadow_tr(DevScene s, const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
-            InstancedView iv, Queue shadow, PixelState ps, uint32_t *err, int *trace_err) {
+            InstancedView iv, Queue shadow, PixelState ps, const int32_t *__restrict__ order,
+            uint32_t *err, int *trace_err) {
     int n = min(*shadow.count, shadow.cap);   // an overflowed queue holds cap items
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int ii = blockIdx.x * blockDim.x + threadIdx.x; ii < n; ii += gridDim.x * blockDim.x) {
+        const int i = order ? order[ii] : ii;
         float4 c0 = shadow.at(0, i), c1 = shadow.at(1, i), c2 = shadow.at(2, i), c3 = shadow.at(3, i),
                c4 = shadow.at(4, i);
         V3 o = f3(c0), d = f3(c1);
@@ -1640,6 +1719,7 @@ void free_queues(krr_wf *wf) {
     cudaFree(wf->hits); wf->hits = nullptr;
     cudaFree(wf->occluded); wf->occluded = nullptr;
     cudaFree(wf->scatter_lists); wf->scatter_lists = nullptr;
+    cudaFree(wf->work_counts); wf->work_counts = nullptr;
     cudaFree(wf->ps.L); cudaFree(wf->ps.pixel); cudaFree(wf->ps.rng);
     wf->ps = PixelState{};
     cudaFree(wf->d_pixel_part); wf->d_pixel_part = nullptr;
@@ -2227,6 +2307,7 @@ static int set_layout(krr_wf *wf, std::vector<DevView> layout) {
     KRR_CUDA(cudaMalloc(&wf->hits, wf->qcap * sizeof(float4)));
     KRR_CUDA(cudaMalloc(&wf->occluded, wf->qcap));
     KRR_CUDA(cudaMalloc(&wf->scatter_lists, 2 * wf->qcap * sizeof(int32_t)));
+    KRR_CUDA(cudaMalloc(&wf->work_counts, 2 * kWorkClasses * sizeof(int32_t)));
     KRR_CUDA(cudaMalloc(&wf->ps.L, wf->n * sizeof(float4)));
     KRR_CUDA(cudaMalloc(&wf->ps.pixel, wf->n * sizeof(float4)));
     KRR_CUDA(cudaMalloc(&wf->ps.rng, wf->n * sizeof(ulonglong2)));
@@ -2731,6 +2812,12 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
     return KRR_OK;
 }
 
+extern "C" int krr_wf_set_media_order(krr_wf *wf, int32_t order) {
+    KRR_CHECK_ARG(wf && (order == 0 || order == 1), "order must be 0 or 1");
+    wf->media_order = order;
+    return KRR_OK;
+}
+
 extern "C" int krr_wf_set_megakernel_reorder(krr_wf *wf, int32_t reorder) {
     KRR_CHECK_ARG(wf && (reorder == 0 || reorder == 1), "reorder must be 0 or 1");
     wf->mk_reorder = reorder;
@@ -3015,12 +3102,29 @@ extern "C" int krr_wf_group_launch(krr_wf_group *g, int64_t frame_index, void *s
 }
 
 namespace krr {
+// The permutation of a tracking queue's items by work class (media work
+// order, above), in the scatter-list buffer (free during the media stages).
+static int work_order(krr_wf *wf, const Queue &q, int items, cudaStream_t st, const int32_t **order) {
+    *order = nullptr;
+    if (!wf->media_order) return KRR_OK;
+    uint8_t *classes = reinterpret_cast<uint8_t *>(wf->scatter_lists + wf->qcap);
+    int32_t *counts = wf->work_counts;
+    KRR_CUDA(cudaMemsetAsync(counts, 0, 2 * kWorkClasses * sizeof(int32_t), st));
+    if (items == 0) k_work_classes<0><<<wf->grid, wf->block, 0, st>>>(wf->scene, q, classes, counts);
+    else k_work_classes<1><<<wf->grid, wf->block, 0, st>>>(wf->scene, q, classes, counts);
+    k_work_order<<<wf->grid, wf->block, 0, st>>>(q, classes, counts, wf->scatter_lists);
+    KRR_CUDA(cudaGetLastError());
+    *order = wf->scatter_lists;
+    return KRR_OK;
+}
+
 int launch_medium_sample(krr_wf *wf, int depth, cudaStream_t st) {
+    const int32_t *order = nullptr;
+    KRR_TRY(work_order(wf, wf->q(Q_MEDIUM_SAMPLE), 0, st, &order));
     k_medium_sample<<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->q(Q_MEDIUM_SAMPLE),
                                                     wf->q((depth & 1) ^ 1), wf->q(Q_MISS),
                                                     wf->q(Q_HIT_LIGHT), wf->q(Q_SCATTER),
-                                                    wf->q(Q_MEDIUM_SCATTER), wf->ps,
-                                                    wf->params.max_depth, wf->err());
+                                                    wf->q(Q_MEDIUM_SCATTER), wf->ps, order, wf->err());
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }
@@ -3041,17 +3145,20 @@ int launch_trace_shadow_tr(krr_wf *wf, cudaStream_t st) {
     KRR_CUDA(cudaMemsetAsync(tracked.count, 0, sizeof(int32_t), st));
     int *terr = wf->accel.d_scratch + 4;
     const InstancedView iv = wf->accel.levels == 2 ? instanced_view(&wf->accel) : InstancedView{};
-    if (wf->accel.node_format == 1) {
+    const int32_t *order = nullptr;
+    if (wf->accel.node_format == 1)
         k_shadow_split<1><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
                                                           wf->q(Q_SHADOW), tracked, wf->ps, wf->err(), terr);
-        k_shadow_tr<1><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
-                                                       tracked, wf->ps, wf->err(), terr);
-    } else {
+    else
         k_shadow_split<0><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
                                                           wf->q(Q_SHADOW), tracked, wf->ps, wf->err(), terr);
+    KRR_TRY(work_order(wf, tracked, 1, st, &order));
+    if (wf->accel.node_format == 1)
+        k_shadow_tr<1><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
+                                                       tracked, wf->ps, order, wf->err(), terr);
+    else
         k_shadow_tr<0><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
-                                                       tracked, wf->ps, wf->err(), terr);
-    }
+                                                       tracked, wf->ps, order, wf->err(), terr);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }

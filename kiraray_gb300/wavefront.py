@@ -170,6 +170,11 @@ class WavefrontPathTracer:
         check(self.lib.krr_wf_set_megakernel_reorder(self._h, int(bool(reorder))),
               "krr_wf_set_megakernel_reorder")
 
+    def set_media_order(self, order: bool) -> None:
+        """Medium tracking items taken by estimated optical depth (default)
+        or in queue order."""
+        check(self.lib.krr_wf_set_media_order(self._h, int(bool(order))), "krr_wf_set_media_order")
+
     def set_accel_levels(self, levels: int) -> None:
         """1: flattened instances (default), 2: two-level structure."""
         check(self.lib.krr_wf_set_accel_levels(self._h, levels), "krr_wf_set_accel_levels")

@@ -66,3 +66,19 @@ def test_loop_limits_raise_the_flag_and_end_the_walk(krr_lib, cuda):
     assert pt.device_errors() == 0
     oL, _ = O.PathTracer(sc).render({"max_depth": 8}, 1)
     compare(L[:, :3], oL, "volume frame after the limits are restored")
+
+
+def test_media_work_order_keeps_the_frame(krr_lib, cuda):
+    """Tracking items taken by estimated optical depth or in queue order:
+    the same frame bit for bit."""
+    sc = scenes.volume_box(80, 64, max_depth=10, grid=48)
+    imgs = []
+    for order in (1, 0):
+        pt = WavefrontPathTracer({"max_depth": 10})
+        pt.set_media_order(order)
+        pt.set_scene(sc)
+        pt.resize(sc.width, sc.height)
+        pt.begin_frame(3, sc.camera)
+        imgs.append(pt.render().cpu().numpy())
+        assert pt.device_errors() == 0
+    assert np.array_equal(imgs[0].view(np.uint32), imgs[1].view(np.uint32))
