@@ -419,9 +419,9 @@ def config_frames(args):
             if f > 3:
                 ms.append(e0.elapsed_time(e1))
         gpu_ms = sorted(ms)[len(ms) // 2]
-        queue_order_ms = None
-        if sc.media:   # the tracking kernels in queue order, for comparison
-            pt.set_media_order(0)
+        work_order_ms = None
+        if sc.media:   # the tracking kernels by work class, for comparison
+            pt.set_media_order(1)
             qo = []
             for f in range(9, 14):
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -431,8 +431,8 @@ def config_frames(args):
                 e1.record(s)
                 e1.synchronize()
                 qo.append(e0.elapsed_time(e1))
-            queue_order_ms = round(sorted(qo)[len(qo) // 2], 3)
-            pt.set_media_order(1)
+            work_order_ms = round(sorted(qo)[len(qo) // 2], 3)
+            pt.set_media_order(0)
         n = sc.width * sc.height
         band = n // frac
         lo = (n - band) // 2 // sc.width * sc.width
@@ -444,8 +444,8 @@ def config_frames(args):
                      "cpu_frame_ms_est": round(cpu_ms, 1), "cpu_cores": os.cpu_count() or 1,
                      "cpu_sample": f"rows {lo // sc.width}..{(lo + band) // sc.width} (1/{frac} of the pixels)",
                      "device_errors": pt.device_errors()}
-        if queue_order_ms is not None:
-            out[name]["gpu_frame_ms_tracking_in_queue_order"] = queue_order_ms
+        if work_order_ms is not None:
+            out[name]["gpu_frame_ms_tracking_by_work_class"] = work_order_ms
     return out
 
 

@@ -183,6 +183,15 @@ int krr_set_bvh_full_node_leaf(int32_t triangles);
  * is collapsed into the same 8-wide nodes; hits are the same with any
  * builder. */
 int krr_set_bvh_builder(int32_t builder);
+/* How the binary tree becomes 8-wide nodes in the BVHs built from now on,
+ * process-wide: 0 = greedy (a node opens its largest child until it has
+ * eight; default), 1 = cost-optimal (the cut of the binary tree into wide
+ * nodes of least surface-area cost, Ylitie, Karras and Laine 2017; with
+ * one-triangle leaves every triangle's test costs the same in any cut, so
+ * the cut of least total wide-node area; other leaf settings use the
+ * greedy collapse).  Replaces nothing in the reference (OptiX builds its
+ * own tree); hits are the same with either. */
+int krr_set_bvh_collapse(int32_t mode);
 
 /* Build from host arrays of world-space triangles: h_vertices float3[3*n]. */
 int krr_accel_create_from_triangles(const float *h_vertices, int64_t n_triangles,
@@ -267,10 +276,10 @@ int krr_accel_trace_stats(const krr_accel *accel, const krr_ray *d_rays, int64_t
  * KRR_NOALLOC_MAX_RAYS rays (about 1 MiB), resident on every GPU that loads
  * the library until exit; n must be 1..KRR_NOALLOC_MAX_RAYS or the call
  * returns KRR_ERR_INVALID_ARGUMENT.  The first call on each device looks up
- * the array's device address and keeps it for the life of the process (a
- * device reset after that first call is not supported).  The call is
- * synchronous (it waits for the stream and writes h_counts), so it cannot
- * be recorded by stream capture.  All calls share the array, so calls that
+ * the array's device address and keeps it for the life of the process:
+ * make that first call before any stream capture begins on the device, and
+ * do not reset the device after it.  The call is synchronous (it waits for
+ * the stream and writes h_counts).  All calls share the array, so calls that
  * overlap on the GPU race; counters are cleared at the start of each call.
  * Calls no cudaMalloc, cudaFree or other allocating routine.  Returns
  * KRR_ERR_OVERFLOW when the stack limit cut a ray off. */
@@ -401,11 +410,12 @@ int krr_wf_render_megakernel(krr_wf *wf, float *d_out_rgba, void *stream);
  * optixReorder(hit, 1) (src/render/megakernel/device.cu:173-176).  0: one
  * path per thread from start to end.  Frames are the same either way. */
 int krr_wf_set_megakernel_reorder(krr_wf *wf, int32_t reorder);
-/* Order of the medium tracking launches (default 1): their items are taken
- * class by class of estimated optical depth (the ray's length inside the
- * media's boxes times the largest sigma_t), so that a warp's rays take
- * similar numbers of null collisions; 0 = queue order.  Frames are the same
- * either way. */
+/* Order of the medium tracking launches (default 0, queue order): with 1
+ * their items are taken class by class of estimated optical depth (the
+ * ray's length inside the media's boxes times the largest sigma_t), so that
+ * a warp's rays take similar numbers of null collisions.  The ordering costs
+ * more than it saves on the 1024x1024 volume frame (11.1 against 10.1 ms),
+ * hence off by default.  Frames are the same either way. */
 int krr_wf_set_media_order(krr_wf *wf, int32_t order);
 
 /* Batched views: many cameras of different sizes in one wavefront (one

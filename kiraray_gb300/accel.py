@@ -37,6 +37,12 @@ def set_builder(builder: int) -> None:
     check(_lib.load().krr_set_bvh_builder(builder), "krr_set_bvh_builder")
 
 
+def set_collapse(mode: int) -> None:
+    """How the binary tree becomes 8-wide nodes in the BVHs built from now
+    on: 0 greedy (default), 1 cost-optimal (least total wide-node area)."""
+    check(_lib.load().krr_set_bvh_collapse(mode), "krr_set_bvh_collapse")
+
+
 def set_full_node_leaf(triangles: int) -> None:
     """Largest leaf (1..3 triangles) among the children of a full node."""
     check(_lib.load().krr_set_bvh_full_node_leaf(triangles), "krr_set_bvh_full_node_leaf")

@@ -240,9 +240,11 @@ __device__ __forceinline__ float half_area(V3 lo, V3 hi) {
 // ------------------------------------------------------------------ PLOC
 // Parallel locally-ordered clustering (Meister and Bittner, IEEE TVCG 2018):
 // the clusters stay in Morton order; each looks for the cluster within
-// `radius` positions whose merged box has the smallest surface area (ties to
-// the smaller position, so the globally closest pair is always mutual and
-// every round merges); mutual nearest neighbours merge into a new internal
+// `radius` positions whose merged box has the smallest surface area, ties to
+// the smallest i XOR j (the pair of least area and, among those, least XOR is
+// mutual, so every round merges; coincident boxes pair up as (2k, 2k + 1)
+// and give a balanced tree rather than a chain); mutual nearest neighbours
+// merge into a new internal
 // node at the smaller position, the other position drops out, and the
 // survivors are compacted in order.  Higher-quality trees than the radix
 // tree for the same Morton order.
@@ -280,9 +282,9 @@ k_ploc_nn(const Cluster *__restrict__ c, int n, int r, uint32_t *__restrict__ nn
         if (j == i) continue;
         const int k = j - base + r;
         const float a = half_area(vmin(lo, f3(slo[k])), vmax(hi, f3(shi[k])));
-        best = min(best, ((unsigned long long)__float_as_uint(a) << 32) | (uint32_t)j);
+        best = min(best, ((unsigned long long)__float_as_uint(a) << 32) | (uint32_t)(i ^ j));
     }
-    nn[i] = (uint32_t)best;
+    nn[i] = (uint32_t)i ^ (uint32_t)best;
 }
 
 __global__ void k_ploc_merge(const Cluster *__restrict__ c, const uint32_t *__restrict__ nn, int n,
@@ -392,10 +394,89 @@ __device__ void write_node_boxes(float4 *np, int format, const V3 *slo, const V3
                         __uint_as_float(qhi[2][0]), __uint_as_float(qhi[2][1]));
 }
 
+// ------------------------------------------------ cost-optimal collapse
+// The 8-wide tree that minimises the surface-area cost over all ways of
+// cutting the binary tree into wide nodes (Ylitie, Karras and Laine, "Efficient
+// incoherent ray traversal on GPUs through compressed wide BVHs", HPG 2017,
+// section 3.1), for one-triangle leaves.  With one triangle per leaf every
+// triangle is tested when its own box is hit, whatever the cut, so the cost
+// left to minimise is the wide nodes' visits: the sum of their areas.  For a
+// binary node n and i = 1..8, C(n, i) is the least total area of the wide
+// nodes when n's subtree is represented as at most i roots (wide nodes or
+// triangles) plus everything below them:
+//   triangle n:  C(n, i) = 0
+//   internal n:  D(n, i) = min over 1 <= k < i of C(left, k) + C(right, i - k)
+//                C(n, 1) = A(n) + D(n, 8)             (n becomes a wide node)
+//                C(n, i) = min(C(n, i - 1), D(n, i))  (i >= 2)
+// with A the half surface area.  A binary node's table needs only its
+// children's, so the tables are filled bottom-up in one pass; each node keeps
+// the split k of D(n, 8) (byte 0 of its choice word) and, for i = 2..8, the
+// split taken by C(n, i) or 0 where C(n, i) = C(n, i - 1) (byte i - 1).  The
+// collapse then reads a wide node's children off those choices.
+__global__ void k_parents(int ni, const uint32_t *__restrict__ left, const uint32_t *__restrict__ right,
+                          int *par_int, int *par_leaf) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ni) return;
+    for (uint32_t c : {left[i], right[i]}) {
+        if (c & kLeafBit) par_leaf[c & ~kLeafBit] = i;
+        else par_int[c] = i;
+    }
+}
+
+__device__ __forceinline__ void cost_table(const BinTree &t, uint32_t ref, const float4 *cost, float out[8]) {
+    if (ref & kLeafBit) {
+        for (int i = 0; i < 8; ++i) out[i] = 0.f;
+        return;
+    }
+    const float4 c0 = __ldcg(cost + 2 * (size_t)ref), c1 = __ldcg(cost + 2 * (size_t)ref + 1);
+    out[0] = c0.x; out[1] = c0.y; out[2] = c0.z; out[3] = c0.w;
+    out[4] = c1.x; out[5] = c1.y; out[6] = c1.z; out[7] = c1.w;
+}
+
+__global__ void k_collapse_cost(int n, BinTree t, const int *__restrict__ par_int,
+                                const int *__restrict__ par_leaf, float4 *cost, uint2 *choice, int *flags) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int node = par_leaf[i];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(flags + node, 1) == 0) return;
+        __threadfence();
+        float cl[8], cr[8], d[9], c[8];
+        int arg[9];
+        cost_table(t, t.left[node], cost, cl);
+        cost_table(t, t.right[node], cost, cr);
+        for (int w = 2; w <= 8; ++w) {
+            d[w] = INFINITY;
+            arg[w] = 1;
+            for (int k = 1; k < w; ++k) {
+                const float v = cl[k - 1] + cr[w - k - 1];
+                if (v < d[w]) { d[w] = v; arg[w] = k; }
+            }
+        }
+        c[0] = half_area(f3(t.int_lo[node]), f3(t.int_hi[node])) + d[8];
+        uint32_t word[2] = {(uint32_t)arg[8], 0u};
+        for (int w = 2; w <= 8; ++w) {
+            uint32_t k = 0;
+            if (d[w] < c[w - 2]) { c[w - 1] = d[w]; k = (uint32_t)arg[w]; }
+            else c[w - 1] = c[w - 2];
+            word[(w - 1) >> 2] |= k << (8 * ((w - 1) & 3));
+        }
+        __stcg(cost + 2 * (size_t)node, make_float4(c[0], c[1], c[2], c[3]));
+        __stcg(cost + 2 * (size_t)node + 1, make_float4(c[4], c[5], c[6], c[7]));
+        choice[node] = make_uint2(word[0], word[1]);
+        node = par_int[node];
+    }
+}
+
+__device__ __forceinline__ uint32_t choice_byte(uint2 w, int b) {
+    return ((b < 4 ? w.x : w.y) >> (8 * (b & 3))) & 0xffu;
+}
+
 __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const int *n_in,
                            CollapseItem *out, int *n_out, float4 *nodes, int *node_counter,
                            uint32_t *leaf_order, int *tri_counter, int *max_depth, int format,
-                           int max_leaf, int full_leaf) {
+                           int max_leaf, int full_leaf, const uint2 *__restrict__ choice) {
     int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= *n_in) return;
     CollapseItem item = in[w];
@@ -406,10 +487,38 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
     int nc = 1;
     ref[0] = item.bref;
     ref_info(t, ref[0], clo[0], chi[0], ccount[0]);
+    if (choice && !(item.bref & kLeafBit)) {
+        // cost-optimal children: D(n, 8) of the node, expanded through the
+        // children's choices (the i of the stacked entries sum to at most 8,
+        // so at most eight roots come out)
+        uint32_t st_ref[8];
+        int st_i[8], sp = 0;
+        const int k8 = min(max((int)choice_byte(choice[item.bref], 0), 1), 7);
+        st_ref[sp] = t.right[item.bref]; st_i[sp++] = 8 - k8;
+        st_ref[sp] = t.left[item.bref]; st_i[sp++] = k8;
+        nc = 0;
+        while (sp > 0) {
+            const uint32_t m = st_ref[--sp];
+            int i = st_i[sp];
+            int k = 0;
+            if (!(m & kLeafBit)) {
+                const uint2 cw = choice[m];
+                while (i > 1 && (k = (int)choice_byte(cw, i - 1)) == 0) --i;
+            }
+            if (k == 0 || k >= i || nc + sp >= 7) {
+                ref[nc] = m;
+                ref_info(t, m, clo[nc], chi[nc], ccount[nc]);
+                ++nc;
+            } else {
+                st_ref[sp] = t.right[m]; st_i[sp++] = i - k;
+                st_ref[sp] = t.left[m]; st_i[sp++] = k;
+            }
+        }
+    }
     // Greedily open the largest child that cannot be a leaf (more than three
     // triangles) or, once all can be leaves, the largest internal one while
     // slots remain.
-    while (nc < 8) {
+    while (!choice && nc < 8) {
         int best = -1;
         float best_area = -1.f;
         bool best_must = false;
@@ -441,13 +550,23 @@ __global__ void k_collapse(BinTree t, const CollapseItem *__restrict__ in, const
     for (int c = 1; c < nc; ++c) { lo = vmin(lo, clo[c]); hi = vmax(hi, chi[c]); }
 
     // Octant slot assignment: slot s gets the child nearest for direction
-    // octant s (greedy on dot(child centre - node centre, dir_s)).
+    // octant s (greedy on dot(child centre - node centre, dir_s)).  A node of
+    // at most four children that are all leaves takes slots 0-3 in child
+    // order instead: the order of its children does not matter (every hit
+    // triangle is tested), and with slots 4-7 empty the traversal skips
+    // their box tests.
     V3 pc = (lo + hi) * 0.5f;
     int slot_of[8];
     int child_in_slot[8];
     for (int s = 0; s < 8; ++s) child_in_slot[s] = -1;
     for (int c = 0; c < nc; ++c) slot_of[c] = -1;
-    for (int it = 0; it < nc; ++it) {
+    bool any_internal = false;
+    for (int c = 0; c < nc; ++c) any_internal |= internal[c];
+    const bool packed = !any_internal && nc <= 4;
+    if (packed) {
+        for (int c = 0; c < nc; ++c) { slot_of[c] = c; child_in_slot[c] = c; }
+    }
+    for (int it = 0; it < nc && !packed; ++it) {
         float best = INFINITY;
         int bc = -1, bs = -1;
         for (int c = 0; c < nc; ++c) {
@@ -959,6 +1078,10 @@ int accel_refit(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     return KRR_OK;
 }
 
+// krr_set_bvh_collapse: how the binary tree becomes 8-wide nodes (0 greedy,
+// 1 cost-optimal).
+static int g_collapse = 0;
+
 // PLOC rounds over the Morton-ordered leaves until one cluster is left (its
 // ref is the root).  Internal nodes are numbered in creation order.
 static int build_ploc(int n, const float4 *leaf_lo, const float4 *leaf_hi, uint32_t *left,
@@ -1074,6 +1197,25 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
         KRR_CUDA(cudaStreamSynchronize(s));   // the scratch above is freed on return
     }
 
+    BinTree bt{left.p, right.p, count.p, ilo.p, ihi.p, llo.p, lhi.p, sidx};
+    // cost tables of the cost-optimal collapse (one-triangle leaves only)
+    DevBuf<uint2> choice;
+    a->collapse = g_collapse == 1 && a->max_leaf == 1 && a->full_leaf == 1 && n > 1 ? 1 : 0;
+    if (a->collapse) {
+        DevBuf<int> par_int, par_leaf, flags;
+        DevBuf<float4> cost;
+        KRR_CUDA(par_int.alloc(ni)); KRR_CUDA(par_leaf.alloc(n)); KRR_CUDA(flags.alloc(ni));
+        KRR_CUDA(cost.alloc(2 * ni)); KRR_CUDA(choice.alloc(ni));
+        KRR_CUDA(cudaMemsetAsync(flags.p, 0, ni * sizeof(int), s));
+        KRR_CUDA(cudaMemsetAsync(par_int.p, 0xff, ni * sizeof(int), s));   // the root's parent: -1
+        k_parents<<<blocks_for(n - 1), kBuildThreads, 0, s>>>((int)(n - 1), left.p, right.p, par_int.p,
+                                                               par_leaf.p);
+        k_collapse_cost<<<blocks_for(n), kBuildThreads, 0, s>>>((int)n, bt, par_int.p, par_leaf.p, cost.p,
+                                                                 choice.p, flags.p);
+        KRR_CUDA(cudaGetLastError());
+        KRR_CUDA(cudaStreamSynchronize(s));   // the scratch above is freed on return
+    }
+
     // collapse, level by level
     int64_t max_nodes = std::max<int64_t>(n, 2);
     DevBuf<float4> nodes_tmp;
@@ -1086,33 +1228,45 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     KRR_CUDA(leaf_order.alloc(n));
     KRR_CUDA(qa.alloc(max_nodes)); KRR_CUDA(qb.alloc(max_nodes));
     KRR_CUDA(counters.alloc(8));
-    int hc[8] = {1, 0, 0, 1, 0, 0, 0, 0};
-    KRR_CUDA(cudaMemcpyAsync(counters.p, hc, sizeof(hc), cudaMemcpyHostToDevice, s));
-    CollapseItem root{root_ref, 0u, 1};
-    KRR_CUDA(cudaMemcpyAsync(qa.p, &root, sizeof(root), cudaMemcpyHostToDevice, s));
-    BinTree bt{left.p, right.p, count.p, ilo.p, ihi.p, llo.p, lhi.p, sidx};
-    int n_in = 1;
-    a->level_first.assign({0, 1});
-    CollapseItem *qin = qa.p, *qout = qb.p;
-    int *c_in = counters.p + 3, *c_out = counters.p + 4;
-    int levels = 0;
-    while (n_in > 0) {
-        KRR_CUDA(cudaMemsetAsync(c_out, 0, sizeof(int), s));
-        k_collapse<<<blocks_for(n_in, 128), 128, 0, s>>>(bt, qin, c_in, qout, c_out, nodes_tmp.p,
-                                                         counters.p, leaf_order.p, counters.p + 1,
-                                                         counters.p + 2, fmt, a->max_leaf, a->full_leaf);
-        KRR_CUDA(cudaGetLastError());
-        int allocated = 0;
-        KRR_CUDA(cudaMemcpyAsync(&n_in, c_out, sizeof(int), cudaMemcpyDeviceToHost, s));
-        KRR_CUDA(cudaMemcpyAsync(&allocated, counters.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-        KRR_CUDA(cudaMemcpyAsync(c_in, c_out, sizeof(int), cudaMemcpyDeviceToDevice, s));
+    int hc[8];
+    for (int attempt = 0;; ++attempt) {
+        const int init[8] = {1, 0, 0, 1, 0, 0, 0, 0};
+        std::memcpy(hc, init, sizeof(hc));
+        KRR_CUDA(cudaMemcpyAsync(counters.p, hc, sizeof(hc), cudaMemcpyHostToDevice, s));
+        CollapseItem root{root_ref, 0u, 1};
+        KRR_CUDA(cudaMemcpyAsync(qa.p, &root, sizeof(root), cudaMemcpyHostToDevice, s));
+        int n_in = 1;
+        a->level_first.assign({0, 1});
+        CollapseItem *qin = qa.p, *qout = qb.p;
+        int *c_in = counters.p + 3, *c_out = counters.p + 4;
+        int levels = 0;
+        while (n_in > 0) {
+            KRR_CUDA(cudaMemsetAsync(c_out, 0, sizeof(int), s));
+            k_collapse<<<blocks_for(n_in, 128), 128, 0, s>>>(bt, qin, c_in, qout, c_out, nodes_tmp.p,
+                                                             counters.p, leaf_order.p, counters.p + 1,
+                                                             counters.p + 2, fmt, a->max_leaf, a->full_leaf,
+                                                             a->collapse ? choice.p : nullptr);
+            KRR_CUDA(cudaGetLastError());
+            int allocated = 0;
+            KRR_CUDA(cudaMemcpyAsync(&n_in, c_out, sizeof(int), cudaMemcpyDeviceToHost, s));
+            KRR_CUDA(cudaMemcpyAsync(&allocated, counters.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+            KRR_CUDA(cudaMemcpyAsync(c_in, c_out, sizeof(int), cudaMemcpyDeviceToDevice, s));
+            KRR_CUDA(cudaStreamSynchronize(s));
+            if (n_in > 0) a->level_first.push_back(allocated);   // the next level's nodes end here
+            std::swap(qin, qout);
+            if (++levels > 4096) return fail(KRR_ERR_OVERFLOW, "BVH collapse did not terminate");
+        }
+        KRR_CUDA(cudaMemcpyAsync(hc, counters.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
         KRR_CUDA(cudaStreamSynchronize(s));
-        if (n_in > 0) a->level_first.push_back(allocated);   // the next level's nodes end here
-        std::swap(qin, qout);
-        if (++levels > 4096) return fail(KRR_ERR_OVERFLOW, "BVH collapse did not terminate");
+        // a cost-optimal tree deeper than the traversal stack (possible on
+        // degenerate input, where nodes of two children can chain) is
+        // replaced by the greedy collapse, whose nodes open three levels
+        if (a->collapse && hc[2] > kTraversalStack && attempt == 0) {
+            a->collapse = 0;
+            continue;
+        }
+        break;
     }
-    KRR_CUDA(cudaMemcpyAsync(hc, counters.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
-    KRR_CUDA(cudaStreamSynchronize(s));
     a->n_nodes = hc[0];
     a->max_depth = hc[2];
     if (hc[1] != n) return fail(KRR_ERR_OVERFLOW, "BVH collapse emitted %d of %lld triangles", hc[1], (long long)n);
@@ -1318,6 +1472,12 @@ extern "C" int krr_accel_refit_triangles(krr_accel *a, const float *h_vertices, 
 // more.
 static int g_builder = 2;
 int krr::default_builder() { return g_builder; }
+
+extern "C" int krr_set_bvh_collapse(int32_t mode) {
+    KRR_CHECK_ARG(mode == 0 || mode == 1, "collapse must be 0 (greedy) or 1 (cost-optimal)");
+    g_collapse = mode;
+    return KRR_OK;
+}
 
 extern "C" int krr_set_bvh_builder(int32_t builder) {
     KRR_CHECK_ARG(builder >= 0 && builder <= 2,

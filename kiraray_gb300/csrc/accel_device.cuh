@@ -130,20 +130,27 @@ __device__ __forceinline__ void visit_node(const float4 *__restrict__ nodes, uin
     const float tlimit = tmax + fabsf(tmax) * 5e-7f;
     const int tmin_i = __float_as_int(r.tmin), tlim_i = __float_as_int(tlimit);
     uint32_t hitmask = 0;
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        const int k = c & 3;
-        uint32_t m = __byte_perm(c < 4 ? meta0 : meta1, 0u, 0x4440u + (uint32_t)k);
-        int tnx = __float_as_int(fmaf(plane256(c < 4 ? nx0 : nx1, k), dx, nox));
-        int tny = __float_as_int(fmaf(plane256(c < 4 ? ny0 : ny1, k), dy, noy));
-        int tnz = __float_as_int(fmaf(plane256(c < 4 ? nz0 : nz1, k), dz, noz));
-        int tfx = __float_as_int(fmaf(plane256(c < 4 ? fx0 : fx1, k), dx, fox));
-        int tfy = __float_as_int(fmaf(plane256(c < 4 ? fy0 : fy1, k), dy, foy));
-        int tfz = __float_as_int(fmaf(plane256(c < 4 ? fz0 : fz1, k), dz, foz));
+    // children in slots 0-3, then 4-7 unless all four are empty (meta bytes
+    // 0: nodes of at most four leaf children keep their slots 4-7 empty)
+    auto test_child = [&](uint32_t meta, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t fx, uint32_t fy,
+                          uint32_t fz, int k) {
+        uint32_t m = __byte_perm(meta, 0u, 0x4440u + (uint32_t)k);
+        int tnx = __float_as_int(fmaf(plane256(nx, k), dx, nox));
+        int tny = __float_as_int(fmaf(plane256(ny, k), dy, noy));
+        int tnz = __float_as_int(fmaf(plane256(nz, k), dz, noz));
+        int tfx = __float_as_int(fmaf(plane256(fx, k), dx, fox));
+        int tfy = __float_as_int(fmaf(plane256(fy, k), dy, foy));
+        int tfz = __float_as_int(fmaf(plane256(fz, k), dz, foz));
         int t0 = __vimax3_s32(tnx, tny, max(tnz, tmin_i));
         int t1 = __vimin3_s32(tfx, tfy, min(tfz, tlim_i));
         uint32_t bits = SINGLE ? __funnelshift_l(0u, 1u, m) : (m >> 5) << (m & 31u);
         hitmask |= (t0 <= t1) ? bits : 0u;
+    };
+#pragma unroll
+    for (int k = 0; k < 4; ++k) test_child(meta0, nx0, ny0, nz0, fx0, fy0, fz0, k);
+    if (meta1 != 0u) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) test_child(meta1, nx1, ny1, nz1, fx1, fy1, fz1, k);
     }
     uint32_t cimask = ew >> 24;
     ng = make_uint2(__float_as_uint(q1.x), (hitmask >> 24) | (cimask << 8));

@@ -20,12 +20,12 @@
 // Set-up: host code cannot use the array's name as a device address (on the
 // host it names a stand-in object, not device memory), so the first call on
 // each device looks the address up with cudaGetSymbolAddress, with that
-// device current, and caches it for the life of the process: a device reset
-// (cudaDeviceReset) after that first call is not supported.
+// device current, and caches it for the life of the process: make that first
+// call before any stream capture begins on the device, and do not reset the
+// device (cudaDeviceReset) after it.
 //
 // The call is synchronous: it waits for the stream and copies the counts to
-// the caller's host array before it returns, so it cannot be recorded into
-// a CUDA graph by stream capture.  A traversal cut off by the stack limit
+// the caller's host array before it returns.  A traversal cut off by the stack limit
 // (krr_accel_set_stack_limit) makes it return KRR_ERR_OVERFLOW, as the
 // allocating entry point does.
 #include <mutex>

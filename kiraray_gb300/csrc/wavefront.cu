@@ -29,8 +29,10 @@ using namespace krr;
 namespace krr {
 int accel_set_mask(krr_accel *a, const uint8_t *d_mask, cudaStream_t s);
 int launch_medium_sample(krr_wf *wf, int depth, cudaStream_t s);
-int launch_medium_scatter(krr_wf *wf, int depth, cudaStream_t s);
+int launch_medium_scatter(krr_wf *wf, int depth, cudaStream_t s, bool to_tracker = false);
 int launch_trace_shadow_tr(krr_wf *wf, cudaStream_t s);
+int launch_shadow_tracker(krr_wf *wf, cudaStream_t s);
+bool split_shadows(const krr_wf *wf);
 }
 
 struct DevCamera {
@@ -91,7 +93,7 @@ struct krr_wf {
     std::vector<int32_t> part_own_depth;   // -1: the pass's max_depth
     int32_t levels = 1;                    // 1: flattened instances, 2: two-level structure
     int32_t mk_reorder = 1;                // megakernel: reorder paths by hit class per bounce
-    int32_t media_order = 1;               // tracking kernels take their items by work class
+    int32_t media_order = 0;               // 1: tracking kernels take their items by work class
     int32_t *work_counts = nullptr;        // [32] work-class counts and cursors
     std::vector<DevMesh> h_mesh;           // host copies of the device meshes
     std::vector<int64_t> h_mesh_tris;      // triangles per mesh
@@ -172,6 +174,8 @@ namespace {
 constexpr int kThreads = 256;
 
 // ---------------------------------------------------------------- pushes
+// Warp-aggregated push: every active lane of the warp must push to the same
+// queue (one atomic per warp).
 __device__ __forceinline__ int push_slot(int32_t *count, int cap, uint32_t *err) {
     unsigned m = __activemask();
     int lane = threadIdx.x & 31;
@@ -180,6 +184,24 @@ __device__ __forceinline__ int push_slot(int32_t *count, int cap, uint32_t *err)
     if (lane == leader) base = atomicAdd(count, __popc(m));
     base = __shfl_sync(m, base, leader);
     int slot = base + __popc(m & ((1u << lane) - 1u));
+    if (slot >= cap) {
+        atomicOr(err, (uint32_t)kErrQueueOverflow);
+        return -1;
+    }
+    return slot;
+}
+
+// push_slot for a push whose queue differs between the lanes of a warp: the
+// lanes are grouped by counter and each group takes its slots together.
+__device__ __forceinline__ int push_slot_grouped(int32_t *count, int cap, uint32_t *err) {
+    const unsigned m = __activemask();
+    const unsigned peers = __match_any_sync(m, (unsigned long long)(uintptr_t)count);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    const int slot = base + __popc(peers & ((1u << lane) - 1u));
     if (slot >= cap) {
         atomicOr(err, (uint32_t)kErrQueueOverflow);
         return -1;
@@ -778,9 +800,14 @@ __global__ void k_handle_miss(DevScene s, Queue miss, PixelState ps, int nee) {
 
 // generateScatterRays (integrator.cpp:110-164) for one item whose Russian
 // roulette draw has survived; `rng` is the pixel's sampler after that draw.
+// When `tracked` has a counter (a pass of several scenes, some with media),
+// the shadow ray of a scene with media goes straight to the transmittance
+// tracker's queue and `shadow` keeps only the rays that an any-hit test
+// decides.
 __device__ __forceinline__ void scatter_item(const DevScene &s, const Queue &scat, int i, Pcg rng,
-                                             const Queue &next, const Queue &shadow,
-                                             const PixelState &ps, int nee, float rr, uint32_t *err) {
+                                             const Queue &next, const Queue &shadow_q,
+                                             const Queue &tracked, const PixelState &ps, int nee,
+                                             float rr, uint32_t *err) {
     float4 c0 = scat.at(0, i), c1 = scat.at(1, i), c2 = scat.at(2, i), c3 = scat.at(3, i);
     float4 c4 = scat.at(4, i), c5 = scat.at(5, i), c6 = scat.at(6, i), c7 = scat.at(7, i);
     uint32_t pixel = ubits(c2.w), depth = ubits(c1.w);
@@ -799,6 +826,7 @@ __device__ __forceinline__ void scatter_item(const DevScene &s, const Queue &sca
     // a scene without emitters has nothing to sample (the reference indexes an
     // empty light list there); NEE and its draws are skipped
     const DevScenePart &P = part_of(s, pixel);
+    const Queue &shadow = (tracked.count && P.has_media) ? tracked : shadow_q;
     if (nee && (bsdf_type & BSDF_SMOOTH) && P.n_lights > 0) {
         float ul = rng.get1d();
         uint32_t lid = (uint32_t)(ul * (float)P.n_lights);
@@ -817,7 +845,9 @@ __device__ __forceinline__ void scatter_item(const DevScene &s, const Queue &sca
         if (light_pdf > 0 && any(fv)) {
             V3 Ld = ls.L * thp * fv * fabsf(wi_local.z);
             if (any(Ld)) {
-                int j = push_slot(shadow.count, shadow.cap, err);
+                // with a tracker queue the lanes of a warp may push to two queues
+                int j = tracked.count ? push_slot_grouped(shadow.count, shadow.cap, err)
+                                      : push_slot(shadow.count, shadow.cap, err);
                 if (j >= 0) {
                     int32_t med = medium_towards(mi, mo, ray_medium, nrm, d);
                     shadow.at(0, j) = f4(po, 0.f);
@@ -887,8 +917,8 @@ __global__ void k_scatter_classify(DevScene s, Queue scat, PixelState ps, float 
 
 __global__ void __launch_bounds__(kThreads, 4)
 k_scatter_process(DevScene s, Queue scat, const int32_t *__restrict__ lists,
-                  const int32_t *__restrict__ counts, Queue next, Queue shadow, PixelState ps,
-                  int nee, float rr, uint32_t *err) {
+                  const int32_t *__restrict__ counts, Queue next, Queue shadow, Queue tracked,
+                  PixelState ps, int nee, float rr, uint32_t *err) {
     const int cap = scat.cap;
     const int c0 = counts[0], c01 = c0 + counts[1], c012 = c01 + counts[2], total = c012 + counts[3];
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
@@ -898,7 +928,7 @@ k_scatter_process(DevScene s, Queue scat, const int32_t *__restrict__ lists,
                     : lists[2 * (size_t)cap - 1 - (g - c012)];
         Pcg rng = load_rng(ps, ubits(scat.at(2, i).w));
         rng.get1d();   // the roulette draw taken by k_scatter_classify
-        scatter_item(s, scat, i, rng, next, shadow, ps, nee, rr, err);
+        scatter_item(s, scat, i, rng, next, shadow, tracked, ps, nee, rr, err);
     }
 }
 
@@ -1105,9 +1135,12 @@ k_medium_sample(DevScene s, Queue msq, Queue next, Queue miss, Queue hitl, Queue
     }
 }
 
-// sampleMediumScattering, medium.cpp:105-153
-__global__ void k_medium_scatter(DevScene s, Queue mscat, Queue next, Queue shadow, PixelState ps,
-                                 int nee, uint32_t *err) {
+// sampleMediumScattering, medium.cpp:105-153.  Every item is in a scene
+// with media: with `tracked` given (a counter set), its shadow ray goes
+// straight to the transmittance tracker's queue, as in scatter_item.
+__global__ void k_medium_scatter(DevScene s, Queue mscat, Queue next, Queue shadow_q, Queue tracked,
+                                 PixelState ps, int nee, uint32_t *err) {
+    const Queue &shadow = tracked.count ? tracked : shadow_q;
     int n = min(*mscat.count, mscat.cap);   // an overflowed queue holds cap items
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 c0 = mscat.at(0, i), c1 = mscat.at(1, i), c2 = mscat.at(2, i), c3 = mscat.at(3, i);
@@ -2618,20 +2651,27 @@ extern "C" int krr_wf_handle_miss(krr_wf *wf, void *stream) {
     return KRR_OK;
 }
 
-extern "C" int krr_wf_generate_scatter_rays(krr_wf *wf, int32_t depth, void *stream) {
-    KRR_TRY(ready(wf));
+// generateScatterRays; with `to_tracker` the shadow rays of scenes with
+// media go to the transmittance tracker's queue (split_shadows()).
+static int scatter_stage(krr_wf *wf, int depth, cudaStream_t st, bool to_tracker) {
     int cur = depth & 1;
-    cudaStream_t st = as_stream(stream);
+    const Queue tracked = to_tracker ? Queue{wf->qbuf[Q_MEDIUM_SAMPLE], (int32_t)wf->qcap, wf->shadow_tracked_count()}
+                                     : Queue{};
     KRR_CUDA(cudaMemsetAsync(wf->scatter_class_counts(), 0, 4 * sizeof(int32_t), st));
     k_scatter_classify<<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->q(Q_SCATTER), wf->ps,
                                                       wf->params.rr, wf->scatter_lists,
                                                       wf->scatter_class_counts());
     k_scatter_process<<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->q(Q_SCATTER), wf->scatter_lists,
                                                      wf->scatter_class_counts(), wf->q(cur ^ 1),
-                                                     wf->q(Q_SHADOW), wf->ps, wf->params.nee,
+                                                     wf->q(Q_SHADOW), tracked, wf->ps, wf->params.nee,
                                                      wf->params.rr, wf->err());
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
+}
+
+extern "C" int krr_wf_generate_scatter_rays(krr_wf *wf, int32_t depth, void *stream) {
+    KRR_TRY(ready(wf));
+    return scatter_stage(wf, depth, as_stream(stream), false);
 }
 
 extern "C" int krr_wf_trace_shadow(krr_wf *wf, void *stream) {
@@ -2776,7 +2816,12 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
     // The pixels go through the bounces in waves of the queue capacity (all
     // at once by default); a pixel's path touches only its own state, so the
     // waves give the same frame as one pass over all pixels.
-    const bool fuse = wf->params.nee && !wf->medium;
+    // In a pass of several scenes where only some have media, the shadow
+    // rays of the scenes without media are traced with the next bounce's
+    // rays too; those of the scenes with media go to the tracker
+    // (split_shadows()).
+    const bool split = split_shadows(wf);
+    const bool fuse = (wf->params.nee && !wf->medium) || split;
     for (int s = 0; s < wf->params.spp; ++s) {
         for (int64_t p0 = 0; p0 < wf->n; p0 += wf->qcap) {
             KRR_TRY(krr_wf_reset_queues(wf, -1, stream));
@@ -2792,8 +2837,10 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
                     KRR_TRY(krr_wf_handle_miss(wf, stream));
                 }
                 if (depth == loop_depth(wf)) break;
-                if (wf->medium) KRR_TRY(krr_wf_sample_medium_scattering(wf, depth, stream));
-                KRR_TRY(krr_wf_generate_scatter_rays(wf, depth, stream));
+                if (split) KRR_CUDA(cudaMemsetAsync(wf->shadow_tracked_count(), 0, sizeof(int32_t), st));
+                if (wf->medium) KRR_TRY(launch_medium_scatter(wf, depth, st, split));
+                KRR_TRY(scatter_stage(wf, depth, st, split));
+                if (split) KRR_TRY(launch_shadow_tracker(wf, st));
                 traced = fuse;
                 if (fuse) KRR_TRY(trace_shadow_and_next(wf, depth, st));
                 else if (wf->params.nee) KRR_TRY(krr_wf_trace_shadow(wf, stream));
@@ -3128,9 +3175,28 @@ int launch_medium_sample(krr_wf *wf, int depth, cudaStream_t st) {
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }
-int launch_medium_scatter(krr_wf *wf, int depth, cudaStream_t st) {
+// The tracked shadow rays are staged in the medium-sample queue's storage
+// (consumed earlier in the bounce) with their own counter.
+static Queue tracked_queue(krr_wf *wf) {
+    return Queue{wf->qbuf[Q_MEDIUM_SAMPLE], (int32_t)wf->qcap, wf->shadow_tracked_count()};
+}
+
+// A pass of several scenes of which some have media and some do not: the
+// shadow rays of the scenes without media are traced with the next bounce's
+// rays in one launch (as in a pass without media), those of the scenes with
+// media go straight to the tracker.  A pixel's shadow rays all go one way,
+// so each pixel gets the same terms in the same order.
+bool split_shadows(const krr_wf *wf) {
+    if (!wf->medium || !wf->params.nee || wf->n_parts <= 1) return false;
+    bool with = false, without = false;
+    for (const DevScenePart &P : wf->parts) (P.has_media ? with : without) = true;
+    return with && without;
+}
+
+int launch_medium_scatter(krr_wf *wf, int depth, cudaStream_t st, bool to_tracker) {
     k_medium_scatter<<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->q(Q_MEDIUM_SCATTER),
-                                                     wf->q((depth & 1) ^ 1), wf->q(Q_SHADOW), wf->ps,
+                                                     wf->q((depth & 1) ^ 1), wf->q(Q_SHADOW),
+                                                     to_tracker ? tracked_queue(wf) : Queue{}, wf->ps,
                                                      wf->params.nee, wf->err());
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
@@ -3141,17 +3207,26 @@ int launch_medium_scatter(krr_wf *wf, int depth, cudaStream_t st) {
 // own counter and ratio-tracked by k_shadow_tr.
 int launch_trace_shadow_tr(krr_wf *wf, cudaStream_t st) {
     static_assert(kMediumSampleCh >= kShadowCh, "tracked shadow rays need five planes");
-    Queue tracked{wf->qbuf[Q_MEDIUM_SAMPLE], (int32_t)wf->qcap, wf->shadow_tracked_count()};
+    const Queue tracked = tracked_queue(wf);
     KRR_CUDA(cudaMemsetAsync(tracked.count, 0, sizeof(int32_t), st));
     int *terr = wf->accel.d_scratch + 4;
     const InstancedView iv = wf->accel.levels == 2 ? instanced_view(&wf->accel) : InstancedView{};
-    const int32_t *order = nullptr;
     if (wf->accel.node_format == 1)
         k_shadow_split<1><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
                                                           wf->q(Q_SHADOW), tracked, wf->ps, wf->err(), terr);
     else
         k_shadow_split<0><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
                                                           wf->q(Q_SHADOW), tracked, wf->ps, wf->err(), terr);
+    KRR_CUDA(cudaGetLastError());
+    return launch_shadow_tracker(wf, st);
+}
+
+// Ratio tracking of the shadow rays in the tracker's queue.
+int launch_shadow_tracker(krr_wf *wf, cudaStream_t st) {
+    const Queue tracked = tracked_queue(wf);
+    int *terr = wf->accel.d_scratch + 4;
+    const InstancedView iv = wf->accel.levels == 2 ? instanced_view(&wf->accel) : InstancedView{};
+    const int32_t *order = nullptr;
     KRR_TRY(work_order(wf, tracked, 1, st, &order));
     if (wf->accel.node_format == 1)
         k_shadow_tr<1><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
