@@ -34,8 +34,6 @@ namespace krr {
 namespace {
 
 constexpr uint32_t kLeafBit = 0x80000000u;
-// best-hit marker of a ray whose traversal the stack limit cut off
-constexpr uint32_t kCutRay = KRR_MISS - 1u;
 constexpr int kBuildThreads = 256;
 
 __device__ __forceinline__ void atomic_min_f(float *addr, float v) {

@@ -99,6 +99,8 @@ struct krr_accel {
 namespace krr {
 
 constexpr int kTraversalStack = 48;
+// best-hit marker of a ray whose traversal the stack limit cut off
+constexpr uint32_t kCutRay = KRR_MISS - 1u;
 constexpr int kNodeQuads[2] = {5, 14};   // float4 per node, by node format
 // Process-wide node format used by builds (krr_set_bvh_node_format).
 int default_node_format();

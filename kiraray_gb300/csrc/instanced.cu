@@ -5,7 +5,7 @@
 // with 3x4 transforms (src/core/device/optix.cpp:357-398) and updates only
 // the instance level when instances move (optix.cpp:618-669).
 //
-// Traversal (one ray per thread): the world ray walks the top level; at an
+// Traversal: the world ray walks the top level; at an
 // instance leaf the ray is carried into the instance's object space by the
 // instance's world-to-object 3x4 matrix (row by row, m0 x + m1 y + m2 z
 // (+ m3), each operation rounded), the instance's tree is searched for the
@@ -31,23 +31,168 @@ namespace {
 constexpr int kInstThreads = 128;
 
 // MODE 0 closest, 1 any, 2 mixed (any-hit set first), as the one-level
-// kernels; a grid-stride loop, one ray per thread.
+// kernels: persistent warps that refill idle lanes from a work counter, as
+// the one-level kernel (accel.cu), with one loop over both levels.
+// At an instance leaf the lane saves its pending top-level work (node group,
+// remaining instance leaves) and a return marker on its stack, carries the
+// ray into the instance's object space and walks the geometry tree there,
+// comparing every triangle's (t, global id) with the best so far; popping
+// the marker reloads the world ray.  Each instance leaf and each triangle is
+// tested exactly as in trace_two_level, and the result is the smallest
+// (t, global id) as there.
+constexpr uint32_t kTriGroupBit = 0x80000000u;   // stack entry: pending leaf group
+constexpr uint32_t kReturnBit = 0x40000000u;     // stack entry: back to the world ray
+
 template <int MODE, int FMT>
-__global__ void __launch_bounds__(kInstThreads)
-k_trace_two_level(InstancedView v, TraceLaunch L) {
+__global__ void __launch_bounds__(kInstThreads, 6)
+k_trace_two_level_p(InstancedView v, TraceLaunch L) {
+    const int lane = threadIdx.x & 31;
     const int64_t n_any = MODE == 2 ? min((int64_t)*L.d_any_count, L.n) : 0;
     const int64_t n = (L.d_count ? min((int64_t)*L.d_count, L.n) : L.n) + n_any;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const bool any = MODE == 1 || (MODE == 2 && i < n_any);
-        const int64_t idx = MODE == 2 && !any ? i - n_any : i;
-        const float4 *po = any && MODE == 2 ? L.any_o : L.ray_o, *pd = any && MODE == 2 ? L.any_d : L.ray_d;
-        const float4 ro = po[idx * L.ray_stride], rd = pd[idx * L.ray_stride];
-        if (any) {
-            const float4 h = trace_two_level<true, FMT>(v, f3(ro), f3(rd), ro.w, rd.w, L.err);
-            L.occluded[idx] = __float_as_uint(h.w) != KRR_MISS ? 1 : 0;
-        } else {
-            L.hits[idx] = trace_two_level<false, FMT>(v, f3(ro), f3(rd), ro.w, rd.w, L.err);
+    bool any_ray = MODE == 1;
+    uint2 stack[kTraversalStack];
+    int sp = 0;
+    bool active = false, exhausted = false, in_geom = false;
+    int64_t ray_id = 0;
+    RayPre r;
+    V3 inv, oinv;
+    int oct = 0;
+    float tmax = 0.f, tmin0 = 0.f;
+    uint2 ng = make_uint2(0, 0), tg = make_uint2(0, 0);
+    float best_b1 = 0.f, best_b2 = 0.f;
+    uint32_t best_prim = KRR_MISS, id_delta = 0;
+
+    auto world_ray = [&](V3 &o, V3 &d) {
+        const float4 *po = (MODE == 2 && any_ray) ? L.any_o : L.ray_o;
+        const float4 *pd = (MODE == 2 && any_ray) ? L.any_d : L.ray_d;
+        const float4 ro = po[ray_id * L.ray_stride], rd = pd[ray_id * L.ray_stride];
+        o = f3(ro);
+        d = f3(rd);
+        tmin0 = ro.w;
+    };
+    auto set_ray = [&](V3 o, V3 d) {
+        r = ray_pre(o, d, tmin0);
+        inv = box_inverse(d);
+        oinv = V3{-o.x * inv.x, -o.y * inv.y, -o.z * inv.z};
+        oct = (inv.x < 0.f ? 1 : 0) | (inv.y < 0.f ? 2 : 0) | (inv.z < 0.f ? 4 : 0);
+    };
+
+    while (true) {
+        unsigned act = __ballot_sync(0xffffffffu, active);
+        if (__popc(act) < L.refill_below && !exhausted) {
+            unsigned need = ~act;
+            int leader = __ffs(need) - 1;
+            long long base = 0;
+            if (lane == leader) base = atomicAdd(reinterpret_cast<unsigned long long *>(L.counter),
+                                                 (unsigned long long)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (base + __popc(need) >= n) exhausted = true;
+            if (!active) {
+                int64_t idx = base + __popc(need & ((1u << lane) - 1));
+                if (idx < n) {
+                    if (MODE == 2) {
+                        any_ray = idx < n_any;
+                        if (!any_ray) idx -= n_any;
+                    }
+                    ray_id = idx;
+                    V3 o, d;
+                    world_ray(o, d);
+                    tmax = ((MODE == 2 && any_ray) ? L.any_d : L.ray_d)[ray_id * L.ray_stride].w;
+                    set_ray(o, d);
+                    ng = make_uint2(0u, (1u << oct) | (1u << 8));
+                    tg = make_uint2(0u, 0u);
+                    sp = 0;
+                    in_geom = false;
+                    best_prim = KRR_MISS;
+                    active = true;
+                }
+            }
+            act = __ballot_sync(0xffffffffu, active);
+        }
+        if (act == 0) break;
+
+        bool done = false;
+        if (active && (ng.y & 0xffu)) {
+            int p = __ffs(ng.y & 0xffu) - 1;
+            ng.y &= ~(1u << p);
+            int slot = p ^ oct;
+            uint32_t imask = ng.y >> 8;
+            uint32_t child = ng.x + __popc(imask & ((1u << slot) - 1u));
+            if (ng.y & 0xffu) {
+                if (sp < L.stack_limit) stack[sp++] = ng;
+                else { atomicOr(L.err, (int)kErrStackOverflow); done = true; best_prim = kCutRay; }
+            }
+            visit<FMT>(in_geom ? v.blas_nodes : v.tlas_nodes, child, r, inv, oinv, oct, tmax, ng, tg);
+        }
+        // instance leaves: enter the first one not masked off (the remaining
+        // ones wait on the stack); the step ends with no leaf group pending
+        while (active && !done && tg.y && !in_geom) {
+            const int b = __ffs(tg.y) - 1;
+            tg.y &= tg.y - 1u;
+            const uint32_t k = __float_as_uint(__ldg(v.tlas_tris + 3 * (size_t)(tg.x + b)).w);
+            const TraceInst I = v.inst[k];
+            if (any_ray && !I.mask) continue;
+            const int need_slots = ((ng.y & 0xffu) ? 1 : 0) + (tg.y ? 1 : 0) + 1;
+            if (sp + need_slots > L.stack_limit) {
+                atomicOr(L.err, (int)kErrStackOverflow);
+                done = true;
+                best_prim = kCutRay;
+                break;
+            }
+            if (ng.y & 0xffu) stack[sp++] = ng;
+            if (tg.y) stack[sp++] = make_uint2(tg.x, tg.y | kTriGroupBit);
+            stack[sp++] = make_uint2(0u, kReturnBit);
+            V3 o, d;
+            world_ray(o, d);
+            set_ray(inst_point(I.inv, o), inst_vector(I.inv, d));
+            ng = make_uint2(I.blas_root, (1u << oct) | (1u << 8));
+            tg = make_uint2(0u, 0u);
+            id_delta = I.id_delta;
+            in_geom = true;
+        }
+        while (active && in_geom && tg.y && !done) {
+            const int b = __ffs(tg.y) - 1;
+            tg.y &= tg.y - 1u;
+            const float4 *tp = v.blas_tris + 3 * (size_t)(tg.x + b);
+            const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+            float b1, b2;
+            const float t = tri_test(r, v0, v1, v2, b1, b2);
+            const uint32_t gid = __float_as_uint(v0.w) + id_delta;
+            if (any_ray) {
+                if (t > r.tmin && t <= tmax) { best_prim = gid; done = true; }
+            } else if (t > r.tmin && (t < tmax || (t == tmax && gid < best_prim))) {
+                tmax = t; best_b1 = b1; best_b2 = b2; best_prim = gid;
+            }
+        }
+        if (active && !done && !(ng.y & 0xffu) && tg.y == 0u) {
+            if (sp > 0) {
+                const uint2 e = stack[--sp];
+                if (e.y & kReturnBit) {
+                    V3 o, d;
+                    world_ray(o, d);
+                    set_ray(o, d);
+                    in_geom = false;
+                    ng = make_uint2(0u, 0u);
+                } else if (e.y & kTriGroupBit) {
+                    tg = make_uint2(e.x, e.y & 0x00ffffffu);
+                } else {
+                    ng = e;
+                }
+            } else {
+                done = true;
+            }
+        }
+        if (!active) continue;
+        if (done) {
+            if (any_ray) {
+                L.occluded[ray_id] = best_prim == kCutRay ? 0xFF : (best_prim != KRR_MISS ? 1 : 0);
+            } else {
+                L.hits[ray_id] = best_prim < kCutRay
+                                     ? make_float4(tmax, best_b1, best_b2, __uint_as_float(best_prim))
+                                     : make_float4(best_prim == kCutRay ? __int_as_float(0x7fffffff) : INFINITY,
+                                                   0.f, 0.f, __uint_as_float(KRR_MISS));
+            }
+            active = false;
         }
     }
 }
@@ -193,21 +338,24 @@ int accel_update_instances(krr_accel *a, const float *inst_xf, cudaStream_t s) {
 
 int launch_trace_instanced(const krr_accel *a, const TraceLaunch &l, int mode, cudaStream_t s) {
     const InstancedView v = instanced_view(a);
+    const bool fmt1 = a->node_format == 1;
     static int grid = 0;
     if (!grid) {
-        int dev = 0, sms = 0;
+        int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        grid = std::max(1, sms) * 16;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_two_level_p<0, 0>, kInstThreads, 0);
+        grid = std::max(1, sms) * std::max(1, per_sm);
     }
-    const bool fmt1 = a->node_format == 1;
+    KRR_CHECK_ARG(l.counter != nullptr, "the two-level traversal needs a work counter");
+    KRR_CUDA(cudaMemsetAsync(l.counter, 0, sizeof(unsigned long long), s));
     switch (mode) {
-        case 0: fmt1 ? k_trace_two_level<0, 1><<<grid, kInstThreads, 0, s>>>(v, l)
-                     : k_trace_two_level<0, 0><<<grid, kInstThreads, 0, s>>>(v, l); break;
-        case 1: fmt1 ? k_trace_two_level<1, 1><<<grid, kInstThreads, 0, s>>>(v, l)
-                     : k_trace_two_level<1, 0><<<grid, kInstThreads, 0, s>>>(v, l); break;
-        default: fmt1 ? k_trace_two_level<2, 1><<<grid, kInstThreads, 0, s>>>(v, l)
-                      : k_trace_two_level<2, 0><<<grid, kInstThreads, 0, s>>>(v, l); break;
+        case 0: fmt1 ? k_trace_two_level_p<0, 1><<<grid, kInstThreads, 0, s>>>(v, l)
+                     : k_trace_two_level_p<0, 0><<<grid, kInstThreads, 0, s>>>(v, l); break;
+        case 1: fmt1 ? k_trace_two_level_p<1, 1><<<grid, kInstThreads, 0, s>>>(v, l)
+                     : k_trace_two_level_p<1, 0><<<grid, kInstThreads, 0, s>>>(v, l); break;
+        default: fmt1 ? k_trace_two_level_p<2, 1><<<grid, kInstThreads, 0, s>>>(v, l)
+                      : k_trace_two_level_p<2, 0><<<grid, kInstThreads, 0, s>>>(v, l); break;
     }
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
