@@ -561,6 +561,12 @@ typedef struct krr_nrc_config {
                                     and takes the cache's answer once its
                                     spread a(x1..xn) exceeds this fraction
                                     of a0 (0.01; 0 = at the first bounce) */
+    float ema_decay;             /* 0 (default): queries read the trained
+                                    parameters; d in (0, 1): queries read an
+                                    exponential moving average of them,
+                                    e <- d e + (1 - d) w after each Adam
+                                    step (not in the reference, which has no
+                                    cache)                                  */
 } krr_nrc_config;
 
 typedef struct krr_nrc_info_t {
@@ -586,7 +592,9 @@ int krr_nrc_train_step(krr_nrc *nrc, const float *d_inputs, const float *d_targe
  * as krr_nrc_get_params); synchronises the device. */
 int krr_nrc_gradients(krr_nrc *nrc, const float *d_inputs, const float *d_targets, int64_t count,
                       float *h_grad_mlp, float *h_grad_table, float *h_loss);
-/* which: 0 = MLP weights [layer][out rows][64], 1 = hash table [entry][2]. */
+/* which: 0 = MLP weights [layer][out rows][64], 1 = hash table [entry][2];
+ * get_params also 2, 3 = the same arrays of the queries' moving average
+ * (ema_decay > 0).  set_params restarts that average from the new values. */
 int krr_nrc_get_params(const krr_nrc *nrc, int32_t which, float *h_dst, int64_t count);
 int krr_nrc_set_params(krr_nrc *nrc, int32_t which, const float *h_src, int64_t count);
 /* Device-side status of the cache (synchronises the stream): out_flags =

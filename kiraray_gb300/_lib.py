@@ -91,7 +91,8 @@ class NrcConfig(C.Structure):
                 ("epsilon", C.c_float), ("loss_scale", C.c_float), ("batch_size", C.c_int32),
                 ("train_pixel_stride", C.c_int32), ("seed", C.c_uint32),
                 ("scene_lo", C.c_float * 3), ("scene_hi", C.c_float * 3),
-                ("tensor_cores", C.c_int32), ("termination_spread", C.c_float)]
+                ("tensor_cores", C.c_int32), ("termination_spread", C.c_float),
+                ("ema_decay", C.c_float)]
 
 
 class NrcInfo(C.Structure):

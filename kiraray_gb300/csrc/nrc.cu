@@ -46,6 +46,12 @@ struct krr_nrc {
     uint8_t *packed = nullptr;               // weights in tcgen05 canonical tiles
     uint8_t *packed_t = nullptr;             // transposed weights (backward)
     uint32_t *err = nullptr;                 // device error flags
+    // inference copy (ema_decay > 0): exponential moving average of the
+    // parameters after each Adam step, FP32 and BF16, and its packed tiles;
+    // queries read it, training reads the parameters themselves
+    float *ema_w = nullptr, *ema_table = nullptr;
+    __nv_bfloat16 *ema_weights = nullptr, *ema_table_bf = nullptr;
+    uint8_t *ema_packed = nullptr;
 };
 
 namespace {
@@ -329,6 +335,12 @@ __device__ __forceinline__ void adam4(const AdamArgs &a, float4 g, float4 &mm, f
     ww.w = adam_one(a, g.w, mm.w, vv.w, ww.w);
 }
 
+__device__ __forceinline__ void store_bf16x4(__nv_bfloat16 *dst, int64_t i, float4 x) {
+    __nv_bfloat162 lo = __floats2bfloat162_rn(x.x, x.y), hi = __floats2bfloat162_rn(x.z, x.w);
+    reinterpret_cast<uint2 *>(dst)[i] =
+        make_uint2(*reinterpret_cast<uint32_t *>(&lo), *reinterpret_cast<uint32_t *>(&hi));
+}
+
 __device__ __forceinline__ void adam_store4(float *m, float *v, float *w, float *grad,
                                             __nv_bfloat16 *wb, int64_t i, float4 mm, float4 vv,
                                             float4 ww) {
@@ -336,15 +348,27 @@ __device__ __forceinline__ void adam_store4(float *m, float *v, float *w, float 
     reinterpret_cast<float4 *>(m)[i] = mm;
     reinterpret_cast<float4 *>(v)[i] = vv;
     reinterpret_cast<float4 *>(w)[i] = ww;
-    __nv_bfloat162 lo = __floats2bfloat162_rn(ww.x, ww.y), hi = __floats2bfloat162_rn(ww.z, ww.w);
-    reinterpret_cast<uint2 *>(wb)[i] =
-        make_uint2(*reinterpret_cast<uint32_t *>(&lo), *reinterpret_cast<uint32_t *>(&hi));
+    store_bf16x4(wb, i, ww);
+}
+
+// ema <- d ema + (1 - d) w, FP32 and BF16
+struct EmaArgs {
+    float *e;
+    __nv_bfloat16 *eb;
+    float d;
+};
+__device__ __forceinline__ void ema_store4(const EmaArgs &x, int64_t i, float4 ww) {
+    float4 e = reinterpret_cast<const float4 *>(x.e)[i];
+    const float c = 1.f - x.d;
+    e = make_float4(x.d * e.x + c * ww.x, x.d * e.y + c * ww.y, x.d * e.z + c * ww.z, x.d * e.w + c * ww.w);
+    reinterpret_cast<float4 *>(x.e)[i] = e;
+    store_bf16x4(x.eb, i, e);
 }
 
 __global__ void k_adam(float *__restrict__ w, float *__restrict__ m, float *__restrict__ v,
                        float *__restrict__ grad, __nv_bfloat16 *__restrict__ wb, int64_t n, float lr,
                        float b1, float b2, float eps, float grad_scale, const int64_t *__restrict__ step,
-                       const uint32_t *__restrict__ diverged) {
+                       const uint32_t *__restrict__ diverged, EmaArgs ema) {
     if (*diverged) {   // keep the parameters; drop the gradient
         for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
              i += (int64_t)gridDim.x * blockDim.x)
@@ -371,9 +395,11 @@ __global__ void k_adam(float *__restrict__ w, float *__restrict__ m, float *__re
         }
         adam4(a, g0, m0, v0, w0);
         adam_store4(m, v, w, grad, wb, i, m0, v0, w0);
+        if (ema.e) ema_store4(ema, i, w0);
         if (two) {
             adam4(a, g1, m1, v1, w1);
             adam_store4(m, v, w, grad, wb, j, m1, v1, w1);
+            if (ema.e) ema_store4(ema, j, w1);
         }
     }
     for (int64_t i = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
@@ -384,6 +410,11 @@ __global__ void k_adam(float *__restrict__ w, float *__restrict__ m, float *__re
         v[i] = vv;
         w[i] = ww;
         wb[i] = __float2bfloat16_rn(ww);
+        if (ema.e) {
+            const float e = ema.d * ema.e[i] + (1.f - ema.d) * ww;
+            ema.e[i] = e;
+            ema.eb[i] = __float2bfloat16_rn(e);
+        }
     }
 }
 
@@ -428,19 +459,24 @@ int ensure_capacity(krr_nrc *n, int64_t cap) {
 
 // Forward pass over `cap` rows (live count on the device); leaves the layer
 // inputs in n->act and the output in n->out.
+// inference = true: the inference copy of the parameters (the moving
+// average when ema_decay > 0), for queries; false: the trained parameters.
 int forward(krr_nrc *n, const float *d_inputs, const int32_t *d_count, int64_t cap, cudaStream_t s,
-            bool keep_acts = true) {
+            bool keep_acts = true, bool inference = false) {
     KRR_TRY(ensure_capacity(n, cap));
     __nv_bfloat16 *A = n->act;
+    const bool ema = inference && n->ema_w;
+    const __nv_bfloat16 *table = ema ? n->ema_table_bf : n->table;
+    const __nv_bfloat16 *weights = ema ? n->ema_weights : n->weights;
     if (n->cfg.tensor_cores)
-        return nrc_forward_tc(n->grid, n->mlp, d_inputs, d_count, cap, n->table, n->packed, n->out,
-                              keep_acts ? A : nullptr, n->err, s);
-    k_encode<<<grid_for(cap), kThreads, 0, s>>>(n->grid, d_inputs, d_count, cap, n->table, A);
+        return nrc_forward_tc(n->grid, n->mlp, d_inputs, d_count, cap, table, ema ? n->ema_packed : n->packed,
+                              n->out, keep_acts ? A : nullptr, n->err, s);
+    k_encode<<<grid_for(cap), kThreads, 0, s>>>(n->grid, d_inputs, d_count, cap, table, A);
     KRR_CUDA(cudaGetLastError());
     int blocks = grid_for(cap, 128);
     for (int l = 0; l < n->mlp.layers; ++l) {
         const __nv_bfloat16 *X = A + (size_t)l * cap * kNrcIn;
-        const __nv_bfloat16 *W = n->weights + n->mlp.w_offset[l];
+        const __nv_bfloat16 *W = weights + n->mlp.w_offset[l];
         if (l + 1 < n->mlp.layers) {
             __nv_bfloat16 *Y = A + (size_t)(l + 1) * cap * kNrcIn;
             k_dense_fwd<kNrcWidth, true, false><<<blocks, kThreads, 0, s>>>(X, W, d_count, cap, Y, nullptr);
@@ -474,7 +510,7 @@ uint32_t *nrc_error_flags(krr_nrc *n) { return n->err; }
 int nrc_query_device(krr_nrc *n, const float *d_inputs, const int32_t *d_count, int64_t cap,
                      float *d_out, cudaStream_t s) {
     if (cap <= 0) return KRR_OK;
-    KRR_TRY(forward(n, d_inputs, d_count, cap, s, false));
+    KRR_TRY(forward(n, d_inputs, d_count, cap, s, false, true));
     k_write_rgb<<<grid_for(cap), kThreads, 0, s>>>(n->out, d_count, cap, d_out);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
@@ -523,11 +559,25 @@ int backward(krr_nrc *n, const float *d_inputs, const float *d_targets, const in
     return KRR_OK;
 }
 
-// Both weight layouts of the tensor-core kernels, from the BF16 weights.
+// Both weight layouts of the tensor-core kernels, from the BF16 weights, and
+// the forward layout of the inference copy.
 int pack_weights(krr_nrc *n, cudaStream_t s) {
     if (!n->cfg.tensor_cores) return KRR_OK;
     KRR_TRY(nrc_pack_weights(n->weights, n->mlp, n->packed, s));
+    if (n->ema_w) KRR_TRY(nrc_pack_weights(n->ema_weights, n->mlp, n->ema_packed, s));
     return nrc_pack_weights_t(n->weights, n->mlp, n->packed_t, s);
+}
+
+// The inference copy restarts from the trained parameters.
+int reset_ema(krr_nrc *n, cudaStream_t s) {
+    if (!n->ema_w) return KRR_OK;
+    const int64_t tn = (int64_t)n->n_entries * n->grid.features;
+    KRR_CUDA(cudaMemcpyAsync(n->ema_w, n->w_master, n->mlp.n_params * 4, cudaMemcpyDeviceToDevice, s));
+    KRR_CUDA(cudaMemcpyAsync(n->ema_table, n->table_master, tn * 4, cudaMemcpyDeviceToDevice, s));
+    k_to_bf16<<<grid_for(n->mlp.n_params), kThreads, 0, s>>>(n->ema_w, n->ema_weights, n->mlp.n_params);
+    k_to_bf16<<<grid_for(tn), kThreads, 0, s>>>(n->ema_table, n->ema_table_bf, tn);
+    KRR_CUDA(cudaGetLastError());
+    return KRR_OK;
 }
 
 int nrc_train_device(krr_nrc *n, const float *d_inputs, const float *d_targets,
@@ -539,14 +589,15 @@ int nrc_train_device(krr_nrc *n, const float *d_inputs, const float *d_targets,
     // Adam
     const krr_nrc_config &c = n->cfg;
     k_adam_step<<<1, 1, 0, s>>>(n->step, (double)c.beta1, (double)c.beta2, n->loss, n->err);
+    const EmaArgs ew{n->ema_w, n->ema_weights, c.ema_decay}, et{n->ema_table, n->ema_table_bf, c.ema_decay};
     k_adam<<<grid_for(n->mlp.n_params), kThreads, 0, s>>>(n->w_master, n->w_m, n->w_v, n->w_grad,
                                                            n->weights, n->mlp.n_params, c.learning_rate,
                                                            c.beta1, c.beta2, c.epsilon, 1.f / scale,
-                                                           n->step, n->err + 1);
+                                                           n->step, n->err + 1, ew);
     int64_t tn = (int64_t)n->n_entries * n->grid.features;
     k_adam<<<grid_for(tn), kThreads, 0, s>>>(n->table_master, n->table_m, n->table_v, n->table_grad,
                                              n->table, tn, c.learning_rate, c.beta1, c.beta2,
-                                             c.epsilon, 1.f / scale, n->step, n->err + 1);
+                                             c.epsilon, 1.f / scale, n->step, n->err + 1, et);
     KRR_CUDA(cudaGetLastError());
     return pack_weights(n, s);
 }
@@ -586,6 +637,7 @@ extern "C" int krr_nrc_create(const krr_nrc_config *cfg, krr_nrc **out) {
     KRR_CHECK_ARG(cfg->base_resolution >= 2 && cfg->max_resolution >= cfg->base_resolution,
                   "bad resolutions");
     KRR_CHECK_ARG(cfg->batch_size > 0, "batch_size must be positive");
+    KRR_CHECK_ARG(cfg->ema_decay >= 0.f && cfg->ema_decay < 1.f, "ema_decay must be in [0, 1)");
     krr_nrc *n = new krr_nrc();
     n->cfg = *cfg;
     if (n->cfg.train_pixel_stride < 1) n->cfg.train_pixel_stride = 1;
@@ -655,11 +707,19 @@ extern "C" int krr_nrc_create(const krr_nrc_config *cfg, krr_nrc **out) {
     alloc((void **)&n->packed_t, (size_t)(m.layers - 1) * kNrcWidth * kNrcIn * 2 + kNrcIn * kNrcOutPad * 2);
     alloc((void **)&n->err, 16);
     alloc((void **)&n->step, 16);
+    if (cfg->ema_decay > 0.f) {
+        alloc((void **)&n->ema_w, m.n_params * 4);
+        alloc((void **)&n->ema_weights, m.n_params * 2);
+        alloc((void **)&n->ema_table, tn * 4);
+        alloc((void **)&n->ema_table_bf, tn * 2);
+        alloc((void **)&n->ema_packed, (size_t)(m.layers - 1) * kNrcWidth * kNrcIn * 2 + kNrcOutPad * kNrcIn * 2);
+    }
     if (st == KRR_OK) {
         cudaMemcpy(n->w_master, w.data(), m.n_params * 4, cudaMemcpyHostToDevice);
         cudaMemcpy(n->table_master, t.data(), tn * 4, cudaMemcpyHostToDevice);
         k_to_bf16<<<grid_for(m.n_params), kThreads>>>(n->w_master, n->weights, m.n_params);
         k_to_bf16<<<grid_for((int64_t)tn), kThreads>>>(n->table_master, n->table, (int64_t)tn);
+        reset_ema(n, 0);
         pack_weights(n, 0);
         cudaError_t e = cudaDeviceSynchronize();
         if (e != cudaSuccess) st = cuda_status(e, "krr_nrc_create", __FILE__, __LINE__);
@@ -679,7 +739,9 @@ extern "C" int krr_nrc_destroy(krr_nrc *n) {
                     (void *)n->table_grad, (void *)n->table, (void *)n->w_master, (void *)n->w_m,
                     (void *)n->w_v, (void *)n->w_grad, (void *)n->weights, (void *)n->act,
                     (void *)n->out, (void *)n->dA, (void *)n->dB, (void *)n->loss,
-                    (void *)n->packed, (void *)n->packed_t, (void *)n->err, (void *)n->step})
+                    (void *)n->packed, (void *)n->packed_t, (void *)n->err, (void *)n->step,
+                    (void *)n->ema_w, (void *)n->ema_weights, (void *)n->ema_table,
+                    (void *)n->ema_table_bf, (void *)n->ema_packed})
         cudaFree(p);
     delete n;
     return KRR_OK;
@@ -721,14 +783,16 @@ extern "C" int krr_nrc_info(const krr_nrc *n, krr_nrc_info_t *info) {
 }
 
 // Parameter access for tests and checkpoints: which = 0 MLP weights (FP32
-// master, [layer][out][64]), 1 hash table (FP32 master, [entry][2]).
+// master, [layer][out][64]), 1 hash table (FP32 master, [entry][2]); 2 and 3
+// the same arrays of the inference copy (ema_decay > 0).
 extern "C" int krr_nrc_get_params(const krr_nrc *n, int32_t which, float *h_dst, int64_t count) {
-    KRR_CHECK_ARG(n && h_dst, "NULL argument");
-    int64_t total = which == 0 ? n->mlp.n_params : (int64_t)n->n_entries * 2;
+    KRR_CHECK_ARG(n && h_dst && which >= 0 && which <= 3, "bad argument");
+    KRR_CHECK_ARG(which < 2 || n->ema_w, "the cache keeps no inference copy (ema_decay 0)");
+    int64_t total = (which & 1) == 0 ? n->mlp.n_params : (int64_t)n->n_entries * 2;
     KRR_CHECK_ARG(count == total, "count does not match the parameter array");
+    const float *src[4] = {n->w_master, n->table_master, n->ema_w, n->ema_table};
     KRR_CUDA(cudaDeviceSynchronize());
-    KRR_CUDA(cudaMemcpy(h_dst, which == 0 ? n->w_master : n->table_master, total * 4,
-                        cudaMemcpyDeviceToHost));
+    KRR_CUDA(cudaMemcpy(h_dst, src[which], total * 4, cudaMemcpyDeviceToHost));
     return KRR_OK;
 }
 
@@ -741,7 +805,8 @@ extern "C" int krr_nrc_set_params(krr_nrc *n, int32_t which, const float *h_src,
     KRR_CUDA(cudaDeviceSynchronize());
     KRR_CUDA(cudaMemcpy(dst, h_src, total * 4, cudaMemcpyHostToDevice));
     k_to_bf16<<<grid_for(total), kThreads>>>(dst, bdst, total);
-    if (which == 0) KRR_TRY(pack_weights(n, 0));
+    KRR_TRY(reset_ema(n, 0));   // the inference copy restarts from the new parameters
+    KRR_TRY(pack_weights(n, 0));
     KRR_CUDA(cudaMemset(n->err + 1, 0, sizeof(uint32_t)));   // new parameters: not diverged
     KRR_CUDA(cudaDeviceSynchronize());
     return KRR_OK;
@@ -760,10 +825,11 @@ extern "C" int krr_nrc_status(krr_nrc *n, uint32_t *out_flags, int32_t *out_dive
 }
 
 // Checkpoint file: a fixed header, then the FP32 arrays in this order: MLP
-// weights, their Adam moments m and v, hash table, its moments m and v.
+// weights, their Adam moments m and v, hash table, its moments m and v; with
+// cfg.ema_decay > 0 then the inference copy's MLP weights and table.
 namespace {
 struct NrcFileHeader {
-    char magic[8];              // "KRRNRC01"
+    char magic[8];              // "KRRNRC02"
     uint32_t header_bytes;      // sizeof(NrcFileHeader)
     uint32_t config_bytes;      // sizeof(krr_nrc_config)
     krr_nrc_config cfg;
@@ -774,7 +840,7 @@ struct NrcFileHeader {
     uint32_t diverged;
     uint32_t reserved;
 };
-constexpr char kNrcMagic[8] = {'K', 'R', 'R', 'N', 'R', 'C', '0', '1'};
+constexpr char kNrcMagic[8] = {'K', 'R', 'R', 'N', 'R', 'C', '0', '2'};
 
 bool same_structure(const krr_nrc_config &a, const krr_nrc_config &b) {
     return a.n_levels == b.n_levels && a.features_per_level == b.features_per_level &&
@@ -804,9 +870,11 @@ extern "C" int krr_nrc_save(const krr_nrc *n, const char *path) {
     if (!f) return fail(KRR_ERR_INVALID_ARGUMENT, "krr_nrc_save: cannot open %s", path);
     bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1;
     std::vector<float> buf;
-    const float *arrays[6] = {n->w_master, n->w_m, n->w_v, n->table_master, n->table_m, n->table_v};
-    for (int k = 0; k < 6 && ok; ++k) {
-        const size_t cnt = (size_t)(k < 3 ? h.n_params : h.n_table_values);
+    const float *arrays[8] = {n->w_master, n->w_m, n->w_v, n->table_master, n->table_m, n->table_v,
+                              n->ema_w, n->ema_table};
+    const int n_arrays = n->ema_w ? 8 : 6;
+    for (int k = 0; k < n_arrays && ok; ++k) {
+        const size_t cnt = (size_t)(k < 3 || k == 6 ? h.n_params : h.n_table_values);
         buf.resize(cnt);
         if (cudaMemcpy(buf.data(), arrays[k], cnt * 4, cudaMemcpyDeviceToHost) != cudaSuccess) {
             std::fclose(f);
@@ -838,20 +906,26 @@ extern "C" int krr_nrc_load(krr_nrc *n, const char *path) {
     }
     KRR_CUDA(cudaDeviceSynchronize());
     std::vector<float> buf;
-    float *arrays[6] = {n->w_master, n->w_m, n->w_v, n->table_master, n->table_m, n->table_v};
-    for (int k = 0; k < 6; ++k) {
-        const size_t cnt = (size_t)(k < 3 ? h.n_params : h.n_table_values);
+    // the inference copy is read into the cache's own when both keep one
+    float *arrays[8] = {n->w_master, n->w_m, n->w_v, n->table_master, n->table_m, n->table_v,
+                        n->ema_w, n->ema_table};
+    const int n_arrays = h.cfg.ema_decay > 0.f ? 8 : 6;
+    for (int k = 0; k < n_arrays; ++k) {
+        const size_t cnt = (size_t)(k < 3 || k == 6 ? h.n_params : h.n_table_values);
         buf.resize(cnt);
         if (std::fread(buf.data(), 4, cnt, f) != cnt) {
             std::fclose(f);
             return fail(KRR_ERR_INVALID_ARGUMENT, "krr_nrc_load: %s is truncated", path);
         }
-        KRR_CUDA(cudaMemcpy(arrays[k], buf.data(), cnt * 4, cudaMemcpyHostToDevice));
+        if (arrays[k]) KRR_CUDA(cudaMemcpy(arrays[k], buf.data(), cnt * 4, cudaMemcpyHostToDevice));
     }
     std::fclose(f);
     // training settings (learning rate, batch, stride, ...) and the scene box
-    // the table was trained over come with the checkpoint
+    // the table was trained over come with the checkpoint; whether the cache
+    // keeps an inference copy stays the cache's own setting
+    const float own_decay = n->cfg.ema_decay;
     n->cfg = h.cfg;
+    n->cfg.ema_decay = n->ema_w ? (h.cfg.ema_decay > 0.f ? h.cfg.ema_decay : own_decay) : 0.f;
     if (n->cfg.train_pixel_stride < 1) n->cfg.train_pixel_stride = 1;
     for (int a = 0; a < 3; ++a) {
         n->grid.lo[a] = h.cfg.scene_lo[a];
@@ -868,6 +942,12 @@ extern "C" int krr_nrc_load(krr_nrc *n, const char *path) {
     KRR_CUDA(cudaMemset(n->table_grad, 0, (size_t)h.n_table_values * 4));
     k_to_bf16<<<grid_for(h.n_params), kThreads>>>(n->w_master, n->weights, h.n_params);
     k_to_bf16<<<grid_for(h.n_table_values), kThreads>>>(n->table_master, n->table, h.n_table_values);
+    if (n->ema_w && h.cfg.ema_decay > 0.f) {
+        k_to_bf16<<<grid_for(h.n_params), kThreads>>>(n->ema_w, n->ema_weights, h.n_params);
+        k_to_bf16<<<grid_for(h.n_table_values), kThreads>>>(n->ema_table, n->ema_table_bf, h.n_table_values);
+    } else {
+        KRR_TRY(reset_ema(n, 0));
+    }
     KRR_TRY(pack_weights(n, 0));
     KRR_CUDA(cudaDeviceSynchronize());
     return KRR_OK;

@@ -18,7 +18,7 @@ from ._lib import check
 CONFIG_KEYS = ("n_levels", "features_per_level", "log2_table_size", "base_resolution",
                "max_resolution", "hidden_layers", "learning_rate", "beta1", "beta2", "epsilon",
                "loss_scale", "batch_size", "train_pixel_stride", "seed", "tensor_cores",
-               "termination_spread")
+               "termination_spread", "ema_decay")
 
 
 RECORD_FLOATS = 13   # position 3, normal 3, roughness 1, albedo 3, outgoing direction 3
@@ -87,7 +87,7 @@ class NeuralRadianceCache:
 
     def params(self, which: int) -> np.ndarray:
         i = self.info()
-        n = i.n_params_mlp if which == 0 else i.n_table_entries * 2
+        n = i.n_params_mlp if which % 2 == 0 else i.n_table_entries * 2
         out = np.empty(n, np.float32)
         check(self.lib.krr_nrc_get_params(self._h, which, out.ctypes.data, n), "get_params")
         return out

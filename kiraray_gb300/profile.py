@@ -4,6 +4,9 @@ and single-kernel captures); prints the device time of each repetition.
     python -m kiraray_gb300.profile trace [--reps 4] [--builder 0]
         closest hits of the 1920x1080 camera rays of the 10.9M-triangle scene
         (BVH builder as krr_set_bvh_builder)
+    python -m kiraray_gb300.profile cache [--configs JSON] [--res 480x270]
+        relMSE curves (2k-32k samples per pixel, 8 replica views per launch)
+        of the neural-cache tracer on the large scene for cache configurations
     python -m kiraray_gb300.profile update [--reps 5]
         an instance update of the large scene (re-flatten + BVH refit) against
         a full BVH rebuild, host wall time per call
@@ -105,12 +108,48 @@ def frame(res: str, views: int, nrc: bool, frames: int, scene: str = "large", se
             "device_errors": pt.device_errors()}
 
 
+def cache_curves(configs: list, res: str = "480x270", copies: int = 8, spp: int = 32768) -> list:
+    """relMSE against a 65,536-spp reference of the neural-cache tracer on
+    the large scene (seed 3) at 2k-32k samples per pixel, one entry per cache
+    configuration (keyword arguments of NeuralRadianceCache)."""
+    from . import scenes
+    from .convergence import render_reference_views, time_to_error_views
+    from .nrc import NeuralRadianceCache
+    from .wavefront import WavefrontPathTracer
+
+    w, h = (int(x) for x in res.split("x"))
+    sc = scenes.large_scene(width=w, height=h, seed=3)
+    plain = WavefrontPathTracer({"max_depth": 8}, seed=3)
+    plain.set_scene(sc)
+    ref = render_reference_views(plain, sc, copies, 65536 // copies)
+    tris = sc.world_triangles().reshape(-1, 3)
+    out = []
+    for cfg in configs:
+        pt = WavefrontPathTracer({"max_depth": 8}, seed=3)
+        pt.set_scene(sc)
+        pt.set_nrc(NeuralRadianceCache(tris.min(0), tris.max(0), seed=3, **cfg), train=True)
+        r = time_to_error_views(pt, sc, ref, copies, target=0.0, max_frames=spp // copies,
+                                check_every=64, max_seconds=120)
+        marks = {}
+        for n, e in zip(r["curve"]["timesteps"], r["curve"]["data"]):
+            for m in (2048, 4096, 8192, 16384, 32768):
+                if n >= m and m not in marks:
+                    marks[m] = round(e, 5)
+        out.append({"config": cfg, "ms_per_frame": round(r["ms_per_frame"], 3), "relmse_at_spp": marks})
+        pt.close()
+    return out
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     sub = ap.add_subparsers(dest="cmd", required=True)
     t = sub.add_parser("trace")
     t.add_argument("--reps", type=int, default=4)
     t.add_argument("--builder", type=int, default=2, choices=[0, 1, 2])
+    c = sub.add_parser("cache")
+    c.add_argument("--configs", default='[{"termination_spread": 0.0}]',
+                   help="JSON list of cache configurations")
+    c.add_argument("--res", default="480x270")
     u = sub.add_parser("update")
     u.add_argument("--reps", type=int, default=5)
     f = sub.add_parser("frame")
@@ -127,6 +166,8 @@ def main() -> None:
         r = trace(a.reps, a.builder)
     elif a.cmd == "update":
         r = update(a.reps)
+    elif a.cmd == "cache":
+        r = cache_curves(json.loads(a.configs), a.res)
     else:
         r = frame(a.res, a.views, a.nrc, a.frames, a.scene, a.seed)
     print(json.dumps(r))

@@ -45,6 +45,44 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
 
 
+def test_moving_average_for_queries(krr_lib, cuda):
+    """ema_decay d: after each Adam step the queries' copy of the parameters
+    becomes d e + (1 - d) w, and queries read that copy (the oracle's forward
+    on it), while training keeps reading the parameters themselves."""
+    lo, hi = (-1, -1, -1), (1, 1, 1)
+    cache = NeuralRadianceCache(lo, hi, ema_decay=0.75, **SMALL)
+    rec = _records(3000, 5)
+    r, t = torch.from_numpy(rec).cuda(), torch.from_numpy(_targets(rec)).cuda()
+    for which in (0, 1):
+        assert np.array_equal(cache.params(which), cache.params(which + 2))
+    e = [cache.params(0).astype(np.float64), cache.params(1).astype(np.float64)]
+    for s in range(12):
+        cache.train_step(r, t)
+        for which in (0, 1):
+            w = cache.params(which).astype(np.float64)
+            e[which] = 0.75 * e[which] + 0.25 * w
+            got = cache.params(which + 2)
+            assert np.allclose(got, e[which], rtol=1e-5, atol=1e-8), (s, which)
+    got = cache.query(r).cpu().numpy()
+    info = cache.info()
+    grid = R.Grid(info, lo, hi, 1 << cache.cfg.log2_table_size)
+    mlp = R.Mlp(cache.params(2).astype(np.float64), cache.cfg.hidden_layers + 1)
+    X0, _ = R.encode(grid, cache.params(3).astype(np.float64), rec)
+    want, _ = R.forward(mlp, X0)
+    assert _rel(got, want) < 2e-2
+    # the average lags the trained parameters: their forward differs
+    mlp_w = R.Mlp(cache.params(0).astype(np.float64), cache.cfg.hidden_layers + 1)
+    X0w, _ = R.encode(grid, cache.params(1).astype(np.float64), rec)
+    trained, _ = R.forward(mlp_w, X0w)
+    assert _rel(got, trained) > 1.5 * _rel(got, want)
+    # set_params restarts the average from the new values
+    cache.set_params(0, cache.params(0))
+    assert np.array_equal(cache.params(0), cache.params(2))
+    plain = NeuralRadianceCache(lo, hi, **SMALL)
+    with pytest.raises(Exception):
+        plain.params(2)
+
+
 def test_forward_matches_oracle(krr_lib, cuda):
     lo, hi = (-1, -1, -1), (1, 1, 1)
     cache = NeuralRadianceCache(lo, hi, **SMALL)

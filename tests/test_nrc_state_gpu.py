@@ -58,6 +58,29 @@ def test_checkpoint_round_trip(krr_lib, cuda, tmp_path):
     assert a.info().step == b.info().step == 8
 
 
+def test_checkpoint_keeps_the_moving_average(krr_lib, cuda, tmp_path):
+    """With a moving average for the queries the checkpoint carries it: the
+    loaded cache answers queries bit for bit like the saved one; a cache
+    without one loads the same file and queries the trained parameters."""
+    lo, hi = (-1, -1, -1), (1, 1, 1)
+    rec = torch.from_numpy(_records(4096, 43)).cuda()
+    tgt = torch.from_numpy(_targets(rec.cpu().numpy())).cuda()
+    a = NeuralRadianceCache(lo, hi, seed=1, ema_decay=0.9, **SMALL)
+    _train(a, rec, tgt, 6)
+    path = tmp_path / "cache_ema.bin"
+    a.save(path)
+    b = NeuralRadianceCache(lo, hi, seed=2, ema_decay=0.5, **SMALL)
+    b.load(path)
+    for which in (0, 1, 2, 3):
+        assert np.array_equal(a.params(which).view(np.uint32), b.params(which).view(np.uint32)), which
+    q = torch.from_numpy(_records(2000, 44)).cuda()
+    assert np.array_equal(a.query(q).cpu().numpy().view(np.uint32), b.query(q).cpu().numpy().view(np.uint32))
+    c = NeuralRadianceCache(lo, hi, seed=2, **SMALL)
+    c.load(path)
+    for which in (0, 1):
+        assert np.array_equal(a.params(which).view(np.uint32), c.params(which).view(np.uint32))
+
+
 def test_checkpoint_rejects_another_shape(krr_lib, cuda, tmp_path):
     a = NeuralRadianceCache((0, 0, 0), (1, 1, 1), **SMALL)
     path = tmp_path / "cache.bin"
