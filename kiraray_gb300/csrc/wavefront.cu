@@ -32,7 +32,9 @@ int launch_medium_sample(krr_wf *wf, int depth, cudaStream_t s);
 int launch_medium_scatter(krr_wf *wf, int depth, cudaStream_t s, bool to_tracker = false);
 int launch_trace_shadow_tr(krr_wf *wf, cudaStream_t s);
 int launch_shadow_tracker(krr_wf *wf, cudaStream_t s);
+int launch_shadow_split(krr_wf *wf, cudaStream_t s, bool media_candidates);
 bool split_shadows(const krr_wf *wf);
+int ensure_split_buffers(krr_wf *wf);
 }
 
 struct DevCamera {
@@ -117,7 +119,9 @@ struct krr_wf {
     float4 *qbuf[Q_COUNT] = {};
     int32_t *d_counts = nullptr;   // [0..7] queue sizes, [8] error flags, [9-10] cache
                                    // batches, [11] ratio-tracked shadow rays, [12-15]
-                                   // scatter items per material class
+                                   // scatter items per material class, [16] shadow
+                                   // rays of scenes with media (split routing)
+    float4 *media_shadow = nullptr;   // [kShadowCh][qcap], split routing only
     float4 *hits = nullptr;
     uint8_t *occluded = nullptr;
     int32_t *scatter_lists = nullptr;   // [2][n] scatter items by material class
@@ -149,6 +153,7 @@ struct krr_wf {
     int32_t *nrc_b_count() const { return d_counts + 10; }
     int32_t *shadow_tracked_count() const { return d_counts + 11; }
     int32_t *scatter_class_counts() const { return d_counts + 12; }
+    int32_t *media_shadow_count() const { return d_counts + 16; }
     uint32_t *err() const { return reinterpret_cast<uint32_t *>(d_counts + 8); }
     WfConst consts() const {
         WfConst c;
@@ -1751,6 +1756,7 @@ void free_queues(krr_wf *wf) {
     cudaFree(wf->d_counts); wf->d_counts = nullptr;
     cudaFree(wf->hits); wf->hits = nullptr;
     cudaFree(wf->occluded); wf->occluded = nullptr;
+    cudaFree(wf->media_shadow); wf->media_shadow = nullptr;
     cudaFree(wf->scatter_lists); wf->scatter_lists = nullptr;
     cudaFree(wf->work_counts); wf->work_counts = nullptr;
     cudaFree(wf->ps.L); cudaFree(wf->ps.pixel); cudaFree(wf->ps.rng);
@@ -1875,6 +1881,7 @@ extern "C" int krr_wf_set_params(krr_wf *wf, const krr_wf_params *params) {
     KRR_CHECK_ARG(params->max_depth >= 0 && params->spp >= 1, "bad parameters");
     wf->params = *params;
     wf->medium = wf->params.enable_medium && wf->scene.n_media > 0;
+    KRR_TRY(ensure_split_buffers(wf));
     return sync_part_depths(wf);
 }
 
@@ -2284,6 +2291,7 @@ extern "C" int krr_wf_set_scenes(krr_wf *wf, const krr_scene_desc *scenes, int32
     wf->scene = s;   // rebuild_bvh reads the uploaded instances and updates parts and radii
     KRR_TRY(rebuild_bvh(wf, st));
     wf->has_scene = true;
+    KRR_TRY(ensure_split_buffers(wf));
     wf->medium = wf->params.enable_medium && wf->scene.n_media > 0;
     KRR_TRY(fill_pixel_parts(wf, st));
     KRR_CUDA(cudaStreamSynchronize(st));
@@ -2335,8 +2343,8 @@ static int set_layout(krr_wf *wf, std::vector<DevView> layout) {
     wf->qcap = wf->wave > 0 ? std::min(wf->wave, n) : n;
     for (int k = 0; k < Q_COUNT; ++k)
         KRR_CUDA(cudaMalloc(&wf->qbuf[k], (size_t)kChannels[k] * wf->qcap * sizeof(float4)));
-    KRR_CUDA(cudaMalloc(&wf->d_counts, 16 * sizeof(int32_t)));
-    KRR_CUDA(cudaMemset(wf->d_counts, 0, 16 * sizeof(int32_t)));
+    KRR_CUDA(cudaMalloc(&wf->d_counts, 32 * sizeof(int32_t)));
+    KRR_CUDA(cudaMemset(wf->d_counts, 0, 32 * sizeof(int32_t)));
     KRR_CUDA(cudaMalloc(&wf->hits, wf->qcap * sizeof(float4)));
     KRR_CUDA(cudaMalloc(&wf->occluded, wf->qcap));
     KRR_CUDA(cudaMalloc(&wf->scatter_lists, 2 * wf->qcap * sizeof(int32_t)));
@@ -2347,6 +2355,7 @@ static int set_layout(krr_wf *wf, std::vector<DevView> layout) {
     wf->grid = stage_grid(wf, wf->n);
     KRR_TRY(fill_pixel_parts(wf, 0));
     KRR_CUDA(cudaDeviceSynchronize());
+    KRR_TRY(ensure_split_buffers(wf));
     return alloc_nrc_buffers(wf);
 }
 
@@ -2652,10 +2661,10 @@ extern "C" int krr_wf_handle_miss(krr_wf *wf, void *stream) {
 }
 
 // generateScatterRays; with `to_tracker` the shadow rays of scenes with
-// media go to the transmittance tracker's queue (split_shadows()).
+// media go to their own queue for k_shadow_split (split_shadows()).
 static int scatter_stage(krr_wf *wf, int depth, cudaStream_t st, bool to_tracker) {
     int cur = depth & 1;
-    const Queue tracked = to_tracker ? Queue{wf->qbuf[Q_MEDIUM_SAMPLE], (int32_t)wf->qcap, wf->shadow_tracked_count()}
+    const Queue tracked = to_tracker ? Queue{wf->media_shadow, (int32_t)wf->qcap, wf->media_shadow_count()}
                                      : Queue{};
     KRR_CUDA(cudaMemsetAsync(wf->scatter_class_counts(), 0, 4 * sizeof(int32_t), st));
     k_scatter_classify<<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->q(Q_SCATTER), wf->ps,
@@ -2820,7 +2829,7 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
     // rays of the scenes without media are traced with the next bounce's
     // rays too; those of the scenes with media go to the tracker
     // (split_shadows()).
-    const bool split = split_shadows(wf);
+    const bool split = split_shadows(wf) && wf->media_shadow;
     const bool fuse = (wf->params.nee && !wf->medium) || split;
     for (int s = 0; s < wf->params.spp; ++s) {
         for (int64_t p0 = 0; p0 < wf->n; p0 += wf->qcap) {
@@ -2837,10 +2846,16 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
                     KRR_TRY(krr_wf_handle_miss(wf, stream));
                 }
                 if (depth == loop_depth(wf)) break;
-                if (split) KRR_CUDA(cudaMemsetAsync(wf->shadow_tracked_count(), 0, sizeof(int32_t), st));
+                if (split) {
+                    KRR_CUDA(cudaMemsetAsync(wf->shadow_tracked_count(), 0, sizeof(int32_t), st));
+                    KRR_CUDA(cudaMemsetAsync(wf->media_shadow_count(), 0, sizeof(int32_t), st));
+                }
                 if (wf->medium) KRR_TRY(launch_medium_scatter(wf, depth, st, split));
                 KRR_TRY(scatter_stage(wf, depth, st, split));
-                if (split) KRR_TRY(launch_shadow_tracker(wf, st));
+                if (split) {
+                    KRR_TRY(launch_shadow_split(wf, st, true));
+                    KRR_TRY(launch_shadow_tracker(wf, st));
+                }
                 traced = fuse;
                 if (fuse) KRR_TRY(trace_shadow_and_next(wf, depth, st));
                 else if (wf->params.nee) KRR_TRY(krr_wf_trace_shadow(wf, stream));
@@ -3183,14 +3198,25 @@ static Queue tracked_queue(krr_wf *wf) {
 
 // A pass of several scenes of which some have media and some do not: the
 // shadow rays of the scenes without media are traced with the next bounce's
-// rays in one launch (as in a pass without media), those of the scenes with
-// media go straight to the tracker.  A pixel's shadow rays all go one way,
-// so each pixel gets the same terms in the same order.
+// rays in one launch (as in a pass without media); those of the scenes with
+// media go through k_shadow_split from a queue of their own (surface
+// vertices) or straight to the tracker (medium vertices, which start inside
+// a medium).  A pixel's shadow rays all go one way, so each pixel gets the
+// same terms in the same order.
 bool split_shadows(const krr_wf *wf) {
     if (!wf->medium || !wf->params.nee || wf->n_parts <= 1) return false;
     bool with = false, without = false;
     for (const DevScenePart &P : wf->parts) (P.has_media ? with : without) = true;
     return with && without;
+}
+
+// The queue of media-scene shadow rays for split routing, allocated with the
+// queues once the scenes and the parameters call for it (never inside a
+// frame, so that frames can be captured).
+int ensure_split_buffers(krr_wf *wf) {
+    if (wf->media_shadow || wf->qcap <= 0 || !split_shadows(wf)) return KRR_OK;
+    KRR_CUDA(cudaMalloc(&wf->media_shadow, (size_t)kShadowCh * wf->qcap * sizeof(float4)));
+    return KRR_OK;
 }
 
 int launch_medium_scatter(krr_wf *wf, int depth, cudaStream_t st, bool to_tracker) {
@@ -3207,18 +3233,28 @@ int launch_medium_scatter(krr_wf *wf, int depth, cudaStream_t st, bool to_tracke
 // own counter and ratio-tracked by k_shadow_tr.
 int launch_trace_shadow_tr(krr_wf *wf, cudaStream_t st) {
     static_assert(kMediumSampleCh >= kShadowCh, "tracked shadow rays need five planes");
+    KRR_CUDA(cudaMemsetAsync(wf->shadow_tracked_count(), 0, sizeof(int32_t), st));
+    KRR_TRY(launch_shadow_split(wf, st, false));
+    return launch_shadow_tracker(wf, st);
+}
+
+// k_shadow_split over the shadow queue, or over the media-scene shadow rays
+// of split routing; the rays it does not finish are appended to the
+// tracker's queue.
+int launch_shadow_split(krr_wf *wf, cudaStream_t st, bool media_candidates) {
     const Queue tracked = tracked_queue(wf);
-    KRR_CUDA(cudaMemsetAsync(tracked.count, 0, sizeof(int32_t), st));
+    const Queue from = media_candidates ? Queue{wf->media_shadow, (int32_t)wf->qcap, wf->media_shadow_count()}
+                                        : wf->q(Q_SHADOW);
     int *terr = wf->accel.d_scratch + 4;
     const InstancedView iv = wf->accel.levels == 2 ? instanced_view(&wf->accel) : InstancedView{};
     if (wf->accel.node_format == 1)
         k_shadow_split<1><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
-                                                          wf->q(Q_SHADOW), tracked, wf->ps, wf->err(), terr);
+                                                          from, tracked, wf->ps, wf->err(), terr);
     else
         k_shadow_split<0><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
-                                                          wf->q(Q_SHADOW), tracked, wf->ps, wf->err(), terr);
+                                                          from, tracked, wf->ps, wf->err(), terr);
     KRR_CUDA(cudaGetLastError());
-    return launch_shadow_tracker(wf, st);
+    return KRR_OK;
 }
 
 // Ratio tracking of the shadow rays in the tracker's queue.

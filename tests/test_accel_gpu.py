@@ -460,3 +460,16 @@ def test_two_level_structure_matches_the_instanced_oracle(krr_lib, cuda):
     _assert_bits_equal(_gpu_closest(acc, rays), O.trace_instanced(geos, moved, inv2, rays),
                        "two-level closest after an update")
     assert acc.device_errors() == 0
+    # a stack limit below the two levels' needs cuts rays off (flag raised,
+    # t = NaN and a miss); the others keep their exact hits
+    want2 = O.trace_instanced(geos, moved, inv2, rays)
+    acc.set_stack_limit(3)
+    got = _gpu_closest(acc, rays)
+    assert acc.device_errors() & 1
+    cut = np.isnan(got[:, 0])
+    assert 0 < cut.sum() < rays.shape[0]
+    assert np.all(got[cut, 3].view(np.uint32) == 0xFFFFFFFF)
+    _assert_bits_equal(got[~cut], want2[~cut], "two-level rays within the stack limit")
+    acc.set_stack_limit(48)
+    _assert_bits_equal(_gpu_closest(acc, rays), want2, "two-level default stack limit")
+    assert acc.device_errors() == 0
