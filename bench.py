@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--views", type=int, default=64,
                     help="batched-views run: number of views (0 = skip)")
     ap.add_argument("--view-frames", type=int, default=5)
+    ap.add_argument("--conv", type=int, default=0,
+                    help="1: plain tracer's time to relMSE 0.01 on the Cornell and volume boxes")
+    ap.add_argument("--conv-ref-spp", type=int, default=65536)
     ap.add_argument("--two-level", type=int, default=1,
                     help="1: also the scene as a two-level structure (memory, Mrays/s, updates)")
     ap.add_argument("--frame", type=int, default=1,
@@ -611,6 +614,43 @@ def batched_views(args):
 NRC_TUNED = {"learning_rate": 3e-3, "batch_size": 16384, "termination_spread": 0.05}
 
 
+def plain_convergence(args, frames):
+    """Plain tracer's time to relMSE 0.01 on the Cornell box (512x512, max
+    depth 5) and the volume box (1024x1024, max depth 16) against an
+    FP64-accumulated reference of the same tracer (--conv-ref-spp samples per
+    pixel for the Cornell box, a quarter of that for the volume box), with
+    the CPU restatement's time estimated as the samples per pixel the GPU
+    needed times its measured frame time (`config_frames`)."""
+    if not args.conv:
+        return None
+    import torch
+    from kiraray_gb300 import scenes
+    from kiraray_gb300.convergence import render_reference_views, time_to_error_views
+    from kiraray_gb300.wavefront import WavefrontPathTracer
+
+    out = {}
+    for name, sc, copies, ref_spp in (("cornell_box_512", scenes.cornell_box(512, 512, max_depth=5), 4,
+                                       args.conv_ref_spp),
+                                      ("volume_box_1024", scenes.volume_box(1024, 1024), 1,
+                                       max(1, args.conv_ref_spp // 4))):
+        pt = WavefrontPathTracer({"max_depth": sc.max_depth}, seed=sc.seed)
+        pt.set_scene(sc)
+        t0 = time.perf_counter()
+        ref = render_reference_views(pt, sc, copies, max(1, ref_spp // copies))
+        torch.cuda.synchronize()
+        ref_s = time.perf_counter() - t0
+        res = time_to_error_views(pt, sc, ref, copies, target=0.01, max_frames=max(1, ref_spp // copies // 4),
+                                  check_every=max(1, 64 // copies), max_seconds=120)
+        cpu_ms = (frames or {}).get(name, {}).get("cpu_frame_ms_est")
+        out[name] = {"reference_spp": max(1, ref_spp // copies) * copies, "reference_seconds": round(ref_s, 2),
+                     "gpu_seconds": res["seconds"], "spp": res["spp"], "final_relmse": res["final_error"],
+                     "gpu_ms_per_sample": round(res["ms_per_frame"] / copies, 4),
+                     "cpu_seconds_est": (round(res["spp"] * cpu_ms / 1e3, 1)
+                                         if res["seconds"] and cpu_ms else None)}
+        del pt
+    return out
+
+
 def time_to_relmse(args):
     """Time to relMSE 0.01 of the plain tracer and of the neural-cache tracer
     on the large scene (max depth 8), against an FP64-accumulated reference
@@ -848,6 +888,7 @@ def run_ours(args, rank, world, local):
     two = two_level(sc, {"primary": rays0, "bounce": rays1}, dev) if args.two_level else None
     batched = batched_views(args)
     frames = config_frames(args)
+    conv = plain_convergence(args, frames)
     nrc = time_to_relmse(args)
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world,
@@ -900,6 +941,7 @@ def run_ours(args, rank, world, local):
         "batched_views": batched,
         "config_frames": frames,
         "time_to_relmse": nrc,
+        "plain_time_to_relmse": conv,
     }
     l2 = line["roofline"]["l2"]
     l2["frac"] = l2["achieved_gbs"] / l2["peak_gbs"] if l2["achieved_gbs"] else None
