@@ -179,10 +179,10 @@ class ClockSampler:
 
 def profile_figures():
     """Per-launch figures of the traversal kernel from the committed ncu
-    summary (profiles/trace_closest_large_scene.md): DRAM bytes, L2 bytes
-    and executed warp instructions of the camera-ray launch, keyed lines
-    `name: value`."""
-    p = ROOT / "profiles" / "trace_closest_large_scene.md"
+    counters (profiles/trace_closest_large_scene_figures.txt): DRAM bytes, L2
+    bytes and executed warp instructions of the camera-ray launch, keyed
+    lines `name: value`."""
+    p = ROOT / "profiles" / "trace_closest_large_scene_figures.txt"
     out = {}
     if not p.exists():
         return out

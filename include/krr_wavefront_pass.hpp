@@ -9,8 +9,8 @@
 // src/util/check.h:8-51).
 //
 // A host binds it into its own RenderPass hierarchy by holding one
-// krr::WavefrontPass and forwarding its virtuals; INTEGRATION.md shows the
-// binding.  Only the C ABI crosses the library boundary.
+// krr::WavefrontPass and forwarding its virtuals (resize, setScene,
+// beginFrame, render).  Only the C ABI crosses the library boundary.
 #pragma once
 
 #include <stdexcept>

@@ -1,5 +1,6 @@
-// The RenderPass binding a maintainer adds to the host application (the
-// same class as in INTEGRATION.md), compiled here against host_stub.h.
+// The RenderPass binding a maintainer adds to the host application: a
+// RenderPass subclass registered by name that holds a krr::WavefrontPass and
+// forwards its virtuals; compiled here against host_stub.h.
 #pragma once
 
 #include "host_stub.h"

@@ -1,4 +1,4 @@
-"""The C++ RenderPass binding of INTEGRATION.md (tests/integration/
+"""The C++ RenderPass binding a host application adds (tests/integration/
 wavefront_gb300_pass.h over include/krr_wavefront_pass.hpp), compiled with
 g++ against stand-ins for the host's RenderPass types and linked to
 libkrr_gb300.so.  On the CPU: the pass is made by name from its JSON
