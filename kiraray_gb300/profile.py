@@ -1,9 +1,10 @@
 """Fixed workloads for profiling the pass under a profiler (ncu launch lists
 and single-kernel captures); prints the device time of each repetition.
 
-    python -m kiraray_gb300.profile trace [--reps 4] [--builder 0]
+    python -m kiraray_gb300.profile trace [--reps 4] [--builder 0] [--levels 2]
         closest hits of the 1920x1080 camera rays of the 10.9M-triangle scene
-        (BVH builder as krr_set_bvh_builder)
+        (BVH builder as krr_set_bvh_builder; --levels 2: the two-level
+        structure, per-geometry trees and an instance tree)
     python -m kiraray_gb300.profile cache [--configs JSON] [--res 480x270]
         relMSE curves (2k-32k samples per pixel, 8 replica views per launch)
         of the neural-cache tracer on the large scene for cache configurations
@@ -35,17 +36,31 @@ def _timed(fn) -> float:
     return e0.elapsed_time(e1)
 
 
-def trace(reps: int, builder: int = 2) -> dict:
+def trace(reps: int, builder: int = 2, levels: int = 1) -> dict:
+    import numpy as np
+
     from . import scenes
     from .accel import Accel, set_builder
 
     sc = scenes.large_scene()
     set_builder(builder)
-    acc = Accel(sc.world_triangles())
+    if levels == 2:
+        # each mesh geometry once, an instance tree over them
+        geoms, key_of, inst = [], {}, []
+        for mi, xf in sc.instances:
+            m = sc.meshes[mi]
+            key = (id(m.positions), id(m.indices))
+            if key not in key_of:
+                key_of[key] = len(geoms)
+                geoms.append(np.asarray(m.positions, np.float32)[np.asarray(m.indices)].reshape(-1, 9))
+            inst.append((key_of[key], np.asarray(xf, np.float32)))
+        acc = Accel.instanced(geoms, inst)
+    else:
+        acc = Accel(sc.world_triangles())
     set_builder(2)
     rays = torch.from_numpy(scenes.pinhole_rays(sc)).cuda()
     ms = [_timed(lambda: acc.trace_closest(rays)) for _ in range(reps)]
-    return {"workload": "trace", "rays": int(rays.shape[0]), "ms": ms}
+    return {"workload": "trace", "levels": levels, "rays": int(rays.shape[0]), "ms": ms}
 
 
 def update(reps: int) -> dict:
@@ -146,6 +161,7 @@ def main() -> None:
     t = sub.add_parser("trace")
     t.add_argument("--reps", type=int, default=4)
     t.add_argument("--builder", type=int, default=2, choices=[0, 1, 2])
+    t.add_argument("--levels", type=int, default=1, choices=[1, 2])
     c = sub.add_parser("cache")
     c.add_argument("--configs", default='[{"termination_spread": 0.0}]',
                    help="JSON list of cache configurations")
@@ -163,7 +179,7 @@ def main() -> None:
     from .build import build
     build()
     if a.cmd == "trace":
-        r = trace(a.reps, a.builder)
+        r = trace(a.reps, a.builder, a.levels)
     elif a.cmd == "update":
         r = update(a.reps)
     elif a.cmd == "cache":
