@@ -436,6 +436,8 @@ def test_two_level_structure_matches_the_instanced_oracle(krr_lib, cuda):
     instances move (only the instance level is rebuilt)."""
     from tests.test_oracle import _instanced_scene
     geos, insts = _instanced_scene(seed=5, n_inst=60)
+    # an identity instance: its object-space ray is the world ray bit for bit
+    insts.append((1, np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 0]], np.float32)))
     mask = np.ones(len(insts), np.uint8)
     mask[::7] = 0
     acc = Accel.instanced(geos, insts, mask)
