@@ -920,7 +920,9 @@ __global__ void k_scatter_classify(DevScene s, Queue scat, PixelState ps, float 
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 4)
+// Three blocks per SM (80 registers, 104 bytes spilled): 0.8 % faster per
+// 1080p frame than four blocks at 64 registers (236 bytes spilled).
+__global__ void __launch_bounds__(kThreads, 3)
 k_scatter_process(DevScene s, Queue scat, const int32_t *__restrict__ lists,
                   const int32_t *__restrict__ counts, Queue next, Queue shadow, Queue tracked,
                   PixelState ps, int nee, float rr, uint32_t *err) {
