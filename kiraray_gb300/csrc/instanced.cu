@@ -43,8 +43,10 @@ constexpr int kInstThreads = 128;
 constexpr uint32_t kTriGroupBit = 0x80000000u;   // stack entry: pending leaf group
 constexpr uint32_t kReturnBit = 0x40000000u;     // stack entry: back to the world ray
 
+// Eight blocks per SM (64 registers, the mixed variant spills 96 bytes):
+// 1.31 against 1.39 ms per 2.07M camera rays at six blocks (80 registers).
 template <int MODE, int FMT>
-__global__ void __launch_bounds__(kInstThreads, 6)
+__global__ void __launch_bounds__(kInstThreads, 8)
 k_trace_two_level_p(InstancedView v, TraceLaunch L) {
     const int lane = threadIdx.x & 31;
     const int64_t n_any = MODE == 2 ? min((int64_t)*L.d_any_count, L.n) : 0;
