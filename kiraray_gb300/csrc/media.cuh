@@ -37,16 +37,27 @@ __device__ __forceinline__ float density_at(const DevMedium &m, V3 p) {
     float u = fx - ix, v = fy - iy, w = fz - iz;
     int x0 = (int)ix, y0 = (int)iy, z0 = (int)iz;
     float c[2][2][2];
+    const uint32_t *pairs = reinterpret_cast<const uint32_t *>(m.density);
 #pragma unroll
-    for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b)
 #pragma unroll
-        for (int b = 0; b < 2; ++b)
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-                int x = x0 + a, y = y0 + b, z = z0 + e;
-                bool in = x >= 0 && y >= 0 && z >= 0 && x < m.nx && y < m.ny && z < m.nz;
-                c[a][b][e] = in ? half_to_float(__ldg(m.density + ((size_t)z * m.ny + y) * m.nx + x)) : 0.f;
+        for (int e = 0; e < 2; ++e) {
+            const int y = y0 + b, z = z0 + e;
+            float v0 = 0.f, v1 = 0.f;
+            if (y >= 0 && z >= 0 && y < m.ny && z < m.nz) {
+                const size_t row = ((size_t)z * m.ny + y) * m.nx;
+                if (x0 >= 0 && x0 < m.nx) {
+                    // the pair holds 0 for the +x neighbour past the last column
+                    const uint32_t w = __ldg(pairs + row + x0);
+                    v0 = half_to_float((uint16_t)(w & 0xffffu));
+                    v1 = half_to_float((uint16_t)(w >> 16));
+                } else if (x0 == -1) {
+                    v1 = half_to_float((uint16_t)(__ldg(pairs + row) & 0xffffu));
+                }
             }
+            c[0][b][e] = v0;
+            c[1][b][e] = v1;
+        }
     auto lerp = [](float a, float b, float t) { return a + t * (b - a); };
     return lerp(lerp(lerp(c[0][0][0], c[0][0][1], w), lerp(c[0][1][0], c[0][1][1], w), v),
                 lerp(lerp(c[1][0][0], c[1][0][1], w), lerp(c[1][1][0], c[1][1][1], w), v), u);
@@ -274,6 +285,14 @@ __device__ V3 sample_t_maj(const DevMedium &m, V3 o, V3 d, float tmax, Pcg &rng,
     }
 }
 
+// x-fastest densities [nz][ny][nx] -> pairs (voxel, +x neighbour or 0).
+__global__ void k_pair_density(const uint16_t *__restrict__ lin, int nx, int64_t n, uint32_t *pairs) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const bool last = (i % nx) == nx - 1;
+        pairs[i] = (uint32_t)lin[i] | ((uint32_t)(last ? 0 : lin[i + 1]) << 16);
+    }
+}
+
 // initializeMajorantGrid, media.cpp:18-75 (dense grid, filter slop 1 voxel)
 __global__ void k_build_majorant(DevMedium m, float *out) {
     int n = m.mres[0] * m.mres[1] * m.mres[2];
@@ -296,7 +315,7 @@ __global__ void k_build_majorant(DevMedium m, float *out) {
         for (int k = r0[2]; k <= r1[2]; ++k)
             for (int j = r0[1]; j <= r1[1]; ++j)
                 for (int i = r0[0]; i <= r1[0]; ++i)
-                    mx = fmaxf(mx, half_to_float(m.density[((size_t)k * m.ny + j) * m.nx + i]));
+                    mx = fmaxf(mx, half_to_float(m.density[2 * (((size_t)k * m.ny + j) * m.nx + i)]));
         out[idx] = mx;
     }
 }

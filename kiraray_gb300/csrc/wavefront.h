@@ -54,7 +54,10 @@ struct DevInfinite {
 };
 
 struct DevMedium {
-    const uint16_t *density;   // half, [nz][ny][nx], nullptr = homogeneous
+    // half pairs [nz][ny][nx][2]: voxel (x, y, z) and its +x neighbour (0
+    // past the last column), so that a trilinear lookup reads each row's two
+    // corners with one 4-byte load; nullptr = homogeneous
+    const uint16_t *density;
     int32_t nx, ny, nz;
     float lo[3], hi[3];
     float sigma_t[3];
