@@ -36,28 +36,30 @@ __device__ __forceinline__ float density_at(const DevMedium &m, V3 p) {
     float ix = floorf(fx), iy = floorf(fy), iz = floorf(fz);
     float u = fx - ix, v = fy - iy, w = fz - iz;
     int x0 = (int)ix, y0 = (int)iy, z0 = (int)iz;
-    float c[2][2][2];
-    const uint32_t *pairs = reinterpret_cast<const uint32_t *>(m.density);
+    // the octet of corner (x0 + sx, y0 + sy, z0 + sz): sx = 1 when x0 = -1
+    // (column -1 lies outside, column 0 is the octet's first), likewise sy, sz
+    const int sx = x0 == -1 ? 1 : 0, sy = y0 == -1 ? 1 : 0, sz = z0 == -1 ? 1 : 0;
+    float o[2][2][2] = {{{0.f, 0.f}, {0.f, 0.f}}, {{0.f, 0.f}, {0.f, 0.f}}};   // o[i][j][k]: +i x, +j y, +k z
+    if (x0 >= -1 && x0 < m.nx && y0 >= -1 && y0 < m.ny && z0 >= -1 && z0 < m.nz) {
+        const uint4 q = __ldg(reinterpret_cast<const uint4 *>(m.density) +
+                              ((size_t)(z0 + sz) * m.ny + (y0 + sy)) * m.nx + (x0 + sx));
+        const uint32_t wd[4] = {q.x, q.y, q.z, q.w};   // word 2k + j: (x, x+1) at +j y, +k z
 #pragma unroll
-    for (int b = 0; b < 2; ++b)
+        for (int k = 0; k < 2; ++k)
 #pragma unroll
-        for (int e = 0; e < 2; ++e) {
-            const int y = y0 + b, z = z0 + e;
-            float v0 = 0.f, v1 = 0.f;
-            if (y >= 0 && z >= 0 && y < m.ny && z < m.nz) {
-                const size_t row = ((size_t)z * m.ny + y) * m.nx;
-                if (x0 >= 0 && x0 < m.nx) {
-                    // the pair holds 0 for the +x neighbour past the last column
-                    const uint32_t w = __ldg(pairs + row + x0);
-                    v0 = half_to_float((uint16_t)(w & 0xffffu));
-                    v1 = half_to_float((uint16_t)(w >> 16));
-                } else if (x0 == -1) {
-                    v1 = half_to_float((uint16_t)(__ldg(pairs + row) & 0xffffu));
-                }
+            for (int j = 0; j < 2; ++j) {
+                o[0][j][k] = half_to_float((uint16_t)(wd[2 * k + j] & 0xffffu));
+                o[1][j][k] = half_to_float((uint16_t)(wd[2 * k + j] >> 16));
             }
-            c[0][b][e] = v0;
-            c[1][b][e] = v1;
-        }
+    }
+    float c[2][2][2];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int e = 0; e < 2; ++e)
+                c[a][b][e] = (a >= sx && b >= sy && e >= sz) ? o[a - sx][b - sy][e - sz] : 0.f;
     auto lerp = [](float a, float b, float t) { return a + t * (b - a); };
     return lerp(lerp(lerp(c[0][0][0], c[0][0][1], w), lerp(c[0][1][0], c[0][1][1], w), v),
                 lerp(lerp(c[1][0][0], c[1][0][1], w), lerp(c[1][1][0], c[1][1][1], w), v), u);
@@ -285,11 +287,23 @@ __device__ V3 sample_t_maj(const DevMedium &m, V3 o, V3 d, float tmax, Pcg &rng,
     }
 }
 
-// x-fastest densities [nz][ny][nx] -> pairs (voxel, +x neighbour or 0).
-__global__ void k_pair_density(const uint16_t *__restrict__ lin, int nx, int64_t n, uint32_t *pairs) {
+// x-fastest densities [nz][ny][nx] -> octets (voxel and its neighbours at
+// +x, +y, +z, 0 past the last column, row or slice).
+__global__ void k_octet_density(const uint16_t *__restrict__ lin, int nx, int ny, int nz, int64_t n,
+                                uint4 *octets) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const bool last = (i % nx) == nx - 1;
-        pairs[i] = (uint32_t)lin[i] | ((uint32_t)(last ? 0 : lin[i + 1]) << 16);
+        const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((int64_t)nx * ny));
+        uint32_t w[4];
+        for (int k = 0; k < 2; ++k)
+            for (int j = 0; j < 2; ++j) {
+                uint32_t v[2];
+                for (int a = 0; a < 2; ++a) {
+                    const bool in = x + a < nx && y + j < ny && z + k < nz;
+                    v[a] = in ? lin[i + a + (int64_t)j * nx + (int64_t)k * nx * ny] : 0u;
+                }
+                w[2 * k + j] = v[0] | (v[1] << 16);
+            }
+        octets[i] = make_uint4(w[0], w[1], w[2], w[3]);
     }
 }
 
@@ -315,7 +329,7 @@ __global__ void k_build_majorant(DevMedium m, float *out) {
         for (int k = r0[2]; k <= r1[2]; ++k)
             for (int j = r0[1]; j <= r1[1]; ++j)
                 for (int i = r0[0]; i <= r1[0]; ++i)
-                    mx = fmaxf(mx, half_to_float(m.density[2 * (((size_t)k * m.ny + j) * m.nx + i)]));
+                    mx = fmaxf(mx, half_to_float(m.density[8 * (((size_t)k * m.ny + j) * m.nx + i)]));
         out[idx] = mx;
     }
 }

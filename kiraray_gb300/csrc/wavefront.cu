@@ -2256,19 +2256,20 @@ extern "C" int krr_wf_set_scenes(krr_wf *wf, const krr_scene_desc *scenes, int32
                 KRR_CHECK_ARG(m.nx > 0 && m.ny > 0 && m.nz > 0, "density grid size");
                 const size_t nv = (size_t)m.nx * m.ny * m.nz;
                 uint16_t *lin = nullptr;
-                uint32_t *pairs = nullptr;
-                KRR_CUDA(cudaMalloc(&pairs, nv * sizeof(uint32_t)));
-                wf->scene_allocs.push_back(pairs);
+                uint4 *octets = nullptr;
+                KRR_CUDA(cudaMalloc(&octets, nv * sizeof(uint4)));
+                wf->scene_allocs.push_back(octets);
                 KRR_CUDA(cudaMalloc(&lin, nv * sizeof(uint16_t)));
                 cudaError_t ce = cudaMemcpyAsync(lin, m.h_density, nv * sizeof(uint16_t), cudaMemcpyHostToDevice, st);
                 if (ce == cudaSuccess) {
-                    k_pair_density<<<grid_for((int64_t)nv), kThreads, 0, st>>>(lin, m.nx, (int64_t)nv, pairs);
+                    k_octet_density<<<grid_for((int64_t)nv), kThreads, 0, st>>>(lin, m.nx, m.ny, m.nz,
+                                                                                (int64_t)nv, octets);
                     ce = cudaGetLastError();
                 }
                 if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
                 cudaFree(lin);
                 if (ce != cudaSuccess) return cuda_status(ce, "density upload", __FILE__, __LINE__);
-                d.density = reinterpret_cast<const uint16_t *>(pairs);
+                d.density = reinterpret_cast<const uint16_t *>(octets);
                 float *maj = nullptr;
                 size_t nm = (size_t)d.mres[0] * d.mres[1] * d.mres[2];
                 KRR_CUDA(cudaMalloc(&maj, nm * sizeof(float)));

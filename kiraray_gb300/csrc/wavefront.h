@@ -54,9 +54,10 @@ struct DevInfinite {
 };
 
 struct DevMedium {
-    // half pairs [nz][ny][nx][2]: voxel (x, y, z) and its +x neighbour (0
-    // past the last column), so that a trilinear lookup reads each row's two
-    // corners with one 4-byte load; nullptr = homogeneous
+    // half octets [nz][ny][nx][8]: voxel (x, y, z) and its seven neighbours
+    // at +x, +y, +z (0 past the grid's last column, row or slice), so that a
+    // trilinear lookup reads its eight corners with one 16-byte load;
+    // nullptr = homogeneous
     const uint16_t *density;
     int32_t nx, ny, nz;
     float lo[3], hi[3];
