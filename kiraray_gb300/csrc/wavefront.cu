@@ -1218,15 +1218,17 @@ __global__ void k_medium_scatter(DevScene s, Queue mscat, Queue next, Queue shad
 // Three blocks per SM, as k_medium_sample.
 // With a two-level structure (iv.inst != nullptr) every traversal goes
 // through the instance level.
-template <bool ANY, int FMT, bool MASKED>
+// LEVELS 2: the two-level structure (a compile-time choice, so that a
+// kernel holds one traversal stack, not one per structure).
+template <bool ANY, int FMT, bool MASKED, int LEVELS>
 __device__ __forceinline__ float4 shadow_trace(const InstancedView &iv, const float4 *__restrict__ nodes,
                                                const float4 *__restrict__ tris, V3 o, V3 d, float tmax,
                                                int *trace_err, uint32_t root) {
-    if (iv.inst) return trace_two_level<ANY, FMT, MASKED>(iv, o, d, 0.f, tmax, trace_err);
-    return traverse_ray<ANY, FMT, MASKED>(nodes, tris, o, d, 0.f, tmax, trace_err, root);
+    if constexpr (LEVELS == 2) return trace_two_level<ANY, FMT, MASKED>(iv, o, d, 0.f, tmax, trace_err);
+    else return traverse_ray<ANY, FMT, MASKED>(nodes, tris, o, d, 0.f, tmax, trace_err, root);
 }
 
-template <int FMT>
+template <int FMT, int LEVELS>
 __global__ void __launch_bounds__(kThreads, 3)
 k_shadow_tr(DevScene s, const float4 *__restrict__ nodes, const float4 *__restrict__ tris,
             InstancedView iv, Queue shadow, PixelState ps, const int32_t *__restrict__ order,
@@ -1247,7 +1249,7 @@ k_shadow_tr(DevScene s, const float4 *__restrict__ nodes, const float4 *__restri
         int crossings = 0;
         const uint32_t root = root_of(s, pixel);
         while (fabsf(d.x) > kRayEps * 2 || fabsf(d.y) > kRayEps * 2 || fabsf(d.z) > kRayEps * 2) {
-            float4 h = shadow_trace<false, FMT, true>(iv, nodes, tris, o, d, tmax, trace_err, root);
+            float4 h = shadow_trace<false, FMT, true, LEVELS>(iv, nodes, tris, o, d, tmax, trace_err, root);
             bool visible = ubits(h.w) == KRR_MISS;
             Surf sf;
             if (!visible) {
@@ -1313,7 +1315,7 @@ k_shadow_tr(DevScene s, const float4 *__restrict__ nodes, const float4 *__restri
 // draws no samples and ends at the first opaque surface, so an any-hit test
 // that ignores null-material surfaces decides them, as traceShadow does
 // without media.
-template <int FMT>
+template <int FMT, int LEVELS>
 __global__ void k_shadow_split(DevScene s, const float4 *__restrict__ nodes,
                                const float4 *__restrict__ tris, InstancedView iv, Queue shadow,
                                Queue tracked, PixelState ps, uint32_t *err, int *trace_err) {
@@ -1325,7 +1327,7 @@ __global__ void k_shadow_split(DevScene s, const float4 *__restrict__ nodes,
         const uint32_t root = root_of(s, pixel);
         bool moving = fabsf(d.x) > kRayEps * 2 || fabsf(d.y) > kRayEps * 2 || fabsf(d.z) > kRayEps * 2;
         if (s.pixel_part && !part_of(s, pixel).has_media) {
-            float4 h = shadow_trace<true, FMT, true>(iv, nodes, tris, f3(c0), d, c1.w, trace_err, root);
+            float4 h = shadow_trace<true, FMT, true, LEVELS>(iv, nodes, tris, f3(c0), d, c1.w, trace_err, root);
             if (ubits(h.w) == KRR_MISS) {
                 float4 c4 = shadow.at(4, i);
                 add_radiance(ps, pixel, f3(c2) * v3(1.f) / mean(f3(c3) * v3(1.f) + f3(c4) * v3(1.f)));
@@ -1333,7 +1335,7 @@ __global__ void k_shadow_split(DevScene s, const float4 *__restrict__ nodes,
             continue;
         }
         if (sbits(c3.w) < 0 && moving) {
-            float4 h = shadow_trace<true, FMT, false>(iv, nodes, tris, f3(c0), d, c1.w, trace_err, root);
+            float4 h = shadow_trace<true, FMT, false, LEVELS>(iv, nodes, tris, f3(c0), d, c1.w, trace_err, root);
             if (ubits(h.w) == KRR_MISS) {
                 float4 c4 = shadow.at(4, i);
                 add_radiance(ps, pixel, f3(c2) * v3(1.f) / mean(f3(c3) * v3(1.f) + f3(c4) * v3(1.f)));
@@ -3262,12 +3264,13 @@ int launch_shadow_split(krr_wf *wf, cudaStream_t st, bool media_candidates) {
                                         : wf->q(Q_SHADOW);
     int *terr = wf->accel.d_scratch + 4;
     const InstancedView iv = wf->accel.levels == 2 ? instanced_view(&wf->accel) : InstancedView{};
-    if (wf->accel.node_format == 1)
-        k_shadow_split<1><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
-                                                          from, tracked, wf->ps, wf->err(), terr);
-    else
-        k_shadow_split<0><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
-                                                          from, tracked, wf->ps, wf->err(), terr);
+#define KRR_SHADOW_SPLIT(F, LV)                                                                        \
+    k_shadow_split<F, LV><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv, \
+                                                          from, tracked, wf->ps, wf->err(), terr)
+    const bool two = wf->accel.levels == 2, f1 = wf->accel.node_format == 1;
+    if (two) { if (f1) KRR_SHADOW_SPLIT(1, 2); else KRR_SHADOW_SPLIT(0, 2); }
+    else { if (f1) KRR_SHADOW_SPLIT(1, 1); else KRR_SHADOW_SPLIT(0, 1); }
+#undef KRR_SHADOW_SPLIT
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }
@@ -3279,12 +3282,13 @@ int launch_shadow_tracker(krr_wf *wf, cudaStream_t st) {
     const InstancedView iv = wf->accel.levels == 2 ? instanced_view(&wf->accel) : InstancedView{};
     const int32_t *order = nullptr;
     KRR_TRY(work_order(wf, tracked, 1, st, &order));
-    if (wf->accel.node_format == 1)
-        k_shadow_tr<1><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
-                                                       tracked, wf->ps, order, wf->err(), terr);
-    else
-        k_shadow_tr<0><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,
-                                                       tracked, wf->ps, order, wf->err(), terr);
+#define KRR_SHADOW_TR(F, LV)                                                                           \
+    k_shadow_tr<F, LV><<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->accel.d_nodes, wf->accel.d_tris, iv,    \
+                                                       tracked, wf->ps, order, wf->err(), terr)
+    const bool two = wf->accel.levels == 2, f1 = wf->accel.node_format == 1;
+    if (two) { if (f1) KRR_SHADOW_TR(1, 2); else KRR_SHADOW_TR(0, 2); }
+    else { if (f1) KRR_SHADOW_TR(1, 1); else KRR_SHADOW_TR(0, 1); }
+#undef KRR_SHADOW_TR
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }
