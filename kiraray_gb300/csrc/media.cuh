@@ -172,8 +172,8 @@ struct MajorantIter {
         }
         int bits = ((next_cross[0] < next_cross[1]) << 2) + ((next_cross[0] < next_cross[2]) << 1) +
                    (next_cross[1] < next_cross[2]);
-        const int cmp_to_axis[8] = {2, 1, 2, 1, 2, 2, 0, 0};
-        int ax = cmp_to_axis[bits];
+        // cmp -> axis {2, 1, 2, 1, 2, 2, 0, 0}, two bits per entry (no table in local memory)
+        int ax = (0xA66 >> (2 * bits)) & 3;
         float exit = fminf(tmax, next_cross[ax]);
         float maj = m->majorant[voxel[0] + m->mres[0] * (voxel[1] + m->mres[1] * voxel[2])];
         seg = MajorantSeg{tmin, exit, sigma_t * maj};
