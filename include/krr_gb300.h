@@ -192,6 +192,15 @@ int krr_set_bvh_builder(int32_t builder);
  * greedy collapse).  Replaces nothing in the reference (OptiX builds its
  * own tree); hits are the same with either. */
 int krr_set_bvh_collapse(int32_t mode);
+/* Treelet restructuring passes (0..3, default 0) over the binary tree of
+ * the BVHs built from now on, process-wide, before the collapse: each pass
+ * visits the tree bottom-up and rebuilds, at every node over at least eight
+ * triangles, the treelet of its seven largest descendants as the binary
+ * topology of least total surface area (Karras and Aila, HPG 2013).  A
+ * restructured tree deeper than the traversal stack is built again without.
+ * Replaces nothing in the reference (OptiX builds its own tree); hits are
+ * the same with any setting. */
+int krr_set_bvh_treelets(int32_t passes);
 
 /* Build from host arrays of world-space triangles: h_vertices float3[3*n]. */
 int krr_accel_create_from_triangles(const float *h_vertices, int64_t n_triangles,

@@ -138,6 +138,7 @@ SIGNATURES = {
     "krr_accel_set_tuning": (_I, [_P, C.c_int32, C.c_int32]),
     "krr_set_bvh_builder": (_I, [C.c_int32]),
     "krr_set_bvh_collapse": (_I, [C.c_int32]),
+    "krr_set_bvh_treelets": (_I, [C.c_int32]),
     "krr_accel_set_stack_limit": (_I, [_P, C.c_int32]),
     "krr_accel_create_instanced": (_I, [_P, _P, C.c_int32, _P, C.c_int32, _P, C.POINTER(_P), _P]),
     "krr_accel_update_instances": (_I, [_P, _P, _P]),

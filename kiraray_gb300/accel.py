@@ -43,6 +43,13 @@ def set_collapse(mode: int) -> None:
     check(_lib.load().krr_set_bvh_collapse(mode), "krr_set_bvh_collapse")
 
 
+def set_treelets(passes: int) -> None:
+    """Treelet restructuring passes (0..3) over the binary tree of the BVHs
+    built from now on (Karras and Aila 2013: seven-leaf treelets rebuilt as
+    their topology of least surface area)."""
+    check(_lib.load().krr_set_bvh_treelets(passes), "krr_set_bvh_treelets")
+
+
 def set_full_node_leaf(triangles: int) -> None:
     """Largest leaf (1..3 triangles) among the children of a full node."""
     check(_lib.load().krr_set_bvh_full_node_leaf(triangles), "krr_set_bvh_full_node_leaf")

@@ -235,6 +235,152 @@ __device__ __forceinline__ float half_area(V3 lo, V3 hi) {
     return e.x * e.y + e.y * e.z + e.z * e.x;
 }
 
+// ------------------------------------------------------- treelet restructuring
+// Treelet restructuring (Karras and Aila, "Fast Parallel Construction of
+// High-Quality Bounding Volume Hierarchies", HPG 2013) of the binary tree
+// before the collapse.  Nodes are visited bottom-up (a node is taken by the
+// second of its children's walks, as in k_bottom_up); at each node with at
+// least `min_count` triangles below it, the treelet of up to seven leaves
+// grown by opening the largest-area leaf is rebuilt as the binary topology
+// of least total internal surface area, found by dynamic programming over
+// the 127 subsets of its leaves.  The treelet's internal nodes keep their
+// indices (reassigned within the treelet); a topology no better than the
+// current one by a relative 1e-5 is left alone, so ties (coincident
+// triangles) never rearrange a balanced subtree into a chain.  All reads of
+// the tree go through L2 (__ldcg): other threads rewrote the subtree.
+constexpr int kTreeletLeaves = 7;
+constexpr int kTreeletMinCount = 8;   // smaller subtrees are left as built
+
+__device__ __forceinline__ void treelet_ref(const uint32_t ref, const float4 *int_lo,
+                                            const float4 *int_hi, const float4 *leaf_lo,
+                                            const float4 *leaf_hi, const int *count, V3 &lo,
+                                            V3 &hi, int &n) {
+    if (ref & kLeafBit) {
+        lo = f3(leaf_lo[ref & ~kLeafBit]);
+        hi = f3(leaf_hi[ref & ~kLeafBit]);
+        n = 1;
+    } else {
+        lo = f3(__ldcg(int_lo + ref));
+        hi = f3(__ldcg(int_hi + ref));
+        n = __ldcg(count + ref);
+    }
+}
+
+__device__ void restructure_treelet(uint32_t root, uint32_t *left, uint32_t *right, int *count,
+                                    float4 *int_lo, float4 *int_hi, const float4 *leaf_lo,
+                                    const float4 *leaf_hi) {
+    uint32_t ref[kTreeletLeaves], inner[kTreeletLeaves - 2];
+    V3 lo[kTreeletLeaves], hi[kTreeletLeaves];
+    int cnt[kTreeletLeaves];
+    float area[kTreeletLeaves];
+    ref[0] = __ldcg(left + root);
+    ref[1] = __ldcg(right + root);
+    for (int k = 0; k < 2; ++k) {
+        treelet_ref(ref[k], int_lo, int_hi, leaf_lo, leaf_hi, count, lo[k], hi[k], cnt[k]);
+        area[k] = half_area(lo[k], hi[k]);
+    }
+    int nl = 2, ni = 0;
+    float current = 0.f;   // internal area of the treelet below its root
+    while (nl < kTreeletLeaves) {
+        int pick = -1;
+        float best = -1.f;
+        for (int k = 0; k < nl; ++k)
+            if (!(ref[k] & kLeafBit) && area[k] > best) { best = area[k]; pick = k; }
+        if (pick < 0) break;
+        const uint32_t open = ref[pick];
+        inner[ni++] = open;
+        current += area[pick];
+        ref[pick] = __ldcg(left + open);
+        ref[nl] = __ldcg(right + open);
+        for (int k : {pick, nl}) {
+            treelet_ref(ref[k], int_lo, int_hi, leaf_lo, leaf_hi, count, lo[k], hi[k], cnt[k]);
+            area[k] = half_area(lo[k], hi[k]);
+        }
+        ++nl;
+    }
+    if (ni == 0) return;
+    // cost[s]: least internal area of a binary tree over the leaf subset s
+    // (its own root included); split[s]: the part of s holding s's lowest
+    // leaf in that tree
+    float cost[1 << kTreeletLeaves];
+    uint8_t split[1 << kTreeletLeaves];
+    const int full = (1 << nl) - 1;
+    for (int s = 1; s <= full; ++s) {
+        if ((s & (s - 1)) == 0) { cost[s] = 0.f; continue; }
+        V3 slo = lo[__ffs(s) - 1], shi = hi[__ffs(s) - 1];
+        for (int k = __ffs(s); k < nl; ++k)
+            if (s >> k & 1) { slo = vmin(slo, lo[k]); shi = vmax(shi, hi[k]); }
+        const int low = s & -s;
+        float best = INFINITY;
+        int arg = low;
+        for (int p = (s - 1) & s; p; p = (p - 1) & s) {
+            if (!(p & low)) continue;
+            const float c = cost[p] + cost[s ^ p];
+            if (c < best) { best = c; arg = p; }
+        }
+        cost[s] = half_area(slo, shi) + best;
+        split[s] = (uint8_t)arg;
+    }
+    V3 rlo = lo[0], rhi = hi[0];
+    for (int k = 1; k < nl; ++k) { rlo = vmin(rlo, lo[k]); rhi = vmax(rhi, hi[k]); }
+    const float optimal = cost[full] - half_area(rlo, rhi);
+    if (!(optimal < current * (1.f - 1e-5f))) return;
+    // rewrite the treelet top-down from its root
+    uint32_t st_node[kTreeletLeaves];
+    int st_set[kTreeletLeaves];
+    int sp = 0, na = ni;
+    st_node[sp] = root;
+    st_set[sp++] = full;
+    while (sp > 0) {
+        const uint32_t node = st_node[--sp];
+        const int s = st_set[sp];
+        const int parts[2] = {split[s], s ^ split[s]};
+        uint32_t child[2];
+        for (int h = 0; h < 2; ++h) {
+            const int q = parts[h];
+            if ((q & (q - 1)) == 0) {
+                child[h] = ref[__ffs(q) - 1];
+            } else {
+                child[h] = inner[--na];
+                st_node[sp] = child[h];
+                st_set[sp++] = q;
+            }
+        }
+        V3 slo = rlo, shi = rhi;
+        int n = 0;
+        bool first = true;
+        for (int k = 0; k < nl; ++k) {
+            if (!(s >> k & 1)) continue;
+            slo = first ? lo[k] : vmin(slo, lo[k]);
+            shi = first ? hi[k] : vmax(shi, hi[k]);
+            first = false;
+            n += cnt[k];
+        }
+        __stcg(left + node, child[0]);
+        __stcg(right + node, child[1]);
+        __stcg(count + node, n);
+        __stcg(int_lo + node, make_float4(slo.x, slo.y, slo.z, 0.f));
+        __stcg(int_hi + node, make_float4(shi.x, shi.y, shi.z, 0.f));
+    }
+}
+
+__global__ void k_treelet(int n, uint32_t *left, uint32_t *right, int *count,
+                          const int *__restrict__ par_int, const int *__restrict__ par_leaf,
+                          float4 *int_lo, float4 *int_hi, const float4 *__restrict__ leaf_lo,
+                          const float4 *__restrict__ leaf_hi, int *flags, int min_count) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int node = par_leaf[i];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(flags + node, 1) == 0) return;
+        __threadfence();
+        if (__ldcg(count + node) >= min_count)
+            restructure_treelet((uint32_t)node, left, right, count, int_lo, int_hi, leaf_lo, leaf_hi);
+        node = par_int[node];
+    }
+}
+
 // ------------------------------------------------------------------ PLOC
 // Parallel locally-ordered clustering (Meister and Bittner, IEEE TVCG 2018):
 // the clusters stay in Morton order; each looks for the cluster within
@@ -1120,7 +1266,7 @@ static int build_ploc(int n, const float4 *leaf_lo, const float4 *leaf_hi, uint3
     return KRR_OK;
 }
 
-int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
+static int build_tree(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s, int treelets) {
     KRR_CHECK_ARG(n >= 0 && n < (int64_t)0x7fffffff, "triangle count out of range");
     accel_free(a);
     a->node_format = default_node_format();
@@ -1192,6 +1338,24 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
                                                              flags.p);
         KRR_CUDA(cudaGetLastError());
         root_ref = 0;
+        KRR_CUDA(cudaStreamSynchronize(s));   // the scratch above is freed on return
+    }
+
+    // treelet restructuring passes over the binary tree
+    a->treelets = n > 2 ? treelets : 0;
+    if (a->treelets > 0) {
+        DevBuf<int> par_int, par_leaf, flags;
+        KRR_CUDA(par_int.alloc(ni)); KRR_CUDA(par_leaf.alloc(n)); KRR_CUDA(flags.alloc(ni));
+        for (int pass = 0; pass < a->treelets; ++pass) {
+            KRR_CUDA(cudaMemsetAsync(flags.p, 0, ni * sizeof(int), s));
+            KRR_CUDA(cudaMemsetAsync(par_int.p, 0xff, ni * sizeof(int), s));   // the root's parent: -1
+            k_parents<<<blocks_for(n - 1), kBuildThreads, 0, s>>>((int)(n - 1), left.p, right.p,
+                                                                   par_int.p, par_leaf.p);
+            k_treelet<<<blocks_for(n), kBuildThreads, 0, s>>>((int)n, left.p, right.p, count.p, par_int.p,
+                                                               par_leaf.p, ilo.p, ihi.p, llo.p, lhi.p,
+                                                               flags.p, kTreeletMinCount);
+            KRR_CUDA(cudaGetLastError());
+        }
         KRR_CUDA(cudaStreamSynchronize(s));   // the scratch above is freed on return
     }
 
@@ -1288,6 +1452,18 @@ int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return KRR_OK;
+}
+
+// Treelet passes of the BVHs built from now on (krr_set_bvh_treelets).
+static int g_treelets = 0;
+
+int accel_build(krr_accel *a, const float *d_v, int64_t n, cudaStream_t s) {
+    int st = build_tree(a, d_v, n, s, g_treelets);
+    // a restructured tree deeper than the traversal stack (possible on
+    // degenerate input) is built again without restructuring
+    if (st == KRR_ERR_OVERFLOW && g_treelets > 0 && a->max_depth > kTraversalStack)
+        st = build_tree(a, d_v, n, s, 0);
+    return st;
 }
 
 // Relocation of one part's tree into the combined arrays: child and
@@ -1474,6 +1650,12 @@ int krr::default_builder() { return g_builder; }
 extern "C" int krr_set_bvh_collapse(int32_t mode) {
     KRR_CHECK_ARG(mode == 0 || mode == 1, "collapse must be 0 (greedy) or 1 (cost-optimal)");
     g_collapse = mode;
+    return KRR_OK;
+}
+
+extern "C" int krr_set_bvh_treelets(int32_t passes) {
+    KRR_CHECK_ARG(passes >= 0 && passes <= 3, "treelet passes must be 0..3");
+    g_treelets = passes;
     return KRR_OK;
 }
 

@@ -63,6 +63,7 @@ struct krr_accel {
     int full_leaf = 1;           // triangles per leaf child of a full node (max_leaf..3)
     int builder = 0;             // binary tree: 0 radix tree, 1 PLOC, 2 radix tree on cubic cells
     int collapse = 0;            // wide nodes: 0 greedy, 1 cost-optimal
+    int treelets = 0;            // treelet restructuring passes applied to the binary tree
     // host-buffer entry point (krr_accel_trace_closest_host): device staging
     // for rays (2 float4 each) and hits, grown on demand, and a second stream
     // with two events, kept across calls so that a call allocates nothing

@@ -429,6 +429,52 @@ def test_cost_optimal_collapse_gives_identical_hits(krr_lib, cuda, builder):
         assert a.device_errors() == 0
 
 
+@pytest.mark.parametrize("builder,passes,collapse", [(2, 1, 0), (2, 3, 0), (1, 2, 0), (0, 1, 1)])
+def test_treelet_restructuring_gives_identical_hits(krr_lib, cuda, builder, passes, collapse):
+    """Treelet passes rebuild parts of the binary tree before the collapse;
+    hits stay the oracle's bit for bit (scene, soup, one triangle, a pile of
+    coincident triangles), and the restructured scene tree has other wide
+    nodes than the tree as built."""
+    from kiraray_gb300._lib import KrrError
+    from kiraray_gb300.accel import set_builder, set_collapse, set_treelets
+    sc = scenes.large_scene(width=160, height=90, grid=256, n_spheres=60, sky_size=(64, 32))
+    tris = sc.world_triangles()
+    rays = H.pinhole_rays(sc, jitter_seed=31)
+    ob = O.Bvh(tris)
+    want = ob.closest(rays)
+    b = H.bounce_rays(tris, rays, want, 6)
+    soup = H.random_soup(3000, 33)
+    pile = np.repeat(soup[:1], 700, axis=0)
+    set_builder(builder)
+    set_collapse(collapse)
+    try:
+        plain = Accel(tris)
+        set_treelets(passes)
+        acc = Accel(tris)
+        acc_soup = Accel(soup)
+        single = Accel(soup[:1])
+        acc_pile = Accel(pile)
+    finally:
+        set_builder(2)
+        set_collapse(0)
+        set_treelets(0)
+    tag = f"builder {builder}, {passes} treelet passes"
+    _assert_bits_equal(_gpu_closest(acc, rays), want, f"{tag} camera rays")
+    _assert_bits_equal(_gpu_closest(acc, b), ob.closest(b), f"{tag} bounce rays")
+    occ = acc.trace_any(torch.from_numpy(b).cuda()).cpu().numpy()
+    assert np.array_equal(occ, ob.any(b))
+    r = H.random_rays(2000, 34)
+    _assert_bits_equal(_gpu_closest(acc_soup, r), O.closest_brute(soup, r), f"{tag} soup")
+    _assert_bits_equal(_gpu_closest(single, r), O.closest_brute(soup[:1], r), "one triangle")
+    _assert_bits_equal(_gpu_closest(acc_pile, r), O.closest_brute(pile, r), "coincident triangles")
+    assert acc.stats()["n_nodes"] != plain.stats()["n_nodes"]
+    assert acc.stats()["max_depth"] <= 48 and acc_pile.stats()["max_depth"] <= 48
+    for a in (acc, acc_soup, single, acc_pile):
+        assert a.device_errors() == 0
+    with pytest.raises(KrrError):
+        set_treelets(4)
+
+
 def test_two_level_structure_matches_the_instanced_oracle(krr_lib, cuda):
     """Geometry trees in object space plus an instance tree: closest hits
     bit-exact against the oracle's two-level restatement (same world-to-object
