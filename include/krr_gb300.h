@@ -426,6 +426,13 @@ int krr_wf_set_megakernel_reorder(krr_wf *wf, int32_t reorder);
  * more than it saves on the 1024x1024 volume frame (11.1 against 10.1 ms),
  * hence off by default.  Frames are the same either way. */
 int krr_wf_set_media_order(krr_wf *wf, int32_t order);
+/* Order in which the camera stage queues each view's pixels (default 1):
+ * 1 = 8x8 pixel tiles (bands of eight rows, eight columns at a time, the
+ * last tile of a band and the last band narrower), 0 = row-major, the order
+ * in which the reference's generateCameraRays pushes them
+ * (src/render/wavefront/integrator.cpp:166-179).  Frames are the same
+ * either way; the tiles keep the rays a warp traces close together. */
+int krr_wf_set_camera_order(krr_wf *wf, int32_t order);
 
 /* Batched views: many cameras of different sizes in one wavefront (one
  * launch per stage per bounce).  krr_wf_resize_views replaces resize; each

@@ -188,6 +188,7 @@ SIGNATURES = {
     "krr_wf_set_accel_levels": (_I, [_P, C.c_int32]),
     "krr_wf_set_megakernel_reorder": (_I, [_P, C.c_int32]),
     "krr_wf_set_media_order": (_I, [_P, C.c_int32]),
+    "krr_wf_set_camera_order": (_I, [_P, C.c_int32]),
     "krr_wf_get_launch": (_I, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "krr_wf_autotune": (_I, [_P, _P, C.c_int32, C.POINTER(WfTuning), _P]),

@@ -96,6 +96,7 @@ struct krr_wf {
     int32_t levels = 1;                    // 1: flattened instances, 2: two-level structure
     int32_t mk_reorder = 1;                // megakernel: reorder paths by hit class per bounce
     int32_t media_order = 0;               // 1: tracking kernels take their items by work class
+    int32_t camera_order = 1;              // 1: camera rays in 8x8 pixel tiles, 0: row-major
     int32_t *work_counts = nullptr;        // [32] work-class counts and cursors
     std::vector<DevMesh> h_mesh;           // host copies of the device meshes
     std::vector<int64_t> h_mesh_tris;      // triangles per mesh
@@ -457,17 +458,41 @@ __global__ void k_begin_frame(PixelState ps, const DevView *__restrict__ views,
 }
 
 // generateCameraRays + CameraData::getRay, integrator.cpp:166-179, camera.h:32-58
-// Pixels [p0, p0 + n) of the frame into ray queue items 0..n-1.
+// Camera order: a view's pixels in bands of kCamTile rows, each band in
+// chunks of kCamTile columns (8x8 tiles, row-major inside a tile; the last
+// chunk of a band and the last band may be narrower).  Position i of the
+// order -> row-major pixel index; a bijection on the view's w x h pixels.
+constexpr int kCamTile = 8;
+__device__ __forceinline__ int64_t tile_pixel(int64_t i, int w, int h) {
+    const int64_t band_px = (int64_t)w * kCamTile;
+    const int64_t band = i / band_px;
+    const int bh = min(kCamTile, h - (int)band * kCamTile);
+    const int64_t r = i - band * band_px;
+    const int c = (int)(r / (kCamTile * bh));
+    const int o = (int)(r - (int64_t)c * kCamTile * bh);
+    const int cw = min(kCamTile, w - c * kCamTile);
+    return (int64_t)((int)band * kCamTile + o / cw) * w + c * kCamTile + o % cw;
+}
+
+// Positions [p0, p0 + n) of the frame's camera order into ray queue items
+// 0..n-1.  tiled = 0: position = pixel (row-major); tiled = 1: each view's
+// pixels in 8x8 tiles (tile_pixel), so that the rays a warp takes up
+// together cover a compact patch of the image (a few per cent fewer node
+// visits' worth of time in the traversal on the 1920x1080 camera rays).
+// Each view's positions map onto its own pixels, so waves (ranges of
+// positions) still cover every pixel once; a path depends only on its
+// pixel, so frames are the same in either order.
 __global__ void k_camera_rays(PixelState ps, Queue rq, const DevView *__restrict__ views,
-                              const FrameConst *__restrict__ fc, int64_t p0, int64_t n) {
+                              const FrameConst *__restrict__ fc, int64_t p0, int64_t n, int tiled) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *rq.count = (int32_t)n;
     const int nv = fc->n_views;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
          q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t g = p0 + q;
-        const DevView &v = views[view_of(views, nv, g)];
+        const int64_t pos = p0 + q;
+        const DevView &v = views[view_of(views, nv, pos)];
         const DevCamera &cam = v.cam;
-        int64_t i = g - v.offset;
+        const int64_t i = tiled ? tile_pixel(pos - v.offset, v.w, v.h) : pos - v.offset;
+        const int64_t g = v.offset + i;
         Pcg p = load_rng(ps, (uint32_t)g);
         float fx = p.get1d(), fy = p.get1d();
         float lx = p.get1d(), ly = p.get1d();
@@ -2540,7 +2565,7 @@ extern "C" int krr_wf_begin_frame_views(krr_wf *wf, int64_t frame_index, const k
 
 static int camera_rays(krr_wf *wf, int64_t p0, int64_t count, cudaStream_t st) {
     k_camera_rays<<<stage_grid(wf, count), wf->block, 0, st>>>(wf->ps, wf->q(Q_RAY0), wf->d_views,
-                                                               wf->d_frame, p0, count);
+                                                               wf->d_frame, p0, count, wf->camera_order);
     KRR_CUDA(cudaGetLastError());
     return KRR_OK;
 }
@@ -2894,6 +2919,12 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
 extern "C" int krr_wf_set_media_order(krr_wf *wf, int32_t order) {
     KRR_CHECK_ARG(wf && (order == 0 || order == 1), "order must be 0 or 1");
     wf->media_order = order;
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_set_camera_order(krr_wf *wf, int32_t order) {
+    KRR_CHECK_ARG(wf && (order == 0 || order == 1), "order must be 0 or 1");
+    wf->camera_order = order;
     return KRR_OK;
 }
 

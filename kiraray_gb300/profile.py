@@ -92,7 +92,8 @@ def update(reps: int) -> dict:
     return out
 
 
-def frame(res: str, views: int, nrc: bool, frames: int, scene: str = "large", seed: int = 3) -> dict:
+def frame(res: str, views: int, nrc: bool, frames: int, scene: str = "large", seed: int = 3,
+          camera_order: int = 1) -> dict:
     from . import scenes
     from .convergence import replica_views
     from .nrc import NeuralRadianceCache
@@ -107,6 +108,7 @@ def frame(res: str, views: int, nrc: bool, frames: int, scene: str = "large", se
         sc = scenes.volume_box(w, h)
     pt = WavefrontPathTracer({"max_depth": sc.max_depth}, seed=3)
     pt.set_scene(sc)
+    pt.set_camera_order(bool(camera_order))
     if nrc:
         tris = sc.world_triangles().reshape(-1, 3)
         cache = NeuralRadianceCache(tris.min(0), tris.max(0), seed=3)
@@ -119,7 +121,8 @@ def frame(res: str, views: int, nrc: bool, frames: int, scene: str = "large", se
         pt.render_flat(out)
 
     ms = [_timed(lambda: one(f)) for f in range(1, frames + 1)]
-    return {"workload": "frame", "scene": scene, "res": res, "views": views, "nrc": nrc, "ms": ms,
+    return {"workload": "frame", "scene": scene, "res": res, "views": views, "nrc": nrc,
+            "camera_order": "tiles" if camera_order else "rows", "ms": ms,
             "device_errors": pt.device_errors()}
 
 
@@ -175,6 +178,8 @@ def main() -> None:
     f.add_argument("--nrc", action="store_true")
     f.add_argument("--frames", type=int, default=3)
     f.add_argument("--seed", type=int, default=3, help="large-scene seed (the bench's 1080p frame: 1)")
+    f.add_argument("--camera-order", type=int, default=1, choices=[0, 1],
+                   help="camera rays in 8x8 pixel tiles (1) or row-major (0)")
     a = ap.parse_args()
     from .build import build
     build()
@@ -185,7 +190,7 @@ def main() -> None:
     elif a.cmd == "cache":
         r = cache_curves(json.loads(a.configs), a.res)
     else:
-        r = frame(a.res, a.views, a.nrc, a.frames, a.scene, a.seed)
+        r = frame(a.res, a.views, a.nrc, a.frames, a.scene, a.seed, a.camera_order)
     print(json.dumps(r))
 
 

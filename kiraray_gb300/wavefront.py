@@ -171,9 +171,13 @@ class WavefrontPathTracer:
               "krr_wf_set_megakernel_reorder")
 
     def set_media_order(self, order: bool) -> None:
-        """Medium tracking items taken by estimated optical depth (default)
-        or in queue order."""
+        """Medium tracking items taken by estimated optical depth (True) or
+        in queue order (False, default)."""
         check(self.lib.krr_wf_set_media_order(self._h, int(bool(order))), "krr_wf_set_media_order")
+
+    def set_camera_order(self, tiled: bool) -> None:
+        """Camera rays queued in 8x8 pixel tiles (True, default) or row-major."""
+        check(self.lib.krr_wf_set_camera_order(self._h, int(bool(tiled))), "krr_wf_set_camera_order")
 
     def set_accel_levels(self, levels: int) -> None:
         """1: flattened instances (default), 2: two-level structure."""

@@ -260,6 +260,30 @@ def test_launch_shapes_and_waves_keep_the_frame(krr_lib, cuda):
         pt.generate_camera_rays()
 
 
+def test_camera_order_keeps_the_frame(krr_lib, cuda):
+    """Camera rays queued in 8x8 pixel tiles (the default) or row-major give
+    the same frame bit for bit, with views whose sizes are not multiples of
+    eight and with waves that end inside a view."""
+    (big, vol), views = _two_scene_views()
+    pt = WavefrontPathTracer({"max_depth": 8})
+    pt.set_scenes([big, vol])
+    pt.resize_views(views)
+    pt.set_camera_order(False)
+    pt.begin_frame_views(5)
+    want = pt.render_flat().cpu().numpy()
+    n = pt.n_pixels
+    pt.set_camera_order(True)
+    for wave in (0, n // 3 + 5, 999):
+        pt.set_launch(256, 8, wave)
+        pt.begin_frame_views(5)
+        got = pt.render_flat().cpu().numpy()
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), wave
+    assert pt.device_errors() == 0
+    from kiraray_gb300._lib import KrrError, check
+    with pytest.raises(KrrError):
+        check(pt.lib.krr_wf_set_camera_order(pt._h, 2), "krr_wf_set_camera_order")
+
+
 def test_autotuner_keeps_the_frame(krr_lib, cuda):
     (big, vol), views = _two_scene_views()
     pt = WavefrontPathTracer({"max_depth": 8})
