@@ -516,30 +516,13 @@ def batched_views(args):
     in one graph (a branch per pass, each with its own cache)."""
     if args.views <= 0:
         return None
-    import math
-
     import torch
-    from kiraray_gb300 import scenes
     from kiraray_gb300.nrc import NeuralRadianceCache
+    from kiraray_gb300.profile import batched_workload
     from kiraray_gb300.wavefront import FrameGroup, WavefrontPathTracer
 
-    big = scenes.large_scene(width=64, height=64, seed=1)
-    vol = scenes.volume_box(64, 64)
-    views = []
-    total = 0
-    for i in range(args.views):
-        rng = np.random.default_rng(100 + i)
-        w = int(round(math.exp(rng.uniform(math.log(256), math.log(1024)))))
-        h = int(round(math.exp(rng.uniform(math.log(256), math.log(1024)))))
-        a = math.radians(rng.uniform(-10, 10))
-        if i % 2 == 0:
-            pos = (62.0 * math.sin(a), 22.0, -62.0 * math.cos(a))
-            cam = scenes._camera(pos, (0.0, 2.0, 0.0), 45.0, w, h)
-        else:
-            pos = (0.5 + 1.9 * math.sin(a), 0.5, 0.5 - 1.9 * math.cos(a))
-            cam = scenes._camera(pos, (0.5, 0.5, 0.0), 40.0, w, h)
-        views.append((cam, w, h, 100 + i, i % 2))
-        total += w * h
+    big, vol, views = batched_workload(args.views)
+    total = sum(v[1] * v[2] for v in views)
     stream = torch.cuda.Stream()
 
     def timed(fn, frames):

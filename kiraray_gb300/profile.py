@@ -12,17 +12,22 @@ and single-kernel captures); prints the device time of each repetition.
         an instance update of the large scene (re-flatten + BVH refit) against
         a full BVH rebuild, host wall time per call
     python -m kiraray_gb300.profile frame [--scene large] [--res 480x270] [--views 8] [--nrc]
-                                          [--frames 3] [--seed 3]
+                                          [--frames 3] [--seed 3] [--camera-order 1]
         frames of the wavefront pass on the large scene (max depth 8), the
         Cornell box (5) or the volume box (16), the camera replicated into
         `views` batched views, optionally with the neural radiance cache
         attached and training
+    python -m kiraray_gb300.profile batched [--frames 3] [--views 64]
+        eager frames of the batched configuration: 64 views of uneven sizes
+        on the large scene and the volume box in one wavefront, the neural
+        radiance cache attached and training
 """
 from __future__ import annotations
 
 import argparse
 import json
 
+import numpy as np
 import torch
 
 
@@ -126,6 +131,56 @@ def frame(res: str, views: int, nrc: bool, frames: int, scene: str = "large", se
             "device_errors": pt.device_errors()}
 
 
+def batched_workload(n_views: int = 64):
+    """The batched configuration: n_views views with sides log-uniform in
+    [256, 1024] (view i seeded 100 + i), even views on the large scene
+    (max depth 8), odd views on the volume box (max depth 16).  Returns the
+    two scenes and the views as (camera, w, h, seed, scene)."""
+    import math
+
+    from . import scenes
+    big = scenes.large_scene(width=64, height=64, seed=1)
+    vol = scenes.volume_box(64, 64)
+    views = []
+    for i in range(n_views):
+        rng = np.random.default_rng(100 + i)
+        w = int(round(math.exp(rng.uniform(math.log(256), math.log(1024)))))
+        h = int(round(math.exp(rng.uniform(math.log(256), math.log(1024)))))
+        a = math.radians(rng.uniform(-10, 10))
+        if i % 2 == 0:
+            pos = (62.0 * math.sin(a), 22.0, -62.0 * math.cos(a))
+            cam = scenes._camera(pos, (0.0, 2.0, 0.0), 45.0, w, h)
+        else:
+            pos = (0.5 + 1.9 * math.sin(a), 0.5, 0.5 - 1.9 * math.cos(a))
+            cam = scenes._camera(pos, (0.5, 0.5, 0.0), 40.0, w, h)
+        views.append((cam, w, h, 100 + i, i % 2))
+    return big, vol, views
+
+
+def batched(frames: int, n_views: int = 64) -> dict:
+    """Eager frames of the batched configuration in one wavefront with the
+    cache attached and training (default launch shapes), for launch lists."""
+    from .nrc import NeuralRadianceCache
+    from .wavefront import WavefrontPathTracer
+
+    big, vol, views = batched_workload(n_views)
+    pt = WavefrontPathTracer({"max_depth": 8}, seed=0)
+    pt.set_scenes([big, vol])
+    pt.set_scene_max_depth(1, vol.max_depth)
+    pt.resize_views(views)
+    lo, hi = pt.cache_box()
+    pt.set_nrc(NeuralRadianceCache(lo, hi, seed=3), train=True)
+    out = torch.empty((pt.n_pixels, 4), device="cuda")
+
+    def one(f):
+        pt.begin_frame_views(f)
+        pt.render_flat(out)
+
+    ms = [_timed(lambda: one(f)) for f in range(1, frames + 1)]
+    return {"workload": "batched", "views": n_views, "pixels": pt.n_pixels, "ms": ms,
+            "device_errors": pt.device_errors()}
+
+
 def cache_curves(configs: list, res: str = "480x270", copies: int = 8, spp: int = 32768) -> list:
     """relMSE against a 65,536-spp reference of the neural-cache tracer on
     the large scene (seed 3) at 2k-32k samples per pixel, one entry per cache
@@ -178,6 +233,9 @@ def main() -> None:
     f.add_argument("--nrc", action="store_true")
     f.add_argument("--frames", type=int, default=3)
     f.add_argument("--seed", type=int, default=3, help="large-scene seed (the bench's 1080p frame: 1)")
+    b = sub.add_parser("batched", help="eager frames of the 64-view, two-scene configuration")
+    b.add_argument("--frames", type=int, default=3)
+    b.add_argument("--views", type=int, default=64)
     f.add_argument("--camera-order", type=int, default=1, choices=[0, 1],
                    help="camera rays in 8x8 pixel tiles (1) or row-major (0)")
     a = ap.parse_args()
@@ -187,6 +245,8 @@ def main() -> None:
         r = trace(a.reps, a.builder, a.levels)
     elif a.cmd == "update":
         r = update(a.reps)
+    elif a.cmd == "batched":
+        r = batched(a.frames, a.views)
     elif a.cmd == "cache":
         r = cache_curves(json.loads(a.configs), a.res)
     else:
