@@ -1008,6 +1008,21 @@ extern "C" int oracle_pt_create(const krr_scene_desc *sd, int threads, oracle_pt
 
 extern "C" void oracle_pt_free(oracle_pt *s) { delete s; }
 
+// Henyey-Greenstein phase function of the restatement (known-answer tests).
+extern "C" float oracle_hg_p(float g, const float *wo, const float *wi) {
+    return hg_p(g, V3{wo[0], wo[1], wo[2]}, V3{wi[0], wi[1], wi[2]});
+}
+
+// n samples of the HG phase function around wo; out[n][4] = wi xyz, pdf
+extern "C" void oracle_hg_sample(float g, const float *wo, const float *u, int64_t n, float *out) {
+    const V3 o{wo[0], wo[1], wo[2]};
+    for (int64_t i = 0; i < n; ++i) {
+        float pdf = 0.f;
+        const V3 wi = hg_sample(g, o, u[2 * i], u[2 * i + 1], pdf);
+        out[4 * i] = wi.x; out[4 * i + 1] = wi.y; out[4 * i + 2] = wi.z; out[4 * i + 3] = pdf;
+    }
+}
+
 // Mean of the ratio-tracking transmittance estimator along one segment inside
 // medium 0 of the scene (no surfaces), over n independent PCG streams.
 extern "C" double oracle_medium_transmittance(const oracle_pt *s, const float *o, const float *d,

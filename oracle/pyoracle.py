@@ -37,6 +37,11 @@ def load() -> C.CDLL:
             "oracle_pcg_floats": (None, [C.c_uint32, C.c_uint32, C.c_uint32, I64, C.c_int, P]),
             "oracle_pcg_u32": (None, [C.c_uint64, C.c_uint64, C.c_int, P]),
             "oracle_interleave_32bit": (C.c_uint32, [C.c_uint32, C.c_uint32]),
+            "oracle_fr_dielectric": (C.c_float, [C.c_float, C.c_float]),
+            "oracle_bsdf_eval": (None, [P, P, P, I64, P]),
+            "oracle_bsdf_sample": (None, [P, P, P, I64, P]),
+            "oracle_hg_p": (C.c_float, [C.c_float, P, P]),
+            "oracle_hg_sample": (None, [C.c_float, P, P, I64, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -131,6 +136,53 @@ def pcg_floats(px: int, py: int, sample_index: int, advance: int, count: int) ->
 def pcg_u32(initstate: int, initseq: int, count: int) -> np.ndarray:
     out = np.empty(count, np.uint32)
     load().oracle_pcg_u32(initstate, initseq, count, out.ctypes.data)
+    return out
+
+
+MAT_DIFFUSE, MAT_DIELECTRIC, MAT_CONDUCTOR = 1, 2, 3
+
+
+def material(kind: int, color=(0.8, 0.8, 0.8), roughness: float = 0.5, spec_trans: float = 0.0,
+              ior: float = 1.5, anisotropic: float = 0.0) -> np.ndarray:
+    return np.array([kind, *color, roughness, spec_trans, ior, anisotropic], np.float32)
+
+
+def fr_dielectric(cos_i: float, eta: float) -> float:
+    return float(load().oracle_fr_dielectric(cos_i, eta))
+
+
+def bsdf_eval(material: np.ndarray, wo: np.ndarray, wi: np.ndarray) -> np.ndarray:
+    """f (rgb) and pdf [n, 4] of direction pairs in the local shading frame."""
+    wo = np.ascontiguousarray(np.broadcast_to(wo, np.shape(wi)), np.float32).reshape(-1, 3)
+    wi = np.ascontiguousarray(wi, np.float32).reshape(-1, 3)
+    out = np.empty((wi.shape[0], 4), np.float32)
+    load().oracle_bsdf_eval(material.ctypes.data, wo.ctypes.data, wi.ctypes.data, wi.shape[0],
+                            out.ctypes.data)
+    return out
+
+
+def bsdf_sample(material: np.ndarray, wo, u: np.ndarray) -> np.ndarray:
+    """Samples [n, 8] (f rgb, wi xyz, pdf, flags) for one wo, row i drawing u[i, 0..2]."""
+    wo = np.ascontiguousarray(wo, np.float32)
+    u = np.ascontiguousarray(u, np.float32).reshape(-1, 3)
+    out = np.empty((u.shape[0], 8), np.float32)
+    load().oracle_bsdf_sample(material.ctypes.data, wo.ctypes.data, u.ctypes.data, u.shape[0],
+                              out.ctypes.data)
+    return out
+
+
+def hg_p(g: float, wo, wi) -> float:
+    wo = np.ascontiguousarray(wo, np.float32)
+    wi = np.ascontiguousarray(wi, np.float32)
+    return float(load().oracle_hg_p(g, wo.ctypes.data, wi.ctypes.data))
+
+
+def hg_sample(g: float, wo, u: np.ndarray) -> np.ndarray:
+    """Samples [n, 4] (wi xyz, pdf) of the HG phase function around wo."""
+    wo = np.ascontiguousarray(wo, np.float32)
+    u = np.ascontiguousarray(u, np.float32).reshape(-1, 2)
+    out = np.empty((u.shape[0], 4), np.float32)
+    load().oracle_hg_sample(g, wo.ctypes.data, u.ctypes.data, u.shape[0], out.ctypes.data)
     return out
 
 
