@@ -68,9 +68,10 @@ int oracle_pt_render(const oracle_pt *pt, const struct krr_wf_params *params,
 double oracle_medium_transmittance(const oracle_pt *pt, const float *o, const float *d, float tmax,
                                    int n, uint32_t seed);
 
-/* Shading known answers (src/render/materials/*.h, media.cpp:83-111), local
- * shading frame.  mat: type (1 diffuse, 2 dielectric, 3 conductor), diffuse
- * rgb, roughness, specular transmission, ior, anisotropic. */
+/* Shading known answers (the material headers of src/render/materials/ and
+ * media.cpp:83-111), in the local shading frame.  mat: type (1 diffuse,
+ * 2 dielectric, 3 conductor), diffuse rgb, roughness, specular transmission,
+ * ior, anisotropic. */
 float oracle_fr_dielectric(float cos_i, float eta);
 /* f rgb and pdf of n (wo, wi) pairs -> out[4 n] */
 void oracle_bsdf_eval(const float *mat, const float *wo, const float *wi, int64_t n, float *out);
