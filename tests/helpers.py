@@ -62,3 +62,27 @@ def vertex_edge_rays(n: int, seed: int) -> np.ndarray:
     out[:, 4:7] = d
     out[:, 7] = np.inf
     return out
+
+
+def furnace_sphere(le=(1.0, 2.0, 0.5), albedo: float = 0.5, max_depth: int = 40, size: int = 24):
+    """A closed icosphere seen from its centre, emitting `le` and reflecting
+    with Lambertian `albedo` on its inside (flat normals pointing inward):
+    its radiance is le (1 - albedo^(max_depth+1)) / (1 - albedo) everywhere."""
+    from kiraray_gb300 import _lib as L
+    from kiraray_gb300 import scenes
+
+    sph = scenes.icosphere(2)
+    tri = sph.positions[sph.indices[:, [0, 2, 1]]]          # reversed winding: normals point inward
+    n = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    pos = tri.reshape(-1, 3).astype(np.float32)
+    nrm = np.repeat(n, 3, axis=0).astype(np.float32)
+    idx = np.arange(pos.shape[0], dtype=np.uint32).reshape(-1, 3)
+    mesh = scenes.Mesh(pos, nrm, idx, material=0, emission=tuple(float(x) for x in le))
+    mats = [scenes.Material(type=L.MATERIAL_DIFFUSE, diffuse=(albedo, albedo, albedo))]
+    cam = scenes._camera((0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 60.0, size, size)
+    sc = scenes.Scene([mesh], [(0, scenes.IDENTITY)], mats, cam, size, size, max_depth=max_depth,
+                      name="furnace")
+    want = np.asarray(le, np.float64) * (1 - albedo ** (max_depth + 1)) / (1 - albedo)
+    return sc, want
+

@@ -217,28 +217,13 @@ def test_closed_lambertian_sphere_radiance(oracle_lib, nee):
     """Inside a closed sphere whose surface emits Le and reflects with
     Lambertian albedo a, the radiance is Le / (1 - a) everywhere (here up to
     max_depth bounces: Le (1 - a^(D+1)) / (1 - a))."""
-    from kiraray_gb300 import scenes
-    from kiraray_gb300 import _lib as L
+    from tests.helpers import furnace_sphere
 
-    sph = scenes.icosphere(2)
-    tri = sph.positions[sph.indices[:, [0, 2, 1]]]          # reversed winding: normals point inward
-    n = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
-    n /= np.linalg.norm(n, axis=1, keepdims=True)
-    pos = tri.reshape(-1, 3).astype(np.float32)
-    nrm = np.repeat(n, 3, axis=0).astype(np.float32)
-    idx = np.arange(pos.shape[0], dtype=np.uint32).reshape(-1, 3)
-    le, a, depth = np.array([1.0, 2.0, 0.5]), 0.5, 40
-    mesh = scenes.Mesh(pos, nrm, idx, material=0, emission=tuple(le))
-    mats = [scenes.Material(type=L.MATERIAL_DIFFUSE, diffuse=(a, a, a))]
-    w = h = 24
-    cam = scenes._camera((0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 60.0, w, h)
-    sc = scenes.Scene([mesh], [(0, scenes.IDENTITY)], mats, cam, w, h, max_depth=depth, name="furnace")
+    sc, want = furnace_sphere()
     pt = O.PathTracer(sc)
     acc = np.zeros(3)
     frames = 48
     for f in range(1, frames + 1):
-        Lrad, _ = pt.render({"max_depth": depth, "nee": nee, "spp": 1}, f)
+        Lrad, _ = pt.render({"max_depth": sc.max_depth, "nee": nee, "spp": 1}, f)
         acc += Lrad.mean(axis=0)
-    got = acc / frames
-    want = le * (1 - a ** (depth + 1)) / (1 - a)
-    np.testing.assert_allclose(got, want, rtol=0.02)
+    np.testing.assert_allclose(acc / frames, want, rtol=0.02)

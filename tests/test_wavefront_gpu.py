@@ -17,6 +17,7 @@ import torch
 from kiraray_gb300 import scenes
 from kiraray_gb300.wavefront import WavefrontPathTracer
 from oracle import pyoracle as O
+from tests import helpers as H
 
 pytestmark = pytest.mark.gpu
 
@@ -394,3 +395,23 @@ def test_two_level_structure_in_the_pass(krr_lib, cuda):
     assert pv.device_errors() == 0
     oL, _ = O.PathTracer(vb).render({"max_depth": 8}, 1)
     compare(L[:, :3], oL, "two-level volume box", max_outliers=0.01)
+
+
+@pytest.mark.parametrize("nee", [1, 0])
+def test_closed_lambertian_sphere_radiance(krr_lib, cuda, nee):
+    """Known answer through the CUDA pass: inside a closed sphere that emits
+    Le and reflects with Lambertian albedo a, every pixel converges to
+    Le (1 - a^(D+1)) / (1 - a)."""
+    sc, want = H.furnace_sphere()
+    pt = WavefrontPathTracer({"max_depth": sc.max_depth, "nee": nee})
+    pt.set_scene(sc)
+    pt.resize(sc.width, sc.height)
+    acc = torch.zeros(3, dtype=torch.float64, device="cuda")
+    frames = 64
+    for f in range(1, frames + 1):
+        pt.begin_frame(f, sc.camera)
+        acc += pt.render()[..., :3].reshape(-1, 3).double().mean(0)
+    got = (acc / frames).cpu().numpy()
+    np.testing.assert_allclose(got, want, rtol=0.02)
+    assert pt.device_errors() == 0
+
