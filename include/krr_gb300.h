@@ -434,6 +434,22 @@ int krr_wf_set_media_order(krr_wf *wf, int32_t order);
  * either way; the tiles keep the rays a warp traces close together. */
 int krr_wf_set_camera_order(krr_wf *wf, int32_t order);
 
+/* Stage timers, the counterpart of the reference's PROFILE("...") events
+ * (src/util/profiler.h:212-235; stage names from integrator.cpp and
+ * medium.cpp): with profiling on (default off), every stage's launches are
+ * bracketed by two CUDA events on the stage's stream (not while the stream
+ * is being captured into a graph).  krr_wf_profile_read waits for the
+ * recorded events, writes up to `cap` stages with their call counts and
+ * summed device milliseconds since the last read, sets *n_out to the number
+ * of stages that ran, and starts a new interval. */
+typedef struct krr_stage_time {
+    char name[40];
+    int64_t calls;
+    double ms;
+} krr_stage_time;
+int krr_wf_set_profiling(krr_wf *wf, int32_t on);
+int krr_wf_profile_read(krr_wf *wf, krr_stage_time *out, int32_t cap, int32_t *n_out);
+
 /* Batched views: many cameras of different sizes in one wavefront (one
  * launch per stage per bounce).  krr_wf_resize_views replaces resize; each
  * frame krr_wf_begin_frame_views gives the cameras (sizes must match) and

@@ -83,6 +83,10 @@ class AccelStats(C.Structure):
                 ("triangle_bytes", C.c_double)]
 
 
+class StageTime(C.Structure):
+    _fields_ = [("name", C.c_char * 40), ("calls", C.c_int64), ("ms", C.c_double)]
+
+
 class NrcConfig(C.Structure):
     _fields_ = [("n_levels", C.c_int32), ("features_per_level", C.c_int32),
                 ("log2_table_size", C.c_int32), ("base_resolution", C.c_int32),
@@ -189,6 +193,8 @@ SIGNATURES = {
     "krr_wf_set_megakernel_reorder": (_I, [_P, C.c_int32]),
     "krr_wf_set_media_order": (_I, [_P, C.c_int32]),
     "krr_wf_set_camera_order": (_I, [_P, C.c_int32]),
+    "krr_wf_set_profiling": (_I, [_P, C.c_int32]),
+    "krr_wf_profile_read": (_I, [_P, _P, C.c_int32, C.POINTER(C.c_int32)]),
     "krr_wf_get_launch": (_I, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "krr_wf_autotune": (_I, [_P, _P, C.c_int32, C.POINTER(WfTuning), _P]),

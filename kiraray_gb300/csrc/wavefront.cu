@@ -97,6 +97,12 @@ struct krr_wf {
     int32_t mk_reorder = 1;                // megakernel: reorder paths by hit class per bounce
     int32_t media_order = 0;               // 1: tracking kernels take their items by work class
     int32_t camera_order = 1;              // 1: camera rays in 8x8 pixel tiles, 0: row-major
+    // stage timers (krr_wf_set_profiling): event pairs recorded since the
+    // last krr_wf_profile_read, and a pool of spare events
+    int32_t profiling = 0;
+    struct ProfRecord { int32_t stage; cudaEvent_t e0, e1; };
+    std::vector<ProfRecord> prof;
+    std::vector<cudaEvent_t> prof_pool;
     int32_t *work_counts = nullptr;        // [32] work-class counts and cursors
     std::vector<DevMesh> h_mesh;           // host copies of the device meshes
     std::vector<int64_t> h_mesh_tris;      // triangles per mesh
@@ -167,6 +173,73 @@ struct krr_wf {
 };
 
 static int sync_part_depths(krr_wf *wf);
+
+// Stage timers, the pass's counterpart of the reference's PROFILE("...")
+// events (src/util/profiler.h:212-235, names from integrator.cpp and
+// medium.cpp): with profiling on, each stage's launches are bracketed by two
+// CUDA events on the stage's stream; krr_wf_profile_read waits for them and
+// sums the device time per stage.  Off by default; nothing is recorded while
+// the stream is being captured into a graph, and at most kProfMaxRecords
+// pairs are kept between reads.
+enum ProfStage : int {
+    PS_BEGIN_FRAME, PS_CAMERA, PS_TRACE_CLOSEST, PS_ROUTE, PS_HIT, PS_MISS, PS_SCATTER, PS_SHADOW,
+    PS_SHADOW_NEXT, PS_MEDIUM_SAMPLE, PS_MEDIUM_SCATTER, PS_CACHE_QUERY, PS_CACHE_TRAIN, PS_RESOLVE,
+    PS_COUNT
+};
+static const char *const kProfNames[PS_COUNT] = {
+    "Begin frame", "Generate camera rays", "Trace intersect rays", "Route closest hits",
+    "Process intersected rays", "Process escaped rays", "Generate scatter rays", "Trace shadow rays",
+    "Trace shadow and next rays", "Sample medium interaction", "Sample medium scattering",
+    "Cache queries", "Cache training", "Accumulate and resolve"};
+constexpr size_t kProfMaxRecords = 1 << 16;
+
+static cudaEvent_t prof_event(krr_wf *wf) {
+    if (!wf->prof_pool.empty()) {
+        cudaEvent_t e = wf->prof_pool.back();
+        wf->prof_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return e;
+}
+
+struct ProfScope {
+    krr_wf *wf;
+    int stage;
+    cudaStream_t st;
+    cudaEvent_t e0 = nullptr;
+    ProfScope(krr_wf *w, int s, cudaStream_t t) : wf(w), stage(s), st(t) {
+        if (!wf->profiling || wf->prof.size() >= kProfMaxRecords) return;
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+            cudaGetLastError();
+            return;
+        }
+        e0 = prof_event(wf);
+        if (e0 && cudaEventRecord(e0, st) != cudaSuccess) {
+            cudaGetLastError();
+            wf->prof_pool.push_back(e0);
+            e0 = nullptr;
+        }
+    }
+    ~ProfScope() {
+        if (!e0) return;
+        cudaEvent_t e1 = prof_event(wf);
+        if (!e1 || cudaEventRecord(e1, st) != cudaSuccess) {
+            cudaGetLastError();
+            wf->prof_pool.push_back(e0);
+            if (e1) wf->prof_pool.push_back(e1);
+            return;
+        }
+        wf->prof.push_back(krr_wf::ProfRecord{stage, e0, e1});
+    }
+    ProfScope(const ProfScope &) = delete;
+    ProfScope &operator=(const ProfScope &) = delete;
+};
 
 // Bounces of the render loop: the largest path depth of the pass's scenes.
 static int loop_depth(const krr_wf *wf) {
@@ -1842,6 +1915,7 @@ static int alloc_nrc_buffers(krr_wf *wf) {
 // End of a frame with training: build the batch from the recorded vertices
 // and take one optimiser step.
 static int nrc_train_frame(krr_wf *wf, cudaStream_t st) {
+    ProfScope prof(wf, PS_CACHE_TRAIN, st);
     int stride = nrc_train_stride(wf->nrc);
     int64_t batch = nrc_batch_size(wf->nrc);
     KRR_CUDA(cudaMemsetAsync(wf->nrc_b_count(), 0, sizeof(int32_t), st));
@@ -1891,6 +1965,8 @@ extern "C" int krr_wf_destroy(krr_wf *wf) {
     free_scene(wf);
     free_nrc_buffers(wf);
     if (wf->graph) cudaGraphExecDestroy(wf->graph);
+    for (auto &r : wf->prof) { cudaEventDestroy(r.e0); cudaEventDestroy(r.e1); }
+    for (cudaEvent_t e : wf->prof_pool) cudaEventDestroy(e);
     cudaFreeHost(wf->h_views);
     cudaFreeHost(wf->h_frame);
     cudaFree(wf->d_views);
@@ -2529,6 +2605,7 @@ static int fill_frame(krr_wf *wf, int64_t frame_index, const krr_camera_desc *si
 }
 
 static int launch_begin_frame(krr_wf *wf, cudaStream_t st) {
+    ProfScope prof(wf, PS_BEGIN_FRAME, st);
     k_begin_frame<<<wf->grid, wf->block, 0, st>>>(wf->ps, wf->d_views, wf->d_frame, wf->n);
     KRR_CUDA(cudaGetLastError());
     if (wf->nrc && wf->nrc_rec_count)
@@ -2564,6 +2641,7 @@ extern "C" int krr_wf_begin_frame_views(krr_wf *wf, int64_t frame_index, const k
 }
 
 static int camera_rays(krr_wf *wf, int64_t p0, int64_t count, cudaStream_t st) {
+    ProfScope prof(wf, PS_CAMERA, st);
     k_camera_rays<<<stage_grid(wf, count), wf->block, 0, st>>>(wf->ps, wf->q(Q_RAY0), wf->d_views,
                                                                wf->d_frame, p0, count, wf->camera_order);
     KRR_CUDA(cudaGetLastError());
@@ -2611,6 +2689,7 @@ static TraceLaunch closest_launch(krr_wf *wf, int depth) {
 
 // L[pixel] += throughput x cache(query) for the queued cache queries.
 static int nrc_evaluate_queries(krr_wf *wf, cudaStream_t st) {
+    ProfScope prof(wf, PS_CACHE_QUERY, st);
     KRR_TRY(nrc_query_device(wf->nrc, wf->nrc_q_in, wf->nrc_q_count(), wf->n, wf->nrc_q_out, st));
     k_nrc_apply<<<wf->grid, wf->block, 0, st>>>(wf->nrc_q_out, wf->nrc_q_meta, wf->nrc_q_count(),
                                                 (int)wf->n, wf->ps);
@@ -2635,7 +2714,10 @@ static int closest_stage(krr_wf *wf, int depth, cudaStream_t st, bool traced,
     const int inline_lights = in_render ? 1 : 0;
     int cur = depth & 1;
     Queue rq = wf->q(cur);
-    if (!traced) KRR_TRY(launch_trace_closest(&wf->accel, closest_launch(wf, depth), st));
+    if (!traced) {
+        ProfScope prof(wf, PS_TRACE_CLOSEST, st);
+        KRR_TRY(launch_trace_closest(&wf->accel, closest_launch(wf, depth), st));
+    }
     NrcHook hook{};
     if (wf->nrc) {
         hook.mode = 1;
@@ -2653,11 +2735,14 @@ static int closest_stage(krr_wf *wf, int depth, cudaStream_t st, bool traced,
         hook.spread_c = nrc_termination_spread(wf->nrc);
         if (!defer_cache) KRR_CUDA(cudaMemsetAsync(wf->nrc_q_count(), 0, sizeof(int32_t), st));
     }
-    k_hit_process<<<wf->grid, wf->block, 0, st>>>(wf->scene, rq, wf->hits, wf->q(cur ^ 1),
-                                                  wf->q(Q_MISS), wf->q(Q_HIT_LIGHT), wf->q(Q_SCATTER),
-                                                  wf->q(Q_MEDIUM_SAMPLE), wf->medium ? 1 : 0, wf->err(),
-                                                  hook, wf->ps, inline_lights, wf->params.nee);
-    KRR_CUDA(cudaGetLastError());
+    {
+        ProfScope prof(wf, PS_ROUTE, st);
+        k_hit_process<<<wf->grid, wf->block, 0, st>>>(wf->scene, rq, wf->hits, wf->q(cur ^ 1),
+                                                      wf->q(Q_MISS), wf->q(Q_HIT_LIGHT), wf->q(Q_SCATTER),
+                                                      wf->q(Q_MEDIUM_SAMPLE), wf->medium ? 1 : 0, wf->err(),
+                                                      hook, wf->ps, inline_lights, wf->params.nee);
+        KRR_CUDA(cudaGetLastError());
+    }
     if (wf->nrc && !defer_cache) KRR_TRY(nrc_evaluate_queries(wf, st));
     return KRR_OK;
 }
@@ -2672,6 +2757,7 @@ extern "C" int krr_wf_trace_closest(krr_wf *wf, int32_t depth, void *stream) {
 // transmittance tracking).  The shadow results are resolved right away, as
 // traceShadow does; the hits wait in wf->hits for closest_stage(depth + 1).
 static int trace_shadow_and_next(krr_wf *wf, int depth, cudaStream_t st) {
+    ProfScope prof(wf, PS_SHADOW_NEXT, st);
     Queue sq = wf->q(Q_SHADOW);
     TraceLaunch l = closest_launch(wf, depth + 1);
     l.any_o = sq.base;
@@ -2687,6 +2773,7 @@ static int trace_shadow_and_next(krr_wf *wf, int depth, cudaStream_t st) {
 
 extern "C" int krr_wf_handle_hit(krr_wf *wf, void *stream) {
     KRR_TRY(ready(wf));
+    ProfScope prof(wf, PS_HIT, as_stream(stream));
     k_handle_hit<<<wf->grid, wf->block, 0, as_stream(stream)>>>(wf->scene, wf->q(Q_HIT_LIGHT), wf->ps,
                                                                wf->params.nee);
     KRR_CUDA(cudaGetLastError());
@@ -2696,6 +2783,7 @@ extern "C" int krr_wf_handle_hit(krr_wf *wf, void *stream) {
 extern "C" int krr_wf_handle_miss(krr_wf *wf, void *stream) {
     KRR_TRY(ready(wf));
     if (wf->scene.n_infinite == 0) return KRR_OK;
+    ProfScope prof(wf, PS_MISS, as_stream(stream));
     k_handle_miss<<<wf->grid, wf->block, 0, as_stream(stream)>>>(wf->scene, wf->q(Q_MISS), wf->ps,
                                                                 wf->params.nee);
     KRR_CUDA(cudaGetLastError());
@@ -2705,6 +2793,7 @@ extern "C" int krr_wf_handle_miss(krr_wf *wf, void *stream) {
 // generateScatterRays; with `to_tracker` the shadow rays of scenes with
 // media go to their own queue for k_shadow_split (split_shadows()).
 static int scatter_stage(krr_wf *wf, int depth, cudaStream_t st, bool to_tracker) {
+    ProfScope prof(wf, PS_SCATTER, st);
     int cur = depth & 1;
     const Queue tracked = to_tracker ? Queue{wf->media_shadow, (int32_t)wf->qcap, wf->media_shadow_count()}
                                      : Queue{};
@@ -2728,6 +2817,7 @@ extern "C" int krr_wf_generate_scatter_rays(krr_wf *wf, int32_t depth, void *str
 extern "C" int krr_wf_trace_shadow(krr_wf *wf, void *stream) {
     KRR_TRY(ready(wf));
     cudaStream_t st = as_stream(stream);
+    ProfScope prof(wf, PS_SHADOW, st);
     if (wf->medium) return launch_trace_shadow_tr(wf, st);
     Queue sq = wf->q(Q_SHADOW);
     TraceLaunch l{};
@@ -2749,6 +2839,7 @@ extern "C" int krr_wf_trace_shadow(krr_wf *wf, void *stream) {
 extern "C" int krr_wf_sample_medium_interaction(krr_wf *wf, int32_t depth, void *stream) {
     KRR_TRY(ready(wf));
     if (!wf->medium) return KRR_OK;
+    ProfScope prof(wf, PS_MEDIUM_SAMPLE, as_stream(stream));
     return launch_medium_sample(wf, depth, as_stream(stream));
 }
 
@@ -2895,6 +2986,7 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
                 if (wf->medium) KRR_TRY(launch_medium_scatter(wf, depth, st, split));
                 KRR_TRY(scatter_stage(wf, depth, st, split));
                 if (split) {
+                    ProfScope prof(wf, PS_SHADOW, st);
                     KRR_TRY(launch_shadow_split(wf, st, true));
                     KRR_TRY(launch_shadow_tracker(wf, st));
                 }
@@ -2905,10 +2997,12 @@ extern "C" int krr_wf_render(krr_wf *wf, float *d_out, void *stream) {
             if (wf->nrc) KRR_TRY(nrc_evaluate_queries(wf, st));
         }
         if (wf->nrc && wf->nrc_train) KRR_TRY(nrc_train_frame(wf, st));
+        ProfScope prof(wf, PS_RESOLVE, st);
         k_accumulate<<<wf->grid, wf->block, 0, st>>>(wf->ps, wf->n,
                                                      wf->params.independent_samples && s + 1 < wf->params.spp);
         KRR_CUDA(cudaGetLastError());
     }
+    ProfScope prof(wf, PS_RESOLVE, st);
     k_resolve<<<wf->grid, wf->block, 0, st>>>(wf->ps, reinterpret_cast<float4 *>(d_out), wf->d_views,
                                               wf->d_frame, wf->n, (float)wf->params.spp,
                                               wf->params.enable_clamp, wf->params.clamp_max);
@@ -2926,6 +3020,45 @@ extern "C" int krr_wf_set_camera_order(krr_wf *wf, int32_t order) {
     KRR_CHECK_ARG(wf && (order == 0 || order == 1), "order must be 0 or 1");
     wf->camera_order = order;
     return KRR_OK;
+}
+
+extern "C" int krr_wf_set_profiling(krr_wf *wf, int32_t on) {
+    KRR_CHECK_ARG(wf && (on == 0 || on == 1), "profiling must be 0 or 1");
+    wf->profiling = on;
+    return KRR_OK;
+}
+
+extern "C" int krr_wf_profile_read(krr_wf *wf, krr_stage_time *out, int32_t cap, int32_t *n_out) {
+    KRR_CHECK_ARG(wf && n_out && cap >= 0 && (cap == 0 || out), "NULL argument");
+    double ms[PS_COUNT] = {};
+    int64_t calls[PS_COUNT] = {};
+    int status = KRR_OK;
+    for (const auto &r : wf->prof) {
+        float t = 0.f;
+        cudaError_t e = cudaEventSynchronize(r.e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, r.e0, r.e1);
+        if (e != cudaSuccess && status == KRR_OK)
+            status = cuda_status(e, "cudaEventElapsedTime", __FILE__, __LINE__);
+        ms[r.stage] += t;
+        ++calls[r.stage];
+        wf->prof_pool.push_back(r.e0);
+        wf->prof_pool.push_back(r.e1);
+    }
+    wf->prof.clear();
+    int32_t n = 0;
+    for (int k = 0; k < PS_COUNT; ++k) {
+        if (!calls[k]) continue;
+        if (n < cap) {
+            krr_stage_time &o = out[n];
+            std::memset(o.name, 0, sizeof(o.name));
+            std::strncpy(o.name, kProfNames[k], sizeof(o.name) - 1);
+            o.calls = calls[k];
+            o.ms = ms[k];
+        }
+        ++n;
+    }
+    *n_out = n;
+    return status;
 }
 
 extern "C" int krr_wf_set_megakernel_reorder(krr_wf *wf, int32_t reorder) {
@@ -3268,6 +3401,7 @@ int ensure_split_buffers(krr_wf *wf) {
 }
 
 int launch_medium_scatter(krr_wf *wf, int depth, cudaStream_t st, bool to_tracker) {
+    ProfScope prof(wf, PS_MEDIUM_SCATTER, st);
     k_medium_scatter<<<wf->grid, wf->block, 0, st>>>(wf->scene, wf->q(Q_MEDIUM_SCATTER),
                                                      wf->q((depth & 1) ^ 1), wf->q(Q_SHADOW),
                                                      to_tracker ? tracked_queue(wf) : Queue{}, wf->ps,

@@ -175,6 +175,18 @@ class WavefrontPathTracer:
         in queue order (False, default)."""
         check(self.lib.krr_wf_set_media_order(self._h, int(bool(order))), "krr_wf_set_media_order")
 
+    def set_profiling(self, on: bool) -> None:
+        """Per-stage device timers (the reference's PROFILE events), off by default."""
+        check(self.lib.krr_wf_set_profiling(self._h, int(bool(on))), "krr_wf_set_profiling")
+
+    def profile(self) -> dict:
+        """Stage -> (calls, device ms) since the last call; waits for the timed work."""
+        buf = (_lib.StageTime * 32)()
+        n = C.c_int32()
+        check(self.lib.krr_wf_profile_read(self._h, buf, 32, C.byref(n)), "krr_wf_profile_read")
+        return {buf[i].name.decode(): (int(buf[i].calls), float(buf[i].ms))
+                for i in range(min(n.value, 32))}
+
     def set_camera_order(self, tiled: bool) -> None:
         """Camera rays queued in 8x8 pixel tiles (True, default) or row-major."""
         check(self.lib.krr_wf_set_camera_order(self._h, int(bool(tiled))), "krr_wf_set_camera_order")

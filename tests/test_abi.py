@@ -61,3 +61,5 @@ def test_invalid_arguments_fail_without_gpu_work(krr_lib):
     assert krr_lib.krr_set_bvh_node_format(2) == 1
     assert krr_lib.krr_set_bvh_treelets(4) == 1 and krr_lib.krr_set_bvh_treelets(-1) == 1
     assert krr_lib.krr_wf_set_camera_order(None, 1) == 1
+    assert krr_lib.krr_wf_set_profiling(None, 1) == 1
+    assert krr_lib.krr_wf_profile_read(None, None, 0, None) == 1

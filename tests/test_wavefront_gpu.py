@@ -415,3 +415,53 @@ def test_closed_lambertian_sphere_radiance(krr_lib, cuda, nee):
     np.testing.assert_allclose(got, want, rtol=0.02)
     assert pt.device_errors() == 0
 
+
+def test_stage_timers(krr_lib, cuda):
+    """Per-stage device timers (the reference's PROFILE events): off by
+    default, named after the reference's stages, counted per launch, reset by
+    each read, skipped while a frame is captured into a graph, and without
+    effect on the frame."""
+    sc = scenes.large_scene(width=64, height=48, grid=128, n_spheres=20, sky_size=(64, 32))
+    pt = WavefrontPathTracer({"max_depth": 4})
+    pt.set_scene(sc)
+    pt.resize(64, 48)
+    pt.begin_frame(1, sc.camera)
+    want = pt.render().cpu().numpy()
+    assert pt.profile() == {}
+    pt.set_profiling(True)
+    for f in (1, 2):
+        pt.begin_frame(f, sc.camera)
+        got = pt.render()
+        if f == 1:
+            assert np.array_equal(got.cpu().numpy().view(np.uint32), want.view(np.uint32))
+    prof = pt.profile()
+    assert prof["Begin frame"][0] == 2 and prof["Generate camera rays"][0] == 2
+    assert prof["Trace intersect rays"][0] == 2          # camera rays; later bounces go with the shadows
+    assert prof["Trace shadow and next rays"][0] >= 2
+    assert prof["Route closest hits"][0] >= 4 and prof["Generate scatter rays"][0] >= 4
+    assert prof["Accumulate and resolve"][0] == 4
+    assert all(ms >= 0 for _, ms in prof.values()) and sum(ms for _, ms in prof.values()) > 0
+    assert pt.profile() == {}
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        out = torch.empty((48, 64, 4), device="cuda")
+        pt.capture_frame(out)
+        pt.launch_frame(3)
+        s.synchronize()
+        assert pt.profile() == {}
+    pt.set_profiling(False)
+    pt.begin_frame(4, sc.camera)
+    pt.render()
+    assert pt.profile() == {}
+    # a pass with media times its tracking stages
+    vol = scenes.volume_box(32, 32, max_depth=6, grid=32)
+    pv = WavefrontPathTracer({"max_depth": 6})
+    pv.set_scene(vol)
+    pv.resize(32, 32)
+    pv.set_profiling(True)
+    pv.begin_frame(1, vol.camera)
+    pv.render()
+    pm = pv.profile()
+    assert pm["Sample medium interaction"][0] >= 1 and pm["Trace shadow rays"][0] >= 1
+    assert pt.device_errors() == 0 and pv.device_errors() == 0
+
