@@ -80,6 +80,12 @@ void oracle_bsdf_sample(const float *mat, const float *wo, const float *u, int64
 float oracle_hg_p(float g, const float *wo, const float *wi);
 /* n samples from u[n][2] -> out[4 n]: wi xyz, pdf */
 void oracle_hg_sample(float g, const float *wo, const float *u, int64_t n, float *out);
+/* Light sampling (light.h:167-180, shape.h:54-123): n samples of light
+ * `light` seen from cp -> out[8 n]: p xyz, L rgb, solid-angle pdf, and the
+ * pdf the hit-side MIS weight uses for the same point. */
+int oracle_light_sample(const oracle_pt *pt, int32_t light, const float *cp, const float *u, int64_t n,
+                        float *out);
+int32_t oracle_light_count(const oracle_pt *pt);
 
 #ifdef __cplusplus
 }

@@ -1008,6 +1008,27 @@ extern "C" int oracle_pt_create(const krr_scene_desc *sd, int threads, oracle_pt
 
 extern "C" void oracle_pt_free(oracle_pt *s) { delete s; }
 
+// Light sampling of the restatement (known-answer tests): n samples of light
+// `light` seen from cp, from u[n][2]; out[n][8] = p xyz, L rgb, solid-angle
+// pdf, and the pdf that area_pdf() gives the same point (MIS side).
+extern "C" int oracle_light_sample(const oracle_pt *s, int32_t light, const float *cp, const float *u,
+                                   int64_t n, float *out) {
+    if (light < 0 || light >= (int32_t)s->lights.size()) return 1;
+    const Light &l = s->lights[light];
+    const V3 c{cp[0], cp[1], cp[2]};
+    for (int64_t i = 0; i < n; ++i) {
+        const LightSample ls = sample_li(*s, l, u[2 * i], u[2 * i + 1], c);
+        float *r = out + 8 * i;
+        r[0] = ls.p.x; r[1] = ls.p.y; r[2] = ls.p.z;
+        r[3] = ls.L.x; r[4] = ls.L.y; r[5] = ls.L.z;
+        r[6] = ls.pdf;
+        r[7] = l.kind == 0 ? area_pdf(*s, l, ls.p, ls.n, c) : kInv4Pi;
+    }
+    return 0;
+}
+
+extern "C" int32_t oracle_light_count(const oracle_pt *s) { return (int32_t)s->lights.size(); }
+
 // Henyey-Greenstein phase function of the restatement (known-answer tests).
 extern "C" float oracle_hg_p(float g, const float *wo, const float *wi) {
     return hg_p(g, V3{wo[0], wo[1], wo[2]}, V3{wi[0], wi[1], wi[2]});

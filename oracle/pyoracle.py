@@ -42,6 +42,8 @@ def load() -> C.CDLL:
             "oracle_bsdf_sample": (None, [P, P, P, I64, P]),
             "oracle_hg_p": (C.c_float, [C.c_float, P, P]),
             "oracle_hg_sample": (None, [C.c_float, P, P, I64, P]),
+            "oracle_light_sample": (C.c_int, [P, C.c_int32, P, P, I64, P]),
+            "oracle_light_count": (C.c_int32, [P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -224,6 +226,19 @@ class PathTracer:
                                 frame_index, px_begin, px_end, out_L.ctypes.data,
                                 out_px.ctypes.data, threads())
         return out_L, out_px
+
+    def light_count(self) -> int:
+        return int(load().oracle_light_count(self._h))
+
+    def light_sample(self, light: int, cp, u: np.ndarray) -> np.ndarray:
+        """[n, 8]: p xyz, L rgb, solid-angle pdf, hit-side pdf of the same point."""
+        cp = np.ascontiguousarray(cp, np.float32)
+        u = np.ascontiguousarray(u, np.float32).reshape(-1, 2)
+        out = np.empty((u.shape[0], 8), np.float32)
+        if load().oracle_light_sample(self._h, light, cp.ctypes.data, u.ctypes.data, u.shape[0],
+                                      out.ctypes.data):
+            raise IndexError(light)
+        return out
 
     def __del__(self):
         try:

@@ -3,8 +3,9 @@ oracle/pathtracer.cpp): Fresnel at normal incidence and total internal
 reflection, the Lambert estimator and white furnace, pdf normalisation and
 sample/evaluation consistency of the GGX conductor and rough dielectric
 (legacy stretched visible-normal sampling, microfacet.h:86-164), conductor
-reciprocity, the Henyey-Greenstein phase function (media.cpp:83-111), and a
-closed emissive Lambertian sphere whose radiance is Le / (1 - albedo).
+reciprocity, the Henyey-Greenstein phase function (media.cpp:83-111),
+area-light sampling against a triangle's solid angle, and a closed emissive
+Lambertian sphere whose radiance is Le / (1 - albedo).
 
 These pin the restatement to analytic answers; the reference itself cannot be
 built here, so they are the oracle's anchor for T9-T13 and T17."""
@@ -209,6 +210,57 @@ def test_henyey_greenstein_normalised_mean_cosine_and_sampling(oracle_lib, g):
     # (wo points away from the scattering point, as in the reference)
     mean_cos = float(np.mean(s[:, 0:3] @ wo))
     assert mean_cos == pytest.approx(-g, abs=5e-3)
+
+
+# ------------------------------------------------------------ area lights
+def _solid_angle(a, b, c):
+    """Solid angle of a triangle seen from the origin (Van Oosterom and Strackee 1983)."""
+    la, lb, lc = (np.linalg.norm(v) for v in (a, b, c))
+    num = abs(np.dot(a, np.cross(b, c)))
+    den = la * lb * lc + np.dot(a, b) * lc + np.dot(a, c) * lb + np.dot(b, c) * la
+    return 2 * np.arctan2(num, den)
+
+
+def test_area_light_sampling_solid_angle_and_one_sided_emission(oracle_lib):
+    """Uniform area sampling of an emissive triangle under an instance
+    transform (shape.h:54-123, light.h:167-193): E[1 / pdf] over samples is
+    the triangle's solid angle, the sampled pdf equals the one the hit side
+    uses for MIS, samples lie on the triangle, and the triangle emits only
+    towards the side its normal faces."""
+    from kiraray_gb300 import _lib as L
+    from kiraray_gb300 import scenes
+
+    pos = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0]], np.float32)  # normal +z
+    nrm = np.tile(np.array([0.0, 0.0, 1.0], np.float32), (3, 1))
+    le = (5.0, 4.0, 3.0)
+    mesh = scenes.Mesh(pos, nrm, np.array([[0, 1, 2]], np.uint32), material=0, emission=le)
+    xf = scenes._xform((2.0, 1.5, 1.0), 30.0, (0.3, -0.2, 0.5))
+    cam = scenes._camera((0.0, 0.0, 3.0), (0.0, 0.0, 0.0), 40.0, 8, 8)
+    sc = scenes.Scene([mesh], [(0, xf)], [scenes.Material(type=L.MATERIAL_DIFFUSE)], cam, 8, 8)
+    pt = O.PathTracer(sc)
+    assert pt.light_count() == 1
+    world = (xf[:, :3].astype(np.float64) @ pos.T.astype(np.float64)).T + xf[:, 3]
+    n_world = np.cross(world[1] - world[0], world[2] - world[0])
+    n_world /= np.linalg.norm(n_world)
+    centre = world.mean(0)
+    u = np.random.default_rng(21).random((200000, 2), dtype=np.float32)
+    for side, cp in ((1, centre + 1.3 * n_world + np.array([0.2, 0.1, -0.3])),
+                     (-1, centre - 0.9 * n_world + np.array([-0.1, 0.3, 0.2]))):
+        s = pt.light_sample(0, cp.astype(np.float32), u)
+        assert np.all(s[:, 6] > 0)
+        np.testing.assert_allclose(s[:, 7], s[:, 6], rtol=1e-4)
+        est = 1.0 / s[:, 6].astype(np.float64)
+        omega = _solid_angle(*(world - cp))
+        assert est.mean() == pytest.approx(omega, abs=4 * est.std() / np.sqrt(est.size))
+        # on the triangle: in its plane, barycentrics in [0, 1]
+        p = s[:, 0:3].astype(np.float64)
+        assert np.abs((p - world[0]) @ n_world).max() < 1e-5
+        e1, e2, q = world[1] - world[0], world[2] - world[0], p - world[0]
+        g = np.array([[e1 @ e1, e1 @ e2], [e1 @ e2, e2 @ e2]])
+        b = np.linalg.solve(g, np.stack([q @ e1, q @ e2]))
+        assert b.min() > -1e-5 and (b.sum(0)).max() < 1 + 1e-5
+        want = np.array(le) if side > 0 else np.zeros(3)
+        np.testing.assert_allclose(s[:, 3:6], np.broadcast_to(want, (u.shape[0], 3)), rtol=1e-6)
 
 
 # ------------------------------------------------- closed-sphere furnace
