@@ -72,8 +72,17 @@ k_trace_two_level_p(InstancedView v, TraceLaunch L) {
         d = f3(rd);
         tmin0 = ro.w;
     };
+    // Box tests need only the ray's origin, inverse direction and octant; the
+    // triangle test's shear and axis permutation (ray_pre, three correctly
+    // rounded divisions) are computed when a geometry tree first hands the
+    // ray a triangle, so the world ray (instance boxes only) and instances
+    // whose triangles are never reached skip them.
+    bool tri_ready = false;
     auto set_ray = [&](V3 o, V3 d) {
-        r = ray_pre(o, d, tmin0);
+        r.o = o;
+        r.d = d;
+        r.tmin = tmin0 > 0.f ? tmin0 : 0.f;
+        tri_ready = false;
         inv = box_inverse(d);
         oinv = V3{-o.x * inv.x, -o.y * inv.y, -o.z * inv.z};
         oct = (inv.x < 0.f ? 1 : 0) | (inv.y < 0.f ? 2 : 0) | (inv.z < 0.f ? 4 : 0);
@@ -151,6 +160,10 @@ k_trace_two_level_p(InstancedView v, TraceLaunch L) {
             tg = make_uint2(0u, 0u);
             id_delta = I.id_delta;
             in_geom = true;
+        }
+        if (active && in_geom && tg.y && !done && !tri_ready) {
+            r = ray_pre(r.o, r.d, tmin0);
+            tri_ready = true;
         }
         while (active && in_geom && tg.y && !done) {
             const int b = __ffs(tg.y) - 1;
