@@ -308,7 +308,12 @@ __device__ __forceinline__ V3 inst_vector(const float *m, V3 d) {
 // Closest (ANY: any masked) hit of one world ray over the two levels.
 template <bool ANY, int FMT, bool MASKED = true>
 __device__ float4 trace_two_level(const InstancedView &v, V3 o, V3 d, float tmin, float tmax, int *err) {
-    RayPre r = ray_pre(o, d, tmin);
+    // the instance tree holds no triangles: the world ray needs only what the
+    // box tests read (origin and tmin), not the triangle test's shear
+    RayPre r;
+    r.o = o;
+    r.d = d;
+    r.tmin = tmin > 0.f ? tmin : 0.f;
     V3 inv = box_inverse(d);
     V3 oinv = V3{-o.x * inv.x, -o.y * inv.y, -o.z * inv.z};
     int oct = (inv.x < 0.f ? 1 : 0) | (inv.y < 0.f ? 2 : 0) | (inv.z < 0.f ? 4 : 0);
